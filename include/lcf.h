@@ -1,0 +1,209 @@
+/*
+ * lcf.h — C ABI of the GB300 (sm_103a) parametric light-curve fitting library
+ * (liblcf_gb300.so).
+ *
+ * Two groups of entry points:
+ *
+ *  1. The fused batch fit.  One call runs, for every band of every source,
+ *     what the reference's per-band `fit_parametric_model` does
+ *     (src/parametric.rs:3563-3739): PSO model selection over the eight flux
+ *     models with three restarts, bounded L-BFGS polish and BIC selection,
+ *     then SVI or Laplace uncertainty, the t0 / all-parameter profile
+ *     refinements, the magnitude-space chi2 and the MultiBazin fit of the
+ *     most populated band.  It replaces the reference's host-driven PSO loop
+ *     (src/gpu_cuda.rs:368-637), its GPU SVI driver (src/gpu_cuda.rs:1315-1422)
+ *     and the CPU finalisation (src/parametric.rs:3126-3553) with one
+ *     device-resident pipeline.
+ *
+ *  2. Drop-in exports with the exact names and signatures the reference's
+ *     Rust host binds (src/gpu_cuda.rs:31-40 and :102-164), so that an
+ *     unmodified `GpuContext` links against this library instead of the
+ *     reference's `liblightcurve_cuda.a` (build.rs:14-18).  They take device
+ *     pointers and launch on the legacy default stream, as the reference's do.
+ *
+ * Conventions of the fused API:
+ *   - every function returns an int status: 0 = success, <0 = error code
+ *     (LCF_E_*); the message is available from lcf_last_error();
+ *   - inputs and outputs are caller-owned host arrays in FP64 (the reference's
+ *     arithmetic type) unless stated otherwise;
+ *   - one context per host thread; a context owns its stream, its device
+ *     buffers and its captured CUDA graph.
+ *
+ * Model ids follow the reference (src/gpu_types.rs:51-62,
+ * src/parametric.rs:3279-3288): 0 Bazin, 1 Villar, 2 Tde, 3 Arnett,
+ * 4 Magnetar, 5 ShockCooling, 6 Afterglow, 7 MetzgerKN.
+ */
+#ifndef LCF_H
+#define LCF_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define LCF_N_MODELS 8
+#define LCF_MAX_PARAMS 7          /* Villar / Tde */
+#define LCF_MB_MAX_K 4            /* MULTI_BAZIN_MAX_K, src/parametric.rs:915 */
+#define LCF_MB_MAX_PARAMS 18      /* 4*K + 2 at K = 4 */
+
+/* status codes */
+#define LCF_OK 0
+#define LCF_E_INVALID (-1)        /* bad argument (sizes, offsets, options) */
+#define LCF_E_CUDA (-2)           /* a CUDA runtime call failed */
+#define LCF_E_NOMEM (-3)          /* device or pinned allocation failed */
+#define LCF_E_TIMEOUT (-4)        /* a bounded device wait expired */
+#define LCF_E_UNSUPPORTED (-5)    /* option combination not built */
+
+/* UncertaintyMethod, src/parametric.rs:13-21 */
+#define LCF_METHOD_SVI 0
+#define LCF_METHOD_LAPLACE 1
+
+/*
+ * Batch of sources in CSR form.  Source s owns bands
+ * [source_band_offsets[s], source_band_offsets[s+1]); band b owns
+ * observations [band_obs_offsets[b], band_obs_offsets[b+1]).  `times`,
+ * `flux` and `flux_err` are one band's `BandData{times, values, errors}`
+ * (src/common.rs:11-15) concatenated: times relative to the source's first
+ * observation, flux and errors in linear flux units.  Band order within a
+ * source is the caller's; the fit ranks bands by observation count,
+ * descending, with ties kept in caller order (the reference sorts a HashMap's
+ * iteration order, src/parametric.rs:3632).
+ */
+typedef struct lcf_bands_csr {
+    int32_t n_sources;
+    int32_t n_bands;
+    const int32_t* source_band_offsets; /* [n_sources + 1] */
+    const int64_t* band_obs_offsets;    /* [n_bands + 1]   */
+    const double* times;                /* [n_obs] */
+    const double* flux;                 /* [n_obs] */
+    const double* flux_err;             /* [n_obs] */
+} lcf_bands_csr;
+
+typedef struct lcf_fit_options {
+    int32_t fit_all_models;   /* fit_parametric_model(.., fit_all_models, ..) */
+    int32_t method;           /* LCF_METHOD_SVI or LCF_METHOD_LAPLACE */
+    int32_t forced_model;     /* -1: model selection; else the model id */
+    int32_t run_multi_bazin;  /* 1: fit MultiBazin on each source's rank-0 band (reference behaviour) */
+} lcf_fit_options;
+
+/*
+ * Per-band outputs (caller-allocated, indexed by the caller's band index b).
+ * A band the reference would skip (no data, or peak flux <= 0) has
+ * model[b] = -1 and rank[b] = -1.  Parameter rows are padded to
+ * LCF_MAX_PARAMS with NaN.  NaN stands for the reference's `None`
+ * (`finite_or_none`, src/common.rs:463).
+ */
+typedef struct lcf_fit_outputs {
+    int32_t* model;             /* [n_bands] selected model id */
+    int32_t* rank;              /* [n_bands] position after the by-count sort */
+    int32_t* n_obs;             /* [n_bands] */
+    double* pso_params;         /* [n_bands * 7] */
+    double* pso_chi2;           /* [n_bands] */
+    double* svi_mu;             /* [n_bands * 7] */
+    double* svi_log_sigma;      /* [n_bands * 7] */
+    double* svi_elbo;           /* [n_bands] */
+    double* mag_chi2;           /* [n_bands] */
+    double* per_model_chi2;     /* [n_bands * 8], by model id; NaN = None or not fitted */
+    double* per_model_params;   /* [n_bands * 8 * 7]; filled when fit_all_models */
+    int32_t* mb_best_k;         /* [n_bands]; 0 = no MultiBazin result */
+    double* mb_params;          /* [n_bands * 18] */
+    double* mb_cost;            /* [n_bands] */
+    double* mb_bic;             /* [n_bands] */
+    double* mb_per_k_cost;      /* [n_bands * 4] */
+    double* mb_per_k_bic;       /* [n_bands * 4] */
+} lcf_fit_outputs;
+
+/* Timing and work counters of the last fit, filled by lcf_last_stats(). */
+typedef struct lcf_fit_stats {
+    double ms_total;            /* device time of the whole pipeline (CUDA events) */
+    double ms_pso;              /* model-selection PSO launch */
+    double ms_lbfgs;            /* restart reduce + L-BFGS polish + BIC select */
+    double ms_t0_search;        /* SVI-mode profile t0 search (two PSO launches) */
+    double ms_uncertainty;      /* SVI or Laplace */
+    double ms_refine;           /* profile refinements + mag chi2 */
+    double ms_multi_bazin;      /* MultiBazin K = 2..4 launches */
+    double particle_obs_evals;  /* device-counted particle x observation evaluations in PSO launches */
+    double ode_steps;           /* device-counted MetzgerKN Euler steps in PSO launches */
+    int64_t pso_tasks;          /* PSO runs executed */
+    int64_t kernel_launches;    /* kernels launched by the last fit */
+} lcf_fit_stats;
+
+typedef struct lcf_ctx lcf_ctx;
+
+/* Context management.  The context binds `device` and creates its stream. */
+int lcf_ctx_create(int device, lcf_ctx** out);
+void lcf_ctx_destroy(lcf_ctx* ctx);
+const char* lcf_last_error(const lcf_ctx* ctx);  /* never NULL */
+int lcf_last_stats(const lcf_ctx* ctx, lcf_fit_stats* out);
+
+/*
+ * Fused batch fit of host-resident data: copies the CSR into pinned staging,
+ * then to the device, runs the pipeline and copies the outputs back.
+ * Replaces, per band, fit_parametric_model(bands, fit_all_models, method,
+ * forced_model) (src/parametric.rs:3563-3739).
+ */
+int lcf_fit_parametric_batch(lcf_ctx* ctx, const lcf_bands_csr* bands,
+                             const lcf_fit_options* opts, lcf_fit_outputs* out);
+
+/*
+ * Same pipeline on data that is already resident on the device: the three
+ * observation arrays and two offset arrays are device pointers, the outputs
+ * stay on the device in the context's buffers.  Used to time the kernels
+ * without host transfers; lcf_download_outputs() copies them out.
+ */
+int lcf_fit_parametric_device(lcf_ctx* ctx, const lcf_bands_csr* dev_bands,
+                              const lcf_fit_options* opts);
+int lcf_download_outputs(lcf_ctx* ctx, lcf_fit_outputs* out);
+
+/* The context's CUDA stream (a cudaStream_t), for callers that time with events. */
+void* lcf_ctx_stream(lcf_ctx* ctx);
+
+/*
+ * Batched likelihood: cost of `n_eval` parameter vectors of one model on one
+ * band, exactly PsoCost::cost_from_slice (src/parametric.rs:1303-1370):
+ * per-observation Gaussian / upper-limit negative log-likelihood over the
+ * band, divided by n, plus the population prior / n^2 when with_prior != 0.
+ * The band arrays are host FP64 (already peak-normalised, as BandFitData);
+ * evaluation runs in the fused kernel's FP32 arithmetic.  `params` is
+ * [n_eval * n_params(model)].
+ */
+int lcf_band_cost(lcf_ctx* ctx, int model, const double* times, const double* flux,
+                  const double* obs_var, const uint8_t* is_upper, const double* upper_flux,
+                  int n_obs, const double* params, int n_eval, int with_prior,
+                  double* costs);
+
+/* ---------------------------------------------------------------------------
+ * Reference drop-in exports (device pointers, default stream, void return;
+ * errors surface through cudaGetLastError as in the reference).
+ * ------------------------------------------------------------------------- */
+
+/* cuda/models.cu launch_* eval wrappers, bound at src/gpu_cuda.rs:31-40:
+ * out[d * n_times + t] = model(params[d * n_params ..], times[t]), FP64. */
+void launch_bazin(const double* p, const double* t, double* o, int nd, int nt, int np, int grid, int block);
+void launch_villar(const double* p, const double* t, double* o, int nd, int nt, int np, int grid, int block);
+void launch_tde(const double* p, const double* t, double* o, int nd, int nt, int np, int grid, int block);
+void launch_arnett(const double* p, const double* t, double* o, int nd, int nt, int np, int grid, int block);
+void launch_magnetar(const double* p, const double* t, double* o, int nd, int nt, int np, int grid, int block);
+void launch_shock_cooling(const double* p, const double* t, double* o, int nd, int nt, int np, int grid, int block);
+void launch_afterglow(const double* p, const double* t, double* o, int nd, int nt, int np, int grid, int block);
+/* MetzgerKN over the whole times array per draw, as metzger_kn_eval_batch
+ * (src/parametric.rs:544-648). */
+void launch_metzger_kn(const double* p, const double* t, double* o, int nd, int nt, int np, int grid, int block);
+
+/* launch_batch_pso_cost, bound at src/gpu_cuda.rs:102-118:
+ * costs[s * n_particles + k] = sum_obs NLL / n for positions
+ * [s][k][n_params]; sigma_extra is the last parameter; 1e99 on a non-finite
+ * prediction.  `grid` and `block` are accepted and ignored (the launch shape
+ * is this library's). */
+void launch_batch_pso_cost(const double* all_times, const double* all_flux,
+                           const double* all_obs_var, const int* all_is_upper,
+                           const double* all_upper_flux, const int* source_offsets,
+                           const double* positions, double* costs, int n_sources,
+                           int n_particles, int n_params, int model_id, int grid, int block);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* LCF_H */

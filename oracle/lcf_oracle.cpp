@@ -1,0 +1,1853 @@
+// lcf_oracle.cpp — TEST INFRASTRUCTURE ONLY (the parity oracle and the CPU
+// baseline).  Nothing in the shipped library links, loads or calls this file;
+// only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline / reference
+// arm may use it, always as the checker or the timed CPU path.
+//
+// An FP64 C++ restatement of the per-band parametric fitting path of the
+// reference crate boom-astro/lightcurve-fitting, src/parametric.rs.  Each
+// function names the reference lines it follows.  Two third-party algorithms
+// that the reference takes from crates absent here are restated from their
+// published descriptions:
+//   * rand 0.9.2 SmallRng (Cargo.lock:881-883) = xoshiro256++ (Blackman &
+//     Vigna, 2018) seeded by SplitMix64; f64 = top 53 bits * 2^-53.
+//   * argmin 0.11.0 LBFGS + MoreThuenteLineSearch (Cargo.lock:77-95) = the
+//     L-BFGS two-loop recursion (Nocedal & Wright, Alg. 7.4) and the
+//     Moré–Thuente line search (Moré & Thuente 1994; MINPACK cvsrch/cstep).
+// Neither can be executed here (no Rust toolchain), so their parity with the
+// reference is unpinned; the model formulas, the log-normal CDF and the erf
+// approximation are pinned against the reference's own device header
+// (cuda/models_device.h) compiled as host code (see oracle/ref_pin/).
+#include <algorithm>
+#include <cmath>
+#include <cstdint>
+#include <cstring>
+#include <limits>
+#include <vector>
+
+#include "lcf.h"
+
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+namespace orc {
+
+static const double INF = std::numeric_limits<double>::infinity();
+static const double NaN = std::numeric_limits<double>::quiet_NaN();
+static const double PI = 3.14159265358979323846;
+static const double LN10 = 2.302585092994045684;
+
+// ---------------------------------------------------------------------------
+// SmallRng (xoshiro256++), src/parametric.rs:6-7 use sites :1171, :1656, :2239
+// ---------------------------------------------------------------------------
+struct SmallRng {
+    uint64_t s[4];
+    explicit SmallRng(uint64_t seed) {
+        uint64_t st = seed;
+        for (int i = 0; i < 4; i++) {
+            st += 0x9e3779b97f4a7c15ULL;
+            uint64_t z = st;
+            z = (z ^ (z >> 30)) * 0xbf58476d1ce4e5b9ULL;
+            z = (z ^ (z >> 27)) * 0x94d049bb133111ebULL;
+            s[i] = z ^ (z >> 31);
+        }
+    }
+    static inline uint64_t rotl(uint64_t x, int k) { return (x << k) | (x >> (64 - k)); }
+    uint64_t next_u64() {
+        uint64_t res = rotl(s[0] + s[3], 23) + s[0];
+        uint64_t t = s[1] << 17;
+        s[2] ^= s[0];
+        s[3] ^= s[1];
+        s[1] ^= s[2];
+        s[0] ^= s[3];
+        s[2] ^= t;
+        s[3] = rotl(s[3], 45);
+        return res;
+    }
+    double f64() { return (double)(next_u64() >> 11) * (1.0 / 9007199254740992.0); }
+};
+
+// ---------------------------------------------------------------------------
+// Model metadata, src/parametric.rs:124-162 (ids: src/parametric.rs:3279-3288)
+// ---------------------------------------------------------------------------
+enum { BAZIN = 0, VILLAR = 1, TDE = 2, ARNETT = 3, MAGNETAR = 4, SHOCK = 5, AFTERGLOW = 6, METZGER = 7 };
+static const int N_PARAMS[8] = {6, 7, 7, 5, 5, 5, 6, 5};
+static const int SE_IDX[8] = {5, 6, 6, 4, 4, 4, 5, 4};
+static const int T0_IDX[8] = {2, 3, 2, 1, 1, 1, 1, 3};
+// pso_model_select order, src/parametric.rs:2002-2011
+static const int SELECT_ORDER[8] = {BAZIN, ARNETT, TDE, AFTERGLOW, VILLAR, MAGNETAR, SHOCK, METZGER};
+
+// pso_bounds, src/parametric.rs:1541-1579
+static void pso_bounds(int m, std::vector<double>& lo, std::vector<double>& hi) {
+    switch (m) {
+        case BAZIN: lo = {-3.0, -0.3, -100.0, -2.0, -2.0, -5.0}; hi = {3.0, 0.3, 100.0, 5.0, 6.0, 0.0}; break;
+        case VILLAR: lo = {-1.5, -0.02, 1.0, -60.0, -1.0, 1.0, -6.0}; hi = {1.5, 0.05, 5.0, 40.0, 3.0, 5.5, 0.0}; break;
+        case METZGER: lo = {-3.0, -2.0, -1.0, -2.0, -5.0}; hi = {-0.5, -0.5, 2.0, 1.0, 0.0}; break;
+        case TDE: lo = {-3.0, -1.0, -100.0, -2.0, -1.0, 0.5, -5.0}; hi = {3.0, 1.0, 100.0, 5.0, 6.0, 4.0, 0.0}; break;
+        case ARNETT: lo = {-3.0, -100.0, 0.5, -3.0, -5.0}; hi = {3.0, 100.0, 4.5, 3.0, 0.0}; break;
+        case MAGNETAR: lo = {-3.0, -100.0, 0.0, 0.5, -5.0}; hi = {3.0, 100.0, 6.0, 4.5, 0.0}; break;
+        case SHOCK: lo = {-3.0, -100.0, 0.1, -1.0, -5.0}; hi = {3.0, 100.0, 3.0, 4.0, 0.0}; break;
+        default: lo = {-3.0, -100.0, -2.0, -2.0, 0.5, -5.0}; hi = {3.0, 100.0, 6.0, 3.0, 5.0, 0.0}; break;
+    }
+}
+
+// population_priors, src/parametric.rs:1588-1621
+static void population_priors(int m, std::vector<double>& c, std::vector<double>& w) {
+    if (m == VILLAR) {
+        c = {-0.009 * LN10, 0.009, 1.327 * LN10, -12.0, 0.360 * LN10, 1.454 * LN10, -1.033 * LN10};
+        w = {0.10 * LN10, 0.010, 0.40 * LN10, 15.0, 0.35 * LN10, 0.40 * LN10, 0.50 * LN10};
+    } else if (m == BAZIN) {
+        c = {0.0, 0.0, 0.0, 1.5, 3.0, -3.0};
+        w = {2.0, 0.2, 30.0, 2.5, 2.5, 2.0};
+    } else {
+        c.assign(N_PARAMS[m], 0.0);
+        w.assign(N_PARAMS[m], 5.0);
+    }
+}
+
+// prior_params, src/parametric.rs:2072-2115
+static void prior_params(int m, std::vector<double>& c, std::vector<double>& w) {
+    int np = N_PARAMS[m];
+    c.assign(np, 0.0);
+    w.assign(np, 2.0);
+    switch (m) {
+        case METZGER: c = {-1.75, -1.25, 0.5, -0.5, 0.0}; w = {1.25, 0.75, 1.5, 1.5, 2.0}; break;
+        case TDE: c[5] = 1.67; w[5] = 1.0; break;
+        case ARNETT: c[2] = 2.3; w[2] = 1.0; break;
+        case MAGNETAR: c[2] = 3.0; w[2] = 1.5; c[3] = 2.3; w[3] = 1.0; break;
+        case SHOCK: c[2] = 0.5; w[2] = 1.0; c[3] = 1.0; w[3] = 2.0; break;
+        case AFTERGLOW: c[2] = 1.0; w[2] = 2.0; c[3] = 0.8; w[3] = 1.0; c[4] = 2.0; w[4] = 1.0; break;
+        default: break;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Model formulas and analytic gradients, src/parametric.rs:199-538
+// ---------------------------------------------------------------------------
+static inline double bazin(const double* p, double t) {
+    double a = std::exp(p[0]), b = p[1], t0 = p[2], tr = std::exp(p[3]), tf = std::exp(p[4]);
+    double dt = t - t0;
+    double e_fall = std::exp(-dt / tf);
+    double sig = 1.0 / (1.0 + std::exp(-dt / tr));
+    return a * e_fall * sig + b;
+}
+static inline void bazin_grad(const double* p, double t, double* o) {
+    double a = std::exp(p[0]), t0 = p[2], tr = std::exp(p[3]), tf = std::exp(p[4]);
+    double dt = t - t0;
+    double e_fall = std::exp(-dt / tf);
+    double sig = 1.0 / (1.0 + std::exp(-dt / tr));
+    double base = a * e_fall * sig;
+    o[0] = base;
+    o[1] = 1.0;
+    o[2] = base * (1.0 / tf - (1.0 - sig) / tr);
+    o[3] = -base * (1.0 - sig) * dt / tr;
+    o[4] = base * dt / tf;
+    o[5] = 0.0;
+}
+static inline double villar(const double* p, double t) {
+    double a = std::exp(p[0]), beta = p[1], gamma = std::exp(p[2]), t0 = p[3];
+    double tr = std::exp(p[4]), tf = std::exp(p[5]);
+    double phase = t - t0;
+    double sig_rise = 1.0 / (1.0 + std::exp(-phase / tr));
+    double k = 10.0;
+    double w = 1.0 / (1.0 + std::exp(-k * (phase - gamma)));
+    double pl = 1.0 - beta * phase;
+    double pr = (1.0 - beta * gamma) * std::exp((gamma - phase) / tf);
+    double piece = (1.0 - w) * pl + w * pr;
+    return a * sig_rise * piece;
+}
+static inline void villar_grad(const double* p, double t, double* o) {
+    double a = std::exp(p[0]), beta = p[1], gamma = std::exp(p[2]), t0 = p[3];
+    double tr = std::exp(p[4]), tf = std::exp(p[5]);
+    double phase = t - t0;
+    double k = 10.0;
+    double sig_rise = 1.0 / (1.0 + std::exp(-phase / tr));
+    double w = 1.0 / (1.0 + std::exp(-k * (phase - gamma)));
+    double pl = 1.0 - beta * phase;
+    double e_decay = std::exp((gamma - phase) / tf);
+    double pr = (1.0 - beta * gamma) * e_decay;
+    double piece = (1.0 - w) * pl + w * pr;
+    double flux = a * sig_rise * piece;
+    o[0] = flux;
+    double d_pl_dbeta = -phase;
+    double d_pr_dbeta = -gamma * e_decay;
+    o[1] = a * sig_rise * ((1.0 - w) * d_pl_dbeta + w * d_pr_dbeta);
+    double dw_dgamma = -k * w * (1.0 - w);
+    double dw_dloggamma = dw_dgamma * gamma;
+    double dpr_dgamma = e_decay * (-beta + (1.0 - beta * gamma) / tf);
+    double dpr_dloggamma = dpr_dgamma * gamma;
+    double d_piece_dloggamma = dw_dloggamma * (pr - pl) + w * dpr_dloggamma;
+    o[2] = a * sig_rise * d_piece_dloggamma;
+    double dsig_dphase = sig_rise * (1.0 - sig_rise) / tr;
+    double dsig_dt0 = -dsig_dphase;
+    double dw_dphase = k * w * (1.0 - w);
+    double dw_dt0 = -dw_dphase;
+    double dpl_dt0 = beta;
+    double dpr_dt0 = (1.0 - beta * gamma) * e_decay / tf;
+    double d_piece_dt0 = dw_dt0 * (pr - pl) + (1.0 - w) * dpl_dt0 + w * dpr_dt0;
+    o[3] = a * (dsig_dt0 * piece + sig_rise * d_piece_dt0);
+    o[4] = a * piece * sig_rise * (1.0 - sig_rise) * (-phase / tr);
+    double d_pr_dlogtf = pr * (phase - gamma) / tf;
+    o[5] = a * sig_rise * w * d_pr_dlogtf;
+    o[6] = 0.0;
+}
+static inline double tde(const double* p, double t) {
+    double a = std::exp(p[0]), b = p[1], t0 = p[2], tr = std::exp(p[3]), tf = std::exp(p[4]), alpha = p[5];
+    double phase = t - t0;
+    double sig = 1.0 / (1.0 + std::exp(-phase / tr));
+    double ps = std::log(1.0 + std::exp(phase)) + 1e-6;
+    double w = 1.0 + ps / tf;
+    double decay = std::pow(w, -alpha);
+    return a * sig * decay + b;
+}
+static inline void tde_grad(const double* p, double t, double* o) {
+    double a = std::exp(p[0]), t0 = p[2], tr = std::exp(p[3]), tf = std::exp(p[4]), alpha = p[5];
+    double phase = t - t0;
+    double sig = 1.0 / (1.0 + std::exp(-phase / tr));
+    double ps = std::log(1.0 + std::exp(phase)) + 1e-6;
+    double sig_phase = std::exp(phase) / (1.0 + std::exp(phase));
+    double w = 1.0 + ps / tf;
+    double decay = std::pow(w, -alpha);
+    double base = a * sig * decay;
+    o[0] = base;
+    o[1] = 1.0;
+    double dsig_dt0 = -sig * (1.0 - sig) / tr;
+    double ddecay_dt0 = alpha * std::pow(w, -alpha - 1.0) * sig_phase / tf;
+    o[2] = a * (dsig_dt0 * decay + sig * ddecay_dt0);
+    o[3] = a * decay * (-sig * (1.0 - sig) * phase / tr);
+    o[4] = a * sig * alpha * std::pow(w, -alpha - 1.0) * ps / tf;
+    o[5] = a * sig * (-std::log(w)) * decay;
+    o[6] = 0.0;
+}
+static const double TAU_NI = 8.8, TAU_CO = 111.3;
+static inline double arnett(const double* p, double t) {
+    double a = std::exp(p[0]), t0 = p[1], tm = std::exp(p[2]), lf = p[3];
+    double phase = t - t0;
+    double ps = std::log(1.0 + std::exp(phase)) + 1e-6;
+    double f = 1.0 / (1.0 + std::exp(-lf));
+    double e_ni = std::exp(-ps / TAU_NI), e_co = std::exp(-ps / TAU_CO);
+    double heat = f * e_ni + (1.0 - f) * e_co;
+    double x = ps / tm;
+    double trap = 1.0 - std::exp(-x * x);
+    return a * heat * trap;
+}
+static inline void arnett_grad(const double* p, double t, double* o) {
+    double a = std::exp(p[0]), t0 = p[1], tm = std::exp(p[2]), lf = p[3];
+    double phase = t - t0;
+    double ps = std::log(1.0 + std::exp(phase)) + 1e-6;
+    double sig_p = std::exp(phase) / (1.0 + std::exp(phase));
+    double f = 1.0 / (1.0 + std::exp(-lf));
+    double e_ni = std::exp(-ps / TAU_NI), e_co = std::exp(-ps / TAU_CO);
+    double heat = f * e_ni + (1.0 - f) * e_co;
+    double x = ps / tm;
+    double exp_x2 = std::exp(-x * x);
+    double trap = 1.0 - exp_x2;
+    double flux = a * heat * trap;
+    o[0] = flux;
+    double dheat_dps = -f * e_ni / TAU_NI - (1.0 - f) * e_co / TAU_CO;
+    double dtrap_dps = 2.0 * ps * exp_x2 / (tm * tm);
+    o[1] = a * (-sig_p) * (dheat_dps * trap + heat * dtrap_dps);
+    o[2] = -2.0 * a * heat * exp_x2 * x * x;
+    o[3] = a * trap * (e_ni - e_co) * f * (1.0 - f);
+    o[4] = 0.0;
+}
+static inline double magnetar(const double* p, double t) {
+    double a = std::exp(p[0]), t0 = p[1], tsd = std::exp(p[2]), tdiff = std::exp(p[3]);
+    double phase = t - t0;
+    double ps = std::log(1.0 + std::exp(phase)) + 1e-6;
+    double w = 1.0 + ps / tsd;
+    double spindown = 1.0 / (w * w);
+    double x = ps / tdiff;
+    double trap = 1.0 - std::exp(-x * x);
+    return a * spindown * trap;
+}
+static inline void magnetar_grad(const double* p, double t, double* o) {
+    double a = std::exp(p[0]), t0 = p[1], tsd = std::exp(p[2]), tdiff = std::exp(p[3]);
+    double phase = t - t0;
+    double ps = std::log(1.0 + std::exp(phase)) + 1e-6;
+    double sig_p = std::exp(phase) / (1.0 + std::exp(phase));
+    double w = 1.0 + ps / tsd;
+    double spindown = 1.0 / (w * w);
+    double x = ps / tdiff;
+    double exp_x2 = std::exp(-x * x);
+    double trap = 1.0 - exp_x2;
+    double flux = a * spindown * trap;
+    o[0] = flux;
+    double w3 = 1.0 / (w * w * w);
+    double dspindown_dps = -2.0 * w3 / tsd;
+    double dtrap_dps = 2.0 * ps * exp_x2 / (tdiff * tdiff);
+    o[1] = a * (-sig_p) * (dspindown_dps * trap + spindown * dtrap_dps);
+    o[2] = a * trap * 2.0 * ps * w3 / tsd;
+    o[3] = -2.0 * a * spindown * exp_x2 * x * x;
+    o[4] = 0.0;
+}
+static inline double shock(const double* p, double t) {
+    double a = std::exp(p[0]), t0 = p[1], n = p[2], ttr = std::exp(p[3]);
+    double phase = t - t0;
+    double sig5 = 1.0 / (1.0 + std::exp(-phase * 5.0));
+    double ps = std::log(1.0 + std::exp(phase)) + 1e-6;
+    double cooling = std::pow(ps, -n);
+    double ratio = ps / ttr;
+    double cutoff = std::exp(-ratio * ratio);
+    return a * sig5 * cooling * cutoff;
+}
+static inline void shock_grad(const double* p, double t, double* o) {
+    double a = std::exp(p[0]), t0 = p[1], n = p[2], ttr = std::exp(p[3]);
+    double phase = t - t0;
+    double sig5 = 1.0 / (1.0 + std::exp(-phase * 5.0));
+    double ps = std::log(1.0 + std::exp(phase)) + 1e-6;
+    double sig_p = std::exp(phase) / (1.0 + std::exp(phase));
+    double cooling = std::pow(ps, -n);
+    double ratio = ps / ttr;
+    double cutoff = std::exp(-ratio * ratio);
+    double base = cooling * cutoff;
+    double flux = a * sig5 * base;
+    o[0] = flux;
+    o[1] = a * base * (-5.0 * sig5 * (1.0 - sig5) + sig5 * sig_p * (n / ps + 2.0 * ps / (ttr * ttr)));
+    o[2] = -flux * std::log(ps);
+    o[3] = flux * 2.0 * ratio * ratio;
+    o[4] = 0.0;
+}
+static inline double afterglow(const double* p, double t) {
+    double a = std::exp(p[0]), t0 = p[1], tb = std::exp(p[2]), a1 = p[3], a2 = p[4];
+    double phase = t - t0;
+    double ps = std::log(1.0 + std::exp(phase)) + 1e-6;
+    double ln_r = std::log(ps / tb);
+    double u1 = std::exp(2.0 * a1 * ln_r), u2 = std::exp(2.0 * a2 * ln_r);
+    return a * std::pow(u1 + u2, -0.5);
+}
+static inline void afterglow_grad(const double* p, double t, double* o) {
+    double a = std::exp(p[0]), t0 = p[1], tb = std::exp(p[2]), a1 = p[3], a2 = p[4];
+    double phase = t - t0;
+    double ps = std::log(1.0 + std::exp(phase)) + 1e-6;
+    double sig_p = std::exp(phase) / (1.0 + std::exp(phase));
+    double ln_r = std::log(ps / tb);
+    double u1 = std::exp(2.0 * a1 * ln_r), u2 = std::exp(2.0 * a2 * ln_r);
+    double u = u1 + u2;
+    double flux = a * std::pow(u, -0.5);
+    o[0] = flux;
+    double um15 = std::pow(u, -1.5);
+    double du_dps = (2.0 * a1 * u1 + 2.0 * a2 * u2) / ps;
+    double dflux_dps = a * (-0.5) * um15 * du_dps;
+    o[1] = dflux_dps * (-sig_p);
+    double du_dlog_tb = -(2.0 * a1 * u1 + 2.0 * a2 * u2);
+    o[2] = a * (-0.5) * um15 * du_dlog_tb;
+    o[3] = a * (-0.5) * um15 * 2.0 * ln_r * u1;
+    o[4] = a * (-0.5) * um15 * 2.0 * ln_r * u2;
+    o[5] = 0.0;
+}
+
+static inline double eval_model(int m, const double* p, double t) {
+    switch (m) {
+        case BAZIN: return bazin(p, t);
+        case VILLAR: return villar(p, t);
+        case TDE: return tde(p, t);
+        case ARNETT: return arnett(p, t);
+        case MAGNETAR: return magnetar(p, t);
+        case SHOCK: return shock(p, t);
+        default: return afterglow(p, t);
+    }
+}
+static inline void eval_grad(int m, const double* p, double t, double* o) {
+    switch (m) {
+        case BAZIN: bazin_grad(p, t, o); break;
+        case VILLAR: villar_grad(p, t, o); break;
+        case TDE: tde_grad(p, t, o); break;
+        case ARNETT: arnett_grad(p, t, o); break;
+        case MAGNETAR: magnetar_grad(p, t, o); break;
+        case SHOCK: shock_grad(p, t, o); break;
+        default: afterglow_grad(p, t, o); break;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// MetzgerKN one-zone kilonova, metzger_kn_eval_batch src/parametric.rs:544-648
+// ---------------------------------------------------------------------------
+static const double MSUN_CGS = 1.989e33, C_CGS = 2.998e10, SECS_PER_DAY = 86400.0;
+static void metzger_batch(const double* p, const double* times, int n, double* out) {
+    double m_ej = std::pow(10.0, p[0]) * MSUN_CGS;
+    double v_ej = std::pow(10.0, p[1]) * C_CGS;
+    double kappa_r = std::pow(10.0, p[2]);
+    double t0 = p[3];
+    double phase_max = 0.01;
+    for (int i = 0; i < n; i++) phase_max = std::fmax(phase_max, times[i] - t0);
+    if (phase_max <= 0.01) {
+        for (int i = 0; i < n; i++) out[i] = 0.0;
+        return;
+    }
+    const int NG = 200;
+    double grid_t[NG], grid_l[NG];
+    double lmin = std::log(0.01), lmax = std::log(phase_max * 1.05);
+    for (int i = 0; i < NG; i++) grid_t[i] = std::exp(lmin + (lmax - lmin) * (double)i / (double)(NG - 1));
+    double ye = 0.1, xn0 = 1.0 - 2.0 * ye, scale = 1e40;
+    double e0 = 0.5 * m_ej * v_ej * v_ej;
+    double e_th = e0 / scale, e_kin = e0 / scale, v = v_ej;
+    double r = grid_t[0] * SECS_PER_DAY * v;
+    for (int i = 0; i < NG; i++) {
+        double t_day = grid_t[i], t_sec = t_day * SECS_PER_DAY;
+        double eth_factor = 0.34 * std::pow(t_day, 0.74);
+        double eth = 0.36 * (std::exp(-0.56 * t_day) + (eth_factor > 1e-10 ? std::log(1.0 + eth_factor) / eth_factor : 1.0));
+        double xn = xn0 * std::exp(-t_sec / 900.0);
+        double eps_neutron = 3.2e14 * xn;
+        double time_term = std::fmax(0.5 - std::atan((t_sec - 1.3) / 0.11) / PI, 1e-30);
+        double eps_rp = 2e18 * eth * std::pow(time_term, 1.3);
+        double l_heat = m_ej * (eps_neutron + eps_rp) / scale;
+        double xr = 1.0 - xn0;
+        double xn_decayed = xn0 - xn;
+        double kappa_eff = 0.4 * xn_decayed + kappa_r * xr;
+        double t_diff = 3.0 * kappa_eff * m_ej / (4.0 * PI * C_CGS * v * t_sec) + r / C_CGS;
+        double l_rad = (e_th > 0.0 && t_diff > 0.0) ? e_th / t_diff : 0.0;
+        grid_l[i] = l_rad;
+        double l_pdv = r > 0.0 ? e_th * v / r : 0.0;
+        if (i < NG - 1) {
+            double dt_sec = (grid_t[i + 1] - grid_t[i]) * SECS_PER_DAY;
+            e_th += (l_heat - l_pdv - l_rad) * dt_sec;
+            if (e_th < 0.0) e_th = 0.0;
+            e_kin += l_pdv * dt_sec;
+            v = std::fmin(std::sqrt(2.0 * e_kin * scale / m_ej), C_CGS);
+            r += v * dt_sec;
+        }
+    }
+    double l_peak = -INF;
+    for (int i = 0; i < NG; i++) l_peak = std::fmax(l_peak, grid_l[i]);
+    if (l_peak <= 0.0 || !std::isfinite(l_peak)) {
+        for (int i = 0; i < n; i++) out[i] = 0.0;
+        return;
+    }
+    for (int k = 0; k < n; k++) {
+        double ph = times[k] - t0;
+        if (ph <= 0.0) { out[k] = 0.0; continue; }
+        if (ph <= grid_t[0]) { out[k] = grid_l[0] / l_peak; continue; }
+        if (ph >= grid_t[NG - 1]) { out[k] = grid_l[NG - 1] / l_peak; continue; }
+        int idx = (int)(std::lower_bound(grid_t, grid_t + NG, ph) - grid_t);  // partition_point(gt < ph)
+        idx = std::max(1, std::min(idx, NG - 1));
+        double frac = (ph - grid_t[idx - 1]) / (grid_t[idx] - grid_t[idx - 1]);
+        double g0 = grid_l[idx - 1] / l_peak, g1 = grid_l[idx] / l_peak;
+        out[k] = g0 + frac * (g1 - g0);
+    }
+}
+// metzger_kn_grad_batch_into, src/parametric.rs:843-860 (forward differences)
+static void metzger_grad_batch(const double* p, const double* times, int n, double* out) {
+    std::vector<double> base(n), fp(n);
+    metzger_batch(p, times, n, base.data());
+    const double eps = 1e-5;
+    for (int i = 0; i < n * 5; i++) out[i] = 0.0;
+    for (int j = 0; j < 4; j++) {
+        double pp[5];
+        for (int q = 0; q < 5; q++) pp[q] = p[q];
+        pp[j] += eps;
+        metzger_batch(pp, times, n, fp.data());
+        for (int i = 0; i < n; i++) out[i * 5 + j] = (fp[i] - base[i]) / eps;
+    }
+}
+
+// eval_model_batch_into, src/parametric.rs:832-841
+static void eval_batch(int m, const double* p, const double* times, int n, double* out) {
+    if (m == METZGER) {
+        metzger_batch(p, times, n, out);
+    } else {
+        for (int i = 0; i < n; i++) out[i] = eval_model(m, p, times[i]);
+    }
+}
+
+// ---------------------------------------------------------------------------
+// erf / log normal CDF, src/parametric.rs:866-901
+// ---------------------------------------------------------------------------
+static inline double erf_approx(double x) {
+    double a = std::fabs(x);
+    double t = 1.0 / (1.0 + 0.3275911 * a);
+    double poly = t * (0.254829592 + t * (-0.284496736 + t * (1.421413741 + t * (-1.453152027 + t * 1.061405429))));
+    double val = 1.0 - poly * std::exp(-a * a);
+    return x >= 0.0 ? val : -val;
+}
+static inline double log_normal_cdf(double x) {
+    if (x > 8.0) return 0.0;
+    if (x < -30.0) return -0.5 * x * x - 0.5 * std::log(2.0 * PI) - std::log(-x);
+    double z = -x * 0.70710678118654752440;
+    double t = 1.0 / (1.0 + 0.3275911 * std::fabs(z));
+    double poly = t * (0.254829592 + t * (-0.284496736 + t * (1.421413741 + t * (-1.453152027 + t * 1.061405429))));
+    double erfc_z = poly * std::exp(-z * z);
+    double phi = z >= 0.0 ? 0.5 * erfc_z : 1.0 - 0.5 * erfc_z;
+    return std::log(std::fmax(phi, 1e-300));
+}
+
+// ---------------------------------------------------------------------------
+// Band preparation, src/parametric.rs:3581-3630 and BandFitData :3014-3025
+// ---------------------------------------------------------------------------
+struct Band {
+    std::vector<double> t, f, fe, var, uf, mags;
+    std::vector<uint8_t> up;
+    double peak = 0.0;
+    int n() const { return (int)t.size(); }
+};
+static bool prepare_band(const double* times, const double* flux, const double* err, int n, Band& b) {
+    if (n <= 0) return false;
+    double peak = std::numeric_limits<double>::lowest();
+    for (int i = 0; i < n; i++) peak = std::fmax(peak, flux[i]);  // fold(f64::MIN, f64::max)
+    if (!(peak > 0.0)) return false;
+    b.peak = peak;
+    b.t.assign(times, times + n);
+    b.f.resize(n); b.fe.resize(n); b.var.resize(n); b.uf.resize(n); b.mags.resize(n); b.up.resize(n);
+    for (int i = 0; i < n; i++) {
+        b.f[i] = flux[i] / peak;
+        b.fe[i] = err[i] / peak;
+        b.up[i] = (err[i] > 0.0 && (flux[i] / err[i]) < 3.0) ? 1 : 0;
+        b.uf[i] = 3.0 * err[i] / peak;
+        b.mags[i] = -2.5 * std::log10(flux[i]) + 23.9;
+        b.var[i] = b.fe[i] * b.fe[i] + 1e-10;
+    }
+    return true;
+}
+
+// ---------------------------------------------------------------------------
+// PsoCost, src/parametric.rs:1285-1446
+// ---------------------------------------------------------------------------
+struct Cost {
+    const Band* b;
+    int m;
+    bool use_prior;
+    std::vector<double> pc, pw;
+    mutable std::vector<double> pred;
+    Cost(const Band* band, int model, bool prior) : b(band), m(model), use_prior(prior) {
+        if (prior) population_priors(model, pc, pw);
+        pred.resize(band->n());
+    }
+    // cost_from_slice, :1303-1370
+    double operator()(const double* p) const {
+        if (m == VILLAR) {
+            double beta = p[1], gamma = std::exp(p[2]), tr = std::exp(p[4]), tf = std::exp(p[5]);
+            double c1 = std::fmax(gamma * beta - 1.0, 0.0);
+            double c2 = std::fmax(std::exp(-gamma / tr) * (tf / tr - 1.0) - 1.0, 0.0);
+            double c3 = std::fmax(beta * tf - 1.0 + beta * gamma, 0.0);
+            double c = c1 + c2 + c3;
+            if (c > 0.0) return 1e12 + 10000.0 * c;
+        }
+        int n = b->n();
+        double se = std::exp(p[SE_IDX[m]]);
+        double se2 = se * se;
+        eval_batch(m, p, b->t.data(), n, pred.data());
+        if (m == METZGER) {
+            double mx = -INF;
+            for (int i = 0; i < n; i++) if (!b->up[i]) mx = std::fmax(mx, pred[i]);
+            if (mx > 1e-10 && std::isfinite(mx)) {
+                double s = std::min(std::max(1.0 / mx, 0.1), 10.0);
+                for (int i = 0; i < n; i++) pred[i] *= s;
+            }
+        }
+        double nn = (double)std::max(n, 1);
+        double nll = 0.0;
+        for (int i = 0; i < n; i++) {
+            double pr = pred[i];
+            if (!std::isfinite(pr)) return 1e99;
+            double tv = b->var[i] + se2;
+            if (b->up[i]) {
+                double z = (b->uf[i] - pr) / std::sqrt(tv);
+                nll -= log_normal_cdf(z);
+            } else {
+                double d = pr - b->f[i];
+                nll += d * d / tv + std::log(tv);
+            }
+        }
+        if (use_prior) {
+            double nlp = 0.0;
+            for (size_t j = 0; j < pc.size(); j++) {
+                if (pw[j] > 0.0) {
+                    double z = (p[j] - pc[j]) / pw[j];
+                    nlp += 0.5 * z * z;
+                }
+            }
+            nll += nlp / nn;
+        }
+        return nll / nn;
+    }
+    // gradient, :1387-1445 (population prior and Villar constraint are not differentiated)
+    void gradient(const double* p, double* g) const {
+        int n = b->n(), np = N_PARAMS[m], se_idx = SE_IDX[m];
+        double nn = (double)std::max(n, 1);
+        double se = std::exp(p[se_idx]);
+        double se2 = se * se;
+        eval_batch(m, p, b->t.data(), n, pred.data());
+        for (int j = 0; j < np; j++) g[j] = 0.0;
+        double mg[LCF_MAX_PARAMS];
+        std::vector<double> kn;
+        if (m == METZGER) {
+            kn.resize((size_t)n * 5);
+            metzger_grad_batch(p, b->t.data(), n, kn.data());
+        }
+        for (int i = 0; i < n; i++) {
+            double pr = pred[i];
+            if (!std::isfinite(pr)) {
+                for (int j = 0; j < np; j++) g[j] = 0.0;
+                return;
+            }
+            double tv = b->var[i] + se2;
+            if (m == METZGER) {
+                for (int j = 0; j < np; j++) mg[j] = kn[(size_t)i * 5 + j];
+            } else {
+                eval_grad(m, p, b->t[i], mg);
+            }
+            if (b->up[i]) {
+                double sv = std::sqrt(tv);
+                double z = (b->uf[i] - pr) / sv;
+                double phi = std::exp(-0.5 * z * z) / std::sqrt(2.0 * PI);
+                double cdf = 0.5 * (1.0 + erf_approx(z / 1.41421356237309504880));
+                double ratio = phi / std::fmax(cdf, 1e-300);
+                for (int j = 0; j < np; j++) g[j] += ratio * mg[j] / sv;
+                g[se_idx] += ratio * z * se2 / tv;
+            } else {
+                double d = pr - b->f[i];
+                double sc = 2.0 * d / tv;
+                for (int j = 0; j < np; j++) g[j] += sc * mg[j];
+                double dvar = 2.0 * se2;
+                g[se_idx] += (-d * d / (tv * tv) + 1.0 / tv) * dvar;
+            }
+        }
+        for (int j = 0; j < np; j++) g[j] /= nn;
+    }
+};
+
+// ---------------------------------------------------------------------------
+// PSO, pso_minimize src/parametric.rs:1646-1757 and
+// pso_minimize_seeded :1160-1266
+// ---------------------------------------------------------------------------
+struct PsoStats {
+    long long runs = 0, iters = 0, gbest_changes = 0, evals = 0;
+};
+static thread_local PsoStats g_pso_stats;
+
+template <class F>
+static double pso_minimize(F& cost_fn, const std::vector<double>& lo, const std::vector<double>& hi,
+                           int P, int max_iters, int stall_iters, uint64_t seed,
+                           const double* seed_particle, std::vector<double>& gbest_out) {
+    int dim = (int)lo.size();
+    SmallRng rng(seed);
+    const double w_max = 0.9, w_min = 0.4, c1 = 1.5, c2 = 1.5;
+    std::vector<double> vmax(dim);
+    for (int d = 0; d < dim; d++) vmax[d] = 0.5 * (hi[d] - lo[d]);
+    std::vector<double> pos((size_t)P * dim), vel((size_t)P * dim), pb((size_t)P * dim), pbc(P, INF);
+    std::vector<double> gb(dim, 0.0);
+    double gbc = INF;
+    g_pso_stats.runs++;
+    for (int p = 0; p < P; p++) {
+        double* x = &pos[(size_t)p * dim];
+        double* v = &vel[(size_t)p * dim];
+        if (seed_particle) {
+            if (p == 0) {
+                for (int d = 0; d < dim; d++) x[d] = seed_particle[d];
+            } else {
+                for (int d = 0; d < dim; d++) x[d] = lo[d] + rng.f64() * (hi[d] - lo[d]);
+            }
+            for (int d = 0; d < dim; d++) v[d] = vmax[d] * 0.2 * (2.0 * rng.f64() - 1.0);
+        } else {
+            for (int d = 0; d < dim; d++) {
+                x[d] = lo[d] + rng.f64() * (hi[d] - lo[d]);
+                v[d] = vmax[d] * 0.2 * (2.0 * rng.f64() - 1.0);
+            }
+        }
+        double c = cost_fn(x);
+        g_pso_stats.evals++;
+        pbc[p] = c;
+        std::copy(x, x + dim, &pb[(size_t)p * dim]);
+        if (c < gbc) {
+            gbc = c;
+            std::copy(x, x + dim, gb.begin());
+        }
+    }
+    int stall = 0;
+    double prev = gbc;
+    double inv = 1.0 / (double)max_iters;
+    for (int it = 0; it < max_iters; it++) {
+        g_pso_stats.iters++;
+        double w = w_max - (w_max - w_min) * (double)it * inv;
+        for (int p = 0; p < P; p++) {
+            double* x = &pos[(size_t)p * dim];
+            double* v = &vel[(size_t)p * dim];
+            double* pbp = &pb[(size_t)p * dim];
+            for (int d = 0; d < dim; d++) {
+                double r1 = rng.f64();
+                double r2 = rng.f64();
+                double vv = w * v[d] + c1 * r1 * (pbp[d] - x[d]) + c2 * r2 * (gb[d] - x[d]);
+                vv = std::min(std::max(vv, -vmax[d]), vmax[d]);
+                double np = x[d] + vv;
+                if (np <= lo[d]) { x[d] = lo[d]; v[d] = 0.0; }
+                else if (np >= hi[d]) { x[d] = hi[d]; v[d] = 0.0; }
+                else { x[d] = np; v[d] = vv; }
+            }
+            double c = cost_fn(x);
+            g_pso_stats.evals++;
+            if (c < pbc[p]) {
+                pbc[p] = c;
+                std::copy(x, x + dim, pbp);
+                if (c < gbc) {
+                    gbc = c;
+                    std::copy(x, x + dim, gb.begin());
+                    g_pso_stats.gbest_changes++;
+                }
+            }
+        }
+        bool improved = prev - gbc > 0.01 * std::fmax(std::fabs(prev), 1e-10);
+        if (improved) {
+            stall = 0;
+            prev = gbc;
+        } else {
+            stall++;
+            if (stall >= stall_iters) break;
+        }
+    }
+    gbest_out = gb;
+    return gbc;
+}
+
+// ---------------------------------------------------------------------------
+// L-BFGS polish, lbfgs_refine src/parametric.rs:1453-1535, with argmin's
+// LBFGS::new(MoreThuente, 7).with_tolerance_grad(1e-6), max_iters 50.
+// ---------------------------------------------------------------------------
+struct Bounded {
+    const Cost* c;
+    const std::vector<double>* lo;
+    const std::vector<double>* hi;
+    int dim;
+    void clamp(const double* p, double* q) const {
+        for (int d = 0; d < dim; d++) q[d] = std::min(std::max(p[d], (*lo)[d]), (*hi)[d]);
+    }
+    double cost(const double* p) const {
+        double q[LCF_MAX_PARAMS] = {0.0};
+        clamp(p, q);
+        return (*c)(q);
+    }
+    void grad(const double* p, double* g) const {
+        double q[LCF_MAX_PARAMS] = {0.0};
+        clamp(p, q);
+        c->gradient(q, g);
+        for (int d = 0; d < dim; d++) {
+            if ((p[d] <= (*lo)[d] && g[d] > 0.0) || (p[d] >= (*hi)[d] && g[d] < 0.0)) g[d] = 0.0;
+        }
+    }
+};
+
+// Moré–Thuente safeguarded step (MINPACK cstep).  Returns info (0 = bad input).
+// min/max follow Rust's f64::min/max (a NaN operand is ignored), as in argmin.
+static int cstep(double& stx, double& fx, double& dx, double& sty, double& fy, double& dy,
+                 double& stp, double fp, double dp, bool& brackt, double stpmin, double stpmax) {
+    if ((brackt && (stp <= std::fmin(stx, sty) || stp >= std::fmax(stx, sty))) || dx * (stp - stx) >= 0.0 ||
+        stpmax < stpmin)
+        return 0;
+    int info;
+    bool bound;
+    double sgnd = dp * (dx / std::fabs(dx));
+    double stpf, stpc, stpq, theta, s, gamma, p, q, r;
+    if (fp > fx) {
+        info = 1; bound = true;
+        theta = 3.0 * (fx - fp) / (stp - stx) + dx + dp;
+        s = std::fmax(std::fmax(std::fabs(theta), std::fabs(dx)), std::fabs(dp));
+        gamma = s * std::sqrt((theta / s) * (theta / s) - (dx / s) * (dp / s));
+        if (stp < stx) gamma = -gamma;
+        p = (gamma - dx) + theta;
+        q = ((gamma - dx) + gamma) + dp;
+        r = p / q;
+        stpc = stx + r * (stp - stx);
+        stpq = stx + ((dx / ((fx - fp) / (stp - stx) + dx)) / 2.0) * (stp - stx);
+        if (std::fabs(stpc - stx) < std::fabs(stpq - stx)) stpf = stpc;
+        else stpf = stpc + (stpq - stpc) / 2.0;
+        brackt = true;
+    } else if (sgnd < 0.0) {
+        info = 2; bound = false;
+        theta = 3.0 * (fx - fp) / (stp - stx) + dx + dp;
+        s = std::fmax(std::fmax(std::fabs(theta), std::fabs(dx)), std::fabs(dp));
+        gamma = s * std::sqrt((theta / s) * (theta / s) - (dx / s) * (dp / s));
+        if (stp > stx) gamma = -gamma;
+        p = (gamma - dp) + theta;
+        q = ((gamma - dp) + gamma) + dx;
+        r = p / q;
+        stpc = stp + r * (stx - stp);
+        stpq = stp + (dp / (dp - dx)) * (stx - stp);
+        if (std::fabs(stpc - stp) > std::fabs(stpq - stp)) stpf = stpc;
+        else stpf = stpq;
+        brackt = true;
+    } else if (std::fabs(dp) < std::fabs(dx)) {
+        info = 3; bound = true;
+        theta = 3.0 * (fx - fp) / (stp - stx) + dx + dp;
+        s = std::fmax(std::fmax(std::fabs(theta), std::fabs(dx)), std::fabs(dp));
+        gamma = s * std::sqrt(std::fmax(0.0, (theta / s) * (theta / s) - (dx / s) * (dp / s)));
+        if (stp > stx) gamma = -gamma;
+        p = (gamma - dp) + theta;
+        q = (gamma + (dx - dp)) + gamma;
+        r = p / q;
+        if (r < 0.0 && gamma != 0.0) stpc = stp + r * (stx - stp);
+        else if (stp > stx) stpc = stpmax;
+        else stpc = stpmin;
+        stpq = stp + (dp / (dp - dx)) * (stx - stp);
+        if (brackt) {
+            if (std::fabs(stp - stpc) < std::fabs(stp - stpq)) stpf = stpc;
+            else stpf = stpq;
+        } else {
+            if (std::fabs(stp - stpc) > std::fabs(stp - stpq)) stpf = stpc;
+            else stpf = stpq;
+        }
+    } else {
+        info = 4; bound = false;
+        if (brackt) {
+            theta = 3.0 * (fp - fy) / (sty - stp) + dy + dp;
+            s = std::fmax(std::fmax(std::fabs(theta), std::fabs(dy)), std::fabs(dp));
+            gamma = s * std::sqrt((theta / s) * (theta / s) - (dy / s) * (dp / s));
+            if (stp > sty) gamma = -gamma;
+            p = (gamma - dp) + theta;
+            q = ((gamma - dp) + gamma) + dy;
+            r = p / q;
+            stpc = stp + r * (sty - stp);
+            stpf = stpc;
+        } else if (stp > stx) {
+            stpf = stpmax;
+        } else {
+            stpf = stpmin;
+        }
+    }
+    if (fp > fx) {
+        sty = stp; fy = fp; dy = dp;
+    } else {
+        if (sgnd < 0.0) { sty = stx; fy = fx; dy = dx; }
+        stx = stp; fx = fp; dx = dp;
+    }
+    stpf = std::fmin(stpmax, stpf);
+    stpf = std::fmax(stpmin, stpf);
+    stp = stpf;
+    if (brackt && bound) {
+        if (sty > stx) stp = std::fmin(stx + 0.66 * (sty - stx), stp);
+        else stp = std::fmax(stx + 0.66 * (sty - stx), stp);
+    }
+    return info;
+}
+
+static inline double dot(const double* a, const double* b, int n) {
+    double s = 0.0;
+    for (int i = 0; i < n; i++) s += a[i] * b[i];
+    return s;
+}
+
+// Moré–Thuente line search (MINPACK cvsrch) from x along d; on success
+// writes the accepted point, its cost and gradient.  Returns false when d is
+// not a descent direction (argmin raises an error, which aborts the L-BFGS
+// run).  ftol 1e-4, gtol 0.9, xtol 1e-10, step bounds [0, inf), first step 1.
+static bool more_thuente(const Bounded& fn, const double* x, double f0, const double* g0, const double* d, int n,
+                         double* xo, double& fo, double* go) {
+    const double ftol = 1e-4, gtol = 0.9, xtol = 1e-10, xtrapf = 4.0;
+    const double stpmin_g = 0.0, stpmax_g = INF;
+    double dginit = dot(g0, d, n);
+    if (dginit >= 0.0) return false;
+    bool brackt = false, stage1 = true;
+    int infoc = 1;
+    double finit = f0, dgtest = ftol * dginit;
+    double width = stpmax_g - stpmin_g, width1 = 2.0 * width;
+    double stx = 0.0, fx = finit, dgx = dginit, sty = 0.0, fy = finit, dgy = dginit;
+    double stp = 1.0;
+    for (int iter = 0; iter < 100; iter++) {
+        double stmin, stmax;
+        if (brackt) { stmin = std::fmin(stx, sty); stmax = std::fmax(stx, sty); }
+        else { stmin = stx; stmax = stp + xtrapf * (stp - stx); }
+        stp = std::fmax(stp, stpmin_g);
+        stp = std::fmin(stp, stpmax_g);
+        if ((brackt && (stp <= stmin || stp >= stmax)) || infoc == 0 || (brackt && stmax - stmin <= xtol * stmax))
+            stp = stx;
+        for (int i = 0; i < n; i++) xo[i] = x[i] + stp * d[i];
+        double f = fn.cost(xo);
+        fn.grad(xo, go);
+        double dg = dot(go, d, n);
+        double ftest1 = finit + stp * dgtest;
+        int info = 0;
+        if ((brackt && (stp <= stmin || stp >= stmax)) || infoc == 0) info = 6;
+        if (stp == stpmax_g && f <= ftest1 && dg <= dgtest) info = 5;
+        if (stp == stpmin_g && (f > ftest1 || dg >= dgtest)) info = 4;
+        if (brackt && stmax - stmin <= xtol * stmax) info = 2;
+        if (f <= ftest1 && std::fabs(dg) <= gtol * (-dginit)) info = 1;
+        if (info != 0) { fo = f; return true; }
+        if (stage1 && f <= ftest1 && dg >= std::fmin(ftol, gtol) * dginit) stage1 = false;
+        if (stage1 && f <= fx && f > ftest1) {
+            double fm = f - stp * dgtest, fxm = fx - stx * dgtest, fym = fy - sty * dgtest;
+            double dgm = dg - dgtest, dgxm = dgx - dgtest, dgym = dgy - dgtest;
+            infoc = cstep(stx, fxm, dgxm, sty, fym, dgym, stp, fm, dgm, brackt, stmin, stmax);
+            fx = fxm + stx * dgtest; fy = fym + sty * dgtest;
+            dgx = dgxm + dgtest; dgy = dgym + dgtest;
+        } else {
+            infoc = cstep(stx, fx, dgx, sty, fy, dgy, stp, f, dg, brackt, stmin, stmax);
+        }
+        if (brackt) {
+            if (std::fabs(sty - stx) >= 0.66 * width1) stp = stx + 0.5 * (sty - stx);
+            width1 = width;
+            width = std::fabs(sty - stx);
+        }
+    }
+    fo = fn.cost(xo);
+    return true;
+}
+
+static double lbfgs_refine(const Cost& prob, std::vector<double>& params, double pso_cost,
+                           const std::vector<double>& lo, const std::vector<double>& hi) {
+    if (prob.m == METZGER) return pso_cost;
+    const int n = (int)params.size(), M = 7, MAXIT = 50;
+    const double tol_grad = 1e-6, tol_cost = std::numeric_limits<double>::epsilon();
+    Bounded fn{&prob, &lo, &hi, n};
+    double x[LCF_MAX_PARAMS], g[LCF_MAX_PARAMS];
+    for (int i = 0; i < n; i++) x[i] = params[i];
+    double f = fn.cost(x);
+    fn.grad(x, g);
+    double best_x[LCF_MAX_PARAMS], best_f = INF, prev_f = INF;
+    if (f < best_f) { best_f = f; std::copy(x, x + n, best_x); }
+    std::vector<std::vector<double>> S, Y;
+    int it = 0;
+    bool ok = true;
+    auto converged = [&](void) {
+        if (std::sqrt(dot(g, g, n)) < tol_grad) return true;
+        if (std::fabs(prev_f - f) < tol_cost) return true;
+        return false;
+    };
+    bool stop = converged() || it >= MAXIT;
+    while (!stop) {
+        int cm = (int)S.size();
+        double gamma = 1.0;
+        if (cm > 0) gamma = dot(S.back().data(), Y.back().data(), n) / dot(Y.back().data(), Y.back().data(), n);
+        double q[LCF_MAX_PARAMS];
+        std::copy(g, g + n, q);
+        double alpha[8], rho[8];
+        for (int i = 0; i < cm; i++) {
+            const double* sk = S[cm - 1 - i].data();
+            const double* yk = Y[cm - 1 - i].data();
+            double rt = 1.0 / dot(yk, sk, n);
+            alpha[i] = rt * dot(sk, q, n);
+            for (int k = 0; k < n; k++) q[k] -= yk[k] * alpha[i];
+            rho[i] = rt;
+        }
+        double r[LCF_MAX_PARAMS];
+        for (int k = 0; k < n; k++) r[k] = q[k] * gamma;
+        for (int i = 0; i < cm; i++) {
+            const double* sk = S[i].data();
+            const double* yk = Y[i].data();
+            double beta = dot(yk, r, n) * rho[cm - i - 1];
+            for (int k = 0; k < n; k++) r[k] += sk[k] * (alpha[cm - i - 1] - beta);
+        }
+        double dvec[LCF_MAX_PARAMS];
+        for (int k = 0; k < n; k++) dvec[k] = -r[k];
+        double xn[LCF_MAX_PARAMS], gn[LCF_MAX_PARAMS], fnew;
+        if (!more_thuente(fn, x, f, g, dvec, n, xn, fnew, gn)) { ok = false; break; }
+        fn.grad(xn, gn);
+        std::vector<double> s(n), y(n);
+        for (int k = 0; k < n; k++) { s[k] = xn[k] - x[k]; y[k] = gn[k] - g[k]; }
+        S.push_back(s); Y.push_back(y);
+        if ((int)S.size() > M) { S.erase(S.begin()); Y.erase(Y.begin()); }
+        std::copy(xn, xn + n, x);
+        std::copy(gn, gn + n, g);
+        prev_f = f;
+        f = fnew;
+        if (f < best_f) { best_f = f; std::copy(x, x + n, best_x); }
+        it++;
+        stop = converged() || it >= MAXIT;
+    }
+    if (!ok) return pso_cost;
+    double cl[LCF_MAX_PARAMS];
+    fn.clamp(best_x, cl);
+    double fc = prob(cl);
+    if (fc < pso_cost && std::isfinite(fc)) {
+        for (int i = 0; i < n; i++) params[i] = cl[i];
+        return fc;
+    }
+    return pso_cost;
+}
+
+// ---------------------------------------------------------------------------
+// pso_fit_single_model, src/parametric.rs:1864-1999
+// ---------------------------------------------------------------------------
+static inline double clampd(double v, double lo, double hi) { return std::min(std::max(v, lo), hi); }
+
+struct SingleFit {
+    std::vector<double> params;
+    double cost;
+};
+static SingleFit pso_fit_single_model(const Band& b, int m) {
+    std::vector<double> lo, hi;
+    pso_bounds(m, lo, hi);
+    Cost prob(&b, m, true);
+    int t0i = T0_IDX[m], n = b.n();
+    double peak_time = b.t[0], peak_flux = -INF;
+    for (int i = 0; i < n; i++) if (!b.up[i] && b.f[i] > peak_flux) { peak_flux = b.f[i]; peak_time = b.t[i]; }
+    double t_first = INF;
+    for (int i = 0; i < n; i++) t_first = std::fmin(t_first, b.t[i]);
+    if (n > 0) {
+        double t0_lo = std::fmax(t_first - 30.0, lo[t0i]);
+        double t0_hi = std::fmin(peak_time + 10.0, hi[t0i]);
+        if (t0_lo < t0_hi) { lo[t0i] = t0_lo; hi[t0i] = t0_hi; }
+    }
+    std::vector<double> pc, pw;
+    population_priors(m, pc, pw);
+    int dim = (int)lo.size();
+    std::vector<double> seed_a(dim), seed_b(dim);
+    for (int d = 0; d < dim; d++) {
+        double v = d < (int)pc.size() ? clampd(pc[d], lo[d], hi[d]) : 0.5 * (lo[d] + hi[d]);
+        seed_a[d] = v;
+        seed_b[d] = v;
+    }
+    seed_a[t0i] = clampd(peak_time - 5.0, lo[t0i], hi[t0i]);
+    seed_b[t0i] = clampd(t_first - 15.0, lo[t0i], hi[t0i]);
+    const uint64_t seeds[3] = {42, 137, 271};
+    std::vector<double> best;
+    double best_c = INF;
+    for (int i = 0; i < 3; i++) {
+        std::vector<double> gp;
+        const double* sp = i == 1 ? seed_a.data() : (i == 2 ? seed_b.data() : nullptr);
+        double c = pso_minimize(prob, lo, hi, 30, 60, 12, seeds[i], n > 0 ? sp : nullptr, gp);
+        if (c < best_c) { best_c = c; best = gp; }
+    }
+    SingleFit r;
+    r.params = best;
+    r.cost = lbfgs_refine(prob, r.params, best_c, lo, hi);
+    return r;
+}
+
+// pso_model_select, src/parametric.rs:2001-2066
+struct Selection {
+    int model;
+    std::vector<double> params;
+    double cost;
+    double per_chi2[8];
+    std::vector<double> per_params[8];
+};
+static Selection pso_model_select(const Band& b, bool fit_all) {
+    Selection s;
+    for (int i = 0; i < 8; i++) s.per_chi2[i] = NaN;
+    double nn = (double)std::max(b.n(), 1);
+    double ln_n = std::log(nn);
+    auto bic = [&](double c, int m) { return 2.0 * c * nn + (double)N_PARAMS[m] * ln_n; };
+    SingleFit bz = pso_fit_single_model(b, BAZIN);
+    s.per_chi2[BAZIN] = std::isfinite(bz.cost) ? bz.cost : NaN;
+    if (fit_all) s.per_params[BAZIN] = bz.params;
+    s.model = BAZIN;
+    s.params = bz.params;
+    s.cost = bz.cost;
+    double best_bic = bic(bz.cost, BAZIN);
+    if (!fit_all && bz.cost < 2.0) return s;  // BAZIN_GOOD_ENOUGH, :1862
+    for (int k = 1; k < 8; k++) {
+        int m = SELECT_ORDER[k];
+        SingleFit r = pso_fit_single_model(b, m);
+        s.per_chi2[m] = std::isfinite(r.cost) ? r.cost : NaN;
+        if (fit_all) s.per_params[m] = r.params;
+        double mb = bic(r.cost, m);
+        if (mb < best_bic) { best_bic = mb; s.cost = r.cost; s.model = m; s.params = r.params; }
+    }
+    return s;
+}
+
+// profile_t0_search, src/parametric.rs:1767-1849
+static double linspace_at(double a, double b, int n, int i) {
+    if (n <= 1) return a;
+    double step = (b - a) / (double)(n - 1);
+    return a + (double)i * step;
+}
+static void profile_t0_search(const Band& b, int m, std::vector<double>& params, double& cost) {
+    int t0i = T0_IDX[m];
+    double pilot_t0 = params[t0i];
+    double t_first = INF;
+    for (int i = 0; i < b.n(); i++) t_first = std::fmin(t_first, b.t[i]);
+    double t0_min = std::fmax(pilot_t0 - 5.0, t_first - 10.0), t0_max = pilot_t0 + 5.0;
+    std::vector<double> lo, hi;
+    pso_bounds(m, lo, hi);
+    lo.erase(lo.begin() + t0i);
+    hi.erase(hi.begin() + t0i);
+    Cost prob(&b, m, false);
+    auto run_at = [&](double t0, std::vector<double>& full) {
+        double fullbuf[LCF_MAX_PARAMS];
+        auto fn = [&](const double* q) {
+            int fi = 0;
+            for (int i = 0; i < (int)lo.size(); i++) {
+                if (i == t0i) fullbuf[fi++] = t0;
+                fullbuf[fi++] = q[i];
+            }
+            if (t0i >= (int)lo.size()) fullbuf[fi] = t0;
+            return prob(fullbuf);
+        };
+        std::vector<double> red;
+        double c = pso_minimize(fn, lo, hi, 30, 60, 12, 42, nullptr, red);
+        full.clear();
+        for (int i = 0; i < (int)red.size(); i++) {
+            if (i == t0i) full.push_back(t0);
+            full.push_back(red[i]);
+        }
+        if (t0i >= (int)red.size()) full.push_back(t0);
+        return c;
+    };
+    std::vector<double> best = params;
+    double best_c = cost, best_t0 = pilot_t0;
+    for (int k = 0; k < 5; k++) {
+        double t0 = linspace_at(t0_min, t0_max, 5, k);
+        std::vector<double> full;
+        double c = run_at(t0, full);
+        if (c < best_c && !full.empty()) { best_c = c; best = full; best_t0 = t0; }
+    }
+    double fmin_ = std::fmax(best_t0 - 0.5, t0_min), fmax_ = std::fmin(best_t0 + 0.5, t0_max);
+    for (int k = 0; k < 3; k++) {
+        double t0 = linspace_at(fmin_, fmax_, 3, k);
+        std::vector<double> full;
+        double c = run_at(t0, full);
+        if (c < best_c && !full.empty()) { best_c = c; best = full; }
+    }
+    params = best;
+    cost = best_c;
+}
+
+// ---------------------------------------------------------------------------
+// SVI, svi_fit src/parametric.rs:2215-2454 (ManualAdam :40-79)
+// ---------------------------------------------------------------------------
+struct Uncert {
+    std::vector<double> mu, log_sigma;
+    double elbo;
+    int steps = 0;
+};
+static Uncert svi_fit(int m, const Band& b, int n_steps, int n_samples, double lr, const std::vector<double>& init) {
+    int np = N_PARAMS[m], nv = 2 * np, n = b.n(), se = SE_IDX[m];
+    std::vector<double> vp(nv);
+    for (int i = 0; i < np; i++) { vp[i] = init[i]; vp[np + i] = -1.0; }
+    std::vector<double> am(nv, 0.0), av(nv, 0.0);
+    int at = 0;
+    const double b1 = 0.9, b2 = 0.999, aeps = 1e-8;
+    SmallRng rng(42);
+    std::vector<double> pc, pw;
+    prior_params(m, pc, pw);
+    std::vector<double> eps(np), th(np), sg(np), preds(n), gb(np), gmu(np), gls(np), dll(np), neg(nv);
+    std::vector<double> kn;
+    if (m == METZGER) kn.resize((size_t)n * np);
+    double final_elbo = -INF;
+    const int stall_iters = 50, min_iters = 200;
+    const double ema_alpha = 0.1;
+    double ema = -INF, best_ema = -INF;
+    int no_imp = 0, steps_run = 0;
+    for (int step = 0; step < n_steps; step++) {
+        steps_run = step + 1;
+        for (int j = 0; j < np; j++) sg[j] = std::exp(vp[np + j]);
+        for (int j = 0; j < np; j++) { gmu[j] = 0.0; gls[j] = 0.0; }
+        double elbo_sum = 0.0;
+        for (int smp = 0; smp < n_samples; smp++) {
+            for (int j = 0; j < np; j++) {
+                double u1 = std::fmax(rng.f64(), 1e-10);
+                double u2 = rng.f64();
+                eps[j] = std::sqrt(-2.0 * std::log(u1)) * std::cos(2.0 * PI * u2);
+                th[j] = vp[j] + sg[j] * eps[j];
+            }
+            double sx = std::exp(th[se]);
+            double sx2 = sx * sx;
+            if (m == METZGER) {
+                metzger_batch(th.data(), b.t.data(), n, preds.data());
+                metzger_grad_batch(th.data(), b.t.data(), n, kn.data());
+                double mx = -INF;
+                for (int i = 0; i < n; i++) if (!b.up[i]) mx = std::fmax(mx, preds[i]);
+                if (mx > 1e-10 && std::isfinite(mx)) {
+                    double raw = 1.0 / mx;
+                    double scl = std::min(std::max(raw, 0.1), 10.0);
+                    if (std::fabs(raw - scl) / raw > 0.5) continue;
+                    for (int i = 0; i < n; i++) preds[i] *= scl;
+                    for (auto& g : kn) g *= scl;
+                }
+            } else {
+                for (int i = 0; i < n; i++) preds[i] = eval_model(m, th.data(), b.t[i]);
+            }
+            double ll = 0.0;
+            for (int j = 0; j < np; j++) dll[j] = 0.0;
+            for (int i = 0; i < n; i++) {
+                double pr = preds[i];
+                if (!std::isfinite(pr)) continue;
+                double tv = b.var[i] + sx2;
+                double st = std::sqrt(tv);
+                if (m == METZGER) {
+                    for (int j = 0; j < np; j++) gb[j] = kn[(size_t)i * np + j];
+                } else {
+                    eval_grad(m, th.data(), b.t[i], gb.data());
+                }
+                if (b.up[i]) {
+                    double z = (b.uf[i] - pr) / st;
+                    ll += log_normal_cdf(z);
+                    double phi = std::exp(-0.5 * z * z) / std::sqrt(2.0 * PI);
+                    double cdf = std::fmax(0.5 * (1.0 + erf_approx(z * 0.70710678118654752440)), 1e-300);
+                    double dpred = -phi / (cdf * st);
+                    for (int j = 0; j < np; j++) if (j != se && std::isfinite(gb[j])) dll[j] += dpred * gb[j];
+                    double dz = -(b.uf[i] - pr) * sx2 / (st * tv);
+                    dll[se] += (phi / cdf) * dz;
+                } else {
+                    double res = b.f[i] - pr;
+                    double it = 1.0 / tv;
+                    double r2 = res * res;
+                    ll += -0.5 * (r2 * it + std::log(2.0 * PI * tv));
+                    for (int j = 0; j < np; j++) if (j != se && std::isfinite(gb[j])) dll[j] += res * it * gb[j];
+                    dll[se] += (r2 * it * it - it) * sx2;
+                }
+            }
+            double lp = 0.0;
+            for (int j = 0; j < np; j++) {
+                double center = j == se ? pc[j] : init[j];
+                double var = pw[j] * pw[j];
+                double dd = th[j] - center;
+                lp += -0.5 * dd * dd / var;
+                double dlp = -dd / var;
+                double df = dll[j] + dlp;
+                gmu[j] += df;
+                gls[j] += df * sg[j] * eps[j];
+            }
+            elbo_sum += ll + lp;
+        }
+        double ns = (double)n_samples;
+        for (int j = 0; j < np; j++) { gmu[j] /= ns; gls[j] /= ns; }
+        elbo_sum /= ns;
+        double ent = 0.0;
+        for (int j = 0; j < np; j++) ent += vp[np + j];
+        ent += 0.5 * (double)np * std::log(2.0 * PI * 2.71828182845904523536);
+        final_elbo = elbo_sum + ent;
+        for (int j = 0; j < np; j++) { neg[j] = -gmu[j]; neg[np + j] = -(gls[j] + 1.0); }
+        at++;
+        double bc1 = 1.0 - std::pow(b1, (double)at), bc2 = 1.0 - std::pow(b2, (double)at);
+        for (int i = 0; i < nv; i++) {
+            double g = neg[i];
+            if (!std::isfinite(g)) continue;
+            am[i] = b1 * am[i] + (1.0 - b1) * g;
+            av[i] = b2 * av[i] + (1.0 - b2) * g * g;
+            double mh = am[i] / bc1, vh = av[i] / bc2;
+            vp[i] -= lr * mh / (std::sqrt(vh) + aeps);
+        }
+        for (int i = 0; i < np; i++) vp[np + i] = clampd(vp[np + i], -6.0, 2.0);
+        if (step >= min_iters) {
+            if (ema == -INF) ema = final_elbo;
+            else ema = ema_alpha * final_elbo + (1.0 - ema_alpha) * ema;
+            bool imp = ema - best_ema > 0.01 * std::fmax(std::fabs(best_ema), 1e-10);
+            if (imp) { best_ema = ema; no_imp = 0; }
+            else { no_imp++; if (no_imp >= stall_iters) break; }
+        }
+    }
+    Uncert u;
+    u.mu.assign(vp.begin(), vp.begin() + np);
+    u.log_sigma.resize(np);
+    double linf = std::log(4.0);  // SIGMA_INFLATION_FACTOR, :34
+    for (int j = 0; j < np; j++) u.log_sigma[j] = vp[np + j] + linf;
+    u.elbo = final_elbo;
+    u.steps = steps_run;
+    return u;
+}
+
+// ---------------------------------------------------------------------------
+// Laplace, src/parametric.rs:2464-2693
+// ---------------------------------------------------------------------------
+static double neg_log_posterior(int m, const Band& b, const double* p) {
+    int n = b.n(), se = SE_IDX[m];
+    double sx = std::exp(p[se]);
+    double sx2 = sx * sx;
+    std::vector<double> preds(n);
+    eval_batch(m, p, b.t.data(), n, preds.data());
+    if (m == METZGER) {
+        double mx = -INF;
+        for (int i = 0; i < n; i++) if (!b.up[i]) mx = std::fmax(mx, preds[i]);
+        if (mx > 1e-10 && std::isfinite(mx)) {
+            double s = clampd(1.0 / mx, 0.1, 10.0);
+            for (int i = 0; i < n; i++) preds[i] *= s;
+        }
+    }
+    double nll = 0.0;
+    for (int i = 0; i < n; i++) {
+        double pr = preds[i];
+        if (!std::isfinite(pr)) return 1e99;
+        double tv = b.var[i] + sx2;
+        if (b.up[i]) {
+            nll -= log_normal_cdf((b.uf[i] - pr) / std::sqrt(tv));
+        } else {
+            double d = pr - b.f[i];
+            nll += 0.5 * (d * d / tv + std::log(2.0 * PI * tv));
+        }
+    }
+    std::vector<double> pc, pw;
+    prior_params(m, pc, pw);
+    double nlp = 0.0;
+    for (int j = 0; j < N_PARAMS[m]; j++) {
+        double var = pw[j] * pw[j];
+        double d = p[j] - pc[j];
+        nlp += 0.5 * d * d / var;
+    }
+    return nll + nlp;
+}
+// symmetric_eigen (Jacobi), :2517-2587
+static void symmetric_eigen(const double* mat, int n, double* ev, double* V) {
+    double a[36];
+    for (int i = 0; i < n * n; i++) a[i] = mat[i];
+    for (int i = 0; i < n * n; i++) V[i] = 0.0;
+    for (int i = 0; i < n; i++) V[i * n + i] = 1.0;
+    int max_iter = 100 * n * n;
+    for (int itr = 0; itr < max_iter; itr++) {
+        double mv = 0.0;
+        int p = 0, q = 1;
+        for (int i = 0; i < n; i++)
+            for (int j = i + 1; j < n; j++) {
+                double v = std::fabs(a[i * n + j]);
+                if (v > mv) { mv = v; p = i; q = j; }
+            }
+        if (mv < 1e-15) break;
+        double app = a[p * n + p], aqq = a[q * n + q], apq = a[p * n + q];
+        double theta = std::fabs(app - aqq) < 1e-30 ? PI / 4.0 : 0.5 * std::atan(2.0 * apq / (app - aqq));
+        double c = std::cos(theta), s = std::sin(theta);
+        for (int i = 0; i < n; i++) {
+            double aip = a[i * n + p], aiq = a[i * n + q];
+            a[i * n + p] = c * aip + s * aiq;
+            a[i * n + q] = -s * aip + c * aiq;
+        }
+        for (int j = 0; j < n; j++) {
+            double apj = a[p * n + j], aqj = a[q * n + j];
+            a[p * n + j] = c * apj + s * aqj;
+            a[q * n + j] = -s * apj + c * aqj;
+        }
+        a[p * n + p] = c * c * app + 2.0 * c * s * apq + s * s * aqq;
+        a[q * n + q] = s * s * app - 2.0 * c * s * apq + c * c * aqq;
+        a[p * n + q] = 0.0;
+        a[q * n + p] = 0.0;
+        for (int i = 0; i < n; i++) {
+            double vip = V[i * n + p], viq = V[i * n + q];
+            V[i * n + p] = c * vip + s * viq;
+            V[i * n + q] = -s * vip + c * viq;
+        }
+    }
+    for (int i = 0; i < n; i++) ev[i] = a[i * n + i];
+}
+static Uncert laplace_fit(int m, const Band& b, const std::vector<double>& mp) {
+    int nf = (int)mp.size(), se = SE_IDX[m];
+    double f0 = neg_log_posterior(m, b, mp.data());
+    int idx[LCF_MAX_PARAMS], ns = 0;
+    for (int i = 0; i < nf; i++) if (i != se) idx[ns++] = i;
+    double H[36];
+    std::vector<double> pp(mp), pm(mp), mpp(mp), mm(mp);
+    for (int si = 0; si < ns; si++) {
+        int i = idx[si];
+        double hi = 1e-4 * std::fmax(std::fabs(mp[i]), 1.0);
+        for (int sj = si; sj < ns; sj++) {
+            int j = idx[sj];
+            double hj = 1e-4 * std::fmax(std::fabs(mp[j]), 1.0);
+            pp = mp; pm = mp; mpp = mp; mm = mp;
+            pp[i] += hi; pp[j] += hj;
+            pm[i] += hi; pm[j] -= hj;
+            mpp[i] -= hi; mpp[j] += hj;
+            mm[i] -= hi; mm[j] -= hj;
+            double fpp = neg_log_posterior(m, b, pp.data()), fpm = neg_log_posterior(m, b, pm.data());
+            double fmp = neg_log_posterior(m, b, mpp.data()), fmm = neg_log_posterior(m, b, mm.data());
+            double h = (fpp - fpm - fmp + fmm) / (4.0 * hi * hj);
+            H[si * ns + sj] = h;
+            H[sj * ns + si] = h;
+        }
+    }
+    double ev[LCF_MAX_PARAMS], V[36];
+    symmetric_eigen(H, ns, ev, V);
+    double shape_ls[LCF_MAX_PARAMS];
+    for (int i = 0; i < ns; i++) {
+        double sum = 0.0;
+        for (int k = 0; k < ns; k++) {
+            double v = V[i * ns + k];
+            sum += v * v * (1.0 / std::fmax(ev[k], 1e-6));
+        }
+        shape_ls[i] = 0.5 * std::log(std::fmax(sum, 1e-30));
+    }
+    std::vector<double> pc, pw;
+    prior_params(m, pc, pw);
+    Uncert u;
+    u.mu = mp;
+    u.log_sigma.resize(nf);
+    int si = 0;
+    for (int i = 0; i < nf; i++) {
+        if (i == se) u.log_sigma[i] = std::log(pw[i]);
+        else u.log_sigma[i] = shape_ls[si++];
+    }
+    u.elbo = -f0;
+    return u;
+}
+
+// ---------------------------------------------------------------------------
+// Profile refinements, src/parametric.rs:2705-3008
+// ---------------------------------------------------------------------------
+static double band_loglik_skip(int m, const Band& b, const double* p, bool metzger_rescale) {
+    int n = b.n(), se = SE_IDX[m];
+    std::vector<double> preds(n);
+    eval_batch(m, p, b.t.data(), n, preds.data());
+    if (metzger_rescale && m == METZGER) {
+        double mx = -INF;
+        for (int i = 0; i < n; i++) if (!b.up[i]) mx = std::fmax(mx, preds[i]);
+        if (mx > 1e-10 && std::isfinite(mx)) {
+            double s = clampd(1.0 / mx, 0.1, 10.0);
+            for (int i = 0; i < n; i++) preds[i] *= s;
+        }
+    }
+    double sx = std::exp(p[se]);
+    double sx2 = sx * sx;
+    double ll = 0.0;
+    for (int i = 0; i < n; i++) {
+        if (!std::isfinite(preds[i])) continue;
+        double tv = b.var[i] + sx2;
+        if (b.up[i]) {
+            ll += log_normal_cdf((b.uf[i] - preds[i]) / std::sqrt(tv));
+        } else {
+            double r = b.f[i] - preds[i];
+            ll += -0.5 * (r * r / tv + std::log(2.0 * PI * tv));
+        }
+    }
+    return ll;
+}
+static void profile_refine_all(int m, Uncert& u, const Band& b) {
+    int np = (int)u.mu.size(), se = SE_IDX[m];
+    double map_ll = band_loglik_skip(m, b, u.mu.data(), false);
+    double thr = map_ll - 0.5;
+    std::vector<double> lo, hi, pc, pw;
+    pso_bounds(m, lo, hi);
+    population_priors(m, pc, pw);
+    for (int j = 0; j < np; j++) {
+        if (j == se) continue;
+        double mu_j = u.mu[j];
+        double svi_sigma = std::exp(u.log_sigma[j]);
+        double slo = lo[j], shi = hi[j];
+        if (shi - slo < 1e-10) continue;
+        const int NG = 15;
+        double l1 = mu_j, h1 = mu_j;
+        std::vector<double> p(u.mu);
+        for (int gi = 0; gi < NG; gi++) {
+            double val = slo + (shi - slo) * (double)gi / (double)(NG - 1);
+            p = u.mu;
+            p[j] = val;
+            double ll = band_loglik_skip(m, b, p.data(), false);
+            if (ll >= thr) { l1 = std::fmin(l1, val); h1 = std::fmax(h1, val); }
+        }
+        double prof = std::fmax((h1 - l1) / 2.0, 1e-6);
+        double prior_sigma = j < (int)pw.size() ? pw[j] : 0.0;
+        double best = std::fmax(std::fmax(svi_sigma, prof), prior_sigma);
+        u.log_sigma[j] = std::log(best);
+    }
+}
+static void profile_t0_refine(int m, Uncert& u, const Band& b) {
+    int t0i = T0_IDX[m], se = SE_IDX[m], n = b.n();
+    double mu_t0 = u.mu[t0i];
+    double t_first = INF;
+    for (int i = 0; i < n; i++) t_first = std::fmin(t_first, b.t[i]);
+    int pk = 0;
+    double pv = -INF;
+    for (int i = 0; i < n; i++) if (b.f[i] > pv) { pv = b.f[i]; pk = i; }
+    double t_peak = b.t[pk];
+    double t0_lo = t_first - 30.0, t0_hi = t_peak + 5.0;
+    if (t0_lo >= t0_hi) return;
+    const int NG = 25;
+    double sx = std::exp(u.mu[se]);
+    double sx2 = sx * sx;
+    std::vector<double> params(u.mu), shapes(n);
+    double best_t0 = mu_t0, best_ll = -INF;
+    bool has_b = (m == BAZIN || m == TDE);
+    for (int gi = 0; gi < NG; gi++) {
+        double t0 = t0_lo + (t0_hi - t0_lo) * (double)gi / (double)(NG - 1);
+        params = u.mu;
+        params[t0i] = t0;
+        double saved_la = params[0];
+        params[0] = 0.0;
+        double saved_b = 0.0;
+        if (has_b) { saved_b = params[1]; params[1] = 0.0; }
+        eval_batch(m, params.data(), b.t.data(), n, shapes.data());
+        if (has_b) {
+            double sw = 0, sy = 0, sf = 0, syf = 0, sff = 0;
+            for (int i = 0; i < n; i++) {
+                if (b.up[i] || !std::isfinite(shapes[i])) continue;
+                double w = 1.0 / (b.var[i] + sx2);
+                sw += w; sy += w * b.f[i]; sf += w * shapes[i];
+                syf += w * b.f[i] * shapes[i]; sff += w * shapes[i] * shapes[i];
+            }
+            double det = sw * sff - sf * sf;
+            if (std::fabs(det) > 1e-20) {
+                double a_opt = (sw * syf - sf * sy) / det;
+                double b_opt = (sff * sy - sf * syf) / det;
+                if (a_opt > 1e-10) { params[0] = std::log(a_opt); params[1] = b_opt; }
+                else { params[0] = saved_la; params[1] = saved_b; }
+            } else {
+                params[0] = saved_la; params[1] = saved_b;
+            }
+        } else {
+            double num = 0, den = 0;
+            for (int i = 0; i < n; i++) {
+                if (b.up[i] || !std::isfinite(shapes[i])) continue;
+                double w = 1.0 / (b.var[i] + sx2);
+                num += w * b.f[i] * shapes[i];
+                den += w * shapes[i] * shapes[i];
+            }
+            if (den > 1e-20 && num / den > 1e-10) params[0] = std::log(num / den);
+            else params[0] = saved_la;
+        }
+        double ll = band_loglik_skip(m, b, params.data(), true);
+        if (ll > best_ll) { best_ll = ll; best_t0 = t0; }
+    }
+    double lo1 = best_t0, hi1 = best_t0, thr = best_ll - 0.5;
+    std::vector<double> p(u.mu);
+    for (int gi = NG - 1; gi >= 0; gi--) {
+        double t0 = t0_lo + (t0_hi - t0_lo) * (double)gi / (double)(NG - 1);
+        if (t0 >= best_t0) continue;
+        p = u.mu;
+        p[t0i] = t0;
+        if (band_loglik_skip(m, b, p.data(), false) >= thr) lo1 = t0;
+        else break;
+    }
+    for (int gi = 0; gi < NG; gi++) {
+        double t0 = t0_lo + (t0_hi - t0_lo) * (double)gi / (double)(NG - 1);
+        if (t0 <= best_t0) continue;
+        p = u.mu;
+        p[t0i] = t0;
+        if (band_loglik_skip(m, b, p.data(), false) >= thr) hi1 = t0;
+        else break;
+    }
+    double prof = std::fmax((hi1 - lo1) / 2.0, 0.1);
+    u.mu[t0i] = best_t0;
+    u.log_sigma[t0i] = std::log(prof);
+}
+
+// ---------------------------------------------------------------------------
+// MultiBazin, src/parametric.rs:904-1157
+// ---------------------------------------------------------------------------
+struct MultiBazinCost {
+    const Band* b;
+    int k;
+    double operator()(const double* p) const {
+        int n = b->n();
+        double se = std::exp(p[4 * k + 1]);
+        double se2 = se * se;
+        double nn = (double)std::max(n, 1);
+        double nll = 0.0;
+        for (int i = 0; i < n; i++) {
+            double sum = 0.0;
+            for (int c = 0; c < k; c++) {
+                const double* q = p + 4 * c;
+                double a = std::exp(q[0]), tr = std::exp(q[2]), tf = std::exp(q[3]);
+                double dt = b->t[i] - q[1];
+                sum += a * std::exp(-dt / tf) * (1.0 / (1.0 + std::exp(-dt / tr)));
+            }
+            double pr = sum + p[4 * k];
+            if (!std::isfinite(pr)) return 1e99;
+            double tv = b->var[i] + se2;
+            if (b->up[i]) {
+                nll -= log_normal_cdf((b->uf[i] - pr) / std::sqrt(tv));
+            } else {
+                double d = pr - b->f[i];
+                nll += d * d / tv + std::log(tv);
+            }
+        }
+        return nll / nn;
+    }
+};
+static double multi_bazin_eval(const double* p, int k, double t) {
+    double sum = 0.0;
+    for (int c = 0; c < k; c++) {
+        const double* q = p + 4 * c;
+        double a = std::exp(q[0]), tr = std::exp(q[2]), tf = std::exp(q[3]);
+        double dt = t - q[1];
+        sum += a * std::exp(-dt / tf) * (1.0 / (1.0 + std::exp(-dt / tr)));
+    }
+    return sum + p[4 * k];
+}
+struct MBResult {
+    int best_k = 1;
+    std::vector<double> params;
+    double cost = NaN, bic = NaN;
+    std::vector<double> per_k_cost, per_k_bic;
+};
+static MBResult fit_multi_bazin(const Band& b) {
+    MBResult r;
+    int n = b.n();
+    if (n < 5) return r;
+    double tmin = INF, tmax = -INF;
+    for (int i = 0; i < n; i++) { tmin = std::fmin(tmin, b.t[i]); tmax = std::fmax(tmax, b.t[i]); }
+    double nf = (double)n, ln_n = std::log(nf);
+    double best_cost = INF, best_bic = INF;
+    std::vector<double> prev;
+    for (int k = 1; k <= 4; k++) {
+        int np = 4 * k + 2;
+        std::vector<double> lo, hi;
+        for (int c = 0; c < k; c++) {
+            lo.insert(lo.end(), {-3.0, tmin - 30.0, -2.0, -2.0});
+            hi.insert(hi.end(), {3.0, tmax + 30.0, 5.0, 6.0});
+        }
+        lo.push_back(-0.3); hi.push_back(0.3);
+        lo.push_back(-5.0); hi.push_back(0.0);
+        bool have_init = false;
+        std::vector<double> init;
+        if (k > 1 && (int)prev.size() == 4 * (k - 1) + 2) {
+            int pn = (k - 1) * 4;
+            init.assign(prev.begin(), prev.begin() + pn);
+            int pk = 0;
+            double pv = -INF;
+            for (int i = 0; i < n; i++) {
+                double res = b.f[i] - multi_bazin_eval(prev.data(), k - 1, b.t[i]);
+                if (!b.up[i] && res > pv) { pv = res; pk = i; }
+            }
+            init.push_back(std::log(std::fmax(pv, 1e-10)));
+            init.push_back(b.t[pk]);
+            init.push_back(1.0);
+            init.push_back(1.0);
+            init.push_back(prev[pn]);
+            init.push_back(prev[pn + 1]);
+            for (int i = 0; i < np; i++) init[i] = clampd(init[i], lo[i], hi[i]);
+            have_init = true;
+        }
+        MultiBazinCost cost{&b, k};
+        std::vector<double> p1, p2, p3;
+        double c1 = pso_minimize(cost, lo, hi, 30, 60, 12, 42, nullptr, p1);
+        if (have_init) {
+            double c2 = pso_minimize(cost, lo, hi, 30, 60, 12, 137, init.data(), p2);
+            if (c2 < c1) { p1 = p2; c1 = c2; }
+        }
+        double c3 = pso_minimize(cost, lo, hi, 30, 60, 12, 271, nullptr, p3);
+        if (c3 < c1) { p1 = p3; c1 = c3; }
+        double kb = 2.0 * c1 * nf + (double)np * ln_n;
+        r.per_k_cost.push_back(c1);
+        r.per_k_bic.push_back(kb);
+        if (kb < best_bic) { best_bic = kb; best_cost = c1; r.best_k = k; r.params = p1; }
+        prev = p1;
+        if (k > 1 && kb > r.per_k_bic[k - 2] + 2.0) {
+            for (int kk = k + 1; kk <= 4; kk++) { r.per_k_cost.push_back(NaN); r.per_k_bic.push_back(NaN); }
+            break;
+        }
+    }
+    r.cost = best_cost;
+    r.bic = best_bic;
+    return r;
+}
+
+// ---------------------------------------------------------------------------
+// fit_parametric_model, src/parametric.rs:3563-3739 (one source)
+// ---------------------------------------------------------------------------
+static inline double fon(double v) { return std::isfinite(v) ? v : NaN; }
+
+static void fit_source(const lcf_bands_csr* in, const lcf_fit_options* o, int src, lcf_fit_outputs* out) {
+    int b0 = in->source_band_offsets[src], b1 = in->source_band_offsets[src + 1];
+    struct Entry { int band; Band data; };
+    std::vector<Entry> entries;
+    for (int bi = b0; bi < b1; bi++) {
+        out->model[bi] = -1;
+        out->rank[bi] = -1;
+        out->n_obs[bi] = 0;
+        out->mb_best_k[bi] = 0;
+        int64_t o0 = in->band_obs_offsets[bi], o1 = in->band_obs_offsets[bi + 1];
+        Entry e;
+        e.band = bi;
+        if (prepare_band(in->times + o0, in->flux + o0, in->flux_err + o0, (int)(o1 - o0), e.data))
+            entries.push_back(std::move(e));
+    }
+    std::stable_sort(entries.begin(), entries.end(),
+                     [](const Entry& a, const Entry& b) { return a.data.n() > b.data.n(); });
+    for (int rk = 0; rk < (int)entries.size(); rk++) {
+        const Band& b = entries[rk].data;
+        int bi = entries[rk].band;
+        Selection sel;
+        if (o->forced_model >= 0) {
+            SingleFit f = pso_fit_single_model(b, o->forced_model);
+            for (int i = 0; i < 8; i++) sel.per_chi2[i] = NaN;
+            sel.per_chi2[o->forced_model] = fon(f.cost);
+            if (o->fit_all_models) sel.per_params[o->forced_model] = f.params;
+            sel.model = o->forced_model;
+            sel.params = f.params;
+            sel.cost = f.cost;
+        } else {
+            sel = pso_model_select(b, o->fit_all_models != 0);
+        }
+        if (sel.params.empty()) continue;
+        int m = sel.model;
+        std::vector<double> pso_params = sel.params;
+        double pso_chi2 = sel.cost;
+        if (rk == 0 && o->method == LCF_METHOD_SVI) profile_t0_search(b, m, pso_params, pso_chi2);
+        Uncert u = o->method == LCF_METHOD_SVI ? svi_fit(m, b, 1000, 4, 0.01, pso_params) : laplace_fit(m, b, pso_params);
+        profile_t0_refine(m, u, b);
+        profile_refine_all(m, u, b);
+        int n = b.n();
+        std::vector<double> sp(n), mp(n);
+        eval_batch(m, u.mu.data(), b.t.data(), n, sp.data());
+        int npos = 0;
+        for (int i = 0; i < n; i++) if (sp[i] * b.peak > 0.0) npos++;
+        if (npos < n / 2) eval_batch(m, pso_params.data(), b.t.data(), n, mp.data());
+        else mp = sp;
+        double msum = 0.0;
+        int mcount = 0;
+        for (int i = 0; i < n; i++) {
+            double pf = mp[i] * b.peak;
+            if (pf > 0.0 && b.f[i] > 0.0) {
+                double mpred = -2.5 * std::log10(pf) + 23.9;
+                double merr = 1.0857 * b.fe[i] / b.f[i];
+                if (merr > 0.0) {
+                    double res = b.mags[i] - mpred;
+                    msum += res * res / (merr * merr);
+                    mcount++;
+                }
+            }
+        }
+        double mag_chi2 = mcount > 0 ? msum / (double)mcount : NaN;
+        out->model[bi] = m;
+        out->rank[bi] = rk;
+        out->n_obs[bi] = n;
+        int np = N_PARAMS[m];
+        for (int j = 0; j < LCF_MAX_PARAMS; j++) {
+            out->pso_params[bi * 7 + j] = j < np ? pso_params[j] : NaN;
+            out->svi_mu[bi * 7 + j] = j < np ? u.mu[j] : NaN;
+            out->svi_log_sigma[bi * 7 + j] = j < np ? u.log_sigma[j] : NaN;
+        }
+        out->pso_chi2[bi] = fon(pso_chi2);
+        out->svi_elbo[bi] = fon(u.elbo);
+        out->mag_chi2[bi] = fon(mag_chi2);
+        for (int mm = 0; mm < 8; mm++) {
+            out->per_model_chi2[bi * 8 + mm] = sel.per_chi2[mm];
+            for (int j = 0; j < 7; j++) {
+                const std::vector<double>& pp = sel.per_params[mm];
+                out->per_model_params[(bi * 8 + mm) * 7 + j] = j < (int)pp.size() ? pp[j] : NaN;
+            }
+        }
+        out->mb_best_k[bi] = 0;
+        if (rk == 0 && o->run_multi_bazin) {
+            MBResult mb = fit_multi_bazin(b);
+            if (!mb.params.empty()) {
+                out->mb_best_k[bi] = mb.best_k;
+                for (int j = 0; j < LCF_MB_MAX_PARAMS; j++)
+                    out->mb_params[bi * 18 + j] = j < (int)mb.params.size() ? mb.params[j] : NaN;
+                out->mb_cost[bi] = mb.cost;
+                out->mb_bic[bi] = mb.bic;
+                for (int kk = 0; kk < 4; kk++) {
+                    out->mb_per_k_cost[bi * 4 + kk] = kk < (int)mb.per_k_cost.size() ? mb.per_k_cost[kk] : NaN;
+                    out->mb_per_k_bic[bi * 4 + kk] = kk < (int)mb.per_k_bic.size() ? mb.per_k_bic[kk] : NaN;
+                }
+            }
+        }
+    }
+}
+
+}  // namespace orc
+
+// ---------------------------------------------------------------------------
+// C ABI for the tests (ctypes) and the CPU baseline
+// ---------------------------------------------------------------------------
+using namespace orc;
+
+extern "C" {
+
+void orc_rng_stream(uint64_t seed, int n, uint64_t* out) {
+    SmallRng r(seed);
+    for (int i = 0; i < n; i++) out[i] = r.next_u64();
+}
+void orc_rng_f64(uint64_t seed, int n, double* out) {
+    SmallRng r(seed);
+    for (int i = 0; i < n; i++) out[i] = r.f64();
+}
+double orc_log_normal_cdf(double x) { return log_normal_cdf(x); }
+double orc_erf_approx(double x) { return erf_approx(x); }
+
+int orc_eval_model(int m, const double* p, const double* times, int n, double* out) {
+    if (m < 0 || m > 7) return -1;
+    eval_batch(m, p, times, n, out);
+    return 0;
+}
+int orc_eval_grad(int m, const double* p, const double* times, int n, double* out) {
+    if (m < 0 || m > 7) return -1;
+    if (m == METZGER) {
+        metzger_grad_batch(p, times, n, out);
+        return 0;
+    }
+    int np = N_PARAMS[m];
+    for (int i = 0; i < n; i++) eval_grad(m, p, times[i], out + (size_t)i * np);
+    return 0;
+}
+
+static Band make_band(const double* t, const double* f, const double* var, const uint8_t* up, const double* uf, int n) {
+    Band b;
+    b.t.assign(t, t + n);
+    b.f.assign(f, f + n);
+    b.var.assign(var, var + n);
+    b.up.assign(up, up + n);
+    b.uf.assign(uf, uf + n);
+    b.fe.resize(n);
+    for (int i = 0; i < n; i++) b.fe[i] = std::sqrt(std::fmax(var[i] - 1e-10, 0.0));
+    b.peak = 1.0;
+    return b;
+}
+
+// PsoCost::cost_from_slice for n_eval parameter vectors
+int orc_band_cost(int m, const double* t, const double* f, const double* var, const uint8_t* up, const double* uf,
+                  int n, const double* params, int n_eval, int with_prior, double* out) {
+    if (m < 0 || m > 7) return -1;
+    Band b = make_band(t, f, var, up, uf, n);
+    Cost c(&b, m, with_prior != 0);
+    int np = N_PARAMS[m];
+    for (int e = 0; e < n_eval; e++) out[e] = c(params + (size_t)e * np);
+    return 0;
+}
+int orc_band_cost_grad(int m, const double* t, const double* f, const double* var, const uint8_t* up,
+                       const double* uf, int n, const double* params, double* grad) {
+    if (m < 0 || m > 7) return -1;
+    Band b = make_band(t, f, var, up, uf, n);
+    Cost c(&b, m, false);
+    c.gradient(params, grad);
+    return 0;
+}
+// One PSO run of PsoCost(model, prior) within [lo, hi]; seed particle optional.
+double orc_pso_run(int m, const double* t, const double* f, const double* var, const uint8_t* up, const double* uf,
+                   int n, const double* lo, const double* hi, uint64_t seed, const double* seed_particle,
+                   int with_prior, double* gbest) {
+    Band b = make_band(t, f, var, up, uf, n);
+    Cost c(&b, m, with_prior != 0);
+    int np = N_PARAMS[m];
+    std::vector<double> L(lo, lo + np), H(hi, hi + np), g;
+    double cost = pso_minimize(c, L, H, 30, 60, 12, seed, seed_particle, g);
+    for (int j = 0; j < np; j++) gbest[j] = g[j];
+    return cost;
+}
+// lbfgs_refine of `params` (in/out) starting from cost `pso_cost`.
+double orc_lbfgs_refine(int m, const double* t, const double* f, const double* var, const uint8_t* up,
+                        const double* uf, int n, const double* lo, const double* hi, double* params, double pso_cost) {
+    Band b = make_band(t, f, var, up, uf, n);
+    Cost c(&b, m, true);
+    int np = N_PARAMS[m];
+    std::vector<double> L(lo, lo + np), H(hi, hi + np), p(params, params + np);
+    double r = lbfgs_refine(c, p, pso_cost, L, H);
+    for (int j = 0; j < np; j++) params[j] = p[j];
+    return r;
+}
+// svi_fit from init (mu, log_sigma, elbo out); returns steps run
+int orc_svi_fit(int m, const double* t, const double* f, const double* var, const uint8_t* up, const double* uf,
+                int n, const double* init, int n_steps, int n_samples, double lr, double* mu, double* log_sigma,
+                double* elbo) {
+    Band b = make_band(t, f, var, up, uf, n);
+    std::vector<double> ini(init, init + N_PARAMS[m]);
+    Uncert u = svi_fit(m, b, n_steps, n_samples, lr, ini);
+    for (int j = 0; j < N_PARAMS[m]; j++) { mu[j] = u.mu[j]; log_sigma[j] = u.log_sigma[j]; }
+    *elbo = u.elbo;
+    return u.steps;
+}
+int orc_laplace_fit(int m, const double* t, const double* f, const double* var, const uint8_t* up, const double* uf,
+                    int n, const double* map, double* log_sigma, double* elbo) {
+    Band b = make_band(t, f, var, up, uf, n);
+    std::vector<double> mp(map, map + N_PARAMS[m]);
+    Uncert u = laplace_fit(m, b, mp);
+    for (int j = 0; j < N_PARAMS[m]; j++) log_sigma[j] = u.log_sigma[j];
+    *elbo = u.elbo;
+    return 0;
+}
+
+// Whole-batch fit: fit_parametric_model per source, OpenMP over sources.
+int orc_fit_batch(const lcf_bands_csr* in, const lcf_fit_options* o, lcf_fit_outputs* out, int n_threads) {
+    if (!in || !o || !out || in->n_sources < 0) return -1;
+#ifdef _OPENMP
+    if (n_threads > 0) omp_set_num_threads(n_threads);
+#pragma omp parallel for schedule(dynamic, 1)
+#endif
+    for (int s = 0; s < in->n_sources; s++) fit_source(in, o, s, out);
+    return 0;
+}
+
+// PSO instrumentation of the calling thread (runs, iterations, async gbest
+// changes, cost evaluations) since the last reset.
+void orc_pso_stats(long long* out4, int reset) {
+    out4[0] = g_pso_stats.runs;
+    out4[1] = g_pso_stats.iters;
+    out4[2] = g_pso_stats.gbest_changes;
+    out4[3] = g_pso_stats.evals;
+    if (reset) g_pso_stats = PsoStats();
+}
+
+int orc_max_threads(void) {
+#ifdef _OPENMP
+    return omp_get_max_threads();
+#else
+    return 1;
+#endif
+}
+
+}  // extern "C"

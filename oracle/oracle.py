@@ -1,0 +1,182 @@
+"""TEST INFRASTRUCTURE ONLY — ctypes binding of the FP64 C++ oracle
+(oracle/lcf_oracle.cpp), a restatement of the reference's CPU fitting path
+(src/parametric.rs).  Only tests/, __graft_entry__.smoke() and bench.py's
+CPU-baseline / reference arm may import this module; the shipped library never
+does.  The shared library is built by ``build()`` (plain g++ through
+oracle/Makefile) into oracle/_build/."""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(HERE)
+if ROOT not in sys.path:
+    sys.path.insert(0, ROOT)
+
+from lightcurve_fitting_gb300 import abi  # noqa: E402
+
+LIB_PATH = os.path.join(HERE, "_build", "liblcf_oracle.so")
+REF_LIB_PATH = os.path.join(HERE, "_ref", "libref_models.so")
+REF_HEADER = "/root/reference/cuda/models_device.h"
+
+_lib = None
+
+
+def build(force: bool = False) -> str:
+    """Compile the oracle (and the reference pin harness when the reference
+    checkout is present).  Returns the oracle library path."""
+    target = ["all"]
+    if os.path.exists(REF_HEADER):
+        target.append("ref")
+    if force:
+        subprocess.check_call(["make", "-C", HERE, "clean"], stdout=subprocess.DEVNULL)
+    subprocess.check_call(["make", "-C", HERE, *target], stdout=subprocess.DEVNULL)
+    return LIB_PATH
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            build()
+        L = C.CDLL(LIB_PATH)
+        d, i, u64 = C.c_double, C.c_int, C.c_uint64
+        vp = C.c_void_p
+        L.orc_rng_stream.argtypes = [u64, i, vp]
+        L.orc_rng_f64.argtypes = [u64, i, vp]
+        L.orc_log_normal_cdf.argtypes = [d]
+        L.orc_log_normal_cdf.restype = d
+        L.orc_erf_approx.argtypes = [d]
+        L.orc_erf_approx.restype = d
+        L.orc_eval_model.argtypes = [i, vp, vp, i, vp]
+        L.orc_eval_grad.argtypes = [i, vp, vp, i, vp]
+        L.orc_band_cost.argtypes = [i, vp, vp, vp, vp, vp, i, vp, i, i, vp]
+        L.orc_band_cost_grad.argtypes = [i, vp, vp, vp, vp, vp, i, vp, vp]
+        L.orc_pso_run.argtypes = [i, vp, vp, vp, vp, vp, i, vp, vp, u64, vp, i, vp]
+        L.orc_pso_run.restype = d
+        L.orc_lbfgs_refine.argtypes = [i, vp, vp, vp, vp, vp, i, vp, vp, vp, d]
+        L.orc_lbfgs_refine.restype = d
+        L.orc_svi_fit.argtypes = [i, vp, vp, vp, vp, vp, i, vp, i, i, d, vp, vp, vp]
+        L.orc_laplace_fit.argtypes = [i, vp, vp, vp, vp, vp, i, vp, vp, vp]
+        L.orc_fit_batch.argtypes = [C.POINTER(abi.BandsCSR), C.POINTER(abi.FitOptions), C.POINTER(abi.FitOutputs), i]
+        L.orc_pso_stats.argtypes = [vp, i]
+        L.orc_max_threads.restype = i
+        _lib = L
+    return _lib
+
+
+def _p(a):
+    return a.ctypes.data
+
+
+def rng_stream(seed: int, n: int) -> np.ndarray:
+    out = np.zeros(n, np.uint64)
+    lib().orc_rng_stream(seed, n, _p(out))
+    return out
+
+
+def rng_f64(seed: int, n: int) -> np.ndarray:
+    out = np.zeros(n, np.float64)
+    lib().orc_rng_f64(seed, n, _p(out))
+    return out
+
+
+def eval_model(model: int, params, times) -> np.ndarray:
+    p = np.ascontiguousarray(params, np.float64)
+    t = np.ascontiguousarray(times, np.float64)
+    out = np.zeros(t.size)
+    assert lib().orc_eval_model(model, _p(p), _p(t), t.size, _p(out)) == 0
+    return out
+
+
+def eval_grad(model: int, params, times) -> np.ndarray:
+    p = np.ascontiguousarray(params, np.float64)
+    t = np.ascontiguousarray(times, np.float64)
+    npar = abi.N_PARAMS[model]
+    out = np.zeros((t.size, npar))
+    assert lib().orc_eval_grad(model, _p(p), _p(t), t.size, _p(out)) == 0
+    return out
+
+
+class Band:
+    """A peak-normalised band (BandFitData, src/parametric.rs:3014-3025)."""
+
+    def __init__(self, times, flux, flux_err):
+        times = np.asarray(times, np.float64)
+        flux = np.asarray(flux, np.float64)
+        err = np.asarray(flux_err, np.float64)
+        peak = np.max(flux)
+        self.peak = peak
+        self.t = np.ascontiguousarray(times)
+        self.f = np.ascontiguousarray(flux / peak)
+        self.fe = err / peak
+        self.var = np.ascontiguousarray(self.fe ** 2 + 1e-10)
+        self.up = np.ascontiguousarray(((err > 0) & (flux / err < 3.0)).astype(np.uint8))
+        self.uf = np.ascontiguousarray(3.0 * err / peak)
+
+    @property
+    def n(self):
+        return self.t.size
+
+    def args(self):
+        return (_p(self.t), _p(self.f), _p(self.var), _p(self.up), _p(self.uf), self.n)
+
+
+def band_cost(model: int, band: Band, params, with_prior: bool = True) -> np.ndarray:
+    p = np.ascontiguousarray(np.atleast_2d(params), np.float64)
+    out = np.zeros(p.shape[0])
+    assert lib().orc_band_cost(model, *band.args(), _p(p), p.shape[0], int(with_prior), _p(out)) == 0
+    return out
+
+
+def band_cost_grad(model: int, band: Band, params) -> np.ndarray:
+    p = np.ascontiguousarray(params, np.float64)
+    g = np.zeros(abi.N_PARAMS[model])
+    assert lib().orc_band_cost_grad(model, *band.args(), _p(p), _p(g)) == 0
+    return g
+
+
+def pso_run(model: int, band: Band, lo, hi, seed: int, seed_particle=None, with_prior=True):
+    lo = np.ascontiguousarray(lo, np.float64)
+    hi = np.ascontiguousarray(hi, np.float64)
+    g = np.zeros(abi.N_PARAMS[model])
+    sp = None if seed_particle is None else np.ascontiguousarray(seed_particle, np.float64)
+    c = lib().orc_pso_run(model, *band.args(), _p(lo), _p(hi), seed, None if sp is None else _p(sp),
+                          int(with_prior), _p(g))
+    return g, c
+
+
+def svi_fit(model: int, band: Band, init, n_steps=1000, n_samples=4, lr=0.01):
+    ini = np.ascontiguousarray(init, np.float64)
+    npar = abi.N_PARAMS[model]
+    mu, ls, elbo = np.zeros(npar), np.zeros(npar), np.zeros(1)
+    steps = lib().orc_svi_fit(model, *band.args(), _p(ini), n_steps, n_samples, lr, _p(mu), _p(ls), _p(elbo))
+    return mu, ls, float(elbo[0]), steps
+
+
+def fit_batch(batch, fit_all_models=True, method=abi.METHOD_SVI, forced_model=-1, run_multi_bazin=True,
+              n_threads=0) -> abi.FitResult:
+    keep = []
+    csr = abi.csr_struct(batch, keep)
+    opts = abi.options(fit_all_models, method, forced_model, run_multi_bazin)
+    res = abi.FitResult(batch.n_bands)
+    outs = res.as_struct()
+    rc = lib().orc_fit_batch(C.byref(csr), C.byref(opts), C.byref(outs), int(n_threads))
+    if rc != 0:
+        raise RuntimeError(f"oracle fit failed: {rc}")
+    return res
+
+
+def pso_stats(reset=True):
+    out = np.zeros(4, np.int64)
+    lib().orc_pso_stats(_p(out), int(reset))
+    return dict(runs=int(out[0]), iters=int(out[1]), gbest_changes=int(out[2]), evals=int(out[3]))
+
+
+def max_threads() -> int:
+    return int(lib().orc_max_threads())
