@@ -159,6 +159,10 @@ int lcf_download_outputs(lcf_ctx* ctx, lcf_fit_outputs* out);
 /* The context's CUDA stream (a cudaStream_t), for callers that time with events. */
 void* lcf_ctx_stream(lcf_ctx* ctx);
 
+/* Replay the stage sequence from a CUDA graph captured per batch layout
+ * (default 1), or launch the kernels one by one (0). */
+int lcf_set_graph(lcf_ctx* ctx, int enabled);
+
 /*
  * Batched likelihood: cost of `n_eval` parameter vectors of one model on one
  * band, exactly PsoCost::cost_from_slice (src/parametric.rs:1303-1370):

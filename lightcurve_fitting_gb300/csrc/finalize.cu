@@ -1,0 +1,751 @@
+// finalize.cu — the FP64 stages after model selection and the dependent
+// PSO stages' task builders:
+//   * Laplace (laplace_fit, src/parametric.rs:2623-2693): central finite
+//     difference Hessian of the unnormalised negative log-posterior over the
+//     shape parameters, Jacobi eigen-decomposition, eigenvalue clamp 1e-6;
+//   * profile_t0_refine (:2788-3008), profile_refine_all (:2705-2786) and the
+//     magnitude-space chi2 (:3680-3711);
+//   * the profile t0 search (:1767-1849) and the greedy MultiBazin K = 1..4
+//     fit (:1008-1157), whose PSO runs execute in pso.cu and whose task lists
+//     are appended here on the device, so the whole sequence needs no host
+//     round trip;
+//   * the reference's drop-in `launch_*` exports (cuda/models.cu:590-636).
+// One warp per band; the lanes split the observations, the FP64 sums are
+// reduced across the warp.
+#include <cuda_runtime.h>
+
+#include "lcf_internal.cuh"
+#include "models_f64.cuh"
+
+namespace lcf {
+
+#define FULL 0xffffffffu
+
+__device__ __forceinline__ double wsum(double v) {
+    for (int k = 16; k; k >>= 1) v += __shfl_xor_sync(FULL, v, k);
+    return v;
+}
+__device__ __forceinline__ double wmax(double v) {
+    for (int k = 16; k; k >>= 1) v = fmax(v, __shfl_xor_sync(FULL, v, k));
+    return v;
+}
+
+struct BandView {
+    const double *t, *f, *fe, *var, *uf, *mag;
+    const uint8_t* up;
+    int n;
+    double peak;
+};
+__device__ __forceinline__ BandView band_view(const DeviceBatch& d, const BandStats& bs) {
+    BandView v;
+    v.t = d.t64 + bs.off; v.f = d.f64 + bs.off; v.fe = d.fe64 + bs.off; v.var = d.var64 + bs.off;
+    v.uf = d.uf64 + bs.off; v.mag = d.mag64 + bs.off; v.up = d.up + bs.off;
+    v.n = bs.n; v.peak = bs.peak;
+    return v;
+}
+
+// Prediction of observation i (lanes call with their own i).  For MetzgerKN
+// the whole band is first evaluated by lane 0 into `scr` (the sweep is
+// sequential over the grid).
+struct Predictor {
+    int m;
+    const double* p;
+    const double* scr;
+    __device__ double operator()(const BandView& b, int i) const {
+        return m == 7 ? scr[i] : eval_model_f64(m, p, b.t[i]);
+    }
+};
+__device__ void metzger_prepare(int m, const double* p, const BandView& b, double* scr) {
+    if (m != 7) return;
+    if ((threadIdx.x & 31) == 0) metzger_f64(p, b.t, b.n, scr);
+    __syncwarp();
+}
+
+// MetzgerKN rescale of the non-upper peak to 1 (src/parametric.rs:1325-1337)
+__device__ double metzger_scale(const Predictor& P, const BandView& b) {
+    int lane = threadIdx.x & 31;
+    double mx = -INFINITY;
+    for (int i = lane; i < b.n; i += 32)
+        if (!b.up[i]) mx = fmax(mx, P(b, i));
+    mx = wmax(mx);
+    if (mx > 1e-10 && isfinite(mx)) return fmin(fmax(1.0 / mx, 0.1), 10.0);
+    return 1.0;
+}
+
+// neg_log_posterior, src/parametric.rs:2464-2511
+__device__ double neg_log_posterior_w(int m, const BandView& b, const double* p, double* scr) {
+    int lane = threadIdx.x & 31;
+    metzger_prepare(m, p, b, scr);
+    Predictor P{m, p, scr};
+    double scale = m == 7 ? metzger_scale(P, b) : 1.0;
+    double se2 = exp(2.0 * p[se_idx_of(m)]);
+    double nll = 0.0;
+    int nonfinite = 0;
+    for (int i = lane; i < b.n; i += 32) {
+        double pr = P(b, i) * scale;
+        if (!isfinite(pr)) { nonfinite = 1; continue; }
+        double tv = b.var[i] + se2;
+        if (b.up[i]) nll -= log_normal_cdf_f64((b.uf[i] - pr) / sqrt(tv));
+        else {
+            double dd = pr - b.f[i];
+            nll += 0.5 * (dd * dd / tv + log(2.0 * 3.14159265358979323846 * tv));
+        }
+    }
+    if (__any_sync(FULL, nonfinite)) return 1e99;
+    nll = wsum(nll);
+    double nlp = 0.0;
+    for (int j = 0; j < n_params_of(m); j++) {
+        double w = c_pri_w[m][j], dd = p[j] - c_pri_c[m][j];
+        nlp += 0.5 * dd * dd / (w * w);
+    }
+    __syncwarp();
+    return nll + nlp;
+}
+
+// Band log-likelihood skipping non-finite predictions (the profile scans,
+// src/parametric.rs:2716-2726, :2916-2932)
+__device__ double band_ll_w(int m, const BandView& b, const double* p, double* scr, bool metzger_rescale) {
+    int lane = threadIdx.x & 31;
+    metzger_prepare(m, p, b, scr);
+    Predictor P{m, p, scr};
+    double scale = (m == 7 && metzger_rescale) ? metzger_scale(P, b) : 1.0;
+    double se2 = exp(2.0 * p[se_idx_of(m)]);
+    double ll = 0.0;
+    for (int i = lane; i < b.n; i += 32) {
+        double pr = P(b, i) * scale;
+        if (!isfinite(pr)) continue;
+        double tv = b.var[i] + se2;
+        if (b.up[i]) ll += log_normal_cdf_f64((b.uf[i] - pr) / sqrt(tv));
+        else {
+            double r = b.f[i] - pr;
+            ll += -0.5 * (r * r / tv + log(2.0 * 3.14159265358979323846 * tv));
+        }
+    }
+    ll = wsum(ll);
+    __syncwarp();
+    return ll;
+}
+
+// symmetric_eigen (Jacobi), src/parametric.rs:2517-2587
+__device__ void jacobi_eigen(double* a, int n, double* ev, double* V) {
+    for (int i = 0; i < n * n; i++) V[i] = 0.0;
+    for (int i = 0; i < n; i++) V[i * n + i] = 1.0;
+    int max_iter = 100 * n * n;
+    for (int itr = 0; itr < max_iter; itr++) {
+        double mv = 0.0;
+        int p = 0, q = 1;
+        for (int i = 0; i < n; i++)
+            for (int j = i + 1; j < n; j++) {
+                double v = fabs(a[i * n + j]);
+                if (v > mv) { mv = v; p = i; q = j; }
+            }
+        if (mv < 1e-15) break;
+        double app = a[p * n + p], aqq = a[q * n + q], apq = a[p * n + q];
+        double th = fabs(app - aqq) < 1e-30 ? 0.78539816339744830962 : 0.5 * atan(2.0 * apq / (app - aqq));
+        double c = cos(th), s = sin(th);
+        for (int i = 0; i < n; i++) {
+            double aip = a[i * n + p], aiq = a[i * n + q];
+            a[i * n + p] = c * aip + s * aiq;
+            a[i * n + q] = -s * aip + c * aiq;
+        }
+        for (int j = 0; j < n; j++) {
+            double apj = a[p * n + j], aqj = a[q * n + j];
+            a[p * n + j] = c * apj + s * aqj;
+            a[q * n + j] = -s * apj + c * aqj;
+        }
+        a[p * n + p] = c * c * app + 2.0 * c * s * apq + s * s * aqq;
+        a[q * n + q] = s * s * app - 2.0 * c * s * apq + c * c * aqq;
+        a[p * n + q] = 0.0;
+        a[q * n + p] = 0.0;
+        for (int i = 0; i < n; i++) {
+            double vip = V[i * n + p], viq = V[i * n + q];
+            V[i * n + p] = c * vip + s * viq;
+            V[i * n + q] = -s * vip + c * viq;
+        }
+    }
+    for (int i = 0; i < n; i++) ev[i] = a[i * n + i];
+}
+
+__global__ void laplace_kernel(DeviceBatch d) {
+    int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    if (warp >= d.n_bands) return;
+    BandStats bs = d.stats[warp];
+    BandOut& o = d.out[warp];
+    if (!bs.valid || o.model < 0) return;
+    BandView b = band_view(d, bs);
+    int m = o.model, nf = n_params_of(m), se = se_idx_of(m);
+    double* scr = d.scratch64 + 5 * bs.off;
+    double mp[MAXP];
+    for (int j = 0; j < nf; j++) mp[j] = o.pso_params[j];
+    double f0 = neg_log_posterior_w(m, b, mp, scr);
+    int idx[MAXP], ns = 0;
+    for (int i = 0; i < nf; i++)
+        if (i != se) idx[ns++] = i;
+    double H[36];
+    for (int si = 0; si < ns; si++) {
+        int i = idx[si];
+        double hi = 1e-4 * fmax(fabs(mp[i]), 1.0);
+        for (int sj = si; sj < ns; sj++) {
+            int j = idx[sj];
+            double hj = 1e-4 * fmax(fabs(mp[j]), 1.0);
+            double q[MAXP];
+            double fv[4];
+            const double si_[4] = {1, 1, -1, -1}, sj_[4] = {1, -1, 1, -1};
+            for (int k = 0; k < 4; k++) {
+                for (int t = 0; t < nf; t++) q[t] = mp[t];
+                q[i] += si_[k] * hi;
+                q[j] += sj_[k] * hj;
+                fv[k] = neg_log_posterior_w(m, b, q, scr);
+            }
+            double h = (fv[0] - fv[1] - fv[2] + fv[3]) / (4.0 * hi * hj);
+            H[si * ns + sj] = h;
+            H[sj * ns + si] = h;
+        }
+    }
+    if ((threadIdx.x & 31) == 0) {
+        double ev[MAXP], V[36];
+        jacobi_eigen(H, ns, ev, V);
+        double sls[MAXP];
+        for (int i = 0; i < ns; i++) {
+            double sum = 0.0;
+            for (int k = 0; k < ns; k++) sum += V[i * ns + k] * V[i * ns + k] * (1.0 / fmax(ev[k], 1e-6));
+            sls[i] = 0.5 * log(fmax(sum, 1e-30));
+        }
+        int s2 = 0;
+        for (int i = 0; i < MAXP; i++) {
+            o.mu[i] = i < nf ? mp[i] : NAN;
+            if (i >= nf) o.log_sigma[i] = NAN;
+            else if (i == se) o.log_sigma[i] = log(c_pri_w[m][i]);
+            else o.log_sigma[i] = sls[s2++];
+        }
+        o.elbo = -f0;
+        o.svi_steps = 0;
+    }
+}
+
+void launch_laplace(const DeviceBatch& d, cudaStream_t s) {
+    if (d.n_bands == 0) return;
+    int64_t threads = (int64_t)d.n_bands * 32;
+    laplace_kernel<<<(int)((threads + 127) / 128), 128, 0, s>>>(d);
+}
+
+// profile_t0_refine + profile_refine_all + mag chi2
+__global__ void refine_kernel(DeviceBatch d) {
+    int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    int lane = threadIdx.x & 31;
+    if (warp >= d.n_bands) return;
+    BandStats bs = d.stats[warp];
+    BandOut& o = d.out[warp];
+    if (!bs.valid || o.model < 0) return;
+    BandView b = band_view(d, bs);
+    int m = o.model, np = n_params_of(m), se = se_idx_of(m), t0i = t0_idx_of(m);
+    double* scr = d.scratch64 + 5 * bs.off;
+    double mu[MAXP], ls[MAXP];
+    for (int j = 0; j < np; j++) { mu[j] = o.mu[j]; ls[j] = o.log_sigma[j]; }
+    // ---- profile_t0_refine
+    {
+        double t0_lo = bs.t_first - 30.0, t0_hi = bs.t_peak_all + 5.0;
+        if (t0_lo < t0_hi) {
+            const int NG = 25;
+            double sx2 = exp(2.0 * mu[se]);
+            bool has_b = (m == BAZIN || m == TDE);
+            double best_t0 = mu[t0i], best_ll = -INFINITY;
+            for (int gi = 0; gi < NG; gi++) {
+                double t0 = t0_lo + (t0_hi - t0_lo) * (double)gi / (double)(NG - 1);
+                double p[MAXP];
+                for (int j = 0; j < np; j++) p[j] = mu[j];
+                p[t0i] = t0;
+                double saved_la = p[0];
+                p[0] = 0.0;
+                double saved_b = 0.0;
+                if (has_b) { saved_b = p[1]; p[1] = 0.0; }
+                metzger_prepare(m, p, b, scr);
+                Predictor P{m, p, scr};
+                double sw = 0, sy = 0, sf = 0, syf = 0, sff = 0;
+                for (int i = lane; i < b.n; i += 32) {
+                    double sh = P(b, i);
+                    if (b.up[i] || !isfinite(sh)) continue;
+                    double w = 1.0 / (b.var[i] + sx2);
+                    sw += w; sy += w * b.f[i]; sf += w * sh; syf += w * b.f[i] * sh; sff += w * sh * sh;
+                }
+                sw = wsum(sw); sy = wsum(sy); sf = wsum(sf); syf = wsum(syf); sff = wsum(sff);
+                __syncwarp();
+                if (has_b) {
+                    double det = sw * sff - sf * sf;
+                    if (fabs(det) > 1e-20) {
+                        double a_opt = (sw * syf - sf * sy) / det, b_opt = (sff * sy - sf * syf) / det;
+                        if (a_opt > 1e-10) { p[0] = log(a_opt); p[1] = b_opt; }
+                        else { p[0] = saved_la; p[1] = saved_b; }
+                    } else { p[0] = saved_la; p[1] = saved_b; }
+                } else {
+                    if (sff > 1e-20 && syf / sff > 1e-10) p[0] = log(syf / sff);
+                    else p[0] = saved_la;
+                }
+                double ll = band_ll_w(m, b, p, scr, true);
+                if (ll > best_ll) { best_ll = ll; best_t0 = t0; }
+            }
+            double lo1 = best_t0, hi1 = best_t0, thr = best_ll - 0.5;
+            for (int gi = NG - 1; gi >= 0; gi--) {
+                double t0 = t0_lo + (t0_hi - t0_lo) * (double)gi / (double)(NG - 1);
+                if (t0 >= best_t0) continue;
+                double p[MAXP];
+                for (int j = 0; j < np; j++) p[j] = mu[j];
+                p[t0i] = t0;
+                if (band_ll_w(m, b, p, scr, false) >= thr) lo1 = t0;
+                else break;
+            }
+            for (int gi = 0; gi < NG; gi++) {
+                double t0 = t0_lo + (t0_hi - t0_lo) * (double)gi / (double)(NG - 1);
+                if (t0 <= best_t0) continue;
+                double p[MAXP];
+                for (int j = 0; j < np; j++) p[j] = mu[j];
+                p[t0i] = t0;
+                if (band_ll_w(m, b, p, scr, false) >= thr) hi1 = t0;
+                else break;
+            }
+            mu[t0i] = best_t0;
+            ls[t0i] = log(fmax((hi1 - lo1) / 2.0, 0.1));
+        }
+    }
+    // ---- profile_refine_all
+    {
+        double map_ll = band_ll_w(m, b, mu, scr, false);
+        double thr = map_ll - 0.5;
+        for (int j = 0; j < np; j++) {
+            if (j == se) continue;
+            double mu_j = mu[j];
+            double svi_sigma = exp(ls[j]);
+            double slo = c_lo[m][j], shi = c_hi[m][j];
+            if (shi - slo < 1e-10) continue;
+            double l1 = mu_j, h1 = mu_j;
+            for (int gi = 0; gi < 15; gi++) {
+                double val = slo + (shi - slo) * (double)gi / 14.0;
+                double p[MAXP];
+                for (int k = 0; k < np; k++) p[k] = mu[k];
+                p[j] = val;
+                double ll = band_ll_w(m, b, p, scr, false);
+                if (ll >= thr) { l1 = fmin(l1, val); h1 = fmax(h1, val); }
+            }
+            double prof = fmax((h1 - l1) / 2.0, 1e-6);
+            double prior_sigma = c_pop_w[m][j];
+            ls[j] = log(fmax(fmax(svi_sigma, prof), prior_sigma));
+        }
+    }
+    // ---- magnitude-space chi2 with the refined mu (PSO params if fewer
+    // than half of the predictions are positive)
+    double msum = 0.0;
+    int mcount = 0;
+    {
+        metzger_prepare(m, mu, b, scr);
+        Predictor P{m, mu, scr};
+        int npos = 0;
+        for (int i = lane; i < b.n; i += 32) npos += (P(b, i) * b.peak > 0.0) ? 1 : 0;
+        for (int k = 16; k; k >>= 1) npos += __shfl_xor_sync(FULL, npos, k);
+        __syncwarp();
+        const double* use = mu;
+        double pso[MAXP];
+        if (npos < b.n / 2) {
+            for (int j = 0; j < np; j++) pso[j] = o.pso_params[j];
+            use = pso;
+        }
+        metzger_prepare(m, use, b, scr);
+        Predictor Q{m, use, scr};
+        for (int i = lane; i < b.n; i += 32) {
+            double pf = Q(b, i) * b.peak;
+            if (pf > 0.0 && b.f[i] > 0.0) {
+                double mpred = -2.5 * log10(pf) + 23.9;
+                double merr = 1.0857 * b.fe[i] / b.f[i];
+                if (merr > 0.0) {
+                    double r = b.mag[i] - mpred;
+                    msum += r * r / (merr * merr);
+                    mcount++;
+                }
+            }
+        }
+        msum = wsum(msum);
+        for (int k = 16; k; k >>= 1) mcount += __shfl_xor_sync(FULL, mcount, k);
+    }
+    if (lane == 0) {
+        for (int j = 0; j < np; j++) { o.mu[j] = mu[j]; o.log_sigma[j] = ls[j]; }
+        o.mag_chi2 = mcount > 0 ? msum / (double)mcount : NAN;
+    }
+}
+
+void launch_refine(const DeviceBatch& d, cudaStream_t s) {
+    if (d.n_bands == 0) return;
+    int64_t threads = (int64_t)d.n_bands * 32;
+    refine_kernel<<<(int)((threads + 127) / 128), 128, 0, s>>>(d);
+}
+
+// ---------------------------------------------------------------------------
+// Profile t0 search (SVI mode, rank-0 band): task builders and pickers.
+// Coarse: 5 runs on linspace(t0_min, t0_max, 5); fine: 3 runs on
+// linspace(best_t0 -/+ 0.5 clipped); results in t0 slots (band * 8 + k).
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ double lin_at(double a, double b, int n, int i) {
+    return n <= 1 ? a : a + (double)i * ((b - a) / (double)(n - 1));
+}
+
+__global__ void t0_build_kernel(DeviceBatch d, int slot, int fine, int64_t t0_base) {
+    int b = blockIdx.x * blockDim.x + threadIdx.x;
+    if (b >= d.n_bands) return;
+    BandStats bs = d.stats[b];
+    BandOut& o = d.out[b];
+    if (!bs.valid || bs.rank != 0 || o.model < 0) return;
+    int m = o.model, t0i = t0_idx_of(m);
+    double* ts = d.t0_state + 3 * (int64_t)b;
+    if (!fine) {
+        double pilot = o.pso_params[t0i];
+        ts[0] = fmax(pilot - 5.0, bs.t_first - 10.0);
+        ts[1] = pilot + 5.0;
+        ts[2] = pilot;
+    }
+    double t0_min = ts[0], t0_max = ts[1];
+    int cnt = fine ? 3 : 5;
+    double a = t0_min, z = t0_max;
+    if (fine) {
+        a = fmax(ts[2] - 0.5, t0_min);
+        z = fmin(ts[2] + 0.5, t0_max);
+    }
+    int base = atomicAdd(&d.ctr->task_count[slot], cnt);
+    for (int k = 0; k < cnt; k++) {
+        PsoTask t;
+        t.band = b;
+        t.kind = (int16_t)m;
+        t.restart = 0;
+        t.flags = TASK_T0_FIXED;
+        t.out = (int)(t0_base + (int64_t)b * 8 + (fine ? 5 : 0) + k);
+        t.aux = -1;
+        t.t0_fixed = lin_at(a, z, cnt, k);
+        d.tasks[slot][base + k] = t;
+    }
+}
+
+__global__ void t0_pick_kernel(DeviceBatch d, int fine, int64_t t0_base) {
+    int b = blockIdx.x * blockDim.x + threadIdx.x;
+    if (b >= d.n_bands) return;
+    BandStats bs = d.stats[b];
+    BandOut& o = d.out[b];
+    if (!bs.valid || bs.rank != 0 || o.model < 0) return;
+    int m = o.model, np = n_params_of(m), t0i = t0_idx_of(m);
+    double* ts = d.t0_state + 3 * (int64_t)b;
+    double t0_min = ts[0], t0_max = ts[1];
+    double best_c = o.pso_cost;
+    double best_t0 = ts[2];
+    double a = t0_min, z = t0_max;
+    int cnt = fine ? 3 : 5;
+    if (fine) { a = fmax(best_t0 - 0.5, t0_min); z = fmin(best_t0 + 0.5, t0_max); }
+    int best_k = -1;
+    for (int k = 0; k < cnt; k++) {
+        const PsoResult& R = d.pso_res[t0_base + (int64_t)b * 8 + (fine ? 5 : 0) + k];
+        if (R.cost < best_c) { best_c = R.cost; best_k = k; if (!fine) best_t0 = lin_at(a, z, cnt, k); }
+    }
+    if (!fine) ts[2] = best_t0;
+    if (best_k >= 0) {
+        const PsoResult& R = d.pso_res[t0_base + (int64_t)b * 8 + (fine ? 5 : 0) + best_k];
+        double t0v = lin_at(a, z, cnt, best_k);
+        int fi = 0;
+        for (int i = 0; i < np - 1; i++) {
+            if (i == t0i) o.pso_params[fi++] = t0v;
+            o.pso_params[fi++] = (double)R.params[i];
+        }
+        if (t0i >= np - 1) o.pso_params[fi] = t0v;
+        o.pso_cost = best_c;
+    }
+}
+
+void launch_t0_build(const DeviceBatch& d, int slot, int fine, cudaStream_t s) {
+    if (d.n_bands == 0) return;
+    t0_build_kernel<<<(d.n_bands + 127) / 128, 128, 0, s>>>(d, slot, fine, d.t0_slot_base);
+}
+void launch_t0_pick(const DeviceBatch& d, int slot, int fine, cudaStream_t s) {
+    (void)slot;
+    if (d.n_bands == 0) return;
+    t0_pick_kernel<<<(d.n_bands + 127) / 128, 128, 0, s>>>(d, fine, d.t0_slot_base);
+}
+
+// Bazin gate of fit_all_models == false (src/parametric.rs:2037): the bands
+// whose polished Bazin cost is >= 2 get the remaining seven models.
+__global__ void gate_build_kernel(DeviceBatch d, int slot) {
+    int b = blockIdx.x * blockDim.x + threadIdx.x;
+    if (b >= d.n_bands) return;
+    BandStats bs = d.stats[b];
+    if (!bs.valid) return;
+    if (!(d.fits[b * 8 + BAZIN].cost >= 2.0)) return;
+    int base = atomicAdd(&d.ctr->task_count[slot], 21);
+    int k = 0;
+    for (int mi = 1; mi < 8; mi++) {
+        int m = c_select_order[mi];
+        for (int r = 0; r < 3; r++) {
+            PsoTask t;
+            t.band = b;
+            t.kind = (int16_t)m;
+            t.restart = (int8_t)r;
+            t.flags = TASK_PRIOR | TASK_T0_BOUNDS | (r > 0 ? TASK_SEEDED : 0);
+            t.out = (b * 8 + m) * 3 + r;
+            t.aux = -1;
+            t.t0_fixed = 0.0;
+            d.tasks[slot][base + k++] = t;
+        }
+    }
+}
+void launch_gate_build(const DeviceBatch& d, int slot, cudaStream_t s) {
+    if (d.n_bands == 0) return;
+    gate_build_kernel<<<(d.n_bands + 127) / 128, 128, 0, s>>>(d, slot);
+}
+
+// ---------------------------------------------------------------------------
+// MultiBazin (fit_multi_bazin, src/parametric.rs:1008-1157) on rank-0 bands
+// with n >= 5.  Results of K live in slots mb_base + (band * 4 + K - 1) * 3 + r.
+// ---------------------------------------------------------------------------
+__device__ double mb_eval(const double* p, int k, double t) {
+    double sum = 0.0;
+    for (int c = 0; c < k; c++) {
+        const double* q = p + 4 * c;
+        double dt = t - q[1];
+        sum += exp(q[0]) * exp(-dt / exp(q[3])) * (1.0 / (1.0 + exp(-dt / exp(q[2]))));
+    }
+    return sum + p[4 * k];
+}
+
+__global__ void mb_pick_kernel(DeviceBatch d, int k, int64_t mb_base) {
+    int b = blockIdx.x * blockDim.x + threadIdx.x;
+    if (b >= d.n_bands) return;
+    BandStats bs = d.stats[b];
+    if (!bs.valid || bs.rank != 0 || bs.n < 5) return;
+    MbState& S = d.mb[b];
+    if (k == 1) {
+        S.best_k = 1; S.done = 0; S.k_done = 0;
+        S.best_cost = INFINITY; S.best_bic = INFINITY;
+        for (int i = 0; i < LCF_MB_MAX_K; i++) { S.per_k_cost[i] = NAN; S.per_k_bic[i] = NAN; }
+    }
+    if (S.done) return;
+    const PsoResult* R = d.pso_res + mb_base + ((int64_t)b * 4 + (k - 1)) * 3;
+    int np = 4 * k + 2;
+    int best = 0;
+    double c1 = R[0].cost;
+    if (k > 1 && R[1].cost < c1) { c1 = R[1].cost; best = 1; }
+    if (R[2].cost < c1) { c1 = R[2].cost; best = 2; }
+    double nf = (double)bs.n;
+    double kb = 2.0 * c1 * nf + (double)np * log(nf);
+    S.per_k_cost[k - 1] = c1;
+    S.per_k_bic[k - 1] = kb;
+    if (kb < S.best_bic) {
+        S.best_bic = kb;
+        S.best_cost = c1;
+        S.best_k = k;
+        for (int j = 0; j < MB_MAXP; j++) S.best_params[j] = j < np ? (double)R[best].params[j] : NAN;
+    }
+    for (int j = 0; j < MB_MAXP; j++) S.prev_params[j] = j < np ? (double)R[best].params[j] : NAN;
+    S.k_done = k;
+    if (k > 1 && kb > S.per_k_bic[k - 2] + 2.0) S.done = 1;
+}
+
+// Builds the K tasks (K >= 2): the seed particle extends the K-1 fit with a
+// component at the largest positive residual of a detection.
+__global__ void mb_build_kernel(DeviceBatch d, int slot, int k, int64_t mb_base) {
+    int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    int lane = threadIdx.x & 31;
+    if (warp >= d.n_bands) return;
+    int b = warp;
+    BandStats bs = d.stats[b];
+    if (!bs.valid || bs.rank != 0 || bs.n < 5) return;
+    MbState& S = d.mb[b];
+    if (S.done || S.k_done != k - 1) return;
+    BandView v = band_view(d, bs);
+    const double* prev = S.prev_params;
+    double best = -INFINITY;
+    int bi = 0x7fffffff;
+    for (int i = lane; i < v.n; i += 32) {
+        if (v.up[i]) continue;
+        double res = v.f[i] - mb_eval(prev, k - 1, v.t[i]);
+        if (res > best) { best = res; bi = i; }
+    }
+    for (int s = 16; s; s >>= 1) {
+        double ob = __shfl_xor_sync(FULL, best, s);
+        int oi = __shfl_xor_sync(FULL, bi, s);
+        if (ob > best || (ob == best && oi < bi)) { best = ob; bi = oi; }
+    }
+    if (lane != 0) return;
+    if (bi == 0x7fffffff) bi = 0;
+    int np = 4 * k + 2, pn = 4 * (k - 1);
+    double init[MB_MAXP];
+    for (int j = 0; j < pn; j++) init[j] = prev[j];
+    init[pn] = log(fmax(best, 1e-10));
+    init[pn + 1] = v.t[bi];
+    init[pn + 2] = 1.0;
+    init[pn + 3] = 1.0;
+    init[pn + 4] = prev[pn];
+    init[pn + 5] = prev[pn + 1];
+    for (int c = 0; c < k; c++) {
+        const double lo[4] = {-3.0, bs.t_first - 30.0, -2.0, -2.0}, hi[4] = {3.0, bs.t_last + 30.0, 5.0, 6.0};
+        for (int q = 0; q < 4; q++) init[4 * c + q] = fmin(fmax(init[4 * c + q], lo[q]), hi[q]);
+    }
+    init[4 * k] = fmin(fmax(init[4 * k], -0.3), 0.3);
+    init[4 * k + 1] = fmin(fmax(init[4 * k + 1], -5.0), 0.0);
+    for (int j = 0; j < MB_MAXP; j++) S.seed[j] = j < np ? init[j] : 0.0;
+    int base = atomicAdd(&d.ctr->task_count[slot], 3);
+    for (int r = 0; r < 3; r++) {
+        PsoTask t;
+        t.band = b;
+        t.kind = (int16_t)(KIND_MB1 + k - 1);
+        t.restart = (int8_t)r;
+        t.flags = r == 1 ? TASK_SEEDED : 0;
+        t.out = (int)(mb_base + ((int64_t)b * 4 + (k - 1)) * 3 + r);
+        t.aux = r == 1 ? b : -1;
+        t.t0_fixed = 0.0;
+        d.tasks[slot][base + r] = t;
+    }
+}
+
+void launch_mb_pick(const DeviceBatch& d, int k, cudaStream_t s) {
+    if (d.n_bands == 0) return;
+    mb_pick_kernel<<<(d.n_bands + 127) / 128, 128, 0, s>>>(d, k, d.mb_slot_base);
+}
+void launch_mb_build(const DeviceBatch& d, int slot, int k, cudaStream_t s) {
+    if (d.n_bands == 0) return;
+    int64_t threads = (int64_t)d.n_bands * 32;
+    mb_build_kernel<<<(int)((threads + 127) / 128), 128, 0, s>>>(d, slot, k, d.mb_slot_base);
+}
+
+}  // namespace lcf
+
+// ---------------------------------------------------------------------------
+// Reference drop-in exports (cuda/models.cu:590-636 as bound by
+// src/gpu_cuda.rs:31-40, :102-118): FP64, device pointers, default stream.
+// ---------------------------------------------------------------------------
+namespace {
+
+__global__ void eval_draws_kernel(int m, const double* p, const double* t, double* o, int nd, int nt, int np) {
+    int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= (int64_t)nd * nt) return;
+    int dd = (int)(idx / nt), ti = (int)(idx % nt);
+    o[idx] = lcf::eval_model_f64(m, p + (int64_t)dd * np, t[ti]);
+}
+
+// MetzgerKN over the whole (unsorted) times array of one draw
+__global__ void metzger_draws_kernel(const double* p, const double* t, double* o, int nd, int nt, int np,
+                                     double* tmp) {
+    int dd = blockIdx.x * blockDim.x + threadIdx.x;
+    if (dd >= nd) return;
+    // sort the times by insertion into tmp (stable), evaluate, scatter back
+    double* ts = tmp + (int64_t)dd * 2 * nt;
+    double* ys = ts + nt;
+    for (int i = 0; i < nt; i++) {
+        double v = t[i];
+        int j = i;
+        while (j > 0 && ts[j - 1] > v) { ts[j] = ts[j - 1]; j--; }
+        ts[j] = v;
+    }
+    lcf::metzger_f64(p + (int64_t)dd * np, ts, nt, ys);
+    for (int i = 0; i < nt; i++) {
+        // position of t[i] in the sorted array (first match of equal times)
+        int lo = 0, hi = nt;
+        while (lo < hi) {
+            int mid = (lo + hi) / 2;
+            if (ts[mid] < t[i]) lo = mid + 1; else hi = mid;
+        }
+        o[(int64_t)dd * nt + i] = ys[lo];
+    }
+}
+
+void eval_draws(int m, const double* p, const double* t, double* o, int nd, int nt, int np) {
+    int64_t total = (int64_t)nd * nt;
+    if (total <= 0) return;
+    eval_draws_kernel<<<(int)((total + 255) / 256), 256>>>(m, p, t, o, nd, nt, np);
+}
+
+// tmp (MetzgerKN only): per (source, particle) 2 * n doubles at
+// 2 * (offs[s] * n_part + k * n)
+__global__ void pso_cost_compat_kernel(const double* all_t, const double* all_f, const double* all_var,
+                                       const int* all_up, const double* all_uf, const int* offs,
+                                       const double* pos, double* costs, int n_src, int n_part, int np, int model,
+                                       double* tmp) {
+    int idx = blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= n_src * n_part) return;
+    int s = idx / n_part, k = idx % n_part;
+    int o0 = offs[s], o1 = offs[s + 1], n = o1 - o0;
+    const double* p = pos + (int64_t)idx * np;
+    double se = exp(p[np - 1]);
+    double se2 = se * se;
+    double nll = 0.0;
+    double* ts = nullptr;
+    double* ys = nullptr;
+    double scale = 1.0;
+    if (model == 7) {
+        ts = tmp + 2 * ((int64_t)o0 * n_part + (int64_t)k * n);
+        ys = ts + n;
+        for (int i = 0; i < n; i++) {
+            double v = all_t[o0 + i];
+            int j = i;
+            while (j > 0 && ts[j - 1] > v) { ts[j] = ts[j - 1]; j--; }
+            ts[j] = v;
+        }
+        lcf::metzger_f64(p, ts, n, ys);
+        double mx = -INFINITY;
+        for (int i = 0; i < n; i++) {
+            int lo = 0, hi = n;
+            while (lo < hi) { int mid = (lo + hi) / 2; if (ts[mid] < all_t[o0 + i]) lo = mid + 1; else hi = mid; }
+            if (!all_up[o0 + i]) mx = fmax(mx, ys[lo]);
+        }
+        if (mx > 1e-10 && isfinite(mx)) scale = fmin(fmax(1.0 / mx, 0.1), 10.0);
+    }
+    for (int i = 0; i < n; i++) {
+        double y;
+        if (model == 7) {
+            int lo = 0, hi = n;
+            while (lo < hi) { int mid = (lo + hi) / 2; if (ts[mid] < all_t[o0 + i]) lo = mid + 1; else hi = mid; }
+            y = ys[lo] * scale;
+        } else {
+            y = lcf::eval_model_f64(model, p, all_t[o0 + i]);
+        }
+        if (!isfinite(y)) { nll = 1e99; break; }
+        double tv = all_var[o0 + i] + se2;
+        if (all_up[o0 + i]) nll -= lcf::log_normal_cdf_f64((all_uf[o0 + i] - y) / sqrt(tv));
+        else {
+            double dd = y - all_f[o0 + i];
+            nll += dd * dd / tv + log(tv);
+        }
+    }
+    costs[idx] = nll >= 1e99 ? 1e99 : nll / (double)(n > 0 ? n : 1);
+}
+
+}  // namespace
+
+extern "C" {
+void launch_bazin(const double* p, const double* t, double* o, int nd, int nt, int np, int, int) { eval_draws(0, p, t, o, nd, nt, np); }
+void launch_villar(const double* p, const double* t, double* o, int nd, int nt, int np, int, int) { eval_draws(1, p, t, o, nd, nt, np); }
+void launch_tde(const double* p, const double* t, double* o, int nd, int nt, int np, int, int) { eval_draws(2, p, t, o, nd, nt, np); }
+void launch_arnett(const double* p, const double* t, double* o, int nd, int nt, int np, int, int) { eval_draws(3, p, t, o, nd, nt, np); }
+void launch_magnetar(const double* p, const double* t, double* o, int nd, int nt, int np, int, int) { eval_draws(4, p, t, o, nd, nt, np); }
+void launch_shock_cooling(const double* p, const double* t, double* o, int nd, int nt, int np, int, int) { eval_draws(5, p, t, o, nd, nt, np); }
+void launch_afterglow(const double* p, const double* t, double* o, int nd, int nt, int np, int, int) { eval_draws(6, p, t, o, nd, nt, np); }
+void launch_metzger_kn(const double* p, const double* t, double* o, int nd, int nt, int np, int, int) {
+    if (nd <= 0 || nt <= 0) return;
+    double* tmp = nullptr;
+    if (cudaMalloc(&tmp, (size_t)nd * 2 * nt * sizeof(double)) != cudaSuccess) return;
+    metzger_draws_kernel<<<(nd + 63) / 64, 64>>>(p, t, o, nd, nt, np, tmp);
+    cudaFree(tmp);
+}
+void launch_batch_pso_cost(const double* all_times, const double* all_flux, const double* all_obs_var,
+                           const int* all_is_upper, const double* all_upper_flux, const int* source_offsets,
+                           const double* positions, double* costs, int n_sources, int n_particles, int n_params,
+                           int model_id, int, int) {
+    int total = n_sources * n_particles;
+    if (total <= 0) return;
+    double* tmp = nullptr;
+    if (model_id == 7) {
+        int n_obs = 0;
+        if (cudaMemcpy(&n_obs, source_offsets + n_sources, sizeof(int), cudaMemcpyDeviceToHost) != cudaSuccess) return;
+        if (cudaMalloc(&tmp, (size_t)2 * n_particles * (size_t)(n_obs > 0 ? n_obs : 1) * sizeof(double)) != cudaSuccess)
+            return;
+    }
+    pso_cost_compat_kernel<<<(total + 127) / 128, 128>>>(all_times, all_flux, all_obs_var, all_is_upper,
+                                                         all_upper_flux, source_offsets, positions, costs, n_sources,
+                                                         n_particles, n_params, model_id, tmp);
+    if (tmp) {
+        cudaDeviceSynchronize();
+        cudaFree(tmp);
+    }
+}
+}

@@ -1,0 +1,749 @@
+// host.cu — context, device memory, the stage sequence of the fused fit,
+// CUDA-graph capture, and the C ABI of include/lcf.h.
+//
+// Stage sequence of one fit (all on the context's stream, captured once per
+// batch layout into a CUDA graph and replayed):
+//   prep          normalise bands, FP32 records, stats, rank inside source
+//   pso[0]        3 restarts x 8 models per band + MultiBazin K = 1
+//   lbfgs         best restart + bounded L-BFGS per (band, model)
+//   select        BIC model selection
+//   (gate)        fit_all_models == false: Bazin first, the 7 others only
+//                 for bands whose Bazin cost is >= 2 (device-built tasks)
+//   t0 search     SVI mode, rank-0 bands: 5 coarse + 3 fine PSO runs
+//   svi | laplace
+//   refine        profile t0 + all-parameter refinement + mag chi2
+//   MultiBazin    K = 2, 3, 4 (device-built tasks, early stop)
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <new>
+#include <string>
+#include <vector>
+
+#include "lcf.h"
+#include "lcf_internal.cuh"
+
+using namespace lcf;
+
+namespace lcf {
+
+// xoshiro256++ seeded by SplitMix64 (rand 0.9 SmallRng::seed_from_u64)
+struct Xoshiro {
+    uint64_t s[4];
+    explicit Xoshiro(uint64_t seed) {
+        uint64_t st = seed;
+        for (int i = 0; i < 4; i++) {
+            st += 0x9e3779b97f4a7c15ULL;
+            uint64_t z = st;
+            z = (z ^ (z >> 30)) * 0xbf58476d1ce4e5b9ULL;
+            z = (z ^ (z >> 27)) * 0x94d049bb133111ebULL;
+            s[i] = z ^ (z >> 31);
+        }
+    }
+    static uint64_t rotl(uint64_t x, int k) { return (x << k) | (x >> (64 - k)); }
+    uint64_t next() {
+        uint64_t r = rotl(s[0] + s[3], 23) + s[0];
+        uint64_t t = s[1] << 17;
+        s[2] ^= s[0]; s[3] ^= s[1]; s[1] ^= s[2]; s[0] ^= s[3]; s[2] ^= t;
+        s[3] = rotl(s[3], 45);
+        return r;
+    }
+    double f64() { return (double)(next() >> 11) * (1.0 / 9007199254740992.0); }
+};
+
+void make_draw_tables(float* draws, float* svi_eps) {
+    const uint64_t seeds[3] = {42, 137, 271};
+    for (int k = 0; k < 3; k++) {
+        Xoshiro r(seeds[k]);
+        for (int i = 0; i < DRAWS_PER_SEED; i++) draws[(size_t)k * DRAWS_PER_SEED + i] = (float)r.f64();
+    }
+    // svi_fit, src/parametric.rs:2282-2288: SmallRng(42); per step, sample
+    // and parameter: u1 = max(U, 1e-10), u2 = U, eps = sqrt(-2 ln u1) cos(2 pi u2)
+    for (int np = 5; np <= 7; np++) {
+        Xoshiro r(42);
+        float* tab = svi_eps + (size_t)(np - 5) * SVI_STEPS * SVI_SAMPLES * 7;
+        for (int s = 0; s < SVI_STEPS; s++)
+            for (int k = 0; k < SVI_SAMPLES; k++)
+                for (int j = 0; j < 7; j++) {
+                    float v = 0.0f;
+                    if (j < np) {
+                        double u1 = std::fmax(r.f64(), 1e-10);
+                        double u2 = r.f64();
+                        v = (float)(std::sqrt(-2.0 * std::log(u1)) * std::cos(2.0 * 3.14159265358979323846 * u2));
+                    }
+                    tab[((size_t)s * SVI_SAMPLES + k) * 7 + j] = v;
+                }
+    }
+}
+
+}  // namespace lcf
+
+// ---------------------------------------------------------------------------
+// Context
+// ---------------------------------------------------------------------------
+enum { N_EVENTS = 10 };
+
+struct DevArr {
+    void* p = nullptr;
+    size_t bytes = 0;
+};
+
+struct lcf_ctx {
+    int device = 0;
+    int num_sms = 0;
+    int pso_block = 256;
+    int pso_blocks_per_sm = 1;
+    int smem_obs = 512;
+    cudaStream_t stream = nullptr;
+    std::string err;
+    lcf_fit_stats stats{};
+    cudaEvent_t ev[N_EVENTS]{};
+    // tables
+    float* d_draws = nullptr;
+    float* d_eps = nullptr;
+    // device buffers (capacity-sized)
+    DevArr times, flux, ferr, boff, soff, stats_b, obs, t64, f64, fe64, var64, uf64, mag64, up, res, fits, out, mb,
+        ctr, scratch, scratch64, t0state, tasks[7];
+    int64_t task_cap[7] = {0, 0, 0, 0, 0, 0, 0};
+    // pinned staging
+    DevArr h_in, h_out;
+    // band-cost scratch
+    DevArr bc_obs, bc_params, bc_costs, bc_scratch;
+    // layout cache
+    std::vector<int64_t> h_boff;
+    std::vector<int32_t> h_soff;
+    std::vector<PsoTask> h_tasks0;
+    uint64_t layout_key = 0;
+    int n_tasks0 = 0;
+    int64_t n_max = 0;
+    // graph
+    cudaGraphExec_t graph = nullptr;
+    uint64_t graph_key = 0;
+    bool use_graph = true;
+    DeviceBatch db{};
+    int n_sources = 0, n_bands = 0;
+    int64_t n_obs = 0;
+    lcf_fit_options opts{};
+    int64_t launches = 0;
+};
+
+static int set_err(lcf_ctx* c, int code, const std::string& msg) {
+    if (c) c->err = msg;
+    return code;
+}
+#define CK(call)                                                                                         \
+    do {                                                                                                 \
+        cudaError_t e_ = (call);                                                                         \
+        if (e_ != cudaSuccess)                                                                           \
+            return set_err(ctx, LCF_E_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_));        \
+    } while (0)
+
+static int grow(lcf_ctx* ctx, DevArr& a, size_t bytes) {
+    if (bytes == 0) bytes = 16;
+    if (a.bytes >= bytes) return 0;
+    if (a.p) cudaFree(a.p);
+    a.p = nullptr;
+    a.bytes = 0;
+    size_t want = bytes + bytes / 4;
+    cudaError_t e = cudaMalloc(&a.p, want);
+    if (e != cudaSuccess) {
+        a.p = nullptr;
+        return set_err(ctx, LCF_E_NOMEM, std::string("cudaMalloc: ") + cudaGetErrorString(e));
+    }
+    a.bytes = want;
+    if (ctx->graph) {
+        cudaGraphExecDestroy(ctx->graph);
+        ctx->graph = nullptr;
+        ctx->graph_key = 0;
+    }
+    return 0;
+}
+static int grow_pinned(lcf_ctx* ctx, DevArr& a, size_t bytes) {
+    if (bytes == 0) bytes = 16;
+    if (a.bytes >= bytes) return 0;
+    if (a.p) cudaFreeHost(a.p);
+    a.p = nullptr;
+    a.bytes = 0;
+    size_t want = bytes + bytes / 4;
+    cudaError_t e = cudaMallocHost(&a.p, want);
+    if (e != cudaSuccess) {
+        a.p = nullptr;
+        return set_err(ctx, LCF_E_NOMEM, std::string("cudaMallocHost: ") + cudaGetErrorString(e));
+    }
+    a.bytes = want;
+    return 0;
+}
+static void free_arr(DevArr& a) {
+    if (a.p) cudaFree(a.p);
+    a = DevArr();
+}
+
+extern "C" int lcf_ctx_create(int device, lcf_ctx** out) {
+    if (!out) return LCF_E_INVALID;
+    *out = nullptr;
+    lcf_ctx* ctx = new (std::nothrow) lcf_ctx();
+    if (!ctx) return LCF_E_NOMEM;
+    ctx->device = device;
+    cudaError_t e = cudaSetDevice(device);
+    if (e != cudaSuccess) {
+        delete ctx;
+        return LCF_E_CUDA;
+    }
+    cudaDeviceProp prop;
+    if (cudaGetDeviceProperties(&prop, device) != cudaSuccess) {
+        delete ctx;
+        return LCF_E_CUDA;
+    }
+    ctx->num_sms = prop.multiProcessorCount;
+    if (cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking) != cudaSuccess) {
+        delete ctx;
+        return LCF_E_CUDA;
+    }
+    for (int i = 0; i < N_EVENTS; i++) cudaEventCreate(&ctx->ev[i]);
+    int rc = pso_init_attributes(ctx->pso_block, ctx->smem_obs);
+    if (rc != 0) {
+        lcf_ctx_destroy(ctx);
+        return LCF_E_CUDA;
+    }
+    // occupancy of the 7-dimension instantiation decides the persistent grid
+    int bps = pso_blocks_per_sm(ctx->pso_block, pso_smem_bytes(ctx->pso_block, ctx->smem_obs));
+    ctx->pso_blocks_per_sm = std::max(1, bps);
+    // RNG tables
+    std::vector<float> draws((size_t)3 * DRAWS_PER_SEED), eps((size_t)3 * SVI_STEPS * SVI_SAMPLES * 7);
+    make_draw_tables(draws.data(), eps.data());
+    if (cudaMalloc(&ctx->d_draws, draws.size() * sizeof(float)) != cudaSuccess ||
+        cudaMalloc(&ctx->d_eps, eps.size() * sizeof(float)) != cudaSuccess) {
+        lcf_ctx_destroy(ctx);
+        return LCF_E_NOMEM;
+    }
+    cudaMemcpy(ctx->d_draws, draws.data(), draws.size() * sizeof(float), cudaMemcpyHostToDevice);
+    cudaMemcpy(ctx->d_eps, eps.data(), eps.size() * sizeof(float), cudaMemcpyHostToDevice);
+    *out = ctx;
+    return LCF_OK;
+}
+
+extern "C" void lcf_ctx_destroy(lcf_ctx* ctx) {
+    if (!ctx) return;
+    cudaSetDevice(ctx->device);
+    if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+    if (ctx->graph) cudaGraphExecDestroy(ctx->graph);
+    DevArr* all[] = {&ctx->times, &ctx->flux, &ctx->ferr, &ctx->boff, &ctx->soff, &ctx->stats_b, &ctx->obs,
+                     &ctx->t64, &ctx->f64, &ctx->fe64, &ctx->var64, &ctx->uf64, &ctx->mag64, &ctx->up, &ctx->res,
+                     &ctx->fits, &ctx->out, &ctx->mb, &ctx->ctr, &ctx->scratch, &ctx->scratch64, &ctx->t0state,
+                     &ctx->bc_obs, &ctx->bc_params, &ctx->bc_costs, &ctx->bc_scratch};
+    for (DevArr* a : all) free_arr(*a);
+    for (auto& a : ctx->tasks) free_arr(a);
+    if (ctx->h_in.p) cudaFreeHost(ctx->h_in.p);
+    if (ctx->h_out.p) cudaFreeHost(ctx->h_out.p);
+    if (ctx->d_draws) cudaFree(ctx->d_draws);
+    if (ctx->d_eps) cudaFree(ctx->d_eps);
+    for (int i = 0; i < N_EVENTS; i++)
+        if (ctx->ev[i]) cudaEventDestroy(ctx->ev[i]);
+    if (ctx->stream) cudaStreamDestroy(ctx->stream);
+    delete ctx;
+}
+
+extern "C" const char* lcf_last_error(const lcf_ctx* ctx) {
+    if (!ctx) return "null context";
+    return ctx->err.c_str();
+}
+
+extern "C" int lcf_last_stats(const lcf_ctx* ctx, lcf_fit_stats* out) {
+    if (!ctx || !out) return LCF_E_INVALID;
+    *out = ctx->stats;
+    return LCF_OK;
+}
+
+extern "C" void* lcf_ctx_stream(lcf_ctx* ctx) { return ctx ? (void*)ctx->stream : nullptr; }
+
+// ---------------------------------------------------------------------------
+// Layout: validation, capacity, stage-1 task list
+// ---------------------------------------------------------------------------
+static int validate_layout(lcf_ctx* ctx, int n_sources, int n_bands, const int32_t* soff, const int64_t* boff) {
+    if (n_sources < 0 || n_bands < 0) return set_err(ctx, LCF_E_INVALID, "negative source or band count");
+    if (soff[0] != 0 || soff[n_sources] != n_bands)
+        return set_err(ctx, LCF_E_INVALID, "source_band_offsets must start at 0 and end at n_bands");
+    for (int s = 0; s < n_sources; s++)
+        if (soff[s + 1] < soff[s]) return set_err(ctx, LCF_E_INVALID, "source_band_offsets not monotone");
+    if (boff[0] != 0) return set_err(ctx, LCF_E_INVALID, "band_obs_offsets must start at 0");
+    for (int b = 0; b < n_bands; b++) {
+        if (boff[b + 1] < boff[b]) return set_err(ctx, LCF_E_INVALID, "band_obs_offsets not monotone");
+        if (boff[b + 1] - boff[b] > (1 << 24)) return set_err(ctx, LCF_E_INVALID, "band longer than 2^24 points");
+    }
+    return 0;
+}
+
+static uint64_t hash_layout(const std::vector<int64_t>& boff, const std::vector<int32_t>& soff,
+                            const lcf_fit_options& o) {
+    uint64_t h = 1469598103934665603ULL;
+    auto mix = [&](uint64_t v) { h = (h ^ v) * 1099511628211ULL; };
+    for (int64_t v : boff) mix((uint64_t)v);
+    mix(0xabcdefULL);
+    for (int32_t v : soff) mix((uint64_t)(uint32_t)v);
+    mix((uint64_t)o.fit_all_models);
+    mix((uint64_t)o.method + 7);
+    mix((uint64_t)(o.forced_model + 100));
+    mix((uint64_t)o.run_multi_bazin + 11);
+    return h;
+}
+
+// Estimated cost of a PSO task, in observation evaluations, for the
+// longest-first order of the work queue.
+static double task_cost(int kind, int n) {
+    if (kind == METZGER) return 330.0 + 0.8 * n;
+    if (kind >= KIND_MB1) return 0.9 * n * (kind - KIND_MB1 + 1);
+    return (double)n;
+}
+
+static int prepare_layout(lcf_ctx* ctx, int n_sources, int n_bands, int64_t n_obs, const lcf_fit_options& o) {
+    uint64_t key = hash_layout(ctx->h_boff, ctx->h_soff, o);
+    bool same = key == ctx->layout_key && ctx->n_bands == n_bands && ctx->n_obs == n_obs;
+    ctx->n_sources = n_sources;
+    ctx->n_bands = n_bands;
+    ctx->n_obs = n_obs;
+    ctx->opts = o;
+    int64_t n_max = 1;
+    for (int b = 0; b < n_bands; b++) n_max = std::max<int64_t>(n_max, ctx->h_boff[b + 1] - ctx->h_boff[b]);
+    ctx->n_max = n_max;
+    // capacity
+    size_t nb = (size_t)std::max(n_bands, 1), no = (size_t)std::max<int64_t>(n_obs, 1);
+    int rc = 0;
+    rc |= grow(ctx, ctx->times, no * 8);
+    rc |= grow(ctx, ctx->flux, no * 8);
+    rc |= grow(ctx, ctx->ferr, no * 8);
+    rc |= grow(ctx, ctx->boff, (nb + 1) * 8);
+    rc |= grow(ctx, ctx->soff, ((size_t)n_sources + 1) * 4);
+    rc |= grow(ctx, ctx->stats_b, nb * sizeof(BandStats));
+    rc |= grow(ctx, ctx->obs, no * sizeof(float4));
+    rc |= grow(ctx, ctx->t64, no * 8);
+    rc |= grow(ctx, ctx->f64, no * 8);
+    rc |= grow(ctx, ctx->fe64, no * 8);
+    rc |= grow(ctx, ctx->var64, no * 8);
+    rc |= grow(ctx, ctx->uf64, no * 8);
+    rc |= grow(ctx, ctx->mag64, no * 8);
+    rc |= grow(ctx, ctx->up, no);
+    rc |= grow(ctx, ctx->res, nb * 44 * sizeof(PsoResult));
+    rc |= grow(ctx, ctx->fits, nb * 8 * sizeof(ModelFit));
+    rc |= grow(ctx, ctx->out, nb * sizeof(BandOut));
+    rc |= grow(ctx, ctx->mb, nb * sizeof(MbState));
+    rc |= grow(ctx, ctx->ctr, sizeof(Counters));
+    rc |= grow(ctx, ctx->scratch64, no * 5 * 8);
+    rc |= grow(ctx, ctx->t0state, nb * 3 * 8);
+    int grid_pso = ctx->num_sms * ctx->pso_blocks_per_sm;
+    size_t warps = (size_t)grid_pso * (ctx->pso_block / 32);
+    rc |= grow(ctx, ctx->scratch, warps * 32 * (size_t)n_max * sizeof(float));
+    const int64_t caps[7] = {(int64_t)nb * 26, (int64_t)nb * 21, (int64_t)nb * 5, (int64_t)nb * 3, (int64_t)nb * 3,
+                             (int64_t)nb * 3, (int64_t)nb * 3};
+    for (int s = 0; s < 7; s++) {
+        rc |= grow(ctx, ctx->tasks[s], (size_t)caps[s] * sizeof(PsoTask));
+        ctx->task_cap[s] = caps[s];
+    }
+    if (rc) return rc;
+    // stage-1 task list (bands, models, restarts; MultiBazin K = 1), longest first
+    if (!same) {
+        std::vector<PsoTask>& T = ctx->h_tasks0;
+        T.clear();
+        int64_t mb_base = (int64_t)n_bands * 32;
+        for (int b = 0; b < n_bands; b++) {
+            int n = (int)(ctx->h_boff[b + 1] - ctx->h_boff[b]);
+            if (n <= 0) continue;
+            int models[8], nm = 0;
+            if (o.forced_model >= 0) models[nm++] = o.forced_model;
+            else if (o.fit_all_models) for (int m = 0; m < 8; m++) models[nm++] = m;
+            else models[nm++] = BAZIN;
+            for (int i = 0; i < nm; i++)
+                for (int r = 0; r < 3; r++) {
+                    PsoTask t;
+                    t.band = b;
+                    t.kind = (int16_t)models[i];
+                    t.restart = (int8_t)r;
+                    t.flags = TASK_PRIOR | TASK_T0_BOUNDS | (r > 0 ? TASK_SEEDED : 0);
+                    t.out = (b * 8 + models[i]) * 3 + r;
+                    t.aux = -1;
+                    t.t0_fixed = 0.0;
+                    T.push_back(t);
+                }
+            if (o.run_multi_bazin && n >= 5)
+                for (int r = 0; r < 3; r += 2) {
+                    PsoTask t;
+                    t.band = b;
+                    t.kind = (int16_t)KIND_MB1;
+                    t.restart = (int8_t)r;
+                    t.flags = TASK_RANK0;
+                    t.out = (int)(mb_base + ((int64_t)b * 4) * 3 + r);
+                    t.aux = -1;
+                    t.t0_fixed = 0.0;
+                    T.push_back(t);
+                }
+        }
+        std::vector<double> key(T.size());
+        for (size_t i = 0; i < T.size(); i++)
+            key[i] = task_cost(T[i].kind, (int)(ctx->h_boff[T[i].band + 1] - ctx->h_boff[T[i].band]));
+        std::vector<size_t> ord(T.size());
+        for (size_t i = 0; i < ord.size(); i++) ord[i] = i;
+        std::stable_sort(ord.begin(), ord.end(), [&](size_t a, size_t b) { return key[a] > key[b]; });
+        std::vector<PsoTask> S(T.size());
+        for (size_t i = 0; i < ord.size(); i++) S[i] = T[ord[i]];
+        T.swap(S);
+        ctx->n_tasks0 = (int)T.size();
+        CK(cudaMemcpyAsync(ctx->tasks[0].p, T.data(), T.size() * sizeof(PsoTask), cudaMemcpyHostToDevice,
+                           ctx->stream));
+        ctx->layout_key = hash_layout(ctx->h_boff, ctx->h_soff, o);
+        if (ctx->graph) {
+            cudaGraphExecDestroy(ctx->graph);
+            ctx->graph = nullptr;
+            ctx->graph_key = 0;
+        }
+    }
+    // device batch view
+    DeviceBatch& d = ctx->db;
+    d.times = (const double*)ctx->times.p;
+    d.flux = (const double*)ctx->flux.p;
+    d.err = (const double*)ctx->ferr.p;
+    d.band_off = (const int64_t*)ctx->boff.p;
+    d.src_off = (const int32_t*)ctx->soff.p;
+    d.n_sources = n_sources;
+    d.n_bands = n_bands;
+    d.n_obs = n_obs;
+    d.stats = (BandStats*)ctx->stats_b.p;
+    d.obs = (float4*)ctx->obs.p;
+    d.t64 = (double*)ctx->t64.p;
+    d.f64 = (double*)ctx->f64.p;
+    d.fe64 = (double*)ctx->fe64.p;
+    d.var64 = (double*)ctx->var64.p;
+    d.uf64 = (double*)ctx->uf64.p;
+    d.mag64 = (double*)ctx->mag64.p;
+    d.up = (uint8_t*)ctx->up.p;
+    d.draws = ctx->d_draws;
+    d.svi_eps = ctx->d_eps;
+    d.pso_res = (PsoResult*)ctx->res.p;
+    d.fits = (ModelFit*)ctx->fits.p;
+    d.out = (BandOut*)ctx->out.p;
+    d.mb = (MbState*)ctx->mb.p;
+    for (int s = 0; s < 7; s++) {
+        d.tasks[s] = (PsoTask*)ctx->tasks[s].p;
+        d.task_cap[s] = (int)ctx->task_cap[s];
+    }
+    d.tasks[7] = nullptr;
+    d.task_cap[7] = 0;
+    d.ctr = (Counters*)ctx->ctr.p;
+    d.scratch = (float*)ctx->scratch.p;
+    d.scratch_per_warp = 32 * n_max;
+    d.scratch64 = (double*)ctx->scratch64.p;
+    d.t0_state = (double*)ctx->t0state.p;
+    d.t0_slot_base = (int64_t)n_bands * 24;
+    d.mb_slot_base = (int64_t)n_bands * 32;
+    d.smem_obs = ctx->smem_obs;
+    return 0;
+}
+
+// ---------------------------------------------------------------------------
+// Stage sequence
+// ---------------------------------------------------------------------------
+static void enqueue_pipeline(lcf_ctx* ctx) {
+    const DeviceBatch& d = ctx->db;
+    const lcf_fit_options& o = ctx->opts;
+    cudaStream_t s = ctx->stream;
+    int grid = ctx->num_sms * ctx->pso_blocks_per_sm;
+    int block = ctx->pso_block;
+    int64_t L = 0;
+    cudaEventRecord(ctx->ev[0], s);
+    cudaMemsetAsync(ctx->res.p, 0xff, (size_t)std::max(ctx->n_bands, 1) * 44 * sizeof(PsoResult), s);
+    cudaMemsetAsync(ctx->ctr.p, 0, sizeof(Counters), s);
+    cudaMemsetAsync(ctx->fits.p, 0xff, (size_t)std::max(ctx->n_bands, 1) * 8 * sizeof(ModelFit), s);
+    launch_prep(d, s); L++;
+    cudaEventRecord(ctx->ev[1], s);
+    launch_pso(d, 0, ctx->n_tasks0, 7, grid, block, s); L++;
+    cudaEventRecord(ctx->ev[2], s);
+    int gated = (o.forced_model < 0 && !o.fit_all_models);
+    launch_lbfgs(d, gated ? 1 : 0xff, s); L++;
+    if (gated) {
+        launch_gate_build(d, 1, s); L++;
+        launch_pso(d, 1, -1, 7, grid, block, s); L++;
+        launch_lbfgs(d, 0xfe, s); L++;
+    }
+    launch_select(d, o.fit_all_models, o.forced_model, s); L++;
+    cudaEventRecord(ctx->ev[3], s);
+    if (o.method == LCF_METHOD_SVI) {
+        launch_t0_build(d, 2, 0, s); L++;
+        launch_pso(d, 2, -1, 7, grid, block, s); L++;
+        launch_t0_pick(d, 2, 0, s); L++;
+        launch_t0_build(d, 3, 1, s); L++;
+        launch_pso(d, 3, -1, 7, grid, block, s); L++;
+        launch_t0_pick(d, 3, 1, s); L++;
+    }
+    cudaEventRecord(ctx->ev[4], s);
+    if (o.method == LCF_METHOD_SVI) launch_svi(d, s);
+    else launch_laplace(d, s);
+    L++;
+    cudaEventRecord(ctx->ev[5], s);
+    launch_refine(d, s); L++;
+    cudaEventRecord(ctx->ev[6], s);
+    if (o.run_multi_bazin) {
+        launch_mb_pick(d, 1, s); L++;
+        for (int k = 2; k <= 4; k++) {
+            launch_mb_build(d, 2 + k, k, s); L++;
+            launch_pso(d, 2 + k, -1, 4 * k + 2, grid, block, s); L++;
+            launch_mb_pick(d, k, s); L++;
+        }
+    }
+    cudaEventRecord(ctx->ev[7], s);
+    ctx->launches = L;
+}
+
+static int run_pipeline(lcf_ctx* ctx) {
+    uint64_t gkey = ctx->layout_key ^ ((uint64_t)(uintptr_t)ctx->db.times * 31) ^ ((uint64_t)ctx->n_obs << 7);
+    if (ctx->use_graph) {
+        if (!ctx->graph || ctx->graph_key != gkey) {
+            if (ctx->graph) {
+                cudaGraphExecDestroy(ctx->graph);
+                ctx->graph = nullptr;
+            }
+            cudaGraph_t g;
+            CK(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
+            enqueue_pipeline(ctx);
+            CK(cudaStreamEndCapture(ctx->stream, &g));
+            cudaError_t e = cudaGraphInstantiate(&ctx->graph, g, 0);
+            cudaGraphDestroy(g);
+            if (e != cudaSuccess) {
+                ctx->graph = nullptr;
+                return set_err(ctx, LCF_E_CUDA, std::string("cudaGraphInstantiate: ") + cudaGetErrorString(e));
+            }
+            ctx->graph_key = gkey;
+        }
+        CK(cudaGraphLaunch(ctx->graph, ctx->stream));
+    } else {
+        enqueue_pipeline(ctx);
+        CK(cudaGetLastError());
+    }
+    return 0;
+}
+
+static int finish_stats(lcf_ctx* ctx) {
+    CK(cudaStreamSynchronize(ctx->stream));
+    CK(cudaGetLastError());
+    Counters c;
+    CK(cudaMemcpy(&c, ctx->ctr.p, sizeof(Counters), cudaMemcpyDeviceToHost));
+    float ms[8] = {0};
+    for (int i = 1; i < 8; i++) cudaEventElapsedTime(&ms[i], ctx->ev[i - 1], ctx->ev[i]);
+    float tot = 0;
+    cudaEventElapsedTime(&tot, ctx->ev[0], ctx->ev[7]);
+    lcf_fit_stats& st = ctx->stats;
+    st.ms_total = tot;
+    st.ms_pso = ms[2];
+    st.ms_lbfgs = ms[3];
+    st.ms_t0_search = ms[4];
+    st.ms_uncertainty = ms[5];
+    st.ms_refine = ms[6];
+    st.ms_multi_bazin = ms[7];
+    st.particle_obs_evals = (double)c.particle_obs_evals;
+    st.ode_steps = (double)c.ode_steps;
+    st.pso_tasks = ctx->n_tasks0;
+    st.kernel_launches = ctx->launches;
+    if (c.error) return set_err(ctx, c.error, "a bounded device wait expired");
+    return 0;
+}
+
+// ---------------------------------------------------------------------------
+// Output unpacking
+// ---------------------------------------------------------------------------
+static int unpack_outputs(lcf_ctx* ctx, lcf_fit_outputs* out) {
+    int nb = ctx->n_bands;
+    size_t bytes = (size_t)nb * (sizeof(BandOut) + sizeof(BandStats) + sizeof(MbState) +
+                                 (ctx->opts.fit_all_models ? 8 * sizeof(ModelFit) : 0));
+    if (grow_pinned(ctx, ctx->h_out, bytes)) return LCF_E_NOMEM;
+    char* hp = (char*)ctx->h_out.p;
+    BandOut* ho = (BandOut*)hp;
+    BandStats* hs = (BandStats*)(hp + (size_t)nb * sizeof(BandOut));
+    MbState* hm = (MbState*)((char*)hs + (size_t)nb * sizeof(BandStats));
+    ModelFit* hf = (ModelFit*)((char*)hm + (size_t)nb * sizeof(MbState));
+    if (nb > 0) {
+        CK(cudaMemcpyAsync(ho, ctx->out.p, (size_t)nb * sizeof(BandOut), cudaMemcpyDeviceToHost, ctx->stream));
+        CK(cudaMemcpyAsync(hs, ctx->stats_b.p, (size_t)nb * sizeof(BandStats), cudaMemcpyDeviceToHost, ctx->stream));
+        if (ctx->opts.run_multi_bazin)
+            CK(cudaMemcpyAsync(hm, ctx->mb.p, (size_t)nb * sizeof(MbState), cudaMemcpyDeviceToHost, ctx->stream));
+        if (ctx->opts.fit_all_models)
+            CK(cudaMemcpyAsync(hf, ctx->fits.p, (size_t)nb * 8 * sizeof(ModelFit), cudaMemcpyDeviceToHost,
+                               ctx->stream));
+        CK(cudaStreamSynchronize(ctx->stream));
+    }
+    const double nan = std::nan("");
+    for (int b = 0; b < nb; b++) {
+        const BandStats& st = hs[b];
+        const BandOut& o = ho[b];
+        bool ok = st.valid && o.model >= 0;
+        out->model[b] = ok ? o.model : -1;
+        out->rank[b] = ok ? st.rank : -1;
+        out->n_obs[b] = ok ? st.n : 0;
+        int np = ok ? n_params_of(o.model) : 0;
+        for (int j = 0; j < MAXP; j++) {
+            out->pso_params[b * 7 + j] = j < np ? o.pso_params[j] : nan;
+            out->svi_mu[b * 7 + j] = j < np ? o.mu[j] : nan;
+            out->svi_log_sigma[b * 7 + j] = j < np ? o.log_sigma[j] : nan;
+        }
+        out->pso_chi2[b] = ok && std::isfinite(o.pso_cost) ? o.pso_cost : nan;
+        out->svi_elbo[b] = ok && std::isfinite(o.elbo) ? o.elbo : nan;
+        out->mag_chi2[b] = ok && std::isfinite(o.mag_chi2) ? o.mag_chi2 : nan;
+        for (int m = 0; m < 8; m++) {
+            out->per_model_chi2[b * 8 + m] = ok ? o.per_chi2[m] : nan;
+            // fits are reset to NaN before each run: a NaN cost means "not fitted"
+            bool have = ok && ctx->opts.fit_all_models && !std::isnan(hf[b * 8 + m].cost);
+            int npm = n_params_of(m);
+            for (int j = 0; j < 7; j++)
+                out->per_model_params[(b * 8 + m) * 7 + j] = (have && j < npm) ? hf[b * 8 + m].params[j] : nan;
+        }
+        out->mb_best_k[b] = 0;
+        for (int j = 0; j < LCF_MB_MAX_PARAMS; j++) out->mb_params[b * 18 + j] = nan;
+        out->mb_cost[b] = nan;
+        out->mb_bic[b] = nan;
+        for (int k = 0; k < 4; k++) {
+            out->mb_per_k_cost[b * 4 + k] = nan;
+            out->mb_per_k_bic[b * 4 + k] = nan;
+        }
+        if (ok && ctx->opts.run_multi_bazin && st.rank == 0 && st.n >= 5) {
+            const MbState& S = hm[b];
+            out->mb_best_k[b] = S.best_k;
+            for (int j = 0; j < LCF_MB_MAX_PARAMS; j++) out->mb_params[b * 18 + j] = S.best_params[j];
+            out->mb_cost[b] = S.best_cost;
+            out->mb_bic[b] = S.best_bic;
+            for (int k = 0; k < 4; k++) {
+                out->mb_per_k_cost[b * 4 + k] = S.per_k_cost[k];
+                out->mb_per_k_bic[b * 4 + k] = S.per_k_bic[k];
+            }
+        }
+    }
+    return 0;
+}
+
+static int check_opts(lcf_ctx* ctx, const lcf_fit_options* o) {
+    if (!o) return set_err(ctx, LCF_E_INVALID, "null options");
+    if (o->method != LCF_METHOD_SVI && o->method != LCF_METHOD_LAPLACE)
+        return set_err(ctx, LCF_E_INVALID, "method must be LCF_METHOD_SVI or LCF_METHOD_LAPLACE");
+    if (o->forced_model < -1 || o->forced_model > 7) return set_err(ctx, LCF_E_INVALID, "forced_model out of range");
+    return 0;
+}
+
+extern "C" int lcf_fit_parametric_batch(lcf_ctx* ctx, const lcf_bands_csr* in, const lcf_fit_options* o,
+                                        lcf_fit_outputs* out) {
+    if (!ctx) return LCF_E_INVALID;
+    if (!in || !out) return set_err(ctx, LCF_E_INVALID, "null argument");
+    if (int rc = check_opts(ctx, o)) return rc;
+    CK(cudaSetDevice(ctx->device));
+    int ns = in->n_sources, nb = in->n_bands;
+    if (ns < 0 || nb < 0 || !in->source_band_offsets || (nb > 0 && !in->band_obs_offsets))
+        return set_err(ctx, LCF_E_INVALID, "bad CSR header");
+    if (int rc = validate_layout(ctx, ns, nb, in->source_band_offsets, in->band_obs_offsets)) return rc;
+    int64_t n_obs = nb > 0 ? in->band_obs_offsets[nb] : 0;
+    if (n_obs > 0 && (!in->times || !in->flux || !in->flux_err)) return set_err(ctx, LCF_E_INVALID, "null data array");
+    ctx->h_boff.assign(in->band_obs_offsets, in->band_obs_offsets + nb + 1);
+    ctx->h_soff.assign(in->source_band_offsets, in->source_band_offsets + ns + 1);
+    if (int rc = prepare_layout(ctx, ns, nb, n_obs, *o)) return rc;
+    // stage the inputs through pinned memory
+    size_t in_bytes = (size_t)n_obs * 24 + (size_t)(nb + 1) * 8 + (size_t)(ns + 1) * 4;
+    if (grow_pinned(ctx, ctx->h_in, in_bytes)) return LCF_E_NOMEM;
+    char* hp = (char*)ctx->h_in.p;
+    std::memcpy(hp, in->times, (size_t)n_obs * 8);
+    std::memcpy(hp + (size_t)n_obs * 8, in->flux, (size_t)n_obs * 8);
+    std::memcpy(hp + (size_t)n_obs * 16, in->flux_err, (size_t)n_obs * 8);
+    std::memcpy(hp + (size_t)n_obs * 24, in->band_obs_offsets, (size_t)(nb + 1) * 8);
+    std::memcpy(hp + (size_t)n_obs * 24 + (size_t)(nb + 1) * 8, in->source_band_offsets, (size_t)(ns + 1) * 4);
+    cudaStream_t s = ctx->stream;
+    if (n_obs > 0) {
+        CK(cudaMemcpyAsync(ctx->times.p, hp, (size_t)n_obs * 8, cudaMemcpyHostToDevice, s));
+        CK(cudaMemcpyAsync(ctx->flux.p, hp + (size_t)n_obs * 8, (size_t)n_obs * 8, cudaMemcpyHostToDevice, s));
+        CK(cudaMemcpyAsync(ctx->ferr.p, hp + (size_t)n_obs * 16, (size_t)n_obs * 8, cudaMemcpyHostToDevice, s));
+    }
+    CK(cudaMemcpyAsync(ctx->boff.p, hp + (size_t)n_obs * 24, (size_t)(nb + 1) * 8, cudaMemcpyHostToDevice, s));
+    CK(cudaMemcpyAsync(ctx->soff.p, hp + (size_t)n_obs * 24 + (size_t)(nb + 1) * 8, (size_t)(ns + 1) * 4,
+                       cudaMemcpyHostToDevice, s));
+    if (nb == 0) return 0;
+    if (int rc = run_pipeline(ctx)) return rc;
+    if (int rc = finish_stats(ctx)) return rc;
+    return unpack_outputs(ctx, out);
+}
+
+extern "C" int lcf_fit_parametric_device(lcf_ctx* ctx, const lcf_bands_csr* dev, const lcf_fit_options* o) {
+    if (!ctx) return LCF_E_INVALID;
+    if (!dev) return set_err(ctx, LCF_E_INVALID, "null argument");
+    if (int rc = check_opts(ctx, o)) return rc;
+    CK(cudaSetDevice(ctx->device));
+    int ns = dev->n_sources, nb = dev->n_bands;
+    if (ns < 0 || nb < 0) return set_err(ctx, LCF_E_INVALID, "bad CSR header");
+    // the offsets drive the host-side task list: read them back
+    std::vector<int64_t> boff((size_t)nb + 1);
+    std::vector<int32_t> soff((size_t)ns + 1);
+    CK(cudaMemcpy(boff.data(), dev->band_obs_offsets, boff.size() * 8, cudaMemcpyDeviceToHost));
+    CK(cudaMemcpy(soff.data(), dev->source_band_offsets, soff.size() * 4, cudaMemcpyDeviceToHost));
+    if (int rc = validate_layout(ctx, ns, nb, soff.data(), boff.data())) return rc;
+    ctx->h_boff.swap(boff);
+    ctx->h_soff.swap(soff);
+    int64_t n_obs = ctx->h_boff[nb];
+    if (int rc = prepare_layout(ctx, ns, nb, n_obs, *o)) return rc;
+    // point the batch at the caller's device arrays
+    ctx->db.times = dev->times;
+    ctx->db.flux = dev->flux;
+    ctx->db.err = dev->flux_err;
+    ctx->db.band_off = dev->band_obs_offsets;
+    ctx->db.src_off = dev->source_band_offsets;
+    if (nb == 0) return 0;
+    if (int rc = run_pipeline(ctx)) return rc;
+    return finish_stats(ctx);
+}
+
+extern "C" int lcf_download_outputs(lcf_ctx* ctx, lcf_fit_outputs* out) {
+    if (!ctx || !out) return LCF_E_INVALID;
+    return unpack_outputs(ctx, out);
+}
+
+// ---------------------------------------------------------------------------
+// Batched likelihood on one band (PsoCost::cost_from_slice)
+// ---------------------------------------------------------------------------
+extern "C" int lcf_band_cost(lcf_ctx* ctx, int model, const double* times, const double* flux, const double* obs_var,
+                             const uint8_t* is_upper, const double* upper_flux, int n_obs, const double* params,
+                             int n_eval, int with_prior, double* costs) {
+    if (!ctx) return LCF_E_INVALID;
+    if (model < 0 || model > 7 || n_obs < 0 || n_eval < 0) return set_err(ctx, LCF_E_INVALID, "bad argument");
+    if (n_eval == 0) return 0;
+    CK(cudaSetDevice(ctx->device));
+    // FP32 records sorted by time (stable)
+    std::vector<int> ord(n_obs);
+    for (int i = 0; i < n_obs; i++) ord[i] = i;
+    std::stable_sort(ord.begin(), ord.end(), [&](int a, int b) { return times[a] < times[b]; });
+    std::vector<float4> rec(std::max(n_obs, 1));
+    double t_last = -INFINITY;
+    for (int k = 0; k < n_obs; k++) {
+        int i = ord[k];
+        double t = times[i];
+        t_last = std::fmax(t_last, t);
+        float th = (float)t;
+        bool up = is_upper[i] != 0;
+        rec[k] = make_float4(th, (float)(t - (double)th), (float)(up ? upper_flux[i] : flux[i]),
+                             up ? -(float)obs_var[i] : (float)obs_var[i]);
+    }
+    int np = n_params_of(model);
+    int rc = 0;
+    rc |= grow(ctx, ctx->bc_obs, rec.size() * sizeof(float4));
+    rc |= grow(ctx, ctx->bc_params, (size_t)n_eval * np * 8);
+    rc |= grow(ctx, ctx->bc_costs, (size_t)n_eval * 8);
+    rc |= grow(ctx, ctx->bc_scratch, (size_t)((n_eval + 31) / 32) * 32 * (size_t)std::max(n_obs, 1) * 4);
+    if (rc) return rc;
+    cudaStream_t s = ctx->stream;
+    CK(cudaMemcpyAsync(ctx->bc_obs.p, rec.data(), rec.size() * sizeof(float4), cudaMemcpyHostToDevice, s));
+    CK(cudaMemcpyAsync(ctx->bc_params.p, params, (size_t)n_eval * np * 8, cudaMemcpyHostToDevice, s));
+    launch_band_cost(model, (const float4*)ctx->bc_obs.p, n_obs, (float)t_last, (const double*)ctx->bc_params.p,
+                     n_eval, with_prior, (double*)ctx->bc_costs.p, (float*)ctx->bc_scratch.p, s);
+    CK(cudaGetLastError());
+    CK(cudaMemcpyAsync(costs, ctx->bc_costs.p, (size_t)n_eval * 8, cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+    return 0;
+}
+
+// Switch CUDA-graph replay of the stage sequence on or off (on by default).
+extern "C" int lcf_set_graph(lcf_ctx* ctx, int enabled) {
+    if (!ctx) return LCF_E_INVALID;
+    ctx->use_graph = enabled != 0;
+    return 0;
+}

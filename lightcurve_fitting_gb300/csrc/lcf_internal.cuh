@@ -1,0 +1,262 @@
+// lcf_internal.cuh — shared declarations of liblcf_gb300: model tables,
+// device data layout, task and result records, and the launch wrappers each
+// translation unit exports to the host orchestrator (host.cpp).
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "lcf.h"
+
+namespace lcf {
+
+// ---------------------------------------------------------------------------
+// Model tables (src/parametric.rs:124-162, :1541-1621, :2072-2115).
+// Model ids: 0 Bazin, 1 Villar, 2 Tde, 3 Arnett, 4 Magnetar, 5 ShockCooling,
+// 6 Afterglow, 7 MetzgerKN.  Task kinds 8..11 are MultiBazin with K = 1..4.
+// ---------------------------------------------------------------------------
+enum : int { BAZIN = 0, VILLAR = 1, TDE = 2, ARNETT = 3, MAGNETAR = 4, SHOCK = 5, AFTERGLOW = 6, METZGER = 7 };
+enum : int { KIND_MB1 = 8 };  // kind = KIND_MB1 + (K - 1)
+
+constexpr int NP = 30;          // particles, src/parametric.rs:1974-1987
+constexpr int MAX_ITERS = 60;
+constexpr int STALL_ITERS = 12;
+constexpr int MAXP = LCF_MAX_PARAMS;
+constexpr int MB_MAXP = LCF_MB_MAX_PARAMS;
+// Length of the per-seed uniform-draw table: the longest PSO run (18
+// dimensions) consumes 30*2*18 initial draws plus 60*30*2*18 in its iterations.
+constexpr int DRAWS_PER_SEED = 66000;
+// SVI reparameterisation noise table: 1000 steps x 4 samples x up to 7 params.
+constexpr int SVI_STEPS = 1000;
+constexpr int SVI_SAMPLES = 4;
+constexpr double SVI_LR = 0.01;
+
+__host__ __device__ constexpr int n_params_of(int m) {
+    return m == BAZIN ? 6 : m == VILLAR ? 7 : m == TDE ? 7 : m == ARNETT ? 5 : m == MAGNETAR ? 5 : m == SHOCK ? 5
+         : m == AFTERGLOW ? 6 : 5;
+}
+__host__ __device__ constexpr int se_idx_of(int m) {
+    return m == BAZIN ? 5 : m == VILLAR ? 6 : m == TDE ? 6 : m == ARNETT ? 4 : m == MAGNETAR ? 4 : m == SHOCK ? 4
+         : m == AFTERGLOW ? 5 : 4;
+}
+__host__ __device__ constexpr int t0_idx_of(int m) {
+    return m == BAZIN ? 2 : m == VILLAR ? 3 : m == TDE ? 2 : m == ARNETT ? 1 : m == MAGNETAR ? 1 : m == SHOCK ? 1
+         : m == AFTERGLOW ? 1 : 3;
+}
+
+// pso_bounds, src/parametric.rs:1541-1579 (row = model id)
+static __device__ __constant__ double c_lo[8][MAXP] = {
+    {-3.0, -0.3, -100.0, -2.0, -2.0, -5.0, 0.0},
+    {-1.5, -0.02, 1.0, -60.0, -1.0, 1.0, -6.0},
+    {-3.0, -1.0, -100.0, -2.0, -1.0, 0.5, -5.0},
+    {-3.0, -100.0, 0.5, -3.0, -5.0, 0.0, 0.0},
+    {-3.0, -100.0, 0.0, 0.5, -5.0, 0.0, 0.0},
+    {-3.0, -100.0, 0.1, -1.0, -5.0, 0.0, 0.0},
+    {-3.0, -100.0, -2.0, -2.0, 0.5, -5.0, 0.0},
+    {-3.0, -2.0, -1.0, -2.0, -5.0, 0.0, 0.0}};
+static __device__ __constant__ double c_hi[8][MAXP] = {
+    {3.0, 0.3, 100.0, 5.0, 6.0, 0.0, 0.0},
+    {1.5, 0.05, 5.0, 40.0, 3.0, 5.5, 0.0},
+    {3.0, 1.0, 100.0, 5.0, 6.0, 4.0, 0.0},
+    {3.0, 100.0, 4.5, 3.0, 0.0, 0.0, 0.0},
+    {3.0, 100.0, 6.0, 4.5, 0.0, 0.0, 0.0},
+    {3.0, 100.0, 3.0, 4.0, 0.0, 0.0, 0.0},
+    {3.0, 100.0, 6.0, 3.0, 5.0, 0.0, 0.0},
+    {-0.5, -0.5, 2.0, 1.0, 0.0, 0.0, 0.0}};
+
+#define LCF_LN10 2.302585092994045684
+// population_priors (center, width), src/parametric.rs:1588-1621
+static __device__ __constant__ double c_pop_c[8][MAXP] = {
+    {0.0, 0.0, 0.0, 1.5, 3.0, -3.0, 0.0},
+    {-0.009 * LCF_LN10, 0.009, 1.327 * LCF_LN10, -12.0, 0.360 * LCF_LN10, 1.454 * LCF_LN10, -1.033 * LCF_LN10},
+    {0, 0, 0, 0, 0, 0, 0}, {0, 0, 0, 0, 0, 0, 0}, {0, 0, 0, 0, 0, 0, 0},
+    {0, 0, 0, 0, 0, 0, 0}, {0, 0, 0, 0, 0, 0, 0}, {0, 0, 0, 0, 0, 0, 0}};
+static __device__ __constant__ double c_pop_w[8][MAXP] = {
+    {2.0, 0.2, 30.0, 2.5, 2.5, 2.0, 0.0},
+    {0.10 * LCF_LN10, 0.010, 0.40 * LCF_LN10, 15.0, 0.35 * LCF_LN10, 0.40 * LCF_LN10, 0.50 * LCF_LN10},
+    {5, 5, 5, 5, 5, 5, 5}, {5, 5, 5, 5, 5, 0, 0}, {5, 5, 5, 5, 5, 0, 0},
+    {5, 5, 5, 5, 5, 0, 0}, {5, 5, 5, 5, 5, 5, 0}, {5, 5, 5, 5, 5, 0, 0}};
+// prior_params (center, width), src/parametric.rs:2072-2115
+static __device__ __constant__ double c_pri_c[8][MAXP] = {
+    {0, 0, 0, 0, 0, 0, 0},
+    {0, 0, 0, 0, 0, 0, 0},
+    {0, 0, 0, 0, 0, 1.67, 0},
+    {0, 0, 2.3, 0, 0, 0, 0},
+    {0, 0, 3.0, 2.3, 0, 0, 0},
+    {0, 0, 0.5, 1.0, 0, 0, 0},
+    {0, 0, 1.0, 0.8, 2.0, 0, 0},
+    {-1.75, -1.25, 0.5, -0.5, 0.0, 0, 0}};
+static __device__ __constant__ double c_pri_w[8][MAXP] = {
+    {2, 2, 2, 2, 2, 2, 0},
+    {2, 2, 2, 2, 2, 2, 2},
+    {2, 2, 2, 2, 2, 1.0, 2},
+    {2, 2, 1.0, 2, 2, 0, 0},
+    {2, 2, 1.5, 1.0, 2, 0, 0},
+    {2, 2, 1.0, 2.0, 2, 0, 0},
+    {2, 2, 2.0, 1.0, 1.0, 2, 0},
+    {1.25, 0.75, 1.5, 1.5, 2.0, 0, 0}};
+// model order of pso_model_select, src/parametric.rs:2002-2011
+static __device__ __constant__ int c_select_order[8] = {BAZIN, ARNETT, TDE, AFTERGLOW, VILLAR, MAGNETAR, SHOCK, METZGER};
+
+// ---------------------------------------------------------------------------
+// Device data layout (all arrays in HBM, sized for the batch)
+// ---------------------------------------------------------------------------
+// One observation of a peak-normalised band, as staged for the FP32 kernels:
+//   x = time (FP32 high part), y = time low part (t - x),
+//   z = flux / peak for detections, 3*err/peak (the upper limit) for upper
+//       limits,
+//   w = obs_var = (err/peak)^2 + 1e-10, negated for upper limits.
+// Observations are stored sorted by time within each band (16 B each; the
+// 16-byte granule is what the TMA bulk copy into shared memory needs).
+struct BandStats {
+    int64_t off;        // first observation (into the observation arrays)
+    int32_t n;          // observations
+    int32_t valid;      // 1 if the reference would fit this band
+    double peak;        // peak raw flux
+    double t_first;     // min time
+    double t_last;      // max time
+    double t_peak;      // time of the first maximum detection flux (original order)
+    double t_peak_all;  // time of the first maximum flux over all observations
+    int32_t source;
+    int32_t rank;       // position after the by-count sort inside the source
+};
+
+// A PSO task: one swarm run.
+struct PsoTask {
+    int32_t band;
+    int16_t kind;       // model id, or KIND_MB1 + K - 1
+    int8_t restart;     // 0, 1, 2 -> seed 42, 137, 271
+    uint8_t flags;      // TASK_*
+    int32_t out;        // result slot
+    int32_t aux;        // seed-particle slot (MultiBazin seeded restart) or -1
+    double t0_fixed;    // profile t0 search: value t0 is held at
+};
+enum : uint8_t {
+    TASK_PRIOR = 1,       // add the population prior
+    TASK_T0_BOUNDS = 2,   // data-informed t0 bounds (pso_fit_single_model)
+    TASK_SEEDED = 4,      // first particle is a seed particle
+    TASK_T0_FIXED = 8,    // t0 removed from the search (profile_t0_search)
+    TASK_RANK0 = 16,      // run only if the band is its source's rank-0 band with n >= 5
+};
+
+// Result of one PSO run.
+struct PsoResult {
+    double cost;
+    int32_t iters;
+    int32_t evals;
+    float params[MB_MAXP];
+    float pad[2];
+};
+
+// Per (band, model) polished fit.
+struct ModelFit {
+    double cost;
+    double params[MAXP];
+};
+
+// Per band selected fit and final outputs (device side, FP64).
+struct BandOut {
+    int32_t model;
+    int32_t svi_steps;
+    double pso_cost;
+    double pso_params[MAXP];
+    double mu[MAXP];
+    double log_sigma[MAXP];
+    double elbo;
+    double mag_chi2;
+    double per_chi2[8];
+};
+
+// MultiBazin state per band (only rank-0 bands).
+struct MbState {
+    int32_t best_k;
+    int32_t done;       // early stop reached
+    int32_t k_done;     // last K fitted
+    int32_t pad;
+    double best_cost, best_bic;
+    double per_k_cost[LCF_MB_MAX_K];
+    double per_k_bic[LCF_MB_MAX_K];
+    double best_params[MB_MAXP];
+    double prev_params[MB_MAXP];
+    double seed[MB_MAXP];
+};
+
+// Device counters shared by the kernels of one fit.
+struct Counters {
+    int32_t task_head[8];       // dynamic work queues (one per PSO launch slot)
+    int32_t task_count[8];      // tasks appended by device task builders
+    unsigned long long particle_obs_evals;
+    unsigned long long ode_steps;
+    int32_t error;              // first error code raised on the device
+    int32_t pad;
+};
+
+struct DeviceBatch {
+    // raw inputs (FP64, caller layout)
+    const double* times;
+    const double* flux;
+    const double* err;
+    const int64_t* band_off;
+    const int32_t* src_off;
+    int n_sources, n_bands;
+    int64_t n_obs;
+    // prepared
+    BandStats* stats;
+    float4* obs;            // [n_obs] sorted FP32 records
+    double* t64;            // [n_obs] sorted FP64 copies for the FP64 stages
+    double* f64;            // flux / peak
+    double* fe64;           // err / peak
+    double* var64;          // obs_var
+    double* uf64;           // upper flux
+    double* mag64;          // observed magnitude
+    uint8_t* up;            // is_upper
+    // tables
+    const float* draws;     // [3][DRAWS_PER_SEED] uniforms of seeds 42, 137, 271
+    const float* svi_eps;   // [3][SVI_STEPS][SVI_SAMPLES][7] noise for 5, 6, 7 params
+    // results
+    PsoResult* pso_res;     // per task slot
+    ModelFit* fits;         // [n_bands * 8]
+    BandOut* out;           // [n_bands]
+    MbState* mb;            // [n_bands]
+    PsoTask* tasks[8];      // per launch slot
+    int task_cap[8];
+    Counters* ctr;
+    float* scratch;         // MetzgerKN per-warp scratch: [warps][n_max][32]
+    int64_t scratch_per_warp;
+    double* scratch64;      // FP64 scratch, 5 values per observation
+    double* t0_state;       // per band: t0_min, t0_max, best t0 of the profile search
+    int64_t t0_slot_base;   // first PsoResult slot of the t0 search region
+    int64_t mb_slot_base;   // first PsoResult slot of the MultiBazin region
+    int smem_obs;           // observations staged per warp in the PSO kernel
+};
+
+// ---------------------------------------------------------------------------
+// Launch wrappers (defined in the .cu files, called by host.cpp)
+// ---------------------------------------------------------------------------
+// pso.cu
+void launch_prep(const DeviceBatch& d, cudaStream_t s);
+// Run the PSO tasks of `slot` (count = n_host if >= 0, else the device
+// counter of the slot).  `max_dim` selects the kernel instantiation.
+void launch_pso(const DeviceBatch& d, int slot, int n_host, int max_dim, int grid, int block, cudaStream_t s);
+size_t pso_smem_bytes(int block, int smem_obs);
+int pso_blocks_per_sm(int block, size_t smem);
+int pso_init_attributes(int block, int smem_obs);
+void launch_t0_build(const DeviceBatch& d, int slot, int fine, cudaStream_t s);
+void launch_t0_pick(const DeviceBatch& d, int slot, int fine, cudaStream_t s);
+void launch_gate_build(const DeviceBatch& d, int slot, cudaStream_t s);
+void launch_mb_pick(const DeviceBatch& d, int k, cudaStream_t s);
+void launch_mb_build(const DeviceBatch& d, int slot, int k, cudaStream_t s);
+// polish.cu
+void launch_lbfgs(const DeviceBatch& d, int model_mask, cudaStream_t s);
+void launch_select(const DeviceBatch& d, int fit_all, int forced, cudaStream_t s);
+void launch_svi(const DeviceBatch& d, cudaStream_t s);
+// finalize.cu
+void launch_laplace(const DeviceBatch& d, cudaStream_t s);
+void launch_refine(const DeviceBatch& d, cudaStream_t s);
+void launch_band_cost(int model, const float4* obs, int n, float t_last, const double* params, int n_eval,
+                      int with_prior, double* costs, float* scratch, cudaStream_t s);
+
+// Host-side generation of the RNG tables (host.cpp)
+void make_draw_tables(float* draws, float* svi_eps);
+
+}  // namespace lcf

@@ -1,0 +1,358 @@
+// models_f32.cuh — FP32 model evaluation for the fused kernels.
+//
+// The reference evaluates every model in FP64 (src/parametric.rs:199-538).
+// These FP32 forms keep that arithmetic's results, including where FP64
+// overflows:
+//   * a prediction the reference computes as non-finite makes the cost 1e99
+//     (src/parametric.rs:1343-1344); FP32 would overflow at e^88.7 instead of
+//     e^709.78, so each model tests the FP64 overflow point of its own
+//     formula explicitly (status ST_NONFINITE);
+//   * a finite but huge prediction (|pred| > e^60) is carried as its natural
+//     log (status ST_BIG) so that the negative log-likelihood can still order
+//     such particles the way FP64 does (including +inf costs once d*d or
+//     d*d/tv overflow in FP64);
+//   * ln(1 + e^phase) overflows in FP64 for phase > 709.78, which turns the
+//     decay factors of Tde/Arnett/Magnetar/ShockCooling/Afterglow into exact
+//     zeros; that is reproduced, while below that point softplus is evaluated
+//     stably;
+//   * products of a growing and a decaying exponential that fit in FP64 are
+//     formed in log space.
+// Times come as (hi, lo) FP32 pairs so that phase = t - t0 keeps FP64-level
+// accuracy near t0, where the sigmoid rises are steep.
+#pragma once
+
+#include "lcf_internal.cuh"
+
+#include <math.h>
+#include <stdint.h>
+
+namespace lcf {
+
+constexpr float LN_DBL_MAX = 709.782712893384f;   // ln(DBL_MAX)
+constexpr float LN_SQRT_DBL_MAX = 354.891356446692f;
+constexpr float BIG_L = 60.0f;                     // carry |pred| > e^60 in log form
+constexpr float LN_2PI_F = 1.8378770664093453f;
+constexpr double BIG_COST = 1e99;
+
+enum : int { ST_OK = 0, ST_BIG = 1, ST_NONFINITE = 2 };
+
+__device__ __forceinline__ float softplus_f(float x) {
+    // ln(1 + e^x) without overflow or cancellation
+    return x > 15.0f ? x + expf(-x) : log1pf(expf(x));
+}
+
+// phase_soft = ln(1 + e^phase) + 1e-6 (src/parametric.rs:306).  Returns
+// false when the FP64 reference overflows (phase > 709.78 -> +inf).
+__device__ __forceinline__ bool phase_soft_f(float phase, float& ps) {
+    if (phase > LN_DBL_MAX) return false;
+    ps = softplus_f(phase) + 1e-6f;
+    return true;
+}
+
+__device__ __forceinline__ float sigmoid_f(float x) {
+    // 1 / (1 + e^-x); saturates to 0 exactly where FP32 e^-x overflows
+    return 1.0f / (1.0f + expf(-x));
+}
+
+// ---------------------------------------------------------------------------
+// Per-particle model state: hoists exp(log-param) and reciprocals out of the
+// observation loop.  eval(th, tl, st) returns the prediction (or its log when
+// st == ST_BIG).
+// ---------------------------------------------------------------------------
+struct BazinF {
+    float a, la, b, t0, itr, itf;
+    __device__ void init(const float* p) {
+        la = p[0]; a = expf(p[0]); b = p[1]; t0 = p[2]; itr = expf(-p[3]); itf = expf(-p[4]);
+    }
+    __device__ __forceinline__ float eval(float th, float tl, int& st) const {
+        float dt = (th - t0) + tl;
+        float xf = -dt * itf, xr = -dt * itr;
+        if (xf < 80.0f && xr < 80.0f) {
+            float ef = expf(xf);
+            float sig = 1.0f / (1.0f + expf(xr));
+            return a * ef * sig + b;
+        }
+        // FP64: a*e_fall overflows (-> non-finite) once la + xf > ln DBL_MAX
+        if (xf > LN_DBL_MAX || la + xf > LN_DBL_MAX) { st = ST_NONFINITE; return 0.0f; }
+        if (xr > LN_DBL_MAX) return b;  // sigmoid is exactly 0 in FP64
+        float L = la + xf - softplus_f(xr);
+        if (L > BIG_L) { st = ST_BIG; return L; }
+        return expf(L) + b;
+    }
+};
+
+struct VillarF {
+    float a, beta, gamma, t0, itr, itf, omb;
+    __device__ void init(const float* p) {
+        a = expf(p[0]); beta = p[1]; gamma = expf(p[2]); t0 = p[3]; itr = expf(-p[4]); itf = expf(-p[5]);
+        omb = 1.0f - beta * gamma;
+    }
+    __device__ __forceinline__ float eval(float th, float tl, int& st) const {
+        // Within the Villar box every exponent stays below 70, so FP32 holds
+        // the FP64 result without special cases.
+        float ph = (th - t0) + tl;
+        float sig = 1.0f / (1.0f + expf(-ph * itr));
+        float w = 1.0f / (1.0f + expf(-10.0f * (ph - gamma)));
+        float pl = 1.0f - beta * ph;
+        float pr = omb * expf((gamma - ph) * itf);
+        return a * sig * ((1.0f - w) * pl + w * pr);
+    }
+    // Villar physical constraint of PsoCost, src/parametric.rs:1305-1318
+    __device__ static float constraint(const float* p) {
+        float beta = p[1], gamma = expf(p[2]), tr = expf(p[4]), tf = expf(p[5]);
+        float c1 = fmaxf(gamma * beta - 1.0f, 0.0f);
+        float c2 = fmaxf(expf(-gamma / tr) * (tf / tr - 1.0f) - 1.0f, 0.0f);
+        float c3 = fmaxf(beta * tf - 1.0f + beta * gamma, 0.0f);
+        return c1 + c2 + c3;
+    }
+};
+
+struct TdeF {
+    float a, b, t0, itr, itf, alpha;
+    __device__ void init(const float* p) {
+        a = expf(p[0]); b = p[1]; t0 = p[2]; itr = expf(-p[3]); itf = expf(-p[4]); alpha = p[5];
+    }
+    __device__ __forceinline__ float eval(float th, float tl, int& st) const {
+        float ph = (th - t0) + tl;
+        float sig = 1.0f / (1.0f + expf(-ph * itr));
+        float ps;
+        if (!phase_soft_f(ph, ps)) return b;  // w = inf -> decay = 0
+        float decay = expf(-alpha * log1pf(ps * itf));
+        return a * sig * decay + b;
+    }
+};
+
+struct ArnettF {
+    float a, t0, itm, f;
+    __device__ void init(const float* p) {
+        a = expf(p[0]); t0 = p[1]; itm = expf(-p[2]); f = 1.0f / (1.0f + expf(-p[3]));
+    }
+    __device__ __forceinline__ float eval(float th, float tl, int& st) const {
+        float ph = (th - t0) + tl;
+        float ps;
+        if (!phase_soft_f(ph, ps)) return 0.0f;  // heat = 0
+        float heat = f * expf(-ps * (1.0f / 8.8f)) + (1.0f - f) * expf(-ps * (1.0f / 111.3f));
+        float x = ps * itm;
+        return a * heat * (-expm1f(-x * x));
+    }
+};
+
+struct MagnetarF {
+    float a, t0, itsd, itd;
+    __device__ void init(const float* p) {
+        a = expf(p[0]); t0 = p[1]; itsd = expf(-p[2]); itd = expf(-p[3]);
+    }
+    __device__ __forceinline__ float eval(float th, float tl, int& st) const {
+        float ph = (th - t0) + tl;
+        float ps;
+        if (!phase_soft_f(ph, ps)) return 0.0f;  // spindown = 0
+        float w = 1.0f + ps * itsd;
+        float x = ps * itd;
+        return a * (-expm1f(-x * x)) / (w * w);
+    }
+};
+
+struct ShockF {
+    float a, t0, n, ittr;
+    __device__ void init(const float* p) {
+        a = expf(p[0]); t0 = p[1]; n = p[2]; ittr = expf(-p[3]);
+    }
+    __device__ __forceinline__ float eval(float th, float tl, int& st) const {
+        float ph = (th - t0) + tl;
+        float ps;
+        if (!phase_soft_f(ph, ps)) return 0.0f;  // cooling = cutoff = 0
+        float sig5 = 1.0f / (1.0f + expf(-5.0f * ph));
+        float r = ps * ittr;
+        // ps^-n * exp(-r^2) in one exponential
+        return a * sig5 * expf(-n * logf(ps) - r * r);
+    }
+};
+
+struct AfterglowF {
+    float la, t0, ltb, a1, a2;
+    __device__ void init(const float* p) {
+        la = p[0]; t0 = p[1]; ltb = p[2]; a1 = p[3]; a2 = p[4];
+    }
+    __device__ __forceinline__ float eval(float th, float tl, int& st) const {
+        float ph = (th - t0) + tl;
+        float ps;
+        if (!phase_soft_f(ph, ps)) return 0.0f;  // u = inf -> flux 0
+        float lr = logf(ps) - ltb;
+        float s1 = 2.0f * a1 * lr, s2 = 2.0f * a2 * lr;
+        float mx = fmaxf(s1, s2);
+        float lu = mx + log1pf(expf(-fabsf(s1 - s2)));
+        float L = la - 0.5f * lu;
+        if (L > BIG_L) { st = ST_BIG; return L; }
+        return expf(L);
+    }
+};
+
+// ---------------------------------------------------------------------------
+// Negative log-likelihood accumulator of PsoCost::cost_from_slice
+// (src/parametric.rs:1339-1354): Kahan-compensated FP32 sum of the ordinary
+// terms, a log-domain sum of the huge ones, and the two FP64 overflow flags.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ float log_normal_cdf_f(float x) {
+    // log_normal_cdf, src/parametric.rs:882-901, evaluated in log space
+    if (x > 8.0f) return 0.0f;
+    if (x < -30.0f) return -0.5f * x * x - 0.5f * LN_2PI_F - logf(-x);
+    float z = -x * 0.70710678118654752f;
+    float t = 1.0f / (1.0f + 0.3275911f * fabsf(z));
+    float poly = t * (0.254829592f + t * (-0.284496736f + t * (1.421413741f + t * (-1.453152027f + t * 1.061405429f))));
+    if (z >= 0.0f) return logf(0.5f * poly) - z * z;
+    return log1pf(-0.5f * poly * expf(-z * z));
+}
+
+struct Nll {
+    float s, c;       // Kahan sum
+    float big;        // log of the sum of huge terms (-inf: none)
+    int nonfinite;    // a prediction was non-finite in FP64 -> 1e99
+    int inf;          // a term overflowed in FP64 -> +inf
+    __device__ __forceinline__ void reset() { s = 0.0f; c = 0.0f; big = -INFINITY; nonfinite = 0; inf = 0; }
+    __device__ __forceinline__ void add(float term) {
+        float y = term - c;
+        float t = s + y;
+        c = (t - s) - y;
+        s = t;
+    }
+    __device__ __forceinline__ void add_big(float lt) {
+        if (lt > LN_DBL_MAX) { inf = 1; return; }
+        float m = fmaxf(big, lt);
+        big = m + log1pf(expf(-fabsf(big - lt)));
+    }
+    // one observation: record = (time hi, time lo, y, +/-var), pred with status
+    __device__ __forceinline__ void obs(const float4& o, float pred, int st, float se2) {
+        bool upper = o.w < 0.0f;
+        float tv = fabsf(o.w) + se2;
+        if (st == ST_OK) {
+            if (upper) {
+                float z = (o.z - pred) * rsqrtf(tv);
+                add(-log_normal_cdf_f(z));
+            } else {
+                float d = pred - o.z;
+                add(d * d / tv + logf(tv));
+            }
+        } else if (st == ST_BIG) {
+            // |pred| = e^pred (pred > e^60 >> |y|); FP64 d*d overflows past e^354.89
+            float L = pred;
+            float ltv = logf(tv);
+            if (upper) {
+                float lz = L - 0.5f * ltv;  // ln(-z), z < -30 branch of log_normal_cdf
+                if (lz > LN_SQRT_DBL_MAX) { inf = 1; return; }
+                add(0.5f * LN_2PI_F + lz);
+                add_big(2.0f * lz - 0.69314718f);
+            } else {
+                if (L > LN_SQRT_DBL_MAX) { inf = 1; return; }
+                add(ltv);
+                add_big(2.0f * L - ltv);
+            }
+        } else {
+            nonfinite = 1;
+        }
+    }
+    // cost = (sum + prior / n) / n in FP64, with the reference's special values
+    __device__ __forceinline__ double finish(double prior, double n) const {
+        if (nonfinite) return BIG_COST;
+        if (inf) return INFINITY;
+        double tot = (double)s - (double)c;
+        if (big > -INFINITY) {
+            if (big > LN_DBL_MAX) return INFINITY;
+            tot += exp((double)big);
+        }
+        return (tot + prior / n) / n;
+    }
+};
+
+// ---------------------------------------------------------------------------
+// MetzgerKN one-zone kilonova (metzger_kn_eval_batch, src/parametric.rs:544-648)
+// in FP32.  Quantities are carried in scaled units so that no intermediate
+// leaves the FP32 range (the reference forms m_ej * eps ~ 1e51 erg/s in
+// FP64): masses in units of 1e30 g, energies in the reference's 1e40 erg
+// scale.  0.5 - atan(x)/pi is evaluated as atan(1/x)/pi (x > 0 on the whole
+// grid), which removes the FP64 cancellation.
+// The sweep walks the 200-point log grid once and interpolates the
+// observations, which are sorted by time, as the grid passes them.  The
+// unnormalised interpolants go to `lv` (per-lane strided scratch), the peak
+// luminosity to `l_peak`.  Returns false if every prediction is zero.
+// ---------------------------------------------------------------------------
+struct MetzgerF {
+    static constexpr int NG = 200;
+    // p: [log10 M_ej/Msun, log10 v_ej/c, log10 kappa, t0, log sigma_extra]
+    template <class Obs>
+    __device__ static bool sweep(const float* p, float t_last, const Obs& obs, int n, float* lv, int lv_stride,
+                                 float& l_peak_out, unsigned long long* steps) {
+        const float MSUN30 = 1.989e3f;      // Msun in 1e30 g
+        const float C = 2.998e10f;
+        const float SPD = 86400.0f;
+        const float PI_F = 3.14159265358979f;
+        float m30 = exp10f(p[0]) * MSUN30;  // M_ej / 1e30 g
+        float v = exp10f(p[1]) * C;
+        float kappa_r = exp10f(p[2]);
+        float t0 = p[3];
+        float phase_max = fmaxf(0.01f, t_last - t0);
+        if (phase_max <= 0.01f) return false;
+        float lmin = -4.605170185988091f;   // ln 0.01
+        float lmax = logf(phase_max * 1.05f);
+        float dl = (lmax - lmin) / (float)(NG - 1);
+        const float xn0 = 0.8f, xr = 0.2f;
+        // e0 / 1e40 = 0.5 * m * v^2 / 1e40 = 0.5 * m30 * (v^2 / 1e10)
+        float e_th = 0.5f * m30 * (v * 1e-5f) * (v * 1e-5f);
+        float e_kin = e_th;
+        float t_day = 0.01f;
+        float r = t_day * SPD * v;
+        float m_over_scale = m30 * 1e-10f;  // M_ej / 1e40
+        float diff_k = 3.0f * m30 / (4.0f * PI_F * C) * 1e30f;  // 3 M_ej / (4 pi c), FP32 safe up to 6e32 g
+        float l_peak = -INFINITY;
+        float prev_t = t_day, prev_l = 0.0f;
+        int j = 0;
+        // observations before t0 (phase <= 0) predict 0
+        while (j < n && obs.t(j) - t0 <= 0.0f) { lv[j * lv_stride] = 0.0f; j++; }
+        for (int i = 0; i < NG; i++) {
+            float t_next = expf(lmin + dl * (float)(i + 1));
+            float t_sec = t_day * SPD;
+            float ef = 0.34f * exp2f(0.74f * log2f(t_day));
+            float eth = 0.36f * (expf(-0.56f * t_day) + (ef > 1e-10f ? log1pf(ef) / ef : 1.0f));
+            float xn = xn0 * expf(-t_sec * (1.0f / 900.0f));
+            float tt = atanf(0.11f / (t_sec - 1.3f)) * (1.0f / PI_F);
+            tt = fmaxf(tt, 1e-30f);
+            float eps_rp = 2e18f * eth * exp2f(1.3f * log2f(tt));
+            float l_heat = m_over_scale * (3.2e14f * xn + eps_rp);
+            float kappa_eff = 0.4f * (xn0 - xn) + kappa_r * xr;
+            float t_diff = kappa_eff * diff_k / (v * t_sec) + r / C;
+            float l_rad = (e_th > 0.0f && t_diff > 0.0f) ? e_th / t_diff : 0.0f;
+            l_peak = fmaxf(l_peak, l_rad);
+            // interpolate the observations whose phase lies in (prev_t, t_day]
+            if (i == 0) {
+                while (j < n && obs.t(j) - t0 <= t_day) { lv[j * lv_stride] = l_rad; j++; }
+            } else {
+                float inv = 1.0f / (t_day - prev_t);
+                while (j < n) {
+                    float ph = obs.t(j) - t0;
+                    if (ph > t_day) break;
+                    lv[j * lv_stride] = prev_l + (ph - prev_t) * inv * (l_rad - prev_l);
+                    j++;
+                }
+            }
+            prev_t = t_day;
+            prev_l = l_rad;
+            float l_pdv = r > 0.0f ? e_th * v / r : 0.0f;
+            if (i < NG - 1) {
+                float dt_sec = (t_next - t_day) * SPD;
+                e_th += (l_heat - l_pdv - l_rad) * dt_sec;
+                if (e_th < 0.0f) e_th = 0.0f;
+                e_kin += l_pdv * dt_sec;
+                // v = sqrt(2 e_kin * 1e40 / M_ej) = sqrt(2 e_kin / (m30 * 1e-10))
+                v = fminf(sqrtf(2.0f * e_kin / m_over_scale), C);
+                r += v * dt_sec;
+            }
+            t_day = t_next;
+        }
+        // phases at or beyond the last grid point
+        while (j < n) { lv[j * lv_stride] = prev_l; j++; }
+        if (steps) atomicAdd(steps, (unsigned long long)NG);
+        l_peak_out = l_peak;
+        return l_peak > 0.0f && isfinite(l_peak);
+    }
+};
+
+}  // namespace lcf

@@ -1,0 +1,652 @@
+// polish.cu — restart reduction, bounded L-BFGS polish and BIC model
+// selection (pso_fit_single_model / pso_model_select, src/parametric.rs:
+// 1864-2066), and the SVI uncertainty kernel (svi_fit, :2215-2454).
+//
+// L-BFGS: one warp per (band, model).  Cost and gradient are accumulated by
+// the lanes over the band's observations in FP32 (Kahan for the cost) and
+// reduced across the warp; the quasi-Newton algebra (two-loop recursion,
+// memory 7) and the Moré–Thuente line search run in FP64, identically in
+// every lane, following the argmin 0.11 algorithm the reference calls
+// (restated from the published method, as in the test oracle).
+//
+// SVI: one warp per band.  Per step the four reparameterised samples
+// theta = mu + sigma * eps are evaluated with the lanes over observations;
+// the adjoint of the log-likelihood with respect to each prediction is
+// propagated through the model's analytic gradient and reduced across the
+// warp.  The noise eps is regenerated from the reference's SmallRng(42)
+// stream (a table indexed by step, sample and parameter) instead of being
+// stored.  Adam runs in FP64 with one variational parameter per lane.
+#include <cuda_runtime.h>
+
+#include "grads_f32.cuh"
+#include "lcf_internal.cuh"
+#include "models_f32.cuh"
+#include "models_f64.cuh"
+
+namespace lcf {
+
+#define FULL 0xffffffffu
+
+__device__ __forceinline__ double warp_sum_d(double v) {
+    for (int k = 16; k; k >>= 1) v += __shfl_xor_sync(FULL, v, k);
+    return v;
+}
+__device__ __forceinline__ float warp_sum_f(float v) {
+    for (int k = 16; k; k >>= 1) v += __shfl_xor_sync(FULL, v, k);
+    return v;
+}
+__device__ __forceinline__ int warp_or(int v) { return __any_sync(FULL, v) ? 1 : 0; }
+
+// Warp-wide negative log-likelihood of a parameter vector (cost of PsoCost
+// without the Villar constraint and prior): lanes over observations.
+__device__ double warp_nll(int m, const float* p, const float4* obs, int n, double nd, double prior) {
+    float se = expf(p[se_idx_of(m)]);
+    float se2 = se * se;
+    Nll acc;
+    acc.reset();
+    int lane = threadIdx.x & 31;
+    for (int i = lane; i < n; i += 32) {
+        float4 o = obs[i];
+        int st = ST_OK;
+        float pr;
+        switch (m) {
+            case BAZIN: { BazinF e; e.init(p); pr = e.eval(o.x, o.y, st); break; }
+            case VILLAR: { VillarF e; e.init(p); pr = e.eval(o.x, o.y, st); break; }
+            case TDE: { TdeF e; e.init(p); pr = e.eval(o.x, o.y, st); break; }
+            case ARNETT: { ArnettF e; e.init(p); pr = e.eval(o.x, o.y, st); break; }
+            case MAGNETAR: { MagnetarF e; e.init(p); pr = e.eval(o.x, o.y, st); break; }
+            case SHOCK: { ShockF e; e.init(p); pr = e.eval(o.x, o.y, st); break; }
+            default: { AfterglowF e; e.init(p); pr = e.eval(o.x, o.y, st); break; }
+        }
+        acc.obs(o, pr, st, se2);
+    }
+    // combine the lanes
+    double s = warp_sum_d((double)acc.s - (double)acc.c);
+    int nf = warp_or(acc.nonfinite), inf = warp_or(acc.inf);
+    float big = acc.big;
+    for (int k = 16; k; k >>= 1) {
+        float o = __shfl_xor_sync(FULL, big, k);
+        float mx = fmaxf(big, o);
+        big = (mx == -INFINITY) ? -INFINITY : mx + log1pf(expf(-fabsf(big - o)));
+    }
+    if (nf) return BIG_COST;
+    if (inf) return INFINITY;
+    if (big > -INFINITY) {
+        if (big > LN_DBL_MAX) return INFINITY;
+        s += exp((double)big);
+    }
+    return (s + prior / nd) / nd;
+}
+
+struct LbCtx {
+    const float4* obs;
+    int n, m, np;
+    double nd;
+    double lo[MAXP], hi[MAXP];
+    int aborted;   // a gradient hit the reference's 1e-300 CDF floor
+};
+
+// Cost and projected gradient of the bounded problem (BoundedPsoCost,
+// src/parametric.rs:1500-1535) at x.
+__device__ void lb_cost_grad(LbCtx& c, const double* x, double& f, double* g, bool want_grad) {
+    float p[MAXP];
+    double q[MAXP];
+    for (int j = 0; j < c.np; j++) {
+        q[j] = fmin(fmax(x[j], c.lo[j]), c.hi[j]);
+        p[j] = (float)q[j];
+    }
+    // cost: PsoCost::cost_from_slice with the population prior
+    bool constrained = false;
+    if (c.m == VILLAR) {
+        float cv = VillarF::constraint(p);
+        if (cv > 0.0f) { f = 1e12 + 10000.0 * (double)cv; constrained = true; }
+    }
+    if (!constrained) {
+        double prior = 0.0;
+        for (int j = 0; j < c.np; j++) {
+            double w = c_pop_w[c.m][j];
+            if (w > 0.0) {
+                double z = (q[j] - c_pop_c[c.m][j]) / w;
+                prior += 0.5 * z * z;
+            }
+        }
+        f = warp_nll(c.m, p, c.obs, c.n, c.nd, prior);
+    }
+    if (!want_grad) return;
+    // gradient: PsoCost::gradient (no prior, no constraint term)
+    int lane = threadIdx.x & 31;
+    int se = se_idx_of(c.m);
+    float sx = expf(p[se]);
+    float se2 = sx * sx;
+    float gl[MAXP];
+    for (int j = 0; j < MAXP; j++) gl[j] = 0.0f;
+    int nonfinite = 0, huge = 0;
+    for (int i = lane; i < c.n; i += 32) {
+        float4 o = c.obs[i];
+        float mg[MAXP];
+        int st;
+        float pr = model_grad_f32(c.m, p, o.x, o.y, mg, st);
+        if (st == ST_NONFINITE) { nonfinite = 1; continue; }
+        float tv = fabsf(o.w) + se2;
+        if (o.w < 0.0f) {
+            float sv = sqrtf(tv);
+            float z = (o.z - pr) / sv;
+            bool hg;
+            float ratio = upper_ratio_f32(z, hg);
+            if (hg) huge = 1;
+            for (int j = 0; j < c.np; j++) gl[j] += ratio * mg[j] / sv;
+            gl[se] += ratio * z * se2 / tv;
+        } else {
+            float dd = pr - o.z;
+            float sc = 2.0f * dd / tv;
+            for (int j = 0; j < c.np; j++) gl[j] += sc * mg[j];
+            gl[se] += (-dd * dd / (tv * tv) + 1.0f / tv) * (2.0f * se2);
+        }
+    }
+    nonfinite = warp_or(nonfinite);
+    if (warp_or(huge)) c.aborted = 1;
+    for (int j = 0; j < c.np; j++) {
+        double gj = (double)warp_sum_f(gl[j]);
+        g[j] = nonfinite ? 0.0 : gj / c.nd;
+    }
+    for (int j = 0; j < c.np; j++)
+        if ((x[j] <= c.lo[j] && g[j] > 0.0) || (x[j] >= c.hi[j] && g[j] < 0.0)) g[j] = 0.0;
+}
+
+// MINPACK cstep (Moré–Thuente), min/max with Rust's NaN-ignoring semantics
+__device__ int lb_cstep(double& stx, double& fx, double& dx, double& sty, double& fy, double& dy, double& stp, double fp,
+                        double dp, bool& brackt, double stpmin, double stpmax) {
+    if ((brackt && (stp <= fmin(stx, sty) || stp >= fmax(stx, sty))) || dx * (stp - stx) >= 0.0 || stpmax < stpmin)
+        return 0;
+    int info;
+    bool bound;
+    double sgnd = dp * (dx / fabs(dx));
+    double stpf, stpc, stpq, theta, s, gamma, p, q, r;
+    if (fp > fx) {
+        info = 1; bound = true;
+        theta = 3.0 * (fx - fp) / (stp - stx) + dx + dp;
+        s = fmax(fmax(fabs(theta), fabs(dx)), fabs(dp));
+        gamma = s * sqrt((theta / s) * (theta / s) - (dx / s) * (dp / s));
+        if (stp < stx) gamma = -gamma;
+        p = (gamma - dx) + theta;
+        q = ((gamma - dx) + gamma) + dp;
+        r = p / q;
+        stpc = stx + r * (stp - stx);
+        stpq = stx + ((dx / ((fx - fp) / (stp - stx) + dx)) / 2.0) * (stp - stx);
+        stpf = fabs(stpc - stx) < fabs(stpq - stx) ? stpc : stpc + (stpq - stpc) / 2.0;
+        brackt = true;
+    } else if (sgnd < 0.0) {
+        info = 2; bound = false;
+        theta = 3.0 * (fx - fp) / (stp - stx) + dx + dp;
+        s = fmax(fmax(fabs(theta), fabs(dx)), fabs(dp));
+        gamma = s * sqrt((theta / s) * (theta / s) - (dx / s) * (dp / s));
+        if (stp > stx) gamma = -gamma;
+        p = (gamma - dp) + theta;
+        q = ((gamma - dp) + gamma) + dx;
+        r = p / q;
+        stpc = stp + r * (stx - stp);
+        stpq = stp + (dp / (dp - dx)) * (stx - stp);
+        stpf = fabs(stpc - stp) > fabs(stpq - stp) ? stpc : stpq;
+        brackt = true;
+    } else if (fabs(dp) < fabs(dx)) {
+        info = 3; bound = true;
+        theta = 3.0 * (fx - fp) / (stp - stx) + dx + dp;
+        s = fmax(fmax(fabs(theta), fabs(dx)), fabs(dp));
+        gamma = s * sqrt(fmax(0.0, (theta / s) * (theta / s) - (dx / s) * (dp / s)));
+        if (stp > stx) gamma = -gamma;
+        p = (gamma - dp) + theta;
+        q = (gamma + (dx - dp)) + gamma;
+        r = p / q;
+        if (r < 0.0 && gamma != 0.0) stpc = stp + r * (stx - stp);
+        else if (stp > stx) stpc = stpmax;
+        else stpc = stpmin;
+        stpq = stp + (dp / (dp - dx)) * (stx - stp);
+        if (brackt) stpf = fabs(stp - stpc) < fabs(stp - stpq) ? stpc : stpq;
+        else stpf = fabs(stp - stpc) > fabs(stp - stpq) ? stpc : stpq;
+    } else {
+        info = 4; bound = false;
+        if (brackt) {
+            theta = 3.0 * (fp - fy) / (sty - stp) + dy + dp;
+            s = fmax(fmax(fabs(theta), fabs(dy)), fabs(dp));
+            gamma = s * sqrt((theta / s) * (theta / s) - (dy / s) * (dp / s));
+            if (stp > sty) gamma = -gamma;
+            p = (gamma - dp) + theta;
+            q = ((gamma - dp) + gamma) + dy;
+            r = p / q;
+            stpc = stp + r * (sty - stp);
+            stpf = stpc;
+        } else {
+            stpf = stp > stx ? stpmax : stpmin;
+        }
+    }
+    if (fp > fx) {
+        sty = stp; fy = fp; dy = dp;
+    } else {
+        if (sgnd < 0.0) { sty = stx; fy = fx; dy = dx; }
+        stx = stp; fx = fp; dx = dp;
+    }
+    stpf = fmin(stpmax, stpf);
+    stpf = fmax(stpmin, stpf);
+    stp = stpf;
+    if (brackt && bound) {
+        if (sty > stx) stp = fmin(stx + 0.66 * (sty - stx), stp);
+        else stp = fmax(stx + 0.66 * (sty - stx), stp);
+    }
+    return info;
+}
+
+__device__ __forceinline__ double dotn(const double* a, const double* b, int n) {
+    double s = 0.0;
+    for (int i = 0; i < n; i++) s += a[i] * b[i];
+    return s;
+}
+
+// Moré–Thuente line search; false = not a descent direction (argmin error)
+__device__ bool lb_linesearch(LbCtx& c, const double* x, double f0, const double* g0, const double* d, double* xo,
+                              double& fo, double* go) {
+    const int n = c.np;
+    const double ftol = 1e-4, gtol = 0.9, xtol = 1e-10, xtrapf = 4.0, stpmin_g = 0.0, stpmax_g = INFINITY;
+    double dginit = dotn(g0, d, n);
+    if (dginit >= 0.0) return false;
+    bool brackt = false, stage1 = true;
+    int infoc = 1;
+    double finit = f0, dgtest = ftol * dginit, width = stpmax_g - stpmin_g, width1 = 2.0 * width;
+    double stx = 0.0, fx = finit, dgx = dginit, sty = 0.0, fy = finit, dgy = dginit, stp = 1.0;
+    for (int iter = 0; iter < 100; iter++) {
+        double stmin, stmax;
+        if (brackt) { stmin = fmin(stx, sty); stmax = fmax(stx, sty); }
+        else { stmin = stx; stmax = stp + xtrapf * (stp - stx); }
+        stp = fmax(stp, stpmin_g);
+        stp = fmin(stp, stpmax_g);
+        if ((brackt && (stp <= stmin || stp >= stmax)) || infoc == 0 || (brackt && stmax - stmin <= xtol * stmax))
+            stp = stx;
+        for (int i = 0; i < n; i++) xo[i] = x[i] + stp * d[i];
+        double f;
+        lb_cost_grad(c, xo, f, go, true);
+        double dg = dotn(go, d, n);
+        double ftest1 = finit + stp * dgtest;
+        int info = 0;
+        if ((brackt && (stp <= stmin || stp >= stmax)) || infoc == 0) info = 6;
+        if (stp == stpmax_g && f <= ftest1 && dg <= dgtest) info = 5;
+        if (stp == stpmin_g && (f > ftest1 || dg >= dgtest)) info = 4;
+        if (brackt && stmax - stmin <= xtol * stmax) info = 2;
+        if (f <= ftest1 && fabs(dg) <= gtol * (-dginit)) info = 1;
+        if (info != 0) { fo = f; return true; }
+        if (stage1 && f <= ftest1 && dg >= fmin(ftol, gtol) * dginit) stage1 = false;
+        if (stage1 && f <= fx && f > ftest1) {
+            double fm = f - stp * dgtest, fxm = fx - stx * dgtest, fym = fy - sty * dgtest;
+            double dgm = dg - dgtest, dgxm = dgx - dgtest, dgym = dgy - dgtest;
+            infoc = lb_cstep(stx, fxm, dgxm, sty, fym, dgym, stp, fm, dgm, brackt, stmin, stmax);
+            fx = fxm + stx * dgtest; fy = fym + sty * dgtest;
+            dgx = dgxm + dgtest; dgy = dgym + dgtest;
+        } else {
+            infoc = lb_cstep(stx, fx, dgx, sty, fy, dgy, stp, f, dg, brackt, stmin, stmax);
+        }
+        if (brackt) {
+            if (fabs(sty - stx) >= 0.66 * width1) stp = stx + 0.5 * (sty - stx);
+            width1 = width;
+            width = fabs(sty - stx);
+        }
+    }
+    double g_unused[MAXP];
+    lb_cost_grad(c, xo, fo, g_unused, false);
+    return true;
+}
+
+// lbfgs_refine, src/parametric.rs:1453-1497: returns the polished cost and
+// writes the parameters when the polish improved the PSO result.
+__device__ double lbfgs_polish(LbCtx& c, double* params, double pso_cost) {
+    const int n = c.np, M = 7, MAXIT = 50;
+    const double tol_grad = 1e-6, tol_cost = 2.220446049250313e-16;
+    double x[MAXP], g[MAXP], f;
+    for (int i = 0; i < n; i++) x[i] = params[i];
+    c.aborted = 0;
+    lb_cost_grad(c, x, f, g, true);
+    double best_x[MAXP], best_f = INFINITY, prev_f = INFINITY;
+    if (f < best_f) { best_f = f; for (int i = 0; i < n; i++) best_x[i] = x[i]; }
+    double S[M][MAXP], Y[M][MAXP];
+    int cm = 0, head = 0;  // ring buffer: oldest at head
+    int it = 0;
+    bool ok = true;
+    auto converged = [&]() { return sqrt(dotn(g, g, n)) < tol_grad || fabs(prev_f - f) < tol_cost; };
+    bool stop = converged() || it >= MAXIT;
+    while (!stop && !c.aborted) {
+        double gamma = 1.0;
+        if (cm > 0) {
+            int last = (head + cm - 1) % M;
+            gamma = dotn(S[last], Y[last], n) / dotn(Y[last], Y[last], n);
+        }
+        double q[MAXP], alpha[M], rho[M];
+        for (int k = 0; k < n; k++) q[k] = g[k];
+        for (int i = 0; i < cm; i++) {
+            int idx = (head + cm - 1 - i) % M;
+            double rt = 1.0 / dotn(Y[idx], S[idx], n);
+            alpha[i] = rt * dotn(S[idx], q, n);
+            for (int k = 0; k < n; k++) q[k] -= Y[idx][k] * alpha[i];
+            rho[i] = rt;
+        }
+        double r[MAXP];
+        for (int k = 0; k < n; k++) r[k] = q[k] * gamma;
+        for (int i = 0; i < cm; i++) {
+            int idx = (head + i) % M;
+            double beta = dotn(Y[idx], r, n) * rho[cm - i - 1];
+            for (int k = 0; k < n; k++) r[k] += S[idx][k] * (alpha[cm - i - 1] - beta);
+        }
+        double dvec[MAXP], xn[MAXP], gn[MAXP], fnew;
+        for (int k = 0; k < n; k++) dvec[k] = -r[k];
+        if (!lb_linesearch(c, x, f, g, dvec, xn, fnew, gn)) { ok = false; break; }
+        lb_cost_grad(c, xn, fnew, gn, true);
+        int slot;
+        if (cm < M) { slot = (head + cm) % M; cm++; }
+        else { slot = head; head = (head + 1) % M; }
+        for (int k = 0; k < n; k++) { S[slot][k] = xn[k] - x[k]; Y[slot][k] = gn[k] - g[k]; x[k] = xn[k]; g[k] = gn[k]; }
+        prev_f = f;
+        f = fnew;
+        if (f < best_f) { best_f = f; for (int i = 0; i < n; i++) best_x[i] = x[i]; }
+        it++;
+        stop = converged() || it >= MAXIT;
+    }
+    if (!ok || c.aborted) return pso_cost;
+    double cl[MAXP], fc, gdummy[MAXP];
+    for (int i = 0; i < n; i++) cl[i] = fmin(fmax(best_x[i], c.lo[i]), c.hi[i]);
+    lb_cost_grad(c, cl, fc, gdummy, false);
+    if (fc < pso_cost && isfinite(fc)) {
+        for (int i = 0; i < n; i++) params[i] = cl[i];
+        return fc;
+    }
+    return pso_cost;
+}
+
+// One warp per (band, model): best of the three restarts, then L-BFGS.
+__global__ void lbfgs_kernel(DeviceBatch d, int model_mask) {
+    int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    if (warp >= d.n_bands * 8) return;
+    int b = warp >> 3, m = warp & 7;
+    if (!((model_mask >> m) & 1)) return;
+    BandStats bs = d.stats[b];
+    if (!bs.valid) return;
+    const PsoResult* R = d.pso_res + (size_t)(b * 8 + m) * 3;
+    if (R[0].iters < 0) return;  // this model was not fitted for this band
+    double best_c = INFINITY;
+    int best_r = -1;
+    for (int r = 0; r < 3; r++)
+        if (R[r].iters >= 0 && R[r].cost < best_c) { best_c = R[r].cost; best_r = r; }
+    int np = n_params_of(m);
+    double params[MAXP];
+    for (int j = 0; j < MAXP; j++) params[j] = (best_r >= 0 && j < np) ? (double)R[best_r].params[j] : 0.0;
+    double cost = best_c;
+    if (m != METZGER && best_r >= 0) {
+        LbCtx c;
+        c.obs = d.obs + bs.off;
+        c.n = bs.n;
+        c.m = m;
+        c.np = np;
+        c.nd = (double)max(bs.n, 1);
+        for (int j = 0; j < MAXP; j++) { c.lo[j] = c_lo[m][j]; c.hi[j] = c_hi[m][j]; }
+        int t0i = t0_idx_of(m);
+        double t0_lo = fmax(bs.t_first - 30.0, c.lo[t0i]);
+        double t0_hi = fmin(bs.t_peak + 10.0, c.hi[t0i]);
+        if (t0_lo < t0_hi) { c.lo[t0i] = t0_lo; c.hi[t0i] = t0_hi; }
+        cost = lbfgs_polish(c, params, best_c);
+    }
+    if ((threadIdx.x & 31) == 0) {
+        ModelFit& F = d.fits[b * 8 + m];
+        F.cost = cost;
+        for (int j = 0; j < MAXP; j++) F.params[j] = j < np ? params[j] : NAN;
+    }
+}
+
+void launch_lbfgs(const DeviceBatch& d, int model_mask, cudaStream_t s) {
+    if (d.n_bands == 0) return;
+    int block = 128;
+    int64_t threads = (int64_t)d.n_bands * 8 * 32;
+    lbfgs_kernel<<<(int)((threads + block - 1) / block), block, 0, s>>>(d, model_mask);
+}
+
+// ---------------------------------------------------------------------------
+// BIC model selection (pso_model_select, src/parametric.rs:2016-2065), one
+// thread per band.  mode 0: full selection over the fitted models;
+// mode 1: Bazin gate of fit_all_models == false (cost < 2 -> stop).
+// ---------------------------------------------------------------------------
+__global__ void select_kernel(DeviceBatch d, int fit_all, int forced) {
+    int b = blockIdx.x * blockDim.x + threadIdx.x;
+    if (b >= d.n_bands) return;
+    BandStats bs = d.stats[b];
+    BandOut& o = d.out[b];
+    o.model = -1;
+    for (int m = 0; m < 8; m++) o.per_chi2[m] = NAN;
+    if (!bs.valid) return;
+    double nn = (double)max(bs.n, 1), ln_n = log(nn);
+    int best = -1;
+    double best_bic = INFINITY, best_cost = INFINITY;
+    for (int k = 0; k < 8; k++) {
+        int m = forced >= 0 ? (k == 0 ? forced : -1) : c_select_order[k];
+        if (m < 0) break;
+        const PsoResult* R = d.pso_res + (size_t)(b * 8 + m) * 3;
+        if (R[0].iters < 0) continue;
+        double c = d.fits[b * 8 + m].cost;
+        o.per_chi2[m] = isfinite(c) ? c : NAN;
+        double bic = 2.0 * c * nn + (double)n_params_of(m) * ln_n;
+        if (best < 0) { best = m; best_bic = bic; best_cost = c; }
+        else if (bic < best_bic) { best = m; best_bic = bic; best_cost = c; }
+    }
+    o.model = best;
+    o.pso_cost = best_cost;
+    for (int j = 0; j < MAXP; j++) o.pso_params[j] = best >= 0 ? d.fits[b * 8 + best].params[j] : NAN;
+}
+
+void launch_select(const DeviceBatch& d, int fit_all, int forced, cudaStream_t s) {
+    if (d.n_bands == 0) return;
+    select_kernel<<<(d.n_bands + 127) / 128, 128, 0, s>>>(d, fit_all, forced);
+}
+
+// ---------------------------------------------------------------------------
+// SVI, one warp per band
+// ---------------------------------------------------------------------------
+// MetzgerKN: predictions and forward-difference gradients in FP64
+// (metzger_kn_grad_batch_into, src/parametric.rs:843-860).  Lane j < 5
+// solves the model at theta + 1e-5 e_j (lane 4: the base point) over the
+// band into scratch; lanes then read them per observation.
+__device__ bool metzger_svi_sample(const double* th, const double* t64, int n, double* scr, double* pred_out) {
+    int lane = threadIdx.x & 31;
+    if (lane < 5) {
+        double pp[5];
+        for (int q = 0; q < 5; q++) pp[q] = th[q];
+        if (lane < 4) pp[lane] += 1e-5;
+        metzger_f64(pp, t64, n, scr + (size_t)lane * n);
+    }
+    __syncwarp();
+    (void)pred_out;
+    return true;
+}
+
+__global__ void svi_kernel(DeviceBatch d) {
+    const int lane = threadIdx.x & 31;
+    const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    if (warp >= d.n_bands) return;
+    const int b = warp;
+    const BandStats bs = d.stats[b];
+    BandOut& o = d.out[b];
+    if (!bs.valid || o.model < 0) return;
+    const int m = o.model, np = n_params_of(m), se = se_idx_of(m), n = bs.n;
+    const float4* obs = d.obs + bs.off;
+    double init[MAXP];
+    for (int j = 0; j < np; j++) init[j] = o.pso_params[j];
+    // lane i < 2 np owns variational parameter i (mu_j, then log sigma_j)
+    double vp = 0.0, am = 0.0, av = 0.0;
+    bool frozen = false;
+    if (lane < np) vp = init[lane];
+    else if (lane < 2 * np) vp = -1.0;
+    const float* eps_tab = d.svi_eps + (size_t)(np - 5) * SVI_STEPS * SVI_SAMPLES * 7;
+    double pc[MAXP], pw2[MAXP];
+    for (int j = 0; j < np; j++) {
+        pc[j] = j == se ? c_pri_c[m][j] : init[j];
+        double w = c_pri_w[m][j];
+        pw2[j] = w * w;
+    }
+    const double ln_2pie = 2.8378770664093453;  // ln(2 pi e)
+    double b1t = 1.0, b2t = 1.0;
+    double ema = -INFINITY, best_ema = -INFINITY, final_elbo = -INFINITY;
+    int no_imp = 0, steps = 0;
+    double* scr = d.scratch64 + 5 * bs.off;
+    const double* t64 = d.t64 + bs.off;
+    for (int step = 0; step < SVI_STEPS; step++) {
+        steps = step + 1;
+        double mu[MAXP], sg[MAXP];
+        for (int j = 0; j < np; j++) {
+            mu[j] = __shfl_sync(FULL, vp, j);
+            sg[j] = exp(__shfl_sync(FULL, vp, np + j));
+        }
+        double gmu[MAXP], gls[MAXP];
+        for (int j = 0; j < np; j++) { gmu[j] = 0.0; gls[j] = 0.0; }
+        double elbo_sum = 0.0;
+        int huge_any = 0;
+        for (int k = 0; k < SVI_SAMPLES; k++) {
+            const float* ep = eps_tab + ((size_t)step * SVI_SAMPLES + k) * 7;
+            double th[MAXP], eps[MAXP];
+            float pf[MAXP];
+            for (int j = 0; j < np; j++) {
+                eps[j] = (double)ep[j];
+                th[j] = mu[j] + sg[j] * eps[j];
+                pf[j] = (float)th[j];
+            }
+            float sx = expf(pf[se]);
+            float sx2 = sx * sx;
+            float dll[MAXP];
+            for (int j = 0; j < MAXP; j++) dll[j] = 0.0f;
+            Nll ll;
+            ll.reset();
+            int huge = 0;
+            bool skip_sample = false;
+            if (m == METZGER) {
+                // reference path in FP64: base and forward differences
+                metzger_svi_sample(th, t64, n, scr, nullptr);
+                double mx = -INFINITY;
+                for (int i = lane; i < n; i += 32)
+                    if (!d.up[bs.off + i]) mx = fmax(mx, scr[4 * (size_t)n + i]);
+                for (int kk = 16; kk; kk >>= 1) mx = fmax(mx, __shfl_xor_sync(FULL, mx, kk));
+                double scl = 1.0;
+                if (mx > 1e-10 && isfinite(mx)) {
+                    double raw = 1.0 / mx;
+                    scl = fmin(fmax(raw, 0.1), 10.0);
+                    if (fabs(raw - scl) / raw > 0.5) skip_sample = true;
+                }
+                if (!skip_sample) {
+                    double sx2d = exp(2.0 * th[se]);
+                    for (int i = lane; i < n; i += 32) {
+                        double pr = scr[4 * (size_t)n + i] * scl;
+                        if (!isfinite(pr)) continue;
+                        double gb[5];
+                        for (int j = 0; j < 4; j++) gb[j] = (scr[(size_t)j * n + i] - scr[4 * (size_t)n + i]) / 1e-5 * scl;
+                        gb[4] = 0.0;
+                        double tv = d.var64[bs.off + i] + sx2d, st = sqrt(tv);
+                        if (d.up[bs.off + i]) {
+                            double z = (d.uf64[bs.off + i] - pr) / st;
+                            ll.add((float)log_normal_cdf_f64(z));
+                            bool hg;
+                            float ratio = upper_ratio_f32((float)z, hg);
+                            if (hg) huge = 1;
+                            for (int j = 0; j < 4; j++) if (isfinite(gb[j])) dll[j] += (float)(-ratio / st * gb[j]);
+                            dll[se] += (float)(ratio * (-(d.uf64[bs.off + i] - pr) * sx2d / (st * tv)));
+                        } else {
+                            double res = d.f64[bs.off + i] - pr, it = 1.0 / tv, r2 = res * res;
+                            ll.add((float)(-0.5 * (r2 * it + log(2.0 * 3.14159265358979323846 * tv))));
+                            for (int j = 0; j < 4; j++) if (isfinite(gb[j])) dll[j] += (float)(res * it * gb[j]);
+                            dll[se] += (float)((r2 * it * it - it) * sx2d);
+                        }
+                    }
+                }
+                __syncwarp();
+            } else {
+                for (int i = lane; i < n; i += 32) {
+                    float4 ob = obs[i];
+                    float gb[MAXP];
+                    int st;
+                    float pr = model_grad_f32(m, pf, ob.x, ob.y, gb, st);
+                    if (st == ST_NONFINITE || !isfinite(pr)) continue;
+                    float tv = fabsf(ob.w) + sx2;
+                    float stv = sqrtf(tv);
+                    if (ob.w < 0.0f) {
+                        float z = (ob.z - pr) / stv;
+                        ll.add(log_normal_cdf_f(z));
+                        bool hg;
+                        float ratio = upper_ratio_f32(z, hg);
+                        if (hg) huge = 1;
+                        float dpred = -ratio / stv;
+                        for (int j = 0; j < np; j++)
+                            if (j != se && isfinite(gb[j])) dll[j] += dpred * gb[j];
+                        dll[se] += ratio * (-(ob.z - pr) * sx2 / (stv * tv));
+                    } else {
+                        float res = ob.z - pr;
+                        float it = 1.0f / tv;
+                        float r2 = res * res;
+                        ll.add(-0.5f * (r2 * it + logf(6.283185307179586f * tv)));
+                        for (int j = 0; j < np; j++)
+                            if (j != se && isfinite(gb[j])) dll[j] += res * it * gb[j];
+                        dll[se] += (r2 * it * it - it) * sx2;
+                    }
+                }
+            }
+            if (__any_sync(FULL, skip_sample)) continue;
+            if (warp_or(huge)) huge_any = 1;
+            double lls = warp_sum_d((double)ll.s - (double)ll.c);
+            double lp = 0.0;
+            for (int j = 0; j < np; j++) {
+                double dlj = (double)warp_sum_f(dll[j]);
+                double dd = th[j] - pc[j];
+                lp += -0.5 * dd * dd / pw2[j];
+                double df = dlj + (-dd / pw2[j]);
+                gmu[j] += df;
+                gls[j] += df * sg[j] * eps[j];
+            }
+            elbo_sum += lls + lp;
+        }
+        const double ns = (double)SVI_SAMPLES;
+        double ent = 0.0;
+        for (int j = 0; j < np; j++) ent += __shfl_sync(FULL, vp, np + j);
+        ent += 0.5 * (double)np * ln_2pie;
+        final_elbo = elbo_sum / ns + ent;
+        // Adam, lane i owns variational parameter i
+        double gi = 0.0;
+        for (int j = 0; j < np; j++) {
+            if (lane == j) gi = -(gmu[j] / ns);
+            if (lane == np + j) gi = -(gls[j] / ns + 1.0);
+        }
+        b1t *= 0.9;
+        b2t *= 0.999;
+        if (huge_any) frozen = true;  // the reference's v overflows to +inf: updates stop
+        if (lane < 2 * np && isfinite(gi) && !frozen) {
+            am = 0.9 * am + (1.0 - 0.9) * gi;
+            av = 0.999 * av + (1.0 - 0.999) * gi * gi;
+            double mh = am / (1.0 - b1t), vh = av / (1.0 - b2t);
+            vp -= SVI_LR * mh / (sqrt(vh) + 1e-8);
+        }
+        if (lane >= np && lane < 2 * np) vp = fmin(fmax(vp, -6.0), 2.0);
+        if (step >= 200) {
+            if (ema == -INFINITY) ema = final_elbo;
+            else ema = 0.1 * final_elbo + 0.9 * ema;
+            bool imp = ema - best_ema > 0.01 * fmax(fabs(best_ema), 1e-10);
+            if (imp) { best_ema = ema; no_imp = 0; }
+            else if (++no_imp >= 50) break;
+        }
+    }
+    const double ln4 = 1.3862943611198906;
+    double out_v = lane < np ? vp : vp + ln4;
+    if (lane < np) o.mu[lane] = out_v;
+    else if (lane < 2 * np) o.log_sigma[lane - np] = out_v;
+    if (lane >= np && lane < MAXP) o.mu[lane] = NAN;
+    if (lane == 0) {
+        for (int j = np; j < MAXP; j++) o.log_sigma[j] = NAN;
+        o.elbo = final_elbo;
+        o.svi_steps = steps;
+    }
+}
+
+void launch_svi(const DeviceBatch& d, cudaStream_t s) {
+    if (d.n_bands == 0) return;
+    int block = 128;
+    int64_t threads = (int64_t)d.n_bands * 32;
+    svi_kernel<<<(int)((threads + block - 1) / block), block, 0, s>>>(d);
+}
+
+}  // namespace lcf

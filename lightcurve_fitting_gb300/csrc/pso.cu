@@ -1,0 +1,669 @@
+// pso.cu — band preparation and the persistent particle-swarm kernel.
+//
+// One warp runs one swarm (a PSO task: band x model x restart, a profile-t0
+// run, or a MultiBazin run); lane p holds particle p (30 of 32 lanes).  The
+// band's observations are staged once per task into the warp's slice of
+// shared memory with a TMA bulk copy and read by all lanes at the same index
+// (broadcast), so the inner loop touches no HBM.
+//
+// The reference updates the global best *inside* its particle loop
+// (pso_minimize, src/parametric.rs:1698-1741): particle p moves towards the
+// global best as left by particles 0..p-1 of the same iteration.  The warp
+// reproduces that order exactly with speculative rounds: all particles move
+// and are evaluated in parallel against the current best; the first lane q
+// whose cost beats the best is accepted together with lanes < q, the best is
+// updated, and lanes > q are moved again from their pre-iteration state.
+// Every iteration therefore costs 1 + (number of global-best improvements)
+// rounds.  The random draws are the reference's own: rand's SmallRng
+// (xoshiro256++) seeded with 42/137/271 produces a stream that does not
+// depend on the data, so the host generates each seed's stream once and the
+// kernel indexes it by (iteration, particle, dimension) — a counter-based
+// view of the reference's sequence.
+#include <cuda_runtime.h>
+
+#include "lcf_internal.cuh"
+#include "models_f32.cuh"
+
+namespace lcf {
+
+#define FULL 0xffffffffu
+
+// ---------------------------------------------------------------------------
+// Band preparation (src/parametric.rs:3581-3630): warp per band.
+// ---------------------------------------------------------------------------
+__global__ void prep_kernel(DeviceBatch d) {
+    int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    int lane = threadIdx.x & 31;
+    if (warp >= d.n_bands) return;
+    int b = warp;
+    int64_t o0 = d.band_off[b], o1 = d.band_off[b + 1];
+    int n = (int)(o1 - o0);
+    BandStats st;
+    st.off = o0;
+    st.n = n;
+    // source of this band and rank by count inside the source (stable)
+    int lo = 0, hi = d.n_sources;
+    while (hi - lo > 1) {
+        int mid = (lo + hi) >> 1;
+        if (d.src_off[mid] <= b) lo = mid; else hi = mid;
+    }
+    int s = lo;
+    st.source = s;
+    // peak flux: fold(f64::MIN, f64::max) (NaN ignored)
+    double peak = -1.7976931348623157e308;
+    double tmin = INFINITY, tmax = -INFINITY;
+    for (int i = lane; i < n; i += 32) {
+        double f = d.flux[o0 + i];
+        peak = fmax(peak, f);
+        double t = d.times[o0 + i];
+        tmin = fmin(tmin, t);
+        tmax = fmax(tmax, t);
+    }
+    for (int k = 16; k; k >>= 1) {
+        peak = fmax(peak, __shfl_xor_sync(FULL, peak, k));
+        tmin = fmin(tmin, __shfl_xor_sync(FULL, tmin, k));
+        tmax = fmax(tmax, __shfl_xor_sync(FULL, tmax, k));
+    }
+    int valid = (n > 0 && peak > 0.0) ? 1 : 0;
+    // rank: bands of the same source with more points, or equal points and a
+    // lower index, come first; invalid bands are not ranked
+    int rank = 0;
+    if (valid) {
+        for (int ob = d.src_off[s] + lane; ob < d.src_off[s + 1]; ob += 32) {
+            if (ob == b) continue;
+            int64_t q0 = d.band_off[ob], q1 = d.band_off[ob + 1];
+            int nb = (int)(q1 - q0);
+            bool v2 = false;
+            if (nb > 0) {
+                double pk = -1.7976931348623157e308;
+                for (int64_t i = q0; i < q1; i++) pk = fmax(pk, d.flux[i]);
+                v2 = pk > 0.0;
+            }
+            if (v2 && (nb > n || (nb == n && ob < b))) rank++;
+        }
+        for (int k = 16; k; k >>= 1) rank += __shfl_xor_sync(FULL, rank, k);
+    }
+    // first maximum of the normalised detections / of all fluxes (original order)
+    double best_det = -INFINITY, best_all = -INFINITY;
+    int idx_det = 0x7fffffff, idx_all = 0x7fffffff;
+    for (int i = lane; i < n; i += 32) {
+        double f = d.flux[o0 + i], e = d.err[o0 + i];
+        double fn = f / peak;
+        bool up = e > 0.0 && (f / e) < 3.0;
+        if (!up && fn > best_det) { best_det = fn; idx_det = i; }
+        if (fn > best_all) { best_all = fn; idx_all = i; }
+    }
+    for (int k = 16; k; k >>= 1) {
+        double bd = __shfl_xor_sync(FULL, best_det, k);
+        int id = __shfl_xor_sync(FULL, idx_det, k);
+        if (bd > best_det || (bd == best_det && id < idx_det)) { best_det = bd; idx_det = id; }
+        double ba = __shfl_xor_sync(FULL, best_all, k);
+        int ia = __shfl_xor_sync(FULL, idx_all, k);
+        if (ba > best_all || (ba == best_all && ia < idx_all)) { best_all = ba; idx_all = ia; }
+    }
+    st.valid = valid;
+    st.rank = valid ? rank : -1;
+    st.peak = peak;
+    st.t_first = tmin;
+    st.t_last = tmax;
+    // peak_time starts at times[0] and is replaced by the first strict maximum
+    st.t_peak = n > 0 ? d.times[o0 + (idx_det == 0x7fffffff ? 0 : idx_det)] : 0.0;
+    st.t_peak_all = n > 0 ? d.times[o0 + (idx_all == 0x7fffffff ? 0 : idx_all)] : 0.0;
+    // stable time order: position of observation i = #{j: t_j < t_i or (t_j == t_i and j < i)}
+    bool sorted = true;
+    for (int i = lane; i + 1 < n; i += 32)
+        if (d.times[o0 + i + 1] < d.times[o0 + i]) sorted = false;
+    sorted = __all_sync(FULL, sorted);
+    for (int i = lane; i < n; i += 32) {
+        double t = d.times[o0 + i];
+        int pos = i;
+        if (!sorted) {
+            pos = 0;
+            for (int j = 0; j < n; j++) {
+                double tj = d.times[o0 + j];
+                pos += (tj < t || (tj == t && j < i)) ? 1 : 0;
+            }
+        }
+        double f = d.flux[o0 + i], e = d.err[o0 + i];
+        double fn = f / peak, fe = e / peak;
+        bool up = e > 0.0 && (f / e) < 3.0;
+        double uf = 3.0 * e / peak;
+        double var = fe * fe + 1e-10;
+        int64_t q = o0 + pos;
+        float th = (float)t;
+        float4 rec;
+        rec.x = th;
+        rec.y = (float)(t - (double)th);
+        rec.z = (float)(up ? uf : fn);
+        rec.w = up ? -(float)var : (float)var;
+        d.obs[q] = rec;
+        d.t64[q] = t;
+        d.f64[q] = fn;
+        d.fe64[q] = fe;
+        d.var64[q] = var;
+        d.uf64[q] = uf;
+        d.up[q] = up ? 1 : 0;
+        d.mag64[q] = -2.5 * log10(f) + 23.9;
+    }
+    if (lane == 0) d.stats[b] = st;
+}
+
+void launch_prep(const DeviceBatch& d, cudaStream_t s) {
+    if (d.n_bands == 0) return;
+    int block = 256;
+    int grid = (int)(((int64_t)d.n_bands * 32 + block - 1) / block);
+    prep_kernel<<<grid, block, 0, s>>>(d);
+}
+
+// ---------------------------------------------------------------------------
+// TMA bulk copy of a band into shared memory (cp.async.bulk + mbarrier)
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ uint32_t smem_u32(const void* p) {
+    return (uint32_t)__cvta_generic_to_shared(p);
+}
+__device__ __forceinline__ void mbar_init(uint64_t* bar) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(bar)));
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+// Issue the copy (one lane).  Sizes and addresses are multiples of 16 bytes.
+__device__ __forceinline__ void bulk_copy_g2s(void* dst, const void* src, uint32_t bytes, uint64_t* bar) {
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes) : "memory");
+    asm volatile(
+        "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(smem_u32(dst)),
+        "l"(src), "r"(bytes), "r"(smem_u32(bar))
+        : "memory");
+}
+// Bounded wait on the barrier phase; returns false if the bound expired.
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t phase) {
+    uint32_t done = 0;
+    for (int it = 0; it < (1 << 24); it++) {
+        asm volatile(
+            "{\n\t.reg .pred p;\n\t"
+            "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+            "selp.u32 %0, 1, 0, p;\n\t}"
+            : "=r"(done)
+            : "r"(smem_u32(bar)), "r"(phase)
+            : "memory");
+        if (done) return true;
+    }
+    return false;
+}
+
+// ---------------------------------------------------------------------------
+// Particle cost (PsoCost::cost_from_slice, src/parametric.rs:1303-1370, and
+// multi_bazin_cost, :973-1004) for the particle of this lane.
+// ---------------------------------------------------------------------------
+struct TaskCtx {
+    int kind, model, np, D, t0i, flags, n;
+    float t0_fixed;
+    float t_last;
+    const float4* obs;
+    float* mscratch;     // MetzgerKN scratch of this warp ([n][32])
+    double prior_n;      // n as double (max(n, 1))
+};
+
+template <class M>
+__device__ __forceinline__ Nll nll_loop(const M& m, const float4* obs, int n, float se2) {
+    Nll acc;
+    acc.reset();
+#pragma unroll 2
+    for (int i = 0; i < n; i++) {
+        float4 o = obs[i];
+        int st = ST_OK;
+        float pr = m.eval(o.x, o.y, st);
+        acc.obs(o, pr, st, se2);
+    }
+    return acc;
+}
+
+// MultiBazin prediction: sum of K Bazin components + B (src/parametric.rs:932-940)
+template <int K>
+__device__ __forceinline__ Nll nll_multibazin(const float* p, const float4* obs, int n, float se2) {
+    float a[K], la[K], t0[K], itr[K], itf[K];
+#pragma unroll
+    for (int c = 0; c < K; c++) {
+        la[c] = p[4 * c];
+        a[c] = expf(la[c]);
+        t0[c] = p[4 * c + 1];
+        itr[c] = expf(-p[4 * c + 2]);
+        itf[c] = expf(-p[4 * c + 3]);
+    }
+    float B = p[4 * K];
+    Nll acc;
+    acc.reset();
+    for (int i = 0; i < n; i++) {
+        float4 o = obs[i];
+        float sum = 0.0f, bigL = -INFINITY;
+        int st = ST_OK;
+#pragma unroll
+        for (int c = 0; c < K; c++) {
+            float dt = (o.x - t0[c]) + o.y;
+            float xf = -dt * itf[c], xr = -dt * itr[c];
+            if (xf < 80.0f && xr < 80.0f) {
+                sum += a[c] * expf(xf) / (1.0f + expf(xr));
+            } else if (xf > LN_DBL_MAX || la[c] + xf > LN_DBL_MAX) {
+                st = ST_NONFINITE;
+            } else if (xr <= LN_DBL_MAX) {
+                float L = la[c] + xf - softplus_f(xr);
+                if (L > BIG_L) bigL = fmaxf(bigL, L) + log1pf(expf(-fabsf(bigL - L)));
+                else sum += expf(L);
+            }
+        }
+        float pr = 0.0f;
+        if (st == ST_OK && bigL > -INFINITY) {
+            // FP64 sum overflows to +inf past ln DBL_MAX: non-finite prediction
+            if (bigL > LN_DBL_MAX) st = ST_NONFINITE;
+            else { st = ST_BIG; pr = bigL; }
+        } else {
+            pr = sum + B;
+        }
+        acc.obs(o, pr, st, se2);
+    }
+    return acc;
+}
+
+__device__ double particle_cost(const TaskCtx& t, const float* x) {
+    // rebuild the full parameter vector
+    float p[MB_MAXP];
+    if (t.flags & TASK_T0_FIXED) {
+        int fi = 0;
+        for (int i = 0; i < t.D; i++) {
+            if (i == t.t0i) p[fi++] = t.t0_fixed;
+            p[fi++] = x[i];
+        }
+        if (t.t0i >= t.D) p[fi] = t.t0_fixed;
+    } else {
+        for (int i = 0; i < t.D; i++) p[i] = x[i];
+    }
+    double n = t.prior_n;
+    if (t.kind >= KIND_MB1) {
+        int K = t.kind - KIND_MB1 + 1;
+        float se = expf(p[4 * K + 1]);
+        float se2 = se * se;
+        Nll acc;
+        switch (K) {
+            case 1: acc = nll_multibazin<1>(p, t.obs, t.n, se2); break;
+            case 2: acc = nll_multibazin<2>(p, t.obs, t.n, se2); break;
+            case 3: acc = nll_multibazin<3>(p, t.obs, t.n, se2); break;
+            default: acc = nll_multibazin<4>(p, t.obs, t.n, se2); break;
+        }
+        return acc.finish(0.0, n);
+    }
+    int m = t.model;
+    if (m == VILLAR) {
+        float c = VillarF::constraint(p);
+        if (c > 0.0f) return 1e12 + 10000.0 * (double)c;
+    }
+    double prior = 0.0;
+    if (t.flags & TASK_PRIOR) {
+        float s = 0.0f;
+        for (int j = 0; j < t.np; j++) {
+            float w = (float)c_pop_w[m][j];
+            if (w > 0.0f) {
+                float z = (p[j] - (float)c_pop_c[m][j]) / w;
+                s += 0.5f * z * z;
+            }
+        }
+        prior = (double)s;
+    }
+    float se = expf(p[se_idx_of(m)]);
+    float se2 = se * se;
+    Nll acc;
+    switch (m) {
+        case BAZIN: { BazinF e; e.init(p); acc = nll_loop(e, t.obs, t.n, se2); break; }
+        case VILLAR: { VillarF e; e.init(p); acc = nll_loop(e, t.obs, t.n, se2); break; }
+        case TDE: { TdeF e; e.init(p); acc = nll_loop(e, t.obs, t.n, se2); break; }
+        case ARNETT: { ArnettF e; e.init(p); acc = nll_loop(e, t.obs, t.n, se2); break; }
+        case MAGNETAR: { MagnetarF e; e.init(p); acc = nll_loop(e, t.obs, t.n, se2); break; }
+        case SHOCK: { ShockF e; e.init(p); acc = nll_loop(e, t.obs, t.n, se2); break; }
+        case AFTERGLOW: { AfterglowF e; e.init(p); acc = nll_loop(e, t.obs, t.n, se2); break; }
+        default: {
+            // MetzgerKN: ODE sweep -> unnormalised interpolants in scratch
+            struct ObsT {
+                const float4* o;
+                __device__ float t(int j) const { return o[j].x + o[j].y; }
+            } ot{t.obs};
+            int lane = threadIdx.x & 31;
+            float* lv = t.mscratch + lane;
+            float l_peak = 0.0f;
+            bool ok = MetzgerF::sweep(p, t.t_last, ot, t.n, lv, 32, l_peak, nullptr);
+            acc.reset();
+            float scale = 1.0f;
+            if (ok) {
+                float inv = 1.0f / l_peak;
+                float mx = -INFINITY;
+                for (int j = 0; j < t.n; j++)
+                    if (t.obs[j].w >= 0.0f) mx = fmaxf(mx, lv[j * 32] * inv);
+                scale = inv;
+                if (mx > 1e-10f && isfinite(mx)) scale = inv * fminf(fmaxf(1.0f / mx, 0.1f), 10.0f);
+            }
+            for (int j = 0; j < t.n; j++) {
+                float4 o = t.obs[j];
+                float pr = ok ? lv[j * 32] * scale : 0.0f;
+                acc.obs(o, pr, ST_OK, se2);
+            }
+            break;
+        }
+    }
+    return acc.finish(prior, n);
+}
+
+// ---------------------------------------------------------------------------
+// The PSO kernel
+// ---------------------------------------------------------------------------
+struct WarpSmem {
+    uint64_t bar;
+    uint64_t pad;
+};
+
+template <int MAXD>
+__global__ void __launch_bounds__(256) pso_kernel(DeviceBatch d, int slot, int n_host, int smem_obs) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const int lane = threadIdx.x & 31;
+    const int warp = threadIdx.x >> 5;
+    const int nwarps = blockDim.x >> 5;
+    float4* sobs = reinterpret_cast<float4*>(smem_raw) + (size_t)warp * smem_obs;
+    WarpSmem* ws = reinterpret_cast<WarpSmem*>(reinterpret_cast<float4*>(smem_raw) + (size_t)nwarps * smem_obs) + warp;
+    if (lane == 0) mbar_init(&ws->bar);
+    __syncwarp();
+    uint32_t phase = 0;
+    const int n_tasks = n_host >= 0 ? n_host : d.ctr->task_count[slot];
+    const int gwarp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+
+    while (true) {
+        int ti = 0;
+        if (lane == 0) ti = atomicAdd(&d.ctr->task_head[slot], 1);
+        ti = __shfl_sync(FULL, ti, 0);
+        if (ti >= n_tasks) break;
+        const PsoTask task = d.tasks[slot][ti];
+        const BandStats bs = d.stats[task.band];
+        // tasks of bands the reference does not fit (or MultiBazin tasks of
+        // bands that are not their source's rank-0 band with n >= 5) are no-ops
+        if (!bs.valid || ((task.flags & TASK_RANK0) && (bs.rank != 0 || bs.n < 5))) continue;
+        TaskCtx t;
+        t.kind = task.kind;
+        t.flags = task.flags;
+        t.n = bs.n;
+        t.prior_n = (double)max(bs.n, 1);
+        t.t_last = (float)bs.t_last;
+        t.t0_fixed = (float)task.t0_fixed;
+        // stage the band
+        const float4* gobs = d.obs + bs.off;
+        if (bs.n <= smem_obs && bs.n > 0) {
+            __syncwarp();
+            if (lane == 0) bulk_copy_g2s(sobs, gobs, (uint32_t)bs.n * 16u, &ws->bar);
+            bool ok = mbar_wait(&ws->bar, phase);
+            __syncwarp();
+            phase ^= 1u;
+            if (!ok) {
+                if (lane == 0) atomicCAS(&d.ctr->error, 0, LCF_E_TIMEOUT);
+                t.obs = gobs;
+            } else {
+                t.obs = sobs;
+            }
+        } else {
+            t.obs = gobs;
+        }
+        // dimensions and bounds
+        float lo[MAXD], hi[MAXD], seedp[MAXD];
+        bool seeded = (task.flags & TASK_SEEDED) != 0;
+        if (t.kind < KIND_MB1) {
+            int m = t.kind;
+            t.model = m;
+            t.np = n_params_of(m);
+            t.t0i = t0_idx_of(m);
+            double dlo[MAXP], dhi[MAXP];
+            for (int j = 0; j < MAXP; j++) { dlo[j] = c_lo[m][j]; dhi[j] = c_hi[m][j]; }
+            if (task.flags & TASK_T0_BOUNDS) {
+                // data-informed t0 bounds, src/parametric.rs:1881-1909
+                double t0_lo = fmax(bs.t_first - 30.0, dlo[t.t0i]);
+                double t0_hi = fmin(bs.t_peak + 10.0, dhi[t.t0i]);
+                if (t0_lo < t0_hi) { dlo[t.t0i] = t0_lo; dhi[t.t0i] = t0_hi; }
+            }
+            if (task.flags & TASK_T0_FIXED) {
+                t.D = t.np - 1;
+                int k = 0;
+                for (int j = 0; j < t.np; j++) {
+                    if (j == t.t0i) continue;
+                    if (k < MAXD) { lo[k] = (float)dlo[j]; hi[k] = (float)dhi[j]; }
+                    k++;
+                }
+            } else {
+                t.D = t.np;
+                for (int j = 0; j < t.np && j < MAXD; j++) { lo[j] = (float)dlo[j]; hi[j] = (float)dhi[j]; }
+            }
+            if (seeded) {
+                // seed particles of pso_fit_single_model, src/parametric.rs:1924-1964
+                for (int j = 0; j < t.np && j < MAXD; j++) {
+                    double c = c_pop_c[m][j];
+                    double v = fmin(fmax(c, dlo[j]), dhi[j]);
+                    seedp[j] = (float)v;
+                }
+                double t0s = task.restart == 1 ? bs.t_peak - 5.0 : bs.t_first - 15.0;
+                if (t.t0i < MAXD) seedp[t.t0i] = (float)fmin(fmax(t0s, dlo[t.t0i]), dhi[t.t0i]);
+            }
+        } else {
+            int K = t.kind - KIND_MB1 + 1;
+            t.model = BAZIN;
+            t.np = 4 * K + 2;
+            t.D = t.np;
+            t.t0i = -1;
+            // multi_bazin_bounds, src/parametric.rs:958-970
+            for (int c = 0; c < K && 4 * c + 3 < MAXD; c++) {
+                lo[4 * c] = -3.0f; hi[4 * c] = 3.0f;
+                lo[4 * c + 1] = (float)(bs.t_first - 30.0); hi[4 * c + 1] = (float)(bs.t_last + 30.0);
+                lo[4 * c + 2] = -2.0f; hi[4 * c + 2] = 5.0f;
+                lo[4 * c + 3] = -2.0f; hi[4 * c + 3] = 6.0f;
+            }
+            if (4 * K + 1 < MAXD) {
+                lo[4 * K] = -0.3f; hi[4 * K] = 0.3f;
+                lo[4 * K + 1] = -5.0f; hi[4 * K + 1] = 0.0f;
+            }
+            if (seeded && task.aux >= 0) {
+                const double* sp = d.mb[task.aux].seed;
+                for (int j = 0; j < t.np && j < MAXD; j++) seedp[j] = (float)sp[j];
+            }
+        }
+        const int D = t.D;
+        float vmax[MAXD];
+#pragma unroll
+        for (int j = 0; j < MAXD; j++) vmax[j] = j < D ? 0.5f * (hi[j] - lo[j]) : 0.0f;
+        t.mscratch = d.scratch + (size_t)gwarp * (size_t)d.scratch_per_warp;
+        const float* dr = d.draws + (size_t)task.restart * DRAWS_PER_SEED;
+        const int p = lane;
+        const bool live = p < NP;
+        // ---- initialisation (src/parametric.rs:1677-1692, seeded :1189-1210)
+        float x[MAXD], v[MAXD], pb[MAXD], g[MAXD];
+        int base;
+        if (seeded) {
+            if (p == 0) {
+#pragma unroll
+                for (int j = 0; j < MAXD; j++) {
+                    if (j < D) { x[j] = seedp[j]; v[j] = vmax[j] * 0.2f * (2.0f * dr[j] - 1.0f); }
+                }
+            } else if (live) {
+                int o = D + 2 * D * (p - 1);
+#pragma unroll
+                for (int j = 0; j < MAXD; j++) {
+                    if (j < D) {
+                        x[j] = lo[j] + dr[o + j] * (hi[j] - lo[j]);
+                        v[j] = vmax[j] * 0.2f * (2.0f * dr[o + D + j] - 1.0f);
+                    }
+                }
+            }
+            base = 2 * D * NP - D;
+        } else {
+            if (live) {
+                int o = 2 * D * p;
+#pragma unroll
+                for (int j = 0; j < MAXD; j++) {
+                    if (j < D) {
+                        x[j] = lo[j] + dr[o + 2 * j] * (hi[j] - lo[j]);
+                        v[j] = vmax[j] * 0.2f * (2.0f * dr[o + 2 * j + 1] - 1.0f);
+                    }
+                }
+            }
+            base = 2 * D * NP;
+        }
+#pragma unroll
+        for (int j = 0; j < MAXD; j++) {
+            if (!live || j >= D) { x[j] = 0.0f; v[j] = 0.0f; }
+            pb[j] = x[j];
+            g[j] = 0.0f;
+        }
+        double c = live ? particle_cost(t, x) : INFINITY;
+        int evals = 1;
+        double pbc = c;
+        double gc = INFINITY;
+        {
+            // global best after the sequential initial loop: first strict minimum
+            double mn = c;
+            for (int k = 16; k; k >>= 1) mn = fmin(mn, __shfl_xor_sync(FULL, mn, k));
+            unsigned m = __ballot_sync(FULL, live && c == mn && mn < INFINITY);
+            if (m) {
+                int q = __ffs(m) - 1;
+                gc = mn;
+#pragma unroll
+                for (int j = 0; j < MAXD; j++) g[j] = __shfl_sync(FULL, x[j], q);
+            }
+        }
+        // ---- iterations
+        int stall = 0;
+        double prev = gc;
+        const double inv_iters = 1.0 / (double)MAX_ITERS;
+        int it = 0;
+        for (; it < MAX_ITERS; it++) {
+            const float w = (float)(0.9 - (0.9 - 0.4) * (double)it * inv_iters);
+            float x0[MAXD], v0[MAXD];
+#pragma unroll
+            for (int j = 0; j < MAXD; j++) { x0[j] = x[j]; v0[j] = v[j]; }
+            const float* r = dr + base + it * 2 * D * NP + 2 * D * p;
+            int start = 0;
+            while (start < NP) {
+                bool active = live && p >= start;
+                if (active) {
+#pragma unroll
+                    for (int j = 0; j < MAXD; j++) {
+                        if (j < D) {
+                            float r1 = r[2 * j], r2 = r[2 * j + 1];
+                            float vv = w * v0[j] + 1.5f * r1 * (pb[j] - x0[j]) + 1.5f * r2 * (g[j] - x0[j]);
+                            vv = fminf(fmaxf(vv, -vmax[j]), vmax[j]);
+                            float nx = x0[j] + vv;
+                            if (nx <= lo[j]) { x[j] = lo[j]; v[j] = 0.0f; }
+                            else if (nx >= hi[j]) { x[j] = hi[j]; v[j] = 0.0f; }
+                            else { x[j] = nx; v[j] = vv; }
+                        }
+                    }
+                    c = particle_cost(t, x);
+                    evals++;
+                }
+                unsigned m = __ballot_sync(FULL, active && c < gc);
+                int q = m ? __ffs(m) - 1 : NP - 1;
+                bool acc = live && p >= start && p <= q;
+                if (acc && c < pbc) {
+                    pbc = c;
+#pragma unroll
+                    for (int j = 0; j < MAXD; j++) pb[j] = x[j];
+                }
+                if (m) {
+                    gc = __shfl_sync(FULL, c, q);
+#pragma unroll
+                    for (int j = 0; j < MAXD; j++) g[j] = __shfl_sync(FULL, x[j], q);
+                }
+                start = q + 1;
+            }
+            bool improved = prev - gc > 0.01 * fmax(fabs(prev), 1e-10);
+            if (improved) {
+                stall = 0;
+                prev = gc;
+            } else if (++stall >= STALL_ITERS) {
+                it++;
+                break;
+            }
+        }
+        // ---- result
+        int tot_evals = live ? evals : 0;
+        for (int k = 16; k; k >>= 1) tot_evals += __shfl_xor_sync(FULL, tot_evals, k);
+        if (lane == 0) {
+            PsoResult& R = d.pso_res[task.out];
+            R.cost = gc;
+            R.iters = it;
+            R.evals = tot_evals;
+            for (int j = 0; j < MB_MAXP; j++) R.params[j] = 0.0f;
+#pragma unroll
+            for (int j = 0; j < MAXD; j++)
+                if (j < D) R.params[j] = g[j];
+            atomicAdd(&d.ctr->particle_obs_evals, (unsigned long long)tot_evals * (unsigned long long)bs.n);
+            if (t.kind == METZGER) atomicAdd(&d.ctr->ode_steps, (unsigned long long)tot_evals * MetzgerF::NG);
+        }
+        __syncwarp();
+    }
+}
+
+// Batched likelihood of parameter vectors on one band, through the same
+// per-lane cost function the PSO kernel uses (lane = parameter vector).
+__global__ void band_cost_kernel(int model, const float4* obs, int n, float t_last, const double* params, int n_eval,
+                                 int with_prior, double* costs, float* scratch) {
+    int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    int lane = threadIdx.x & 31;
+    int e = warp * 32 + lane;
+    if (warp * 32 >= n_eval) return;
+    TaskCtx t;
+    t.kind = model;
+    t.model = model;
+    t.np = n_params_of(model);
+    t.D = t.np;
+    t.t0i = t0_idx_of(model);
+    t.flags = with_prior ? TASK_PRIOR : 0;
+    t.n = n;
+    t.t0_fixed = 0.0f;
+    t.t_last = t_last;
+    t.obs = obs;
+    t.mscratch = scratch + (size_t)warp * 32 * (size_t)max(n, 1);
+    t.prior_n = (double)max(n, 1);
+    float x[MAXP];
+    for (int j = 0; j < MAXP; j++) x[j] = (e < n_eval && j < t.np) ? (float)params[(size_t)e * t.np + j] : 0.0f;
+    double c = particle_cost(t, x);
+    if (e < n_eval) costs[e] = c;
+}
+
+void launch_band_cost(int model, const float4* obs, int n, float t_last, const double* params, int n_eval,
+                      int with_prior, double* costs, float* scratch, cudaStream_t s) {
+    if (n_eval <= 0) return;
+    int warps = (n_eval + 31) / 32;
+    band_cost_kernel<<<(warps * 32 + 127) / 128, 128, 0, s>>>(model, obs, n, t_last, params, n_eval, with_prior,
+                                                              costs, scratch);
+}
+
+size_t pso_smem_bytes(int block, int smem_obs) {
+    return (size_t)(block / 32) * ((size_t)smem_obs * sizeof(float4) + sizeof(WarpSmem));
+}
+
+int pso_init_attributes(int block, int smem_obs) {
+    int smem = (int)pso_smem_bytes(block, smem_obs);
+    cudaError_t e = cudaSuccess;
+    e = cudaFuncSetAttribute(pso_kernel<7>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    if (e == cudaSuccess) e = cudaFuncSetAttribute(pso_kernel<10>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    if (e == cudaSuccess) e = cudaFuncSetAttribute(pso_kernel<14>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    if (e == cudaSuccess) e = cudaFuncSetAttribute(pso_kernel<18>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    return (int)e;
+}
+
+int pso_blocks_per_sm(int block, size_t smem) {
+    int n = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, pso_kernel<7>, block, smem) != cudaSuccess) return 1;
+    return n;
+}
+
+void launch_pso(const DeviceBatch& d, int slot, int n_host, int max_dim, int grid, int block, cudaStream_t s) {
+    if (n_host == 0) return;
+    int smem_obs = d.smem_obs;
+    size_t smem = pso_smem_bytes(block, smem_obs);
+    if (max_dim <= 7) pso_kernel<7><<<grid, block, smem, s>>>(d, slot, n_host, smem_obs);
+    else if (max_dim <= 10) pso_kernel<10><<<grid, block, smem, s>>>(d, slot, n_host, smem_obs);
+    else if (max_dim <= 14) pso_kernel<14><<<grid, block, smem, s>>>(d, slot, n_host, smem_obs);
+    else pso_kernel<18><<<grid, block, smem, s>>>(d, slot, n_host, smem_obs);
+}
+
+}  // namespace lcf

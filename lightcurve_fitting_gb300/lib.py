@@ -1,0 +1,155 @@
+"""ctypes binding of liblcf_gb300.so (the C ABI of include/lcf.h).
+
+The library is built in-tree by ``lightcurve_fitting_gb300.build``.  There is
+no fallback: if the shared library is missing or no CUDA device is visible,
+``Context`` raises.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+from . import abi
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "liblcf_gb300.so")
+
+_lib = None
+
+
+class LcfError(RuntimeError):
+    pass
+
+
+def load(path: str = LIB_PATH):
+    """Load the shared library (raises if it has not been built)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(path):
+        raise LcfError(f"{path} is missing: build it with `python -m lightcurve_fitting_gb300.build` "
+                       "(or __graft_entry__.build())")
+    L = C.CDLL(path)
+    vp, i, d = C.c_void_p, C.c_int, C.c_double
+    L.lcf_ctx_create.argtypes = [i, C.POINTER(vp)]
+    L.lcf_ctx_destroy.argtypes = [vp]
+    L.lcf_last_error.argtypes = [vp]
+    L.lcf_last_error.restype = C.c_char_p
+    L.lcf_last_stats.argtypes = [vp, C.POINTER(abi.FitStats)]
+    L.lcf_fit_parametric_batch.argtypes = [vp, C.POINTER(abi.BandsCSR), C.POINTER(abi.FitOptions),
+                                           C.POINTER(abi.FitOutputs)]
+    L.lcf_fit_parametric_device.argtypes = [vp, C.POINTER(abi.BandsCSR), C.POINTER(abi.FitOptions)]
+    L.lcf_download_outputs.argtypes = [vp, C.POINTER(abi.FitOutputs)]
+    L.lcf_ctx_stream.argtypes = [vp]
+    L.lcf_ctx_stream.restype = vp
+    L.lcf_set_graph.argtypes = [vp, i]
+    L.lcf_band_cost.argtypes = [vp, i, vp, vp, vp, vp, vp, i, vp, i, i, vp]
+    for name in ["launch_bazin", "launch_villar", "launch_tde", "launch_arnett", "launch_magnetar",
+                 "launch_shock_cooling", "launch_afterglow", "launch_metzger_kn"]:
+        getattr(L, name).argtypes = [vp, vp, vp, i, i, i, i, i]
+        getattr(L, name).restype = None
+    L.launch_batch_pso_cost.argtypes = [vp, vp, vp, vp, vp, vp, vp, vp, i, i, i, i, i, i]
+    L.launch_batch_pso_cost.restype = None
+    _lib = L
+    return L
+
+
+EVAL_EXPORTS = ["launch_bazin", "launch_villar", "launch_tde", "launch_arnett", "launch_magnetar",
+                "launch_shock_cooling", "launch_afterglow", "launch_metzger_kn"]
+
+
+class Context:
+    """A GPU context: one CUDA stream, device buffers and a captured graph."""
+
+    def __init__(self, device: int = 0):
+        self.L = load()
+        h = C.c_void_p()
+        rc = self.L.lcf_ctx_create(int(device), C.byref(h))
+        if rc != 0:
+            raise LcfError(f"lcf_ctx_create({device}) failed with status {rc} (no CUDA device?)")
+        self.h = h
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.L.lcf_ctx_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _check(self, rc: int, what: str):
+        if rc != 0:
+            msg = self.L.lcf_last_error(self.h).decode(errors="replace")
+            raise LcfError(f"{what} failed with status {rc}: {msg}")
+
+    @property
+    def stream(self) -> int:
+        return int(self.L.lcf_ctx_stream(self.h) or 0)
+
+    def set_graph(self, enabled: bool):
+        self._check(self.L.lcf_set_graph(self.h, int(bool(enabled))), "lcf_set_graph")
+
+    def fit_batch(self, batch, fit_all_models=True, method=abi.METHOD_SVI, forced_model=-1,
+                  run_multi_bazin=True) -> abi.FitResult:
+        """lcf_fit_parametric_batch over a PhotometryBatch (host arrays)."""
+        keep = []
+        csr = abi.csr_struct(batch, keep)
+        opts = abi.options(fit_all_models, method, forced_model, run_multi_bazin)
+        res = abi.FitResult(batch.n_bands)
+        outs = res.as_struct()
+        self._check(self.L.lcf_fit_parametric_batch(self.h, C.byref(csr), C.byref(opts), C.byref(outs)),
+                    "lcf_fit_parametric_batch")
+        return res
+
+    def fit_device(self, dev_ptrs: dict, n_sources: int, n_bands: int, fit_all_models=True,
+                   method=abi.METHOD_SVI, forced_model=-1, run_multi_bazin=True):
+        """lcf_fit_parametric_device over device pointers (keys: times, flux,
+        flux_err, band_obs_offsets, source_band_offsets)."""
+        csr = abi.BandsCSR()
+        csr.n_sources, csr.n_bands = n_sources, n_bands
+        csr.source_band_offsets = dev_ptrs["source_band_offsets"]
+        csr.band_obs_offsets = dev_ptrs["band_obs_offsets"]
+        csr.times, csr.flux, csr.flux_err = dev_ptrs["times"], dev_ptrs["flux"], dev_ptrs["flux_err"]
+        opts = abi.options(fit_all_models, method, forced_model, run_multi_bazin)
+        self._check(self.L.lcf_fit_parametric_device(self.h, C.byref(csr), C.byref(opts)),
+                    "lcf_fit_parametric_device")
+
+    def download(self, n_bands: int) -> abi.FitResult:
+        res = abi.FitResult(n_bands)
+        outs = res.as_struct()
+        self._check(self.L.lcf_download_outputs(self.h, C.byref(outs)), "lcf_download_outputs")
+        return res
+
+    def stats(self) -> dict:
+        s = abi.FitStats()
+        self._check(self.L.lcf_last_stats(self.h, C.byref(s)), "lcf_last_stats")
+        return {k: getattr(s, k) for k, _ in abi.FitStats._fields_}
+
+    def band_cost(self, model: int, times, flux, obs_var, is_upper, upper_flux, params, with_prior=True):
+        """PsoCost::cost_from_slice for each row of ``params`` (FP32 kernel)."""
+        t = np.ascontiguousarray(times, np.float64)
+        f = np.ascontiguousarray(flux, np.float64)
+        v = np.ascontiguousarray(obs_var, np.float64)
+        u = np.ascontiguousarray(is_upper, np.uint8)
+        uf = np.ascontiguousarray(upper_flux, np.float64)
+        p = np.ascontiguousarray(np.atleast_2d(params), np.float64)
+        out = np.zeros(p.shape[0])
+        self._check(self.L.lcf_band_cost(self.h, int(model), t.ctypes.data, f.ctypes.data, v.ctypes.data,
+                                         u.ctypes.data, uf.ctypes.data, t.size, p.ctypes.data, p.shape[0],
+                                         int(bool(with_prior)), out.ctypes.data), "lcf_band_cost")
+        return out
+
+
+_default = None
+
+
+def default_context() -> Context:
+    global _default
+    if _default is None:
+        _default = Context(0)
+    return _default

@@ -1,0 +1,171 @@
+"""Python mirror of the reference's parametric API on the GB300 kernels.
+
+Names, arguments and return values follow the reference's Python binding
+(python/src/lib.rs:203-245) and its Rust API (src/parametric.rs:3563-3761):
+results are lists of dicts with the fields of ``ParametricBandResult``
+(src/parametric.rs:3049-3072), ``None`` where the reference has ``None``.
+
+Every call runs on the GPU through liblcf_gb300.so; there is no CPU path.
+The joint multi-band Villar branch of ``fit_parametric`` (taken by the
+reference for >= 2 bands with ``fit_all_models=False``,
+src/parametric.rs:3750-3757) is not built yet and raises NotImplementedError.
+"""
+from __future__ import annotations
+
+import math
+from typing import Dict, List, Sequence
+
+import numpy as np
+
+from . import abi
+from .lib import default_context
+from .synth import PhotometryBatch
+
+FACTOR = 1.0857362047581294
+
+
+def _method(method: str) -> int:
+    m = method.lower() if isinstance(method, str) else method
+    if m == "svi":
+        return abi.METHOD_SVI
+    if m == "laplace":
+        return abi.METHOD_LAPLACE
+    raise ValueError(f"Unknown uncertainty method '{method}'. Expected 'svi' or 'laplace'.")
+
+
+def _model_id(name: str) -> int:
+    table = {"bazin": 0, "villar": 1, "tde": 2, "arnett": 3, "magnetar": 4, "shockcooling": 5,
+             "afterglow": 6, "metzgerkn": 7}
+    key = name.lower()
+    if key not in table:
+        raise ValueError(f"Unknown model '{name}'. Expected one of: Bazin, Villar, Tde, Arnett, Magnetar, "
+                         "ShockCooling, Afterglow, MetzgerKN.")
+    return table[key]
+
+
+def build_flux_bands(times, mags, mag_errs, bands) -> Dict[str, dict]:
+    """build_flux_bands (src/common.rs:79-111): group by band, times relative to
+    the earliest time, mag -> flux with ZP 23.9, drop non-finite or <= 0."""
+    times = np.asarray(times, np.float64)
+    if times.size == 0:
+        return {}
+    jd_min = times.min()
+    out: Dict[str, dict] = {}
+    for t, m, e, b in zip(times, mags, mag_errs, bands):
+        flux = 10.0 ** (-0.4 * (m - 23.9))
+        ferr = e / FACTOR * flux
+        if not (math.isfinite(flux) and math.isfinite(ferr)) or flux <= 0 or ferr <= 0:
+            continue
+        d = out.setdefault(b, {"times": [], "values": [], "errors": []})
+        d["times"].append(t - jd_min)
+        d["values"].append(flux)
+        d["errors"].append(ferr)
+    return out
+
+
+def _batch_from_sources(sources: Sequence[Dict[str, dict]]):
+    t, f, e, bo, so, names = [], [], [], [0], [0], []
+    for bands in sources:
+        keys = list(bands.keys())
+        names.append(keys)
+        for k in keys:
+            bd = bands[k]
+            tt = np.asarray(bd["times"], np.float64)
+            t.append(tt)
+            f.append(np.asarray(bd["values"], np.float64))
+            e.append(np.asarray(bd["errors"], np.float64))
+            bo.append(bo[-1] + tt.size)
+        so.append(so[-1] + len(keys))
+    cat = lambda xs: np.concatenate(xs) if xs else np.zeros(0)
+    batch = PhotometryBatch(cat(t), cat(f), cat(e), np.asarray(bo, np.int64), np.asarray(so, np.int32),
+                            np.zeros(len(sources), np.int32), "api")
+    return batch, names
+
+
+def _opt(v: float):
+    return None if v is None or not math.isfinite(v) else float(v)
+
+
+def results_from_fit(res: abi.FitResult, batch: PhotometryBatch, names, fit_all_models: bool, method: int,
+                     forced_model: int) -> List[List[dict]]:
+    """Per source: the list of ParametricBandResult dicts in the reference's
+    band order (descending observation count)."""
+    out = []
+    for s in range(batch.n_sources):
+        b0, b1 = int(batch.source_band_offsets[s]), int(batch.source_band_offsets[s + 1])
+        rows = []
+        for b in range(b0, b1):
+            if res.model[b] < 0:
+                continue
+            m = int(res.model[b])
+            np_ = abi.N_PARAMS[m]
+            if forced_model >= 0:
+                chi2 = {abi.MODEL_NAMES[forced_model]: _opt(res.per_model_chi2[b, forced_model])}
+            else:
+                chi2 = {abi.MODEL_NAMES[k]: _opt(res.per_model_chi2[b, k]) for k in range(8)}
+            per_params = {}
+            if fit_all_models:
+                for k in range(8):
+                    row = res.per_model_params[b, k, :abi.N_PARAMS[k]]
+                    if not np.all(np.isnan(row)):
+                        per_params[abi.MODEL_NAMES[k]] = [float(x) for x in row]
+            r = {
+                "band": names[s][b - b0],
+                "model": abi.MODEL_NAMES[m],
+                "pso_params": [float(x) for x in res.pso_params[b, :np_]],
+                "pso_chi2": _opt(res.pso_chi2[b]),
+                "svi_mu": [float(x) for x in res.svi_mu[b, :np_]],
+                "svi_log_sigma": [float(x) for x in res.svi_log_sigma[b, :np_]],
+                "svi_elbo": _opt(res.svi_elbo[b]),
+                "n_obs": int(res.n_obs[b]),
+                "mag_chi2": _opt(res.mag_chi2[b]),
+                "per_model_chi2": chi2,
+                "uncertainty_method": "Svi" if method == abi.METHOD_SVI else "Laplace",
+            }
+            if per_params:
+                r["per_model_params"] = per_params
+            if res.mb_best_k[b] > 0:
+                k = int(res.mb_best_k[b])
+                r["multi_bazin"] = {
+                    "best_k": k,
+                    "params": [float(x) for x in res.mb_params[b, :4 * k + 2]],
+                    "cost": float(res.mb_cost[b]),
+                    "bic": float(res.mb_bic[b]),
+                    "per_k_cost": [float(x) for x in res.mb_per_k_cost[b]],
+                    "per_k_bic": [float(x) for x in res.mb_per_k_bic[b]],
+                }
+            rows.append((int(res.rank[b]), r))
+        rows.sort(key=lambda x: x[0])
+        out.append([r for _, r in rows])
+    return out
+
+
+def fit_batch_parametric(sources: Sequence[Dict[str, dict]], fit_all_models: bool = False, method: str = "svi",
+                         model: str | None = None, ctx=None) -> List[List[dict]]:
+    """fit_batch_parametric (src/batch.rs:39-48) of the per-band model
+    selection path: one list of band results per source, all sources in one
+    GPU batch."""
+    meth = _method(method)
+    forced = -1 if model is None else _model_id(model)
+    if forced < 0 and not fit_all_models:
+        for bands in sources:
+            if sum(1 for b in bands.values() if len(b["values"]) > 0) >= 2:
+                raise NotImplementedError(
+                    "fit_parametric with fit_all_models=False and >= 2 bands takes the reference's joint "
+                    "multi-band Villar branch, which this library does not implement yet")
+    batch, names = _batch_from_sources(sources)
+    ctx = ctx or default_context()
+    res = ctx.fit_batch(batch, fit_all_models=fit_all_models, method=meth, forced_model=forced,
+                        run_multi_bazin=True)
+    return results_from_fit(res, batch, names, fit_all_models, meth, forced)
+
+
+def fit_parametric(bands: Dict[str, dict], fit_all_models: bool = False, method: str = "svi", ctx=None):
+    """fit_parametric (src/parametric.rs:3742-3761, python/src/lib.rs:203-215)."""
+    return fit_batch_parametric([bands], fit_all_models, method, None, ctx)[0]
+
+
+def fit_parametric_model(bands: Dict[str, dict], model: str, fit_all_models: bool = False, method: str = "svi",
+                         ctx=None):
+    """fit_parametric_model with a forced model (python/src/lib.rs:219-245)."""
+    return fit_batch_parametric([bands], fit_all_models, method, model, ctx)[0]

@@ -1,0 +1,67 @@
+"""CPU tests of the C ABI: the shared library builds for sm_103a, loads, and
+exports every function include/lcf.h declares (no GPU call is made)."""
+import ctypes
+import os
+import re
+
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def declared_functions():
+    src = open(os.path.join(ROOT, "include", "lcf.h")).read()
+    src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+    names = re.findall(r"^\s*(?:int|void|const char\*|void\*)\s+\**(\w+)\s*\(", src, flags=re.M)
+    return sorted(set(names))
+
+
+@pytest.fixture(scope="session")
+def libpath():
+    from lightcurve_fitting_gb300 import build
+    return build.build()
+
+
+def test_header_declares_the_reference_exports():
+    names = declared_functions()
+    for n in ["launch_bazin", "launch_villar", "launch_tde", "launch_arnett", "launch_magnetar",
+              "launch_shock_cooling", "launch_afterglow", "launch_metzger_kn", "launch_batch_pso_cost",
+              "lcf_ctx_create", "lcf_fit_parametric_batch", "lcf_band_cost"]:
+        assert n in names
+
+
+def test_library_exports_every_declared_symbol(libpath):
+    lib = ctypes.CDLL(libpath)
+    missing = [n for n in declared_functions() if not hasattr(lib, n)]
+    assert not missing, missing
+
+
+def test_context_creation_fails_cleanly_without_gpu(libpath):
+    import torch
+    if torch.cuda.is_available():
+        pytest.skip("a GPU is present")
+    from lightcurve_fitting_gb300.lib import Context, LcfError
+    with pytest.raises(LcfError):
+        Context(0)
+
+
+def test_python_api_validates_arguments():
+    from lightcurve_fitting_gb300 import parametric
+    with pytest.raises(ValueError, match="bogus"):
+        parametric._method("bogus")
+    with pytest.raises(ValueError):
+        parametric._model_id("NotAModel")
+    assert parametric._model_id("tde") == 2
+
+
+def test_build_flux_bands_matches_reference_rules():
+    from lightcurve_fitting_gb300.parametric import build_flux_bands
+    import numpy as np
+    t = [2460000.0, 2460001.0, 2460002.0, 2460003.0]
+    m = [20.0, float("nan"), 19.0, 21.0]
+    e = [0.1, 0.1, 0.1, 0.2]
+    b = ["g", "g", "r", "g"]
+    out = build_flux_bands(t, m, e, b)
+    assert sorted(out) == ["g", "r"]
+    assert out["g"]["times"] == [0.0, 3.0]
+    np.testing.assert_allclose(out["r"]["values"][0], 10 ** (-0.4 * (19.0 - 23.9)))
