@@ -450,14 +450,14 @@ static void enqueue_pipeline(lcf_ctx* ctx) {
     int grid = ctx->num_sms * ctx->pso_blocks_per_sm;
     int block = ctx->pso_block;
     int64_t L = 0;
-    cudaEventRecord(ctx->ev[0], s);
+    cudaEventRecordWithFlags(ctx->ev[0], s, cudaEventRecordExternal);
     cudaMemsetAsync(ctx->res.p, 0xff, (size_t)std::max(ctx->n_bands, 1) * 44 * sizeof(PsoResult), s);
     cudaMemsetAsync(ctx->ctr.p, 0, sizeof(Counters), s);
     cudaMemsetAsync(ctx->fits.p, 0xff, (size_t)std::max(ctx->n_bands, 1) * 8 * sizeof(ModelFit), s);
     launch_prep(d, s); L++;
-    cudaEventRecord(ctx->ev[1], s);
+    cudaEventRecordWithFlags(ctx->ev[1], s, cudaEventRecordExternal);
     launch_pso(d, 0, ctx->n_tasks0, 7, grid, block, s); L++;
-    cudaEventRecord(ctx->ev[2], s);
+    cudaEventRecordWithFlags(ctx->ev[2], s, cudaEventRecordExternal);
     int gated = (o.forced_model < 0 && !o.fit_all_models);
     launch_lbfgs(d, gated ? 1 : 0xff, s); L++;
     if (gated) {
@@ -466,7 +466,7 @@ static void enqueue_pipeline(lcf_ctx* ctx) {
         launch_lbfgs(d, 0xfe, s); L++;
     }
     launch_select(d, o.fit_all_models, o.forced_model, s); L++;
-    cudaEventRecord(ctx->ev[3], s);
+    cudaEventRecordWithFlags(ctx->ev[3], s, cudaEventRecordExternal);
     if (o.method == LCF_METHOD_SVI) {
         launch_t0_build(d, 2, 0, s); L++;
         launch_pso(d, 2, -1, 7, grid, block, s); L++;
@@ -475,13 +475,13 @@ static void enqueue_pipeline(lcf_ctx* ctx) {
         launch_pso(d, 3, -1, 7, grid, block, s); L++;
         launch_t0_pick(d, 3, 1, s); L++;
     }
-    cudaEventRecord(ctx->ev[4], s);
+    cudaEventRecordWithFlags(ctx->ev[4], s, cudaEventRecordExternal);
     if (o.method == LCF_METHOD_SVI) launch_svi(d, s);
     else launch_laplace(d, s);
     L++;
-    cudaEventRecord(ctx->ev[5], s);
+    cudaEventRecordWithFlags(ctx->ev[5], s, cudaEventRecordExternal);
     launch_refine(d, s); L++;
-    cudaEventRecord(ctx->ev[6], s);
+    cudaEventRecordWithFlags(ctx->ev[6], s, cudaEventRecordExternal);
     if (o.run_multi_bazin) {
         launch_mb_pick(d, 1, s); L++;
         for (int k = 2; k <= 4; k++) {
@@ -490,11 +490,12 @@ static void enqueue_pipeline(lcf_ctx* ctx) {
             launch_mb_pick(d, k, s); L++;
         }
     }
-    cudaEventRecord(ctx->ev[7], s);
+    cudaEventRecordWithFlags(ctx->ev[7], s, cudaEventRecordExternal);
     ctx->launches = L;
 }
 
 static int run_pipeline(lcf_ctx* ctx) {
+    cudaGetLastError();  // a failed query elsewhere in the process must not be reported as ours
     uint64_t gkey = ctx->layout_key ^ ((uint64_t)(uintptr_t)ctx->db.times * 31) ^ ((uint64_t)ctx->n_obs << 7);
     if (ctx->use_graph) {
         if (!ctx->graph || ctx->graph_key != gkey) {
@@ -528,9 +529,11 @@ static int finish_stats(lcf_ctx* ctx) {
     Counters c;
     CK(cudaMemcpy(&c, ctx->ctr.p, sizeof(Counters), cudaMemcpyDeviceToHost));
     float ms[8] = {0};
-    for (int i = 1; i < 8; i++) cudaEventElapsedTime(&ms[i], ctx->ev[i - 1], ctx->ev[i]);
+    for (int i = 1; i < 8; i++)
+        if (cudaEventElapsedTime(&ms[i], ctx->ev[i - 1], ctx->ev[i]) != cudaSuccess) ms[i] = 0.0f;
     float tot = 0;
-    cudaEventElapsedTime(&tot, ctx->ev[0], ctx->ev[7]);
+    if (cudaEventElapsedTime(&tot, ctx->ev[0], ctx->ev[7]) != cudaSuccess) tot = 0.0f;
+    cudaGetLastError();
     lcf_fit_stats& st = ctx->stats;
     st.ms_total = tot;
     st.ms_pso = ms[2];

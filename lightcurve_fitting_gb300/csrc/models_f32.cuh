@@ -59,13 +59,26 @@ __device__ __forceinline__ float sigmoid_f(float x) {
 // observation loop.  eval(th, tl, st) returns the prediction (or its log when
 // st == ST_BIG).
 // ---------------------------------------------------------------------------
+// Each model has init(const float*) for FP32 parameter vectors (the swarm's
+// positions) and init64(const double*) for FP64 ones (L-BFGS iterates, the
+// likelihood API): the latter forms the per-particle constants in FP64 and
+// keeps t0 as a (hi, lo) pair, so no parameter rounding enters the result.
+__device__ __forceinline__ void split64(double v, float& hi, float& lo) {
+    hi = (float)v;
+    lo = (float)(v - (double)hi);
+}
+
 struct BazinF {
-    float a, la, b, t0, itr, itf;
+    float a, la, b, t0, t0lo, itr, itf;
     __device__ void init(const float* p) {
-        la = p[0]; a = expf(p[0]); b = p[1]; t0 = p[2]; itr = expf(-p[3]); itf = expf(-p[4]);
+        la = p[0]; a = expf(p[0]); b = p[1]; t0 = p[2]; t0lo = 0.0f; itr = expf(-p[3]); itf = expf(-p[4]);
+    }
+    __device__ void init64(const double* p) {
+        la = (float)p[0]; a = (float)exp(p[0]); b = (float)p[1]; split64(p[2], t0, t0lo);
+        itr = (float)exp(-p[3]); itf = (float)exp(-p[4]);
     }
     __device__ __forceinline__ float eval(float th, float tl, int& st) const {
-        float dt = (th - t0) + tl;
+        float dt = (th - t0) + (tl - t0lo);
         float xf = -dt * itf, xr = -dt * itr;
         if (xf < 80.0f && xr < 80.0f) {
             float ef = expf(xf);
@@ -82,15 +95,19 @@ struct BazinF {
 };
 
 struct VillarF {
-    float a, beta, gamma, t0, itr, itf, omb;
+    float a, beta, gamma, t0, t0lo, itr, itf, omb;
     __device__ void init(const float* p) {
-        a = expf(p[0]); beta = p[1]; gamma = expf(p[2]); t0 = p[3]; itr = expf(-p[4]); itf = expf(-p[5]);
+        a = expf(p[0]); beta = p[1]; gamma = expf(p[2]); t0 = p[3]; t0lo = 0.0f; itr = expf(-p[4]); itf = expf(-p[5]);
         omb = 1.0f - beta * gamma;
+    }
+    __device__ void init64(const double* p) {
+        a = (float)exp(p[0]); beta = (float)p[1]; gamma = (float)exp(p[2]); split64(p[3], t0, t0lo);
+        itr = (float)exp(-p[4]); itf = (float)exp(-p[5]); omb = (float)(1.0 - p[1] * exp(p[2]));
     }
     __device__ __forceinline__ float eval(float th, float tl, int& st) const {
         // Within the Villar box every exponent stays below 70, so FP32 holds
         // the FP64 result without special cases.
-        float ph = (th - t0) + tl;
+        float ph = (th - t0) + (tl - t0lo);
         float sig = 1.0f / (1.0f + expf(-ph * itr));
         float w = 1.0f / (1.0f + expf(-10.0f * (ph - gamma)));
         float pl = 1.0f - beta * ph;
@@ -108,12 +125,16 @@ struct VillarF {
 };
 
 struct TdeF {
-    float a, b, t0, itr, itf, alpha;
+    float a, b, t0, t0lo, itr, itf, alpha;
     __device__ void init(const float* p) {
-        a = expf(p[0]); b = p[1]; t0 = p[2]; itr = expf(-p[3]); itf = expf(-p[4]); alpha = p[5];
+        a = expf(p[0]); b = p[1]; t0 = p[2]; t0lo = 0.0f; itr = expf(-p[3]); itf = expf(-p[4]); alpha = p[5];
+    }
+    __device__ void init64(const double* p) {
+        a = (float)exp(p[0]); b = (float)p[1]; split64(p[2], t0, t0lo); itr = (float)exp(-p[3]);
+        itf = (float)exp(-p[4]); alpha = (float)p[5];
     }
     __device__ __forceinline__ float eval(float th, float tl, int& st) const {
-        float ph = (th - t0) + tl;
+        float ph = (th - t0) + (tl - t0lo);
         float sig = 1.0f / (1.0f + expf(-ph * itr));
         float ps;
         if (!phase_soft_f(ph, ps)) return b;  // w = inf -> decay = 0
@@ -123,12 +144,15 @@ struct TdeF {
 };
 
 struct ArnettF {
-    float a, t0, itm, f;
+    float a, t0, t0lo, itm, f;
     __device__ void init(const float* p) {
-        a = expf(p[0]); t0 = p[1]; itm = expf(-p[2]); f = 1.0f / (1.0f + expf(-p[3]));
+        a = expf(p[0]); t0 = p[1]; t0lo = 0.0f; itm = expf(-p[2]); f = 1.0f / (1.0f + expf(-p[3]));
+    }
+    __device__ void init64(const double* p) {
+        a = (float)exp(p[0]); split64(p[1], t0, t0lo); itm = (float)exp(-p[2]); f = (float)(1.0 / (1.0 + exp(-p[3])));
     }
     __device__ __forceinline__ float eval(float th, float tl, int& st) const {
-        float ph = (th - t0) + tl;
+        float ph = (th - t0) + (tl - t0lo);
         float ps;
         if (!phase_soft_f(ph, ps)) return 0.0f;  // heat = 0
         float heat = f * expf(-ps * (1.0f / 8.8f)) + (1.0f - f) * expf(-ps * (1.0f / 111.3f));
@@ -138,12 +162,15 @@ struct ArnettF {
 };
 
 struct MagnetarF {
-    float a, t0, itsd, itd;
+    float a, t0, t0lo, itsd, itd;
     __device__ void init(const float* p) {
-        a = expf(p[0]); t0 = p[1]; itsd = expf(-p[2]); itd = expf(-p[3]);
+        a = expf(p[0]); t0 = p[1]; t0lo = 0.0f; itsd = expf(-p[2]); itd = expf(-p[3]);
+    }
+    __device__ void init64(const double* p) {
+        a = (float)exp(p[0]); split64(p[1], t0, t0lo); itsd = (float)exp(-p[2]); itd = (float)exp(-p[3]);
     }
     __device__ __forceinline__ float eval(float th, float tl, int& st) const {
-        float ph = (th - t0) + tl;
+        float ph = (th - t0) + (tl - t0lo);
         float ps;
         if (!phase_soft_f(ph, ps)) return 0.0f;  // spindown = 0
         float w = 1.0f + ps * itsd;
@@ -153,12 +180,15 @@ struct MagnetarF {
 };
 
 struct ShockF {
-    float a, t0, n, ittr;
+    float a, t0, t0lo, n, ittr;
     __device__ void init(const float* p) {
-        a = expf(p[0]); t0 = p[1]; n = p[2]; ittr = expf(-p[3]);
+        a = expf(p[0]); t0 = p[1]; t0lo = 0.0f; n = p[2]; ittr = expf(-p[3]);
+    }
+    __device__ void init64(const double* p) {
+        a = (float)exp(p[0]); split64(p[1], t0, t0lo); n = (float)p[2]; ittr = (float)exp(-p[3]);
     }
     __device__ __forceinline__ float eval(float th, float tl, int& st) const {
-        float ph = (th - t0) + tl;
+        float ph = (th - t0) + (tl - t0lo);
         float ps;
         if (!phase_soft_f(ph, ps)) return 0.0f;  // cooling = cutoff = 0
         float sig5 = 1.0f / (1.0f + expf(-5.0f * ph));
@@ -169,12 +199,15 @@ struct ShockF {
 };
 
 struct AfterglowF {
-    float la, t0, ltb, a1, a2;
+    float la, t0, t0lo, ltb, a1, a2;
     __device__ void init(const float* p) {
-        la = p[0]; t0 = p[1]; ltb = p[2]; a1 = p[3]; a2 = p[4];
+        la = p[0]; t0 = p[1]; t0lo = 0.0f; ltb = p[2]; a1 = p[3]; a2 = p[4];
+    }
+    __device__ void init64(const double* p) {
+        la = (float)p[0]; split64(p[1], t0, t0lo); ltb = (float)p[2]; a1 = (float)p[3]; a2 = (float)p[4];
     }
     __device__ __forceinline__ float eval(float th, float tl, int& st) const {
-        float ph = (th - t0) + tl;
+        float ph = (th - t0) + (tl - t0lo);
         float ps;
         if (!phase_soft_f(ph, ps)) return 0.0f;  // u = inf -> flux 0
         float lr = logf(ps) - ltb;
@@ -225,12 +258,24 @@ struct Nll {
         bool upper = o.w < 0.0f;
         float tv = fabsf(o.w) + se2;
         if (st == ST_OK) {
+            // r = residual / sigma; |r| > 1e15 would overflow r*r in FP32, so
+            // such terms go to the log-domain sum like ST_BIG predictions
+            float is = rsqrtf(tv);
             if (upper) {
-                float z = (o.z - pred) * rsqrtf(tv);
-                add(-log_normal_cdf_f(z));
+                float z = (o.z - pred) * is;
+                if (z > -1e15f) { add(-log_normal_cdf_f(z)); return; }
+                float lz = logf(-z);
+                if (lz + 0.5f * logf(tv) > LN_SQRT_DBL_MAX) { inf = 1; return; }
+                add(0.5f * LN_2PI_F + lz);
+                add_big(2.0f * lz - 0.69314718f);
             } else {
-                float d = pred - o.z;
-                add(d * d / tv + logf(tv));
+                float r = (pred - o.z) * is;
+                float ltv = logf(tv);
+                if (fabsf(r) < 1e15f) { add(r * r + ltv); return; }
+                float lr = logf(fabsf(r));
+                if (lr + 0.5f * ltv > LN_SQRT_DBL_MAX) { inf = 1; return; }
+                add(ltv);
+                add_big(2.0f * lr);
             }
         } else if (st == ST_BIG) {
             // |pred| = e^pred (pred > e^60 >> |y|); FP64 d*d overflows past e^354.89

@@ -39,8 +39,8 @@ __device__ __forceinline__ int warp_or(int v) { return __any_sync(FULL, v) ? 1 :
 
 // Warp-wide negative log-likelihood of a parameter vector (cost of PsoCost
 // without the Villar constraint and prior): lanes over observations.
-__device__ double warp_nll(int m, const float* p, const float4* obs, int n, double nd, double prior) {
-    float se = expf(p[se_idx_of(m)]);
+__device__ double warp_nll(int m, const double* pd, const float4* obs, int n, double nd, double prior) {
+    float se = (float)exp(pd[se_idx_of(m)]);
     float se2 = se * se;
     Nll acc;
     acc.reset();
@@ -50,13 +50,13 @@ __device__ double warp_nll(int m, const float* p, const float4* obs, int n, doub
         int st = ST_OK;
         float pr;
         switch (m) {
-            case BAZIN: { BazinF e; e.init(p); pr = e.eval(o.x, o.y, st); break; }
-            case VILLAR: { VillarF e; e.init(p); pr = e.eval(o.x, o.y, st); break; }
-            case TDE: { TdeF e; e.init(p); pr = e.eval(o.x, o.y, st); break; }
-            case ARNETT: { ArnettF e; e.init(p); pr = e.eval(o.x, o.y, st); break; }
-            case MAGNETAR: { MagnetarF e; e.init(p); pr = e.eval(o.x, o.y, st); break; }
-            case SHOCK: { ShockF e; e.init(p); pr = e.eval(o.x, o.y, st); break; }
-            default: { AfterglowF e; e.init(p); pr = e.eval(o.x, o.y, st); break; }
+            case BAZIN: { BazinF e; e.init64(pd); pr = e.eval(o.x, o.y, st); break; }
+            case VILLAR: { VillarF e; e.init64(pd); pr = e.eval(o.x, o.y, st); break; }
+            case TDE: { TdeF e; e.init64(pd); pr = e.eval(o.x, o.y, st); break; }
+            case ARNETT: { ArnettF e; e.init64(pd); pr = e.eval(o.x, o.y, st); break; }
+            case MAGNETAR: { MagnetarF e; e.init64(pd); pr = e.eval(o.x, o.y, st); break; }
+            case SHOCK: { ShockF e; e.init64(pd); pr = e.eval(o.x, o.y, st); break; }
+            default: { AfterglowF e; e.init64(pd); pr = e.eval(o.x, o.y, st); break; }
         }
         acc.obs(o, pr, st, se2);
     }
@@ -110,7 +110,7 @@ __device__ void lb_cost_grad(LbCtx& c, const double* x, double& f, double* g, bo
                 prior += 0.5 * z * z;
             }
         }
-        f = warp_nll(c.m, p, c.obs, c.n, c.nd, prior);
+        f = warp_nll(c.m, q, c.obs, c.n, c.nd, prior);
     }
     if (!want_grad) return;
     // gradient: PsoCost::gradient (no prior, no constraint term)

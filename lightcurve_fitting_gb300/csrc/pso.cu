@@ -263,7 +263,15 @@ __device__ __forceinline__ Nll nll_multibazin(const float* p, const float4* obs,
     return acc;
 }
 
-__device__ double particle_cost(const TaskCtx& t, const float* x) {
+template <class M>
+__device__ __forceinline__ void model_init(M& e, const float* p, const double* pd) {
+    if (pd) e.init64(pd);
+    else e.init(p);
+}
+
+// pd: optional FP64 parameter vector (same values as p) for callers whose
+// parameters are FP64; the per-particle constants are then formed in FP64.
+__device__ double particle_cost(const TaskCtx& t, const float* x, const double* pd = nullptr) {
     // rebuild the full parameter vector
     float p[MB_MAXP];
     if (t.flags & TASK_T0_FIXED) {
@@ -307,17 +315,17 @@ __device__ double particle_cost(const TaskCtx& t, const float* x) {
         }
         prior = (double)s;
     }
-    float se = expf(p[se_idx_of(m)]);
+    float se = pd ? (float)exp(pd[se_idx_of(m)]) : expf(p[se_idx_of(m)]);
     float se2 = se * se;
     Nll acc;
     switch (m) {
-        case BAZIN: { BazinF e; e.init(p); acc = nll_loop(e, t.obs, t.n, se2); break; }
-        case VILLAR: { VillarF e; e.init(p); acc = nll_loop(e, t.obs, t.n, se2); break; }
-        case TDE: { TdeF e; e.init(p); acc = nll_loop(e, t.obs, t.n, se2); break; }
-        case ARNETT: { ArnettF e; e.init(p); acc = nll_loop(e, t.obs, t.n, se2); break; }
-        case MAGNETAR: { MagnetarF e; e.init(p); acc = nll_loop(e, t.obs, t.n, se2); break; }
-        case SHOCK: { ShockF e; e.init(p); acc = nll_loop(e, t.obs, t.n, se2); break; }
-        case AFTERGLOW: { AfterglowF e; e.init(p); acc = nll_loop(e, t.obs, t.n, se2); break; }
+        case BAZIN: { BazinF e; model_init(e, p, pd); acc = nll_loop(e, t.obs, t.n, se2); break; }
+        case VILLAR: { VillarF e; model_init(e, p, pd); acc = nll_loop(e, t.obs, t.n, se2); break; }
+        case TDE: { TdeF e; model_init(e, p, pd); acc = nll_loop(e, t.obs, t.n, se2); break; }
+        case ARNETT: { ArnettF e; model_init(e, p, pd); acc = nll_loop(e, t.obs, t.n, se2); break; }
+        case MAGNETAR: { MagnetarF e; model_init(e, p, pd); acc = nll_loop(e, t.obs, t.n, se2); break; }
+        case SHOCK: { ShockF e; model_init(e, p, pd); acc = nll_loop(e, t.obs, t.n, se2); break; }
+        case AFTERGLOW: { AfterglowF e; model_init(e, p, pd); acc = nll_loop(e, t.obs, t.n, se2); break; }
         default: {
             // MetzgerKN: ODE sweep -> unnormalised interpolants in scratch
             struct ObsT {
@@ -623,8 +631,12 @@ __global__ void band_cost_kernel(int model, const float4* obs, int n, float t_la
     t.mscratch = scratch + (size_t)warp * 32 * (size_t)max(n, 1);
     t.prior_n = (double)max(n, 1);
     float x[MAXP];
-    for (int j = 0; j < MAXP; j++) x[j] = (e < n_eval && j < t.np) ? (float)params[(size_t)e * t.np + j] : 0.0f;
-    double c = particle_cost(t, x);
+    double xd[MAXP];
+    for (int j = 0; j < MAXP; j++) {
+        xd[j] = (e < n_eval && j < t.np) ? params[(size_t)e * t.np + j] : 0.0;
+        x[j] = (float)xd[j];
+    }
+    double c = particle_cost(t, x, xd);
     if (e < n_eval) costs[e] = c;
 }
 
