@@ -1,0 +1,318 @@
+#!/usr/bin/env python
+"""Benchmark of the fused GB300 fit: sources/s of fit_parametric (PSO model
+selection over the eight flux models with three restarts, L-BFGS polish, BIC
+selection, profile t0 search, SVI uncertainty, profile refinements,
+magnitude chi2 and MultiBazin) on 10,000 synthetic sources x 3 bands of
+uneven length (counts round(lognormal(ln 40, 0.9)) clipped to [5, 500]).
+
+One JSON line on rank 0:
+  value     sources/s with the inputs resident in HBM (the device entry point
+            lcf_fit_parametric_device), CUDA events on the library's stream,
+            L2 flushed (256 MB write) between timed steps;
+  e2e       the same metric through lcf_fit_parametric_batch with host
+            buffers (pinned staging, H2D copies, pipeline, D2H of the results
+            all inside the timed region);
+  roofline  the model-selection PSO kernel against the measured SFU (MUFU)
+            and FP32 pipe peaks (the kernel is bound by those pipes, not by
+            HBM or the tensor cores);
+  cpu_baseline  the FP64 C++ restatement of the reference's CPU path
+            (oracle/, "port") on a bounded sample, all host threads.
+
+``--impl reference`` times that CPU path alone (rank 0) on the same workload.
+Under torchrun each rank fits its own 10,000 sources (weak scaling, no
+collective on the data path); value = all ranks' sources / max rank time.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "sources/s, fit_parametric PSO+SVI, 10k uneven sources: fused vs plain GPU"
+WORKLOAD = ("uneven-10000x3: counts round(lognormal(ln 40, 0.9)) clipped [5, 500] per band, t in [0, 300] d "
+            "with 20% of nights dropped, generators Bazin/Villar/TDE/Arnett/Magnetar, sigma = 0.05|F| + 5; "
+            "fit_all_models=true, SVI uncertainty, MultiBazin on the most populated band")
+
+# Algorithmic SFU (MUFU) operations per particle x observation evaluation of
+# each task kind, counted from the FP32 model forms in csrc/models_f32.cuh:
+# exp/log/log1p/expm1 = 1 each, a reciprocal or division = 1, rsqrt = 1, plus
+# the Gaussian term's rsqrt and log (2).  MetzgerKN also spends ~14 per Euler
+# step of its 200-step ODE (counted through ode_steps), MultiBazin K spends
+# 3 per component.
+MUFU_PER_EVAL = {0: 5, 1: 7, 2: 8, 3: 7, 4: 6, 5: 8, 6: 8, 7: 2, 8: 5, 9: 8, 10: 11, 11: 14}
+MUFU_PER_ODE_STEP = 14
+# FP32 pipe operations per evaluation (adds, multiplies, FMAs, compares,
+# including the Kahan update of 4 adds); MetzgerKN ~60 per ODE step.
+FP32_PER_EVAL = {0: 24, 1: 34, 2: 30, 3: 30, 4: 26, 5: 30, 6: 32, 7: 16, 8: 24, 9: 34, 10: 44, 11: 54}
+FP32_PER_ODE_STEP = 60
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="fused", choices=["fused", "reference"])
+    ap.add_argument("--sources", type=int, default=10000)
+    ap.add_argument("--cpu-sample", type=int, default=96, help="sources in the CPU-baseline sample")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    return ap.parse_args()
+
+
+def dist_setup():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if ws > 1:
+        import torch.distributed as dist
+        os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
+        import torch
+        backend = "nccl" if torch.cuda.is_available() else "gloo"
+        dist.init_process_group(backend=backend)
+    return ws, rank, local
+
+
+def dist_max(x: float, ws: int, device) -> float:
+    if ws == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([x], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def dist_barrier(ws: int):
+    if ws > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+class ClockSampler:
+    """nvidia-smi SM clocks and throttle reasons during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        try:
+            fd, self.path = tempfile.mkstemp(suffix=".csv")
+            os.close(fd)
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self) -> dict:
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in open(self.path):
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                mx.append(float(parts[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, parts[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        os.unlink(self.path)
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def cpu_baseline(batch, n_sample: int, threads: int = 0):
+    """The oracle (FP64 port of the reference CPU path) on a bounded sample."""
+    from lightcurve_fitting_gb300 import abi
+    from oracle import oracle as O
+    O.build()
+    sub = batch.subset(np.arange(min(n_sample, batch.n_sources)))
+    t = time.perf_counter()
+    O.fit_batch(sub, fit_all_models=True, method=abi.METHOD_SVI, n_threads=threads)
+    dt = time.perf_counter() - t
+    cores = threads if threads > 0 else O.max_threads()
+    return sub.n_sources / dt, cores, sub.n_sources, dt
+
+
+def run_reference(args, ws, rank):
+    if rank != 0:
+        return
+    from lightcurve_fitting_gb300 import synth
+    batch = synth.config_uneven(args.sources, seed=2)
+    vals, cores, n = [], 0, 0
+    for i in range(args.warmup + args.steps):
+        v, cores, n, dt = cpu_baseline(batch.subset(np.arange(i * 7 % 100, batch.n_sources)), args.cpu_sample)
+        if i >= args.warmup:
+            vals.append(dt)
+    value = args.steps * n / sum(vals)
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": "sources/s", "n_gpus": 0,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * sum(vals) / len(vals),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": WORKLOAD, "sample_sources_per_step": n},
+        "cpu_baseline": {"value": value, "unit": "sources/s", "cores": cores, "kind": "port",
+                         "sample": f"{n} sources of the workload per step, OpenMP over sources"},
+        "e2e": {"value": value, "unit": "sources/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def run_fused(args, ws, rank, local):
+    import torch
+    from lightcurve_fitting_gb300 import abi, build, synth
+    build.build()
+    from lightcurve_fitting_gb300.lib import Context
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    batch = synth.config_uneven(args.sources, seed=2 + rank)
+    ctx = Context(local)
+    stream = torch.cuda.ExternalStream(ctx.stream, device=dev)
+    peaks = ctx.probe_peaks()
+    # device-resident inputs
+    d = {
+        "times": torch.from_numpy(batch.times).to(dev),
+        "flux": torch.from_numpy(batch.flux).to(dev),
+        "flux_err": torch.from_numpy(batch.flux_err).to(dev),
+        "band_obs_offsets": torch.from_numpy(batch.band_obs_offsets).to(dev),
+        "source_band_offsets": torch.from_numpy(batch.source_band_offsets).to(dev),
+    }
+    ptrs = {k: v.data_ptr() for k, v in d.items()}
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
+    torch.cuda.synchronize()
+
+    def fit_dev():
+        ctx.fit_device(ptrs, batch.n_sources, batch.n_bands, fit_all_models=True, method=abi.METHOD_SVI)
+
+    for _ in range(args.warmup):
+        fit_dev()
+    torch.cuda.synchronize()
+    clocks = ClockSampler(local)
+    dist_barrier(ws)
+    clocks.start()
+    times, stage = [], []
+    for _ in range(args.steps):
+        flush.fill_(1.0)
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        fit_dev()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        times.append(e0.elapsed_time(e1))
+        stage.append(ctx.stats())
+    torch.cuda.synchronize()
+    ck = clocks.stop()
+    dist_barrier(ws)
+    ms = float(np.mean(times))
+    ms_max = dist_max(ms, ws, dev)
+    value = ws * batch.n_sources / (ms_max * 1e-3)
+    # end-to-end through the host entry point
+    e2e_t = []
+    res = ctx.fit_batch(batch, fit_all_models=True, method=abi.METHOD_SVI)
+    for _ in range(args.steps):
+        flush.fill_(1.0)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        res = ctx.fit_batch(batch, fit_all_models=True, method=abi.METHOD_SVI)
+        e2e_t.append(time.perf_counter() - t0)
+    st_e2e = ctx.stats()
+    e2e_s = dist_max(float(np.mean(e2e_t)), ws, dev)
+    e2e = {"value": ws * batch.n_sources / e2e_s, "unit": "sources/s",
+           "h2d_bytes_per_step": int(st_e2e["h2d_bytes"]), "d2h_bytes_per_step": int(st_e2e["d2h_bytes"])}
+    if rank != 0:
+        ctx.close()
+        return
+    # roofline of the model-selection PSO launch
+    s0 = stage[-1]
+    ev = s0["pso0_evals_by_kind"]
+    npart = s0["pso0_particles_by_kind"]
+    mufu = sum(ev[k] * MUFU_PER_EVAL[k] for k in range(12)) + npart[7] * 200 * MUFU_PER_ODE_STEP
+    fp32 = sum(ev[k] * FP32_PER_EVAL[k] for k in range(12)) + npart[7] * 200 * FP32_PER_ODE_STEP
+    pso_ms = float(np.mean([s["ms_pso"] for s in stage]))
+    mufu_rate = mufu / (pso_ms * 1e-3) * 1e-9          # Gop/s
+    fp32_rate = 2.0 * fp32 / (pso_ms * 1e-3) * 1e-12   # TFLOP/s counting an op as 2 for FMA parity
+    frac_mufu = mufu_rate / peaks["mufu_gops"] if peaks["mufu_gops"] else None
+    frac_fp32 = fp32_rate / peaks["fp32_tflops"] if peaks["fp32_tflops"] else None
+    bound_sfu = (frac_mufu or 0) >= (frac_fp32 or 0)
+    roofline = {
+        "bound": "sfu" if bound_sfu else "fp32",
+        "achieved": mufu_rate if bound_sfu else fp32_rate,
+        "peak": peaks["mufu_gops"] if bound_sfu else peaks["fp32_tflops"],
+        "unit": "Gop/s" if bound_sfu else "TFLOP/s",
+        "frac": frac_mufu if bound_sfu else frac_fp32,
+        "traffic": None,
+        "kernel": "pso_kernel<7> (model-selection swarm launch)",
+        "peak_source": "measured live by lcf_probe_peaks (dependent ex2 / FMA chains over a full grid)",
+        "other_pipe": ({"bound": "fp32", "achieved": fp32_rate, "peak": peaks["fp32_tflops"], "unit": "TFLOP/s",
+                        "frac": frac_fp32} if bound_sfu else
+                       {"bound": "sfu", "achieved": mufu_rate, "peak": peaks["mufu_gops"], "unit": "Gop/s",
+                        "frac": frac_mufu}),
+        "launch_ms": pso_ms,
+        "particle_obs_evals": float(sum(ev)),
+    }
+    cpu = None
+    if not args.no_cpu_baseline:
+        v, cores, n, dt = cpu_baseline(batch, args.cpu_sample)
+        cpu = {"value": v, "unit": "sources/s", "cores": cores, "kind": "port",
+               "sample": f"first {n} sources of the workload, FP64 C++ restatement of the reference CPU path, "
+                         f"OpenMP over sources ({dt:.1f} s wall)"}
+    line = {
+        "metric": METRIC, "value": value, "unit": "sources/s", "n_gpus": ws, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms_max, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": WORKLOAD, "n_sources_per_gpu": batch.n_sources, "n_bands": batch.n_bands,
+                   "n_obs": batch.n_obs, "l2": "flushed between timed steps (256 MB write)",
+                   "parallelism": f"independent shards x{ws}"},
+        "stage_ms": {k: float(np.mean([s[k] for s in stage])) for k in
+                     ["ms_total", "ms_pso", "ms_lbfgs", "ms_t0_search", "ms_uncertainty", "ms_refine",
+                      "ms_multi_bazin"]},
+        "e2e": e2e,
+        "roofline": roofline,
+        "cpu_baseline": cpu,
+        "clocks": ck,
+        "gpu_launches": int(s0["kernel_launches"]) * args.steps,
+        "peaks": peaks,
+    }
+    print(json.dumps(line), flush=True)
+    ctx.close()
+
+
+def main():
+    args = parse()
+    ws, rank, local = dist_setup()
+    if args.impl == "reference":
+        run_reference(args, ws, rank)
+    else:
+        run_fused(args, ws, rank, local)
+    if ws > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -127,6 +127,10 @@ typedef struct lcf_fit_stats {
     double ode_steps;           /* device-counted MetzgerKN Euler steps in PSO launches */
     int64_t pso_tasks;          /* PSO runs executed */
     int64_t kernel_launches;    /* kernels launched by the last fit */
+    double h2d_bytes;           /* host -> device bytes moved by the last lcf_fit_parametric_batch */
+    double d2h_bytes;           /* device -> host bytes moved by the last output download */
+    double pso0_evals_by_kind[12];      /* particle x observation evaluations of the model-selection PSO launch, by task kind */
+    double pso0_particles_by_kind[12];  /* particle evaluations of that launch, by task kind (kinds 8..11: MultiBazin K = 1..4) */
 } lcf_fit_stats;
 
 typedef struct lcf_ctx lcf_ctx;
@@ -162,6 +166,19 @@ void* lcf_ctx_stream(lcf_ctx* ctx);
 /* Replay the stage sequence from a CUDA graph captured per batch layout
  * (default 1), or launch the kernels one by one (0). */
 int lcf_set_graph(lcf_ctx* ctx, int enabled);
+
+/* Measured pipe peaks of the context's GPU: out[0] = FP32 FMA TFLOP/s,
+ * out[1] = SFU (MUFU ex2) Gop/s, from dependent-chain probe kernels over a
+ * full grid.  The roofline denominators of the fused kernels, which are
+ * bound by these two pipes rather than by HBM or the tensor cores. */
+int lcf_probe_peaks(lcf_ctx* ctx, double* out2);
+
+/* Diagnostic: raw swarm results of the last fit, 21 doubles per result slot
+ * (cost, iterations, particle evaluations, 18 parameters).  Slots
+ * [0, 24 n_bands) hold (band * 8 + model) * 3 + restart of the model
+ * selection, [24 n_bands, 32 n_bands) the profile-t0 runs, [32 n_bands,
+ * 44 n_bands) the MultiBazin runs.  A slot that did not run has cost NaN. */
+int lcf_debug_swarm_results(lcf_ctx* ctx, double* out, int64_t max_rows);
 
 /*
  * Batched likelihood: cost of `n_eval` parameter vectors of one model on one

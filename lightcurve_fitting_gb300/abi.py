@@ -83,6 +83,10 @@ class FitStats(C.Structure):
         ("ode_steps", C.c_double),
         ("pso_tasks", C.c_int64),
         ("kernel_launches", C.c_int64),
+        ("h2d_bytes", C.c_double),
+        ("d2h_bytes", C.c_double),
+        ("pso0_evals_by_kind", C.c_double * 12),
+        ("pso0_particles_by_kind", C.c_double * 12),
     ]
 
 

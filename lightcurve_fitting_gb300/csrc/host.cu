@@ -546,6 +546,10 @@ static int finish_stats(lcf_ctx* ctx) {
     st.ode_steps = (double)c.ode_steps;
     st.pso_tasks = ctx->n_tasks0;
     st.kernel_launches = ctx->launches;
+    for (int k = 0; k < 12; k++) {
+        st.pso0_evals_by_kind[k] = (double)c.slot0_evals[k];
+        st.pso0_particles_by_kind[k] = (double)c.slot0_particles[k];
+    }
     if (c.error) return set_err(ctx, c.error, "a bounded device wait expired");
     return 0;
 }
@@ -557,6 +561,10 @@ static int unpack_outputs(lcf_ctx* ctx, lcf_fit_outputs* out) {
     int nb = ctx->n_bands;
     size_t bytes = (size_t)nb * (sizeof(BandOut) + sizeof(BandStats) + sizeof(MbState) +
                                  (ctx->opts.fit_all_models ? 8 * sizeof(ModelFit) : 0));
+    ctx->stats.d2h_bytes = (double)(nb > 0 ? (size_t)nb * (sizeof(BandOut) + sizeof(BandStats) +
+                                                          (ctx->opts.run_multi_bazin ? sizeof(MbState) : 0) +
+                                                          (ctx->opts.fit_all_models ? 8 * sizeof(ModelFit) : 0))
+                                           : 0);
     if (grow_pinned(ctx, ctx->h_out, bytes)) return LCF_E_NOMEM;
     char* hp = (char*)ctx->h_out.p;
     BandOut* ho = (BandOut*)hp;
@@ -665,6 +673,7 @@ extern "C" int lcf_fit_parametric_batch(lcf_ctx* ctx, const lcf_bands_csr* in, c
     if (nb == 0) return 0;
     if (int rc = run_pipeline(ctx)) return rc;
     if (int rc = finish_stats(ctx)) return rc;
+    ctx->stats.h2d_bytes = (double)in_bytes;
     return unpack_outputs(ctx, out);
 }
 
@@ -741,6 +750,31 @@ extern "C" int lcf_band_cost(lcf_ctx* ctx, int model, const double* times, const
     CK(cudaGetLastError());
     CK(cudaMemcpyAsync(costs, ctx->bc_costs.p, (size_t)n_eval * 8, cudaMemcpyDeviceToHost, s));
     CK(cudaStreamSynchronize(s));
+    return 0;
+}
+
+extern "C" int lcf_debug_swarm_results(lcf_ctx* ctx, double* out, int64_t max_rows) {
+    if (!ctx || !out) return LCF_E_INVALID;
+    int64_t rows = std::min<int64_t>(max_rows, (int64_t)ctx->n_bands * 44);
+    std::vector<PsoResult> h((size_t)std::max<int64_t>(rows, 1));
+    if (rows > 0) CK(cudaMemcpy(h.data(), ctx->res.p, (size_t)rows * sizeof(PsoResult), cudaMemcpyDeviceToHost));
+    for (int64_t r = 0; r < rows; r++) {
+        double* o = out + r * 21;
+        o[0] = h[r].iters < 0 ? std::nan("") : h[r].cost;
+        o[1] = h[r].iters;
+        o[2] = h[r].evals;
+        for (int j = 0; j < MB_MAXP; j++) o[3 + j] = h[r].params[j];
+    }
+    return 0;
+}
+
+extern "C" int lcf_probe_peaks(lcf_ctx* ctx, double* out2) {
+    if (!ctx || !out2) return LCF_E_INVALID;
+    CK(cudaSetDevice(ctx->device));
+    CK(cudaDeviceSynchronize());
+    out2[0] = probe_fp32_tflops(ctx->num_sms);
+    out2[1] = probe_mufu_gops(ctx->num_sms);
+    CK(cudaGetLastError());
     return 0;
 }
 

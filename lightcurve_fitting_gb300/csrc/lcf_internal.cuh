@@ -187,6 +187,8 @@ struct Counters {
     int32_t task_count[8];      // tasks appended by device task builders
     unsigned long long particle_obs_evals;
     unsigned long long ode_steps;
+    unsigned long long slot0_evals[12];      // particle x observation evaluations of the first PSO launch, by kind
+    unsigned long long slot0_particles[12];  // particle evaluations of the first PSO launch, by kind
     int32_t error;              // first error code raised on the device
     int32_t pad;
 };
@@ -253,6 +255,8 @@ void launch_svi(const DeviceBatch& d, cudaStream_t s);
 // finalize.cu
 void launch_laplace(const DeviceBatch& d, cudaStream_t s);
 void launch_refine(const DeviceBatch& d, cudaStream_t s);
+double probe_fp32_tflops(int num_sms);
+double probe_mufu_gops(int num_sms);
 void launch_band_cost(int model, const float4* obs, int n, float t_last, const double* params, int n_eval,
                       int with_prior, double* costs, float* scratch, cudaStream_t s);
 

@@ -604,6 +604,10 @@ __global__ void __launch_bounds__(256) pso_kernel(DeviceBatch d, int slot, int n
                 if (j < D) R.params[j] = g[j];
             atomicAdd(&d.ctr->particle_obs_evals, (unsigned long long)tot_evals * (unsigned long long)bs.n);
             if (t.kind == METZGER) atomicAdd(&d.ctr->ode_steps, (unsigned long long)tot_evals * MetzgerF::NG);
+            if (slot == 0 && t.kind < 12) {
+                atomicAdd(&d.ctr->slot0_evals[t.kind], (unsigned long long)tot_evals * (unsigned long long)bs.n);
+                atomicAdd(&d.ctr->slot0_particles[t.kind], (unsigned long long)tot_evals);
+            }
         }
         __syncwarp();
     }
@@ -647,6 +651,60 @@ void launch_band_cost(int model, const float4* obs, int n, float t_last, const d
     band_cost_kernel<<<(warps * 32 + 127) / 128, 128, 0, s>>>(model, obs, n, t_last, params, n_eval, with_prior,
                                                               costs, scratch);
 }
+
+// ---------------------------------------------------------------------------
+// Peak probes: dependent FMA chains (FP32 pipe) and ex2.approx chains (SFU
+// pipe), eight independent chains per thread, a full persistent grid.
+// ---------------------------------------------------------------------------
+__global__ void probe_fma_kernel(float* out, int iters) {
+    float a[8];
+    for (int k = 0; k < 8; k++) a[k] = threadIdx.x * 1e-7f + k;
+    const float m = 0.999999f, c = 1e-7f;
+    for (int i = 0; i < iters; i++) {
+#pragma unroll
+        for (int k = 0; k < 8; k++) a[k] = fmaf(a[k], m, c);
+    }
+    float s = 0.0f;
+    for (int k = 0; k < 8; k++) s += a[k];
+    if (s == 12345.0f) out[threadIdx.x] = s;
+}
+__global__ void probe_ex2_kernel(float* out, int iters) {
+    float a[8];
+    for (int k = 0; k < 8; k++) a[k] = -1e-3f * (threadIdx.x & 7) - 0.01f * k;
+    for (int i = 0; i < iters; i++) {
+#pragma unroll
+        for (int k = 0; k < 8; k++) {
+            float y;
+            asm volatile("ex2.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(a[k]));
+            a[k] = -y;
+        }
+    }
+    float s = 0.0f;
+    for (int k = 0; k < 8; k++) s += a[k];
+    if (s == 12345.0f) out[threadIdx.x] = s;
+}
+static double time_probe(void (*k)(float*, int), int num_sms, int iters) {
+    float* out = nullptr;
+    cudaMalloc(&out, 1024 * sizeof(float));
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    int grid = num_sms * 8, block = 256;
+    k<<<grid, block>>>(out, iters / 10);
+    cudaEventRecord(e0);
+    k<<<grid, block>>>(out, iters);
+    cudaEventRecord(e1);
+    cudaEventSynchronize(e1);
+    float ms = 0.0f;
+    cudaEventElapsedTime(&ms, e0, e1);
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    cudaFree(out);
+    double ops = (double)grid * block * 8.0 * iters;
+    return ms > 0.0f ? ops / (ms * 1e-3) : 0.0;
+}
+double probe_fp32_tflops(int num_sms) { return 2.0 * time_probe(probe_fma_kernel, num_sms, 1 << 16) * 1e-12; }
+double probe_mufu_gops(int num_sms) { return time_probe(probe_ex2_kernel, num_sms, 1 << 14) * 1e-9; }
 
 size_t pso_smem_bytes(int block, int smem_obs) {
     return (size_t)(block / 32) * ((size_t)smem_obs * sizeof(float4) + sizeof(WarpSmem));

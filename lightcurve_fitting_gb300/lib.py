@@ -46,6 +46,8 @@ def load(path: str = LIB_PATH):
     L.lcf_ctx_stream.restype = vp
     L.lcf_set_graph.argtypes = [vp, i]
     L.lcf_band_cost.argtypes = [vp, i, vp, vp, vp, vp, vp, i, vp, i, i, vp]
+    L.lcf_probe_peaks.argtypes = [vp, vp]
+    L.lcf_debug_swarm_results.argtypes = [vp, vp, C.c_int64]
     for name in ["launch_bazin", "launch_villar", "launch_tde", "launch_arnett", "launch_magnetar",
                  "launch_shock_cooling", "launch_afterglow", "launch_metzger_kn"]:
         getattr(L, name).argtypes = [vp, vp, vp, i, i, i, i, i]
@@ -128,7 +130,23 @@ class Context:
     def stats(self) -> dict:
         s = abi.FitStats()
         self._check(self.L.lcf_last_stats(self.h, C.byref(s)), "lcf_last_stats")
-        return {k: getattr(s, k) for k, _ in abi.FitStats._fields_}
+        out = {}
+        for k, _ in abi.FitStats._fields_:
+            v = getattr(s, k)
+            out[k] = list(v) if hasattr(v, "__len__") else v
+        return out
+
+    def probe_peaks(self) -> dict:
+        buf = np.zeros(2)
+        self._check(self.L.lcf_probe_peaks(self.h, buf.ctypes.data), "lcf_probe_peaks")
+        return {"fp32_tflops": float(buf[0]), "mufu_gops": float(buf[1])}
+
+    def swarm_results(self, n_bands: int) -> np.ndarray:
+        """Raw swarm results of the last fit: (44 * n_bands, 21) rows, see lcf.h."""
+        out = np.zeros((44 * n_bands, 21))
+        self._check(self.L.lcf_debug_swarm_results(self.h, out.ctypes.data, out.shape[0]),
+                    "lcf_debug_swarm_results")
+        return out
 
     def band_cost(self, model: int, times, flux, obs_var, is_upper, upper_flux, params, with_prior=True):
         """PsoCost::cost_from_slice for each row of ``params`` (FP32 kernel)."""
