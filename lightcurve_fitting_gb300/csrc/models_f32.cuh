@@ -69,26 +69,29 @@ __device__ __forceinline__ void split64(double v, float& hi, float& lo) {
 }
 
 struct BazinF {
-    float a, la, b, t0, t0lo, itr, itf;
+    // dif = 1/tau_fall - 1/tau_rise, formed as tr^-1 * expm1(ln tr - ln tf) so
+    // that the log-space slow path does not cancel two large exponents
+    float a, la, b, t0, t0lo, itr, itf, dif;
     __device__ void init(const float* p) {
         la = p[0]; a = expf(p[0]); b = p[1]; t0 = p[2]; t0lo = 0.0f; itr = expf(-p[3]); itf = expf(-p[4]);
+        dif = itr * expm1f(p[3] - p[4]);
     }
     __device__ void init64(const double* p) {
         la = (float)p[0]; a = (float)exp(p[0]); b = (float)p[1]; split64(p[2], t0, t0lo);
-        itr = (float)exp(-p[3]); itf = (float)exp(-p[4]);
+        itr = (float)exp(-p[3]); itf = (float)exp(-p[4]); dif = (float)(exp(-p[4]) - exp(-p[3]));
     }
     __device__ __forceinline__ float eval(float th, float tl, int& st) const {
         float dt = (th - t0) + (tl - t0lo);
         float xf = -dt * itf, xr = -dt * itr;
-        if (xf < 80.0f && xr < 80.0f) {
-            float ef = expf(xf);
-            float sig = 1.0f / (1.0f + expf(xr));
-            return a * ef * sig + b;
+        // FP64: a*e_fall overflows (-> non-finite) once la + xf > ln DBL_MAX,
+        // and the sigmoid is exactly 0 once xr > ln DBL_MAX
+        if (xf > 80.0f) {
+            if (xf > LN_DBL_MAX || la + xf > LN_DBL_MAX) { st = ST_NONFINITE; return 0.0f; }
+            if (xr > LN_DBL_MAX) return b;
         }
-        // FP64: a*e_fall overflows (-> non-finite) once la + xf > ln DBL_MAX
-        if (xf > LN_DBL_MAX || la + xf > LN_DBL_MAX) { st = ST_NONFINITE; return 0.0f; }
-        if (xr > LN_DBL_MAX) return b;  // sigmoid is exactly 0 in FP64
-        float L = la + xf - softplus_f(xr);
+        // ln(a e^xf / (1 + e^xr)) without cancellation: for xr > 0,
+        // xf - softplus(xr) = -dt*dif - log1p(e^-xr)
+        float L = la + (xr > 0.0f ? -dt * dif : xf) - log1pf(expf(-fabsf(xr)));
         if (L > BIG_L) { st = ST_BIG; return L; }
         return expf(L) + b;
     }
@@ -325,7 +328,7 @@ struct MetzgerF {
     // p: [log10 M_ej/Msun, log10 v_ej/c, log10 kappa, t0, log sigma_extra]
     template <class Obs>
     __device__ static bool sweep(const float* p, float t_last, const Obs& obs, int n, float* lv, int lv_stride,
-                                 float& l_peak_out, unsigned long long* steps) {
+                                 float& l_peak_out) {
         const float MSUN30 = 1.989e3f;      // Msun in 1e30 g
         const float C = 2.998e10f;
         const float SPD = 86400.0f;
@@ -394,7 +397,6 @@ struct MetzgerF {
         }
         // phases at or beyond the last grid point
         while (j < n) { lv[j * lv_stride] = prev_l; j++; }
-        if (steps) atomicAdd(steps, (unsigned long long)NG);
         l_peak_out = l_peak;
         return l_peak > 0.0f && isfinite(l_peak);
     }

@@ -64,6 +64,134 @@ __device__ inline double eval_model_f64(int m, const double* p, double t) {
     }
 }
 
+// Analytic d flux / d theta (src/parametric.rs:213-509), FP64; the
+// sigma_extra slot is 0.
+__device__ inline void model_grad_f64(int m, const double* p, double t, double* o) {
+    switch (m) {
+        case 0: {
+            double a = exp(p[0]), dt = t - p[2], tr = exp(p[3]), tf = exp(p[4]);
+            double sig = 1.0 / (1.0 + exp(-dt / tr));
+            double base = a * exp(-dt / tf) * sig;
+            o[0] = base; o[1] = 1.0;
+            o[2] = base * (1.0 / tf - (1.0 - sig) / tr);
+            o[3] = -base * (1.0 - sig) * dt / tr;
+            o[4] = base * dt / tf;
+            o[5] = 0.0;
+            return;
+        }
+        case 1: {
+            double a = exp(p[0]), beta = p[1], gamma = exp(p[2]), ph = t - p[3], tr = exp(p[4]), tf = exp(p[5]);
+            const double k = 10.0;
+            double sig = 1.0 / (1.0 + exp(-ph / tr));
+            double w = 1.0 / (1.0 + exp(-k * (ph - gamma)));
+            double pl = 1.0 - beta * ph;
+            double ed = exp((gamma - ph) / tf);
+            double pr = (1.0 - beta * gamma) * ed;
+            double piece = (1.0 - w) * pl + w * pr;
+            o[0] = a * sig * piece;
+            o[1] = a * sig * ((1.0 - w) * (-ph) + w * (-gamma * ed));
+            double dwdlg = -k * w * (1.0 - w) * gamma;
+            double dprdlg = ed * (-beta + (1.0 - beta * gamma) / tf) * gamma;
+            o[2] = a * sig * (dwdlg * (pr - pl) + w * dprdlg);
+            double dsig_dt0 = -(sig * (1.0 - sig) / tr);
+            double dw_dt0 = -(k * w * (1.0 - w));
+            double dpdt0 = dw_dt0 * (pr - pl) + (1.0 - w) * beta + w * ((1.0 - beta * gamma) * ed / tf);
+            o[3] = a * (dsig_dt0 * piece + sig * dpdt0);
+            o[4] = a * piece * sig * (1.0 - sig) * (-ph / tr);
+            o[5] = a * sig * w * (pr * (ph - gamma) / tf);
+            o[6] = 0.0;
+            return;
+        }
+        case 2: {
+            double a = exp(p[0]), ph = t - p[2], tr = exp(p[3]), tf = exp(p[4]), al = p[5];
+            double sig = 1.0 / (1.0 + exp(-ph / tr));
+            double ps = sp64(ph);
+            double sp = exp(ph) / (1.0 + exp(ph));
+            double w = 1.0 + ps / tf;
+            double decay = pow(w, -al);
+            o[0] = a * sig * decay; o[1] = 1.0;
+            double dsig_dt0 = -sig * (1.0 - sig) / tr;
+            double dd_dt0 = al * pow(w, -al - 1.0) * sp / tf;
+            o[2] = a * (dsig_dt0 * decay + sig * dd_dt0);
+            o[3] = a * decay * (-sig * (1.0 - sig) * ph / tr);
+            o[4] = a * sig * al * pow(w, -al - 1.0) * ps / tf;
+            o[5] = a * sig * (-log(w)) * decay;
+            o[6] = 0.0;
+            return;
+        }
+        case 3: {
+            double a = exp(p[0]), ph = t - p[1], tm = exp(p[2]);
+            double ps = sp64(ph);
+            double sp = exp(ph) / (1.0 + exp(ph));
+            double f = 1.0 / (1.0 + exp(-p[3]));
+            double eni = exp(-ps / 8.8), eco = exp(-ps / 111.3);
+            double heat = f * eni + (1.0 - f) * eco;
+            double x = ps / tm;
+            double ex2 = exp(-x * x);
+            double trap = 1.0 - ex2;
+            o[0] = a * heat * trap;
+            double dheat = -f * eni / 8.8 - (1.0 - f) * eco / 111.3;
+            double dtrap = 2.0 * ps * ex2 / (tm * tm);
+            o[1] = a * (-sp) * (dheat * trap + heat * dtrap);
+            o[2] = -2.0 * a * heat * ex2 * x * x;
+            o[3] = a * trap * (eni - eco) * f * (1.0 - f);
+            o[4] = 0.0;
+            return;
+        }
+        case 4: {
+            double a = exp(p[0]), ph = t - p[1], tsd = exp(p[2]), td = exp(p[3]);
+            double ps = sp64(ph);
+            double sp = exp(ph) / (1.0 + exp(ph));
+            double w = 1.0 + ps / tsd;
+            double sd = 1.0 / (w * w);
+            double x = ps / td;
+            double ex2 = exp(-x * x);
+            double trap = 1.0 - ex2;
+            o[0] = a * sd * trap;
+            double w3 = 1.0 / (w * w * w);
+            o[1] = a * (-sp) * ((-2.0 * w3 / tsd) * trap + sd * (2.0 * ps * ex2 / (td * td)));
+            o[2] = a * trap * 2.0 * ps * w3 / tsd;
+            o[3] = -2.0 * a * sd * ex2 * x * x;
+            o[4] = 0.0;
+            return;
+        }
+        case 5: {
+            double a = exp(p[0]), ph = t - p[1], n = p[2], ttr = exp(p[3]);
+            double sig5 = 1.0 / (1.0 + exp(-ph * 5.0));
+            double ps = sp64(ph);
+            double sp = exp(ph) / (1.0 + exp(ph));
+            double cooling = pow(ps, -n);
+            double r = ps / ttr;
+            double cutoff = exp(-r * r);
+            double base = cooling * cutoff;
+            double flux = a * sig5 * base;
+            o[0] = flux;
+            o[1] = a * base * (-5.0 * sig5 * (1.0 - sig5) + sig5 * sp * (n / ps + 2.0 * ps / (ttr * ttr)));
+            o[2] = -flux * log(ps);
+            o[3] = flux * 2.0 * r * r;
+            o[4] = 0.0;
+            return;
+        }
+        default: {
+            double a = exp(p[0]), ph = t - p[1], tb = exp(p[2]), a1 = p[3], a2 = p[4];
+            double ps = sp64(ph);
+            double sp = exp(ph) / (1.0 + exp(ph));
+            double lr = log(ps / tb);
+            double u1 = exp(2.0 * a1 * lr), u2 = exp(2.0 * a2 * lr);
+            double u = u1 + u2;
+            double um15 = pow(u, -1.5);
+            o[0] = a * pow(u, -0.5);
+            double du_dps = (2.0 * a1 * u1 + 2.0 * a2 * u2) / ps;
+            o[1] = a * (-0.5) * um15 * du_dps * (-sp);
+            o[2] = a * (-0.5) * um15 * (-(2.0 * a1 * u1 + 2.0 * a2 * u2));
+            o[3] = a * (-0.5) * um15 * 2.0 * lr * u1;
+            o[4] = a * (-0.5) * um15 * 2.0 * lr * u2;
+            o[5] = 0.0;
+            return;
+        }
+    }
+}
+
 __device__ __forceinline__ double erf_approx_f64(double x) {
     double a = fabs(x);
     double t = 1.0 / (1.0 + 0.3275911 * a);

@@ -79,74 +79,83 @@ __device__ double warp_nll(int m, const double* pd, const float4* obs, int n, do
 }
 
 struct LbCtx {
-    const float4* obs;
+    const double *t, *f, *var, *uf;
+    const uint8_t* up;
     int n, m, np;
     double nd;
     double lo[MAXP], hi[MAXP];
-    int aborted;   // a gradient hit the reference's 1e-300 CDF floor
 };
 
 // Cost and projected gradient of the bounded problem (BoundedPsoCost,
-// src/parametric.rs:1500-1535) at x.
+// src/parametric.rs:1500-1535) at x, in FP64 with the lanes over the
+// observations: PsoCost::cost_from_slice (with the population prior and the
+// Villar constraint) and PsoCost::gradient (without either).  The polish runs
+// in the reference's arithmetic because its acceptance tests (descent
+// direction, sufficient decrease, curvature) compare quantities that are
+// differences of near-equal costs and gradients near the optimum.
 __device__ void lb_cost_grad(LbCtx& c, const double* x, double& f, double* g, bool want_grad) {
-    float p[MAXP];
     double q[MAXP];
-    for (int j = 0; j < c.np; j++) {
-        q[j] = fmin(fmax(x[j], c.lo[j]), c.hi[j]);
-        p[j] = (float)q[j];
-    }
-    // cost: PsoCost::cost_from_slice with the population prior
+    for (int j = 0; j < c.np; j++) q[j] = fmin(fmax(x[j], c.lo[j]), c.hi[j]);
+    const int lane = threadIdx.x & 31;
+    const int se = se_idx_of(c.m);
+    const double se2 = exp(2.0 * q[se]);
     bool constrained = false;
     if (c.m == VILLAR) {
-        float cv = VillarF::constraint(p);
-        if (cv > 0.0f) { f = 1e12 + 10000.0 * (double)cv; constrained = true; }
+        double beta = q[1], gamma = exp(q[2]), tr = exp(q[4]), tf = exp(q[5]);
+        double c1 = fmax(gamma * beta - 1.0, 0.0);
+        double c2 = fmax(exp(-gamma / tr) * (tf / tr - 1.0) - 1.0, 0.0);
+        double c3 = fmax(beta * tf - 1.0 + beta * gamma, 0.0);
+        double cc = c1 + c2 + c3;
+        if (cc > 0.0) { f = 1e12 + 10000.0 * cc; constrained = true; }
     }
-    if (!constrained) {
-        double prior = 0.0;
-        for (int j = 0; j < c.np; j++) {
-            double w = c_pop_w[c.m][j];
-            if (w > 0.0) {
-                double z = (q[j] - c_pop_c[c.m][j]) / w;
-                prior += 0.5 * z * z;
-            }
-        }
-        f = warp_nll(c.m, q, c.obs, c.n, c.nd, prior);
-    }
-    if (!want_grad) return;
-    // gradient: PsoCost::gradient (no prior, no constraint term)
-    int lane = threadIdx.x & 31;
-    int se = se_idx_of(c.m);
-    float sx = expf(p[se]);
-    float se2 = sx * sx;
-    float gl[MAXP];
-    for (int j = 0; j < MAXP; j++) gl[j] = 0.0f;
-    int nonfinite = 0, huge = 0;
+    double nll = 0.0, gl[MAXP];
+    for (int j = 0; j < MAXP; j++) gl[j] = 0.0;
+    int nonfinite = 0;
     for (int i = lane; i < c.n; i += 32) {
-        float4 o = c.obs[i];
-        float mg[MAXP];
-        int st;
-        float pr = model_grad_f32(c.m, p, o.x, o.y, mg, st);
-        if (st == ST_NONFINITE) { nonfinite = 1; continue; }
-        float tv = fabsf(o.w) + se2;
-        if (o.w < 0.0f) {
-            float sv = sqrtf(tv);
-            float z = (o.z - pr) / sv;
-            bool hg;
-            float ratio = upper_ratio_f32(z, hg);
-            if (hg) huge = 1;
-            for (int j = 0; j < c.np; j++) gl[j] += ratio * mg[j] / sv;
-            gl[se] += ratio * z * se2 / tv;
+        double mg[MAXP];
+        double pr = eval_model_f64(c.m, q, c.t[i]);
+        if (want_grad) model_grad_f64(c.m, q, c.t[i], mg);
+        if (!isfinite(pr)) { nonfinite = 1; continue; }
+        double tv = c.var[i] + se2;
+        if (c.up[i]) {
+            double sv = sqrt(tv);
+            double z = (c.uf[i] - pr) / sv;
+            nll -= log_normal_cdf_f64(z);
+            if (want_grad) {
+                double phi = exp(-0.5 * z * z) / sqrt(2.0 * 3.14159265358979323846);
+                double cdf = 0.5 * (1.0 + erf_approx_f64(z / 1.41421356237309504880));
+                double ratio = phi / fmax(cdf, 1e-300);
+                for (int j = 0; j < c.np; j++) gl[j] += ratio * mg[j] / sv;
+                gl[se] += ratio * z * se2 / tv;
+            }
         } else {
-            float dd = pr - o.z;
-            float sc = 2.0f * dd / tv;
-            for (int j = 0; j < c.np; j++) gl[j] += sc * mg[j];
-            gl[se] += (-dd * dd / (tv * tv) + 1.0f / tv) * (2.0f * se2);
+            double d = pr - c.f[i];
+            nll += d * d / tv + log(tv);
+            if (want_grad) {
+                double sc = 2.0 * d / tv;
+                for (int j = 0; j < c.np; j++) gl[j] += sc * mg[j];
+                gl[se] += (-d * d / (tv * tv) + 1.0 / tv) * (2.0 * se2);
+            }
         }
     }
     nonfinite = warp_or(nonfinite);
-    if (warp_or(huge)) c.aborted = 1;
+    if (!constrained) {
+        if (nonfinite) f = BIG_COST;
+        else {
+            double prior = 0.0;
+            for (int j = 0; j < c.np; j++) {
+                double w = c_pop_w[c.m][j];
+                if (w > 0.0) {
+                    double z = (q[j] - c_pop_c[c.m][j]) / w;
+                    prior += 0.5 * z * z;
+                }
+            }
+            f = (warp_sum_d(nll) + prior / c.nd) / c.nd;
+        }
+    }
+    if (!want_grad) return;
     for (int j = 0; j < c.np; j++) {
-        double gj = (double)warp_sum_f(gl[j]);
+        double gj = warp_sum_d(gl[j]);
         g[j] = nonfinite ? 0.0 : gj / c.nd;
     }
     for (int j = 0; j < c.np; j++)
@@ -300,7 +309,6 @@ __device__ double lbfgs_polish(LbCtx& c, double* params, double pso_cost) {
     const double tol_grad = 1e-6, tol_cost = 2.220446049250313e-16;
     double x[MAXP], g[MAXP], f;
     for (int i = 0; i < n; i++) x[i] = params[i];
-    c.aborted = 0;
     lb_cost_grad(c, x, f, g, true);
     double best_x[MAXP], best_f = INFINITY, prev_f = INFINITY;
     if (f < best_f) { best_f = f; for (int i = 0; i < n; i++) best_x[i] = x[i]; }
@@ -310,7 +318,7 @@ __device__ double lbfgs_polish(LbCtx& c, double* params, double pso_cost) {
     bool ok = true;
     auto converged = [&]() { return sqrt(dotn(g, g, n)) < tol_grad || fabs(prev_f - f) < tol_cost; };
     bool stop = converged() || it >= MAXIT;
-    while (!stop && !c.aborted) {
+    while (!stop) {
         double gamma = 1.0;
         if (cm > 0) {
             int last = (head + cm - 1) % M;
@@ -346,7 +354,7 @@ __device__ double lbfgs_polish(LbCtx& c, double* params, double pso_cost) {
         it++;
         stop = converged() || it >= MAXIT;
     }
-    if (!ok || c.aborted) return pso_cost;
+    if (!ok) return pso_cost;
     double cl[MAXP], fc, gdummy[MAXP];
     for (int i = 0; i < n; i++) cl[i] = fmin(fmax(best_x[i], c.lo[i]), c.hi[i]);
     lb_cost_grad(c, cl, fc, gdummy, false);
@@ -377,7 +385,11 @@ __global__ void lbfgs_kernel(DeviceBatch d, int model_mask) {
     double cost = best_c;
     if (m != METZGER && best_r >= 0) {
         LbCtx c;
-        c.obs = d.obs + bs.off;
+        c.t = d.t64 + bs.off;
+        c.f = d.f64 + bs.off;
+        c.var = d.var64 + bs.off;
+        c.uf = d.uf64 + bs.off;
+        c.up = d.up + bs.off;
         c.n = bs.n;
         c.m = m;
         c.np = np;

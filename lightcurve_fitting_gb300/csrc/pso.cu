@@ -220,14 +220,14 @@ __device__ __forceinline__ Nll nll_loop(const M& m, const float4* obs, int n, fl
 // MultiBazin prediction: sum of K Bazin components + B (src/parametric.rs:932-940)
 template <int K>
 __device__ __forceinline__ Nll nll_multibazin(const float* p, const float4* obs, int n, float se2) {
-    float a[K], la[K], t0[K], itr[K], itf[K];
+    float la[K], t0[K], itr[K], itf[K], dif[K];
 #pragma unroll
     for (int c = 0; c < K; c++) {
         la[c] = p[4 * c];
-        a[c] = expf(la[c]);
         t0[c] = p[4 * c + 1];
         itr[c] = expf(-p[4 * c + 2]);
         itf[c] = expf(-p[4 * c + 3]);
+        dif[c] = itr[c] * expm1f(p[4 * c + 2] - p[4 * c + 3]);
     }
     float B = p[4 * K];
     Nll acc;
@@ -238,17 +238,16 @@ __device__ __forceinline__ Nll nll_multibazin(const float* p, const float4* obs,
         int st = ST_OK;
 #pragma unroll
         for (int c = 0; c < K; c++) {
+            // one Bazin component in log space (as BazinF::eval)
             float dt = (o.x - t0[c]) + o.y;
             float xf = -dt * itf[c], xr = -dt * itr[c];
-            if (xf < 80.0f && xr < 80.0f) {
-                sum += a[c] * expf(xf) / (1.0f + expf(xr));
-            } else if (xf > LN_DBL_MAX || la[c] + xf > LN_DBL_MAX) {
-                st = ST_NONFINITE;
-            } else if (xr <= LN_DBL_MAX) {
-                float L = la[c] + xf - softplus_f(xr);
-                if (L > BIG_L) bigL = fmaxf(bigL, L) + log1pf(expf(-fabsf(bigL - L)));
-                else sum += expf(L);
+            if (xf > 80.0f) {
+                if (xf > LN_DBL_MAX || la[c] + xf > LN_DBL_MAX) { st = ST_NONFINITE; continue; }
+                if (xr > LN_DBL_MAX) continue;  // exact zero in FP64
             }
+            float L = la[c] + (xr > 0.0f ? -dt * dif[c] : xf) - log1pf(expf(-fabsf(xr)));
+            if (L > BIG_L) bigL = fmaxf(bigL, L) + log1pf(expf(-fabsf(bigL - L)));
+            else sum += expf(L);
         }
         float pr = 0.0f;
         if (st == ST_OK && bigL > -INFINITY) {
@@ -335,7 +334,7 @@ __device__ double particle_cost(const TaskCtx& t, const float* x, const double* 
             int lane = threadIdx.x & 31;
             float* lv = t.mscratch + lane;
             float l_peak = 0.0f;
-            bool ok = MetzgerF::sweep(p, t.t_last, ot, t.n, lv, 32, l_peak, nullptr);
+            bool ok = MetzgerF::sweep(p, t.t_last, ot, t.n, lv, 32, l_peak);
             acc.reset();
             float scale = 1.0f;
             if (ok) {
