@@ -51,8 +51,12 @@ struct Predictor {
     int m;
     const double* p;
     const double* scr;
+    Model64 mod;
+    __device__ Predictor(int m_, const double* p_, const double* s_) : m(m_), p(p_), scr(s_) {
+        if (m != 7) mod.init(m, p);
+    }
     __device__ double operator()(const BandView& b, int i) const {
-        return m == 7 ? scr[i] : eval_model_f64(m, p, b.t[i]);
+        return m == 7 ? scr[i] : mod.eval(b.t[i], nullptr);
     }
 };
 __device__ void metzger_prepare(int m, const double* p, const BandView& b, double* scr) {
@@ -76,7 +80,7 @@ __device__ double metzger_scale(const Predictor& P, const BandView& b) {
 __device__ double neg_log_posterior_w(int m, const BandView& b, const double* p, double* scr) {
     int lane = threadIdx.x & 31;
     metzger_prepare(m, p, b, scr);
-    Predictor P{m, p, scr};
+    Predictor P(m, p, scr);
     double scale = m == 7 ? metzger_scale(P, b) : 1.0;
     double se2 = exp(2.0 * p[se_idx_of(m)]);
     double nll = 0.0;
@@ -107,7 +111,7 @@ __device__ double neg_log_posterior_w(int m, const BandView& b, const double* p,
 __device__ double band_ll_w(int m, const BandView& b, const double* p, double* scr, bool metzger_rescale) {
     int lane = threadIdx.x & 31;
     metzger_prepare(m, p, b, scr);
-    Predictor P{m, p, scr};
+    Predictor P(m, p, scr);
     double scale = (m == 7 && metzger_rescale) ? metzger_scale(P, b) : 1.0;
     double se2 = exp(2.0 * p[se_idx_of(m)]);
     double ll = 0.0;
@@ -260,7 +264,7 @@ __global__ void refine_kernel(DeviceBatch d) {
                 double saved_b = 0.0;
                 if (has_b) { saved_b = p[1]; p[1] = 0.0; }
                 metzger_prepare(m, p, b, scr);
-                Predictor P{m, p, scr};
+                Predictor P(m, p, scr);
                 double sw = 0, sy = 0, sf = 0, syf = 0, sff = 0;
                 for (int i = lane; i < b.n; i += 32) {
                     double sh = P(b, i);
@@ -337,7 +341,7 @@ __global__ void refine_kernel(DeviceBatch d) {
     int mcount = 0;
     {
         metzger_prepare(m, mu, b, scr);
-        Predictor P{m, mu, scr};
+        Predictor P(m, mu, scr);
         int npos = 0;
         for (int i = lane; i < b.n; i += 32) npos += (P(b, i) * b.peak > 0.0) ? 1 : 0;
         for (int k = 16; k; k >>= 1) npos += __shfl_xor_sync(FULL, npos, k);
@@ -349,7 +353,7 @@ __global__ void refine_kernel(DeviceBatch d) {
             use = pso;
         }
         metzger_prepare(m, use, b, scr);
-        Predictor Q{m, use, scr};
+        Predictor Q(m, use, scr);
         for (int i = lane; i < b.n; i += 32) {
             double pf = Q(b, i) * b.peak;
             if (pf > 0.0 && b.f[i] > 0.0) {

@@ -379,12 +379,21 @@ static int prepare_layout(lcf_ctx* ctx, int n_sources, int n_bands, int64_t n_ob
                     T.push_back(t);
                 }
         }
+        // Queue order: grouped by task kind so that the warps resident on an
+        // SM at any moment run the same model's code (one kind's loop stays in
+        // the instruction cache), the costliest kind (MetzgerKN) first, and
+        // longest bands first within a kind (longest-processing-time order).
         std::vector<double> key(T.size());
         for (size_t i = 0; i < T.size(); i++)
             key[i] = task_cost(T[i].kind, (int)(ctx->h_boff[T[i].band + 1] - ctx->h_boff[T[i].band]));
+        auto group = [](int kind) { return kind == METZGER ? 0 : 1 + kind; };
         std::vector<size_t> ord(T.size());
         for (size_t i = 0; i < ord.size(); i++) ord[i] = i;
-        std::stable_sort(ord.begin(), ord.end(), [&](size_t a, size_t b) { return key[a] > key[b]; });
+        std::stable_sort(ord.begin(), ord.end(), [&](size_t a, size_t b) {
+            int ga = group(T[a].kind), gb = group(T[b].kind);
+            if (ga != gb) return ga < gb;
+            return key[a] > key[b];
+        });
         std::vector<PsoTask> S(T.size());
         for (size_t i = 0; i < ord.size(); i++) S[i] = T[ord[i]];
         T.swap(S);

@@ -108,14 +108,17 @@ struct VillarF {
         itr = (float)exp(-p[4]); itf = (float)exp(-p[5]); omb = (float)(1.0 - p[1] * exp(p[2]));
     }
     __device__ __forceinline__ float eval(float th, float tl, int& st) const {
-        // Within the Villar box every exponent stays below 70, so FP32 holds
-        // the FP64 result without special cases.
+        // piece = (1 - w) (1 - beta ph) + w (1 - beta gamma) e^{u / tau_f},
+        // u = gamma - ph, w = 1 / (1 + e^{10 u}).  The product w e^{u/tau_f}
+        // is written as 1 / (e^{-u/tau_f} + e^{u (10 - 1/tau_f)}), whose
+        // exponentials overflow only towards the correct limit 0 (FP64 forms
+        // 0 * finite there), for any t0.
         float ph = (th - t0) + (tl - t0lo);
+        float u = gamma - ph;
         float sig = 1.0f / (1.0f + expf(-ph * itr));
-        float w = 1.0f / (1.0f + expf(-10.0f * (ph - gamma)));
-        float pl = 1.0f - beta * ph;
-        float pr = omb * expf((gamma - ph) * itf);
-        return a * sig * ((1.0f - w) * pl + w * pr);
+        float omw = 1.0f / (1.0f + expf(-10.0f * u));
+        float wed = 1.0f / (expf(-u * itf) + expf(u * (10.0f - itf)));
+        return a * sig * (omw * (1.0f - beta * ph) + omb * wed);
     }
     // Villar physical constraint of PsoCost, src/parametric.rs:1305-1318
     __device__ static float constraint(const float* p) {

@@ -192,6 +192,169 @@ __device__ inline void model_grad_f64(int m, const double* p, double t, double* 
     }
 }
 
+// Hoisted FP64 evaluator: the per-parameter-vector constants (exponentials of
+// the log parameters, reciprocals) are formed once in init(); value() and
+// value_grad() then spend only the per-observation transcendentals.  Same
+// formulas as eval_model_f64 / model_grad_f64 (dividing by tau and
+// multiplying by 1/tau differ by at most one rounding).
+struct Model64 {
+    int m;
+    double c[12];
+    __device__ void init(int model, const double* p) {
+        m = model;
+        switch (m) {
+            case 0: c[0] = exp(p[0]); c[1] = p[1]; c[2] = p[2]; c[3] = 1.0 / exp(p[3]); c[4] = 1.0 / exp(p[4]); break;
+            case 1: c[0] = exp(p[0]); c[1] = p[1]; c[2] = exp(p[2]); c[3] = p[3]; c[4] = 1.0 / exp(p[4]);
+                    c[5] = 1.0 / exp(p[5]); c[6] = 1.0 - p[1] * exp(p[2]); break;
+            case 2: c[0] = exp(p[0]); c[1] = p[1]; c[2] = p[2]; c[3] = 1.0 / exp(p[3]); c[4] = 1.0 / exp(p[4]);
+                    c[5] = p[5]; break;
+            case 3: c[0] = exp(p[0]); c[1] = p[1]; c[2] = 1.0 / exp(p[2]); c[3] = 1.0 / (1.0 + exp(-p[3])); break;
+            case 4: c[0] = exp(p[0]); c[1] = p[1]; c[2] = 1.0 / exp(p[2]); c[3] = 1.0 / exp(p[3]); break;
+            case 5: c[0] = exp(p[0]); c[1] = p[1]; c[2] = p[2]; c[3] = 1.0 / exp(p[3]); break;
+            default: c[0] = exp(p[0]); c[1] = p[1]; c[2] = p[2]; c[3] = p[3]; c[4] = p[4]; break;
+        }
+    }
+    // prediction; with g != nullptr also d pred / d theta (sigma_extra slot 0)
+    __device__ double eval(double t, double* g) const {
+        switch (m) {
+            case 0: {
+                double a = c[0], dt = t - c[2], itr = c[3], itf = c[4];
+                double sig = 1.0 / (1.0 + exp(-dt * itr));
+                double base = a * exp(-dt * itf) * sig;
+                if (g) {
+                    g[0] = base; g[1] = 1.0;
+                    g[2] = base * (itf - (1.0 - sig) * itr);
+                    g[3] = -base * (1.0 - sig) * dt * itr;
+                    g[4] = base * dt * itf;
+                    g[5] = 0.0;
+                }
+                return base + c[1];
+            }
+            case 1: {
+                double a = c[0], beta = c[1], gamma = c[2], ph = t - c[3], itr = c[4], itf = c[5], omb = c[6];
+                double sig = 1.0 / (1.0 + exp(-ph * itr));
+                double w = 1.0 / (1.0 + exp(-10.0 * (ph - gamma)));
+                double pl = 1.0 - beta * ph;
+                double ed = exp((gamma - ph) * itf);
+                double pr = omb * ed;
+                double piece = (1.0 - w) * pl + w * pr;
+                if (g) {
+                    const double k = 10.0;
+                    g[0] = a * sig * piece;
+                    g[1] = a * sig * ((1.0 - w) * (-ph) + w * (-gamma * ed));
+                    g[2] = a * sig * ((-k * w * (1.0 - w) * gamma) * (pr - pl) + w * (ed * (-beta + omb * itf) * gamma));
+                    double dpdt0 = (-(k * w * (1.0 - w))) * (pr - pl) + (1.0 - w) * beta + w * (omb * ed * itf);
+                    g[3] = a * ((-(sig * (1.0 - sig) * itr)) * piece + sig * dpdt0);
+                    g[4] = a * piece * sig * (1.0 - sig) * (-ph * itr);
+                    g[5] = a * sig * w * (pr * (ph - gamma) * itf);
+                    g[6] = 0.0;
+                }
+                return a * sig * piece;
+            }
+            case 2: {
+                double a = c[0], ph = t - c[2], itr = c[3], itf = c[4], al = c[5];
+                double sig = 1.0 / (1.0 + exp(-ph * itr));
+                double eph = exp(ph);
+                double ps = log(1.0 + eph) + 1e-6;
+                double w = 1.0 + ps * itf;
+                double lw = log(w);
+                double decay = exp(-al * lw);
+                if (g) {
+                    double sp = eph / (1.0 + eph);
+                    double wm1 = decay / w;
+                    g[0] = a * sig * decay; g[1] = 1.0;
+                    g[2] = a * ((-sig * (1.0 - sig) * itr) * decay + sig * (al * wm1 * sp * itf));
+                    g[3] = a * decay * (-sig * (1.0 - sig) * ph * itr);
+                    g[4] = a * sig * al * wm1 * ps * itf;
+                    g[5] = a * sig * (-lw) * decay;
+                    g[6] = 0.0;
+                }
+                return a * sig * decay + c[1];
+            }
+            case 3: {
+                double a = c[0], ph = t - c[1], itm = c[2], f = c[3];
+                double eph = exp(ph);
+                double ps = log(1.0 + eph) + 1e-6;
+                double eni = exp(-ps / 8.8), eco = exp(-ps / 111.3);
+                double heat = f * eni + (1.0 - f) * eco;
+                double x = ps * itm;
+                double ex2 = exp(-x * x);
+                double trap = 1.0 - ex2;
+                if (g) {
+                    double sp = eph / (1.0 + eph);
+                    g[0] = a * heat * trap;
+                    double dheat = -f * eni / 8.8 - (1.0 - f) * eco / 111.3;
+                    double dtrap = 2.0 * ps * ex2 * itm * itm;
+                    g[1] = a * (-sp) * (dheat * trap + heat * dtrap);
+                    g[2] = -2.0 * a * heat * ex2 * x * x;
+                    g[3] = a * trap * (eni - eco) * f * (1.0 - f);
+                    g[4] = 0.0;
+                }
+                return a * heat * trap;
+            }
+            case 4: {
+                double a = c[0], ph = t - c[1], itsd = c[2], itd = c[3];
+                double eph = exp(ph);
+                double ps = log(1.0 + eph) + 1e-6;
+                double w = 1.0 + ps * itsd;
+                double sd = 1.0 / (w * w);
+                double x = ps * itd;
+                double ex2 = exp(-x * x);
+                double trap = 1.0 - ex2;
+                if (g) {
+                    double sp = eph / (1.0 + eph);
+                    double w3 = sd / w;
+                    g[0] = a * sd * trap;
+                    g[1] = a * (-sp) * ((-2.0 * w3 * itsd) * trap + sd * (2.0 * ps * ex2 * itd * itd));
+                    g[2] = a * trap * 2.0 * ps * w3 * itsd;
+                    g[3] = -2.0 * a * sd * ex2 * x * x;
+                    g[4] = 0.0;
+                }
+                return a * sd * trap;
+            }
+            case 5: {
+                double a = c[0], ph = t - c[1], n = c[2], ittr = c[3];
+                double sig5 = 1.0 / (1.0 + exp(-ph * 5.0));
+                double eph = exp(ph);
+                double ps = log(1.0 + eph) + 1e-6;
+                double lps = log(ps);
+                double r = ps * ittr;
+                double base = exp(-n * lps) * exp(-r * r);
+                double flux = a * sig5 * base;
+                if (g) {
+                    double sp = eph / (1.0 + eph);
+                    g[0] = flux;
+                    g[1] = a * base * (-5.0 * sig5 * (1.0 - sig5) + sig5 * sp * (n / ps + 2.0 * ps * ittr * ittr));
+                    g[2] = -flux * lps;
+                    g[3] = flux * 2.0 * r * r;
+                    g[4] = 0.0;
+                }
+                return flux;
+            }
+            default: {
+                double a = c[0], ph = t - c[1], ltb = c[2], a1 = c[3], a2 = c[4];
+                double eph = exp(ph);
+                double ps = log(1.0 + eph) + 1e-6;
+                double lr = log(ps) - ltb;
+                double u1 = exp(2.0 * a1 * lr), u2 = exp(2.0 * a2 * lr);
+                double u = u1 + u2;
+                double iu = 1.0 / sqrt(u);
+                if (g) {
+                    double sp = eph / (1.0 + eph);
+                    double um15 = iu / u;
+                    g[0] = a * iu;
+                    g[1] = a * (-0.5) * um15 * ((2.0 * a1 * u1 + 2.0 * a2 * u2) / ps) * (-sp);
+                    g[2] = a * (-0.5) * um15 * (-(2.0 * a1 * u1 + 2.0 * a2 * u2));
+                    g[3] = a * (-0.5) * um15 * 2.0 * lr * u1;
+                    g[4] = a * (-0.5) * um15 * 2.0 * lr * u2;
+                    g[5] = 0.0;
+                }
+                return a * iu;
+            }
+        }
+    }
+};
+
 __device__ __forceinline__ double erf_approx_f64(double x) {
     double a = fabs(x);
     double t = 1.0 / (1.0 + 0.3275911 * a);

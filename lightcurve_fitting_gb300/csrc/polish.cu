@@ -111,10 +111,11 @@ __device__ void lb_cost_grad(LbCtx& c, const double* x, double& f, double* g, bo
     double nll = 0.0, gl[MAXP];
     for (int j = 0; j < MAXP; j++) gl[j] = 0.0;
     int nonfinite = 0;
+    Model64 mod;
+    mod.init(c.m, q);
     for (int i = lane; i < c.n; i += 32) {
         double mg[MAXP];
-        double pr = eval_model_f64(c.m, q, c.t[i]);
-        if (want_grad) model_grad_f64(c.m, q, c.t[i], mg);
+        double pr = mod.eval(c.t[i], want_grad ? mg : nullptr);
         if (!isfinite(pr)) { nonfinite = 1; continue; }
         double tv = c.var[i] + se2;
         if (c.up[i]) {
