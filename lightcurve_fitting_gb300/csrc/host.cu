@@ -106,7 +106,7 @@ struct lcf_ctx {
     float* d_eps = nullptr;
     // device buffers (capacity-sized)
     DevArr times, flux, ferr, boff, soff, stats_b, obs, t64, f64, fe64, var64, uf64, mag64, up, res, fits, out, mb,
-        ctr, scratch, scratch64, t0state, tasks[7];
+        ctr, scratch, scratch64, scratch_svi, t0state, tasks[7];
     int64_t task_cap[7] = {0, 0, 0, 0, 0, 0, 0};
     // pinned staging
     DevArr h_in, h_out;
@@ -232,7 +232,8 @@ extern "C" void lcf_ctx_destroy(lcf_ctx* ctx) {
     if (ctx->graph) cudaGraphExecDestroy(ctx->graph);
     DevArr* all[] = {&ctx->times, &ctx->flux, &ctx->ferr, &ctx->boff, &ctx->soff, &ctx->stats_b, &ctx->obs,
                      &ctx->t64, &ctx->f64, &ctx->fe64, &ctx->var64, &ctx->uf64, &ctx->mag64, &ctx->up, &ctx->res,
-                     &ctx->fits, &ctx->out, &ctx->mb, &ctx->ctr, &ctx->scratch, &ctx->scratch64, &ctx->t0state,
+                     &ctx->fits, &ctx->out, &ctx->mb, &ctx->ctr, &ctx->scratch, &ctx->scratch64, &ctx->scratch_svi,
+                     &ctx->t0state,
                      &ctx->bc_obs, &ctx->bc_params, &ctx->bc_costs, &ctx->bc_scratch};
     for (DevArr* a : all) free_arr(*a);
     for (auto& a : ctx->tasks) free_arr(a);
@@ -331,6 +332,7 @@ static int prepare_layout(lcf_ctx* ctx, int n_sources, int n_bands, int64_t n_ob
     rc |= grow(ctx, ctx->mb, nb * sizeof(MbState));
     rc |= grow(ctx, ctx->ctr, sizeof(Counters));
     rc |= grow(ctx, ctx->scratch64, no * 5 * 8);
+    rc |= grow(ctx, ctx->scratch_svi, no * 20 * sizeof(float));
     rc |= grow(ctx, ctx->t0state, nb * 3 * 8);
     int grid_pso = ctx->num_sms * ctx->pso_blocks_per_sm;
     size_t warps = (size_t)grid_pso * (ctx->pso_block / 32);
@@ -442,6 +444,7 @@ static int prepare_layout(lcf_ctx* ctx, int n_sources, int n_bands, int64_t n_ob
     d.scratch = (float*)ctx->scratch.p;
     d.scratch_per_warp = 32 * n_max;
     d.scratch64 = (double*)ctx->scratch64.p;
+    d.scratch_svi = (float*)ctx->scratch_svi.p;
     d.t0_state = (double*)ctx->t0state.p;
     d.t0_slot_base = (int64_t)n_bands * 24;
     d.mb_slot_base = (int64_t)n_bands * 32;

@@ -226,6 +226,7 @@ struct DeviceBatch {
     float* scratch;         // MetzgerKN per-warp scratch: [warps][n_max][32]
     int64_t scratch_per_warp;
     double* scratch64;      // FP64 scratch, 5 values per observation
+    float* scratch_svi;     // MetzgerKN SVI scratch, 20 values per observation
     double* t0_state;       // per band: t0_min, t0_max, best t0 of the profile search
     int64_t t0_slot_base;   // first PsoResult slot of the t0 search region
     int64_t mb_slot_base;   // first PsoResult slot of the MultiBazin region

@@ -21,6 +21,7 @@
 #include "grads_f32.cuh"
 #include "lcf_internal.cuh"
 #include "models_f32.cuh"
+#include "metzger_dual.cuh"
 #include "models_f64.cuh"
 
 namespace lcf {
@@ -456,23 +457,6 @@ void launch_select(const DeviceBatch& d, int fit_all, int forced, cudaStream_t s
 // ---------------------------------------------------------------------------
 // SVI, one warp per band
 // ---------------------------------------------------------------------------
-// MetzgerKN: predictions and forward-difference gradients in FP64
-// (metzger_kn_grad_batch_into, src/parametric.rs:843-860).  Lane j < 5
-// solves the model at theta + 1e-5 e_j (lane 4: the base point) over the
-// band into scratch; lanes then read them per observation.
-__device__ bool metzger_svi_sample(const double* th, const double* t64, int n, double* scr, double* pred_out) {
-    int lane = threadIdx.x & 31;
-    if (lane < 5) {
-        double pp[5];
-        for (int q = 0; q < 5; q++) pp[q] = th[q];
-        if (lane < 4) pp[lane] += 1e-5;
-        metzger_f64(pp, t64, n, scr + (size_t)lane * n);
-    }
-    __syncwarp();
-    (void)pred_out;
-    return true;
-}
-
 __global__ void svi_kernel(DeviceBatch d) {
     const int lane = threadIdx.x & 31;
     const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
@@ -501,8 +485,12 @@ __global__ void svi_kernel(DeviceBatch d) {
     double b1t = 1.0, b2t = 1.0;
     double ema = -INFINITY, best_ema = -INFINITY, final_elbo = -INFINITY;
     int no_imp = 0, steps = 0;
-    double* scr = d.scratch64 + 5 * bs.off;
-    const double* t64 = d.t64 + bs.off;
+    // MetzgerKN: per step, lanes 0..3 sweep samples 0..3 (value + 4 derivatives per observation)
+    float* mscr = d.scratch_svi + 20 * bs.off;
+    struct ObsTimes {
+        const float4* o;
+        __device__ float operator()(int j) const { return o[j].x + o[j].y; }
+    } otimes{obs};
     for (int step = 0; step < SVI_STEPS; step++) {
         steps = step + 1;
         double mu[MAXP], sg[MAXP];
@@ -514,6 +502,15 @@ __global__ void svi_kernel(DeviceBatch d) {
         for (int j = 0; j < np; j++) { gmu[j] = 0.0; gls[j] = 0.0; }
         double elbo_sum = 0.0;
         int huge_any = 0;
+        if (m == METZGER) {
+            if (lane < SVI_SAMPLES) {
+                const float* ep = eps_tab + ((size_t)step * SVI_SAMPLES + lane) * 7;
+                float pv[MAXP];
+                for (int j = 0; j < np; j++) pv[j] = (float)(mu[j] + sg[j] * (double)ep[j]);
+                metzger_dual_sweep(pv, (float)bs.t_last, otimes, n, mscr + (size_t)lane * 5 * n);
+            }
+            __syncwarp();
+        }
         for (int k = 0; k < SVI_SAMPLES; k++) {
             const float* ep = eps_tab + ((size_t)step * SVI_SAMPLES + k) * 7;
             double th[MAXP], eps[MAXP];
@@ -532,44 +529,46 @@ __global__ void svi_kernel(DeviceBatch d) {
             int huge = 0;
             bool skip_sample = false;
             if (m == METZGER) {
-                // reference path in FP64: base and forward differences
-                metzger_svi_sample(th, t64, n, scr, nullptr);
-                double mx = -INFINITY;
+                // predictions and derivatives of the normalised model, then the
+                // reference's peak rescale (src/parametric.rs:2303-2323)
+                const float* ms = mscr + (size_t)k * 5 * n;
+                float mx = -INFINITY;
                 for (int i = lane; i < n; i += 32)
-                    if (!d.up[bs.off + i]) mx = fmax(mx, scr[4 * (size_t)n + i]);
-                for (int kk = 16; kk; kk >>= 1) mx = fmax(mx, __shfl_xor_sync(FULL, mx, kk));
-                double scl = 1.0;
-                if (mx > 1e-10 && isfinite(mx)) {
-                    double raw = 1.0 / mx;
-                    scl = fmin(fmax(raw, 0.1), 10.0);
-                    if (fabs(raw - scl) / raw > 0.5) skip_sample = true;
+                    if (obs[i].w >= 0.0f) mx = fmaxf(mx, ms[i * 5]);
+                for (int kk = 16; kk; kk >>= 1) mx = fmaxf(mx, __shfl_xor_sync(FULL, mx, kk));
+                float scl = 1.0f;
+                if (mx > 1e-10f && isfinite(mx)) {
+                    float raw = 1.0f / mx;
+                    scl = fminf(fmaxf(raw, 0.1f), 10.0f);
+                    if (fabsf(raw - scl) / raw > 0.5f) skip_sample = true;
                 }
                 if (!skip_sample) {
-                    double sx2d = exp(2.0 * th[se]);
                     for (int i = lane; i < n; i += 32) {
-                        double pr = scr[4 * (size_t)n + i] * scl;
-                        if (!isfinite(pr)) continue;
-                        double gb[5];
-                        for (int j = 0; j < 4; j++) gb[j] = (scr[(size_t)j * n + i] - scr[4 * (size_t)n + i]) / 1e-5 * scl;
-                        gb[4] = 0.0;
-                        double tv = d.var64[bs.off + i] + sx2d, st = sqrt(tv);
-                        if (d.up[bs.off + i]) {
-                            double z = (d.uf64[bs.off + i] - pr) / st;
-                            ll.add((float)log_normal_cdf_f64(z));
+                        float4 ob = obs[i];
+                        float pr = ms[i * 5] * scl;
+                        float gb[MAXP];
+                        for (int j = 0; j < 4; j++) gb[j] = ms[i * 5 + 1 + j] * scl;
+                        gb[4] = 0.0f;
+                        float tv = fabsf(ob.w) + sx2;
+                        float stv = sqrtf(tv);
+                        if (ob.w < 0.0f) {
+                            float z = (ob.z - pr) / stv;
+                            ll.add(log_normal_cdf_f(z));
                             bool hg;
-                            float ratio = upper_ratio_f32((float)z, hg);
+                            float ratio = upper_ratio_f32(z, hg);
                             if (hg) huge = 1;
-                            for (int j = 0; j < 4; j++) if (isfinite(gb[j])) dll[j] += (float)(-ratio / st * gb[j]);
-                            dll[se] += (float)(ratio * (-(d.uf64[bs.off + i] - pr) * sx2d / (st * tv)));
+                            for (int j = 0; j < 4; j++) if (isfinite(gb[j])) dll[j] += -ratio / stv * gb[j];
+                            dll[se] += ratio * (-(ob.z - pr) * sx2 / (stv * tv));
                         } else {
-                            double res = d.f64[bs.off + i] - pr, it = 1.0 / tv, r2 = res * res;
-                            ll.add((float)(-0.5 * (r2 * it + log(2.0 * 3.14159265358979323846 * tv))));
-                            for (int j = 0; j < 4; j++) if (isfinite(gb[j])) dll[j] += (float)(res * it * gb[j]);
-                            dll[se] += (float)((r2 * it * it - it) * sx2d);
+                            float res = ob.z - pr;
+                            float it = 1.0f / tv;
+                            float r2 = res * res;
+                            ll.add(-0.5f * (r2 * it + logf(6.283185307179586f * tv)));
+                            for (int j = 0; j < 4; j++) if (isfinite(gb[j])) dll[j] += res * it * gb[j];
+                            dll[se] += (r2 * it * it - it) * sx2;
                         }
                     }
                 }
-                __syncwarp();
             } else {
                 for (int i = lane; i < n; i += 32) {
                     float4 ob = obs[i];
