@@ -54,6 +54,7 @@ extern "C" {
 #define LCF_E_NOMEM (-3)          /* device or pinned allocation failed */
 #define LCF_E_TIMEOUT (-4)        /* a bounded device wait expired */
 #define LCF_E_UNSUPPORTED (-5)    /* option combination not built */
+#define LCF_E_CAPACITY (-6)       /* a size beyond a fixed capacity (lcf_band_cost_static) */
 
 /* UncertaintyMethod, src/parametric.rs:13-21 */
 #define LCF_METHOD_SVI 0
@@ -193,6 +194,30 @@ int lcf_band_cost(lcf_ctx* ctx, int model, const double* times, const double* fl
                   const double* obs_var, const uint8_t* is_upper, const double* upper_flux,
                   int n_obs, const double* params, int n_eval, int with_prior,
                   double* costs);
+
+/*
+ * Allocation-free variant of lcf_band_cost, for callers that cannot call
+ * cudaMalloc: a host framework that owns all device memory through its own
+ * pool or budget, or an embedding where the library must not allocate GPU
+ * memory of its own.  No counterpart in the reference.
+ *
+ * All array arguments are device pointers supplied by the caller (the band
+ * as in lcf_band_cost, params [n_eval * n_params(model)], costs [n_eval]);
+ * the work is enqueued on `stream` (a cudaStream_t of `device`, NULL = the
+ * legacy default stream) and the call returns without synchronising.  The
+ * library's scratch for it is a fixed static device array, so the call
+ * allocates nothing (no cudaMalloc, cudaFree or allocating library routine)
+ * and accepts at most 2048 observations and 512 parameter vectors per call
+ * (LCF_E_CAPACITY beyond that).  The array's device address is looked up
+ * with cudaGetSymbolAddress on the first call on each device: make that
+ * first call before any stream capture.  Every call on a device shares the
+ * array and leaves its contents behind; each call writes everything it reads,
+ * and calls that overlap on the GPU race.
+ */
+int lcf_band_cost_static(int device, int model, const double* times, const double* flux,
+                         const double* obs_var, const uint8_t* is_upper, const double* upper_flux,
+                         int n_obs, const double* params, int n_eval, int with_prior, double* costs,
+                         void* stream);
 
 /* ---------------------------------------------------------------------------
  * Reference drop-in exports (device pointers, default stream, void return;
