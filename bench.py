@@ -16,7 +16,12 @@ One JSON line on rank 0:
             and FP32 pipe peaks (the kernel is bound by those pipes, not by
             HBM or the tensor cores);
   cpu_baseline  the FP64 C++ restatement of the reference's CPU path
-            (oracle/, "port") on a bounded sample, all host threads.
+            (oracle/, "port") on a bounded sample, all host threads;
+  plain_gpu the plain FP64 GPU form (lcf_fit_plain_device: one thread per
+            particle, FP64, global-memory observations, one launch per model
+            per stage, no graph) on the same 10,000 sources, and the fused
+            pipeline's ratio to it — over the whole fused pipeline and over
+            the stages the plain form runs (PSO, L-BFGS, selection, SVI).
 
 ``--impl reference`` times that CPU path alone (rank 0) on the same workload.
 Under torchrun each rank fits its own 10,000 sources (weak scaling, no
@@ -66,6 +71,7 @@ def parse():
     ap.add_argument("--cpu-sample", type=int, default=96, help="sources in the CPU-baseline sample")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true", help="skip the host entry-point measurement (profiling runs)")
+    ap.add_argument("--plain-steps", type=int, default=1, help="timed steps of the plain FP64 GPU form (0: skip)")
     return ap.parse_args()
 
 
@@ -249,6 +255,9 @@ def run_fused(args, ws, rank, local):
                "h2d_bytes_per_step": int(st_e2e["h2d_bytes"]), "d2h_bytes_per_step": int(st_e2e["d2h_bytes"])}
     else:
         e2e = None
+    plain = None
+    if args.plain_steps > 0:
+        plain = run_plain(args, batch, ptrs, dev, flush, stage, ws)
     if rank != 0:
         ctx.close()
         return
@@ -299,12 +308,54 @@ def run_fused(args, ws, rank, local):
         "e2e": e2e,
         "roofline": roofline,
         "cpu_baseline": cpu,
+        "plain_gpu": plain,
         "clocks": ck,
         "gpu_launches": int(s0["kernel_launches"]) * args.steps,
         "peaks": peaks,
     }
     print(json.dumps(line), flush=True)
     ctx.close()
+
+
+def run_plain(args, batch, ptrs, dev, flush, fused_stats, ws):
+    """The plain FP64 GPU form on the same device-resident workload."""
+    import torch
+    from lightcurve_fitting_gb300.lib import Context
+    pctx = Context(dev.index)
+    pstream = torch.cuda.ExternalStream(pctx.stream, device=dev)
+    # warm-up: one plain fit of the first 100 sources (module load)
+    sub = batch.subset(np.arange(min(100, batch.n_sources)))
+    keep = {k: torch.from_numpy(getattr(sub, k)).to(dev) for k in
+            ["times", "flux", "flux_err", "band_obs_offsets", "source_band_offsets"]}
+    pctx.fit_plain_device({k: v.data_ptr() for k, v in keep.items()}, sub.n_sources, sub.n_bands)
+    torch.cuda.synchronize()
+    times, st = [], None
+    for _ in range(args.plain_steps):
+        flush.fill_(1.0)
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(pstream)
+        pctx.fit_plain_device(ptrs, batch.n_sources, batch.n_bands, fit_all_models=True)
+        e1.record(pstream)
+        torch.cuda.synchronize()
+        times.append(e0.elapsed_time(e1))
+        st = pctx.stats()
+    pctx.close()
+    ms = dist_max(float(np.mean(times)), ws, dev)
+    value = ws * batch.n_sources / (ms * 1e-3)
+    f_ms = lambda k: float(np.mean([s[k] for s in fused_stats]))
+    fused_total = dist_max(f_ms("ms_total"), ws, dev)
+    fused_same = dist_max(f_ms("ms_total") - f_ms("ms_t0_search") - f_ms("ms_refine") - f_ms("ms_multi_bazin"), ws, dev)
+    return {
+        "value": value, "unit": "sources/s", "ms_per_step": ms, "steps": args.plain_steps,
+        "warmup": "one plain fit of the first 100 sources",
+        "stages": "PSO (8 models x 3 restarts, synchronous global best), L-BFGS polish, BIC selection, SVI; "
+                  "no profile t0 search, refinements, magnitude chi2 or MultiBazin",
+        "stage_ms": {"ms_pso": st["ms_pso"], "ms_lbfgs_select": st["ms_lbfgs"], "ms_svi": st["ms_uncertainty"]},
+        "kernel_launches": int(st["kernel_launches"]),
+        "fused_over_plain": (ws * batch.n_sources / (fused_total * 1e-3)) / value,
+        "fused_over_plain_same_stages": (ws * batch.n_sources / (fused_same * 1e-3)) / value,
+    }
 
 
 def main():

@@ -132,6 +132,10 @@ typedef struct lcf_fit_stats {
     double d2h_bytes;           /* device -> host bytes moved by the last output download */
     double pso0_evals_by_kind[12];      /* particle x observation evaluations of the model-selection PSO launch, by task kind */
     double pso0_particles_by_kind[12];  /* particle evaluations of that launch, by task kind (kinds 8..11: MultiBazin K = 1..4) */
+    double lbfgs_polishes;      /* L-BFGS polishes run (one per band and polished model) */
+    double lbfgs_iters;         /* their L-BFGS iterations */
+    double lbfgs_evals;         /* their cost + gradient evaluations */
+    double lbfgs_obs_evals;     /* observation x (cost + gradient) evaluations */
 } lcf_fit_stats;
 
 typedef struct lcf_ctx lcf_ctx;
@@ -160,6 +164,22 @@ int lcf_fit_parametric_batch(lcf_ctx* ctx, const lcf_bands_csr* bands,
 int lcf_fit_parametric_device(lcf_ctx* ctx, const lcf_bands_csr* dev_bands,
                               const lcf_fit_options* opts);
 int lcf_download_outputs(lcf_ctx* ctx, lcf_fit_outputs* out);
+
+/*
+ * The plain FP64 GPU form of the same fit, the baseline the fused pipeline is
+ * measured against: PSO model selection (one thread per particle, FP64,
+ * observations from global memory, synchronous global best), L-BFGS polish,
+ * BIC selection and SVI, one kernel launch per model per stage and no CUDA
+ * graph.  It omits the profile t0 search, the refinements, the magnitude chi2
+ * and MultiBazin (those outputs come back NaN / 0).  SVI only
+ * (LCF_E_UNSUPPORTED for Laplace).  Device pointers as in
+ * lcf_fit_parametric_device; outputs via lcf_download_outputs.  It is the
+ * straightforward rendering of the reference's CPU algorithm on the GPU
+ * (src/parametric.rs:1646-2066, 2215-2454, driven the way the reference's
+ * GPU host drives its per-particle kernels, src/gpu_cuda.rs:368-567).
+ */
+int lcf_fit_plain_device(lcf_ctx* ctx, const lcf_bands_csr* dev_bands,
+                         const lcf_fit_options* opts);
 
 /* The context's CUDA stream (a cudaStream_t), for callers that time with events. */
 void* lcf_ctx_stream(lcf_ctx* ctx);

@@ -87,6 +87,10 @@ class FitStats(C.Structure):
         ("d2h_bytes", C.c_double),
         ("pso0_evals_by_kind", C.c_double * 12),
         ("pso0_particles_by_kind", C.c_double * 12),
+        ("lbfgs_polishes", C.c_double),
+        ("lbfgs_iters", C.c_double),
+        ("lbfgs_evals", C.c_double),
+        ("lbfgs_obs_evals", C.c_double),
     ]
 
 

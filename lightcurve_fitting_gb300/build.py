@@ -17,7 +17,7 @@ ROOT = os.path.dirname(HERE)
 CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "liblcf_gb300.so")
-SOURCES = ["pso.cu", "polish.cu", "finalize.cu", "host.cu"]
+SOURCES = ["pso.cu", "polish.cu", "finalize.cu", "plain.cu", "host.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 

@@ -112,6 +112,8 @@ struct lcf_ctx {
     DevArr h_in, h_out;
     // band-cost scratch
     DevArr bc_obs, bc_params, bc_costs, bc_scratch;
+    // plain FP64 form: MetzgerKN prediction rows (96 per observation)
+    DevArr plain_scr;
     // layout cache
     std::vector<int64_t> h_boff;
     std::vector<int32_t> h_soff;
@@ -234,7 +236,7 @@ extern "C" void lcf_ctx_destroy(lcf_ctx* ctx) {
                      &ctx->t64, &ctx->f64, &ctx->fe64, &ctx->var64, &ctx->uf64, &ctx->mag64, &ctx->up, &ctx->res,
                      &ctx->fits, &ctx->out, &ctx->mb, &ctx->ctr, &ctx->scratch, &ctx->scratch64, &ctx->scratch_svi,
                      &ctx->t0state,
-                     &ctx->bc_obs, &ctx->bc_params, &ctx->bc_costs, &ctx->bc_scratch};
+                     &ctx->bc_obs, &ctx->bc_params, &ctx->bc_costs, &ctx->bc_scratch, &ctx->plain_scr};
     for (DevArr* a : all) free_arr(*a);
     for (auto& a : ctx->tasks) free_arr(a);
     if (ctx->h_in.p) cudaFreeHost(ctx->h_in.p);
@@ -535,6 +537,47 @@ static int run_pipeline(lcf_ctx* ctx) {
     return 0;
 }
 
+// The plain FP64 form (plain.cu): same inputs and outputs, one launch per
+// model per stage, no graph.  Stage events: 0 start, 1 prep, 2 PSO,
+// 3 L-BFGS + selection, 5 SVI (4, 6, 7 coincide with their neighbours).
+static void enqueue_plain(lcf_ctx* ctx) {
+    const DeviceBatch& d = ctx->db;
+    const lcf_fit_options& o = ctx->opts;
+    cudaStream_t s = ctx->stream;
+    double* scr = (double*)ctx->plain_scr.p;
+    int64_t L = 0;
+    cudaEventRecord(ctx->ev[0], s);
+    cudaMemsetAsync(ctx->res.p, 0xff, (size_t)std::max(ctx->n_bands, 1) * 44 * sizeof(PsoResult), s);
+    cudaMemsetAsync(ctx->ctr.p, 0, sizeof(Counters), s);
+    cudaMemsetAsync(ctx->fits.p, 0xff, (size_t)std::max(ctx->n_bands, 1) * 8 * sizeof(ModelFit), s);
+    launch_prep(d, s); L++;
+    cudaEventRecord(ctx->ev[1], s);
+    static const int order[8] = {BAZIN, ARNETT, TDE, AFTERGLOW, VILLAR, MAGNETAR, SHOCK, METZGER};
+    if (o.forced_model >= 0) {
+        launch_plain_pso(d, o.forced_model, 0, scr, s); L++;
+        cudaEventRecord(ctx->ev[2], s);
+        launch_plain_lbfgs(d, o.forced_model, s); L++;
+    } else if (!o.fit_all_models) {
+        launch_plain_pso(d, BAZIN, 0, scr, s); L++;
+        launch_plain_lbfgs(d, BAZIN, s); L++;
+        for (int k = 1; k < 8; k++) { launch_plain_pso(d, order[k], 1, scr, s); L++; }
+        cudaEventRecord(ctx->ev[2], s);
+        for (int k = 1; k < 8; k++) { launch_plain_lbfgs(d, order[k], s); L++; }
+    } else {
+        for (int k = 0; k < 8; k++) { launch_plain_pso(d, order[k], 0, scr, s); L++; }
+        cudaEventRecord(ctx->ev[2], s);
+        for (int k = 0; k < 8; k++) { launch_plain_lbfgs(d, order[k], s); L++; }
+    }
+    launch_select(d, o.fit_all_models, o.forced_model, s); L++;
+    cudaEventRecord(ctx->ev[3], s);
+    cudaEventRecord(ctx->ev[4], s);
+    for (int m = 0; m < 8; m++) { launch_plain_svi(d, m, scr, s); L++; }
+    cudaEventRecord(ctx->ev[5], s);
+    cudaEventRecord(ctx->ev[6], s);
+    cudaEventRecord(ctx->ev[7], s);
+    ctx->launches = L;
+}
+
 static int finish_stats(lcf_ctx* ctx) {
     CK(cudaStreamSynchronize(ctx->stream));
     CK(cudaGetLastError());
@@ -558,6 +601,10 @@ static int finish_stats(lcf_ctx* ctx) {
     st.ode_steps = (double)c.ode_steps;
     st.pso_tasks = ctx->n_tasks0;
     st.kernel_launches = ctx->launches;
+    st.lbfgs_polishes = (double)c.lb_polishes;
+    st.lbfgs_iters = (double)c.lb_iters;
+    st.lbfgs_evals = (double)c.lb_evals;
+    st.lbfgs_obs_evals = (double)c.lb_obs_evals;
     for (int k = 0; k < 12; k++) {
         st.pso0_evals_by_kind[k] = (double)c.slot0_evals[k];
         st.pso0_particles_by_kind[k] = (double)c.slot0_particles[k];
@@ -714,6 +761,38 @@ extern "C" int lcf_fit_parametric_device(lcf_ctx* ctx, const lcf_bands_csr* dev,
     ctx->db.src_off = dev->source_band_offsets;
     if (nb == 0) return 0;
     if (int rc = run_pipeline(ctx)) return rc;
+    return finish_stats(ctx);
+}
+
+extern "C" int lcf_fit_plain_device(lcf_ctx* ctx, const lcf_bands_csr* dev, const lcf_fit_options* o) {
+    if (!ctx) return LCF_E_INVALID;
+    if (!dev) return set_err(ctx, LCF_E_INVALID, "null argument");
+    if (int rc = check_opts(ctx, o)) return rc;
+    if (o->method != LCF_METHOD_SVI) return set_err(ctx, LCF_E_UNSUPPORTED, "the plain form runs SVI only");
+    CK(cudaSetDevice(ctx->device));
+    int ns = dev->n_sources, nb = dev->n_bands;
+    if (ns < 0 || nb < 0) return set_err(ctx, LCF_E_INVALID, "bad CSR header");
+    std::vector<int64_t> boff((size_t)nb + 1);
+    std::vector<int32_t> soff((size_t)ns + 1);
+    CK(cudaMemcpy(boff.data(), dev->band_obs_offsets, boff.size() * 8, cudaMemcpyDeviceToHost));
+    CK(cudaMemcpy(soff.data(), dev->source_band_offsets, soff.size() * 4, cudaMemcpyDeviceToHost));
+    if (int rc = validate_layout(ctx, ns, nb, soff.data(), boff.data())) return rc;
+    ctx->h_boff.swap(boff);
+    ctx->h_soff.swap(soff);
+    int64_t n_obs = ctx->h_boff[nb];
+    lcf_fit_options po = *o;
+    po.run_multi_bazin = 0;  // not part of the plain form
+    if (int rc = prepare_layout(ctx, ns, nb, n_obs, po)) return rc;
+    if (int rc = grow(ctx, ctx->plain_scr, (size_t)std::max<int64_t>(n_obs, 1) * 96 * sizeof(double))) return rc;
+    ctx->db.times = dev->times;
+    ctx->db.flux = dev->flux;
+    ctx->db.err = dev->flux_err;
+    ctx->db.band_off = dev->band_obs_offsets;
+    ctx->db.src_off = dev->source_band_offsets;
+    if (nb == 0) return 0;
+    cudaGetLastError();
+    enqueue_plain(ctx);
+    CK(cudaGetLastError());
     return finish_stats(ctx);
 }
 

@@ -189,6 +189,7 @@ struct Counters {
     unsigned long long ode_steps;
     unsigned long long slot0_evals[12];      // particle x observation evaluations of the first PSO launch, by kind
     unsigned long long slot0_particles[12];  // particle evaluations of the first PSO launch, by kind
+    unsigned long long lb_polishes, lb_iters, lb_evals, lb_obs_evals;  // L-BFGS work
     int32_t error;              // first error code raised on the device
     int32_t pad;
 };
@@ -253,6 +254,10 @@ void launch_mb_build(const DeviceBatch& d, int slot, int k, cudaStream_t s);
 void launch_lbfgs(const DeviceBatch& d, int model_mask, cudaStream_t s);
 void launch_select(const DeviceBatch& d, int fit_all, int forced, cudaStream_t s);
 void launch_svi(const DeviceBatch& d, cudaStream_t s);
+// plain.cu (the plain FP64 form)
+void launch_plain_pso(const DeviceBatch& d, int m, int gate, double* mscr, cudaStream_t s);
+void launch_plain_lbfgs(const DeviceBatch& d, int m, cudaStream_t s);
+void launch_plain_svi(const DeviceBatch& d, int m, double* mscr, cudaStream_t s);
 // finalize.cu
 void launch_laplace(const DeviceBatch& d, cudaStream_t s);
 void launch_refine(const DeviceBatch& d, cudaStream_t s);

@@ -41,6 +41,7 @@ def load(path: str = LIB_PATH):
     L.lcf_fit_parametric_batch.argtypes = [vp, C.POINTER(abi.BandsCSR), C.POINTER(abi.FitOptions),
                                            C.POINTER(abi.FitOutputs)]
     L.lcf_fit_parametric_device.argtypes = [vp, C.POINTER(abi.BandsCSR), C.POINTER(abi.FitOptions)]
+    L.lcf_fit_plain_device.argtypes = [vp, C.POINTER(abi.BandsCSR), C.POINTER(abi.FitOptions)]
     L.lcf_download_outputs.argtypes = [vp, C.POINTER(abi.FitOutputs)]
     L.lcf_ctx_stream.argtypes = [vp]
     L.lcf_ctx_stream.restype = vp
@@ -120,6 +121,17 @@ class Context:
         opts = abi.options(fit_all_models, method, forced_model, run_multi_bazin)
         self._check(self.L.lcf_fit_parametric_device(self.h, C.byref(csr), C.byref(opts)),
                     "lcf_fit_parametric_device")
+
+    def fit_plain_device(self, dev_ptrs: dict, n_sources: int, n_bands: int, fit_all_models=True, forced_model=-1):
+        """lcf_fit_plain_device: the plain FP64 GPU form (PSO, L-BFGS,
+        selection, SVI; one launch per model per stage, no graph)."""
+        csr = abi.BandsCSR()
+        csr.n_sources, csr.n_bands = n_sources, n_bands
+        csr.source_band_offsets = dev_ptrs["source_band_offsets"]
+        csr.band_obs_offsets = dev_ptrs["band_obs_offsets"]
+        csr.times, csr.flux, csr.flux_err = dev_ptrs["times"], dev_ptrs["flux"], dev_ptrs["flux_err"]
+        opts = abi.options(fit_all_models, abi.METHOD_SVI, forced_model, False)
+        self._check(self.L.lcf_fit_plain_device(self.h, C.byref(csr), C.byref(opts)), "lcf_fit_plain_device")
 
     def download(self, n_bands: int) -> abi.FitResult:
         res = abi.FitResult(n_bands)
