@@ -1,6 +1,7 @@
 """Build liblcf_gb300.so in-tree with nvcc for sm_103a.
 
-Four translation units are compiled in parallel (pso, polish, finalize, host)
+Five translation units are compiled in parallel (pso, polish, finalize, plain,
+host)
 and linked into lightcurve_fitting_gb300/liblcf_gb300.so with the CUDA runtime
 linked statically.  No cmake; objects go to lightcurve_fitting_gb300/_build/.
 """

@@ -15,6 +15,7 @@
 #include <cuda_runtime.h>
 
 #include "lcf_internal.cuh"
+#include "models_f32.cuh"
 #include "models_f64.cuh"
 
 namespace lcf {
@@ -128,6 +129,107 @@ __device__ double band_ll_w(int m, const BandView& b, const double* p, double* s
     ll = wsum(ll);
     __syncwarp();
     return ll;
+}
+
+// ---------------------------------------------------------------------------
+// The refinement scans of models other than MetzgerKN evaluate the model in
+// FP32 (the evaluators of models_f32.cuh, on the band's FP32 time records)
+// and form each observation's term in FP64 from per-band constants that do
+// not change across the scans (sigma_extra is fixed there): 1/tv, 1/sqrt(tv)
+// and ln(2 pi tv).  The scans compare log-likelihoods against thresholds
+// 0.5 apart and pick grid points, so FP32 prediction rounding (1e-7
+// relative) moves no decision except a value within ~1e-5 of a threshold.
+// ---------------------------------------------------------------------------
+__device__ void scan_constants(const BandView& b, double se2, double* cst) {
+    for (int i = threadIdx.x & 31; i < b.n; i += 32) {
+        double tv = b.var[i] + se2;
+        cst[3 * i] = 1.0 / tv;
+        cst[3 * i + 1] = 1.0 / sqrt(tv);
+        cst[3 * i + 2] = log(2.0 * 3.14159265358979323846 * tv);
+    }
+    __syncwarp();
+}
+
+// FP32 prediction -> FP64 value; false for a prediction the reference finds
+// non-finite (skipped by the scans).  Huge predictions come back through
+// their logarithm (ST_BIG) and are finite in FP64.
+__device__ __forceinline__ bool pred_f64(float pf, int st, double& pr) {
+    if (st == ST_NONFINITE) return false;
+    pr = st == ST_BIG ? exp((double)pf) : (double)pf;
+    return true;
+}
+
+__device__ __forceinline__ double ll_term(const BandView& b, int i, double pr, const double* cst) {
+    const double* c = cst + 3 * i;
+    if (b.up[i]) {
+        double z = (b.uf[i] - pr) * c[1];
+        if (z > -1e15) return (double)log_normal_cdf_f((float)z);
+        return -0.5 * z * z - 0.9189385332046727 - log(-z);
+    }
+    double r = b.f[i] - pr;
+    return -0.5 * (r * r * c[0] + c[2]);
+}
+
+template <class F>
+__device__ double ll_scan_t(const double* p, const float4* obs, const BandView& b, const double* cst) {
+    F e;
+    e.init64(p);
+    double ll = 0.0;
+    for (int i = threadIdx.x & 31; i < b.n; i += 32) {
+        float4 o = obs[i];
+        int st = ST_OK;
+        float pf = e.eval(o.x, o.y, st);
+        double pr;
+        if (!pred_f64(pf, st, pr)) continue;
+        ll += ll_term(b, i, pr, cst);
+    }
+    return wsum(ll);
+}
+
+// band_ll_w for the models other than MetzgerKN, FP32 evaluation
+__device__ double band_ll_fast(int m, const double* p, const float4* obs, const BandView& b, const double* cst) {
+    switch (m) {
+        case BAZIN: return ll_scan_t<BazinF>(p, obs, b, cst);
+        case VILLAR: return ll_scan_t<VillarF>(p, obs, b, cst);
+        case TDE: return ll_scan_t<TdeF>(p, obs, b, cst);
+        case ARNETT: return ll_scan_t<ArnettF>(p, obs, b, cst);
+        case MAGNETAR: return ll_scan_t<MagnetarF>(p, obs, b, cst);
+        case SHOCK: return ll_scan_t<ShockF>(p, obs, b, cst);
+        default: return ll_scan_t<AfterglowF>(p, obs, b, cst);
+    }
+}
+
+// Weighted sums of the unit-amplitude shape for the amplitude (and baseline)
+// solve of profile_t0_refine: sw, sy, sf, syf, sff over detections.
+template <class F>
+__device__ void shape_sums_t(const double* p, const float4* obs, const BandView& b, const double* cst, double* s5) {
+    F e;
+    e.init64(p);
+    double sw = 0, sy = 0, sf = 0, syf = 0, sff = 0;
+    for (int i = threadIdx.x & 31; i < b.n; i += 32) {
+        if (b.up[i]) continue;
+        float4 o = obs[i];
+        int st = ST_OK;
+        float pf = e.eval(o.x, o.y, st);
+        double sh;
+        if (!pred_f64(pf, st, sh) || !isfinite(sh)) continue;
+        double w = cst[3 * i];
+        sw += w; sy += w * b.f[i]; sf += w * sh; syf += w * b.f[i] * sh; sff += w * sh * sh;
+    }
+    s5[0] = wsum(sw); s5[1] = wsum(sy); s5[2] = wsum(sf); s5[3] = wsum(syf); s5[4] = wsum(sff);
+}
+
+__device__ void shape_sums_fast(int m, const double* p, const float4* obs, const BandView& b, const double* cst,
+                                double* s5) {
+    switch (m) {
+        case BAZIN: shape_sums_t<BazinF>(p, obs, b, cst, s5); break;
+        case VILLAR: shape_sums_t<VillarF>(p, obs, b, cst, s5); break;
+        case TDE: shape_sums_t<TdeF>(p, obs, b, cst, s5); break;
+        case ARNETT: shape_sums_t<ArnettF>(p, obs, b, cst, s5); break;
+        case MAGNETAR: shape_sums_t<MagnetarF>(p, obs, b, cst, s5); break;
+        case SHOCK: shape_sums_t<ShockF>(p, obs, b, cst, s5); break;
+        default: shape_sums_t<AfterglowF>(p, obs, b, cst, s5); break;
+    }
 }
 
 // symmetric_eigen (Jacobi), src/parametric.rs:2517-2587
@@ -246,6 +348,13 @@ __global__ void refine_kernel(DeviceBatch d) {
     double* scr = d.scratch64 + 5 * bs.off;
     double mu[MAXP], ls[MAXP];
     for (int j = 0; j < np; j++) { mu[j] = o.mu[j]; ls[j] = o.log_sigma[j]; }
+    // scans of the models other than MetzgerKN: FP32 evaluation, FP64 terms
+    const bool fast = m != METZGER;
+    const float4* obs = d.obs + bs.off;
+    if (fast) scan_constants(b, exp(2.0 * mu[se]), scr);
+    auto scan_ll = [&](const double* p, bool rescale) {
+        return fast ? band_ll_fast(m, p, obs, b, scr) : band_ll_w(m, b, p, scr, rescale);
+    };
     // ---- profile_t0_refine
     {
         double t0_lo = bs.t_first - 30.0, t0_hi = bs.t_peak_all + 5.0;
@@ -263,17 +372,23 @@ __global__ void refine_kernel(DeviceBatch d) {
                 p[0] = 0.0;
                 double saved_b = 0.0;
                 if (has_b) { saved_b = p[1]; p[1] = 0.0; }
-                metzger_prepare(m, p, b, scr);
-                Predictor P(m, p, scr);
                 double sw = 0, sy = 0, sf = 0, syf = 0, sff = 0;
-                for (int i = lane; i < b.n; i += 32) {
-                    double sh = P(b, i);
-                    if (b.up[i] || !isfinite(sh)) continue;
-                    double w = 1.0 / (b.var[i] + sx2);
-                    sw += w; sy += w * b.f[i]; sf += w * sh; syf += w * b.f[i] * sh; sff += w * sh * sh;
+                if (fast) {
+                    double s5[5];
+                    shape_sums_fast(m, p, obs, b, scr, s5);
+                    sw = s5[0]; sy = s5[1]; sf = s5[2]; syf = s5[3]; sff = s5[4];
+                } else {
+                    metzger_prepare(m, p, b, scr);
+                    Predictor P(m, p, scr);
+                    for (int i = lane; i < b.n; i += 32) {
+                        double sh = P(b, i);
+                        if (b.up[i] || !isfinite(sh)) continue;
+                        double w = 1.0 / (b.var[i] + sx2);
+                        sw += w; sy += w * b.f[i]; sf += w * sh; syf += w * b.f[i] * sh; sff += w * sh * sh;
+                    }
+                    sw = wsum(sw); sy = wsum(sy); sf = wsum(sf); syf = wsum(syf); sff = wsum(sff);
+                    __syncwarp();
                 }
-                sw = wsum(sw); sy = wsum(sy); sf = wsum(sf); syf = wsum(syf); sff = wsum(sff);
-                __syncwarp();
                 if (has_b) {
                     double det = sw * sff - sf * sf;
                     if (fabs(det) > 1e-20) {
@@ -285,7 +400,7 @@ __global__ void refine_kernel(DeviceBatch d) {
                     if (sff > 1e-20 && syf / sff > 1e-10) p[0] = log(syf / sff);
                     else p[0] = saved_la;
                 }
-                double ll = band_ll_w(m, b, p, scr, true);
+                double ll = scan_ll(p, true);
                 if (ll > best_ll) { best_ll = ll; best_t0 = t0; }
             }
             double lo1 = best_t0, hi1 = best_t0, thr = best_ll - 0.5;
@@ -295,7 +410,7 @@ __global__ void refine_kernel(DeviceBatch d) {
                 double p[MAXP];
                 for (int j = 0; j < np; j++) p[j] = mu[j];
                 p[t0i] = t0;
-                if (band_ll_w(m, b, p, scr, false) >= thr) lo1 = t0;
+                if (scan_ll(p, false) >= thr) lo1 = t0;
                 else break;
             }
             for (int gi = 0; gi < NG; gi++) {
@@ -304,7 +419,7 @@ __global__ void refine_kernel(DeviceBatch d) {
                 double p[MAXP];
                 for (int j = 0; j < np; j++) p[j] = mu[j];
                 p[t0i] = t0;
-                if (band_ll_w(m, b, p, scr, false) >= thr) hi1 = t0;
+                if (scan_ll(p, false) >= thr) hi1 = t0;
                 else break;
             }
             mu[t0i] = best_t0;
@@ -313,7 +428,7 @@ __global__ void refine_kernel(DeviceBatch d) {
     }
     // ---- profile_refine_all
     {
-        double map_ll = band_ll_w(m, b, mu, scr, false);
+        double map_ll = scan_ll(mu, false);
         double thr = map_ll - 0.5;
         for (int j = 0; j < np; j++) {
             if (j == se) continue;
@@ -327,7 +442,7 @@ __global__ void refine_kernel(DeviceBatch d) {
                 double p[MAXP];
                 for (int k = 0; k < np; k++) p[k] = mu[k];
                 p[j] = val;
-                double ll = band_ll_w(m, b, p, scr, false);
+                double ll = scan_ll(p, false);
                 if (ll >= thr) { l1 = fmin(l1, val); h1 = fmax(h1, val); }
             }
             double prof = fmax((h1 - l1) / 2.0, 1e-6);

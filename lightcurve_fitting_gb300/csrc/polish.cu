@@ -19,7 +19,7 @@
 #include <cuda_runtime.h>
 
 #include "grads_f32.cuh"
-#include "lbfgs.cuh"
+#include "lbfgs_lane.cuh"
 #include "lcf_internal.cuh"
 #include "models_f32.cuh"
 #include "metzger_dual.cuh"
@@ -80,145 +80,169 @@ __device__ double warp_nll(int m, const double* pd, const float4* obs, int n, do
     return (s + prior / nd) / nd;
 }
 
-struct LbCtx {
-    const double *t, *f, *var, *uf;
-    const uint8_t* up;
-    int n, m, np;
-    double nd;
-    double lo[MAXP], hi[MAXP];
-    int evals, iters;
-    __device__ void cost_grad(const double* x, double& f, double* g, bool want_grad);
-};
-
 // Cost and projected gradient of the bounded problem (BoundedPsoCost,
-// src/parametric.rs:1500-1535) at x, in FP64 with the lanes over the
-// observations: PsoCost::cost_from_slice (with the population prior and the
-// Villar constraint) and PsoCost::gradient (without either).  The polish runs
-// in the reference's arithmetic because its acceptance tests (descent
-// direction, sufficient decrease, curvature) compare quantities that are
-// differences of near-equal costs and gradients near the optimum.
-__device__ void lb_cost_grad(LbCtx& c, const double* x, double& f, double* g, bool want_grad) {
-    double q[MAXP];
-    for (int j = 0; j < c.np; j++) q[j] = fmin(fmax(x[j], c.lo[j]), c.hi[j]);
-    const int lane = threadIdx.x & 31;
-    const int se = se_idx_of(c.m);
-    const double se2 = exp(2.0 * q[se]);
-    bool constrained = false;
-    if (c.m == VILLAR) {
-        double beta = q[1], gamma = exp(q[2]), tr = exp(q[4]), tf = exp(q[5]);
-        double c1 = fmax(gamma * beta - 1.0, 0.0);
-        double c2 = fmax(exp(-gamma / tr) * (tf / tr - 1.0) - 1.0, 0.0);
-        double c3 = fmax(beta * tf - 1.0 + beta * gamma, 0.0);
-        double cc = c1 + c2 + c3;
-        if (cc > 0.0) { f = 1e12 + 10000.0 * cc; constrained = true; }
-    }
-    double nll = 0.0, gl[MAXP];
-    for (int j = 0; j < MAXP; j++) gl[j] = 0.0;
-    int nonfinite = 0;
-    Model64 mod;
-    mod.init(c.m, q);
-    for (int i = lane; i < c.n; i += 32) {
-        double mg[MAXP];
-        double pr = mod.eval(c.t[i], want_grad ? mg : nullptr);
-        if (!isfinite(pr)) { nonfinite = 1; continue; }
-        double tv = c.var[i] + se2;
-        if (c.up[i]) {
-            double sv = sqrt(tv);
-            double z = (c.uf[i] - pr) / sv;
-            nll -= log_normal_cdf_f64(z);
-            if (want_grad) {
-                double phi = exp(-0.5 * z * z) / sqrt(2.0 * 3.14159265358979323846);
-                double cdf = 0.5 * (1.0 + erf_approx_f64(z / 1.41421356237309504880));
-                double ratio = phi / fmax(cdf, 1e-300);
-                for (int j = 0; j < c.np; j++) gl[j] += ratio * mg[j] / sv;
-                gl[se] += ratio * z * se2 / tv;
-            }
-        } else {
-            double d = pr - c.f[i];
-            nll += d * d / tv + log(tv);
-            if (want_grad) {
-                double sc = 2.0 * d / tv;
-                for (int j = 0; j < c.np; j++) gl[j] += sc * mg[j];
-                gl[se] += (-d * d / (tv * tv) + 1.0 / tv) * (2.0 * se2);
-            }
+// src/parametric.rs:1500-1535) for the lane-distributed polish: the full
+// parameter vector is gathered from lanes 0..np-1, the lanes split the
+// observations, and each lane keeps its own component of the gradient.
+// FP64 throughout: PsoCost::cost_from_slice (population prior, Villar
+// constraint) and PsoCost::gradient (neither), as in the reference.  The
+// polish runs in the reference's arithmetic because its acceptance tests
+// (descent direction, sufficient decrease, curvature) compare differences of
+// near-equal costs and gradients near the optimum.
+template <int MODEL>
+struct LaneLb {
+    static constexpr int np = n_params_of(MODEL);
+    const double *t, *flux, *var, *uf;
+    const uint8_t* up;
+    int n;
+    double nd;
+    double lo_j, hi_j;
+    int evals, iters;
+
+    __device__ void cost_grad(double xj, double& fo, double& gj, bool want_grad) {
+        evals++;
+        const int lane = threadIdx.x & 31, j = lane & 7;
+        const double qj = fmin(fmax(xj, lo_j), hi_j);
+        double q[MAXP];
+#pragma unroll
+        for (int k = 0; k < MAXP; k++) q[k] = k < np ? __shfl_sync(FULL, qj, k) : 0.0;
+        constexpr int se = se_idx_of(MODEL);
+        const double se2 = exp(2.0 * q[se]);
+        bool constrained = false;
+        double f = 0.0;
+        if (MODEL == VILLAR) {
+            double beta = q[1], gamma = exp(q[2]), tr = exp(q[4]), tf = exp(q[5]);
+            double c1 = fmax(gamma * beta - 1.0, 0.0);
+            double c2 = fmax(exp(-gamma / tr) * (tf / tr - 1.0) - 1.0, 0.0);
+            double c3 = fmax(beta * tf - 1.0 + beta * gamma, 0.0);
+            double cc = c1 + c2 + c3;
+            if (cc > 0.0) { f = 1e12 + 10000.0 * cc; constrained = true; }
         }
-    }
-    nonfinite = warp_or(nonfinite);
-    if (!constrained) {
-        if (nonfinite) f = BIG_COST;
-        else {
-            double prior = 0.0;
-            for (int j = 0; j < c.np; j++) {
-                double w = c_pop_w[c.m][j];
-                if (w > 0.0) {
-                    double z = (q[j] - c_pop_c[c.m][j]) / w;
-                    prior += 0.5 * z * z;
+        double nll = 0.0, gl[MAXP];
+#pragma unroll
+        for (int k = 0; k < MAXP; k++) gl[k] = 0.0;
+        int nonfinite = 0;
+        Model64 mod;
+        mod.init(MODEL, q);
+        for (int i = lane; i < n; i += 32) {
+            double mg[MAXP];
+            double pr = mod.eval(t[i], want_grad ? mg : nullptr);
+            if (!isfinite(pr)) { nonfinite = 1; continue; }
+            double tv = var[i] + se2;
+            if (up[i]) {
+                double sv = sqrt(tv);
+                double z = (uf[i] - pr) / sv;
+                nll -= log_normal_cdf_f64(z);
+                if (want_grad) {
+                    double phi = exp(-0.5 * z * z) / sqrt(2.0 * 3.14159265358979323846);
+                    double cdf = 0.5 * (1.0 + erf_approx_f64(z / 1.41421356237309504880));
+                    double ratio = phi / fmax(cdf, 1e-300);
+#pragma unroll
+                    for (int k = 0; k < np; k++) gl[k] += ratio * mg[k] / sv;
+                    gl[se] += ratio * z * se2 / tv;
+                }
+            } else {
+                double dd = pr - flux[i];
+                nll += dd * dd / tv + log(tv);
+                if (want_grad) {
+                    double sc = 2.0 * dd / tv;
+#pragma unroll
+                    for (int k = 0; k < np; k++) gl[k] += sc * mg[k];
+                    gl[se] += (-dd * dd / (tv * tv) + 1.0 / tv) * (2.0 * se2);
                 }
             }
-            f = (warp_sum_d(nll) + prior / c.nd) / c.nd;
         }
+        nonfinite = warp_or(nonfinite);
+        if (!constrained) {
+            if (nonfinite) f = BIG_COST;
+            else {
+                double prior = 0.0;
+#pragma unroll
+                for (int k = 0; k < np; k++) {
+                    double w = c_pop_w[MODEL][k];
+                    if (w > 0.0) {
+                        double z = (q[k] - c_pop_c[MODEL][k]) / w;
+                        prior += 0.5 * z * z;
+                    }
+                }
+                f = (warp_sum_d(nll) + prior / nd) / nd;
+            }
+        }
+        fo = f;
+        if (!want_grad) return;
+        double gs = 0.0;
+#pragma unroll
+        for (int k = 0; k < np; k++) {
+            double gk = warp_sum_d(gl[k]);
+            if (k == j) gs = gk;
+        }
+        gj = (nonfinite || j >= np) ? 0.0 : gs / nd;
+        if ((xj <= lo_j && gj > 0.0) || (xj >= hi_j && gj < 0.0)) gj = 0.0;
     }
-    if (!want_grad) return;
-    for (int j = 0; j < c.np; j++) {
-        double gj = warp_sum_d(gl[j]);
-        g[j] = nonfinite ? 0.0 : gj / c.nd;
-    }
-    for (int j = 0; j < c.np; j++)
-        if ((x[j] <= c.lo[j] && g[j] > 0.0) || (x[j] >= c.hi[j] && g[j] < 0.0)) g[j] = 0.0;
-}
-__device__ void LbCtx::cost_grad(const double* x, double& f, double* g, bool want_grad) {
-    evals++;
-    lb_cost_grad(*this, x, f, g, want_grad);
-}
+};
 
-// One warp per (band, model): best of the three restarts, then L-BFGS.
-__global__ void lbfgs_kernel(DeviceBatch d, int model_mask) {
-    int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    if (warp >= d.n_bands * 8) return;
-    int b = warp >> 3, m = warp & 7;
-    if (!((model_mask >> m) & 1)) return;
-    BandStats bs = d.stats[b];
+// Best of the three restarts of (band, MODEL), then the polish.
+template <int MODEL>
+__device__ void polish_band(const DeviceBatch& d, int b) {
+    const BandStats bs = d.stats[b];
     if (!bs.valid) return;
-    const PsoResult* R = d.pso_res + (size_t)(b * 8 + m) * 3;
+    const PsoResult* R = d.pso_res + (size_t)(b * 8 + MODEL) * 3;
     if (R[0].iters < 0) return;  // this model was not fitted for this band
     double best_c = INFINITY;
     int best_r = -1;
     for (int r = 0; r < 3; r++)
         if (R[r].iters >= 0 && R[r].cost < best_c) { best_c = R[r].cost; best_r = r; }
-    int np = n_params_of(m);
-    double params[MAXP];
-    for (int j = 0; j < MAXP; j++) params[j] = (best_r >= 0 && j < np) ? (double)R[best_r].params[j] : 0.0;
+    constexpr int np = n_params_of(MODEL);
+    const int lane = threadIdx.x & 31, j = lane & 7;
+    double pj = (best_r >= 0 && j < np) ? (double)R[best_r].params[j] : 0.0;
     double cost = best_c;
-    if (m != METZGER && best_r >= 0) {
-        LbCtx c;
+    if (MODEL != METZGER && best_r >= 0) {
+        LaneLb<MODEL> c;
         c.t = d.t64 + bs.off;
-        c.f = d.f64 + bs.off;
+        c.flux = d.f64 + bs.off;
         c.var = d.var64 + bs.off;
         c.uf = d.uf64 + bs.off;
         c.up = d.up + bs.off;
         c.n = bs.n;
-        c.m = m;
-        c.np = np;
         c.nd = (double)max(bs.n, 1);
         c.evals = 0;
         c.iters = 0;
-        for (int j = 0; j < MAXP; j++) { c.lo[j] = c_lo[m][j]; c.hi[j] = c_hi[m][j]; }
-        int t0i = t0_idx_of(m);
-        double t0_lo = fmax(bs.t_first - 30.0, c.lo[t0i]);
-        double t0_hi = fmin(bs.t_peak + 10.0, c.hi[t0i]);
-        if (t0_lo < t0_hi) { c.lo[t0i] = t0_lo; c.hi[t0i] = t0_hi; }
-        cost = lbfgs_polish(c, params, best_c);
-        if ((threadIdx.x & 31) == 0) {
+        c.lo_j = j < np ? c_lo[MODEL][j] : 0.0;
+        c.hi_j = j < np ? c_hi[MODEL][j] : 0.0;
+        constexpr int t0i = t0_idx_of(MODEL);
+        double t0_lo = fmax(bs.t_first - 30.0, c_lo[MODEL][t0i]);
+        double t0_hi = fmin(bs.t_peak + 10.0, c_hi[MODEL][t0i]);
+        if (j == t0i && t0_lo < t0_hi) { c.lo_j = t0_lo; c.hi_j = t0_hi; }
+        cost = lane_lbfgs_polish(c, pj, best_c);
+        if (lane == 0) {
             atomicAdd(&d.ctr->lb_polishes, 1ull);
             atomicAdd(&d.ctr->lb_iters, (unsigned long long)c.iters);
             atomicAdd(&d.ctr->lb_evals, (unsigned long long)c.evals);
             atomicAdd(&d.ctr->lb_obs_evals, (unsigned long long)c.evals * (unsigned long long)bs.n);
         }
     }
-    if ((threadIdx.x & 31) == 0) {
-        ModelFit& F = d.fits[b * 8 + m];
-        F.cost = cost;
-        for (int j = 0; j < MAXP; j++) F.params[j] = j < np ? params[j] : NAN;
+    ModelFit& F = d.fits[b * 8 + MODEL];
+    if (lane == 0) F.cost = cost;
+    if (lane < MAXP) F.params[lane] = lane < np ? pj : NAN;
+}
+
+// One warp per (band, model), model-major: consecutive warps (and so the
+// warps resident on an SM) polish the same model, whose code then stays in
+// the instruction cache.
+__global__ void __launch_bounds__(128) lbfgs_kernel(DeviceBatch d, int model_mask) {
+    const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    if (warp >= d.n_bands * 8) return;
+    const int m = warp / d.n_bands, b = warp - m * d.n_bands;
+    if (!((model_mask >> m) & 1)) return;
+    switch (m) {
+        case BAZIN: polish_band<BAZIN>(d, b); break;
+        case VILLAR: polish_band<VILLAR>(d, b); break;
+        case TDE: polish_band<TDE>(d, b); break;
+        case ARNETT: polish_band<ARNETT>(d, b); break;
+        case MAGNETAR: polish_band<MAGNETAR>(d, b); break;
+        case SHOCK: polish_band<SHOCK>(d, b); break;
+        case AFTERGLOW: polish_band<AFTERGLOW>(d, b); break;
+        default: polish_band<METZGER>(d, b); break;
     }
 }
 
