@@ -232,6 +232,203 @@ __device__ void shape_sums_fast(int m, const double* p, const float4* obs, const
     }
 }
 
+// ---------------------------------------------------------------------------
+// MetzgerKN refinement scans, one scan point per lane.  The scans evaluate
+// up to ~140 independent parameter vectors per band; each lane integrates
+// its own vector's ODE (FP64, metzger_sweep64 — the arithmetic of
+// metzger_f64) twice: the first sweep finds the peak the predictions are
+// normalised by (and the largest detection prediction for the rescale), the
+// second forms the band's terms in observation order.
+// ---------------------------------------------------------------------------
+struct MzPeak {
+    const uint8_t* up;
+    double mx;  // largest unnormalised detection interpolant
+    __device__ void operator()(int j, double l) {
+        if (!up[j]) mx = fmax(mx, l);
+    }
+};
+
+struct MzLl {
+    const BandView* b;
+    const double* cst;
+    double inv_peak, scale, ll;
+    __device__ void term(int j, double pr) {
+        if (!isfinite(pr)) return;
+        const double* c = cst + 3 * j;
+        if (b->up[j]) {
+            ll += log_normal_cdf_f64((b->uf[j] - pr) * c[1]);
+        } else {
+            double r = b->f[j] - pr;
+            ll += -0.5 * (r * r * c[0] + c[2]);
+        }
+    }
+    __device__ void operator()(int j, double l) { term(j, l * inv_peak * scale); }
+};
+
+// band_ll_w for MetzgerKN by one lane (rescale: the PSO cost's peak rescale)
+__device__ double metzger_ll_lane(const double* p, const BandView& b, const double* cst, bool rescale) {
+    MzPeak pk{b.up, -INFINITY};
+    int j_start;
+    double l_peak;
+    bool ok = metzger_sweep64(p, b.t, b.n, pk, j_start, l_peak);
+    bool valid = ok && l_peak > 0.0 && isfinite(l_peak);
+    double scale = 1.0;
+    if (rescale) {
+        // largest normalised detection prediction; invalid sweeps and the
+        // observations before t0 predict 0
+        double mx = -INFINITY;
+        int z_end = valid ? j_start : b.n;
+        for (int j = 0; j < z_end; j++)
+            if (!b.up[j]) mx = fmax(mx, 0.0);
+        if (valid) mx = fmax(mx, pk.mx / l_peak);
+        if (mx > 1e-10 && isfinite(mx)) scale = fmin(fmax(1.0 / mx, 0.1), 10.0);
+    }
+    MzLl acc{&b, cst, valid ? 1.0 / l_peak : 0.0, scale, 0.0};
+    int z_end = valid ? j_start : b.n;
+    for (int j = 0; j < z_end; j++) acc.term(j, 0.0 * scale);
+    if (valid) {
+        // second sweep: the same interpolants, normalised
+        int js;
+        double lp;
+        struct Norm {
+            MzLl* a;
+            double lpk;
+            __device__ void operator()(int j, double l) { a->term(j, l / lpk * a->scale); }
+        } nv{&acc, l_peak};
+        metzger_sweep64(p, b.t, b.n, nv, js, lp);
+    }
+    return acc.ll;
+}
+
+// shape sums of profile_t0_refine for MetzgerKN by one lane: sw, sy, sf,
+// syf, sff over detections of the normalised prediction
+__device__ void metzger_shape_lane(const double* p, const BandView& b, const double* cst, double* s5) {
+    MzPeak pk{b.up, -INFINITY};
+    int j_start;
+    double l_peak;
+    bool ok = metzger_sweep64(p, b.t, b.n, pk, j_start, l_peak);
+    bool valid = ok && l_peak > 0.0 && isfinite(l_peak);
+    double sw = 0, sy = 0, sf = 0, syf = 0, sff = 0;
+    int z_end = valid ? j_start : b.n;
+    for (int j = 0; j < z_end; j++) {
+        if (b.up[j]) continue;
+        double w = cst[3 * j];
+        sw += w; sy += w * b.f[j];
+    }
+    if (valid) {
+        struct Sums {
+            const BandView* b;
+            const double* cst;
+            double lpk, sw, sy, sf, syf, sff;
+            __device__ void operator()(int j, double l) {
+                if (b->up[j]) return;
+                double sh = l / lpk;
+                if (!isfinite(sh)) return;
+                double w = cst[3 * j], fj = b->f[j];
+                sw += w; sy += w * fj; sf += w * sh; syf += w * fj * sh; sff += w * sh * sh;
+            }
+        } su{&b, cst, l_peak, sw, sy, sf, syf, sff};
+        int js;
+        double lp;
+        metzger_sweep64(p, b.t, b.n, su, js, lp);
+        sw = su.sw; sy = su.sy; sf = su.sf; syf = su.syf; sff = su.sff;
+    }
+    s5[0] = sw; s5[1] = sy; s5[2] = sf; s5[3] = syf; s5[4] = sff;
+}
+
+// profile_t0_refine + profile_refine_all for a MetzgerKN band (np = 5,
+// t0 = p[3], sigma_extra = p[4]; no baseline parameter), lanes over scan
+// points; the sequential decisions run uniformly on the gathered values.
+__device__ void refine_metzger(const BandStats& bs, const BandView& b, const double* cst, double* mu, double* ls) {
+    const int lane = threadIdx.x & 31;
+    constexpr int m = METZGER, np = 5, se = 4, t0i = 3, NG = 25;
+    double t0_lo = bs.t_first - 30.0, t0_hi = bs.t_peak_all + 5.0;
+    if (t0_lo < t0_hi) {
+        auto grid = [&](int gi) { return t0_lo + (t0_hi - t0_lo) * (double)gi / (double)(NG - 1); };
+        // profiled amplitude at each grid t0, then its log-likelihood (rescaled)
+        double my_ll = -INFINITY;
+        if (lane < NG) {
+            double p[MAXP];
+            for (int j = 0; j < np; j++) p[j] = mu[j];
+            p[t0i] = grid(lane);
+            double saved_la = p[0];
+            p[0] = 0.0;
+            double s5[5];
+            metzger_shape_lane(p, b, cst, s5);
+            double syf = s5[3], sff = s5[4];
+            if (sff > 1e-20 && syf / sff > 1e-10) p[0] = log(syf / sff);
+            else p[0] = saved_la;
+            my_ll = metzger_ll_lane(p, b, cst, true);
+        }
+        double best_t0 = mu[t0i], best_ll = -INFINITY;
+        for (int gi = 0; gi < NG; gi++) {
+            double l = __shfl_sync(FULL, my_ll, gi);
+            if (l > best_ll) { best_ll = l; best_t0 = grid(gi); }
+        }
+        // log-likelihood at mu with t0 on each grid point (no rescale)
+        double e_ll = -INFINITY;
+        if (lane < NG) {
+            double p[MAXP];
+            for (int j = 0; j < np; j++) p[j] = mu[j];
+            p[t0i] = grid(lane);
+            e_ll = metzger_ll_lane(p, b, cst, false);
+        }
+        double lo1 = best_t0, hi1 = best_t0, thr = best_ll - 0.5;
+        for (int gi = NG - 1; gi >= 0; gi--) {
+            double t0 = grid(gi);
+            double l = __shfl_sync(FULL, e_ll, gi);
+            if (t0 >= best_t0) continue;
+            if (l >= thr) lo1 = t0;
+            else break;
+        }
+        for (int gi = 0; gi < NG; gi++) {
+            double t0 = grid(gi);
+            double l = __shfl_sync(FULL, e_ll, gi);
+            if (t0 <= best_t0) continue;
+            if (l >= thr) hi1 = t0;
+            else break;
+        }
+        mu[t0i] = best_t0;
+        ls[t0i] = log(fmax((hi1 - lo1) / 2.0, 0.1));
+    }
+    // profile_refine_all: evaluation 0 = mu, 1 + 15 j + gi = parameter j on
+    // grid point gi; two rounds of 32 lanes
+    constexpr int NE = 1 + 4 * 15;
+    double r_ll[2];
+    for (int round = 0; round < 2; round++) {
+        int e = round * 32 + lane;
+        r_ll[round] = -INFINITY;
+        if (e < NE) {
+            double p[MAXP];
+            for (int k = 0; k < np; k++) p[k] = mu[k];
+            if (e > 0) {
+                int j = (e - 1) / 15, gi = (e - 1) % 15;
+                double slo = c_lo[m][j], shi = c_hi[m][j];
+                p[j] = slo + (shi - slo) * (double)gi / 14.0;
+            }
+            r_ll[round] = metzger_ll_lane(p, b, cst, false);
+        }
+    }
+    auto get = [&](int e) {
+        double a = __shfl_sync(FULL, r_ll[0], e & 31), c = __shfl_sync(FULL, r_ll[1], e & 31);
+        return e < 32 ? a : c;
+    };
+    double thr = get(0) - 0.5;
+    for (int j = 0; j < np; j++) {
+        if (j == se) continue;
+        double mu_j = mu[j], svi_sigma = exp(ls[j]);
+        double slo = c_lo[m][j], shi = c_hi[m][j];
+        if (shi - slo < 1e-10) continue;
+        double l1 = mu_j, h1 = mu_j;
+        for (int gi = 0; gi < 15; gi++) {
+            double val = slo + (shi - slo) * (double)gi / 14.0;
+            if (get(1 + j * 15 + gi) >= thr) { l1 = fmin(l1, val); h1 = fmax(h1, val); }
+        }
+        double prof = fmax((h1 - l1) / 2.0, 1e-6);
+        ls[j] = log(fmax(fmax(svi_sigma, prof), c_pop_w[m][j]));
+    }
+}
+
 // symmetric_eigen (Jacobi), src/parametric.rs:2517-2587
 __device__ void jacobi_eigen(double* a, int n, double* ev, double* V) {
     for (int i = 0; i < n * n; i++) V[i] = 0.0;
@@ -348,15 +545,17 @@ __global__ void refine_kernel(DeviceBatch d) {
     double* scr = d.scratch64 + 5 * bs.off;
     double mu[MAXP], ls[MAXP];
     for (int j = 0; j < np; j++) { mu[j] = o.mu[j]; ls[j] = o.log_sigma[j]; }
-    // scans of the models other than MetzgerKN: FP32 evaluation, FP64 terms
+    // scans of the models other than MetzgerKN: FP32 evaluation, FP64 terms;
+    // MetzgerKN: FP64 sweeps, one scan point per lane
     const bool fast = m != METZGER;
     const float4* obs = d.obs + bs.off;
-    if (fast) scan_constants(b, exp(2.0 * mu[se]), scr);
+    scan_constants(b, exp(2.0 * mu[se]), scr);
+    if (!fast) refine_metzger(bs, b, scr, mu, ls);
     auto scan_ll = [&](const double* p, bool rescale) {
         return fast ? band_ll_fast(m, p, obs, b, scr) : band_ll_w(m, b, p, scr, rescale);
     };
     // ---- profile_t0_refine
-    {
+    if (fast) {
         double t0_lo = bs.t_first - 30.0, t0_hi = bs.t_peak_all + 5.0;
         if (t0_lo < t0_hi) {
             const int NG = 25;
@@ -427,7 +626,7 @@ __global__ void refine_kernel(DeviceBatch d) {
         }
     }
     // ---- profile_refine_all
-    {
+    if (fast) {
         double map_ll = scan_ll(mu, false);
         double thr = map_ll - 0.5;
         for (int j = 0; j < np; j++) {

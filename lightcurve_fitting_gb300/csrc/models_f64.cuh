@@ -374,29 +374,35 @@ __device__ __forceinline__ double log_normal_cdf_f64(double x) {
     return log(fmax(phi, 1e-300));
 }
 
-// MetzgerKN over a band whose times are sorted ascending (phase_max over all
-// of them), exactly as metzger_kn_eval_batch; writes n predictions.
-__device__ inline void metzger_f64(const double* p, const double* times, int n, double* out) {
+// MetzgerKN sweep (metzger_kn_eval_batch, src/parametric.rs:544-648) over a
+// band whose times are sorted ascending: integrates the ODE on the 200-point
+// log grid and calls visit(j, l) with the unnormalised luminosity
+// interpolated at every observation j >= j_start (the observations with
+// t - t0 <= 0 come first and predict 0; they are not visited).  Returns
+// false when the reference returns all zeros before integrating
+// (phase_max <= 0.01); l_peak is the grid maximum the predictions are
+// divided by.
+template <class V>
+__device__ __forceinline__ bool metzger_sweep64(const double* p, const double* times, int n, V& visit,
+                                                int& j_start, double& l_peak) {
     const double MSUN = 1.989e33, C = 2.998e10, SPD = 86400.0, PI = 3.14159265358979323846;
     double m_ej = pow(10.0, p[0]) * MSUN, v_ej = pow(10.0, p[1]) * C, kappa_r = pow(10.0, p[2]), t0 = p[3];
     double phase_max = 0.01;
     for (int i = 0; i < n; i++) phase_max = fmax(phase_max, times[i] - t0);
-    if (phase_max <= 0.01) {
-        for (int i = 0; i < n; i++) out[i] = 0.0;
-        return;
-    }
+    j_start = n;
+    l_peak = -INFINITY;
+    if (phase_max <= 0.01) return false;
     const int NG = 200;
     double lmin = log(0.01), lmax = log(phase_max * 1.05);
     double e0 = 0.5 * m_ej * v_ej * v_ej;
     double e_th = e0 / 1e40, e_kin = e0 / 1e40, v = v_ej;
     double gt0 = exp(lmin);
     double r = gt0 * SPD * v;
-    double l_peak = -INFINITY;
     double prev_t = gt0, prev_l = 0.0;
     double t_day = gt0;
     int j = 0;
-    while (j < n && times[j] - t0 <= 0.0) { out[j] = 0.0; j++; }
-    int j_start = j;
+    while (j < n && times[j] - t0 <= 0.0) j++;
+    j_start = j;
     for (int i = 0; i < NG; i++) {
         double t_next = exp(lmin + (lmax - lmin) * (double)(i + 1) / (double)(NG - 1));
         double t_sec = t_day * SPD;
@@ -411,13 +417,13 @@ __device__ inline void metzger_f64(const double* p, const double* times, int n, 
         double l_rad = (e_th > 0.0 && t_diff > 0.0) ? e_th / t_diff : 0.0;
         l_peak = fmax(l_peak, l_rad);
         if (i == 0) {
-            while (j < n && times[j] - t0 <= t_day) { out[j] = l_rad; j++; }
+            while (j < n && times[j] - t0 <= t_day) { visit(j, l_rad); j++; }
         } else {
             while (j < n) {
                 double ph = times[j] - t0;
                 if (ph > t_day) break;
                 double frac = (ph - prev_t) / (t_day - prev_t);
-                out[j] = prev_l + frac * (l_rad - prev_l);
+                visit(j, prev_l + frac * (l_rad - prev_l));
                 j++;
             }
         }
@@ -434,7 +440,22 @@ __device__ inline void metzger_f64(const double* p, const double* times, int n, 
         }
         t_day = t_next;
     }
-    while (j < n) { out[j] = prev_l; j++; }
+    while (j < n) { visit(j, prev_l); j++; }
+    return true;
+}
+
+// MetzgerKN predictions of the band (metzger_kn_eval_batch): the sweep's
+// interpolants divided by l_peak; all zeros when the reference returns
+// zeros (phase_max <= 0.01, or a non-positive / non-finite peak).
+__device__ inline void metzger_f64(const double* p, const double* times, int n, double* out) {
+    for (int i = 0; i < n; i++) out[i] = 0.0;
+    struct Store {
+        double* out;
+        __device__ void operator()(int j, double l) { out[j] = l; }
+    } st{out};
+    int j_start;
+    double l_peak;
+    if (!metzger_sweep64(p, times, n, st, j_start, l_peak)) return;
     if (l_peak <= 0.0 || !isfinite(l_peak)) {
         for (int i = 0; i < n; i++) out[i] = 0.0;
         return;

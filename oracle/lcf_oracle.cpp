@@ -1611,6 +1611,33 @@ static MBResult fit_multi_bazin(const Band& b) {
 // ---------------------------------------------------------------------------
 static inline double fon(double v) { return std::isfinite(v) ? v : NaN; }
 
+// magnitude-space chi2 of the final fit, src/parametric.rs:3680-3711 (the
+// PSO parameters stand in when fewer than half of the predictions are positive)
+static double magnitude_chi2(int m, const Band& b, const Uncert& u, const std::vector<double>& pso_params) {
+    int n = b.n();
+    std::vector<double> sp(n), mp(n);
+    eval_batch(m, u.mu.data(), b.t.data(), n, sp.data());
+    int npos = 0;
+    for (int i = 0; i < n; i++) if (sp[i] * b.peak > 0.0) npos++;
+    if (npos < n / 2) eval_batch(m, pso_params.data(), b.t.data(), n, mp.data());
+    else mp = sp;
+    double msum = 0.0;
+    int mcount = 0;
+    for (int i = 0; i < n; i++) {
+        double pf = mp[i] * b.peak;
+        if (pf > 0.0 && b.f[i] > 0.0) {
+            double mpred = -2.5 * std::log10(pf) + 23.9;
+            double merr = 1.0857 * b.fe[i] / b.f[i];
+            if (merr > 0.0) {
+                double res = b.mags[i] - mpred;
+                msum += res * res / (merr * merr);
+                mcount++;
+            }
+        }
+    }
+    return mcount > 0 ? msum / (double)mcount : NaN;
+}
+
 static void fit_source(const lcf_bands_csr* in, const lcf_fit_options* o, int src, lcf_fit_outputs* out) {
     int b0 = in->source_band_offsets[src], b1 = in->source_band_offsets[src + 1];
     struct Entry { int band; Band data; };
@@ -1652,27 +1679,7 @@ static void fit_source(const lcf_bands_csr* in, const lcf_fit_options* o, int sr
         profile_t0_refine(m, u, b);
         profile_refine_all(m, u, b);
         int n = b.n();
-        std::vector<double> sp(n), mp(n);
-        eval_batch(m, u.mu.data(), b.t.data(), n, sp.data());
-        int npos = 0;
-        for (int i = 0; i < n; i++) if (sp[i] * b.peak > 0.0) npos++;
-        if (npos < n / 2) eval_batch(m, pso_params.data(), b.t.data(), n, mp.data());
-        else mp = sp;
-        double msum = 0.0;
-        int mcount = 0;
-        for (int i = 0; i < n; i++) {
-            double pf = mp[i] * b.peak;
-            if (pf > 0.0 && b.f[i] > 0.0) {
-                double mpred = -2.5 * std::log10(pf) + 23.9;
-                double merr = 1.0857 * b.fe[i] / b.f[i];
-                if (merr > 0.0) {
-                    double res = b.mags[i] - mpred;
-                    msum += res * res / (merr * merr);
-                    mcount++;
-                }
-            }
-        }
-        double mag_chi2 = mcount > 0 ? msum / (double)mcount : NaN;
+        double mag_chi2 = magnitude_chi2(m, b, u, pso_params);
         out->model[bi] = m;
         out->rank[bi] = rk;
         out->n_obs[bi] = n;
@@ -1818,6 +1825,23 @@ int orc_laplace_fit(int m, const double* t, const double* f, const double* var, 
     Uncert u = laplace_fit(m, b, mp);
     for (int j = 0; j < N_PARAMS[m]; j++) log_sigma[j] = u.log_sigma[j];
     *elbo = u.elbo;
+    return 0;
+}
+
+// Laplace at `params` (the polished fit of model m), then profile_t0_refine,
+// profile_refine_all and the magnitude chi2, on a raw band (times, flux,
+// err) prepared as fit_parametric_model does; returns 0, or -1 for a band
+// the reference does not fit.
+int orc_laplace_refine(int m, const double* times, const double* flux, const double* err, int n,
+                       const double* params, double* mu, double* log_sigma, double* mag) {
+    Band b;
+    if (!prepare_band(times, flux, err, n, b)) return -1;
+    std::vector<double> pp(params, params + N_PARAMS[m]);
+    Uncert u = laplace_fit(m, b, pp);
+    profile_t0_refine(m, u, b);
+    profile_refine_all(m, u, b);
+    for (int j = 0; j < N_PARAMS[m]; j++) { mu[j] = u.mu[j]; log_sigma[j] = u.log_sigma[j]; }
+    *mag = magnitude_chi2(m, b, u, pp);
     return 0;
 }
 

@@ -64,6 +64,7 @@ def lib():
         L.orc_svi_fit.argtypes = [i, vp, vp, vp, vp, vp, i, vp, i, i, d, vp, vp, vp]
         L.orc_laplace_fit.argtypes = [i, vp, vp, vp, vp, vp, i, vp, vp, vp]
         L.orc_fit_batch.argtypes = [C.POINTER(abi.BandsCSR), C.POINTER(abi.FitOptions), C.POINTER(abi.FitOutputs), i]
+        L.orc_laplace_refine.argtypes = [i, vp, vp, vp, i, vp, vp, vp, vp]
         L.orc_pso_stats.argtypes = [vp, i]
         L.orc_max_threads.restype = i
         _lib = L
@@ -157,6 +158,20 @@ def svi_fit(model: int, band: Band, init, n_steps=1000, n_samples=4, lr=0.01):
     mu, ls, elbo = np.zeros(npar), np.zeros(npar), np.zeros(1)
     steps = lib().orc_svi_fit(model, *band.args(), _p(ini), n_steps, n_samples, lr, _p(mu), _p(ls), _p(elbo))
     return mu, ls, float(elbo[0]), steps
+
+
+def laplace_refine(model: int, times, flux, flux_err, params):
+    """Laplace at ``params``, then the profile refinements and the magnitude
+    chi2 (src/parametric.rs:2464-3008, 3680-3711) on a raw band: returns
+    (mu, log_sigma, mag_chi2), or None for a band the reference skips."""
+    t = np.ascontiguousarray(times, np.float64)
+    f = np.ascontiguousarray(flux, np.float64)
+    e = np.ascontiguousarray(flux_err, np.float64)
+    k = abi.N_PARAMS[model]
+    p = np.ascontiguousarray(params[:k], np.float64)
+    mu, ls, mag = np.zeros(k), np.zeros(k), np.zeros(1)
+    rc = lib().orc_laplace_refine(int(model), _p(t), _p(f), _p(e), t.size, _p(p), _p(mu), _p(ls), _p(mag))
+    return None if rc != 0 else (mu, ls, float(mag[0]))
 
 
 def fit_batch(batch, fit_all_models=True, method=abi.METHOD_SVI, forced_model=-1, run_multi_bazin=True,

@@ -192,36 +192,57 @@ def test_fit_laplace_matches_oracle(ctx, oracle):
     assert np.isfinite(res.svi_log_sigma[same][:, 0]).all()
 
 
+def _refine_agreement(res, batch, oracle):
+    """Per fitted band: does the GPU's Laplace + refinements + magnitude chi2
+    match the oracle's run from the same model and polished parameters?"""
+    ok = {}
+    for s in range(batch.n_sources):
+        for k, (t, f, e) in enumerate(batch.bands_of(s)):
+            b = batch.source_band_offsets[s] + k
+            m = int(res.model[b])
+            if m < 0:
+                continue
+            mu, ls, mag = oracle.laplace_refine(m, t, f, e, res.pso_params[b])
+            n = abi.N_PARAMS[m]
+            ok_mu = np.allclose(res.svi_mu[b, :n], mu, rtol=1e-9, atol=1e-9)
+            ok_ls = np.allclose(res.svi_log_sigma[b, :n], ls, rtol=0.0, atol=1e-5)
+            ok_mag = np.allclose(res.mag_chi2[b], mag, rtol=1e-6, equal_nan=True)
+            ok[b] = (m, ok_mu, ok_mu and ok_ls and ok_mag)
+    return ok
+
+
 def test_refinements_match_oracle_on_equal_inputs(ctx, oracle):
-    """profile_t0_refine / profile_refine_all (src/parametric.rs:2705-3008) and
-    the magnitude chi2: for bands where the GPU and the oracle reach the same
-    polished parameters (Laplace: mu = those parameters), the refined t0, the
-    refined log sigmas and mag chi2 agree.  The scans of the models other
-    than MetzgerKN evaluate in FP32 against thresholds 0.5 apart, so a grid
-    decision may flip only for a log-likelihood within ~1e-5 of a threshold.
-    Inputs count as equal when the polished parameters agree to 1e-7; the
-    Laplace log sigmas carry the finite-difference Hessian's rounding (h =
-    1e-4 turns 1e-14 cost rounding into ~1e-7), so log sigma is compared to
-    1e-5 and mu / mag chi2 to 1e-6.  At least 95 % of the bands match."""
-    batch = synth.config_uneven(40, seed=17)
+    """Laplace, profile_t0_refine, profile_refine_all and the magnitude chi2
+    (src/parametric.rs:2464-3008, 3680-3711): the oracle repeats them from
+    the GPU's own selected model and polished parameters, so both sides get
+    identical inputs.  The refinement scans of the models other than
+    MetzgerKN evaluate in FP32 against log-likelihood thresholds 0.5 apart,
+    so a grid decision may flip only for a value within ~1e-5 of a
+    threshold; the Laplace log sigmas carry the finite-difference Hessian's
+    rounding (h = 1e-4 turns 1e-14 cost rounding into ~1e-7).  Tolerances:
+    mu 1e-9, log sigma 1e-5, mag chi2 1e-6; >= 95 % of the bands match."""
+    batch = synth.config_uneven(30, seed=17)
     res = ctx.fit_batch(batch, fit_all_models=True, method=abi.METHOD_LAPLACE, run_multi_bazin=False)
-    ref = oracle.fit_batch(batch, fit_all_models=True, method=abi.METHOD_LAPLACE, run_multi_bazin=False)
-    same = (ref.model >= 0) & (res.model == ref.model)
-    idx = []
-    for b in np.flatnonzero(same):
-        k = abi.N_PARAMS[ref.model[b]]
-        d = np.abs(res.pso_params[b, :k] - ref.pso_params[b, :k]) / np.maximum(np.abs(ref.pso_params[b, :k]), 1.0)
-        if d.max() < 1e-7:
-            idx.append(b)
-    assert len(idx) >= 20, len(idx)
-    ok = []
-    for b in idx:
-        k = abi.N_PARAMS[ref.model[b]]
-        m1 = np.allclose(res.svi_mu[b, :k], ref.svi_mu[b, :k], rtol=1e-6, atol=1e-6)
-        m2 = np.allclose(res.svi_log_sigma[b, :k], ref.svi_log_sigma[b, :k], rtol=0.0, atol=1e-5)
-        m3 = np.allclose(res.mag_chi2[b], ref.mag_chi2[b], rtol=1e-6, equal_nan=True)
-        ok.append(m1 and m2 and m3)
-    assert np.mean(ok) >= 0.95, (np.mean(ok), len(idx))
+    ok = _refine_agreement(res, batch, oracle)
+    assert len(ok) >= 60
+    frac = np.mean([v[2] for v in ok.values() if v[0] != 7])
+    assert frac >= 0.95, frac
+
+
+def test_metzger_refinements_match_oracle_on_equal_inputs(ctx, oracle):
+    """The MetzgerKN refinement scans (one FP64 ODE sweep per lane and scan
+    point) from identical inputs.  MetzgerKN's explicit Euler steps amplify
+    the last-bit differences of the device and host libm (exp, pow, atan),
+    so its log-likelihoods agree to ~1e-6 relative and its finite-difference
+    Hessian much less; the refined t0 (a grid point chosen by comparisons of
+    those log-likelihoods) and the other mu match for >= 80 % of the bands."""
+    batch = synth.config_uneven(10, seed=23)
+    res = ctx.fit_batch(batch, fit_all_models=True, method=abi.METHOD_LAPLACE, forced_model=7,
+                        run_multi_bazin=False)
+    ok = _refine_agreement(res, batch, oracle)
+    assert len(ok) >= 20 and all(v[0] == 7 for v in ok.values())
+    frac = np.mean([v[1] for v in ok.values()])
+    assert frac >= 0.8, frac
 
 
 def test_fit_is_deterministic(ctx):
