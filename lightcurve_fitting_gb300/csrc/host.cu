@@ -106,7 +106,7 @@ struct lcf_ctx {
     float* d_eps = nullptr;
     // device buffers (capacity-sized)
     DevArr times, flux, ferr, boff, soff, stats_b, obs, t64, f64, fe64, var64, uf64, mag64, up, res, fits, out, mb,
-        ctr, scratch, scratch64, scratch_svi, t0state, tasks[7];
+        ctr, scratch, scratch64, scratch_svi, t0state, tasks[7], task_sorted;
     int64_t task_cap[7] = {0, 0, 0, 0, 0, 0, 0};
     // pinned staging
     DevArr h_in, h_out;
@@ -235,7 +235,7 @@ extern "C" void lcf_ctx_destroy(lcf_ctx* ctx) {
     DevArr* all[] = {&ctx->times, &ctx->flux, &ctx->ferr, &ctx->boff, &ctx->soff, &ctx->stats_b, &ctx->obs,
                      &ctx->t64, &ctx->f64, &ctx->fe64, &ctx->var64, &ctx->uf64, &ctx->mag64, &ctx->up, &ctx->res,
                      &ctx->fits, &ctx->out, &ctx->mb, &ctx->ctr, &ctx->scratch, &ctx->scratch64, &ctx->scratch_svi,
-                     &ctx->t0state,
+                     &ctx->t0state, &ctx->task_sorted,
                      &ctx->bc_obs, &ctx->bc_params, &ctx->bc_costs, &ctx->bc_scratch, &ctx->plain_scr};
     for (DevArr* a : all) free_arr(*a);
     for (auto& a : ctx->tasks) free_arr(a);
@@ -345,6 +345,7 @@ static int prepare_layout(lcf_ctx* ctx, int n_sources, int n_bands, int64_t n_ob
         rc |= grow(ctx, ctx->tasks[s], (size_t)caps[s] * sizeof(PsoTask));
         ctx->task_cap[s] = caps[s];
     }
+    rc |= grow(ctx, ctx->task_sorted, (size_t)nb * 21 * sizeof(PsoTask));  // the largest of slots 1..6
     if (rc) return rc;
     // stage-1 task list (bands, models, restarts; MultiBazin K = 1), longest first
     if (!same) {
@@ -442,6 +443,7 @@ static int prepare_layout(lcf_ctx* ctx, int n_sources, int n_bands, int64_t n_ob
     }
     d.tasks[7] = nullptr;
     d.task_cap[7] = 0;
+    d.task_sorted = (PsoTask*)ctx->task_sorted.p;
     d.ctr = (Counters*)ctx->ctr.p;
     d.scratch = (float*)ctx->scratch.p;
     d.scratch_per_warp = 32 * n_max;
@@ -470,23 +472,26 @@ static void enqueue_pipeline(lcf_ctx* ctx) {
     cudaMemsetAsync(ctx->fits.p, 0xff, (size_t)std::max(ctx->n_bands, 1) * 8 * sizeof(ModelFit), s);
     launch_prep(d, s); L++;
     cudaEventRecordWithFlags(ctx->ev[1], s, cudaEventRecordExternal);
-    launch_pso(d, 0, ctx->n_tasks0, 7, grid, block, s); L++;
+    launch_pso(d, 0, d.tasks[0], ctx->n_tasks0, 7, grid, block, s); L++;
     cudaEventRecordWithFlags(ctx->ev[2], s, cudaEventRecordExternal);
     int gated = (o.forced_model < 0 && !o.fit_all_models);
     launch_lbfgs(d, gated ? 1 : 0xff, s); L++;
     if (gated) {
         launch_gate_build(d, 1, s); L++;
-        launch_pso(d, 1, -1, 7, grid, block, s); L++;
+        launch_task_sort(d, 1, s); L += 3;
+        launch_pso(d, 1, d.task_sorted, -1, 7, grid, block, s); L++;
         launch_lbfgs(d, 0xfe, s); L++;
     }
     launch_select(d, o.fit_all_models, o.forced_model, s); L++;
     cudaEventRecordWithFlags(ctx->ev[3], s, cudaEventRecordExternal);
     if (o.method == LCF_METHOD_SVI) {
         launch_t0_build(d, 2, 0, s); L++;
-        launch_pso(d, 2, -1, 7, grid, block, s); L++;
+        launch_task_sort(d, 2, s); L += 3;
+        launch_pso(d, 2, d.task_sorted, -1, 7, grid, block, s); L++;
         launch_t0_pick(d, 2, 0, s); L++;
         launch_t0_build(d, 3, 1, s); L++;
-        launch_pso(d, 3, -1, 7, grid, block, s); L++;
+        launch_task_sort(d, 3, s); L += 3;
+        launch_pso(d, 3, d.task_sorted, -1, 7, grid, block, s); L++;
         launch_t0_pick(d, 3, 1, s); L++;
     }
     cudaEventRecordWithFlags(ctx->ev[4], s, cudaEventRecordExternal);
@@ -500,7 +505,8 @@ static void enqueue_pipeline(lcf_ctx* ctx) {
         launch_mb_pick(d, 1, s); L++;
         for (int k = 2; k <= 4; k++) {
             launch_mb_build(d, 2 + k, k, s); L++;
-            launch_pso(d, 2 + k, -1, 4 * k + 2, grid, block, s); L++;
+            launch_task_sort(d, 2 + k, s); L += 3;
+            launch_pso(d, 2 + k, d.task_sorted, -1, 4 * k + 2, grid, block, s); L++;
             launch_mb_pick(d, k, s); L++;
         }
     }

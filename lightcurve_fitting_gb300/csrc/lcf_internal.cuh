@@ -190,6 +190,7 @@ struct Counters {
     unsigned long long slot0_evals[12];      // particle x observation evaluations of the first PSO launch, by kind
     unsigned long long slot0_particles[12];  // particle evaluations of the first PSO launch, by kind
     unsigned long long lb_polishes, lb_iters, lb_evals, lb_obs_evals;  // L-BFGS work
+    int32_t sort_hist[8][256];  // per slot: key histogram, then offsets, of the device task sort
     int32_t error;              // first error code raised on the device
     int32_t pad;
 };
@@ -223,6 +224,7 @@ struct DeviceBatch {
     MbState* mb;            // [n_bands]
     PsoTask* tasks[8];      // per launch slot
     int task_cap[8];
+    PsoTask* task_sorted;   // device-built task lists after the sort (capacity: the largest of slots 1..6)
     Counters* ctr;
     float* scratch;         // MetzgerKN per-warp scratch: [warps][n_max][32]
     int64_t scratch_per_warp;
@@ -241,7 +243,11 @@ struct DeviceBatch {
 void launch_prep(const DeviceBatch& d, cudaStream_t s);
 // Run the PSO tasks of `slot` (count = n_host if >= 0, else the device
 // counter of the slot).  `max_dim` selects the kernel instantiation.
-void launch_pso(const DeviceBatch& d, int slot, int n_host, int max_dim, int grid, int block, cudaStream_t s);
+void launch_pso(const DeviceBatch& d, int slot, const PsoTask* tasks, int n_host, int max_dim, int grid, int block,
+                cudaStream_t s);
+// Sort the device-built task list of `slot` into d.task_sorted: MetzgerKN
+// first, then by kind, longest bands first within a kind.
+void launch_task_sort(const DeviceBatch& d, int slot, cudaStream_t s);
 size_t pso_smem_bytes(int block, int smem_obs);
 int pso_blocks_per_sm(int block, size_t smem);
 int pso_init_attributes(int block, int smem_obs);

@@ -301,8 +301,10 @@ struct Nll {
             nonfinite = 1;
         }
     }
-    // cost = (sum + prior / n) / n in FP64, with the reference's special values
-    __device__ __forceinline__ double finish(double prior, double n) const {
+    // cost = (sum + prior / n) / n in FP64 (inv_n = 1 / n: the FP64 pipe runs
+    // at 1/64 of the FP32 rate, and two divisions per evaluation would cost as
+    // much as the observation loop), with the reference's special values
+    __device__ __forceinline__ double finish(double prior, double inv_n) const {
         if (nonfinite) return BIG_COST;
         if (inf) return INFINITY;
         double tot = (double)s - (double)c;
@@ -310,7 +312,7 @@ struct Nll {
             if (big > LN_DBL_MAX) return INFINITY;
             tot += exp((double)big);
         }
-        return (tot + prior / n) / n;
+        return (tot + prior * inv_n) * inv_n;
     }
 };
 
@@ -361,10 +363,14 @@ struct MetzgerF {
         for (int i = 0; i < NG; i++) {
             float t_next = expf(lmin + dl * (float)(i + 1));
             float t_sec = t_day * SPD;
-            float ef = 0.34f * exp2f(0.74f * log2f(t_day));
+            // t_day^0.74 from ln t_day = lmin + dl * i (the grid's own exponent)
+            float ef = 0.34f * exp2f((0.74f * 1.4426950408889634f) * (lmin + dl * (float)i));
             float eth = 0.36f * (expf(-0.56f * t_day) + (ef > 1e-10f ? log1pf(ef) / ef : 1.0f));
-            float xn = xn0 * expf(-t_sec * (1.0f / 900.0f));
-            float tt = atanf(0.11f / (t_sec - 1.3f)) * (1.0f / PI_F);
+            // e^(-t/900) is 0 in FP32 past 93,600 s
+            float xn = t_sec < 93600.0f ? xn0 * expf(-t_sec * (1.0f / 900.0f)) : 0.0f;
+            // 1/2 - atan((t - 1.3) / 0.11) / pi = atan(y) / pi with y = 0.11 / (t - 1.3)
+            // <= 1.3e-4 on the grid (t >= 864 s), where atan(y) = y in FP32
+            float tt = (0.11f / PI_F) / (t_sec - 1.3f);
             tt = fmaxf(tt, 1e-30f);
             float eps_rp = 2e18f * eth * exp2f(1.3f * log2f(tt));
             float l_heat = m_over_scale * (3.2e14f * xn + eps_rp);

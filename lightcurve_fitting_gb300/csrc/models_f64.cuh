@@ -214,6 +214,21 @@ struct Model64 {
             default: c[0] = exp(p[0]); c[1] = p[1]; c[2] = p[2]; c[3] = p[3]; c[4] = p[4]; break;
         }
     }
+    // init() from precomputed ep[k] = exp(p[k]) and rp[k] = 1.0 / exp(p[k])
+    // (the same constants, bit for bit)
+    __device__ void init_pre(int model, const double* p, const double* ep, const double* rp) {
+        m = model;
+        switch (m) {
+            case 0: c[0] = ep[0]; c[1] = p[1]; c[2] = p[2]; c[3] = rp[3]; c[4] = rp[4]; break;
+            case 1: c[0] = ep[0]; c[1] = p[1]; c[2] = ep[2]; c[3] = p[3]; c[4] = rp[4];
+                    c[5] = rp[5]; c[6] = 1.0 - p[1] * ep[2]; break;
+            case 2: c[0] = ep[0]; c[1] = p[1]; c[2] = p[2]; c[3] = rp[3]; c[4] = rp[4]; c[5] = p[5]; break;
+            case 3: c[0] = ep[0]; c[1] = p[1]; c[2] = rp[2]; c[3] = 1.0 / (1.0 + exp(-p[3])); break;
+            case 4: c[0] = ep[0]; c[1] = p[1]; c[2] = rp[2]; c[3] = rp[3]; break;
+            case 5: c[0] = ep[0]; c[1] = p[1]; c[2] = p[2]; c[3] = rp[3]; break;
+            default: c[0] = ep[0]; c[1] = p[1]; c[2] = p[2]; c[3] = p[3]; c[4] = p[4]; break;
+        }
+    }
     // prediction; with g != nullptr also d pred / d theta (sigma_extra slot 0)
     __device__ double eval(double t, double* g) const {
         switch (m) {

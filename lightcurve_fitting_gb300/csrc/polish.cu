@@ -39,45 +39,27 @@ __device__ __forceinline__ float warp_sum_f(float v) {
 }
 __device__ __forceinline__ int warp_or(int v) { return __any_sync(FULL, v) ? 1 : 0; }
 
-// Warp-wide negative log-likelihood of a parameter vector (cost of PsoCost
-// without the Villar constraint and prior): lanes over observations.
-__device__ double warp_nll(int m, const double* pd, const float4* obs, int n, double nd, double prior) {
-    float se = (float)exp(pd[se_idx_of(m)]);
-    float se2 = se * se;
-    Nll acc;
-    acc.reset();
-    int lane = threadIdx.x & 31;
-    for (int i = lane; i < n; i += 32) {
-        float4 o = obs[i];
-        int st = ST_OK;
-        float pr;
-        switch (m) {
-            case BAZIN: { BazinF e; e.init64(pd); pr = e.eval(o.x, o.y, st); break; }
-            case VILLAR: { VillarF e; e.init64(pd); pr = e.eval(o.x, o.y, st); break; }
-            case TDE: { TdeF e; e.init64(pd); pr = e.eval(o.x, o.y, st); break; }
-            case ARNETT: { ArnettF e; e.init64(pd); pr = e.eval(o.x, o.y, st); break; }
-            case MAGNETAR: { MagnetarF e; e.init64(pd); pr = e.eval(o.x, o.y, st); break; }
-            case SHOCK: { ShockF e; e.init64(pd); pr = e.eval(o.x, o.y, st); break; }
-            default: { AfterglowF e; e.init64(pd); pr = e.eval(o.x, o.y, st); break; }
-        }
-        acc.obs(o, pr, st, se2);
+// Sums 8 per-lane values over the warp by recursive halving: 4 + 2 + 1
+// exchanges halve the values each lane carries, two more finish the sum.
+// Lane l returns the warp total of v[(l >> 2) & 7].
+__device__ __forceinline__ double reduce_scatter8(const double* v) {
+    const int lane = threadIdx.x & 31;
+    const bool b4 = lane & 16, b3 = lane & 8, b2 = lane & 4;
+    double a[4], b[2];
+#pragma unroll
+    for (int i = 0; i < 4; i++) {
+        double keep = b4 ? v[4 + i] : v[i], give = b4 ? v[i] : v[4 + i];
+        a[i] = keep + __shfl_xor_sync(FULL, give, 16);
     }
-    // combine the lanes
-    double s = warp_sum_d((double)acc.s - (double)acc.c);
-    int nf = warp_or(acc.nonfinite), inf = warp_or(acc.inf);
-    float big = acc.big;
-    for (int k = 16; k; k >>= 1) {
-        float o = __shfl_xor_sync(FULL, big, k);
-        float mx = fmaxf(big, o);
-        big = (mx == -INFINITY) ? -INFINITY : mx + log1pf(expf(-fabsf(big - o)));
+#pragma unroll
+    for (int i = 0; i < 2; i++) {
+        double keep = b3 ? a[2 + i] : a[i], give = b3 ? a[i] : a[2 + i];
+        b[i] = keep + __shfl_xor_sync(FULL, give, 8);
     }
-    if (nf) return BIG_COST;
-    if (inf) return INFINITY;
-    if (big > -INFINITY) {
-        if (big > LN_DBL_MAX) return INFINITY;
-        s += exp((double)big);
-    }
-    return (s + prior / nd) / nd;
+    double c = (b2 ? b[1] : b[0]) + __shfl_xor_sync(FULL, b2 ? b[0] : b[1], 4);
+    c += __shfl_xor_sync(FULL, c, 2);
+    c += __shfl_xor_sync(FULL, c, 1);
+    return c;
 }
 
 // Cost and projected gradient of the bounded problem (BoundedPsoCost,
@@ -95,35 +77,56 @@ struct LaneLb {
     const double *t, *flux, *var, *uf;
     const uint8_t* up;
     int n;
-    double nd;
+    double nd, inv_nd;
     double lo_j, hi_j;
     int evals, iters;
 
+#ifdef LCF_LB_INLINE
     __device__ void cost_grad(double xj, double& fo, double& gj, bool want_grad) {
+#else
+    // out of line: one copy of the observation loop per model instead of one
+    // per call site keeps the polish's hot code in the instruction cache
+    __device__ __noinline__ void cost_grad(double xj, double& fo, double& gj, bool want_grad) {
+#endif
         evals++;
         const int lane = threadIdx.x & 31, j = lane & 7;
+        // lane j forms exp and 1/exp of its own component; the full vectors
+        // are gathered by shuffles (one FP64 exp per warp instead of one per
+        // constant: the FP64 pipe is 1/64 of FP32 on this part)
         const double qj = fmin(fmax(xj, lo_j), hi_j);
-        double q[MAXP];
+        const double ej = exp(qj), rj = 1.0 / ej;
+        double q[MAXP], ep[MAXP], rp[MAXP];
 #pragma unroll
-        for (int k = 0; k < MAXP; k++) q[k] = k < np ? __shfl_sync(FULL, qj, k) : 0.0;
+        for (int k = 0; k < MAXP; k++) {
+            q[k] = k < np ? __shfl_sync(FULL, qj, k) : 0.0;
+            ep[k] = k < np ? __shfl_sync(FULL, ej, k) : 1.0;
+            rp[k] = k < np ? __shfl_sync(FULL, rj, k) : 1.0;
+        }
         constexpr int se = se_idx_of(MODEL);
-        const double se2 = exp(2.0 * q[se]);
+        const double se2 = ep[se] * ep[se];  // sigma_extra = exp(p[se]), squared
         bool constrained = false;
         double f = 0.0;
         if (MODEL == VILLAR) {
-            double beta = q[1], gamma = exp(q[2]), tr = exp(q[4]), tf = exp(q[5]);
+            double beta = q[1], gamma = ep[2], tr = ep[4], tf = ep[5];
             double c1 = fmax(gamma * beta - 1.0, 0.0);
             double c2 = fmax(exp(-gamma / tr) * (tf / tr - 1.0) - 1.0, 0.0);
             double c3 = fmax(beta * tf - 1.0 + beta * gamma, 0.0);
             double cc = c1 + c2 + c3;
             if (cc > 0.0) { f = 1e12 + 10000.0 * cc; constrained = true; }
         }
+        // population prior, one component per lane (PsoCost::cost_from_slice)
+        double zj = 0.0;
+        if (j < np) {
+            double w = c_pop_w[MODEL][j];
+            if (w > 0.0) zj = (qj - c_pop_c[MODEL][j]) / w;
+        }
+        const double prior = dot8(0.5 * zj, zj);
         double nll = 0.0, gl[MAXP];
 #pragma unroll
         for (int k = 0; k < MAXP; k++) gl[k] = 0.0;
         int nonfinite = 0;
         Model64 mod;
-        mod.init(MODEL, q);
+        mod.init_pre(MODEL, q, ep, rp);
         for (int i = lane; i < n; i += 32) {
             double mg[MAXP];
             double pr = mod.eval(t[i], want_grad ? mg : nullptr);
@@ -153,29 +156,19 @@ struct LaneLb {
             }
         }
         nonfinite = warp_or(nonfinite);
-        if (!constrained) {
-            if (nonfinite) f = BIG_COST;
-            else {
-                double prior = 0.0;
-#pragma unroll
-                for (int k = 0; k < np; k++) {
-                    double w = c_pop_w[MODEL][k];
-                    if (w > 0.0) {
-                        double z = (q[k] - c_pop_c[MODEL][k]) / w;
-                        prior += 0.5 * z * z;
-                    }
-                }
-                f = (warp_sum_d(nll) + prior / nd) / nd;
-            }
+        double nsum, gs = 0.0;
+        if (want_grad) {
+            // reduce-scatter of the 8 sums: lane l ends with sum (l >> 2) & 7
+            double v[8] = {nll, gl[0], gl[1], gl[2], gl[3], gl[4], gl[5], gl[6]};
+            double tot = reduce_scatter8(v);
+            nsum = __shfl_sync(FULL, tot, 0);
+            gs = __shfl_sync(FULL, tot, (4 * (1 + j)) & 31);
+        } else {
+            nsum = warp_sum_d(nll);
         }
+        if (!constrained) f = nonfinite ? BIG_COST : (nsum + prior * inv_nd) * inv_nd;
         fo = f;
         if (!want_grad) return;
-        double gs = 0.0;
-#pragma unroll
-        for (int k = 0; k < np; k++) {
-            double gk = warp_sum_d(gl[k]);
-            if (k == j) gs = gk;
-        }
         gj = (nonfinite || j >= np) ? 0.0 : gs / nd;
         if ((xj <= lo_j && gj > 0.0) || (xj >= hi_j && gj < 0.0)) gj = 0.0;
     }
@@ -205,6 +198,7 @@ __device__ void polish_band(const DeviceBatch& d, int b) {
         c.up = d.up + bs.off;
         c.n = bs.n;
         c.nd = (double)max(bs.n, 1);
+        c.inv_nd = 1.0 / c.nd;
         c.evals = 0;
         c.iters = 0;
         c.lo_j = j < np ? c_lo[MODEL][j] : 0.0;
@@ -291,32 +285,55 @@ void launch_select(const DeviceBatch& d, int fit_all, int forced, cudaStream_t s
 }
 
 // ---------------------------------------------------------------------------
-// SVI, one warp per band
+// SVI, one warp per band, templated on the band's selected model.  Lanes
+// split the observations for the likelihood and its adjoint; the
+// per-parameter bookkeeping (reparameterisation, prior, ELBO gradient) runs
+// with component j in lane j, and Adam with variational parameter i (mu_i,
+// then log sigma_i) in lane i.
 // ---------------------------------------------------------------------------
-__global__ void svi_kernel(DeviceBatch d) {
+// Sums 8 per-lane FP32 values over the warp (recursive halving, as
+// reduce_scatter8): lane l returns the total of v[(l >> 2) & 7].
+__device__ __forceinline__ float reduce_scatter8f(const float* v) {
     const int lane = threadIdx.x & 31;
-    const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    if (warp >= d.n_bands) return;
-    const int b = warp;
+    const bool b4 = lane & 16, b3 = lane & 8, b2 = lane & 4;
+    float a[4], b[2];
+#pragma unroll
+    for (int i = 0; i < 4; i++) {
+        float keep = b4 ? v[4 + i] : v[i], give = b4 ? v[i] : v[4 + i];
+        a[i] = keep + __shfl_xor_sync(FULL, give, 16);
+    }
+#pragma unroll
+    for (int i = 0; i < 2; i++) {
+        float keep = b3 ? a[2 + i] : a[i], give = b3 ? a[i] : a[2 + i];
+        b[i] = keep + __shfl_xor_sync(FULL, give, 8);
+    }
+    float c = (b2 ? b[1] : b[0]) + __shfl_xor_sync(FULL, b2 ? b[0] : b[1], 4);
+    c += __shfl_xor_sync(FULL, c, 2);
+    c += __shfl_xor_sync(FULL, c, 1);
+    return c;
+}
+
+template <int M>
+__device__ void svi_band(const DeviceBatch& d, int b) {
+    const int lane = threadIdx.x & 31, j = lane & 7;
     const BandStats bs = d.stats[b];
     BandOut& o = d.out[b];
-    if (!bs.valid || o.model < 0) return;
-    const int m = o.model, np = n_params_of(m), se = se_idx_of(m), n = bs.n;
+    if (!bs.valid || o.model != M) return;
+    constexpr int np = n_params_of(M), se = se_idx_of(M);
+    const int n = bs.n;
     const float4* obs = d.obs + bs.off;
-    double init[MAXP];
-    for (int j = 0; j < np; j++) init[j] = o.pso_params[j];
-    // lane i < 2 np owns variational parameter i (mu_j, then log sigma_j)
+    const bool own = j < np;  // this lane's component is a model parameter
+    // prior of component j: centre (the PSO value, or the fixed centre of
+    // sigma_extra) and variance
+    const double init_j = own ? o.pso_params[j] : 0.0;
+    const double pc_j = own ? (j == se ? c_pri_c[M][j] : init_j) : 0.0;
+    const double pw2_j = own ? c_pri_w[M][j] * c_pri_w[M][j] : 1.0;
+    // lane i < 2 np owns variational parameter i (mu_i, then log sigma_i)
     double vp = 0.0, am = 0.0, av = 0.0;
-    bool frozen = false;
-    if (lane < np) vp = init[lane];
+    if (lane < np) vp = o.pso_params[lane];
     else if (lane < 2 * np) vp = -1.0;
+    bool frozen = false;
     const float* eps_tab = d.svi_eps + (size_t)(np - 5) * SVI_STEPS * SVI_SAMPLES * 7;
-    double pc[MAXP], pw2[MAXP];
-    for (int j = 0; j < np; j++) {
-        pc[j] = j == se ? c_pri_c[m][j] : init[j];
-        double w = c_pri_w[m][j];
-        pw2[j] = w * w;
-    }
     const double ln_2pie = 2.8378770664093453;  // ln(2 pi e)
     double b1t = 1.0, b2t = 1.0;
     double ema = -INFINITY, best_ema = -INFINITY, final_elbo = -INFINITY;
@@ -325,46 +342,44 @@ __global__ void svi_kernel(DeviceBatch d) {
     float* mscr = d.scratch_svi + 20 * bs.off;
     struct ObsTimes {
         const float4* o;
-        __device__ float operator()(int j) const { return o[j].x + o[j].y; }
+        __device__ float operator()(int q) const { return o[q].x + o[q].y; }
     } otimes{obs};
     for (int step = 0; step < SVI_STEPS; step++) {
         steps = step + 1;
-        double mu[MAXP], sg[MAXP];
-        for (int j = 0; j < np; j++) {
-            mu[j] = __shfl_sync(FULL, vp, j);
-            sg[j] = exp(__shfl_sync(FULL, vp, np + j));
-        }
-        double gmu[MAXP], gls[MAXP];
-        for (int j = 0; j < np; j++) { gmu[j] = 0.0; gls[j] = 0.0; }
-        double elbo_sum = 0.0;
-        int huge_any = 0;
-        if (m == METZGER) {
+        const double mu_j = __shfl_sync(FULL, vp, j);
+        const double ls_j = __shfl_sync(FULL, vp, (np + j) & 31);
+        const double sg_j = own ? exp(ls_j) : 0.0;
+        if constexpr (M == METZGER) {
+            double mu[MAXP], sg[MAXP];
+#pragma unroll
+            for (int q = 0; q < np; q++) { mu[q] = __shfl_sync(FULL, mu_j, q); sg[q] = __shfl_sync(FULL, sg_j, q); }
             if (lane < SVI_SAMPLES) {
                 const float* ep = eps_tab + ((size_t)step * SVI_SAMPLES + lane) * 7;
                 float pv[MAXP];
-                for (int j = 0; j < np; j++) pv[j] = (float)(mu[j] + sg[j] * (double)ep[j]);
+                for (int q = 0; q < np; q++) pv[q] = (float)(mu[q] + sg[q] * (double)ep[q]);
                 metzger_dual_sweep(pv, (float)bs.t_last, otimes, n, mscr + (size_t)lane * 5 * n);
             }
             __syncwarp();
         }
+        double gmu_j = 0.0, gls_j = 0.0, elbo_sum = 0.0;
+        int huge_any = 0;
         for (int k = 0; k < SVI_SAMPLES; k++) {
             const float* ep = eps_tab + ((size_t)step * SVI_SAMPLES + k) * 7;
-            double th[MAXP], eps[MAXP];
+            const double eps_j = own ? (double)ep[j] : 0.0;
+            const double th_j = mu_j + sg_j * eps_j;
             float pf[MAXP];
-            for (int j = 0; j < np; j++) {
-                eps[j] = (double)ep[j];
-                th[j] = mu[j] + sg[j] * eps[j];
-                pf[j] = (float)th[j];
-            }
+#pragma unroll
+            for (int q = 0; q < MAXP; q++) pf[q] = q < np ? __shfl_sync(FULL, (float)th_j, q) : 0.0f;
             float sx = expf(pf[se]);
             float sx2 = sx * sx;
-            float dll[MAXP];
-            for (int j = 0; j < MAXP; j++) dll[j] = 0.0f;
+            float dll[8];
+#pragma unroll
+            for (int q = 0; q < 8; q++) dll[q] = 0.0f;
             Nll ll;
             ll.reset();
             int huge = 0;
             bool skip_sample = false;
-            if (m == METZGER) {
+            if constexpr (M == METZGER) {
                 // predictions and derivatives of the normalised model, then the
                 // reference's peak rescale (src/parametric.rs:2303-2323)
                 const float* ms = mscr + (size_t)k * 5 * n;
@@ -383,7 +398,7 @@ __global__ void svi_kernel(DeviceBatch d) {
                         float4 ob = obs[i];
                         float pr = ms[i * 5] * scl;
                         float gb[MAXP];
-                        for (int j = 0; j < 4; j++) gb[j] = ms[i * 5 + 1 + j] * scl;
+                        for (int q = 0; q < 4; q++) gb[q] = ms[i * 5 + 1 + q] * scl;
                         gb[4] = 0.0f;
                         float tv = fabsf(ob.w) + sx2;
                         float stv = sqrtf(tv);
@@ -393,14 +408,14 @@ __global__ void svi_kernel(DeviceBatch d) {
                             bool hg;
                             float ratio = upper_ratio_f32(z, hg);
                             if (hg) huge = 1;
-                            for (int j = 0; j < 4; j++) if (isfinite(gb[j])) dll[j] += -ratio / stv * gb[j];
+                            for (int q = 0; q < 4; q++) if (isfinite(gb[q])) dll[q] += -ratio / stv * gb[q];
                             dll[se] += ratio * (-(ob.z - pr) * sx2 / (stv * tv));
                         } else {
                             float res = ob.z - pr;
                             float it = 1.0f / tv;
                             float r2 = res * res;
                             ll.add(-0.5f * (r2 * it + logf(6.283185307179586f * tv)));
-                            for (int j = 0; j < 4; j++) if (isfinite(gb[j])) dll[j] += res * it * gb[j];
+                            for (int q = 0; q < 4; q++) if (isfinite(gb[q])) dll[q] += res * it * gb[q];
                             dll[se] += (r2 * it * it - it) * sx2;
                         }
                     }
@@ -410,7 +425,7 @@ __global__ void svi_kernel(DeviceBatch d) {
                     float4 ob = obs[i];
                     float gb[MAXP];
                     int st;
-                    float pr = model_grad_f32(m, pf, ob.x, ob.y, gb, st);
+                    float pr = model_grad_f32(M, pf, ob.x, ob.y, gb, st);
                     if (st == ST_NONFINITE || !isfinite(pr)) continue;
                     float tv = fabsf(ob.w) + sx2;
                     float stv = sqrtf(tv);
@@ -421,45 +436,48 @@ __global__ void svi_kernel(DeviceBatch d) {
                         float ratio = upper_ratio_f32(z, hg);
                         if (hg) huge = 1;
                         float dpred = -ratio / stv;
-                        for (int j = 0; j < np; j++)
-                            if (j != se && isfinite(gb[j])) dll[j] += dpred * gb[j];
+#pragma unroll
+                        for (int q = 0; q < np; q++)
+                            if (q != se && isfinite(gb[q])) dll[q] += dpred * gb[q];
                         dll[se] += ratio * (-(ob.z - pr) * sx2 / (stv * tv));
                     } else {
                         float res = ob.z - pr;
                         float it = 1.0f / tv;
                         float r2 = res * res;
                         ll.add(-0.5f * (r2 * it + logf(6.283185307179586f * tv)));
-                        for (int j = 0; j < np; j++)
-                            if (j != se && isfinite(gb[j])) dll[j] += res * it * gb[j];
+#pragma unroll
+                        for (int q = 0; q < np; q++)
+                            if (q != se && isfinite(gb[q])) dll[q] += res * it * gb[q];
                         dll[se] += (r2 * it * it - it) * sx2;
                     }
                 }
             }
             if (__any_sync(FULL, skip_sample)) continue;
             if (warp_or(huge)) huge_any = 1;
-            double lls = warp_sum_d((double)ll.s - (double)ll.c);
-            double lp = 0.0;
-            for (int j = 0; j < np; j++) {
-                double dlj = (double)warp_sum_f(dll[j]);
-                double dd = th[j] - pc[j];
-                lp += -0.5 * dd * dd / pw2[j];
-                double df = dlj + (-dd / pw2[j]);
-                gmu[j] += df;
-                gls[j] += df * sg[j] * eps[j];
+            const double lls = warp_sum_d((double)ll.s - (double)ll.c);
+            // lane j: total d loglik / d theta_j, then its prior and ELBO terms
+            const float dl_tot = reduce_scatter8f(dll);
+            const double dl_j = (double)__shfl_sync(FULL, dl_tot, (4 * j) & 31);
+            double lp_j = 0.0;
+            if (own) {
+                const double dd = th_j - pc_j;
+                lp_j = -0.5 * dd * dd / pw2_j;
+                const double df = dl_j + (-dd / pw2_j);
+                gmu_j += df;
+                gls_j += df * sg_j * eps_j;
             }
+            const double lp = dot8(lp_j, 1.0);
             elbo_sum += lls + lp;
         }
         const double ns = (double)SVI_SAMPLES;
-        double ent = 0.0;
-        for (int j = 0; j < np; j++) ent += __shfl_sync(FULL, vp, np + j);
-        ent += 0.5 * (double)np * ln_2pie;
+        const double ent = dot8(own ? ls_j : 0.0, 1.0) + 0.5 * (double)np * ln_2pie;
         final_elbo = elbo_sum / ns + ent;
         // Adam, lane i owns variational parameter i
+        const double gmu_i = __shfl_sync(FULL, gmu_j, lane & 7);
+        const double gls_i = __shfl_sync(FULL, gls_j, (lane - np) & 7);
         double gi = 0.0;
-        for (int j = 0; j < np; j++) {
-            if (lane == j) gi = -(gmu[j] / ns);
-            if (lane == np + j) gi = -(gls[j] / ns + 1.0);
-        }
+        if (lane < np) gi = -(gmu_i / ns);
+        else if (lane < 2 * np) gi = -(gls_i / ns + 1.0);
         b1t *= 0.9;
         b2t *= 0.999;
         if (huge_any) frozen = true;  // the reference's v overflows to +inf: updates stop
@@ -477,6 +495,7 @@ __global__ void svi_kernel(DeviceBatch d) {
             if (imp) { best_ema = ema; no_imp = 0; }
             else if (++no_imp >= 50) break;
         }
+        __syncwarp();  // MetzgerKN scratch rows are rewritten next step
     }
     const double ln4 = 1.3862943611198906;
     double out_v = lane < np ? vp : vp + ln4;
@@ -484,16 +503,35 @@ __global__ void svi_kernel(DeviceBatch d) {
     else if (lane < 2 * np) o.log_sigma[lane - np] = out_v;
     if (lane >= np && lane < MAXP) o.mu[lane] = NAN;
     if (lane == 0) {
-        for (int j = np; j < MAXP; j++) o.log_sigma[j] = NAN;
+        for (int q = np; q < MAXP; q++) o.log_sigma[q] = NAN;
         o.elbo = final_elbo;
         o.svi_steps = steps;
+    }
+}
+
+// One warp per (band, model), model-major (the warps of a model run
+// together and share its code); a warp whose band selected another model
+// returns at once.
+__global__ void __launch_bounds__(128) svi_kernel(DeviceBatch d) {
+    const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    if (warp >= d.n_bands * 8) return;
+    const int m = warp / d.n_bands, b = warp - m * d.n_bands;
+    switch (m) {
+        case BAZIN: svi_band<BAZIN>(d, b); break;
+        case VILLAR: svi_band<VILLAR>(d, b); break;
+        case TDE: svi_band<TDE>(d, b); break;
+        case ARNETT: svi_band<ARNETT>(d, b); break;
+        case MAGNETAR: svi_band<MAGNETAR>(d, b); break;
+        case SHOCK: svi_band<SHOCK>(d, b); break;
+        case AFTERGLOW: svi_band<AFTERGLOW>(d, b); break;
+        default: svi_band<METZGER>(d, b); break;
     }
 }
 
 void launch_svi(const DeviceBatch& d, cudaStream_t s) {
     if (d.n_bands == 0) return;
     int block = 128;
-    int64_t threads = (int64_t)d.n_bands * 32;
+    int64_t threads = (int64_t)d.n_bands * 8 * 32;
     svi_kernel<<<(int)((threads + block - 1) / block), block, 0, s>>>(d);
 }
 

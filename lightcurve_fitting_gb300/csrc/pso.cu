@@ -202,7 +202,7 @@ struct TaskCtx {
     float t_last;
     const float4* obs;
     float* mscratch;     // MetzgerKN scratch of this warp ([n][32])
-    double prior_n;      // n as double (max(n, 1))
+    double inv_n;        // 1 / max(n, 1)
 };
 
 template <class M>
@@ -270,64 +270,61 @@ __device__ __forceinline__ void model_init(M& e, const float* p, const double* p
     else e.init(p);
 }
 
+// Cost of one particle of a task of kind KIND (PsoCost::cost_from_slice,
+// src/parametric.rs:1303-1370, or the MultiBazin cost :985-1006).
 // pd: optional FP64 parameter vector (same values as p) for callers whose
 // parameters are FP64; the per-particle constants are then formed in FP64.
-__device__ double particle_cost(const TaskCtx& t, const float* x, const double* pd = nullptr) {
-    // rebuild the full parameter vector
-    float p[MB_MAXP];
-    if (t.flags & TASK_T0_FIXED) {
-        int fi = 0;
-        for (int i = 0; i < t.D; i++) {
-            if (i == t.t0i) p[fi++] = t.t0_fixed;
-            p[fi++] = x[i];
-        }
-        if (t.t0i >= t.D) p[fi] = t.t0_fixed;
-    } else {
-        for (int i = 0; i < t.D; i++) p[i] = x[i];
-    }
-    double n = t.prior_n;
-    if (t.kind >= KIND_MB1) {
-        int K = t.kind - KIND_MB1 + 1;
+template <int KIND>
+__device__ __forceinline__ double particle_cost_k(const TaskCtx& t, const float* x, const double* pd = nullptr) {
+    if constexpr (KIND >= KIND_MB1) {
+        constexpr int K = KIND - KIND_MB1 + 1;
+        float p[4 * K + 2];
+#pragma unroll
+        for (int i = 0; i < 4 * K + 2; i++) p[i] = x[i];
         float se = expf(p[4 * K + 1]);
+        Nll acc = nll_multibazin<K>(p, t.obs, t.n, se * se);
+        return acc.finish(0.0, t.inv_n);
+    } else {
+        constexpr int m = KIND;
+        constexpr int np = n_params_of(m);
+        // rebuild the full parameter vector (profile t0 search: t0 held fixed)
+        float p[MAXP];
+        if (t.flags & TASK_T0_FIXED) {
+            constexpr int t0i = t0_idx_of(m);
+#pragma unroll
+            for (int i = 0; i < np; i++) p[i] = i < t0i ? x[i] : (i == t0i ? t.t0_fixed : x[i - 1]);
+        } else {
+#pragma unroll
+            for (int i = 0; i < np; i++) p[i] = x[i];
+        }
+        if constexpr (m == VILLAR) {
+            float c = VillarF::constraint(p);
+            if (c > 0.0f) return 1e12 + 10000.0 * (double)c;
+        }
+        double prior = 0.0;
+        if (t.flags & TASK_PRIOR) {
+            float s = 0.0f;
+#pragma unroll
+            for (int j = 0; j < np; j++) {
+                float w = (float)c_pop_w[m][j];
+                if (w > 0.0f) {
+                    float z = (p[j] - (float)c_pop_c[m][j]) / w;
+                    s += 0.5f * z * z;
+                }
+            }
+            prior = (double)s;
+        }
+        float se = pd ? (float)exp(pd[se_idx_of(m)]) : expf(p[se_idx_of(m)]);
         float se2 = se * se;
         Nll acc;
-        switch (K) {
-            case 1: acc = nll_multibazin<1>(p, t.obs, t.n, se2); break;
-            case 2: acc = nll_multibazin<2>(p, t.obs, t.n, se2); break;
-            case 3: acc = nll_multibazin<3>(p, t.obs, t.n, se2); break;
-            default: acc = nll_multibazin<4>(p, t.obs, t.n, se2); break;
-        }
-        return acc.finish(0.0, n);
-    }
-    int m = t.model;
-    if (m == VILLAR) {
-        float c = VillarF::constraint(p);
-        if (c > 0.0f) return 1e12 + 10000.0 * (double)c;
-    }
-    double prior = 0.0;
-    if (t.flags & TASK_PRIOR) {
-        float s = 0.0f;
-        for (int j = 0; j < t.np; j++) {
-            float w = (float)c_pop_w[m][j];
-            if (w > 0.0f) {
-                float z = (p[j] - (float)c_pop_c[m][j]) / w;
-                s += 0.5f * z * z;
-            }
-        }
-        prior = (double)s;
-    }
-    float se = pd ? (float)exp(pd[se_idx_of(m)]) : expf(p[se_idx_of(m)]);
-    float se2 = se * se;
-    Nll acc;
-    switch (m) {
-        case BAZIN: { BazinF e; model_init(e, p, pd); acc = nll_loop(e, t.obs, t.n, se2); break; }
-        case VILLAR: { VillarF e; model_init(e, p, pd); acc = nll_loop(e, t.obs, t.n, se2); break; }
-        case TDE: { TdeF e; model_init(e, p, pd); acc = nll_loop(e, t.obs, t.n, se2); break; }
-        case ARNETT: { ArnettF e; model_init(e, p, pd); acc = nll_loop(e, t.obs, t.n, se2); break; }
-        case MAGNETAR: { MagnetarF e; model_init(e, p, pd); acc = nll_loop(e, t.obs, t.n, se2); break; }
-        case SHOCK: { ShockF e; model_init(e, p, pd); acc = nll_loop(e, t.obs, t.n, se2); break; }
-        case AFTERGLOW: { AfterglowF e; model_init(e, p, pd); acc = nll_loop(e, t.obs, t.n, se2); break; }
-        default: {
+        if constexpr (m == BAZIN) { BazinF e; model_init(e, p, pd); acc = nll_loop(e, t.obs, t.n, se2); }
+        else if constexpr (m == VILLAR) { VillarF e; model_init(e, p, pd); acc = nll_loop(e, t.obs, t.n, se2); }
+        else if constexpr (m == TDE) { TdeF e; model_init(e, p, pd); acc = nll_loop(e, t.obs, t.n, se2); }
+        else if constexpr (m == ARNETT) { ArnettF e; model_init(e, p, pd); acc = nll_loop(e, t.obs, t.n, se2); }
+        else if constexpr (m == MAGNETAR) { MagnetarF e; model_init(e, p, pd); acc = nll_loop(e, t.obs, t.n, se2); }
+        else if constexpr (m == SHOCK) { ShockF e; model_init(e, p, pd); acc = nll_loop(e, t.obs, t.n, se2); }
+        else if constexpr (m == AFTERGLOW) { AfterglowF e; model_init(e, p, pd); acc = nll_loop(e, t.obs, t.n, se2); }
+        else {
             // MetzgerKN: ODE sweep -> unnormalised interpolants in scratch
             struct ObsT {
                 const float4* o;
@@ -352,10 +349,23 @@ __device__ double particle_cost(const TaskCtx& t, const float* x, const double* 
                 float pr = ok ? lv[j * 32] * scale : 0.0f;
                 acc.obs(o, pr, ST_OK, se2);
             }
-            break;
         }
+        return acc.finish(prior, t.inv_n);
     }
-    return acc.finish(prior, n);
+}
+
+// Runtime dispatch on the task kind (the likelihood API).
+__device__ double particle_cost(const TaskCtx& t, const float* x, const double* pd = nullptr) {
+    switch (t.kind) {
+        case BAZIN: return particle_cost_k<BAZIN>(t, x, pd);
+        case VILLAR: return particle_cost_k<VILLAR>(t, x, pd);
+        case TDE: return particle_cost_k<TDE>(t, x, pd);
+        case ARNETT: return particle_cost_k<ARNETT>(t, x, pd);
+        case MAGNETAR: return particle_cost_k<MAGNETAR>(t, x, pd);
+        case SHOCK: return particle_cost_k<SHOCK>(t, x, pd);
+        case AFTERGLOW: return particle_cost_k<AFTERGLOW>(t, x, pd);
+        default: return particle_cost_k<METZGER>(t, x, pd);
+    }
 }
 
 // ---------------------------------------------------------------------------
@@ -366,8 +376,219 @@ struct WarpSmem {
     uint64_t pad;
 };
 
+// One swarm run (pso_minimize / pso_minimize_seeded, src/parametric.rs:1646-1757,
+// 1160-1266) of a task of kind KIND: warp = swarm, lane = particle.
+template <int MAXD, int KIND>
+__device__ __forceinline__ void run_swarm(const DeviceBatch& d, const PsoTask& task, const BandStats& bs, TaskCtx& t,
+                                          int slot, int gwarp) {
+    const int lane = threadIdx.x & 31;
+    // dimensions and bounds
+    float lo[MAXD], hi[MAXD], seedp[MAXD];
+    bool seeded = (task.flags & TASK_SEEDED) != 0;
+    if constexpr (KIND < KIND_MB1) {
+        constexpr int m = KIND;
+        t.model = m;
+        t.np = n_params_of(m);
+        t.t0i = t0_idx_of(m);
+        double dlo[MAXP], dhi[MAXP];
+        for (int j = 0; j < MAXP; j++) { dlo[j] = c_lo[m][j]; dhi[j] = c_hi[m][j]; }
+        if (task.flags & TASK_T0_BOUNDS) {
+            // data-informed t0 bounds, src/parametric.rs:1881-1909
+            double t0_lo = fmax(bs.t_first - 30.0, dlo[t.t0i]);
+            double t0_hi = fmin(bs.t_peak + 10.0, dhi[t.t0i]);
+            if (t0_lo < t0_hi) { dlo[t.t0i] = t0_lo; dhi[t.t0i] = t0_hi; }
+        }
+        if (task.flags & TASK_T0_FIXED) {
+            t.D = t.np - 1;
+            int k = 0;
+            for (int j = 0; j < t.np; j++) {
+                if (j == t.t0i) continue;
+                if (k < MAXD) { lo[k] = (float)dlo[j]; hi[k] = (float)dhi[j]; }
+                k++;
+            }
+        } else {
+            t.D = t.np;
+            for (int j = 0; j < t.np && j < MAXD; j++) { lo[j] = (float)dlo[j]; hi[j] = (float)dhi[j]; }
+        }
+        if (seeded) {
+            // seed particles of pso_fit_single_model, src/parametric.rs:1924-1964
+            for (int j = 0; j < t.np && j < MAXD; j++) {
+                double c = c_pop_c[m][j];
+                double v = fmin(fmax(c, dlo[j]), dhi[j]);
+                seedp[j] = (float)v;
+            }
+            double t0s = task.restart == 1 ? bs.t_peak - 5.0 : bs.t_first - 15.0;
+            if (t.t0i < MAXD) seedp[t.t0i] = (float)fmin(fmax(t0s, dlo[t.t0i]), dhi[t.t0i]);
+        }
+    } else {
+        constexpr int K = KIND - KIND_MB1 + 1;
+        t.model = BAZIN;
+        t.np = 4 * K + 2;
+        t.D = t.np;
+        t.t0i = -1;
+        // multi_bazin_bounds, src/parametric.rs:958-970
+        for (int c = 0; c < K && 4 * c + 3 < MAXD; c++) {
+            lo[4 * c] = -3.0f; hi[4 * c] = 3.0f;
+            lo[4 * c + 1] = (float)(bs.t_first - 30.0); hi[4 * c + 1] = (float)(bs.t_last + 30.0);
+            lo[4 * c + 2] = -2.0f; hi[4 * c + 2] = 5.0f;
+            lo[4 * c + 3] = -2.0f; hi[4 * c + 3] = 6.0f;
+        }
+        if (4 * K + 1 < MAXD) {
+            lo[4 * K] = -0.3f; hi[4 * K] = 0.3f;
+            lo[4 * K + 1] = -5.0f; hi[4 * K + 1] = 0.0f;
+        }
+        if (seeded && task.aux >= 0) {
+            const double* sp = d.mb[task.aux].seed;
+            for (int j = 0; j < t.np && j < MAXD; j++) seedp[j] = (float)sp[j];
+        }
+    }
+    const int D = t.D;
+    float vmax[MAXD];
+#pragma unroll
+    for (int j = 0; j < MAXD; j++) vmax[j] = j < D ? 0.5f * (hi[j] - lo[j]) : 0.0f;
+    t.mscratch = d.scratch + (size_t)gwarp * (size_t)d.scratch_per_warp;
+    const float* dr = d.draws + (size_t)task.restart * DRAWS_PER_SEED;
+    const int p = lane;
+    const bool live = p < NP;
+    // ---- initialisation (src/parametric.rs:1677-1692, seeded :1189-1210)
+    float x[MAXD], v[MAXD], pb[MAXD], g[MAXD];
+    int base;
+    if (seeded) {
+        if (p == 0) {
+#pragma unroll
+            for (int j = 0; j < MAXD; j++) {
+                if (j < D) { x[j] = seedp[j]; v[j] = vmax[j] * 0.2f * (2.0f * dr[j] - 1.0f); }
+            }
+        } else if (live) {
+            int o = D + 2 * D * (p - 1);
+#pragma unroll
+            for (int j = 0; j < MAXD; j++) {
+                if (j < D) {
+                    x[j] = lo[j] + dr[o + j] * (hi[j] - lo[j]);
+                    v[j] = vmax[j] * 0.2f * (2.0f * dr[o + D + j] - 1.0f);
+                }
+            }
+        }
+        base = 2 * D * NP - D;
+    } else {
+        if (live) {
+            int o = 2 * D * p;
+#pragma unroll
+            for (int j = 0; j < MAXD; j++) {
+                if (j < D) {
+                    x[j] = lo[j] + dr[o + 2 * j] * (hi[j] - lo[j]);
+                    v[j] = vmax[j] * 0.2f * (2.0f * dr[o + 2 * j + 1] - 1.0f);
+                }
+            }
+        }
+        base = 2 * D * NP;
+    }
+#pragma unroll
+    for (int j = 0; j < MAXD; j++) {
+        if (!live || j >= D) { x[j] = 0.0f; v[j] = 0.0f; }
+        pb[j] = x[j];
+        g[j] = 0.0f;
+    }
+    double c = live ? particle_cost_k<KIND>(t, x) : INFINITY;
+    int evals = 1;
+    double pbc = c;
+    double gc = INFINITY;
+    {
+        // global best after the sequential initial loop: first strict minimum
+        double mn = c;
+        for (int k = 16; k; k >>= 1) mn = fmin(mn, __shfl_xor_sync(FULL, mn, k));
+        unsigned m = __ballot_sync(FULL, live && c == mn && mn < INFINITY);
+        if (m) {
+            int q = __ffs(m) - 1;
+            gc = mn;
+#pragma unroll
+            for (int j = 0; j < MAXD; j++) g[j] = __shfl_sync(FULL, x[j], q);
+        }
+    }
+    // ---- iterations
+    int stall = 0;
+    double prev = gc;
+    const double inv_iters = 1.0 / (double)MAX_ITERS;
+    int it = 0;
+    for (; it < MAX_ITERS; it++) {
+        const float w = (float)(0.9 - (0.9 - 0.4) * (double)it * inv_iters);
+        float x0[MAXD], v0[MAXD];
+#pragma unroll
+        for (int j = 0; j < MAXD; j++) { x0[j] = x[j]; v0[j] = v[j]; }
+        const float* r = dr + base + it * 2 * D * NP + 2 * D * p;
+        int start = 0;
+        while (start < NP) {
+            bool active = live && p >= start;
+            if (active) {
+#pragma unroll
+                for (int j = 0; j < MAXD; j++) {
+                    if (j < D) {
+                        float r1 = r[2 * j], r2 = r[2 * j + 1];
+                        float vv = w * v0[j] + 1.5f * r1 * (pb[j] - x0[j]) + 1.5f * r2 * (g[j] - x0[j]);
+                        vv = fminf(fmaxf(vv, -vmax[j]), vmax[j]);
+                        float nx = x0[j] + vv;
+                        if (nx <= lo[j]) { x[j] = lo[j]; v[j] = 0.0f; }
+                        else if (nx >= hi[j]) { x[j] = hi[j]; v[j] = 0.0f; }
+                        else { x[j] = nx; v[j] = vv; }
+                    }
+                }
+                c = particle_cost_k<KIND>(t, x);
+                evals++;
+            }
+            unsigned m = __ballot_sync(FULL, active && c < gc);
+            int q = m ? __ffs(m) - 1 : NP - 1;
+            bool acc = live && p >= start && p <= q;
+            if (acc && c < pbc) {
+                pbc = c;
+#pragma unroll
+                for (int j = 0; j < MAXD; j++) pb[j] = x[j];
+            }
+            if (m) {
+                gc = __shfl_sync(FULL, c, q);
+#pragma unroll
+                for (int j = 0; j < MAXD; j++) g[j] = __shfl_sync(FULL, x[j], q);
+            }
+            start = q + 1;
+        }
+        bool improved = prev - gc > 0.01 * fmax(fabs(prev), 1e-10);
+        if (improved) {
+            stall = 0;
+            prev = gc;
+        } else if (++stall >= STALL_ITERS) {
+            it++;
+            break;
+        }
+    }
+    // ---- result
+    int tot_evals = live ? evals : 0;
+    for (int k = 16; k; k >>= 1) tot_evals += __shfl_xor_sync(FULL, tot_evals, k);
+    if (lane == 0) {
+        PsoResult& R = d.pso_res[task.out];
+        R.cost = gc;
+        R.iters = it;
+        R.evals = tot_evals;
+        for (int j = 0; j < MB_MAXP; j++) R.params[j] = 0.0f;
+#pragma unroll
+        for (int j = 0; j < MAXD; j++)
+            if (j < D) R.params[j] = g[j];
+        atomicAdd(&d.ctr->particle_obs_evals, (unsigned long long)tot_evals * (unsigned long long)bs.n);
+        if (KIND == METZGER) atomicAdd(&d.ctr->ode_steps, (unsigned long long)tot_evals * MetzgerF::NG);
+        if (slot == 0) {
+            atomicAdd(&d.ctr->slot0_evals[KIND], (unsigned long long)tot_evals * (unsigned long long)bs.n);
+            atomicAdd(&d.ctr->slot0_particles[KIND], (unsigned long long)tot_evals);
+        }
+    }
+}
+
+// Blocks of 256 threads per SM the register budget is sized for (128
+// registers a thread): measured on GB300, two resident blocks (16 warps) with
+// a few spills run the swarms ~1.7x faster than one block without spills.
+#ifndef LCF_PSO_MINB7
+#define LCF_PSO_MINB7 2
+#endif
 template <int MAXD>
-__global__ void __launch_bounds__(256) pso_kernel(DeviceBatch d, int slot, int n_host, int smem_obs) {
+__global__ void __launch_bounds__(256, LCF_PSO_MINB7)
+    pso_kernel(DeviceBatch d, int slot, const PsoTask* tasks, int n_host, int smem_obs) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const int lane = threadIdx.x & 31;
     const int warp = threadIdx.x >> 5;
@@ -385,7 +606,7 @@ __global__ void __launch_bounds__(256) pso_kernel(DeviceBatch d, int slot, int n
         if (lane == 0) ti = atomicAdd(&d.ctr->task_head[slot], 1);
         ti = __shfl_sync(FULL, ti, 0);
         if (ti >= n_tasks) break;
-        const PsoTask task = d.tasks[slot][ti];
+        const PsoTask task = tasks[ti];
         const BandStats bs = d.stats[task.band];
         // tasks of bands the reference does not fit (or MultiBazin tasks of
         // bands that are not their source's rank-0 band with n >= 5) are no-ops
@@ -394,7 +615,7 @@ __global__ void __launch_bounds__(256) pso_kernel(DeviceBatch d, int slot, int n
         t.kind = task.kind;
         t.flags = task.flags;
         t.n = bs.n;
-        t.prior_n = (double)max(bs.n, 1);
+        t.inv_n = 1.0 / (double)max(bs.n, 1);
         t.t_last = (float)bs.t_last;
         t.t0_fixed = (float)task.t0_fixed;
         // stage the band
@@ -414,206 +635,26 @@ __global__ void __launch_bounds__(256) pso_kernel(DeviceBatch d, int slot, int n
         } else {
             t.obs = gobs;
         }
-        // dimensions and bounds
-        float lo[MAXD], hi[MAXD], seedp[MAXD];
-        bool seeded = (task.flags & TASK_SEEDED) != 0;
-        if (t.kind < KIND_MB1) {
-            int m = t.kind;
-            t.model = m;
-            t.np = n_params_of(m);
-            t.t0i = t0_idx_of(m);
-            double dlo[MAXP], dhi[MAXP];
-            for (int j = 0; j < MAXP; j++) { dlo[j] = c_lo[m][j]; dhi[j] = c_hi[m][j]; }
-            if (task.flags & TASK_T0_BOUNDS) {
-                // data-informed t0 bounds, src/parametric.rs:1881-1909
-                double t0_lo = fmax(bs.t_first - 30.0, dlo[t.t0i]);
-                double t0_hi = fmin(bs.t_peak + 10.0, dhi[t.t0i]);
-                if (t0_lo < t0_hi) { dlo[t.t0i] = t0_lo; dhi[t.t0i] = t0_hi; }
-            }
-            if (task.flags & TASK_T0_FIXED) {
-                t.D = t.np - 1;
-                int k = 0;
-                for (int j = 0; j < t.np; j++) {
-                    if (j == t.t0i) continue;
-                    if (k < MAXD) { lo[k] = (float)dlo[j]; hi[k] = (float)dhi[j]; }
-                    k++;
-                }
-            } else {
-                t.D = t.np;
-                for (int j = 0; j < t.np && j < MAXD; j++) { lo[j] = (float)dlo[j]; hi[j] = (float)dhi[j]; }
-            }
-            if (seeded) {
-                // seed particles of pso_fit_single_model, src/parametric.rs:1924-1964
-                for (int j = 0; j < t.np && j < MAXD; j++) {
-                    double c = c_pop_c[m][j];
-                    double v = fmin(fmax(c, dlo[j]), dhi[j]);
-                    seedp[j] = (float)v;
-                }
-                double t0s = task.restart == 1 ? bs.t_peak - 5.0 : bs.t_first - 15.0;
-                if (t.t0i < MAXD) seedp[t.t0i] = (float)fmin(fmax(t0s, dlo[t.t0i]), dhi[t.t0i]);
-            }
-        } else {
-            int K = t.kind - KIND_MB1 + 1;
-            t.model = BAZIN;
-            t.np = 4 * K + 2;
-            t.D = t.np;
-            t.t0i = -1;
-            // multi_bazin_bounds, src/parametric.rs:958-970
-            for (int c = 0; c < K && 4 * c + 3 < MAXD; c++) {
-                lo[4 * c] = -3.0f; hi[4 * c] = 3.0f;
-                lo[4 * c + 1] = (float)(bs.t_first - 30.0); hi[4 * c + 1] = (float)(bs.t_last + 30.0);
-                lo[4 * c + 2] = -2.0f; hi[4 * c + 2] = 5.0f;
-                lo[4 * c + 3] = -2.0f; hi[4 * c + 3] = 6.0f;
-            }
-            if (4 * K + 1 < MAXD) {
-                lo[4 * K] = -0.3f; hi[4 * K] = 0.3f;
-                lo[4 * K + 1] = -5.0f; hi[4 * K + 1] = 0.0f;
-            }
-            if (seeded && task.aux >= 0) {
-                const double* sp = d.mb[task.aux].seed;
-                for (int j = 0; j < t.np && j < MAXD; j++) seedp[j] = (float)sp[j];
-            }
-        }
-        const int D = t.D;
-        float vmax[MAXD];
-#pragma unroll
-        for (int j = 0; j < MAXD; j++) vmax[j] = j < D ? 0.5f * (hi[j] - lo[j]) : 0.0f;
-        t.mscratch = d.scratch + (size_t)gwarp * (size_t)d.scratch_per_warp;
-        const float* dr = d.draws + (size_t)task.restart * DRAWS_PER_SEED;
-        const int p = lane;
-        const bool live = p < NP;
-        // ---- initialisation (src/parametric.rs:1677-1692, seeded :1189-1210)
-        float x[MAXD], v[MAXD], pb[MAXD], g[MAXD];
-        int base;
-        if (seeded) {
-            if (p == 0) {
-#pragma unroll
-                for (int j = 0; j < MAXD; j++) {
-                    if (j < D) { x[j] = seedp[j]; v[j] = vmax[j] * 0.2f * (2.0f * dr[j] - 1.0f); }
-                }
-            } else if (live) {
-                int o = D + 2 * D * (p - 1);
-#pragma unroll
-                for (int j = 0; j < MAXD; j++) {
-                    if (j < D) {
-                        x[j] = lo[j] + dr[o + j] * (hi[j] - lo[j]);
-                        v[j] = vmax[j] * 0.2f * (2.0f * dr[o + D + j] - 1.0f);
-                    }
-                }
-            }
-            base = 2 * D * NP - D;
-        } else {
-            if (live) {
-                int o = 2 * D * p;
-#pragma unroll
-                for (int j = 0; j < MAXD; j++) {
-                    if (j < D) {
-                        x[j] = lo[j] + dr[o + 2 * j] * (hi[j] - lo[j]);
-                        v[j] = vmax[j] * 0.2f * (2.0f * dr[o + 2 * j + 1] - 1.0f);
-                    }
-                }
-            }
-            base = 2 * D * NP;
-        }
-#pragma unroll
-        for (int j = 0; j < MAXD; j++) {
-            if (!live || j >= D) { x[j] = 0.0f; v[j] = 0.0f; }
-            pb[j] = x[j];
-            g[j] = 0.0f;
-        }
-        double c = live ? particle_cost(t, x) : INFINITY;
-        int evals = 1;
-        double pbc = c;
-        double gc = INFINITY;
-        {
-            // global best after the sequential initial loop: first strict minimum
-            double mn = c;
-            for (int k = 16; k; k >>= 1) mn = fmin(mn, __shfl_xor_sync(FULL, mn, k));
-            unsigned m = __ballot_sync(FULL, live && c == mn && mn < INFINITY);
-            if (m) {
-                int q = __ffs(m) - 1;
-                gc = mn;
-#pragma unroll
-                for (int j = 0; j < MAXD; j++) g[j] = __shfl_sync(FULL, x[j], q);
-            }
-        }
-        // ---- iterations
-        int stall = 0;
-        double prev = gc;
-        const double inv_iters = 1.0 / (double)MAX_ITERS;
-        int it = 0;
-        for (; it < MAX_ITERS; it++) {
-            const float w = (float)(0.9 - (0.9 - 0.4) * (double)it * inv_iters);
-            float x0[MAXD], v0[MAXD];
-#pragma unroll
-            for (int j = 0; j < MAXD; j++) { x0[j] = x[j]; v0[j] = v[j]; }
-            const float* r = dr + base + it * 2 * D * NP + 2 * D * p;
-            int start = 0;
-            while (start < NP) {
-                bool active = live && p >= start;
-                if (active) {
-#pragma unroll
-                    for (int j = 0; j < MAXD; j++) {
-                        if (j < D) {
-                            float r1 = r[2 * j], r2 = r[2 * j + 1];
-                            float vv = w * v0[j] + 1.5f * r1 * (pb[j] - x0[j]) + 1.5f * r2 * (g[j] - x0[j]);
-                            vv = fminf(fmaxf(vv, -vmax[j]), vmax[j]);
-                            float nx = x0[j] + vv;
-                            if (nx <= lo[j]) { x[j] = lo[j]; v[j] = 0.0f; }
-                            else if (nx >= hi[j]) { x[j] = hi[j]; v[j] = 0.0f; }
-                            else { x[j] = nx; v[j] = vv; }
-                        }
-                    }
-                    c = particle_cost(t, x);
-                    evals++;
-                }
-                unsigned m = __ballot_sync(FULL, active && c < gc);
-                int q = m ? __ffs(m) - 1 : NP - 1;
-                bool acc = live && p >= start && p <= q;
-                if (acc && c < pbc) {
-                    pbc = c;
-#pragma unroll
-                    for (int j = 0; j < MAXD; j++) pb[j] = x[j];
-                }
-                if (m) {
-                    gc = __shfl_sync(FULL, c, q);
-#pragma unroll
-                    for (int j = 0; j < MAXD; j++) g[j] = __shfl_sync(FULL, x[j], q);
-                }
-                start = q + 1;
-            }
-            bool improved = prev - gc > 0.01 * fmax(fabs(prev), 1e-10);
-            if (improved) {
-                stall = 0;
-                prev = gc;
-            } else if (++stall >= STALL_ITERS) {
-                it++;
-                break;
-            }
-        }
-        // ---- result
-        int tot_evals = live ? evals : 0;
-        for (int k = 16; k; k >>= 1) tot_evals += __shfl_xor_sync(FULL, tot_evals, k);
-        if (lane == 0) {
-            PsoResult& R = d.pso_res[task.out];
-            R.cost = gc;
-            R.iters = it;
-            R.evals = tot_evals;
-            for (int j = 0; j < MB_MAXP; j++) R.params[j] = 0.0f;
-#pragma unroll
-            for (int j = 0; j < MAXD; j++)
-                if (j < D) R.params[j] = g[j];
-            atomicAdd(&d.ctr->particle_obs_evals, (unsigned long long)tot_evals * (unsigned long long)bs.n);
-            if (t.kind == METZGER) atomicAdd(&d.ctr->ode_steps, (unsigned long long)tot_evals * MetzgerF::NG);
-            if (slot == 0 && t.kind < 12) {
-                atomicAdd(&d.ctr->slot0_evals[t.kind], (unsigned long long)tot_evals * (unsigned long long)bs.n);
-                atomicAdd(&d.ctr->slot0_particles[t.kind], (unsigned long long)tot_evals);
-            }
+        // one specialised swarm loop per task kind: the warps resident on an SM
+        // (the queue is grouped by kind) run one kind's code
+        if constexpr (MAXD != 7) {
+            constexpr int KMB = KIND_MB1 + (MAXD - 2) / 4 - 1;  // D = 4K + 2
+            if (task.kind == KMB) run_swarm<MAXD, KMB>(d, task, bs, t, slot, gwarp);
+        } else switch (task.kind) {
+            case BAZIN: run_swarm<MAXD, BAZIN>(d, task, bs, t, slot, gwarp); break;
+            case VILLAR: run_swarm<MAXD, VILLAR>(d, task, bs, t, slot, gwarp); break;
+            case TDE: run_swarm<MAXD, TDE>(d, task, bs, t, slot, gwarp); break;
+            case ARNETT: run_swarm<MAXD, ARNETT>(d, task, bs, t, slot, gwarp); break;
+            case MAGNETAR: run_swarm<MAXD, MAGNETAR>(d, task, bs, t, slot, gwarp); break;
+            case SHOCK: run_swarm<MAXD, SHOCK>(d, task, bs, t, slot, gwarp); break;
+            case AFTERGLOW: run_swarm<MAXD, AFTERGLOW>(d, task, bs, t, slot, gwarp); break;
+            case METZGER: run_swarm<MAXD, METZGER>(d, task, bs, t, slot, gwarp); break;
+            case KIND_MB1: run_swarm<MAXD, KIND_MB1>(d, task, bs, t, slot, gwarp); break;
+            default: break;
         }
         __syncwarp();
     }
 }
-
 // Batched likelihood of parameter vectors on one band, through the same
 // per-lane cost function the PSO kernel uses (lane = parameter vector).
 __device__ __forceinline__ void band_cost_body(int model, const float4* obs, int n, float t_last, const double* params,
@@ -634,7 +675,7 @@ __device__ __forceinline__ void band_cost_body(int model, const float4* obs, int
     t.t_last = t_last;
     t.obs = obs;
     t.mscratch = scratch + (size_t)warp * 32 * (size_t)max(n, 1);
-    t.prior_n = (double)max(n, 1);
+    t.inv_n = 1.0 / (double)max(n, 1);
     float x[MAXP];
     double xd[MAXP];
     for (int j = 0; j < MAXP; j++) {
@@ -732,14 +773,71 @@ int pso_blocks_per_sm(int block, size_t smem) {
     return n;
 }
 
-void launch_pso(const DeviceBatch& d, int slot, int n_host, int max_dim, int grid, int block, cudaStream_t s) {
+void launch_pso(const DeviceBatch& d, int slot, const PsoTask* tasks, int n_host, int max_dim, int grid, int block,
+                cudaStream_t s) {
     if (n_host == 0) return;
     int smem_obs = d.smem_obs;
     size_t smem = pso_smem_bytes(block, smem_obs);
-    if (max_dim <= 7) pso_kernel<7><<<grid, block, smem, s>>>(d, slot, n_host, smem_obs);
-    else if (max_dim <= 10) pso_kernel<10><<<grid, block, smem, s>>>(d, slot, n_host, smem_obs);
-    else if (max_dim <= 14) pso_kernel<14><<<grid, block, smem, s>>>(d, slot, n_host, smem_obs);
-    else pso_kernel<18><<<grid, block, smem, s>>>(d, slot, n_host, smem_obs);
+    if (max_dim <= 7) pso_kernel<7><<<grid, block, smem, s>>>(d, slot, tasks, n_host, smem_obs);
+    else if (max_dim <= 10) pso_kernel<10><<<grid, block, smem, s>>>(d, slot, tasks, n_host, smem_obs);
+    else if (max_dim <= 14) pso_kernel<14><<<grid, block, smem, s>>>(d, slot, tasks, n_host, smem_obs);
+    else pso_kernel<18><<<grid, block, smem, s>>>(d, slot, tasks, n_host, smem_obs);
+}
+
+// ---------------------------------------------------------------------------
+// Device task sort (counting sort on 256 keys) for the task lists built on
+// the device (t0 search, Bazin gate, MultiBazin K = 2..4): the same order as
+// the host-built model-selection queue, so that the warps resident on an SM
+// run one kind's code and the longest swarms start first.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ int task_sort_key(const PsoTask& t, int n) {
+    int grp = t.kind == METZGER ? 0 : 1 + t.kind;                      // 0..12
+    int lb = (int)(2.0f * log2f((float)max(n, 1))) - 3;                // 16 length buckets
+    lb = min(15, max(0, lb));
+    return grp * 16 + (15 - lb);                                       // < 208
+}
+
+__global__ void task_hist_kernel(DeviceBatch d, int slot) {
+    const int n_tasks = d.ctr->task_count[slot];
+    int* hist = d.ctr->sort_hist[slot];
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n_tasks; i += gridDim.x * blockDim.x) {
+        const PsoTask t = d.tasks[slot][i];
+        atomicAdd(&hist[task_sort_key(t, d.stats[t.band].n)], 1);
+    }
+}
+
+__global__ void task_scan_kernel(DeviceBatch d, int slot) {  // one block of 256 threads
+    __shared__ int sh[256];
+    const int i = threadIdx.x;
+    const int v = d.ctr->sort_hist[slot][i];
+    sh[i] = v;
+    __syncthreads();
+    for (int off = 1; off < 256; off <<= 1) {
+        int a = i >= off ? sh[i - off] : 0;
+        __syncthreads();
+        sh[i] += a;
+        __syncthreads();
+    }
+    d.ctr->sort_hist[slot][i] = sh[i] - v;  // exclusive prefix: first position of key i
+}
+
+__global__ void task_scatter_kernel(DeviceBatch d, int slot) {
+    const int n_tasks = d.ctr->task_count[slot];
+    int* pos = d.ctr->sort_hist[slot];
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n_tasks; i += gridDim.x * blockDim.x) {
+        const PsoTask t = d.tasks[slot][i];
+        int p = atomicAdd(&pos[task_sort_key(t, d.stats[t.band].n)], 1);
+        d.task_sorted[p] = t;
+    }
+}
+
+void launch_task_sort(const DeviceBatch& d, int slot, cudaStream_t s) {
+    if (d.n_bands == 0 || d.task_cap[slot] == 0) return;
+    int grid = (d.task_cap[slot] + 255) / 256;
+    grid = grid < 1024 ? grid : 1024;
+    task_hist_kernel<<<grid, 256, 0, s>>>(d, slot);
+    task_scan_kernel<<<1, 256, 0, s>>>(d, slot);
+    task_scatter_kernel<<<grid, 256, 0, s>>>(d, slot);
 }
 
 // ---------------------------------------------------------------------------

@@ -1845,6 +1845,21 @@ int orc_laplace_refine(int m, const double* times, const double* flux, const dou
     return 0;
 }
 
+// SVI from `init` (1000 steps, 4 samples, lr 0.01, as fit_parametric_model
+// calls it), then the refinements and the magnitude chi2, on a raw band.
+int orc_svi_refine(int m, const double* times, const double* flux, const double* err, int n,
+                   const double* init, double* mu, double* log_sigma, double* mag) {
+    Band b;
+    if (!prepare_band(times, flux, err, n, b)) return -1;
+    std::vector<double> pp(init, init + N_PARAMS[m]);
+    Uncert u = svi_fit(m, b, 1000, 4, 0.01, pp);
+    profile_t0_refine(m, u, b);
+    profile_refine_all(m, u, b);
+    for (int j = 0; j < N_PARAMS[m]; j++) { mu[j] = u.mu[j]; log_sigma[j] = u.log_sigma[j]; }
+    *mag = magnitude_chi2(m, b, u, pp);
+    return 0;
+}
+
 // Whole-batch fit: fit_parametric_model per source, OpenMP over sources.
 int orc_fit_batch(const lcf_bands_csr* in, const lcf_fit_options* o, lcf_fit_outputs* out, int n_threads) {
     if (!in || !o || !out || in->n_sources < 0) return -1;

@@ -65,6 +65,7 @@ def lib():
         L.orc_laplace_fit.argtypes = [i, vp, vp, vp, vp, vp, i, vp, vp, vp]
         L.orc_fit_batch.argtypes = [C.POINTER(abi.BandsCSR), C.POINTER(abi.FitOptions), C.POINTER(abi.FitOutputs), i]
         L.orc_laplace_refine.argtypes = [i, vp, vp, vp, i, vp, vp, vp, vp]
+        L.orc_svi_refine.argtypes = [i, vp, vp, vp, i, vp, vp, vp, vp]
         L.orc_pso_stats.argtypes = [vp, i]
         L.orc_max_threads.restype = i
         _lib = L
@@ -171,6 +172,20 @@ def laplace_refine(model: int, times, flux, flux_err, params):
     p = np.ascontiguousarray(params[:k], np.float64)
     mu, ls, mag = np.zeros(k), np.zeros(k), np.zeros(1)
     rc = lib().orc_laplace_refine(int(model), _p(t), _p(f), _p(e), t.size, _p(p), _p(mu), _p(ls), _p(mag))
+    return None if rc != 0 else (mu, ls, float(mag[0]))
+
+
+def svi_refine(model: int, times, flux, flux_err, init):
+    """SVI from ``init`` (the post-t0-search PSO parameters), then the profile
+    refinements and the magnitude chi2, on a raw band: (mu, log_sigma,
+    mag_chi2), or None for a band the reference skips."""
+    t = np.ascontiguousarray(times, np.float64)
+    f = np.ascontiguousarray(flux, np.float64)
+    e = np.ascontiguousarray(flux_err, np.float64)
+    k = abi.N_PARAMS[model]
+    p = np.ascontiguousarray(init[:k], np.float64)
+    mu, ls, mag = np.zeros(k), np.zeros(k), np.zeros(1)
+    rc = lib().orc_svi_refine(int(model), _p(t), _p(f), _p(e), t.size, _p(p), _p(mu), _p(ls), _p(mag))
     return None if rc != 0 else (mu, ls, float(mag[0]))
 
 
