@@ -88,6 +88,18 @@ def dist_setup():
     return ws, rank, local
 
 
+def rank_workload(n_sources: int, rank: int):
+    """This rank's shard: its own n_sources sources of the uneven workload
+    (seed 2 + rank), fitted with no exchange between ranks (weak scaling)."""
+    from lightcurve_fitting_gb300 import synth
+    return synth.config_uneven(n_sources, seed=2 + rank)
+
+
+def job_value(n_sources_per_rank: int, ws: int, max_ms: float) -> float:
+    """Whole-job sources/s: all ranks' sources over the slowest rank's time."""
+    return ws * n_sources_per_rank / (max_ms * 1e-3)
+
+
 def dist_max(x: float, ws: int, device) -> float:
     if ws == 1:
         return x
@@ -196,10 +208,11 @@ def run_fused(args, ws, rank, local):
     from lightcurve_fitting_gb300.lib import Context
     torch.cuda.set_device(local)
     dev = torch.device("cuda", local)
-    batch = synth.config_uneven(args.sources, seed=2 + rank)
+    batch = rank_workload(args.sources, rank)
     ctx = Context(local)
     stream = torch.cuda.ExternalStream(ctx.stream, device=dev)
     peaks = ctx.probe_peaks()
+    peaks64 = ctx.probe_fp64()
     # device-resident inputs
     d = {
         "times": torch.from_numpy(batch.times).to(dev),
@@ -237,7 +250,7 @@ def run_fused(args, ws, rank, local):
     dist_barrier(ws)
     ms = float(np.mean(times))
     ms_max = dist_max(ms, ws, dev)
-    value = ws * batch.n_sources / (ms_max * 1e-3)
+    value = job_value(batch.n_sources, ws, ms_max)
     # end-to-end through the host entry point
     e2e_t = []
     if not args.no_e2e:
@@ -273,7 +286,7 @@ def run_fused(args, ws, rank, local):
     frac_mufu = mufu_rate / peaks["mufu_gops"] if peaks["mufu_gops"] else None
     frac_fp32 = fp32_rate / peaks["fp32_tflops"] if peaks["fp32_tflops"] else None
     bound_sfu = (frac_mufu or 0) >= (frac_fp32 or 0)
-    roofline = {
+    roofline_pso = {
         "bound": "sfu" if bound_sfu else "fp32",
         "achieved": mufu_rate if bound_sfu else fp32_rate,
         "peak": peaks["mufu_gops"] if bound_sfu else peaks["fp32_tflops"],
@@ -288,6 +301,31 @@ def run_fused(args, ws, rank, local):
                         "frac": frac_mufu}),
         "launch_ms": pso_ms,
         "particle_obs_evals": float(sum(ev)),
+    }
+    # roofline of the dominant kernel, the FP64 L-BFGS polish: its
+    # observation-term evaluations (device-counted, by model) per second of
+    # the launch, against the rate at which the same FP64 term streams at full
+    # occupancy (probe_fp64), for the same model mix
+    lb_ev = s0["lbfgs_obs_evals_by_model"]
+    lb_ms = float(np.mean([s["ms_lbfgs"] for s in stage]))
+    pk = peaks64["obs_evals_per_s"]
+    ideal_s = sum(lb_ev[m] / pk[m] for m in range(7) if pk[m] > 0)
+    lb_rate = sum(lb_ev[:7]) / (lb_ms * 1e-3)
+    lb_peak = sum(lb_ev[:7]) / ideal_s if ideal_s > 0 else None
+    roofline = {
+        "bound": "fp64",
+        "achieved": lb_rate,
+        "peak": lb_peak,
+        "unit": "observation evaluations/s (FP64 value+gradient+cost term)",
+        "frac": lb_rate / lb_peak if lb_peak else None,
+        "traffic": None,
+        "kernel": "lbfgs_kernel (FP64 L-BFGS polish, the largest stage)",
+        "peak_source": "measured live: the polish's own FP64 observation term streamed at full occupancy "
+                       "(lcf_probe_fp64), weighted by this launch's per-model evaluations",
+        "fp64_dfma_tflops": peaks64["fp64_tflops"],
+        "launch_ms": lb_ms,
+        "lbfgs_obs_evals": float(sum(lb_ev[:7])),
+        "pso_kernel": roofline_pso,
     }
     cpu = None
     if not args.no_cpu_baseline:
@@ -311,7 +349,7 @@ def run_fused(args, ws, rank, local):
         "plain_gpu": plain,
         "clocks": ck,
         "gpu_launches": int(s0["kernel_launches"]) * args.steps,
-        "peaks": peaks,
+        "peaks": {**peaks, "fp64_tflops": peaks64["fp64_tflops"]},
     }
     print(json.dumps(line), flush=True)
     ctx.close()

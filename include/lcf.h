@@ -136,6 +136,7 @@ typedef struct lcf_fit_stats {
     double lbfgs_iters;         /* their L-BFGS iterations */
     double lbfgs_evals;         /* their cost + gradient evaluations */
     double lbfgs_obs_evals;     /* observation x (cost + gradient) evaluations */
+    double lbfgs_obs_evals_by_model[8];  /* the same, by model (MetzgerKN: 0, not polished) */
 } lcf_fit_stats;
 
 typedef struct lcf_ctx lcf_ctx;
@@ -193,6 +194,13 @@ int lcf_set_graph(lcf_ctx* ctx, int enabled);
  * full grid.  The roofline denominators of the fused kernels, which are
  * bound by these two pipes rather than by HBM or the tensor cores. */
 int lcf_probe_peaks(lcf_ctx* ctx, double* out2);
+
+/* FP64 ceilings of the L-BFGS polish, which is bound by the FP64 pipe:
+ * out[m] (m = 0..6) = evaluations per second of the polish's own FP64
+ * observation term (value, gradient and cost of one observation of model m)
+ * streamed at full occupancy over a resident band; out[7] = 0 (MetzgerKN is
+ * not polished); out[8] = FP64 TFLOP/s of independent DFMA chains. */
+int lcf_probe_fp64(lcf_ctx* ctx, double* out9);
 
 /* Diagnostic: raw swarm results of the last fit, 21 doubles per result slot
  * (cost, iterations, particle evaluations, 18 parameters).  Slots

@@ -91,6 +91,7 @@ class FitStats(C.Structure):
         ("lbfgs_iters", C.c_double),
         ("lbfgs_evals", C.c_double),
         ("lbfgs_obs_evals", C.c_double),
+        ("lbfgs_obs_evals_by_model", C.c_double * 8),
     ]
 
 

@@ -611,6 +611,7 @@ static int finish_stats(lcf_ctx* ctx) {
     st.lbfgs_iters = (double)c.lb_iters;
     st.lbfgs_evals = (double)c.lb_evals;
     st.lbfgs_obs_evals = (double)c.lb_obs_evals;
+    for (int m = 0; m < 8; m++) st.lbfgs_obs_evals_by_model[m] = (double)c.lb_obs_evals_by_model[m];
     for (int k = 0; k < 12; k++) {
         st.pso0_evals_by_kind[k] = (double)c.slot0_evals[k];
         st.pso0_particles_by_kind[k] = (double)c.slot0_particles[k];
@@ -872,6 +873,14 @@ extern "C" int lcf_probe_peaks(lcf_ctx* ctx, double* out2) {
     out2[0] = probe_fp32_tflops(ctx->num_sms);
     out2[1] = probe_mufu_gops(ctx->num_sms);
     CK(cudaGetLastError());
+    return 0;
+}
+
+extern "C" int lcf_probe_fp64(lcf_ctx* ctx, double* out9) {
+    if (!ctx || !out9) return LCF_E_INVALID;
+    CK(cudaSetDevice(ctx->device));
+    CK(cudaDeviceSynchronize());
+    if (probe_fp64_peaks(ctx->num_sms, out9)) return set_err(ctx, LCF_E_CUDA, "FP64 probe failed");
     return 0;
 }
 

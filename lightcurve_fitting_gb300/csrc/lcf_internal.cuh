@@ -190,6 +190,7 @@ struct Counters {
     unsigned long long slot0_evals[12];      // particle x observation evaluations of the first PSO launch, by kind
     unsigned long long slot0_particles[12];  // particle evaluations of the first PSO launch, by kind
     unsigned long long lb_polishes, lb_iters, lb_evals, lb_obs_evals;  // L-BFGS work
+    unsigned long long lb_obs_evals_by_model[8];  // observation x (cost + gradient) evaluations, by model
     int32_t sort_hist[8][256];  // per slot: key histogram, then offsets, of the device task sort
     int32_t error;              // first error code raised on the device
     int32_t pad;
@@ -268,6 +269,10 @@ void launch_plain_svi(const DeviceBatch& d, int m, double* mscr, cudaStream_t s)
 void launch_laplace(const DeviceBatch& d, cudaStream_t s);
 void launch_refine(const DeviceBatch& d, cudaStream_t s);
 double probe_fp32_tflops(int num_sms);
+// polish.cu: FP64 peaks: out[m] = observation-term evaluations per second of
+// the polish's FP64 cost+gradient term for model m (0..6) at full occupancy,
+// out[7] = 0 (MetzgerKN is not polished), out[8] = FP64 TFLOP/s of DFMA chains
+int probe_fp64_peaks(int num_sms, double* out9);
 double probe_mufu_gops(int num_sms);
 void launch_band_cost(int model, const float4* obs, int n, float t_last, const double* params, int n_eval,
                       int with_prior, double* costs, float* scratch, cudaStream_t s);

@@ -389,6 +389,29 @@ __device__ __forceinline__ double log_normal_cdf_f64(double x) {
     return log(fmax(phi, 1e-300));
 }
 
+// Upper-limit term of the cost and its gradient factor at z = (u - pred) /
+// sigma, sharing one evaluation of the A&S erf pieces (t, the polynomial and
+// e^(-z^2/2)) between log_normal_cdf (the cost, src/parametric.rs:882-901)
+// and the gradient's Gaussian pdf / CDF ratio (PsoCost::gradient, :1420-1431).
+// The CDF keeps the reference's form 0.5 * (1 + erf), so it rounds to exactly
+// 0 (floored at 1e-300) for z below ~-8.3 as the reference's does.
+__device__ __forceinline__ double upper_cost_ratio(double z, bool want_ratio, double& ratio) {
+    const double a = fabs(z) * 0.70710678118654752440;
+    const double t = 1.0 / (1.0 + 0.3275911 * a);
+    const double poly = t * (0.254829592 + t * (-0.284496736 + t * (1.421413741 + t * (-1.453152027 + t * 1.061405429))));
+    const double e = exp(-a * a);
+    const double pe = poly * e;
+    if (want_ratio) {
+        double v = 1.0 - pe;
+        double cdf = 0.5 * (1.0 + (z >= 0.0 ? v : -v));
+        ratio = (e * 0.39894228040143267794) / fmax(cdf, 1e-300);
+    }
+    if (z > 8.0) return 0.0;
+    if (z < -30.0) return -0.5 * z * z - 0.5 * log(2.0 * 3.14159265358979323846) - log(-z);
+    double phi = z <= 0.0 ? 0.5 * pe : 1.0 - 0.5 * pe;
+    return log(fmax(phi, 1e-300));
+}
+
 // MetzgerKN sweep (metzger_kn_eval_batch, src/parametric.rs:544-648) over a
 // band whose times are sorted ascending: integrates the ODE on the 200-point
 // log grid and calls visit(j, l) with the unnormalised luminosity

@@ -62,6 +62,43 @@ __device__ __forceinline__ double reduce_scatter8(const double* v) {
     return c;
 }
 
+// One observation's term of PsoCost::cost_from_slice and PsoCost::gradient
+// (src/parametric.rs:1303-1446) in FP64: adds to the negative log-likelihood
+// and to the gradient partials.  One FP64 reciprocal per observation stands
+// in for a division per term (the FP64 pipe bounds the polish).
+template <int MODEL>
+__device__ __forceinline__ void lb_obs_term(const Model64& mod, double t, double var, double flux, uint8_t up,
+                                            double uf, double se2, bool want_grad, double& nll, double* gl,
+                                            int& nonfinite) {
+    constexpr int np = n_params_of(MODEL), se = se_idx_of(MODEL);
+    double mg[MAXP];
+    double pr = mod.eval(t, want_grad ? mg : nullptr);
+    if (!isfinite(pr)) { nonfinite = 1; return; }
+    double tv = var + se2;
+    if (up) {
+        double isv = 1.0 / sqrt(tv);
+        double z = (uf - pr) * isv;
+        double ratio;
+        nll -= upper_cost_ratio(z, want_grad, ratio);
+        if (want_grad) {
+            double ri = ratio * isv;
+#pragma unroll
+            for (int k = 0; k < np; k++) gl[k] += ri * mg[k];
+            gl[se] += ratio * z * se2 * (isv * isv);
+        }
+    } else {
+        double dd = pr - flux;
+        double itv = 1.0 / tv;
+        nll += dd * dd * itv + log(tv);
+        if (want_grad) {
+            double sc = 2.0 * dd * itv;
+#pragma unroll
+            for (int k = 0; k < np; k++) gl[k] += sc * mg[k];
+            gl[se] += (-dd * dd * itv * itv + itv) * (2.0 * se2);
+        }
+    }
+}
+
 // Cost and projected gradient of the bounded problem (BoundedPsoCost,
 // src/parametric.rs:1500-1535) for the lane-distributed polish: the full
 // parameter vector is gathered from lanes 0..np-1, the lanes split the
@@ -127,34 +164,8 @@ struct LaneLb {
         int nonfinite = 0;
         Model64 mod;
         mod.init_pre(MODEL, q, ep, rp);
-        for (int i = lane; i < n; i += 32) {
-            double mg[MAXP];
-            double pr = mod.eval(t[i], want_grad ? mg : nullptr);
-            if (!isfinite(pr)) { nonfinite = 1; continue; }
-            double tv = var[i] + se2;
-            if (up[i]) {
-                double sv = sqrt(tv);
-                double z = (uf[i] - pr) / sv;
-                nll -= log_normal_cdf_f64(z);
-                if (want_grad) {
-                    double phi = exp(-0.5 * z * z) / sqrt(2.0 * 3.14159265358979323846);
-                    double cdf = 0.5 * (1.0 + erf_approx_f64(z / 1.41421356237309504880));
-                    double ratio = phi / fmax(cdf, 1e-300);
-#pragma unroll
-                    for (int k = 0; k < np; k++) gl[k] += ratio * mg[k] / sv;
-                    gl[se] += ratio * z * se2 / tv;
-                }
-            } else {
-                double dd = pr - flux[i];
-                nll += dd * dd / tv + log(tv);
-                if (want_grad) {
-                    double sc = 2.0 * dd / tv;
-#pragma unroll
-                    for (int k = 0; k < np; k++) gl[k] += sc * mg[k];
-                    gl[se] += (-dd * dd / (tv * tv) + 1.0 / tv) * (2.0 * se2);
-                }
-            }
-        }
+        for (int i = lane; i < n; i += 32)
+            lb_obs_term<MODEL>(mod, t[i], var[i], flux[i], up[i], uf[i], se2, want_grad, nll, gl, nonfinite);
         nonfinite = warp_or(nonfinite);
         double nsum, gs = 0.0;
         if (want_grad) {
@@ -213,6 +224,7 @@ __device__ void polish_band(const DeviceBatch& d, int b) {
             atomicAdd(&d.ctr->lb_iters, (unsigned long long)c.iters);
             atomicAdd(&d.ctr->lb_evals, (unsigned long long)c.evals);
             atomicAdd(&d.ctr->lb_obs_evals, (unsigned long long)c.evals * (unsigned long long)bs.n);
+            atomicAdd(&d.ctr->lb_obs_evals_by_model[MODEL], (unsigned long long)c.evals * (unsigned long long)bs.n);
         }
     }
     ModelFit& F = d.fits[b * 8 + MODEL];
@@ -282,6 +294,121 @@ __global__ void select_kernel(DeviceBatch d, int fit_all, int forced) {
 void launch_select(const DeviceBatch& d, int fit_all, int forced, cudaStream_t s) {
     if (d.n_bands == 0) return;
     select_kernel<<<(d.n_bands + 127) / 128, 128, 0, s>>>(d, fit_all, forced);
+}
+
+// ---------------------------------------------------------------------------
+// FP64 peaks for the polish's roofline.  probe_obs_kernel streams the polish's
+// own observation term (lb_obs_term: value, gradient and cost of one
+// observation, FP64) over a synthetic band held in L1, lanes over
+// observations, with none of the line search, reductions or divergence of a
+// real polish; its rate is the ceiling of the polish's observation work on
+// this GPU.  probe_dfma_kernel: independent DFMA chains (FP64 FLOP/s).
+// ---------------------------------------------------------------------------
+static __device__ __constant__ double c_probe_p[7][MAXP] = {
+    {0.0, 0.0, 30.0, 1.0, 3.0, -3.0, 0.0},
+    {0.0, 0.005, 2.3, 30.0, 1.0, 3.0, -3.0},
+    {0.0, 0.0, 30.0, 1.0, 3.0, 1.67, -3.0},
+    {0.0, 30.0, 2.3, 0.0, -3.0, 0.0, 0.0},
+    {0.0, 30.0, 3.0, 2.3, -3.0, 0.0, 0.0},
+    {0.0, 30.0, 0.5, 1.0, -3.0, 0.0, 0.0},
+    {0.0, 30.0, 1.0, 0.8, 2.2, -3.0, 0.0}};
+
+template <int MODEL>
+__global__ void __launch_bounds__(256) probe_obs_kernel(const double* band, int nb, int reps, double* sink) {
+    const int lane = threadIdx.x & 31;
+    const double *t = band, *var = band + nb, *flux = band + 2 * nb, *uf = band + 3 * nb, *upd = band + 4 * nb;
+    double nll = 0.0, gl[MAXP];
+    for (int k = 0; k < MAXP; k++) gl[k] = 0.0;
+    int nf = 0;
+    for (int r = 0; r < reps; r++) {
+        double q[MAXP];
+        for (int k = 0; k < MAXP; k++) q[k] = c_probe_p[MODEL][k] + 1e-9 * (double)r;  // a new point per pass
+        Model64 mod;
+        mod.init(MODEL, q);
+        const double se2 = exp(2.0 * q[se_idx_of(MODEL)]);
+        for (int i = lane; i < nb; i += 32)
+            lb_obs_term<MODEL>(mod, t[i], var[i], flux[i], upd[i] != 0.0, uf[i], se2, true, nll, gl, nf);
+    }
+    double s = nll + (double)nf;
+    for (int k = 0; k < MAXP; k++) s += gl[k];
+    sink[blockIdx.x * blockDim.x + threadIdx.x] = s;
+}
+
+__global__ void probe_dfma_kernel(double* out, int iters) {
+    double a0 = threadIdx.x * 1e-3, a1 = a0 + 1.0, a2 = a0 + 2.0, a3 = a0 + 3.0;
+    const double b = 1.0000001, c = 1e-9;
+    for (int i = 0; i < iters; i++) {
+        a0 = fma(a0, b, c); a1 = fma(a1, b, c); a2 = fma(a2, b, c); a3 = fma(a3, b, c);
+    }
+    out[blockIdx.x * blockDim.x + threadIdx.x] = a0 + a1 + a2 + a3;
+}
+
+int probe_fp64_peaks(int num_sms, double* out9) {
+    // synthetic band: 64 observations over 100 days, a Bazin-like light curve,
+    // 27 % of them upper limits (the workload's fraction)
+    const int nb = 64;
+    double h[5 * nb];
+    for (int i = 0; i < nb; i++) {
+        double t = 100.0 * i / (nb - 1), dt = t - 30.0;
+        double f = exp(-dt / 20.0) / (1.0 + exp(-dt / 3.0));
+        bool up = (i % 11) < 3;
+        h[i] = t;
+        h[nb + i] = 0.0025 + 1e-10;
+        h[2 * nb + i] = f;
+        h[3 * nb + i] = 0.15;
+        h[4 * nb + i] = up ? 1.0 : 0.0;
+    }
+    const int blocks = num_sms * 8, threads = 256;
+    double *band = nullptr, *sink = nullptr;
+    if (cudaMalloc(&band, sizeof(h)) != cudaSuccess) return -1;
+    if (cudaMalloc(&sink, (size_t)blocks * threads * sizeof(double)) != cudaSuccess) { cudaFree(band); return -1; }
+    cudaMemcpy(band, h, sizeof(h), cudaMemcpyHostToDevice);
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    const int reps = 16;
+    for (int m = 0; m < 7; m++) {
+        float best = 1e30f;
+        for (int rep = 0; rep < 2; rep++) {
+            cudaEventRecord(e0);
+            switch (m) {
+                case 0: probe_obs_kernel<0><<<blocks, threads>>>(band, nb, reps, sink); break;
+                case 1: probe_obs_kernel<1><<<blocks, threads>>>(band, nb, reps, sink); break;
+                case 2: probe_obs_kernel<2><<<blocks, threads>>>(band, nb, reps, sink); break;
+                case 3: probe_obs_kernel<3><<<blocks, threads>>>(band, nb, reps, sink); break;
+                case 4: probe_obs_kernel<4><<<blocks, threads>>>(band, nb, reps, sink); break;
+                case 5: probe_obs_kernel<5><<<blocks, threads>>>(band, nb, reps, sink); break;
+                default: probe_obs_kernel<6><<<blocks, threads>>>(band, nb, reps, sink); break;
+            }
+            cudaEventRecord(e1);
+            cudaEventSynchronize(e1);
+            float ms = 0.0f;
+            cudaEventElapsedTime(&ms, e0, e1);
+            best = ms < best ? ms : best;
+        }
+        double evals = (double)blocks * (threads / 32) * reps * nb;
+        out9[m] = evals / (best * 1e-3);
+    }
+    out9[7] = 0.0;
+    {
+        const int iters = 4000;
+        float best = 1e30f;
+        for (int rep = 0; rep < 2; rep++) {
+            cudaEventRecord(e0);
+            probe_dfma_kernel<<<blocks, threads>>>(sink, iters);
+            cudaEventRecord(e1);
+            cudaEventSynchronize(e1);
+            float ms = 0.0f;
+            cudaEventElapsedTime(&ms, e0, e1);
+            best = ms < best ? ms : best;
+        }
+        out9[8] = 2.0 * 4.0 * iters * (double)blocks * threads / (best * 1e-3) * 1e-12;
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    cudaFree(band);
+    cudaFree(sink);
+    return cudaGetLastError() == cudaSuccess ? 0 : -1;
 }
 
 // ---------------------------------------------------------------------------

@@ -48,6 +48,7 @@ def load(path: str = LIB_PATH):
     L.lcf_set_graph.argtypes = [vp, i]
     L.lcf_band_cost.argtypes = [vp, i, vp, vp, vp, vp, vp, i, vp, i, i, vp]
     L.lcf_probe_peaks.argtypes = [vp, vp]
+    L.lcf_probe_fp64.argtypes = [vp, vp]
     L.lcf_debug_swarm_results.argtypes = [vp, vp, C.c_int64]
     for name in ["launch_bazin", "launch_villar", "launch_tde", "launch_arnett", "launch_magnetar",
                  "launch_shock_cooling", "launch_afterglow", "launch_metzger_kn"]:
@@ -152,6 +153,13 @@ class Context:
         buf = np.zeros(2)
         self._check(self.L.lcf_probe_peaks(self.h, buf.ctypes.data), "lcf_probe_peaks")
         return {"fp32_tflops": float(buf[0]), "mufu_gops": float(buf[1])}
+
+    def probe_fp64(self) -> dict:
+        """FP64 ceilings of the polish: per-model observation-term evaluations
+        per second (models 0..6) and the DFMA-chain FP64 TFLOP/s."""
+        buf = np.zeros(9)
+        self._check(self.L.lcf_probe_fp64(self.h, buf.ctypes.data), "lcf_probe_fp64")
+        return {"obs_evals_per_s": [float(v) for v in buf[:8]], "fp64_tflops": float(buf[8])}
 
     def swarm_results(self, n_bands: int) -> np.ndarray:
         """Raw swarm results of the last fit: (44 * n_bands, 21) rows, see lcf.h."""
