@@ -86,6 +86,10 @@ typedef struct lcf_fit_options {
     int32_t method;           /* LCF_METHOD_SVI or LCF_METHOD_LAPLACE */
     int32_t forced_model;     /* -1: model selection; else the model id */
     int32_t run_multi_bazin;  /* 1: fit MultiBazin on each source's rank-0 band (reference behaviour) */
+    int32_t joint_multiband;  /* 1: fit_parametric's dispatch (src/parametric.rs:3742-3761): with
+                               * fit_all_models == 0 and forced_model == -1, a source with >= 2 non-empty
+                               * bands gets the joint multi-band Villar fit (fit_parametric_multiband,
+                               * :3763-4131); 0: fit_parametric_model for every source */
 } lcf_fit_options;
 
 /*
@@ -137,6 +141,7 @@ typedef struct lcf_fit_stats {
     double lbfgs_evals;         /* their cost + gradient evaluations */
     double lbfgs_obs_evals;     /* observation x (cost + gradient) evaluations */
     double lbfgs_obs_evals_by_model[8];  /* the same, by model (MetzgerKN: 0, not polished) */
+    double ms_joint;            /* joint multi-band swarm + pick (fit_parametric's multi-band branch) */
 } lcf_fit_stats;
 
 typedef struct lcf_ctx lcf_ctx;

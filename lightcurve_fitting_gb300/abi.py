@@ -45,6 +45,7 @@ class FitOptions(C.Structure):
         ("method", C.c_int32),
         ("forced_model", C.c_int32),
         ("run_multi_bazin", C.c_int32),
+        ("joint_multiband", C.c_int32),
     ]
 
 
@@ -92,6 +93,7 @@ class FitStats(C.Structure):
         ("lbfgs_evals", C.c_double),
         ("lbfgs_obs_evals", C.c_double),
         ("lbfgs_obs_evals_by_model", C.c_double * 8),
+        ("ms_joint", C.c_double),
     ]
 
 
@@ -172,10 +174,12 @@ def csr_struct(batch, keep=None) -> BandsCSR:
     return s
 
 
-def options(fit_all_models=True, method=METHOD_SVI, forced_model=-1, run_multi_bazin=True) -> FitOptions:
+def options(fit_all_models=True, method=METHOD_SVI, forced_model=-1, run_multi_bazin=True,
+            joint_multiband=False) -> FitOptions:
     o = FitOptions()
     o.fit_all_models = int(bool(fit_all_models))
     o.method = int(method)
     o.forced_model = int(forced_model)
     o.run_multi_bazin = int(bool(run_multi_bazin))
+    o.joint_multiband = int(bool(joint_multiband))
     return o

@@ -1,7 +1,7 @@
 """Build liblcf_gb300.so in-tree with nvcc for sm_103a.
 
-Five translation units are compiled in parallel (pso, polish, finalize, plain,
-host)
+Six translation units are compiled in parallel (pso, polish, finalize, plain,
+joint, host)
 and linked into lightcurve_fitting_gb300/liblcf_gb300.so with the CUDA runtime
 linked statically.  No cmake; objects go to lightcurve_fitting_gb300/_build/.
 """
@@ -18,7 +18,7 @@ ROOT = os.path.dirname(HERE)
 CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "liblcf_gb300.so")
-SOURCES = ["pso.cu", "polish.cu", "finalize.cu", "plain.cu", "host.cu"]
+SOURCES = ["pso.cu", "polish.cu", "finalize.cu", "plain.cu", "joint.cu", "host.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 

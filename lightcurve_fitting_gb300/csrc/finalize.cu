@@ -662,7 +662,8 @@ __global__ void refine_kernel(DeviceBatch d) {
         __syncwarp();
         const double* use = mu;
         double pso[MAXP];
-        if (npos < b.n / 2) {
+        // the joint fit always takes mu (src/parametric.rs:4057-4073)
+        if (npos < b.n / 2 && !bs.joint) {
             for (int j = 0; j < np; j++) pso[j] = o.pso_params[j];
             use = pso;
         }
@@ -709,7 +710,7 @@ __global__ void t0_build_kernel(DeviceBatch d, int slot, int fine, int64_t t0_ba
     if (b >= d.n_bands) return;
     BandStats bs = d.stats[b];
     BandOut& o = d.out[b];
-    if (!bs.valid || bs.rank != 0 || o.model < 0) return;
+    if (!bs.valid || bs.rank != 0 || o.model < 0 || bs.joint) return;  // no t0 search in the joint fit
     int m = o.model, t0i = t0_idx_of(m);
     double* ts = d.t0_state + 3 * (int64_t)b;
     if (!fine) {
@@ -744,7 +745,7 @@ __global__ void t0_pick_kernel(DeviceBatch d, int fine, int64_t t0_base) {
     if (b >= d.n_bands) return;
     BandStats bs = d.stats[b];
     BandOut& o = d.out[b];
-    if (!bs.valid || bs.rank != 0 || o.model < 0) return;
+    if (!bs.valid || bs.rank != 0 || o.model < 0 || bs.joint) return;
     int m = o.model, np = n_params_of(m), t0i = t0_idx_of(m);
     double* ts = d.t0_state + 3 * (int64_t)b;
     double t0_min = ts[0], t0_max = ts[1];

@@ -79,6 +79,17 @@ void make_draw_tables(float* draws, float* svi_eps) {
     }
 }
 
+// The same three streams, longer: the joint multi-band swarm (200 particles,
+// up to 42 dimensions, 1500 iterations) draws up to ~25 M uniforms per seed.
+void make_joint_draws(float* draws, int64_t per_seed) {
+    const uint64_t seeds[3] = {42, 137, 271};
+    for (int k = 0; k < 3; k++) {
+        Xoshiro r(seeds[k]);
+        float* out = draws + (size_t)k * per_seed;
+        for (int64_t i = 0; i < per_seed; i++) out[i] = (float)r.f64();
+    }
+}
+
 }  // namespace lcf
 
 // ---------------------------------------------------------------------------
@@ -106,7 +117,10 @@ struct lcf_ctx {
     float* d_eps = nullptr;
     // device buffers (capacity-sized)
     DevArr times, flux, ferr, boff, soff, stats_b, obs, t64, f64, fe64, var64, uf64, mag64, up, res, fits, out, mb,
-        ctr, scratch, scratch64, scratch_svi, t0state, tasks[7], task_sorted;
+        ctr, scratch, scratch64, scratch_svi, t0state, tasks[7], task_sorted, joint_flag, joint_src, joint_res,
+        joint_draws;
+    int64_t joint_per_seed = 0;   // uniforms per seed held in joint_draws
+    int n_joint = 0, joint_max_obs = 0, joint_max_d = 0;
     int64_t task_cap[7] = {0, 0, 0, 0, 0, 0, 0};
     // pinned staging
     DevArr h_in, h_out;
@@ -235,7 +249,8 @@ extern "C" void lcf_ctx_destroy(lcf_ctx* ctx) {
     DevArr* all[] = {&ctx->times, &ctx->flux, &ctx->ferr, &ctx->boff, &ctx->soff, &ctx->stats_b, &ctx->obs,
                      &ctx->t64, &ctx->f64, &ctx->fe64, &ctx->var64, &ctx->uf64, &ctx->mag64, &ctx->up, &ctx->res,
                      &ctx->fits, &ctx->out, &ctx->mb, &ctx->ctr, &ctx->scratch, &ctx->scratch64, &ctx->scratch_svi,
-                     &ctx->t0state, &ctx->task_sorted,
+                     &ctx->t0state, &ctx->task_sorted, &ctx->joint_flag, &ctx->joint_src, &ctx->joint_res,
+                     &ctx->joint_draws,
                      &ctx->bc_obs, &ctx->bc_params, &ctx->bc_costs, &ctx->bc_scratch, &ctx->plain_scr};
     for (DevArr* a : all) free_arr(*a);
     for (auto& a : ctx->tasks) free_arr(a);
@@ -290,6 +305,7 @@ static uint64_t hash_layout(const std::vector<int64_t>& boff, const std::vector<
     mix((uint64_t)o.method + 7);
     mix((uint64_t)(o.forced_model + 100));
     mix((uint64_t)o.run_multi_bazin + 11);
+    mix((uint64_t)o.joint_multiband + 13);
     return h;
 }
 
@@ -349,14 +365,68 @@ static int prepare_layout(lcf_ctx* ctx, int n_sources, int n_bands, int64_t n_ob
     if (rc) return rc;
     // stage-1 task list (bands, models, restarts; MultiBazin K = 1), longest first
     if (!same) {
+        // fit_parametric's dispatch (src/parametric.rs:3742-3761): the sources
+        // with >= 2 non-empty bands get the joint multi-band fit
+        std::vector<uint8_t> jflag((size_t)std::max(n_sources, 1), 0);
+        std::vector<int32_t> jsrc;
+        int jmax_obs = 0, jmax_nb = 0;
+        if (o.joint_multiband && !o.fit_all_models && o.forced_model < 0) {
+            for (int sidx = 0; sidx < n_sources; sidx++) {
+                int nwd = 0;
+                int64_t tot = 0;
+                for (int b = ctx->h_soff[sidx]; b < ctx->h_soff[sidx + 1]; b++) {
+                    int64_t n = ctx->h_boff[b + 1] - ctx->h_boff[b];
+                    if (n > 0) { nwd++; tot += n; }
+                }
+                if (nwd < 2) continue;
+                if (nwd > J_MAX_BANDS)
+                    return set_err(ctx, LCF_E_UNSUPPORTED, "joint multi-band fit: at most 6 bands with data per source");
+                jflag[sidx] = 1;
+                jsrc.push_back(sidx);
+                jmax_obs = std::max<int>(jmax_obs, (int)tot);
+                jmax_nb = std::max(jmax_nb, nwd);
+            }
+        }
+        ctx->n_joint = (int)jsrc.size();
+        ctx->joint_max_obs = jmax_obs;
+        ctx->joint_max_d = 7 * jmax_nb;
+        if (ctx->n_joint > 0) {
+            int dev = ctx->device, optin = 0;
+            cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+            if (joint_smem_bytes(jmax_obs, ctx->joint_max_d) > (size_t)optin)
+                return set_err(ctx, LCF_E_UNSUPPORTED, "joint multi-band fit: a source's observations exceed shared memory");
+            int rc2 = 0;
+            rc2 |= grow(ctx, ctx->joint_flag, (size_t)std::max(n_sources, 1));
+            rc2 |= grow(ctx, ctx->joint_src, jsrc.size() * sizeof(int32_t));
+            rc2 |= grow(ctx, ctx->joint_res, jsrc.size() * 3 * sizeof(JointResult));
+            // uniforms per seed: init (2 D P) + 1500 iterations x 2 D P
+            int64_t need = (int64_t)3002 * ctx->joint_max_d * 200;
+            if (need > ctx->joint_per_seed) {
+                rc2 |= grow(ctx, ctx->joint_draws, (size_t)need * 3 * sizeof(float));
+                if (!rc2) {
+                    std::vector<float> h((size_t)need * 3);
+                    make_joint_draws(h.data(), need);
+                    CK(cudaMemcpy(ctx->joint_draws.p, h.data(), h.size() * sizeof(float), cudaMemcpyHostToDevice));
+                    ctx->joint_per_seed = need;
+                }
+            }
+            if (rc2) return rc2;
+            CK(cudaMemcpyAsync(ctx->joint_flag.p, jflag.data(), (size_t)n_sources, cudaMemcpyHostToDevice, ctx->stream));
+            CK(cudaMemcpyAsync(ctx->joint_src.p, jsrc.data(), jsrc.size() * sizeof(int32_t), cudaMemcpyHostToDevice,
+                               ctx->stream));
+            CK(cudaStreamSynchronize(ctx->stream));
+        }
         std::vector<PsoTask>& T = ctx->h_tasks0;
         T.clear();
         int64_t mb_base = (int64_t)n_bands * 32;
         for (int b = 0; b < n_bands; b++) {
             int n = (int)(ctx->h_boff[b + 1] - ctx->h_boff[b]);
             if (n <= 0) continue;
+            int sidx = (int)(std::upper_bound(ctx->h_soff.begin(), ctx->h_soff.end(), b) - ctx->h_soff.begin()) - 1;
+            const bool joint = ctx->n_joint > 0 && jflag[sidx];
             int models[8], nm = 0;
-            if (o.forced_model >= 0) models[nm++] = o.forced_model;
+            if (joint) nm = 0;  // fitted by the joint multi-band swarm
+            else if (o.forced_model >= 0) models[nm++] = o.forced_model;
             else if (o.fit_all_models) for (int m = 0; m < 8; m++) models[nm++] = m;
             else models[nm++] = BAZIN;
             for (int i = 0; i < nm; i++)
@@ -444,6 +514,14 @@ static int prepare_layout(lcf_ctx* ctx, int n_sources, int n_bands, int64_t n_ob
     d.tasks[7] = nullptr;
     d.task_cap[7] = 0;
     d.task_sorted = (PsoTask*)ctx->task_sorted.p;
+    d.n_joint = ctx->n_joint;
+    d.joint_flag = ctx->n_joint > 0 ? (const uint8_t*)ctx->joint_flag.p : nullptr;
+    d.joint_src = (const int32_t*)ctx->joint_src.p;
+    d.joint_res = (JointResult*)ctx->joint_res.p;
+    d.joint_draws = (const float*)ctx->joint_draws.p;
+    d.joint_draws_per_seed = ctx->joint_per_seed;
+    d.joint_max_obs = ctx->joint_max_obs;
+    d.joint_max_d = ctx->joint_max_d;
     d.ctr = (Counters*)ctx->ctr.p;
     d.scratch = (float*)ctx->scratch.p;
     d.scratch_per_warp = 32 * n_max;
@@ -484,6 +562,8 @@ static void enqueue_pipeline(lcf_ctx* ctx) {
     }
     launch_select(d, o.fit_all_models, o.forced_model, s); L++;
     cudaEventRecordWithFlags(ctx->ev[3], s, cudaEventRecordExternal);
+    if (d.n_joint > 0 && launch_joint(d, s) == 0) L += 2;
+    cudaEventRecordWithFlags(ctx->ev[8], s, cudaEventRecordExternal);
     if (o.method == LCF_METHOD_SVI) {
         launch_t0_build(d, 2, 0, s); L++;
         launch_task_sort(d, 2, s); L += 3;
@@ -599,7 +679,11 @@ static int finish_stats(lcf_ctx* ctx) {
     st.ms_total = tot;
     st.ms_pso = ms[2];
     st.ms_lbfgs = ms[3];
-    st.ms_t0_search = ms[4];
+    float mj = 0.0f, mt0 = 0.0f;
+    if (cudaEventElapsedTime(&mj, ctx->ev[3], ctx->ev[8]) != cudaSuccess) mj = 0.0f;
+    if (cudaEventElapsedTime(&mt0, ctx->ev[8], ctx->ev[4]) != cudaSuccess) mt0 = 0.0f;
+    st.ms_joint = mj;
+    st.ms_t0_search = mt0;
     st.ms_uncertainty = ms[5];
     st.ms_refine = ms[6];
     st.ms_multi_bazin = ms[7];

@@ -30,6 +30,10 @@ constexpr int DRAWS_PER_SEED = 66000;
 constexpr int SVI_STEPS = 1000;
 constexpr int SVI_SAMPLES = 4;
 constexpr double SVI_LR = 0.01;
+// Joint multi-band Villar fit (joint.cu): at most 6 bands per source, so
+// 42 joint parameters.
+constexpr int J_MAX_BANDS = 6;
+constexpr int J_MAX_D = 7 * J_MAX_BANDS;
 
 __host__ __device__ constexpr int n_params_of(int m) {
     return m == BAZIN ? 6 : m == VILLAR ? 7 : m == TDE ? 7 : m == ARNETT ? 5 : m == MAGNETAR ? 5 : m == SHOCK ? 5
@@ -119,6 +123,8 @@ struct BandStats {
     double t_peak_all;  // time of the first maximum flux over all observations
     int32_t source;
     int32_t rank;       // position after the by-count sort inside the source
+    int32_t joint;      // 1: the band belongs to a source of the joint multi-band fit
+    int32_t pad;
 };
 
 // A PSO task: one swarm run.
@@ -146,6 +152,14 @@ struct PsoResult {
     int32_t evals;
     float params[MB_MAXP];
     float pad[2];
+};
+
+// Result of one joint multi-band swarm run (one source, one restart).
+struct JointResult {
+    double cost;
+    int32_t iters;
+    int32_t evals;
+    float params[J_MAX_D];
 };
 
 // Per (band, model) polished fit.
@@ -235,6 +249,15 @@ struct DeviceBatch {
     int64_t t0_slot_base;   // first PsoResult slot of the t0 search region
     int64_t mb_slot_base;   // first PsoResult slot of the MultiBazin region
     int smem_obs;           // observations staged per warp in the PSO kernel
+    // joint multi-band fit
+    const uint8_t* joint_flag;   // per source: 1 if fitted jointly
+    const int32_t* joint_src;    // the jointly fitted sources
+    int n_joint;
+    JointResult* joint_res;      // [n_joint][3]
+    const float* joint_draws;    // [3][joint_draws_per_seed] uniforms of seeds 42, 137, 271
+    int64_t joint_draws_per_seed;
+    int joint_max_obs;           // most observations of a joint source
+    int joint_max_d;             // most joint parameters of a joint source
 };
 
 // ---------------------------------------------------------------------------
@@ -265,6 +288,9 @@ void launch_svi(const DeviceBatch& d, cudaStream_t s);
 void launch_plain_pso(const DeviceBatch& d, int m, int gate, double* mscr, cudaStream_t s);
 void launch_plain_lbfgs(const DeviceBatch& d, int m, cudaStream_t s);
 void launch_plain_svi(const DeviceBatch& d, int m, double* mscr, cudaStream_t s);
+// joint.cu
+int launch_joint(const DeviceBatch& d, cudaStream_t s);
+size_t joint_smem_bytes(int max_obs, int max_d);
 // finalize.cu
 void launch_laplace(const DeviceBatch& d, cudaStream_t s);
 void launch_refine(const DeviceBatch& d, cudaStream_t s);
@@ -279,5 +305,6 @@ void launch_band_cost(int model, const float4* obs, int n, float t_last, const d
 
 // Host-side generation of the RNG tables (host.cpp)
 void make_draw_tables(float* draws, float* svi_eps);
+void make_joint_draws(float* draws, int64_t per_seed);
 
 }  // namespace lcf

@@ -105,6 +105,8 @@ __global__ void prep_kernel(DeviceBatch d) {
     }
     st.valid = valid;
     st.rank = valid ? rank : -1;
+    st.joint = d.joint_flag ? (int32_t)d.joint_flag[s] : 0;
+    st.pad = 0;
     st.peak = peak;
     st.t_first = tmin;
     st.t_last = tmax;

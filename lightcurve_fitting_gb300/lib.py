@@ -99,11 +99,11 @@ class Context:
         self._check(self.L.lcf_set_graph(self.h, int(bool(enabled))), "lcf_set_graph")
 
     def fit_batch(self, batch, fit_all_models=True, method=abi.METHOD_SVI, forced_model=-1,
-                  run_multi_bazin=True) -> abi.FitResult:
+                  run_multi_bazin=True, joint_multiband=False) -> abi.FitResult:
         """lcf_fit_parametric_batch over a PhotometryBatch (host arrays)."""
         keep = []
         csr = abi.csr_struct(batch, keep)
-        opts = abi.options(fit_all_models, method, forced_model, run_multi_bazin)
+        opts = abi.options(fit_all_models, method, forced_model, run_multi_bazin, joint_multiband)
         res = abi.FitResult(batch.n_bands)
         outs = res.as_struct()
         self._check(self.L.lcf_fit_parametric_batch(self.h, C.byref(csr), C.byref(opts), C.byref(outs)),
@@ -111,7 +111,7 @@ class Context:
         return res
 
     def fit_device(self, dev_ptrs: dict, n_sources: int, n_bands: int, fit_all_models=True,
-                   method=abi.METHOD_SVI, forced_model=-1, run_multi_bazin=True):
+                   method=abi.METHOD_SVI, forced_model=-1, run_multi_bazin=True, joint_multiband=False):
         """lcf_fit_parametric_device over device pointers (keys: times, flux,
         flux_err, band_obs_offsets, source_band_offsets)."""
         csr = abi.BandsCSR()
@@ -119,7 +119,7 @@ class Context:
         csr.source_band_offsets = dev_ptrs["source_band_offsets"]
         csr.band_obs_offsets = dev_ptrs["band_obs_offsets"]
         csr.times, csr.flux, csr.flux_err = dev_ptrs["times"], dev_ptrs["flux"], dev_ptrs["flux_err"]
-        opts = abi.options(fit_all_models, method, forced_model, run_multi_bazin)
+        opts = abi.options(fit_all_models, method, forced_model, run_multi_bazin, joint_multiband)
         self._check(self.L.lcf_fit_parametric_device(self.h, C.byref(csr), C.byref(opts)),
                     "lcf_fit_parametric_device")
 

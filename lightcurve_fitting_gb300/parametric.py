@@ -6,9 +6,10 @@ results are lists of dicts with the fields of ``ParametricBandResult``
 (src/parametric.rs:3049-3072), ``None`` where the reference has ``None``.
 
 Every call runs on the GPU through liblcf_gb300.so; there is no CPU path.
-The joint multi-band Villar branch of ``fit_parametric`` (taken by the
-reference for >= 2 bands with ``fit_all_models=False``,
-src/parametric.rs:3750-3757) is not built yet and raises NotImplementedError.
+``fit_parametric`` with ``fit_all_models=False`` dispatches a source with
+two or more non-empty bands to the joint multi-band Villar fit
+(src/parametric.rs:3750-3757, fit_parametric_multiband :3815-4131), as the
+reference does.
 """
 from __future__ import annotations
 
@@ -87,9 +88,11 @@ def _opt(v: float):
 
 
 def results_from_fit(res: abi.FitResult, batch: PhotometryBatch, names, fit_all_models: bool, method: int,
-                     forced_model: int) -> List[List[dict]]:
+                     forced_model: int, joint=None) -> List[List[dict]]:
     """Per source: the list of ParametricBandResult dicts in the reference's
-    band order (descending observation count)."""
+    band order (descending observation count); joint[s] marks the sources of
+    the joint multi-band fit."""
+    joint = joint if joint is not None else [False] * batch.n_sources
     out = []
     for s in range(batch.n_sources):
         b0, b1 = int(batch.source_band_offsets[s]), int(batch.source_band_offsets[s + 1])
@@ -101,6 +104,8 @@ def results_from_fit(res: abi.FitResult, batch: PhotometryBatch, names, fit_all_
             np_ = abi.N_PARAMS[m]
             if forced_model >= 0:
                 chi2 = {abi.MODEL_NAMES[forced_model]: _opt(res.per_model_chi2[b, forced_model])}
+            elif joint[s]:
+                chi2 = {abi.MODEL_NAMES[1]: _opt(res.per_model_chi2[b, 1])}  # the joint fit: Villar only
             else:
                 chi2 = {abi.MODEL_NAMES[k]: _opt(res.per_model_chi2[b, k]) for k in range(8)}
             per_params = {}
@@ -147,17 +152,13 @@ def fit_batch_parametric(sources: Sequence[Dict[str, dict]], fit_all_models: boo
     GPU batch."""
     meth = _method(method)
     forced = -1 if model is None else _model_id(model)
-    if forced < 0 and not fit_all_models:
-        for bands in sources:
-            if sum(1 for b in bands.values() if len(b["values"]) > 0) >= 2:
-                raise NotImplementedError(
-                    "fit_parametric with fit_all_models=False and >= 2 bands takes the reference's joint "
-                    "multi-band Villar branch, which this library does not implement yet")
+    joint_on = forced < 0 and not fit_all_models
+    joint = [joint_on and sum(1 for b in bands.values() if len(b["values"]) > 0) >= 2 for bands in sources]
     batch, names = _batch_from_sources(sources)
     ctx = ctx or default_context()
     res = ctx.fit_batch(batch, fit_all_models=fit_all_models, method=meth, forced_model=forced,
-                        run_multi_bazin=True)
-    return results_from_fit(res, batch, names, fit_all_models, meth, forced)
+                        run_multi_bazin=True, joint_multiband=joint_on)
+    return results_from_fit(res, batch, names, fit_all_models, meth, forced, joint)
 
 
 def fit_parametric(bands: Dict[str, dict], fit_all_models: bool = False, method: str = "svi", ctx=None):

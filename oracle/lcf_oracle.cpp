@@ -1638,7 +1638,208 @@ static double magnitude_chi2(int m, const Band& b, const Uncert& u, const std::v
     return mcount > 0 ? msum / (double)mcount : NaN;
 }
 
+// ---------------------------------------------------------------------------
+// Joint multi-band Villar fit, fit_parametric_multiband src/parametric.rs:
+// 3815-4131 (relative priors :3771-3786, constraint :3790-3799).  Returns
+// false (the caller falls back to the per-band fit) when no band is fitted.
+// ---------------------------------------------------------------------------
+static void relative_band_priors(double* mean, double* sigma) {
+    const double ln10 = 2.302585092994045684;
+    const double mu[7] = {-0.015 * ln10, -0.001, -0.095 * ln10, -1.181, -0.195 * ln10, -0.323 * ln10, -0.025 * ln10};
+    const double sg[7] = {0.08 * ln10, 0.008, 0.25 * ln10, 1.5, 0.35 * ln10, 0.25 * ln10, 0.30 * ln10};
+    for (int j = 0; j < 7; j++) { mean[j] = mu[j]; sigma[j] = sg[j]; }
+}
+
+static double villar_constraint(double log_gamma, double beta, double log_tau_rise, double log_tau_fall) {
+    double gamma = std::exp(log_gamma), tau_rise = std::exp(log_tau_rise), tau_fall = std::exp(log_tau_fall);
+    double c1 = std::fmax(gamma * beta - 1.0, 0.0);
+    double c2 = std::fmax(std::exp(-gamma / tau_rise) * (tau_fall / tau_rise - 1.0) - 1.0, 0.0);
+    double c3 = std::fmax(beta * tau_fall - 1.0 + beta * gamma, 0.0);
+    return c1 + c2 + c3;
+}
+
+struct JointCost {
+    const std::vector<const Band*>* bands;
+    int nb;
+    int n_total;
+    std::vector<double> pc, pw;  // Villar population prior
+    double rm[7], rs[7];         // relative priors of the offsets
+    mutable std::vector<double> pred;
+    double operator()(const double* p) const {
+        const int NPV = 7, se = SE_IDX[VILLAR];
+        const double* ref = p;
+        double rc = villar_constraint(ref[2], ref[1], ref[4], ref[5]);
+        if (rc > 0.0) return 1e12 + 10000.0 * rc;
+        double balanced = 0.0;
+        for (int b = 0; b < nb; b++) {
+            const Band& data = *(*bands)[b];
+            double bp[7];
+            for (int j = 0; j < NPV; j++) bp[j] = b == 0 ? ref[j] : ref[j] + p[NPV * b + j];
+            if (b > 0) {
+                double c = villar_constraint(bp[2], bp[1], bp[4], bp[5]);
+                if (c > 0.0) return 1e12 + 10000.0 * c;
+            }
+            int n = data.n();
+            double sx = std::exp(bp[se]);
+            double sx2 = sx * sx;
+            pred.resize(n);
+            eval_batch(VILLAR, bp, data.t.data(), n, pred.data());
+            double band_nll = 0.0;
+            for (int i = 0; i < n; i++) {
+                if (!std::isfinite(pred[i])) return 1e99;
+                double tv = data.var[i] + sx2;
+                if (data.up[i]) {
+                    band_nll -= log_normal_cdf((data.uf[i] - pred[i]) / std::sqrt(tv));
+                } else {
+                    double diff = pred[i] - data.f[i];
+                    band_nll += diff * diff / tv + std::log(tv);
+                }
+            }
+            if (n > 0) balanced += (band_nll / (double)n) * ((double)n_total / (double)nb);
+        }
+        double nt = (double)std::max(n_total, 1);
+        double neg_lp = 0.0;
+        for (size_t j = 0; j < pc.size() && (int)j < NPV; j++) {
+            if (pw[j] > 0.0) {
+                double z = (ref[j] - pc[j]) / pw[j];
+                neg_lp += 0.5 * z * z;
+            }
+        }
+        for (int b = 1; b < nb; b++)
+            for (int j = 0; j < NPV; j++) {
+                if (rs[j] > 0.0) {
+                    double z = (p[NPV * b + j] - rm[j]) / rs[j];
+                    neg_lp += 0.5 * z * z;
+                }
+            }
+        return (balanced + neg_lp) / nt;
+    }
+};
+
+static bool fit_source_multiband(const lcf_bands_csr* in, const lcf_fit_options* o, int src, lcf_fit_outputs* out) {
+    int b0 = in->source_band_offsets[src], b1 = in->source_band_offsets[src + 1];
+    struct Entry { int band; Band data; };
+    std::vector<Entry> entries;
+    for (int bi = b0; bi < b1; bi++) {
+        int64_t o0 = in->band_obs_offsets[bi], o1 = in->band_obs_offsets[bi + 1];
+        Entry e;
+        e.band = bi;
+        if (prepare_band(in->times + o0, in->flux + o0, in->flux_err + o0, (int)(o1 - o0), e.data))
+            entries.push_back(std::move(e));
+    }
+    std::stable_sort(entries.begin(), entries.end(),
+                     [](const Entry& a, const Entry& b) { return a.data.n() > b.data.n(); });
+    if (entries.empty()) return false;
+    const int nb = (int)entries.size(), NPV = 7, D = NPV * nb, t0i = T0_IDX[VILLAR];
+    std::vector<double> lo, hi;
+    pso_bounds(VILLAR, lo, hi);
+    JointCost jc;
+    relative_band_priors(jc.rm, jc.rs);
+    for (int b = 1; b < nb; b++)
+        for (int j = 0; j < NPV; j++) { lo.push_back(-3.0 * jc.rs[j]); hi.push_back(3.0 * jc.rs[j]); }
+    const Band& ref = entries[0].data;
+    double peak_time = ref.t[0], peak_flux = -INF;
+    for (int i = 0; i < ref.n(); i++)
+        if (!ref.up[i] && ref.f[i] > peak_flux) { peak_flux = ref.f[i]; peak_time = ref.t[i]; }
+    double t_first = INF;
+    for (int i = 0; i < ref.n(); i++) t_first = std::fmin(t_first, ref.t[i]);
+    lo[t0i] = std::fmax(t_first - 30.0, lo[t0i]);  // no lo < hi check here (src/parametric.rs:3880-3881)
+    hi[t0i] = std::fmin(peak_time + 10.0, hi[t0i]);
+    std::vector<const Band*> bptr;
+    int n_total = 0;
+    for (auto& e : entries) { bptr.push_back(&e.data); n_total += e.data.n(); }
+    jc.bands = &bptr;
+    jc.nb = nb;
+    jc.n_total = n_total;
+    population_priors(VILLAR, jc.pc, jc.pw);
+    std::vector<double> seed_particle(D);
+    for (int j = 0; j < NPV; j++) seed_particle[j] = clampd(jc.pc[j], lo[j], hi[j]);
+    seed_particle[t0i] = clampd(peak_time - 5.0, lo[t0i], hi[t0i]);
+    for (int b = 1; b < nb; b++)
+        for (int j = 0; j < NPV; j++) seed_particle[NPV * b + j] = clampd(jc.rm[j], lo[NPV * b + j], hi[NPV * b + j]);
+    const uint64_t seeds[3] = {42, 137, 271};
+    std::vector<double> best;
+    double best_c = INF;
+    for (int i = 0; i < 3; i++) {
+        std::vector<double> gp;
+        double c = pso_minimize(jc, lo, hi, 200, 1500, 60, seeds[i], i == 1 ? seed_particle.data() : nullptr, gp);
+        if (c < best_c) { best_c = c; best = gp; }
+    }
+    if (best.empty()) return false;
+    for (int bi = b0; bi < b1; bi++) {
+        out->model[bi] = -1;
+        out->rank[bi] = -1;
+        out->n_obs[bi] = 0;
+        out->mb_best_k[bi] = 0;
+    }
+    for (int k = 0; k < nb; k++) {
+        const Band& data = entries[k].data;
+        int bi = entries[k].band;
+        std::vector<double> bp(NPV);
+        for (int j = 0; j < NPV; j++) bp[j] = k == 0 ? best[j] : best[j] + best[NPV * k + j];
+        Uncert u = o->method == LCF_METHOD_SVI ? svi_fit(VILLAR, data, 1000, 4, 0.01, bp) : laplace_fit(VILLAR, data, bp);
+        profile_t0_refine(VILLAR, u, data);
+        profile_refine_all(VILLAR, u, data);
+        // magnitude chi2 of the refined mu (no PSO fallback here, :4057-4073)
+        int n = data.n();
+        std::vector<double> sp(n);
+        eval_batch(VILLAR, u.mu.data(), data.t.data(), n, sp.data());
+        double msum = 0.0;
+        int mcount = 0;
+        for (int i = 0; i < n; i++) {
+            double pf = sp[i] * data.peak;
+            if (pf > 0.0 && data.f[i] * data.peak > 0.0) {
+                double mpred = -2.5 * std::log10(pf) + 23.9;
+                double merr = 1.0857 * data.fe[i] / data.f[i];
+                if (merr > 0.0) {
+                    double r = data.mags[i] - mpred;
+                    msum += r * r / (merr * merr);
+                    mcount++;
+                }
+            }
+        }
+        out->model[bi] = VILLAR;
+        out->rank[bi] = k;
+        out->n_obs[bi] = n;
+        for (int j = 0; j < LCF_MAX_PARAMS; j++) {
+            out->pso_params[bi * 7 + j] = j < NPV ? bp[j] : NaN;
+            out->svi_mu[bi * 7 + j] = j < NPV ? u.mu[j] : NaN;
+            out->svi_log_sigma[bi * 7 + j] = j < NPV ? u.log_sigma[j] : NaN;
+        }
+        out->pso_chi2[bi] = fon(best_c);
+        out->svi_elbo[bi] = fon(u.elbo);
+        out->mag_chi2[bi] = mcount > 0 ? fon(msum / (double)mcount) : NaN;
+        for (int mm = 0; mm < 8; mm++) {
+            out->per_model_chi2[bi * 8 + mm] = mm == VILLAR ? fon(best_c) : NaN;
+            for (int j = 0; j < 7; j++) out->per_model_params[(bi * 8 + mm) * 7 + j] = NaN;
+        }
+        out->mb_best_k[bi] = 0;
+        if (k == 0 && o->run_multi_bazin) {
+            MBResult mb = fit_multi_bazin(data);
+            if (!mb.params.empty()) {
+                out->mb_best_k[bi] = mb.best_k;
+                for (int j = 0; j < LCF_MB_MAX_PARAMS; j++)
+                    out->mb_params[bi * 18 + j] = j < (int)mb.params.size() ? mb.params[j] : NaN;
+                out->mb_cost[bi] = mb.cost;
+                out->mb_bic[bi] = mb.bic;
+                for (int kk = 0; kk < 4; kk++) {
+                    out->mb_per_k_cost[bi * 4 + kk] = kk < (int)mb.per_k_cost.size() ? mb.per_k_cost[kk] : NaN;
+                    out->mb_per_k_bic[bi * 4 + kk] = kk < (int)mb.per_k_bic.size() ? mb.per_k_bic[kk] : NaN;
+                }
+            }
+        }
+    }
+    return true;
+}
+
 static void fit_source(const lcf_bands_csr* in, const lcf_fit_options* o, int src, lcf_fit_outputs* out) {
+    // fit_parametric's dispatch, src/parametric.rs:3742-3761
+    if (o->joint_multiband && !o->fit_all_models && o->forced_model < 0) {
+        int with_data = 0;
+        for (int bi = in->source_band_offsets[src]; bi < in->source_band_offsets[src + 1]; bi++)
+            if (in->band_obs_offsets[bi + 1] > in->band_obs_offsets[bi]) with_data++;
+        if (with_data >= 2 && fit_source_multiband(in, o, src, out)) return;
+    }
     int b0 = in->source_band_offsets[src], b1 = in->source_band_offsets[src + 1];
     struct Entry { int band; Band data; };
     std::vector<Entry> entries;
@@ -1858,6 +2059,33 @@ int orc_svi_refine(int m, const double* times, const double* flux, const double*
     for (int j = 0; j < N_PARAMS[m]; j++) { mu[j] = u.mu[j]; log_sigma[j] = u.log_sigma[j]; }
     *mag = magnitude_chi2(m, b, u, pp);
     return 0;
+}
+
+// The joint multi-band cost of source `src` at the joint vector p (7 x the
+// number of fitted bands: the rank-0 band's Villar parameters, then the
+// offsets of ranks 1, 2, ...); returns the number of fitted bands (0: none).
+int orc_joint_cost(const lcf_bands_csr* in, int src, const double* p, double* cost) {
+    int b0 = in->source_band_offsets[src], b1 = in->source_band_offsets[src + 1];
+    std::vector<Band> bands;
+    std::vector<int> counts;
+    for (int bi = b0; bi < b1; bi++) {
+        int64_t o0 = in->band_obs_offsets[bi], o1 = in->band_obs_offsets[bi + 1];
+        Band b;
+        if (prepare_band(in->times + o0, in->flux + o0, in->flux_err + o0, (int)(o1 - o0), b)) bands.push_back(std::move(b));
+    }
+    std::stable_sort(bands.begin(), bands.end(), [](const Band& a, const Band& b) { return a.n() > b.n(); });
+    if (bands.empty()) return 0;
+    std::vector<const Band*> bptr;
+    int n_total = 0;
+    for (auto& b : bands) { bptr.push_back(&b); n_total += b.n(); }
+    JointCost jc;
+    relative_band_priors(jc.rm, jc.rs);
+    jc.bands = &bptr;
+    jc.nb = (int)bands.size();
+    jc.n_total = n_total;
+    population_priors(VILLAR, jc.pc, jc.pw);
+    *cost = jc(p);
+    return jc.nb;
 }
 
 // Whole-batch fit: fit_parametric_model per source, OpenMP over sources.

@@ -66,6 +66,7 @@ def lib():
         L.orc_fit_batch.argtypes = [C.POINTER(abi.BandsCSR), C.POINTER(abi.FitOptions), C.POINTER(abi.FitOutputs), i]
         L.orc_laplace_refine.argtypes = [i, vp, vp, vp, i, vp, vp, vp, vp]
         L.orc_svi_refine.argtypes = [i, vp, vp, vp, i, vp, vp, vp, vp]
+        L.orc_joint_cost.argtypes = [C.POINTER(abi.BandsCSR), i, vp, vp]
         L.orc_pso_stats.argtypes = [vp, i]
         L.orc_max_threads.restype = i
         _lib = L
@@ -189,11 +190,23 @@ def svi_refine(model: int, times, flux, flux_err, init):
     return None if rc != 0 else (mu, ls, float(mag[0]))
 
 
-def fit_batch(batch, fit_all_models=True, method=abi.METHOD_SVI, forced_model=-1, run_multi_bazin=True,
-              n_threads=0) -> abi.FitResult:
+def joint_cost(batch, src: int, p) -> float:
+    """The joint multi-band cost (src/parametric.rs:3900-4001) of source
+    `src` at the joint vector p (rank-0 band's Villar parameters, then the
+    offsets of ranks 1, 2, ...)."""
     keep = []
     csr = abi.csr_struct(batch, keep)
-    opts = abi.options(fit_all_models, method, forced_model, run_multi_bazin)
+    pv = np.ascontiguousarray(p, np.float64)
+    out = np.zeros(1)
+    nb = lib().orc_joint_cost(C.byref(csr), int(src), _p(pv), _p(out))
+    return float(out[0]) if nb > 0 else float("nan")
+
+
+def fit_batch(batch, fit_all_models=True, method=abi.METHOD_SVI, forced_model=-1, run_multi_bazin=True,
+              n_threads=0, joint_multiband=False) -> abi.FitResult:
+    keep = []
+    csr = abi.csr_struct(batch, keep)
+    opts = abi.options(fit_all_models, method, forced_model, run_multi_bazin, joint_multiband)
     res = abi.FitResult(batch.n_bands)
     outs = res.as_struct()
     rc = lib().orc_fit_batch(C.byref(csr), C.byref(opts), C.byref(outs), int(n_threads))

@@ -182,3 +182,37 @@ def test_fit_skips_empty_and_nonpositive_bands(oracle):
     r = oracle.fit_batch(batch, fit_all_models=True, method=abi.METHOD_LAPLACE, run_multi_bazin=False)
     assert r.model[1] == -1 and r.rank[1] == -1
     assert r.model[0] >= 0 and r.model[2] >= 0
+
+
+def _two_band_villar_source(oracle):
+    """The synthetic 2-band source of the reference's multiband test
+    (tests/test_metal.rs:67-97): Villar [0.3, 0.01, 2.0, 10.0, 1.0, 3.0, -2.5]
+    at t = 0, 1.5, ..., 43.5 in r, 0.8 x that in g, errors 5 % + 0.01."""
+    t = np.arange(30) * 1.5
+    r = oracle.eval_model(1, np.array([0.3, 0.01, 2.0, 10.0, 1.0, 3.0, -2.5]), t)
+    g = 0.8 * r
+    e = np.abs(r) * 0.05 + 0.01
+    return {"ztfr": {"times": t, "values": r, "errors": e}, "ztfg": {"times": t, "values": g, "errors": e}}
+
+
+def test_oracle_multiband_villar_produces_results(oracle):
+    """fit_parametric with >= 2 bands and fit_all_models = false takes the
+    joint multi-band Villar branch (src/parametric.rs:3750-3757): both bands
+    get a Villar result with the joint (finite) cost, ranked by count
+    (equal counts: input order)."""
+    from lightcurve_fitting_gb300.parametric import _batch_from_sources
+    batch, _ = _batch_from_sources([_two_band_villar_source(oracle)])
+    r = oracle.fit_batch(batch, fit_all_models=False, method=abi.METHOD_LAPLACE, run_multi_bazin=False,
+                         joint_multiband=True)
+    assert list(r.model) == [1, 1] and list(r.rank) == [0, 1]
+    assert np.isfinite(r.pso_chi2).all() and r.pso_chi2[0] == r.pso_chi2[1]
+    assert np.array_equal(r.per_model_chi2[:, 1], r.pso_chi2)
+    assert np.isnan(np.delete(r.per_model_chi2, 1, axis=1)).all()
+    # each band is normalised by its own peak, so g = 0.8 r is the same
+    # curve: the amplitude offset stays near its relative-prior mean
+    # (-0.015 ln 10, sigma 0.08 ln 10 = 0.184)
+    off = r.pso_params[1, :7] - r.pso_params[0, :7]
+    assert abs(off[0] - (-0.015 * np.log(10))) < 2 * 0.08 * np.log(10)
+    # without the dispatch the same source takes the per-band path
+    r2 = oracle.fit_batch(batch, fit_all_models=False, method=abi.METHOD_LAPLACE, run_multi_bazin=False)
+    assert np.isnan(r2.per_model_chi2[:, 1]).all() or (r2.model != 1).any()
