@@ -72,6 +72,8 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true", help="skip the host entry-point measurement (profiling runs)")
     ap.add_argument("--plain-steps", type=int, default=1, help="timed steps of the plain FP64 GPU form (0: skip)")
+    ap.add_argument("--joint-sources", type=int, default=2000,
+                    help="sources of the fit_parametric multi-band (joint Villar) measurement (0: skip)")
     return ap.parse_args()
 
 
@@ -271,6 +273,7 @@ def run_fused(args, ws, rank, local):
     plain = None
     if args.plain_steps > 0:
         plain = run_plain(args, batch, ptrs, dev, flush, stage, ws)
+    joint = run_joint(args, batch, dev, flush, ws) if args.joint_sources > 0 else None
     if rank != 0:
         ctx.close()
         return
@@ -347,6 +350,7 @@ def run_fused(args, ws, rank, local):
         "roofline": roofline,
         "cpu_baseline": cpu,
         "plain_gpu": plain,
+        "fit_parametric_multiband": joint,
         "clocks": ck,
         "gpu_launches": int(s0["kernel_launches"]) * args.steps,
         "peaks": {**peaks, "fp64_tflops": peaks64["fp64_tflops"]},
@@ -394,6 +398,48 @@ def run_plain(args, batch, ptrs, dev, flush, fused_stats, ws):
         "fused_over_plain": (ws * batch.n_sources / (fused_total * 1e-3)) / value,
         "fused_over_plain_same_stages": (ws * batch.n_sources / (fused_same * 1e-3)) / value,
     }
+
+
+def run_joint(args, batch, dev, flush, ws):
+    """fit_parametric with fit_all_models = false (the reference's default):
+    every source of this workload has 3 non-empty bands, so all take the
+    joint multi-band Villar branch (SVI, MultiBazin), on the first
+    `joint_sources` sources, device-resident, one warm-up and two timed steps."""
+    import torch
+    from lightcurve_fitting_gb300 import abi
+    from lightcurve_fitting_gb300.lib import Context
+    sub = batch.subset(np.arange(min(args.joint_sources, batch.n_sources)))
+    keep = {k: torch.from_numpy(getattr(sub, k)).to(dev) for k in
+            ["times", "flux", "flux_err", "band_obs_offsets", "source_band_offsets"]}
+    ptrs = {k: v.data_ptr() for k, v in keep.items()}
+    jctx = Context(dev.index)
+    jstream = torch.cuda.ExternalStream(jctx.stream, device=dev)
+
+    def fit():
+        jctx.fit_device(ptrs, sub.n_sources, sub.n_bands, fit_all_models=False, method=abi.METHOD_SVI,
+                        joint_multiband=True)
+
+    fit()
+    torch.cuda.synchronize()
+    times, st = [], None
+    for _ in range(2):
+        flush.fill_(1.0)
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(jstream)
+        fit()
+        e1.record(jstream)
+        torch.cuda.synchronize()
+        times.append(e0.elapsed_time(e1))
+        st = jctx.stats()
+    jctx.close()
+    ms = dist_max(float(np.mean(times)), ws, dev)
+    return {"value": job_value(sub.n_sources, ws, ms), "unit": "sources/s", "ms_per_step": ms,
+            "sources_per_gpu": sub.n_sources, "steps": 2, "warmup": 1,
+            "config": "fit_parametric(fit_all_models=false, SVI): joint multi-band Villar swarm (200 particles, "
+                      "1500 iterations, stall 60, 3 seeds), per-band SVI, refinements, MultiBazin",
+            "stage_ms": {"ms_joint": st["ms_joint"], "ms_uncertainty": st["ms_uncertainty"],
+                         "ms_refine": st["ms_refine"], "ms_multi_bazin": st["ms_multi_bazin"]}}
 
 
 def main():
