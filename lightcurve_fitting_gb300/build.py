@@ -1,8 +1,7 @@
 """Build liblcf_gb300.so in-tree with nvcc for sm_103a.
 
-Six translation units are compiled in parallel (pso, polish, finalize, plain,
-joint, host)
-and linked into lightcurve_fitting_gb300/liblcf_gb300.so with the CUDA runtime
+Seven translation units are compiled in parallel (pso, polish, finalize,
+plain, joint, likelihood, host) and linked into lightcurve_fitting_gb300/liblcf_gb300.so with the CUDA runtime
 linked statically.  No cmake; objects go to lightcurve_fitting_gb300/_build/.
 """
 from __future__ import annotations
@@ -18,7 +17,13 @@ ROOT = os.path.dirname(HERE)
 CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "liblcf_gb300.so")
-SOURCES = ["pso.cu", "polish.cu", "finalize.cu", "plain.cu", "joint.cu", "host.cu"]
+SOURCES = ["pso.cu", "polish.cu", "finalize.cu", "plain.cu", "joint.cu", "likelihood.cu", "host.cu"]
+# Units whose FP32 arithmetic (the swarms, SVI and the joint swarm) uses nvcc's
+# fast single-precision forms: SFU exp / log, approximate division and square
+# root, denormals flushed.  FP64 arithmetic is unaffected by the flag.  The
+# likelihood API (likelihood.cu), the refinement scans (finalize.cu) and the
+# plain form keep the accurate library forms.
+FAST_MATH = {"pso.cu", "polish.cu", "joint.cu"}
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 
@@ -35,6 +40,7 @@ def _needs_build(obj: str, src: str) -> bool:
     t = os.path.getmtime(obj)
     deps = [src] + [os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith(".cuh")]
     deps.append(os.path.join(ROOT, "include", "lcf.h"))
+    deps.append(os.path.abspath(__file__))  # compiler flags
     return any(os.path.getmtime(d) > t for d in deps)
 
 
@@ -51,7 +57,8 @@ def build(force: bool = False, verbose: bool = False) -> str:
         obj = os.path.join(BUILD, s.replace(".cu", ".o"))
         objs.append(obj)
         if force or _needs_build(obj, src):
-            jobs.append([cc, *flags, "-c", src, "-o", obj])
+            extra = ["--use_fast_math"] if s in FAST_MATH else []
+            jobs.append([cc, *flags, *extra, "-c", src, "-o", obj])
 
     def run(cmd):
         r = subprocess.run(cmd, capture_output=True, text=True)

@@ -21,10 +21,9 @@
 // view of the reference's sequence.
 #include <cuda_runtime.h>
 
-#include <mutex>
-
 #include "lcf_internal.cuh"
 #include "models_f32.cuh"
+#include "swarm_cost.cuh"
 
 namespace lcf {
 
@@ -192,182 +191,6 @@ __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t phase) {
         if (done) return true;
     }
     return false;
-}
-
-// ---------------------------------------------------------------------------
-// Particle cost (PsoCost::cost_from_slice, src/parametric.rs:1303-1370, and
-// multi_bazin_cost, :973-1004) for the particle of this lane.
-// ---------------------------------------------------------------------------
-struct TaskCtx {
-    int kind, model, np, D, t0i, flags, n;
-    float t0_fixed;
-    float t_last;
-    const float4* obs;
-    float* mscratch;     // MetzgerKN scratch of this warp ([n][32])
-    double inv_n;        // 1 / max(n, 1)
-};
-
-template <class M>
-__device__ __forceinline__ Nll nll_loop(const M& m, const float4* obs, int n, float se2) {
-    Nll acc;
-    acc.reset();
-#pragma unroll 2
-    for (int i = 0; i < n; i++) {
-        float4 o = obs[i];
-        int st = ST_OK;
-        float pr = m.eval(o.x, o.y, st);
-        acc.obs(o, pr, st, se2);
-    }
-    return acc;
-}
-
-// MultiBazin prediction: sum of K Bazin components + B (src/parametric.rs:932-940)
-template <int K>
-__device__ __forceinline__ Nll nll_multibazin(const float* p, const float4* obs, int n, float se2) {
-    float la[K], t0[K], itr[K], itf[K], dif[K];
-#pragma unroll
-    for (int c = 0; c < K; c++) {
-        la[c] = p[4 * c];
-        t0[c] = p[4 * c + 1];
-        itr[c] = expf(-p[4 * c + 2]);
-        itf[c] = expf(-p[4 * c + 3]);
-        dif[c] = itr[c] * expm1f(p[4 * c + 2] - p[4 * c + 3]);
-    }
-    float B = p[4 * K];
-    Nll acc;
-    acc.reset();
-    for (int i = 0; i < n; i++) {
-        float4 o = obs[i];
-        float sum = 0.0f, bigL = -INFINITY;
-        int st = ST_OK;
-#pragma unroll
-        for (int c = 0; c < K; c++) {
-            // one Bazin component in log space (as BazinF::eval)
-            float dt = (o.x - t0[c]) + o.y;
-            float xf = -dt * itf[c], xr = -dt * itr[c];
-            if (xf > 80.0f) {
-                if (xf > LN_DBL_MAX || la[c] + xf > LN_DBL_MAX) { st = ST_NONFINITE; continue; }
-                if (xr > LN_DBL_MAX) continue;  // exact zero in FP64
-            }
-            float L = la[c] + (xr > 0.0f ? -dt * dif[c] : xf) - log1pf(expf(-fabsf(xr)));
-            if (L > BIG_L) bigL = fmaxf(bigL, L) + log1pf(expf(-fabsf(bigL - L)));
-            else sum += expf(L);
-        }
-        float pr = 0.0f;
-        if (st == ST_OK && bigL > -INFINITY) {
-            // FP64 sum overflows to +inf past ln DBL_MAX: non-finite prediction
-            if (bigL > LN_DBL_MAX) st = ST_NONFINITE;
-            else { st = ST_BIG; pr = bigL; }
-        } else {
-            pr = sum + B;
-        }
-        acc.obs(o, pr, st, se2);
-    }
-    return acc;
-}
-
-template <class M>
-__device__ __forceinline__ void model_init(M& e, const float* p, const double* pd) {
-    if (pd) e.init64(pd);
-    else e.init(p);
-}
-
-// Cost of one particle of a task of kind KIND (PsoCost::cost_from_slice,
-// src/parametric.rs:1303-1370, or the MultiBazin cost :985-1006).
-// pd: optional FP64 parameter vector (same values as p) for callers whose
-// parameters are FP64; the per-particle constants are then formed in FP64.
-template <int KIND>
-__device__ __forceinline__ double particle_cost_k(const TaskCtx& t, const float* x, const double* pd = nullptr) {
-    if constexpr (KIND >= KIND_MB1) {
-        constexpr int K = KIND - KIND_MB1 + 1;
-        float p[4 * K + 2];
-#pragma unroll
-        for (int i = 0; i < 4 * K + 2; i++) p[i] = x[i];
-        float se = expf(p[4 * K + 1]);
-        Nll acc = nll_multibazin<K>(p, t.obs, t.n, se * se);
-        return acc.finish(0.0, t.inv_n);
-    } else {
-        constexpr int m = KIND;
-        constexpr int np = n_params_of(m);
-        // rebuild the full parameter vector (profile t0 search: t0 held fixed)
-        float p[MAXP];
-        if (t.flags & TASK_T0_FIXED) {
-            constexpr int t0i = t0_idx_of(m);
-#pragma unroll
-            for (int i = 0; i < np; i++) p[i] = i < t0i ? x[i] : (i == t0i ? t.t0_fixed : x[i - 1]);
-        } else {
-#pragma unroll
-            for (int i = 0; i < np; i++) p[i] = x[i];
-        }
-        if constexpr (m == VILLAR) {
-            float c = VillarF::constraint(p);
-            if (c > 0.0f) return 1e12 + 10000.0 * (double)c;
-        }
-        double prior = 0.0;
-        if (t.flags & TASK_PRIOR) {
-            float s = 0.0f;
-#pragma unroll
-            for (int j = 0; j < np; j++) {
-                float w = (float)c_pop_w[m][j];
-                if (w > 0.0f) {
-                    float z = (p[j] - (float)c_pop_c[m][j]) / w;
-                    s += 0.5f * z * z;
-                }
-            }
-            prior = (double)s;
-        }
-        float se = pd ? (float)exp(pd[se_idx_of(m)]) : expf(p[se_idx_of(m)]);
-        float se2 = se * se;
-        Nll acc;
-        if constexpr (m == BAZIN) { BazinF e; model_init(e, p, pd); acc = nll_loop(e, t.obs, t.n, se2); }
-        else if constexpr (m == VILLAR) { VillarF e; model_init(e, p, pd); acc = nll_loop(e, t.obs, t.n, se2); }
-        else if constexpr (m == TDE) { TdeF e; model_init(e, p, pd); acc = nll_loop(e, t.obs, t.n, se2); }
-        else if constexpr (m == ARNETT) { ArnettF e; model_init(e, p, pd); acc = nll_loop(e, t.obs, t.n, se2); }
-        else if constexpr (m == MAGNETAR) { MagnetarF e; model_init(e, p, pd); acc = nll_loop(e, t.obs, t.n, se2); }
-        else if constexpr (m == SHOCK) { ShockF e; model_init(e, p, pd); acc = nll_loop(e, t.obs, t.n, se2); }
-        else if constexpr (m == AFTERGLOW) { AfterglowF e; model_init(e, p, pd); acc = nll_loop(e, t.obs, t.n, se2); }
-        else {
-            // MetzgerKN: ODE sweep -> unnormalised interpolants in scratch
-            struct ObsT {
-                const float4* o;
-                __device__ float t(int j) const { return o[j].x + o[j].y; }
-            } ot{t.obs};
-            int lane = threadIdx.x & 31;
-            float* lv = t.mscratch + lane;
-            float l_peak = 0.0f;
-            bool ok = MetzgerF::sweep(p, t.t_last, ot, t.n, lv, 32, l_peak);
-            acc.reset();
-            float scale = 1.0f;
-            if (ok) {
-                float inv = 1.0f / l_peak;
-                float mx = -INFINITY;
-                for (int j = 0; j < t.n; j++)
-                    if (t.obs[j].w >= 0.0f) mx = fmaxf(mx, lv[j * 32] * inv);
-                scale = inv;
-                if (mx > 1e-10f && isfinite(mx)) scale = inv * fminf(fmaxf(1.0f / mx, 0.1f), 10.0f);
-            }
-            for (int j = 0; j < t.n; j++) {
-                float4 o = t.obs[j];
-                float pr = ok ? lv[j * 32] * scale : 0.0f;
-                acc.obs(o, pr, ST_OK, se2);
-            }
-        }
-        return acc.finish(prior, t.inv_n);
-    }
-}
-
-// Runtime dispatch on the task kind (the likelihood API).
-__device__ double particle_cost(const TaskCtx& t, const float* x, const double* pd = nullptr) {
-    switch (t.kind) {
-        case BAZIN: return particle_cost_k<BAZIN>(t, x, pd);
-        case VILLAR: return particle_cost_k<VILLAR>(t, x, pd);
-        case TDE: return particle_cost_k<TDE>(t, x, pd);
-        case ARNETT: return particle_cost_k<ARNETT>(t, x, pd);
-        case MAGNETAR: return particle_cost_k<MAGNETAR>(t, x, pd);
-        case SHOCK: return particle_cost_k<SHOCK>(t, x, pd);
-        case AFTERGLOW: return particle_cost_k<AFTERGLOW>(t, x, pd);
-        default: return particle_cost_k<METZGER>(t, x, pd);
-    }
 }
 
 // ---------------------------------------------------------------------------
@@ -657,50 +480,6 @@ __global__ void __launch_bounds__(256, LCF_PSO_MINB7)
         __syncwarp();
     }
 }
-// Batched likelihood of parameter vectors on one band, through the same
-// per-lane cost function the PSO kernel uses (lane = parameter vector).
-__device__ __forceinline__ void band_cost_body(int model, const float4* obs, int n, float t_last, const double* params,
-                                               int n_eval, int with_prior, double* costs, float* scratch) {
-    int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    int lane = threadIdx.x & 31;
-    int e = warp * 32 + lane;
-    if (warp * 32 >= n_eval) return;
-    TaskCtx t;
-    t.kind = model;
-    t.model = model;
-    t.np = n_params_of(model);
-    t.D = t.np;
-    t.t0i = t0_idx_of(model);
-    t.flags = with_prior ? TASK_PRIOR : 0;
-    t.n = n;
-    t.t0_fixed = 0.0f;
-    t.t_last = t_last;
-    t.obs = obs;
-    t.mscratch = scratch + (size_t)warp * 32 * (size_t)max(n, 1);
-    t.inv_n = 1.0 / (double)max(n, 1);
-    float x[MAXP];
-    double xd[MAXP];
-    for (int j = 0; j < MAXP; j++) {
-        xd[j] = (e < n_eval && j < t.np) ? params[(size_t)e * t.np + j] : 0.0;
-        x[j] = (float)xd[j];
-    }
-    double c = particle_cost(t, x, xd);
-    if (e < n_eval) costs[e] = c;
-}
-
-__global__ void band_cost_kernel(int model, const float4* obs, int n, float t_last, const double* params, int n_eval,
-                                 int with_prior, double* costs, float* scratch) {
-    band_cost_body(model, obs, n, t_last, params, n_eval, with_prior, costs, scratch);
-}
-
-void launch_band_cost(int model, const float4* obs, int n, float t_last, const double* params, int n_eval,
-                      int with_prior, double* costs, float* scratch, cudaStream_t s) {
-    if (n_eval <= 0) return;
-    int warps = (n_eval + 31) / 32;
-    band_cost_kernel<<<(warps * 32 + 127) / 128, 128, 0, s>>>(model, obs, n, t_last, params, n_eval, with_prior,
-                                                              costs, scratch);
-}
-
 // ---------------------------------------------------------------------------
 // Peak probes: dependent FMA chains (FP32 pipe) and ex2.approx chains (SFU
 // pipe), eight independent chains per thread, a full persistent grid.
@@ -842,99 +621,4 @@ void launch_task_sort(const DeviceBatch& d, int slot, cudaStream_t s) {
     task_scatter_kernel<<<grid, 256, 0, s>>>(d, slot);
 }
 
-// ---------------------------------------------------------------------------
-// Allocation-free likelihood: lcf_band_cost_static (declared in include/lcf.h).
-//
-// For callers that cannot call cudaMalloc.  Its scratch — the band's sorted
-// FP32 records, its last time, and the MetzgerKN per-lane interpolation
-// buffer — lives in the file-scope array below, sized for at most
-// STATIC_MAX_OBS observations and STATIC_MAX_EVAL parameter vectors per call
-// (4.03 MiB, held by every GPU that loads the library until the process
-// exits).  Every value a call reads from the array is first written by that
-// same call, so nothing has to be cleared between calls; the array keeps the
-// last call's contents.  All calls share the one array, so calls that overlap
-// on the GPU (different streams, or host threads without ordering) race.
-// ---------------------------------------------------------------------------
-constexpr int STATIC_MAX_OBS = 2048;
-constexpr int STATIC_MAX_EVAL = 512;
-constexpr size_t STATIC_REC_FLOATS = (size_t)STATIC_MAX_OBS * 4 + 4;  // records, then t_last (16-B padded)
-constexpr size_t STATIC_SCRATCH_FLOATS = STATIC_REC_FLOATS + (size_t)STATIC_MAX_EVAL * STATIC_MAX_OBS;
-static __device__ __align__(256) float g_band_cost_scratch[STATIC_SCRATCH_FLOATS];
-
-// One block: time-sorted FP32 records of the caller's band and its last time
-// into the static array (same records as lcf_band_cost builds on the host).
-__global__ void static_prep_kernel(const double* t, const double* f, const double* var, const uint8_t* up,
-                                   const double* uf, int n, float* scratch) {
-    float4* rec = reinterpret_cast<float4*>(scratch);
-    __shared__ double smax[256];
-    double mx = -INFINITY;
-    for (int i = threadIdx.x; i < n; i += blockDim.x) {
-        double ti = t[i];
-        mx = fmax(mx, ti);
-        int pos = 0;
-        for (int j = 0; j < n; j++) {
-            double tj = t[j];
-            pos += (tj < ti || (tj == ti && j < i)) ? 1 : 0;
-        }
-        float th = (float)ti;
-        bool u = up[i] != 0;
-        rec[pos] = make_float4(th, (float)(ti - (double)th), (float)(u ? uf[i] : f[i]), u ? -(float)var[i] : (float)var[i]);
-    }
-    smax[threadIdx.x] = mx;
-    __syncthreads();
-    for (int s2 = blockDim.x / 2; s2 > 0; s2 >>= 1) {
-        if (threadIdx.x < s2) smax[threadIdx.x] = fmax(smax[threadIdx.x], smax[threadIdx.x + s2]);
-        __syncthreads();
-    }
-    if (threadIdx.x == 0) scratch[(size_t)STATIC_MAX_OBS * 4] = (float)smax[0];
-}
-
-__global__ void band_cost_static_kernel(int model, int n, const double* params, int n_eval, int with_prior,
-                                        double* costs, float* scratch) {
-    const float4* rec = reinterpret_cast<const float4*>(scratch);
-    float t_last = scratch[(size_t)STATIC_MAX_OBS * 4];
-    band_cost_body(model, rec, n, t_last, params, n_eval, with_prior, costs, scratch + STATIC_REC_FLOATS);
-}
-
-// Device address of the static array, looked up once per device.
-static std::mutex g_static_mu;
-static float* g_static_ptr[64] = {nullptr};
-
 }  // namespace lcf
-
-extern "C" int lcf_band_cost_static(int device, int model, const double* times, const double* flux,
-                                    const double* obs_var, const uint8_t* is_upper, const double* upper_flux,
-                                    int n_obs, const double* params, int n_eval, int with_prior, double* costs,
-                                    void* stream) {
-    using namespace lcf;
-    if (device < 0 || device >= 64 || model < 0 || model > 7 || n_obs < 1 || n_eval < 0) return LCF_E_INVALID;
-    if (n_obs > STATIC_MAX_OBS || n_eval > STATIC_MAX_EVAL) return LCF_E_CAPACITY;
-    if (!times || !flux || !obs_var || !is_upper || !upper_flux || (n_eval > 0 && (!params || !costs)))
-        return LCF_E_INVALID;
-    if (n_eval == 0) return LCF_OK;
-    int prev = -1;
-    if (cudaGetDevice(&prev) != cudaSuccess) return LCF_E_CUDA;
-    if (prev != device && cudaSetDevice(device) != cudaSuccess) return LCF_E_CUDA;
-    float* scratch = nullptr;
-    {
-        // set-up, once per device, with that device current
-        std::lock_guard<std::mutex> lock(g_static_mu);
-        if (!g_static_ptr[device]) {
-            void* ptr = nullptr;
-            if (cudaGetSymbolAddress(&ptr, g_band_cost_scratch) != cudaSuccess || !ptr) {
-                if (prev != device) cudaSetDevice(prev);
-                return LCF_E_CUDA;
-            }
-            g_static_ptr[device] = reinterpret_cast<float*>(ptr);
-        }
-        scratch = g_static_ptr[device];
-    }
-    cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
-    static_prep_kernel<<<1, 256, 0, s>>>(times, flux, obs_var, is_upper, upper_flux, n_obs, scratch);
-    int warps = (n_eval + 31) / 32;
-    band_cost_static_kernel<<<(warps * 32 + 127) / 128, 128, 0, s>>>(model, n_obs, params, n_eval, with_prior, costs,
-                                                                      scratch);
-    cudaError_t e = cudaGetLastError();
-    if (prev != device) cudaSetDevice(prev);
-    return e == cudaSuccess ? LCF_OK : LCF_E_CUDA;
-}
