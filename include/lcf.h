@@ -142,6 +142,7 @@ typedef struct lcf_fit_stats {
     double lbfgs_obs_evals;     /* observation x (cost + gradient) evaluations */
     double lbfgs_obs_evals_by_model[8];  /* the same, by model (MetzgerKN: 0, not polished) */
     double ms_joint;            /* joint multi-band swarm + pick (fit_parametric's multi-band branch) */
+    double lbfgs_fp64_obs_evals_by_model[8];  /* polish observation terms evaluated in FP64 (range fallback) */
 } lcf_fit_stats;
 
 typedef struct lcf_ctx lcf_ctx;
@@ -206,6 +207,17 @@ int lcf_probe_peaks(lcf_ctx* ctx, double* out2);
  * streamed at full occupancy over a resident band; out[7] = 0 (MetzgerKN is
  * not polished); out[8] = FP64 TFLOP/s of independent DFMA chains. */
 int lcf_probe_fp64(lcf_ctx* ctx, double* out9);
+
+/* The polish's double-float observation term (its arithmetic wherever the
+ * exponents stay inside FP32's range): out[m] (m = 0..6) = its evaluations
+ * per second, streamed as lcf_probe_fp64 streams the FP64 term; out[7 + m] =
+ * the largest disagreement with the FP64 term over 256 parameter points of
+ * model m inside the PSO box (|ff - FP64| / sum of the terms' magnitudes, over
+ * the cost and the gradient components); out[14 + 8 m + c] = the same per
+ * component (c = 0: cost, 1 + k: gradient component k); out[70 + m] = the
+ * points of the 256 that the range check keeps in double-float; out[77] =
+ * points where exactly one of the two terms was non-finite. */
+int lcf_probe_ff(lcf_ctx* ctx, double* out80);
 
 /* Diagnostic: raw swarm results of the last fit, 21 doubles per result slot
  * (cost, iterations, particle evaluations, 18 parameters).  Slots

@@ -94,6 +94,7 @@ class FitStats(C.Structure):
         ("lbfgs_obs_evals", C.c_double),
         ("lbfgs_obs_evals_by_model", C.c_double * 8),
         ("ms_joint", C.c_double),
+        ("lbfgs_fp64_obs_evals_by_model", C.c_double * 8),
     ]
 
 

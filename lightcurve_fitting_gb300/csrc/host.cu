@@ -116,7 +116,7 @@ struct lcf_ctx {
     float* d_draws = nullptr;
     float* d_eps = nullptr;
     // device buffers (capacity-sized)
-    DevArr times, flux, ferr, boff, soff, stats_b, obs, t64, f64, fe64, var64, uf64, mag64, up, res, fits, out, mb,
+    DevArr times, flux, ferr, boff, soff, stats_b, obs, t64, f64, fe64, var64, uf64, mag64, up, ffa, ffb, res, fits, out, mb,
         ctr, scratch, scratch64, scratch_svi, t0state, tasks[7], task_sorted, joint_flag, joint_src, joint_res,
         joint_draws;
     int64_t joint_per_seed = 0;   // uniforms per seed held in joint_draws
@@ -247,7 +247,7 @@ extern "C" void lcf_ctx_destroy(lcf_ctx* ctx) {
     if (ctx->stream) cudaStreamSynchronize(ctx->stream);
     if (ctx->graph) cudaGraphExecDestroy(ctx->graph);
     DevArr* all[] = {&ctx->times, &ctx->flux, &ctx->ferr, &ctx->boff, &ctx->soff, &ctx->stats_b, &ctx->obs,
-                     &ctx->t64, &ctx->f64, &ctx->fe64, &ctx->var64, &ctx->uf64, &ctx->mag64, &ctx->up, &ctx->res,
+                     &ctx->t64, &ctx->f64, &ctx->fe64, &ctx->var64, &ctx->uf64, &ctx->mag64, &ctx->up, &ctx->ffa, &ctx->ffb, &ctx->res,
                      &ctx->fits, &ctx->out, &ctx->mb, &ctx->ctr, &ctx->scratch, &ctx->scratch64, &ctx->scratch_svi,
                      &ctx->t0state, &ctx->task_sorted, &ctx->joint_flag, &ctx->joint_src, &ctx->joint_res,
                      &ctx->joint_draws,
@@ -344,6 +344,8 @@ static int prepare_layout(lcf_ctx* ctx, int n_sources, int n_bands, int64_t n_ob
     rc |= grow(ctx, ctx->uf64, no * 8);
     rc |= grow(ctx, ctx->mag64, no * 8);
     rc |= grow(ctx, ctx->up, no);
+    rc |= grow(ctx, ctx->ffa, no * sizeof(float4));
+    rc |= grow(ctx, ctx->ffb, no * sizeof(float2));
     rc |= grow(ctx, ctx->res, nb * 44 * sizeof(PsoResult));
     rc |= grow(ctx, ctx->fits, nb * 8 * sizeof(ModelFit));
     rc |= grow(ctx, ctx->out, nb * sizeof(BandOut));
@@ -501,6 +503,8 @@ static int prepare_layout(lcf_ctx* ctx, int n_sources, int n_bands, int64_t n_ob
     d.uf64 = (double*)ctx->uf64.p;
     d.mag64 = (double*)ctx->mag64.p;
     d.up = (uint8_t*)ctx->up.p;
+    d.ffa = (float4*)ctx->ffa.p;
+    d.ffb = (float2*)ctx->ffb.p;
     d.draws = ctx->d_draws;
     d.svi_eps = ctx->d_eps;
     d.pso_res = (PsoResult*)ctx->res.p;
@@ -696,6 +700,7 @@ static int finish_stats(lcf_ctx* ctx) {
     st.lbfgs_evals = (double)c.lb_evals;
     st.lbfgs_obs_evals = (double)c.lb_obs_evals;
     for (int m = 0; m < 8; m++) st.lbfgs_obs_evals_by_model[m] = (double)c.lb_obs_evals_by_model[m];
+    for (int m = 0; m < 8; m++) st.lbfgs_fp64_obs_evals_by_model[m] = (double)c.lb_fp64_obs_evals_by_model[m];
     for (int k = 0; k < 12; k++) {
         st.pso0_evals_by_kind[k] = (double)c.slot0_evals[k];
         st.pso0_particles_by_kind[k] = (double)c.slot0_particles[k];
@@ -965,6 +970,15 @@ extern "C" int lcf_probe_fp64(lcf_ctx* ctx, double* out9) {
     CK(cudaSetDevice(ctx->device));
     CK(cudaDeviceSynchronize());
     if (probe_fp64_peaks(ctx->num_sms, out9)) return set_err(ctx, LCF_E_CUDA, "FP64 probe failed");
+    return 0;
+}
+
+extern "C" int lcf_probe_ff(lcf_ctx* ctx, double* out80) {
+    if (!ctx || !out80) return LCF_E_INVALID;
+    CK(cudaSetDevice(ctx->device));
+    CK(cudaDeviceSynchronize());
+    for (int i = 0; i < 80; i++) out80[i] = 0.0;
+    if (probe_ff(ctx->num_sms, out80)) return set_err(ctx, LCF_E_CUDA, "double-float probe failed");
     return 0;
 }
 

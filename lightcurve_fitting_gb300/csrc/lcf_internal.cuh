@@ -80,6 +80,13 @@ static __device__ __constant__ double c_pop_w[8][MAXP] = {
     {0.10 * LCF_LN10, 0.010, 0.40 * LCF_LN10, 15.0, 0.35 * LCF_LN10, 0.40 * LCF_LN10, 0.50 * LCF_LN10},
     {5, 5, 5, 5, 5, 5, 5}, {5, 5, 5, 5, 5, 0, 0}, {5, 5, 5, 5, 5, 0, 0},
     {5, 5, 5, 5, 5, 0, 0}, {5, 5, 5, 5, 5, 5, 0}, {5, 5, 5, 5, 5, 0, 0}};
+// 1 / width of the population priors (0 where the width is 0)
+static __device__ __constant__ double c_pop_iw[8][MAXP] = {
+    {1.0 / 2.0, 1.0 / 0.2, 1.0 / 30.0, 1.0 / 2.5, 1.0 / 2.5, 1.0 / 2.0, 0.0},
+    {1.0 / (0.10 * LCF_LN10), 1.0 / 0.010, 1.0 / (0.40 * LCF_LN10), 1.0 / 15.0, 1.0 / (0.35 * LCF_LN10),
+     1.0 / (0.40 * LCF_LN10), 1.0 / (0.50 * LCF_LN10)},
+    {0.2, 0.2, 0.2, 0.2, 0.2, 0.2, 0.2}, {0.2, 0.2, 0.2, 0.2, 0.2, 0, 0}, {0.2, 0.2, 0.2, 0.2, 0.2, 0, 0},
+    {0.2, 0.2, 0.2, 0.2, 0.2, 0, 0}, {0.2, 0.2, 0.2, 0.2, 0.2, 0.2, 0}, {0.2, 0.2, 0.2, 0.2, 0.2, 0, 0}};
 // prior_params (center, width), src/parametric.rs:2072-2115
 static __device__ __constant__ double c_pri_c[8][MAXP] = {
     {0, 0, 0, 0, 0, 0, 0},
@@ -205,6 +212,7 @@ struct Counters {
     unsigned long long slot0_particles[12];  // particle evaluations of the first PSO launch, by kind
     unsigned long long lb_polishes, lb_iters, lb_evals, lb_obs_evals;  // L-BFGS work
     unsigned long long lb_obs_evals_by_model[8];  // observation x (cost + gradient) evaluations, by model
+    unsigned long long lb_fp64_obs_evals_by_model[8];  // of which in FP64 (ff range fallback)
     int32_t sort_hist[8][256];  // per slot: key histogram, then offsets, of the device task sort
     int32_t error;              // first error code raised on the device
     int32_t pad;
@@ -229,6 +237,11 @@ struct DeviceBatch {
     double* uf64;           // upper flux
     double* mag64;          // observed magnitude
     uint8_t* up;            // is_upper
+    // the same observations as double-float pairs for the polish (ff.cuh):
+    // ffa = (t hi, t lo, y hi, y lo), y = flux / peak, or the upper flux for
+    // an upper limit; ffb = obs_var (hi, lo), negated for upper limits
+    float4* ffa;
+    float2* ffb;
     // tables
     const float* draws;     // [3][DRAWS_PER_SEED] uniforms of seeds 42, 137, 271
     const float* svi_eps;   // [3][SVI_STEPS][SVI_SAMPLES][7] noise for 5, 6, 7 params
@@ -299,6 +312,7 @@ double probe_fp32_tflops(int num_sms);
 // the polish's FP64 cost+gradient term for model m (0..6) at full occupancy,
 // out[7] = 0 (MetzgerKN is not polished), out[8] = FP64 TFLOP/s of DFMA chains
 int probe_fp64_peaks(int num_sms, double* out9);
+int probe_ff(int num_sms, double* out80);
 double probe_mufu_gops(int num_sms);
 void launch_band_cost(int model, const float4* obs, int n, float t_last, const double* params, int n_eval,
                       int with_prior, double* costs, float* scratch, cudaStream_t s);

@@ -146,6 +146,12 @@ __global__ void prep_kernel(DeviceBatch d) {
         d.var64[q] = var;
         d.uf64[q] = uf;
         d.up[q] = up ? 1 : 0;
+        {
+            double y = up ? uf : fn;
+            float yh = (float)y, vh = (float)var, vl = (float)(var - (double)vh);
+            d.ffa[q] = make_float4(th, rec.y, yh, (float)(y - (double)yh));
+            d.ffb[q] = up ? make_float2(-vh, -vl) : make_float2(vh, vl);
+        }
         d.mag64[q] = -2.5 * log10(f) + 23.9;
     }
     if (lane == 0) d.stats[b] = st;

@@ -49,6 +49,7 @@ def load(path: str = LIB_PATH):
     L.lcf_band_cost.argtypes = [vp, i, vp, vp, vp, vp, vp, i, vp, i, i, vp]
     L.lcf_probe_peaks.argtypes = [vp, vp]
     L.lcf_probe_fp64.argtypes = [vp, vp]
+    L.lcf_probe_ff.argtypes = [vp, vp]
     L.lcf_debug_swarm_results.argtypes = [vp, vp, C.c_int64]
     for name in ["launch_bazin", "launch_villar", "launch_tde", "launch_arnett", "launch_magnetar",
                  "launch_shock_cooling", "launch_afterglow", "launch_metzger_kn"]:
@@ -160,6 +161,16 @@ class Context:
         buf = np.zeros(9)
         self._check(self.L.lcf_probe_fp64(self.h, buf.ctypes.data), "lcf_probe_fp64")
         return {"obs_evals_per_s": [float(v) for v in buf[:8]], "fp64_tflops": float(buf[8])}
+
+    def probe_ff(self) -> dict:
+        """The polish's double-float observation term: per-model evaluations
+        per second, and its largest disagreement with the FP64 term (overall,
+        and per cost / gradient component) over 256 points per model."""
+        buf = np.zeros(80)
+        self._check(self.L.lcf_probe_ff(self.h, buf.ctypes.data), "lcf_probe_ff")
+        return {"obs_evals_per_s": [float(v) for v in buf[:7]], "worst_rel": [float(v) for v in buf[7:14]],
+                "worst_rel_by_component": buf[14:70].reshape(7, 8).tolist(),
+                "points_in_range": [int(v) for v in buf[70:77]], "nonfinite_mismatch": int(buf[77])}
 
     def swarm_results(self, n_bands: int) -> np.ndarray:
         """Raw swarm results of the last fit: (44 * n_bands, 21) rows, see lcf.h."""
