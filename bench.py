@@ -215,6 +215,7 @@ def run_fused(args, ws, rank, local):
     stream = torch.cuda.ExternalStream(ctx.stream, device=dev)
     peaks = ctx.probe_peaks()
     peaks64 = ctx.probe_fp64()
+    peaks_ff = ctx.probe_ff()
     # device-resident inputs
     d = {
         "times": torch.from_numpy(batch.times).to(dev),
@@ -305,26 +306,33 @@ def run_fused(args, ws, rank, local):
         "launch_ms": pso_ms,
         "particle_obs_evals": float(sum(ev)),
     }
-    # roofline of the dominant kernel, the FP64 L-BFGS polish: its
-    # observation-term evaluations (device-counted, by model) per second of
-    # the launch, against the rate at which the same FP64 term streams at full
-    # occupancy (probe_fp64), for the same model mix
+    # roofline of the polish: its observation-term evaluations per second of
+    # the launch, against the rate at which its own observation terms stream at
+    # full occupancy - the double-float term (probe_ff) for the evaluations it
+    # ran, the FP64 term (probe_fp64) for the range fallbacks - for the same
+    # model mix
     lb_ev = s0["lbfgs_obs_evals_by_model"]
+    lb_fb = s0["lbfgs_fp64_obs_evals_by_model"]
     lb_ms = float(np.mean([s["ms_lbfgs"] for s in stage]))
-    pk = peaks64["obs_evals_per_s"]
-    ideal_s = sum(lb_ev[m] / pk[m] for m in range(7) if pk[m] > 0)
+    pk64, pkff = peaks64["obs_evals_per_s"], peaks_ff["obs_evals_per_s"]
+    ideal_s = sum((lb_ev[m] - lb_fb[m]) / pkff[m] + lb_fb[m] / pk64[m] for m in range(7) if pk64[m] > 0 and pkff[m] > 0)
     lb_rate = sum(lb_ev[:7]) / (lb_ms * 1e-3)
     lb_peak = sum(lb_ev[:7]) / ideal_s if ideal_s > 0 else None
     roofline = {
-        "bound": "fp64",
+        "bound": "fp32 (double-float arithmetic)",
         "achieved": lb_rate,
         "peak": lb_peak,
-        "unit": "observation evaluations/s (FP64 value+gradient+cost term)",
+        "unit": "observation evaluations/s (value + gradient + cost term, double-float; FP64 where out of range)",
         "frac": lb_rate / lb_peak if lb_peak else None,
         "traffic": None,
-        "kernel": "lbfgs_kernel (FP64 L-BFGS polish, the largest stage)",
-        "peak_source": "measured live: the polish's own FP64 observation term streamed at full occupancy "
-                       "(lcf_probe_fp64), weighted by this launch's per-model evaluations",
+        "kernel": "lbfgs_kernel (L-BFGS polish, the largest stage)",
+        "peak_source": "measured live: the polish's own observation terms streamed at full occupancy "
+                       "(lcf_probe_ff for the double-float term, lcf_probe_fp64 for the FP64 fallback), "
+                       "weighted by this launch's per-model evaluations",
+        "ff_term_rate_by_model": pkff,
+        "fp64_term_rate_by_model": pk64[:7],
+        "ff_vs_fp64_worst_rel_by_model": peaks_ff["worst_rel"],
+        "fp64_fallback_share": float(sum(lb_fb[:7]) / max(sum(lb_ev[:7]), 1.0)),
         "fp64_dfma_tflops": peaks64["fp64_tflops"],
         "launch_ms": lb_ms,
         "lbfgs_obs_evals": float(sum(lb_ev[:7])),

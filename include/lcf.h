@@ -212,9 +212,11 @@ int lcf_probe_fp64(lcf_ctx* ctx, double* out9);
  * exponents stay inside FP32's range): out[m] (m = 0..6) = its evaluations
  * per second, streamed as lcf_probe_fp64 streams the FP64 term; out[7 + m] =
  * the largest disagreement with the FP64 term over 256 parameter points of
- * model m inside the PSO box (|ff - FP64| / sum of the terms' magnitudes, over
- * the cost and the gradient components); out[14 + 8 m + c] = the same per
- * component (c = 0: cost, 1 + k: gradient component k); out[70 + m] = the
+ * model m inside the PSO box (|ff - FP64| / sum of the terms' magnitudes,
+ * floored for a gradient component at 1e-10 of the whole gradient's, over the
+ * cost and the gradient components; gradients over the detections);
+ * out[14 + 8 m + c] = the same per component (c = 0: cost, 1 + k: gradient
+ * component k); out[70 + m] = the
  * points of the 256 that the range check keeps in double-float; out[77] =
  * points where exactly one of the two terms was non-finite. */
 int lcf_probe_ff(lcf_ctx* ctx, double* out80);

@@ -26,6 +26,16 @@
 
 #include <cuda_runtime.h>
 
+// Linkage of the larger functions: out of line by default, so that the
+// polish's seven model terms share one copy each instead of inlining dozens
+// (the kernel is otherwise bound by instruction fetch).
+#ifndef LCF_FF_BIG
+#define LCF_FF_BIG __device__ __noinline__
+#endif
+#ifndef LCF_FF_SMALL
+#define LCF_FF_SMALL __device__ __forceinline__
+#endif
+
 namespace lcf {
 
 struct ff {
@@ -119,7 +129,7 @@ __device__ __forceinline__ float sfu_lg2(float x) {
 
 // 1 / b: FP32 Newton step on the SFU seed, then one ff step
 // r = r1 + r1 (1 - b r1), the residual formed in ff.
-__device__ __forceinline__ ff ff_rcp(ff b) {
+LCF_FF_SMALL ff ff_rcp(ff b) {
     float r0 = sfu_rcp(b.hi);
     float r1 = fmaf(r0, fmaf(-b.hi, r0, 1.0f), r0);
     ff br = ff_mul(b, r1);                             // ~1
@@ -129,7 +139,7 @@ __device__ __forceinline__ ff ff_rcp(ff b) {
 __device__ __forceinline__ ff ff_div(ff a, ff b) { return ff_mul(a, ff_rcp(b)); }
 
 // 1 / sqrt(b): y = y1 + y1 (1 - b y1^2) / 2, the residual in ff.
-__device__ __forceinline__ ff ff_rsqrt(ff b) {
+LCF_FF_SMALL ff ff_rsqrt(ff b) {
     float y0 = sfu_rsqrt(b.hi);
     float y1 = y0 * fmaf(-0.5f * b.hi * y0, y0, 1.5f);
     float q = __fmul_rn(y1, y1);
@@ -181,7 +191,7 @@ constexpr float FF_EXP_MIN = -87.0f;  // below: flushed to 0
 
 // e^x.  x.hi above FF_EXP_MAX is clamped there (callers keep their exponents
 // below it or fall back to FP64); below FF_EXP_MIN the result is 0.
-__device__ __forceinline__ ff ff_exp(ff x) {
+LCF_FF_BIG ff ff_exp(ff x) {
     if (x.hi < FF_EXP_MIN) return ffm(0.0f, 0.0f);
     if (x.hi > FF_EXP_MAX) x = ffm(FF_EXP_MAX, 0.0f);
     const float INV = 46.16624130844683f;        // 32 / ln 2
@@ -214,7 +224,7 @@ __device__ __forceinline__ ff ff_exp(ff x) {
 __device__ __forceinline__ ff ff_exp(float x) { return ff_exp(ffm(x, 0.0f)); }
 
 // ln x for x > 0 in FP32's normal range.
-__device__ __forceinline__ ff ff_log(ff x) {
+LCF_FF_BIG ff ff_log(ff x) {
     const float y0 = sfu_lg2(x.hi) * 0.6931471805599453f;
     const ff m = ff_mul(x, ff_exp(-y0));               // x e^-y0 = 1 + eps
     const ff e = ff_add(m, -1.0f);                      // exact: m ~ 1

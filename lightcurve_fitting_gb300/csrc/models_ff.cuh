@@ -20,10 +20,14 @@
 #include "ff.cuh"
 #include "lcf_internal.cuh"
 
+#ifndef LCF_FF_MID
+#define LCF_FF_MID __device__ __forceinline__
+#endif
+
 namespace lcf {
 
 // logistic sigma(x) = 1 / (1 + e^-x) and 1 - sigma(x)
-__device__ __forceinline__ void ff_sigmoid(ff x, ff& sig, ff& oms) {
+LCF_FF_MID void ff_sigmoid(ff x, ff& sig, ff& oms) {
     const bool pos = x.hi >= 0.0f;
     const ff s = ff_exp(pos ? ff_neg(x) : x);  // e^-|x| <= 1
     const ff r = ff_rcp(ff_add(s, 1.0f));
@@ -34,7 +38,7 @@ __device__ __forceinline__ void ff_sigmoid(ff x, ff& sig, ff& oms) {
 
 // phase_soft (src/parametric.rs:306): ps = ln(1 + e^ph) + 1e-6, and
 // sp = d ps / d ph = e^ph / (1 + e^ph)
-__device__ __forceinline__ void ff_softplus(ff ph, ff& ps, ff& sp) {
+LCF_FF_MID void ff_softplus(ff ph, ff& ps, ff& sp) {
     const bool pos = ph.hi > 0.0f;
     const ff s = ff_exp(pos ? ff_neg(ph) : ph);  // e^-|ph|
     const ff q = ff_add(s, 1.0f);
@@ -361,7 +365,7 @@ __device__ __forceinline__ ff ff_poly_as(ff t) {
 // below z ~ -8.3, where the 1e-300 floor makes the ratio up to ~1e285); it is
 // therefore formed in FP64 from the ff pieces, and a ratio beyond FP32's
 // range sets `redo` (the evaluation is then repeated in FP64).
-__device__ __forceinline__ ff ff_upper(ff z, bool want_ratio, ff& ratio, int& redo) {
+LCF_FF_MID ff ff_upper(ff z, bool want_ratio, ff& ratio, int& redo) {
     const ff az = z.hi < 0.0f ? ff_neg(z) : z;
     const ff a = ff_mul(az, ffm(0.7071067690849304f, 1.2101617485882343e-08f));
     const ff t = ff_rcp(ff_add(ff_mul(a, ffm(0.32759109139442444f, 8.605575807507648e-09f)), 1.0f));

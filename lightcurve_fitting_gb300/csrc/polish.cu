@@ -285,10 +285,12 @@ __device__ void polish_band(const DeviceBatch& d, int b) {
 // warps resident on an SM) polish the same model, whose code then stays in
 // the instruction cache.
 // Blocks of 128 threads per SM the polish's register budget is sized for
-// (168 registers a thread): measured on GB300, 12 resident warps with a few
-// spills polish ~6 % faster than 8 warps without.
+// (64 registers a thread): measured on GB300 at 10k sources, 32 resident
+// warps polish in 607 ms against 644 ms with 20 warps, 712 ms with 12 and
+// 812 ms with 8, spills included (the double-float polish is bound by
+// latency and instruction fetch, not by one pipe).
 #ifndef LCF_LB_MINB
-#define LCF_LB_MINB 3
+#define LCF_LB_MINB 8
 #endif
 __global__ void __launch_bounds__(128, LCF_LB_MINB) lbfgs_kernel(DeviceBatch d, int model_mask) {
     const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
@@ -420,8 +422,8 @@ __global__ void __launch_bounds__(256) probe_ff_kernel(const float4* fa, const f
 // Agreement of the ff and FP64 observation terms: one warp per parameter
 // point (pts[w], MAXP doubles), lanes over the probe band; writes per point
 // the FP64 sums, the ff sums and the sums of the terms' magnitudes of the
-// cost and of the MAXP gradient components (3 * (1 + MAXP) doubles), and
-// whether the point is inside ff_range_ok.
+// cost (all observations) and of the MAXP gradient components (detections),
+// 3 * (1 + MAXP) doubles, and whether the point stays in double-float.
 template <int MODEL>
 __global__ void ff_check_kernel(const double* band, const float4* fa, const float2* fb, int nb, const double* pts,
                                 int n_pts, double* out) {
@@ -452,7 +454,10 @@ __global__ void ff_check_kernel(const double* band, const float4* fa, const floa
         lb_obs_term<MODEL>(m64, t[i], var[i], flux[i], upd[i] != 0.0, uf[i], se2, true, n1, g1, nf64);
         ff_obs_term<MODEL>(mff, fa[i], fb[i], se2f, true, n2, g2, nfff, redo);
         v64[0] += n1; vff[0] += ff_to(n2); mag[0] += fabs(n1);
-        for (int k = 0; k < MAXP; k++) { v64[1 + k] += g1[k]; vff[1 + k] += ff_to(g2[k]); mag[1 + k] += fabs(g1[k]); }
+        // gradients of detections only: an upper limit's FP64 gradient ratio
+        // carries the reference's cancellation (see ff_upper)
+        if (upd[i] == 0.0)
+            for (int k = 0; k < MAXP; k++) { v64[1 + k] += g1[k]; vff[1 + k] += ff_to(g2[k]); mag[1 + k] += fabs(g1[k]); }
     }
     for (int k = 0; k <= MAXP; k++) {
         v64[k] = warp_sum_d(v64[k]);
@@ -638,8 +643,14 @@ int probe_ff(int num_sms, double* out) {
                 in_range++;
                 if (o[3 * (1 + MAXP) + 1] != 0.0 && o[3 * (1 + MAXP) + 1] != 3.0) out[77] += 1.0;
                 if (o[3 * (1 + MAXP) + 1] != 0.0) continue;
+                // each component against the magnitude of its own terms,
+                // floored at 1e-10 of the gradient's total (a component below
+                // that, e.g. 1e-40 in FP64 against 0 in double-float, is
+                // compared in absolute terms)
+                double gsum = 0.0;
+                for (int c = 1; c <= MAXP; c++) gsum += o[2 * (1 + MAXP) + c];
                 for (int c = 0; c <= MAXP; c++) {
-                    const double mg = o[2 * (1 + MAXP) + c];
+                    const double mg = c == 0 ? o[2 * (1 + MAXP)] : fmax(o[2 * (1 + MAXP) + c], 1e-10 * gsum);
                     if (!(mg > 0.0)) continue;
                     const double rel = fabs(o[1 + MAXP + c] - o[c]) / mg;
                     out[14 + m * 8 + c] = fmax(out[14 + m * 8 + c], rel);
