@@ -21,7 +21,10 @@
 namespace lcf {
 
 // MINPACK cstep (Moré–Thuente), min/max with Rust's NaN-ignoring semantics
-__device__ inline int lb_cstep(double& stx, double& fx, double& dx, double& sty, double& fy, double& dy, double& stp, double fp,
+#ifndef LCF_CSTEP_ATTR
+#define LCF_CSTEP_ATTR static __device__ inline
+#endif
+LCF_CSTEP_ATTR int lb_cstep(double& stx, double& fx, double& dx, double& sty, double& fy, double& dy, double& stp, double fp,
                         double dp, bool& brackt, double stpmin, double stpmax) {
     if ((brackt && (stp <= fmin(stx, sty) || stp >= fmax(stx, sty))) || dx * (stp - stx) >= 0.0 || stpmax < stpmin)
         return 0;

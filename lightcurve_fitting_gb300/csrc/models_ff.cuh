@@ -23,6 +23,11 @@
 #ifndef LCF_FF_MID
 #define LCF_FF_MID __device__ __forceinline__
 #endif
+// the upper-limit term runs for ~1/4 of the observations: out of line it keeps
+// the observation loop's hot code smaller (measured 1.5 % faster polish)
+#ifndef LCF_FF_UPPER
+#define LCF_FF_UPPER __device__ __noinline__
+#endif
 
 namespace lcf {
 
@@ -365,7 +370,7 @@ __device__ __forceinline__ ff ff_poly_as(ff t) {
 // below z ~ -8.3, where the 1e-300 floor makes the ratio up to ~1e285); it is
 // therefore formed in FP64 from the ff pieces, and a ratio beyond FP32's
 // range sets `redo` (the evaluation is then repeated in FP64).
-LCF_FF_MID ff ff_upper(ff z, bool want_ratio, ff& ratio, int& redo) {
+LCF_FF_UPPER ff ff_upper(ff z, bool want_ratio, ff& ratio, int& redo) {
     const ff az = z.hi < 0.0f ? ff_neg(z) : z;
     const ff a = ff_mul(az, ffm(0.7071067690849304f, 1.2101617485882343e-08f));
     const ff t = ff_rcp(ff_add(ff_mul(a, ffm(0.32759109139442444f, 8.605575807507648e-09f)), 1.0f));

@@ -100,6 +100,9 @@ __device__ __forceinline__ void lb_obs_term(const Model64& mod, double t, double
     }
 }
 
+#ifndef LCF_FALLBACK_ATTR
+#define LCF_FALLBACK_ATTR __device__ __forceinline__
+#endif
 // Cost and projected gradient of the bounded problem (BoundedPsoCost,
 // src/parametric.rs:1500-1535) for the lane-distributed polish: the full
 // parameter vector is gathered from lanes 0..np-1, the lanes split the
@@ -121,6 +124,18 @@ struct LaneLb {
     double nd, inv_nd;
     double lo_j, hi_j;
     int evals, iters, fp64_evals;
+
+    // the observation terms in FP64 (lb_obs_term), this lane's share
+    template <int M>
+    LCF_FALLBACK_ATTR int fp64_terms(const double* q, const double* ep, const double* rp, double se2, bool want_grad,
+                                     double& nll, double* gl) const {
+        int nonfinite = 0;
+        Model64 mod;
+        mod.init_pre(M, q, ep, rp);
+        for (int i = (int)(threadIdx.x & 31); i < n; i += 32)
+            lb_obs_term<M>(mod, t[i], var[i], flux[i], up[i], uf[i], se2, want_grad, nll, gl, nonfinite);
+        return nonfinite;
+    }
 
 #ifdef LCF_LB_INLINE
     __device__ void cost_grad(double xj, double& fo, double& gj, bool want_grad) {
@@ -203,11 +218,7 @@ struct LaneLb {
             double nll = 0.0, gl[MAXP];
 #pragma unroll
             for (int k = 0; k < MAXP; k++) gl[k] = 0.0;
-            nonfinite = 0;
-            Model64 mod;
-            mod.init_pre(MODEL, q, ep, rp);
-            for (int i = lane; i < n; i += 32)
-                lb_obs_term<MODEL>(mod, t[i], var[i], flux[i], up[i], uf[i], se2, want_grad, nll, gl, nonfinite);
+            nonfinite = fp64_terms<MODEL>(q, ep, rp, se2, want_grad, nll, gl);
             nonfinite = warp_or(nonfinite);
             if (want_grad) {
                 double v[8] = {nll, gl[0], gl[1], gl[2], gl[3], gl[4], gl[5], gl[6]};
