@@ -243,6 +243,31 @@ int lcf_band_cost(lcf_ctx* ctx, int model, const double* times, const double* fl
                   double* costs);
 
 /*
+ * SVI ELBO gradient at given variational parameters: for each of `n_points`
+ * points, the Monte-Carlo ELBO estimate of one SVI step and its gradient,
+ * as svi_fit forms them (src/parametric.rs:2262-2393; the reference GPU
+ * kernel's per-step gradient, cuda/svi.cu, bound at src/gpu_cuda.rs:139-164):
+ * for each draw eps_s, theta = mu + exp(log_sigma) * eps_s; the log-likelihood
+ * of theta over the band and its gradient by the adjoint through the analytic
+ * model gradient (MetzgerKN: forward-mode duals through the ODE); the Gaussian
+ * prior centred on `prior_init` (the PSO parameters; sigma_extra has its
+ * fixed centre); the sample mean, plus the entropy sum(log_sigma) +
+ * np/2 ln(2 pi e).  The arithmetic is the SVI kernel's own (FP32 likelihood
+ * and adjoint, FP64 bookkeeping).
+ *   band: host FP64, peak-normalised, as lcf_band_cost;
+ *   prior_init [np]; var_params [n_points][2 np] = (mu, log_sigma);
+ *   eps [n_points][n_samples][np] standard-normal draws;
+ *   elbo [n_points]; grad [n_points][2 np] = (d/d mu, d/d log_sigma);
+ *   flags [n_points]: bit 0 = an upper-limit CDF underflowed (the reference's
+ *   gradient is ~1e285 there and its Adam freezes), bit 1 = a MetzgerKN sample
+ *   was skipped by the reference's peak-rescale rule.
+ */
+int lcf_svi_elbo_grad(lcf_ctx* ctx, int model, const double* times, const double* flux,
+                      const double* obs_var, const uint8_t* is_upper, const double* upper_flux, int n_obs,
+                      const double* prior_init, const double* var_params, int n_points,
+                      const double* eps, int n_samples, double* elbo, double* grad, int* flags);
+
+/*
  * Allocation-free variant of lcf_band_cost, for callers that cannot call
  * cudaMalloc: a host framework that owns all device memory through its own
  * pool or budget, or an embedding where the library must not allocate GPU

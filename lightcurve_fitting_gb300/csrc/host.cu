@@ -126,6 +126,8 @@ struct lcf_ctx {
     DevArr h_in, h_out;
     // band-cost scratch
     DevArr bc_obs, bc_params, bc_costs, bc_scratch;
+    // ELBO-gradient check buffers
+    DevArr sg_in, sg_out, sg_scratch;
     // plain FP64 form: MetzgerKN prediction rows (96 per observation)
     DevArr plain_scr;
     // layout cache
@@ -251,7 +253,8 @@ extern "C" void lcf_ctx_destroy(lcf_ctx* ctx) {
                      &ctx->fits, &ctx->out, &ctx->mb, &ctx->ctr, &ctx->scratch, &ctx->scratch64, &ctx->scratch_svi,
                      &ctx->t0state, &ctx->task_sorted, &ctx->joint_flag, &ctx->joint_src, &ctx->joint_res,
                      &ctx->joint_draws,
-                     &ctx->bc_obs, &ctx->bc_params, &ctx->bc_costs, &ctx->bc_scratch, &ctx->plain_scr};
+                     &ctx->bc_obs, &ctx->bc_params, &ctx->bc_costs, &ctx->bc_scratch, &ctx->plain_scr,
+                     &ctx->sg_in, &ctx->sg_out, &ctx->sg_scratch};
     for (DevArr* a : all) free_arr(*a);
     for (auto& a : ctx->tasks) free_arr(a);
     if (ctx->h_in.p) cudaFreeHost(ctx->h_in.p);
@@ -900,18 +903,14 @@ extern "C" int lcf_download_outputs(lcf_ctx* ctx, lcf_fit_outputs* out) {
 // ---------------------------------------------------------------------------
 // Batched likelihood on one band (PsoCost::cost_from_slice)
 // ---------------------------------------------------------------------------
-extern "C" int lcf_band_cost(lcf_ctx* ctx, int model, const double* times, const double* flux, const double* obs_var,
-                             const uint8_t* is_upper, const double* upper_flux, int n_obs, const double* params,
-                             int n_eval, int with_prior, double* costs) {
-    if (!ctx) return LCF_E_INVALID;
-    if (model < 0 || model > 7 || n_obs < 0 || n_eval < 0) return set_err(ctx, LCF_E_INVALID, "bad argument");
-    if (n_eval == 0) return 0;
-    CK(cudaSetDevice(ctx->device));
-    // FP32 records sorted by time (stable)
+// FP32 observation records of one peak-normalised band, sorted by time
+// (stable), as prep_kernel builds them for a fit; returns the last time.
+static double band_records(const double* times, const double* flux, const double* obs_var, const uint8_t* is_upper,
+                           const double* upper_flux, int n_obs, std::vector<float4>& rec) {
     std::vector<int> ord(n_obs);
     for (int i = 0; i < n_obs; i++) ord[i] = i;
     std::stable_sort(ord.begin(), ord.end(), [&](int a, int b) { return times[a] < times[b]; });
-    std::vector<float4> rec(std::max(n_obs, 1));
+    rec.assign(std::max(n_obs, 1), make_float4(0.0f, 0.0f, 0.0f, 0.0f));
     double t_last = -INFINITY;
     for (int k = 0; k < n_obs; k++) {
         int i = ord[k];
@@ -922,6 +921,18 @@ extern "C" int lcf_band_cost(lcf_ctx* ctx, int model, const double* times, const
         rec[k] = make_float4(th, (float)(t - (double)th), (float)(up ? upper_flux[i] : flux[i]),
                              up ? -(float)obs_var[i] : (float)obs_var[i]);
     }
+    return t_last;
+}
+
+extern "C" int lcf_band_cost(lcf_ctx* ctx, int model, const double* times, const double* flux, const double* obs_var,
+                             const uint8_t* is_upper, const double* upper_flux, int n_obs, const double* params,
+                             int n_eval, int with_prior, double* costs) {
+    if (!ctx) return LCF_E_INVALID;
+    if (model < 0 || model > 7 || n_obs < 0 || n_eval < 0) return set_err(ctx, LCF_E_INVALID, "bad argument");
+    if (n_eval == 0) return 0;
+    CK(cudaSetDevice(ctx->device));
+    std::vector<float4> rec;
+    double t_last = band_records(times, flux, obs_var, is_upper, upper_flux, n_obs, rec);
     int np = n_params_of(model);
     int rc = 0;
     rc |= grow(ctx, ctx->bc_obs, rec.size() * sizeof(float4));
@@ -936,6 +947,46 @@ extern "C" int lcf_band_cost(lcf_ctx* ctx, int model, const double* times, const
                      n_eval, with_prior, (double*)ctx->bc_costs.p, (float*)ctx->bc_scratch.p, s);
     CK(cudaGetLastError());
     CK(cudaMemcpyAsync(costs, ctx->bc_costs.p, (size_t)n_eval * 8, cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+    return 0;
+}
+
+extern "C" int lcf_svi_elbo_grad(lcf_ctx* ctx, int model, const double* times, const double* flux,
+                                 const double* obs_var, const uint8_t* is_upper, const double* upper_flux, int n_obs,
+                                 const double* prior_init, const double* var_params, int n_points, const double* eps,
+                                 int n_samples, double* elbo, double* grad, int* flags) {
+    if (!ctx) return LCF_E_INVALID;
+    if (model < 0 || model > 7 || n_obs < 1 || n_points < 0 || n_samples < 1)
+        return set_err(ctx, LCF_E_INVALID, "bad argument");
+    if (!times || !flux || !obs_var || !is_upper || !upper_flux || !prior_init)
+        return set_err(ctx, LCF_E_INVALID, "null band or prior pointer");
+    if (n_points == 0) return 0;
+    if (!var_params || !eps || !elbo || !grad || !flags) return set_err(ctx, LCF_E_INVALID, "null point pointer");
+    CK(cudaSetDevice(ctx->device));
+    std::vector<float4> rec;
+    double t_last = band_records(times, flux, obs_var, is_upper, upper_flux, n_obs, rec);
+    const int np = n_params_of(model);
+    const size_t n_vp = (size_t)n_points * 2 * np, n_eps = (size_t)n_points * n_samples * np;
+    int rc = 0;
+    rc |= grow(ctx, ctx->bc_obs, rec.size() * sizeof(float4));
+    rc |= grow(ctx, ctx->sg_in, (np + n_vp + n_eps) * 8);
+    rc |= grow(ctx, ctx->sg_out, (n_points + n_vp) * 8 + (size_t)n_points * 4);
+    rc |= grow(ctx, ctx->sg_scratch, (size_t)n_points * 5 * n_obs * 4);
+    if (rc) return rc;
+    cudaStream_t s = ctx->stream;
+    double* din = (double*)ctx->sg_in.p;
+    double* dout = (double*)ctx->sg_out.p;
+    int* dflags = (int*)(dout + n_points + n_vp);
+    CK(cudaMemcpyAsync(ctx->bc_obs.p, rec.data(), rec.size() * sizeof(float4), cudaMemcpyHostToDevice, s));
+    CK(cudaMemcpyAsync(din, prior_init, (size_t)np * 8, cudaMemcpyHostToDevice, s));
+    CK(cudaMemcpyAsync(din + np, var_params, n_vp * 8, cudaMemcpyHostToDevice, s));
+    CK(cudaMemcpyAsync(din + np + n_vp, eps, n_eps * 8, cudaMemcpyHostToDevice, s));
+    launch_svi_grad(model, (const float4*)ctx->bc_obs.p, n_obs, (float)t_last, din, din + np, n_points,
+                    din + np + n_vp, n_samples, dout, dout + n_points, dflags, (float*)ctx->sg_scratch.p, s);
+    CK(cudaGetLastError());
+    CK(cudaMemcpyAsync(elbo, dout, (size_t)n_points * 8, cudaMemcpyDeviceToHost, s));
+    CK(cudaMemcpyAsync(grad, dout + n_points, n_vp * 8, cudaMemcpyDeviceToHost, s));
+    CK(cudaMemcpyAsync(flags, dflags, (size_t)n_points * 4, cudaMemcpyDeviceToHost, s));
     CK(cudaStreamSynchronize(s));
     return 0;
 }

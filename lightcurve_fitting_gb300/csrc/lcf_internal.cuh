@@ -297,6 +297,11 @@ void launch_mb_build(const DeviceBatch& d, int slot, int k, cudaStream_t s);
 void launch_lbfgs(const DeviceBatch& d, int model_mask, cudaStream_t s);
 void launch_select(const DeviceBatch& d, int fit_all, int forced, cudaStream_t s);
 void launch_svi(const DeviceBatch& d, cudaStream_t s);
+// one SVI step's ELBO estimate and gradient at given variational parameters
+// (lcf_svi_elbo_grad); scratch = 5 n floats per point
+void launch_svi_grad(int model, const float4* obs, int n, float t_last, const double* init, const double* vpar,
+                     int n_points, const double* eps, int n_samples, double* elbo, double* grad, int* flags,
+                     float* scratch, cudaStream_t s);
 // plain.cu (the plain FP64 form)
 void launch_plain_pso(const DeviceBatch& d, int m, int gate, double* mscr, cudaStream_t s);
 void launch_plain_lbfgs(const DeviceBatch& d, int m, cudaStream_t s);

@@ -709,6 +709,108 @@ __device__ __forceinline__ float reduce_scatter8f(const float* v) {
     return c;
 }
 
+// One reparameterised sample's log-likelihood over the band and its
+// gradient, the adjoint through the analytic model gradient (the body of an
+// SVI step, src/parametric.rs:2280-2330).  pf = the sample's parameters in
+// FP32, held by every lane; ms = this sample's MetzgerKN sweep rows (value +
+// 4 derivatives per observation), unused by the other models.  Returns false
+// when the reference skips the sample (MetzgerKN peak rescale outside its
+// clamp).  Otherwise lls = the log-likelihood (every lane), dl_tot = lane l's
+// total d loglik / d theta_{(l >> 2) & 7} (reduce_scatter8f), huge = 1 when an
+// upper-limit ratio overflowed in some lane (the reference's CDF floor).
+template <int M>
+__device__ __forceinline__ bool svi_sample_loglik(const float4* obs, int n, const float* pf, const float* ms,
+                                                  double& lls, float& dl_tot, int& huge_out) {
+    constexpr int np = n_params_of(M), se = se_idx_of(M);
+    const int lane = threadIdx.x & 31;
+    float sx = expf(pf[se]);
+    float sx2 = sx * sx;
+    float dll[8];
+#pragma unroll
+    for (int q = 0; q < 8; q++) dll[q] = 0.0f;
+    Nll ll;
+    ll.reset();
+    int huge = 0;
+    bool skip_sample = false;
+    if constexpr (M == METZGER) {
+        // predictions and derivatives of the normalised model, then the
+        // reference's peak rescale (src/parametric.rs:2303-2323)
+        float mx = -INFINITY;
+        for (int i = lane; i < n; i += 32)
+            if (obs[i].w >= 0.0f) mx = fmaxf(mx, ms[i * 5]);
+        for (int kk = 16; kk; kk >>= 1) mx = fmaxf(mx, __shfl_xor_sync(FULL, mx, kk));
+        float scl = 1.0f;
+        if (mx > 1e-10f && isfinite(mx)) {
+            float raw = 1.0f / mx;
+            scl = fminf(fmaxf(raw, 0.1f), 10.0f);
+            if (fabsf(raw - scl) / raw > 0.5f) skip_sample = true;
+        }
+        if (!skip_sample) {
+            for (int i = lane; i < n; i += 32) {
+                float4 ob = obs[i];
+                float pr = ms[i * 5] * scl;
+                float gb[MAXP];
+                for (int q = 0; q < 4; q++) gb[q] = ms[i * 5 + 1 + q] * scl;
+                gb[4] = 0.0f;
+                float tv = fabsf(ob.w) + sx2;
+                float stv = sqrtf(tv);
+                if (ob.w < 0.0f) {
+                    float z = (ob.z - pr) / stv;
+                    ll.add(log_normal_cdf_f(z));
+                    bool hg;
+                    float ratio = upper_ratio_f32(z, hg);
+                    if (hg) huge = 1;
+                    for (int q = 0; q < 4; q++) if (isfinite(gb[q])) dll[q] += -ratio / stv * gb[q];
+                    dll[se] += ratio * (-(ob.z - pr) * sx2 / (stv * tv));
+                } else {
+                    float res = ob.z - pr;
+                    float it = 1.0f / tv;
+                    float r2 = res * res;
+                    ll.add(-0.5f * (r2 * it + logf(6.283185307179586f * tv)));
+                    for (int q = 0; q < 4; q++) if (isfinite(gb[q])) dll[q] += res * it * gb[q];
+                    dll[se] += (r2 * it * it - it) * sx2;
+                }
+            }
+        }
+    } else {
+        for (int i = lane; i < n; i += 32) {
+            float4 ob = obs[i];
+            float gb[MAXP];
+            int st;
+            float pr = model_grad_f32(M, pf, ob.x, ob.y, gb, st);
+            if (st == ST_NONFINITE || !isfinite(pr)) continue;
+            float tv = fabsf(ob.w) + sx2;
+            float stv = sqrtf(tv);
+            if (ob.w < 0.0f) {
+                float z = (ob.z - pr) / stv;
+                ll.add(log_normal_cdf_f(z));
+                bool hg;
+                float ratio = upper_ratio_f32(z, hg);
+                if (hg) huge = 1;
+                float dpred = -ratio / stv;
+#pragma unroll
+                for (int q = 0; q < np; q++)
+                    if (q != se && isfinite(gb[q])) dll[q] += dpred * gb[q];
+                dll[se] += ratio * (-(ob.z - pr) * sx2 / (stv * tv));
+            } else {
+                float res = ob.z - pr;
+                float it = 1.0f / tv;
+                float r2 = res * res;
+                ll.add(-0.5f * (r2 * it + logf(6.283185307179586f * tv)));
+#pragma unroll
+                for (int q = 0; q < np; q++)
+                    if (q != se && isfinite(gb[q])) dll[q] += res * it * gb[q];
+                dll[se] += (r2 * it * it - it) * sx2;
+            }
+        }
+    }
+    if (__any_sync(FULL, skip_sample)) return false;
+    huge_out = warp_or(huge);
+    lls = warp_sum_d((double)ll.s - (double)ll.c);
+    dl_tot = reduce_scatter8f(dll);
+    return true;
+}
+
 template <int M>
 __device__ void svi_band(const DeviceBatch& d, int b) {
     const int lane = threadIdx.x & 31, j = lane & 7;
@@ -766,93 +868,12 @@ __device__ void svi_band(const DeviceBatch& d, int b) {
             float pf[MAXP];
 #pragma unroll
             for (int q = 0; q < MAXP; q++) pf[q] = q < np ? __shfl_sync(FULL, (float)th_j, q) : 0.0f;
-            float sx = expf(pf[se]);
-            float sx2 = sx * sx;
-            float dll[8];
-#pragma unroll
-            for (int q = 0; q < 8; q++) dll[q] = 0.0f;
-            Nll ll;
-            ll.reset();
-            int huge = 0;
-            bool skip_sample = false;
-            if constexpr (M == METZGER) {
-                // predictions and derivatives of the normalised model, then the
-                // reference's peak rescale (src/parametric.rs:2303-2323)
-                const float* ms = mscr + (size_t)k * 5 * n;
-                float mx = -INFINITY;
-                for (int i = lane; i < n; i += 32)
-                    if (obs[i].w >= 0.0f) mx = fmaxf(mx, ms[i * 5]);
-                for (int kk = 16; kk; kk >>= 1) mx = fmaxf(mx, __shfl_xor_sync(FULL, mx, kk));
-                float scl = 1.0f;
-                if (mx > 1e-10f && isfinite(mx)) {
-                    float raw = 1.0f / mx;
-                    scl = fminf(fmaxf(raw, 0.1f), 10.0f);
-                    if (fabsf(raw - scl) / raw > 0.5f) skip_sample = true;
-                }
-                if (!skip_sample) {
-                    for (int i = lane; i < n; i += 32) {
-                        float4 ob = obs[i];
-                        float pr = ms[i * 5] * scl;
-                        float gb[MAXP];
-                        for (int q = 0; q < 4; q++) gb[q] = ms[i * 5 + 1 + q] * scl;
-                        gb[4] = 0.0f;
-                        float tv = fabsf(ob.w) + sx2;
-                        float stv = sqrtf(tv);
-                        if (ob.w < 0.0f) {
-                            float z = (ob.z - pr) / stv;
-                            ll.add(log_normal_cdf_f(z));
-                            bool hg;
-                            float ratio = upper_ratio_f32(z, hg);
-                            if (hg) huge = 1;
-                            for (int q = 0; q < 4; q++) if (isfinite(gb[q])) dll[q] += -ratio / stv * gb[q];
-                            dll[se] += ratio * (-(ob.z - pr) * sx2 / (stv * tv));
-                        } else {
-                            float res = ob.z - pr;
-                            float it = 1.0f / tv;
-                            float r2 = res * res;
-                            ll.add(-0.5f * (r2 * it + logf(6.283185307179586f * tv)));
-                            for (int q = 0; q < 4; q++) if (isfinite(gb[q])) dll[q] += res * it * gb[q];
-                            dll[se] += (r2 * it * it - it) * sx2;
-                        }
-                    }
-                }
-            } else {
-                for (int i = lane; i < n; i += 32) {
-                    float4 ob = obs[i];
-                    float gb[MAXP];
-                    int st;
-                    float pr = model_grad_f32(M, pf, ob.x, ob.y, gb, st);
-                    if (st == ST_NONFINITE || !isfinite(pr)) continue;
-                    float tv = fabsf(ob.w) + sx2;
-                    float stv = sqrtf(tv);
-                    if (ob.w < 0.0f) {
-                        float z = (ob.z - pr) / stv;
-                        ll.add(log_normal_cdf_f(z));
-                        bool hg;
-                        float ratio = upper_ratio_f32(z, hg);
-                        if (hg) huge = 1;
-                        float dpred = -ratio / stv;
-#pragma unroll
-                        for (int q = 0; q < np; q++)
-                            if (q != se && isfinite(gb[q])) dll[q] += dpred * gb[q];
-                        dll[se] += ratio * (-(ob.z - pr) * sx2 / (stv * tv));
-                    } else {
-                        float res = ob.z - pr;
-                        float it = 1.0f / tv;
-                        float r2 = res * res;
-                        ll.add(-0.5f * (r2 * it + logf(6.283185307179586f * tv)));
-#pragma unroll
-                        for (int q = 0; q < np; q++)
-                            if (q != se && isfinite(gb[q])) dll[q] += res * it * gb[q];
-                        dll[se] += (r2 * it * it - it) * sx2;
-                    }
-                }
-            }
-            if (__any_sync(FULL, skip_sample)) continue;
-            if (warp_or(huge)) huge_any = 1;
-            const double lls = warp_sum_d((double)ll.s - (double)ll.c);
+            double lls;
+            float dl_tot;
+            int huge;
+            if (!svi_sample_loglik<M>(obs, n, pf, mscr + (size_t)k * 5 * n, lls, dl_tot, huge)) continue;
+            if (huge) huge_any = 1;
             // lane j: total d loglik / d theta_j, then its prior and ELBO terms
-            const float dl_tot = reduce_scatter8f(dll);
             const double dl_j = (double)__shfl_sync(FULL, dl_tot, (4 * j) & 31);
             double lp_j = 0.0;
             if (own) {
@@ -929,6 +950,114 @@ void launch_svi(const DeviceBatch& d, cudaStream_t s) {
     int block = 128;
     int64_t threads = (int64_t)d.n_bands * 8 * 32;
     svi_kernel<<<(int)((threads + block - 1) / block), block, 0, s>>>(d);
+}
+
+// ---------------------------------------------------------------------------
+// ELBO gradient check (lcf_svi_elbo_grad): one SVI step's Monte-Carlo ELBO
+// estimate and its gradient at caller-given variational parameters and
+// standard-normal draws, through svi_sample_loglik and the prior and entropy
+// terms of svi_band — the SVI kernel's step without Adam.  One warp per
+// parameter point; `mscr` holds 5 n floats (one MetzgerKN sweep) per warp.
+// ---------------------------------------------------------------------------
+template <int M>
+__device__ void svi_grad_point(const float4* obs, int n, float t_last, const double* init, const double* vpar,
+                               const double* eps, int n_samples, double* elbo_out, double* grad_out, int* flags_out,
+                               float* mscr) {
+    constexpr int np = n_params_of(M), se = se_idx_of(M);
+    const int lane = threadIdx.x & 31, j = lane & 7;
+    const bool own = j < np;
+    const double init_j = own ? init[j] : 0.0;
+    const double pc_j = own ? (j == se ? c_pri_c[M][j] : init_j) : 0.0;
+    const double pw2_j = own ? c_pri_w[M][j] * c_pri_w[M][j] : 1.0;
+    const double mu_j = own ? vpar[j] : 0.0;
+    const double ls_j = own ? vpar[np + j] : 0.0;
+    const double sg_j = own ? exp(ls_j) : 0.0;
+    const double ln_2pie = 2.8378770664093453;  // ln(2 pi e)
+    struct ObsTimes {
+        const float4* o;
+        __device__ float operator()(int q) const { return o[q].x + o[q].y; }
+    } otimes{obs};
+    double gmu_j = 0.0, gls_j = 0.0, elbo_sum = 0.0;
+    int huge_any = 0, skipped = 0;
+    for (int k = 0; k < n_samples; k++) {
+        const double eps_j = own ? eps[(size_t)k * np + j] : 0.0;
+        const double th_j = mu_j + sg_j * eps_j;
+        float pf[MAXP];
+#pragma unroll
+        for (int q = 0; q < MAXP; q++) pf[q] = q < np ? __shfl_sync(FULL, (float)th_j, q) : 0.0f;
+        if constexpr (M == METZGER) {
+            if (lane == 0) metzger_dual_sweep(pf, t_last, otimes, n, mscr);
+            __syncwarp();
+        }
+        double lls;
+        float dl_tot;
+        int huge;
+        const bool ok = svi_sample_loglik<M>(obs, n, pf, mscr, lls, dl_tot, huge);
+        __syncwarp();  // the MetzgerKN rows are rewritten by the next sample
+        if (!ok) {
+            skipped = 1;
+            continue;
+        }
+        if (huge) huge_any = 1;
+        const double dl_j = (double)__shfl_sync(FULL, dl_tot, (4 * j) & 31);
+        double lp_j = 0.0;
+        if (own) {
+            const double dd = th_j - pc_j;
+            lp_j = -0.5 * dd * dd / pw2_j;
+            const double df = dl_j + (-dd / pw2_j);
+            gmu_j += df;
+            gls_j += df * sg_j * eps_j;
+        }
+        const double lp = dot8(lp_j, 1.0);
+        elbo_sum += lls + lp;
+    }
+    const double ns = (double)n_samples;
+    const double ent = dot8(own ? ls_j : 0.0, 1.0) + 0.5 * (double)np * ln_2pie;
+    if (lane < np) {
+        grad_out[lane] = gmu_j / ns;
+        grad_out[np + lane] = gls_j / ns + 1.0;
+    }
+    if (lane == 0) {
+        *elbo_out = elbo_sum / ns + ent;
+        *flags_out = huge_any | (skipped << 1);
+    }
+}
+
+__global__ void __launch_bounds__(128) svi_grad_kernel(int model, const float4* obs, int n, float t_last,
+                                                       const double* init, const double* vpar, int n_points,
+                                                       const double* eps, int n_samples, double* elbo, double* grad,
+                                                       int* flags, float* scratch) {
+    const int p = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    if (p >= n_points) return;
+    const int np = n_params_of(model);
+    const double* vp = vpar + (size_t)p * 2 * np;
+    const double* ep = eps + (size_t)p * n_samples * np;
+    double* g = grad + (size_t)p * 2 * np;
+    float* ms = scratch + (size_t)p * 5 * n;
+    switch (model) {
+        case BAZIN: svi_grad_point<BAZIN>(obs, n, t_last, init, vp, ep, n_samples, elbo + p, g, flags + p, ms); break;
+        case VILLAR: svi_grad_point<VILLAR>(obs, n, t_last, init, vp, ep, n_samples, elbo + p, g, flags + p, ms); break;
+        case TDE: svi_grad_point<TDE>(obs, n, t_last, init, vp, ep, n_samples, elbo + p, g, flags + p, ms); break;
+        case ARNETT: svi_grad_point<ARNETT>(obs, n, t_last, init, vp, ep, n_samples, elbo + p, g, flags + p, ms); break;
+        case MAGNETAR:
+            svi_grad_point<MAGNETAR>(obs, n, t_last, init, vp, ep, n_samples, elbo + p, g, flags + p, ms);
+            break;
+        case SHOCK: svi_grad_point<SHOCK>(obs, n, t_last, init, vp, ep, n_samples, elbo + p, g, flags + p, ms); break;
+        case AFTERGLOW:
+            svi_grad_point<AFTERGLOW>(obs, n, t_last, init, vp, ep, n_samples, elbo + p, g, flags + p, ms);
+            break;
+        default: svi_grad_point<METZGER>(obs, n, t_last, init, vp, ep, n_samples, elbo + p, g, flags + p, ms); break;
+    }
+}
+
+void launch_svi_grad(int model, const float4* obs, int n, float t_last, const double* init, const double* vpar,
+                     int n_points, const double* eps, int n_samples, double* elbo, double* grad, int* flags,
+                     float* scratch, cudaStream_t s) {
+    if (n_points <= 0) return;
+    const int block = 128;
+    const int64_t threads = (int64_t)n_points * 32;
+    svi_grad_kernel<<<(int)((threads + block - 1) / block), block, 0, s>>>(model, obs, n, t_last, init, vpar, n_points,
+                                                                         eps, n_samples, elbo, grad, flags, scratch);
 }
 
 }  // namespace lcf

@@ -47,6 +47,7 @@ def load(path: str = LIB_PATH):
     L.lcf_ctx_stream.restype = vp
     L.lcf_set_graph.argtypes = [vp, i]
     L.lcf_band_cost.argtypes = [vp, i, vp, vp, vp, vp, vp, i, vp, i, i, vp]
+    L.lcf_svi_elbo_grad.argtypes = [vp, i, vp, vp, vp, vp, vp, i, vp, vp, i, vp, i, vp, vp, vp]
     L.lcf_probe_peaks.argtypes = [vp, vp]
     L.lcf_probe_fp64.argtypes = [vp, vp]
     L.lcf_probe_ff.argtypes = [vp, vp]
@@ -192,6 +193,34 @@ class Context:
                                          u.ctypes.data, uf.ctypes.data, t.size, p.ctypes.data, p.shape[0],
                                          int(bool(with_prior)), out.ctypes.data), "lcf_band_cost")
         return out
+
+    def svi_elbo_grad(self, model: int, times, flux, obs_var, is_upper, upper_flux, prior_init, var_params, eps):
+        """One SVI step's ELBO estimate and its gradient (the SVI kernel's
+        adjoint) at each row of ``var_params`` = [mu, log_sigma] (n_points,
+        2 np), with the standard-normal draws ``eps`` (n_points, n_samples,
+        np).  Returns (elbo [n_points], grad [n_points, 2 np], flags
+        [n_points]), as lcf_svi_elbo_grad."""
+        npar = abi.N_PARAMS[model]
+        t = np.ascontiguousarray(times, np.float64)
+        f = np.ascontiguousarray(flux, np.float64)
+        v = np.ascontiguousarray(obs_var, np.float64)
+        u = np.ascontiguousarray(is_upper, np.uint8)
+        uf = np.ascontiguousarray(upper_flux, np.float64)
+        ini = np.ascontiguousarray(prior_init, np.float64)
+        vpar = np.ascontiguousarray(np.atleast_2d(var_params), np.float64)
+        n_points = vpar.shape[0]
+        e = np.ascontiguousarray(eps, np.float64).reshape(n_points, -1, npar)
+        if ini.size != npar or vpar.shape[1] != 2 * npar:
+            raise LcfError(f"model {model}: prior_init needs {npar} values and var_params {2 * npar} columns")
+        elbo = np.zeros(n_points)
+        grad = np.zeros((n_points, 2 * npar))
+        flags = np.zeros(n_points, np.int32)
+        self._check(self.L.lcf_svi_elbo_grad(self.h, int(model), t.ctypes.data, f.ctypes.data, v.ctypes.data,
+                                             u.ctypes.data, uf.ctypes.data, t.size, ini.ctypes.data,
+                                             vpar.ctypes.data, n_points, e.ctypes.data, e.shape[1],
+                                             elbo.ctypes.data, grad.ctypes.data, flags.ctypes.data),
+                    "lcf_svi_elbo_grad")
+        return elbo, grad, flags
 
 
 _default = None

@@ -1099,8 +1099,104 @@ struct Uncert {
     double elbo;
     int steps = 0;
 };
+// One SVI step's Monte-Carlo ELBO estimate and its gradient
+// (src/parametric.rs:2262-2393): for each of the n_samples reparameterised
+// samples theta = mu + sigma * eps (eps = eps_all[s * np + j]), the Gaussian /
+// upper-limit log-likelihood and its analytic gradient (MetzgerKN: the FD
+// gradient of :843-860 after the peak rescale, the sample skipped when the
+// rescale leaves its clamp), plus the Gaussian prior centred on `init` (the
+// fixed centre for sigma_extra); then the sample means, the entropy
+// sum(log sigma) + np/2 ln(2 pi e) and its +1 in d/d log sigma.
+// vp = [mu (np), log sigma (np)].  Returns bit 0 when an upper-limit CDF hit
+// its 1e-300 floor (the gradient is then ~1e285), bit 1 when a MetzgerKN
+// sample was skipped.
+static int svi_step_terms(int m, const Band& b, const std::vector<double>& init, const std::vector<double>& pc,
+                          const std::vector<double>& pw, const double* vp, const double* eps_all, int n_samples,
+                          double* gmu, double* gls, double* elbo) {
+    int np = N_PARAMS[m], n = b.n(), se = SE_IDX[m];
+    int flags = 0;
+    std::vector<double> th(np), sg(np), preds(n), gb(np), dll(np);
+    std::vector<double> kn;
+    if (m == METZGER) kn.resize((size_t)n * np);
+    for (int j = 0; j < np; j++) sg[j] = std::exp(vp[np + j]);
+    for (int j = 0; j < np; j++) { gmu[j] = 0.0; gls[j] = 0.0; }
+    double elbo_sum = 0.0;
+    for (int smp = 0; smp < n_samples; smp++) {
+        const double* eps = eps_all + (size_t)smp * np;
+        for (int j = 0; j < np; j++) th[j] = vp[j] + sg[j] * eps[j];
+        double sx = std::exp(th[se]);
+        double sx2 = sx * sx;
+        if (m == METZGER) {
+            metzger_batch(th.data(), b.t.data(), n, preds.data());
+            metzger_grad_batch(th.data(), b.t.data(), n, kn.data());
+            double mx = -INF;
+            for (int i = 0; i < n; i++) if (!b.up[i]) mx = std::fmax(mx, preds[i]);
+            if (mx > 1e-10 && std::isfinite(mx)) {
+                double raw = 1.0 / mx;
+                double scl = std::min(std::max(raw, 0.1), 10.0);
+                if (std::fabs(raw - scl) / raw > 0.5) { flags |= 2; continue; }
+                for (int i = 0; i < n; i++) preds[i] *= scl;
+                for (auto& g : kn) g *= scl;
+            }
+        } else {
+            for (int i = 0; i < n; i++) preds[i] = eval_model(m, th.data(), b.t[i]);
+        }
+        double ll = 0.0;
+        for (int j = 0; j < np; j++) dll[j] = 0.0;
+        for (int i = 0; i < n; i++) {
+            double pr = preds[i];
+            if (!std::isfinite(pr)) continue;
+            double tv = b.var[i] + sx2;
+            double st = std::sqrt(tv);
+            if (m == METZGER) {
+                for (int j = 0; j < np; j++) gb[j] = kn[(size_t)i * np + j];
+            } else {
+                eval_grad(m, th.data(), b.t[i], gb.data());
+            }
+            if (b.up[i]) {
+                double z = (b.uf[i] - pr) / st;
+                ll += log_normal_cdf(z);
+                double phi = std::exp(-0.5 * z * z) / std::sqrt(2.0 * PI);
+                double raw_cdf = 0.5 * (1.0 + erf_approx(z * 0.70710678118654752440));
+                if (!(raw_cdf > 1e-300)) flags |= 1;
+                double cdf = std::fmax(raw_cdf, 1e-300);
+                double dpred = -phi / (cdf * st);
+                for (int j = 0; j < np; j++) if (j != se && std::isfinite(gb[j])) dll[j] += dpred * gb[j];
+                double dz = -(b.uf[i] - pr) * sx2 / (st * tv);
+                dll[se] += (phi / cdf) * dz;
+            } else {
+                double res = b.f[i] - pr;
+                double it = 1.0 / tv;
+                double r2 = res * res;
+                ll += -0.5 * (r2 * it + std::log(2.0 * PI * tv));
+                for (int j = 0; j < np; j++) if (j != se && std::isfinite(gb[j])) dll[j] += res * it * gb[j];
+                dll[se] += (r2 * it * it - it) * sx2;
+            }
+        }
+        double lp = 0.0;
+        for (int j = 0; j < np; j++) {
+            double center = j == se ? pc[j] : init[j];
+            double var = pw[j] * pw[j];
+            double dd = th[j] - center;
+            lp += -0.5 * dd * dd / var;
+            double dlp = -dd / var;
+            double df = dll[j] + dlp;
+            gmu[j] += df;
+            gls[j] += df * sg[j] * eps[j];
+        }
+        elbo_sum += ll + lp;
+    }
+    double ns = (double)n_samples;
+    for (int j = 0; j < np; j++) { gmu[j] /= ns; gls[j] = gls[j] / ns + 1.0; }
+    double ent = 0.0;
+    for (int j = 0; j < np; j++) ent += vp[np + j];
+    ent += 0.5 * (double)np * std::log(2.0 * PI * 2.71828182845904523536);
+    *elbo = elbo_sum / ns + ent;
+    return flags;
+}
+
 static Uncert svi_fit(int m, const Band& b, int n_steps, int n_samples, double lr, const std::vector<double>& init) {
-    int np = N_PARAMS[m], nv = 2 * np, n = b.n(), se = SE_IDX[m];
+    int np = N_PARAMS[m], nv = 2 * np;
     std::vector<double> vp(nv);
     for (int i = 0; i < np; i++) { vp[i] = init[i]; vp[np + i] = -1.0; }
     std::vector<double> am(nv, 0.0), av(nv, 0.0);
@@ -1109,9 +1205,7 @@ static Uncert svi_fit(int m, const Band& b, int n_steps, int n_samples, double l
     SmallRng rng(42);
     std::vector<double> pc, pw;
     prior_params(m, pc, pw);
-    std::vector<double> eps(np), th(np), sg(np), preds(n), gb(np), gmu(np), gls(np), dll(np), neg(nv);
-    std::vector<double> kn;
-    if (m == METZGER) kn.resize((size_t)n * np);
+    std::vector<double> eps((size_t)n_samples * np), gmu(np), gls(np), neg(nv);
     double final_elbo = -INF;
     const int stall_iters = 50, min_iters = 200;
     const double ema_alpha = 0.1;
@@ -1119,84 +1213,16 @@ static Uncert svi_fit(int m, const Band& b, int n_steps, int n_samples, double l
     int no_imp = 0, steps_run = 0;
     for (int step = 0; step < n_steps; step++) {
         steps_run = step + 1;
-        for (int j = 0; j < np; j++) sg[j] = std::exp(vp[np + j]);
-        for (int j = 0; j < np; j++) { gmu[j] = 0.0; gls[j] = 0.0; }
-        double elbo_sum = 0.0;
-        for (int smp = 0; smp < n_samples; smp++) {
+        // Box-Muller draws in the reference's order: per sample, per parameter
+        // (u1, u2); a skipped MetzgerKN sample has drawn its own already
+        for (int smp = 0; smp < n_samples; smp++)
             for (int j = 0; j < np; j++) {
                 double u1 = std::fmax(rng.f64(), 1e-10);
                 double u2 = rng.f64();
-                eps[j] = std::sqrt(-2.0 * std::log(u1)) * std::cos(2.0 * PI * u2);
-                th[j] = vp[j] + sg[j] * eps[j];
+                eps[(size_t)smp * np + j] = std::sqrt(-2.0 * std::log(u1)) * std::cos(2.0 * PI * u2);
             }
-            double sx = std::exp(th[se]);
-            double sx2 = sx * sx;
-            if (m == METZGER) {
-                metzger_batch(th.data(), b.t.data(), n, preds.data());
-                metzger_grad_batch(th.data(), b.t.data(), n, kn.data());
-                double mx = -INF;
-                for (int i = 0; i < n; i++) if (!b.up[i]) mx = std::fmax(mx, preds[i]);
-                if (mx > 1e-10 && std::isfinite(mx)) {
-                    double raw = 1.0 / mx;
-                    double scl = std::min(std::max(raw, 0.1), 10.0);
-                    if (std::fabs(raw - scl) / raw > 0.5) continue;
-                    for (int i = 0; i < n; i++) preds[i] *= scl;
-                    for (auto& g : kn) g *= scl;
-                }
-            } else {
-                for (int i = 0; i < n; i++) preds[i] = eval_model(m, th.data(), b.t[i]);
-            }
-            double ll = 0.0;
-            for (int j = 0; j < np; j++) dll[j] = 0.0;
-            for (int i = 0; i < n; i++) {
-                double pr = preds[i];
-                if (!std::isfinite(pr)) continue;
-                double tv = b.var[i] + sx2;
-                double st = std::sqrt(tv);
-                if (m == METZGER) {
-                    for (int j = 0; j < np; j++) gb[j] = kn[(size_t)i * np + j];
-                } else {
-                    eval_grad(m, th.data(), b.t[i], gb.data());
-                }
-                if (b.up[i]) {
-                    double z = (b.uf[i] - pr) / st;
-                    ll += log_normal_cdf(z);
-                    double phi = std::exp(-0.5 * z * z) / std::sqrt(2.0 * PI);
-                    double cdf = std::fmax(0.5 * (1.0 + erf_approx(z * 0.70710678118654752440)), 1e-300);
-                    double dpred = -phi / (cdf * st);
-                    for (int j = 0; j < np; j++) if (j != se && std::isfinite(gb[j])) dll[j] += dpred * gb[j];
-                    double dz = -(b.uf[i] - pr) * sx2 / (st * tv);
-                    dll[se] += (phi / cdf) * dz;
-                } else {
-                    double res = b.f[i] - pr;
-                    double it = 1.0 / tv;
-                    double r2 = res * res;
-                    ll += -0.5 * (r2 * it + std::log(2.0 * PI * tv));
-                    for (int j = 0; j < np; j++) if (j != se && std::isfinite(gb[j])) dll[j] += res * it * gb[j];
-                    dll[se] += (r2 * it * it - it) * sx2;
-                }
-            }
-            double lp = 0.0;
-            for (int j = 0; j < np; j++) {
-                double center = j == se ? pc[j] : init[j];
-                double var = pw[j] * pw[j];
-                double dd = th[j] - center;
-                lp += -0.5 * dd * dd / var;
-                double dlp = -dd / var;
-                double df = dll[j] + dlp;
-                gmu[j] += df;
-                gls[j] += df * sg[j] * eps[j];
-            }
-            elbo_sum += ll + lp;
-        }
-        double ns = (double)n_samples;
-        for (int j = 0; j < np; j++) { gmu[j] /= ns; gls[j] /= ns; }
-        elbo_sum /= ns;
-        double ent = 0.0;
-        for (int j = 0; j < np; j++) ent += vp[np + j];
-        ent += 0.5 * (double)np * std::log(2.0 * PI * 2.71828182845904523536);
-        final_elbo = elbo_sum + ent;
-        for (int j = 0; j < np; j++) { neg[j] = -gmu[j]; neg[np + j] = -(gls[j] + 1.0); }
+        svi_step_terms(m, b, init, pc, pw, vp.data(), eps.data(), n_samples, gmu.data(), gls.data(), &final_elbo);
+        for (int j = 0; j < np; j++) { neg[j] = -gmu[j]; neg[np + j] = -gls[j]; }
         at++;
         double bc1 = 1.0 - std::pow(b1, (double)at), bc2 = 1.0 - std::pow(b2, (double)at);
         for (int i = 0; i < nv; i++) {
@@ -2018,6 +2044,20 @@ int orc_svi_fit(int m, const double* t, const double* f, const double* var, cons
     for (int j = 0; j < N_PARAMS[m]; j++) { mu[j] = u.mu[j]; log_sigma[j] = u.log_sigma[j]; }
     *elbo = u.elbo;
     return u.steps;
+}
+// One SVI step's ELBO estimate and gradient at given variational parameters
+// vp = [mu, log sigma] with caller-given standard-normal draws eps
+// [n_samples * np]; grad = [d/d mu, d/d log sigma].  Returns the flags of
+// svi_step_terms, or -1 for a bad model.
+int orc_svi_elbo_grad(int m, const double* t, const double* f, const double* var, const uint8_t* up,
+                      const double* uf, int n, const double* init, const double* vp, const double* eps,
+                      int n_samples, double* elbo, double* grad) {
+    if (m < 0 || m > 7 || n_samples < 1) return -1;
+    Band b = make_band(t, f, var, up, uf, n);
+    int np = N_PARAMS[m];
+    std::vector<double> ini(init, init + np), pc, pw;
+    prior_params(m, pc, pw);
+    return svi_step_terms(m, b, ini, pc, pw, vp, eps, n_samples, grad, grad + np, elbo);
 }
 int orc_laplace_fit(int m, const double* t, const double* f, const double* var, const uint8_t* up, const double* uf,
                     int n, const double* map, double* log_sigma, double* elbo) {

@@ -63,6 +63,7 @@ def lib():
         L.orc_lbfgs_refine.restype = d
         L.orc_svi_fit.argtypes = [i, vp, vp, vp, vp, vp, i, vp, i, i, d, vp, vp, vp]
         L.orc_laplace_fit.argtypes = [i, vp, vp, vp, vp, vp, i, vp, vp, vp]
+        L.orc_svi_elbo_grad.argtypes = [i, vp, vp, vp, vp, vp, i, vp, vp, vp, i, vp, vp]
         L.orc_fit_batch.argtypes = [C.POINTER(abi.BandsCSR), C.POINTER(abi.FitOptions), C.POINTER(abi.FitOutputs), i]
         L.orc_laplace_refine.argtypes = [i, vp, vp, vp, i, vp, vp, vp, vp]
         L.orc_svi_refine.argtypes = [i, vp, vp, vp, i, vp, vp, vp, vp]
@@ -160,6 +161,23 @@ def svi_fit(model: int, band: Band, init, n_steps=1000, n_samples=4, lr=0.01):
     mu, ls, elbo = np.zeros(npar), np.zeros(npar), np.zeros(1)
     steps = lib().orc_svi_fit(model, *band.args(), _p(ini), n_steps, n_samples, lr, _p(mu), _p(ls), _p(elbo))
     return mu, ls, float(elbo[0]), steps
+
+
+def svi_elbo_grad(model: int, band: Band, init, vparams, eps):
+    """One SVI step's ELBO estimate and its gradient (d/d mu, d/d log sigma)
+    at vparams = [mu, log sigma] with the standard-normal draws eps
+    [n_samples, n_params]; the prior is centred on init.  Returns
+    (elbo, grad, flags): flags bit 0 = an upper-limit CDF hit its floor,
+    bit 1 = a MetzgerKN sample was skipped."""
+    npar = abi.N_PARAMS[model]
+    ini = np.ascontiguousarray(init, np.float64)
+    v = np.ascontiguousarray(vparams, np.float64)
+    e = np.ascontiguousarray(eps, np.float64).reshape(-1, npar)
+    assert ini.size == npar and v.size == 2 * npar
+    elbo, grad = np.zeros(1), np.zeros(2 * npar)
+    flags = lib().orc_svi_elbo_grad(model, *band.args(), _p(ini), _p(v), _p(e), e.shape[0], _p(elbo), _p(grad))
+    assert flags >= 0
+    return float(elbo[0]), grad, int(flags)
 
 
 def laplace_refine(model: int, times, flux, flux_err, params):

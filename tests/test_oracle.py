@@ -216,3 +216,61 @@ def test_oracle_multiband_villar_produces_results(oracle):
     # without the dispatch the same source takes the per-band path
     r2 = oracle.fit_batch(batch, fit_all_models=False, method=abi.METHOD_LAPLACE, run_multi_bazin=False)
     assert np.isnan(r2.per_model_chi2[:, 1]).all() or (r2.model != 1).any()
+
+
+@pytest.mark.parametrize("m", range(7))
+def test_svi_step_gradient_is_the_elbo_derivative_on_detections(oracle, m):
+    """The reference's SVI gradient (src/parametric.rs:2330-2393, restated)
+    equals FP64 central differences of its own ELBO estimate when every
+    observation is a detection (at upper limits the reference divides the
+    exact pdf by the approximate CDF, so it is not the exact derivative)."""
+    from lightcurve_fitting_gb300 import abi, synth
+    batch = synth.config_gradient(2, seed=3)
+    t, f, e = batch.bands_of(0)[0]
+    band = oracle.Band(t, f, e)
+    band.up = np.zeros_like(band.up)
+    rng = np.random.default_rng(50 + m)
+    lo, hi = [np.array(v) for v in _bounds(m)]
+    npar = lo.size
+    checked = 0
+    for _ in range(6):
+        mu = rng.uniform(lo, hi)
+        mu[abi.T0_IDX[m]] = rng.uniform(t.min() - 10, t.max())
+        vp = np.concatenate([mu, rng.uniform(-4.0, -1.5, npar)])
+        init = mu + 0.1 * rng.standard_normal(npar)
+        eps = rng.standard_normal((8, npar))
+        _, g, flags = oracle.svi_elbo_grad(m, band, init, vp, eps)
+        assert flags == 0
+        fd = np.zeros_like(g)
+        for j in range(vp.size):
+            a, b = vp.copy(), vp.copy()
+            a[j] += 1e-6
+            b[j] -= 1e-6
+            fd[j] = (oracle.svi_elbo_grad(m, band, init, a, eps)[0] - oracle.svi_elbo_grad(m, band, init, b, eps)[0]) / 2e-6
+        assert np.max(np.abs(g - fd)) <= 1e-5 * max(np.max(np.abs(fd)), 1.0), (m, g, fd)
+        checked += 1
+    assert checked == 6
+
+
+def test_svi_fit_uses_the_step_gradient(oracle):
+    """One SVI step from the initial point moves mu by lr * sign(gradient)
+    (Adam's first step), with the step gradient taken at the reference's own
+    first Box-Muller draws (SmallRng seed 42)."""
+    from lightcurve_fitting_gb300 import abi, synth
+    batch = synth.config_gradient(2, seed=3)
+    t, f, e = batch.bands_of(0)[0]
+    band = oracle.Band(t, f, e)
+    m = 0
+    npar = abi.N_PARAMS[m]
+    init = np.array([0.0, 0.0, float(t[np.argmax(f)]), 1.0, 3.0, -3.0])
+    u = oracle.rng_f64(42, 2 * 4 * npar).reshape(4, npar, 2)
+    eps = np.sqrt(-2.0 * np.log(np.maximum(u[..., 0], 1e-10))) * np.cos(2.0 * np.pi * u[..., 1])
+    vp0 = np.concatenate([init, np.full(npar, -1.0)])
+    _, g, _ = oracle.svi_elbo_grad(m, band, init, vp0, eps)
+    mu, ls, _, steps = oracle.svi_fit(m, band, init, n_steps=1, n_samples=4)
+    assert steps == 1
+    moved = np.concatenate([mu, ls - np.log(4.0)]) - vp0
+    # Adam's first step is lr * g / (|g| + eps) per component, toward ascent
+    expect = 0.01 * g / (np.abs(g) + 1e-8)
+    expect[npar:] = np.clip(vp0[npar:] + expect[npar:], -6.0, 2.0) - vp0[npar:]
+    np.testing.assert_allclose(moved, expect, rtol=1e-9, atol=1e-12)
