@@ -21,7 +21,9 @@ One JSON line on rank 0:
             particle, FP64, global-memory observations, one launch per model
             per stage, no graph) on the same 10,000 sources, and the fused
             pipeline's ratio to it — over the whole fused pipeline and over
-            the stages the plain form runs (PSO, L-BFGS, selection, SVI).
+            the stages the plain form runs (PSO, L-BFGS, selection, SVI);
+  full_scale  sources/s on 100,000 sources (counts clipped at 1,000, 15 M
+            observations) in one call, device-resident, one timed step.
 
 ``--impl reference`` times that CPU path alone (rank 0) on the same workload.
 Under torchrun each rank fits its own 10,000 sources (weak scaling, no
@@ -72,6 +74,8 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true", help="skip the host entry-point measurement (profiling runs)")
     ap.add_argument("--plain-steps", type=int, default=1, help="timed steps of the plain FP64 GPU form (0: skip)")
+    ap.add_argument("--scale-sources", type=int, default=100_000,
+                    help="sources of the full-scale leg (counts clipped at 1000; 0: skip)")
     ap.add_argument("--joint-sources", type=int, default=2000,
                     help="sources of the fit_parametric multi-band (joint Villar) measurement (0: skip)")
     return ap.parse_args()
@@ -275,6 +279,7 @@ def run_fused(args, ws, rank, local):
     if args.plain_steps > 0:
         plain = run_plain(args, batch, ptrs, dev, flush, stage, ws)
     joint = run_joint(args, batch, dev, flush, ws) if args.joint_sources > 0 else None
+    scale = run_scale(args, dev, flush, ws, rank) if args.scale_sources > 0 else None
     if rank != 0:
         ctx.close()
         return
@@ -359,6 +364,7 @@ def run_fused(args, ws, rank, local):
         "cpu_baseline": cpu,
         "plain_gpu": plain,
         "fit_parametric_multiband": joint,
+        "full_scale": scale,
         "clocks": ck,
         "gpu_launches": int(s0["kernel_launches"]) * args.steps,
         "peaks": {**peaks, "fp64_tflops": peaks64["fp64_tflops"]},
@@ -448,6 +454,45 @@ def run_joint(args, batch, dev, flush, ws):
                       "1500 iterations, stall 60, 3 seeds), per-band SVI, refinements, MultiBazin",
             "stage_ms": {"ms_joint": st["ms_joint"], "ms_uncertainty": st["ms_uncertainty"],
                          "ms_refine": st["ms_refine"], "ms_multi_bazin": st["ms_multi_bazin"]}}
+
+
+def run_scale(args, dev, flush, ws, rank):
+    """The full-scale workload: `scale_sources` sources x 3 bands, counts
+    round(lognormal(ln 40, 0.9)) clipped to [5, 1000], the five generators,
+    PSO + SVI with MultiBazin in one lcf_fit_parametric_device call (one
+    graph), device-resident inputs, one warm-up and one timed step.  Each
+    rank fits its own shard (seed 5 + rank)."""
+    import torch
+    from lightcurve_fitting_gb300 import abi, synth
+    from lightcurve_fitting_gb300.lib import Context
+    batch = synth.config_scale(args.scale_sources, seed=5 + rank)
+    keep = {k: torch.from_numpy(getattr(batch, k)).to(dev) for k in
+            ["times", "flux", "flux_err", "band_obs_offsets", "source_band_offsets"]}
+    ptrs = {k: v.data_ptr() for k, v in keep.items()}
+    sctx = Context(dev.index)
+    sstream = torch.cuda.ExternalStream(sctx.stream, device=dev)
+
+    def fit():
+        sctx.fit_device(ptrs, batch.n_sources, batch.n_bands, fit_all_models=True, method=abi.METHOD_SVI)
+
+    fit()
+    torch.cuda.synchronize()
+    flush.fill_(1.0)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(sstream)
+    fit()
+    e1.record(sstream)
+    torch.cuda.synchronize()
+    st = sctx.stats()
+    sctx.close()
+    ms = dist_max(float(e0.elapsed_time(e1)), ws, dev)
+    return {"value": job_value(batch.n_sources, ws, ms), "unit": "sources/s", "ms_per_step": ms,
+            "sources_per_gpu": batch.n_sources, "n_obs_per_gpu": batch.n_obs, "steps": 1, "warmup": 1,
+            "config": "scale: counts round(lognormal(ln 40, 0.9)) clipped [5, 1000], five generators, "
+                      "fit_all_models=true, SVI, MultiBazin, one graph",
+            "stage_ms": {k: st[k] for k in ["ms_total", "ms_pso", "ms_lbfgs", "ms_t0_search", "ms_uncertainty",
+                                            "ms_refine", "ms_multi_bazin"]}}
 
 
 def main():

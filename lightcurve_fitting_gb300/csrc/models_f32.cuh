@@ -305,9 +305,14 @@ struct Nll {
     // at 1/64 of the FP32 rate, and two divisions per evaluation would cost as
     // much as the observation loop), with the reference's special values
     __device__ __forceinline__ double finish(double prior, double inv_n) const {
+        return finish_sum((double)s - (double)c, big, nonfinite, inf, prior, inv_n);
+    }
+    // the same from a sum of compensated partial sums (the swarm's lane-split
+    // evaluation)
+    __device__ __forceinline__ static double finish_sum(double tot, float big, int nonfinite, int inf, double prior,
+                                                        double inv_n) {
         if (nonfinite) return BIG_COST;
         if (inf) return INFINITY;
-        double tot = (double)s - (double)c;
         if (big > -INFINITY) {
             if (big > LN_DBL_MAX) return INFINITY;
             tot += exp((double)big);

@@ -320,7 +320,19 @@ __device__ __forceinline__ void run_swarm(const DeviceBatch& d, const PsoTask& t
         pb[j] = x[j];
         g[j] = 0.0f;
     }
-    double c = live ? particle_cost_k<KIND>(t, x) : INFINITY;
+    // one evaluation round over the particles of lanes start .. NP - 1
+    // (lane-split, except MetzgerKN); lane p >= start receives its own cost
+    auto eval_round = [&](int start) -> double {
+        if constexpr (KIND == METZGER) {
+            return (live && p >= start) ? particle_cost_k<KIND>(t, x) : INFINITY;
+        } else {
+            const int k = NP - start;
+            const double cs = particle_cost_split<KIND>(t, x, start, k);
+            const double co = __shfl_sync(FULL, cs, ((p - start) * split_lanes(k)) & 31);
+            return (live && p >= start) ? co : INFINITY;
+        }
+    };
+    double c = eval_round(0);
     int evals = 1;
     double pbc = c;
     double gc = INFINITY;
@@ -363,8 +375,13 @@ __device__ __forceinline__ void run_swarm(const DeviceBatch& d, const PsoTask& t
                         else { x[j] = nx; v[j] = vv; }
                     }
                 }
-                c = particle_cost_k<KIND>(t, x);
-                evals++;
+            }
+            {
+                const double cr = eval_round(start);
+                if (active) {
+                    c = cr;
+                    evals++;
+                }
             }
             unsigned m = __ballot_sync(FULL, active && c < gc);
             int q = m ? __ffs(m) - 1 : NP - 1;

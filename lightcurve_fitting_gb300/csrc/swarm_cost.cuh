@@ -11,6 +11,8 @@
 
 namespace lcf {
 
+constexpr unsigned FULL_MASK = 0xffffffffu;
+
 // ---------------------------------------------------------------------------
 // Particle cost (PsoCost::cost_from_slice, src/parametric.rs:1303-1370, and
 // multi_bazin_cost, :973-1004) for the particle of this lane.
@@ -24,12 +26,13 @@ struct TaskCtx {
     double inv_n;        // 1 / max(n, 1)
 };
 
+// Negative log-likelihood terms of observations i0, i0 + stride, ... < n.
 template <class M>
-__device__ __forceinline__ Nll nll_loop(const M& m, const float4* obs, int n, float se2) {
+__device__ __forceinline__ Nll nll_loop(const M& m, const float4* obs, int n, float se2, int i0 = 0, int stride = 1) {
     Nll acc;
     acc.reset();
 #pragma unroll 2
-    for (int i = 0; i < n; i++) {
+    for (int i = i0; i < n; i += stride) {
         float4 o = obs[i];
         int st = ST_OK;
         float pr = m.eval(o.x, o.y, st);
@@ -40,7 +43,8 @@ __device__ __forceinline__ Nll nll_loop(const M& m, const float4* obs, int n, fl
 
 // MultiBazin prediction: sum of K Bazin components + B (src/parametric.rs:932-940)
 template <int K>
-__device__ __forceinline__ Nll nll_multibazin(const float* p, const float4* obs, int n, float se2) {
+__device__ __forceinline__ Nll nll_multibazin(const float* p, const float4* obs, int n, float se2, int i0 = 0,
+                                              int stride = 1) {
     float la[K], t0[K], itr[K], itf[K], dif[K];
 #pragma unroll
     for (int c = 0; c < K; c++) {
@@ -53,7 +57,7 @@ __device__ __forceinline__ Nll nll_multibazin(const float* p, const float4* obs,
     float B = p[4 * K];
     Nll acc;
     acc.reset();
-    for (int i = 0; i < n; i++) {
+    for (int i = i0; i < n; i += stride) {
         float4 o = obs[i];
         float sum = 0.0f, bigL = -INFINITY;
         int st = ST_OK;
@@ -171,6 +175,110 @@ __device__ __forceinline__ double particle_cost_k(const TaskCtx& t, const float*
         }
         return acc.finish(prior, t.inv_n);
     }
+}
+
+// ---------------------------------------------------------------------------
+// Lane-split particle cost for the swarm's evaluation rounds.  A round
+// evaluates the k particles held by lanes base .. base + k - 1 (the
+// speculative rounds that reproduce the reference's in-loop global best
+// re-evaluate only the particles after the first improver, so k shrinks
+// within an iteration).  Each particle is evaluated by s = split_lanes(k)
+// consecutive lanes, lane u of the group taking observations u, u + s, ...;
+// the groups' compensated partial sums are combined in FP64 in lane order.
+// Every lane of group g returns particle base + g's cost.  MetzgerKN (whose
+// cost is dominated by the per-particle ODE sweep) does not use it.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ int split_lanes(int k) {
+    const int s = 32 / k;
+    return s > 8 ? 8 : s;
+}
+
+template <int KIND>
+__device__ __forceinline__ double particle_cost_split(const TaskCtx& t, const float* x, int base, int k) {
+    const int lane = threadIdx.x & 31;
+    const int s = split_lanes(k);
+    const int g = lane / s, u = lane - g * s;
+    const bool on = g < k;
+    const int src = on ? base + g : lane;
+    constexpr bool MB = KIND >= KIND_MB1;
+    constexpr int NX = MB ? 4 * (KIND - KIND_MB1 + 1) + 2 : n_params_of(KIND);
+    float xs[NX];
+#pragma unroll
+    for (int j = 0; j < NX; j++) xs[j] = __shfl_sync(FULL_MASK, x[j], src);
+    Nll acc;
+    acc.reset();
+    double prior = 0.0;
+    float villar_c = 0.0f;
+    if constexpr (MB) {
+        constexpr int K = KIND - KIND_MB1 + 1;
+        float se = expf(xs[4 * K + 1]);
+        if (on) acc = nll_multibazin<K>(xs, t.obs, t.n, se * se, u, s);
+    } else {
+        constexpr int m = KIND;
+        constexpr int np = n_params_of(m);
+        float p[MAXP];
+        if (t.flags & TASK_T0_FIXED) {
+            constexpr int t0i = t0_idx_of(m);
+#pragma unroll
+            for (int i = 0; i < np; i++) p[i] = i < t0i ? xs[i] : (i == t0i ? t.t0_fixed : xs[i - 1]);
+        } else {
+#pragma unroll
+            for (int i = 0; i < np; i++) p[i] = xs[i];
+        }
+        if constexpr (m == VILLAR) villar_c = VillarF::constraint(p);
+        if (t.flags & TASK_PRIOR) {
+            float sp = 0.0f;
+#pragma unroll
+            for (int j = 0; j < np; j++) {
+                float w = (float)c_pop_w[m][j];
+                if (w > 0.0f) {
+                    float z = (p[j] - (float)c_pop_c[m][j]) / w;
+                    sp += 0.5f * z * z;
+                }
+            }
+            prior = (double)sp;
+        }
+        float se = expf(p[se_idx_of(m)]);
+        float se2 = se * se;
+        if (on && !(villar_c > 0.0f)) {
+            if constexpr (m == BAZIN) { BazinF e; e.init(p); acc = nll_loop(e, t.obs, t.n, se2, u, s); }
+            else if constexpr (m == VILLAR) { VillarF e; e.init(p); acc = nll_loop(e, t.obs, t.n, se2, u, s); }
+            else if constexpr (m == TDE) { TdeF e; e.init(p); acc = nll_loop(e, t.obs, t.n, se2, u, s); }
+            else if constexpr (m == ARNETT) { ArnettF e; e.init(p); acc = nll_loop(e, t.obs, t.n, se2, u, s); }
+            else if constexpr (m == MAGNETAR) { MagnetarF e; e.init(p); acc = nll_loop(e, t.obs, t.n, se2, u, s); }
+            else if constexpr (m == SHOCK) { ShockF e; e.init(p); acc = nll_loop(e, t.obs, t.n, se2, u, s); }
+            else if constexpr (m == AFTERGLOW) { AfterglowF e; e.init(p); acc = nll_loop(e, t.obs, t.n, se2, u, s); }
+        }
+    }
+    double tot;
+    float big;
+    int nonfinite, inf;
+    if (s == 1) {
+        tot = (double)acc.s - (double)acc.c;
+        big = acc.big;
+        nonfinite = acc.nonfinite;
+        inf = acc.inf;
+    } else {
+        tot = 0.0;
+        big = -INFINITY;
+        nonfinite = 0;
+        inf = 0;
+        const int flags = acc.nonfinite | (acc.inf << 1);
+        for (int v = 0; v < s; v++) {
+            const int sl = (g * s + v) & 31;
+            const float ps = __shfl_sync(FULL_MASK, acc.s, sl), pc = __shfl_sync(FULL_MASK, acc.c, sl);
+            const float pb = __shfl_sync(FULL_MASK, acc.big, sl);
+            const int pf = __shfl_sync(FULL_MASK, flags, sl);
+            tot += (double)ps - (double)pc;
+            if (pb > -INFINITY) big = big > -INFINITY ? fmaxf(big, pb) + log1pf(expf(-fabsf(big - pb))) : pb;
+            nonfinite |= pf & 1;
+            inf |= pf >> 1;
+        }
+    }
+    if constexpr (!MB && KIND == VILLAR) {
+        if (villar_c > 0.0f) return 1e12 + 10000.0 * (double)villar_c;
+    }
+    return Nll::finish_sum(tot, big, nonfinite, inf, prior, t.inv_n);
 }
 
 // Runtime dispatch on the task kind (the likelihood API).
