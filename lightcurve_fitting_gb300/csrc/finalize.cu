@@ -265,12 +265,43 @@ struct MzLl {
     __device__ void operator()(int j, double l) { term(j, l * inv_peak * scale); }
 };
 
-// band_ll_w for MetzgerKN by one lane (rescale: the PSO cost's peak rescale)
-__device__ double metzger_ll_lane(const double* p, const BandView& b, const double* cst, bool rescale) {
+// Bands of at most MZ_KEEP observations keep the first sweep's interpolants
+// in shared memory (lane-interleaved: entry j of a lane at keep[32 j]) and
+// form the terms from them, in the second sweep's order, instead of
+// integrating the ODE again; longer bands sweep twice.
+constexpr int MZ_KEEP = 32;
+struct MzKeep {
+    const uint8_t* up;
+    double* keep;
+    double mx;
+    __device__ void operator()(int j, double l) {
+        if (!up[j]) mx = fmax(mx, l);
+        keep[32 * j] = l;
+    }
+};
+__device__ __forceinline__ bool metzger_first_sweep(const double* p, const BandView& b, double* keep, double& mx,
+                                                    int& j_start, double& l_peak) {
+    if (keep) {
+        MzKeep kp{b.up, keep, -INFINITY};
+        bool ok = metzger_sweep64(p, b.t, b.n, kp, j_start, l_peak);
+        mx = kp.mx;
+        return ok;
+    }
+    MzPeak pk{b.up, -INFINITY};
+    bool ok = metzger_sweep64(p, b.t, b.n, pk, j_start, l_peak);
+    mx = pk.mx;
+    return ok;
+}
+
+// band_ll_w for MetzgerKN by one lane (rescale: the PSO cost's peak rescale);
+// keep: this lane's interpolant slots (nullptr: sweep twice)
+__device__ double metzger_ll_lane(const double* p, const BandView& b, const double* cst, bool rescale,
+                                  double* keep) {
+    if (b.n > MZ_KEEP) keep = nullptr;
     MzPeak pk{b.up, -INFINITY};
     int j_start;
     double l_peak;
-    bool ok = metzger_sweep64(p, b.t, b.n, pk, j_start, l_peak);
+    bool ok = metzger_first_sweep(p, b, keep, pk.mx, j_start, l_peak);
     bool valid = ok && l_peak > 0.0 && isfinite(l_peak);
     double scale = 1.0;
     if (rescale) {
@@ -287,26 +318,31 @@ __device__ double metzger_ll_lane(const double* p, const BandView& b, const doub
     int z_end = valid ? j_start : b.n;
     for (int j = 0; j < z_end; j++) acc.term(j, 0.0 * scale);
     if (valid) {
-        // second sweep: the same interpolants, normalised
-        int js;
-        double lp;
+        // the same interpolants, normalised
         struct Norm {
             MzLl* a;
             double lpk;
             __device__ void operator()(int j, double l) { a->term(j, l / lpk * a->scale); }
         } nv{&acc, l_peak};
-        metzger_sweep64(p, b.t, b.n, nv, js, lp);
+        if (keep) {
+            for (int j = j_start; j < b.n; j++) nv(j, keep[32 * j]);
+        } else {
+            int js;
+            double lp;
+            metzger_sweep64(p, b.t, b.n, nv, js, lp);
+        }
     }
     return acc.ll;
 }
 
 // shape sums of profile_t0_refine for MetzgerKN by one lane: sw, sy, sf,
 // syf, sff over detections of the normalised prediction
-__device__ void metzger_shape_lane(const double* p, const BandView& b, const double* cst, double* s5) {
-    MzPeak pk{b.up, -INFINITY};
+__device__ void metzger_shape_lane(const double* p, const BandView& b, const double* cst, double* s5, double* keep) {
+    if (b.n > MZ_KEEP) keep = nullptr;
+    double mx_unused;
     int j_start;
     double l_peak;
-    bool ok = metzger_sweep64(p, b.t, b.n, pk, j_start, l_peak);
+    bool ok = metzger_first_sweep(p, b, keep, mx_unused, j_start, l_peak);
     bool valid = ok && l_peak > 0.0 && isfinite(l_peak);
     double sw = 0, sy = 0, sf = 0, syf = 0, sff = 0;
     int z_end = valid ? j_start : b.n;
@@ -328,9 +364,13 @@ __device__ void metzger_shape_lane(const double* p, const BandView& b, const dou
                 sw += w; sy += w * fj; sf += w * sh; syf += w * fj * sh; sff += w * sh * sh;
             }
         } su{&b, cst, l_peak, sw, sy, sf, syf, sff};
-        int js;
-        double lp;
-        metzger_sweep64(p, b.t, b.n, su, js, lp);
+        if (keep) {
+            for (int j = j_start; j < b.n; j++) su(j, keep[32 * j]);
+        } else {
+            int js;
+            double lp;
+            metzger_sweep64(p, b.t, b.n, su, js, lp);
+        }
         sw = su.sw; sy = su.sy; sf = su.sf; syf = su.syf; sff = su.sff;
     }
     s5[0] = sw; s5[1] = sy; s5[2] = sf; s5[3] = syf; s5[4] = sff;
@@ -339,7 +379,8 @@ __device__ void metzger_shape_lane(const double* p, const BandView& b, const dou
 // profile_t0_refine + profile_refine_all for a MetzgerKN band (np = 5,
 // t0 = p[3], sigma_extra = p[4]; no baseline parameter), lanes over scan
 // points; the sequential decisions run uniformly on the gathered values.
-__device__ void refine_metzger(const BandStats& bs, const BandView& b, const double* cst, double* mu, double* ls) {
+__device__ void refine_metzger(const BandStats& bs, const BandView& b, const double* cst, double* mu, double* ls,
+                               double* keep) {
     const int lane = threadIdx.x & 31;
     constexpr int m = METZGER, np = 5, se = 4, t0i = 3, NG = 25;
     double t0_lo = bs.t_first - 30.0, t0_hi = bs.t_peak_all + 5.0;
@@ -354,11 +395,11 @@ __device__ void refine_metzger(const BandStats& bs, const BandView& b, const dou
             double saved_la = p[0];
             p[0] = 0.0;
             double s5[5];
-            metzger_shape_lane(p, b, cst, s5);
+            metzger_shape_lane(p, b, cst, s5, keep);
             double syf = s5[3], sff = s5[4];
             if (sff > 1e-20 && syf / sff > 1e-10) p[0] = log(syf / sff);
             else p[0] = saved_la;
-            my_ll = metzger_ll_lane(p, b, cst, true);
+            my_ll = metzger_ll_lane(p, b, cst, true, keep);
         }
         double best_t0 = mu[t0i], best_ll = -INFINITY;
         for (int gi = 0; gi < NG; gi++) {
@@ -371,7 +412,7 @@ __device__ void refine_metzger(const BandStats& bs, const BandView& b, const dou
             double p[MAXP];
             for (int j = 0; j < np; j++) p[j] = mu[j];
             p[t0i] = grid(lane);
-            e_ll = metzger_ll_lane(p, b, cst, false);
+            e_ll = metzger_ll_lane(p, b, cst, false, keep);
         }
         double lo1 = best_t0, hi1 = best_t0, thr = best_ll - 0.5;
         for (int gi = NG - 1; gi >= 0; gi--) {
@@ -406,7 +447,7 @@ __device__ void refine_metzger(const BandStats& bs, const BandView& b, const dou
                 double slo = c_lo[m][j], shi = c_hi[m][j];
                 p[j] = slo + (shi - slo) * (double)gi / 14.0;
             }
-            r_ll[round] = metzger_ll_lane(p, b, cst, false);
+            r_ll[round] = metzger_ll_lane(p, b, cst, false, keep);
         }
     }
     auto get = [&](int e) {
@@ -533,6 +574,9 @@ void launch_laplace(const DeviceBatch& d, cudaStream_t s) {
 }
 
 // profile_t0_refine + profile_refine_all + mag chi2
+#ifndef LCF_REFINE_BLOCK
+#define LCF_REFINE_BLOCK 128
+#endif
 __global__ void refine_kernel(DeviceBatch d) {
     int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     int lane = threadIdx.x & 31;
@@ -550,7 +594,10 @@ __global__ void refine_kernel(DeviceBatch d) {
     const bool fast = m != METZGER;
     const float4* obs = d.obs + bs.off;
     scan_constants(b, exp(2.0 * mu[se]), scr);
-    if (!fast) refine_metzger(bs, b, scr, mu, ls);
+    if (!fast) {
+        extern __shared__ double rf_keep[];
+        refine_metzger(bs, b, scr, mu, ls, rf_keep + (size_t)(threadIdx.x >> 5) * 32 * MZ_KEEP + lane);
+    }
     auto scan_ll = [&](const double* p, bool rescale) {
         return fast ? band_ll_fast(m, p, obs, b, scr) : band_ll_w(m, b, p, scr, rescale);
     };
@@ -693,7 +740,8 @@ __global__ void refine_kernel(DeviceBatch d) {
 void launch_refine(const DeviceBatch& d, cudaStream_t s) {
     if (d.n_bands == 0) return;
     int64_t threads = (int64_t)d.n_bands * 32;
-    refine_kernel<<<(int)((threads + 127) / 128), 128, 0, s>>>(d);
+    const size_t smem = (size_t)(LCF_REFINE_BLOCK / 32) * 32 * MZ_KEEP * sizeof(double);
+    refine_kernel<<<(int)((threads + LCF_REFINE_BLOCK - 1) / LCF_REFINE_BLOCK), LCF_REFINE_BLOCK, smem, s>>>(d);
 }
 
 // ---------------------------------------------------------------------------

@@ -303,7 +303,10 @@ __device__ void polish_band(const DeviceBatch& d, int b) {
 #ifndef LCF_LB_MINB
 #define LCF_LB_MINB 8
 #endif
-__global__ void __launch_bounds__(128, LCF_LB_MINB) lbfgs_kernel(DeviceBatch d, int model_mask) {
+#ifndef LCF_LB_BLOCK
+#define LCF_LB_BLOCK 128
+#endif
+__global__ void __launch_bounds__(LCF_LB_BLOCK, LCF_LB_MINB) lbfgs_kernel(DeviceBatch d, int model_mask) {
     const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     if (warp >= d.n_bands * 8) return;
     const int m = warp / d.n_bands, b = warp - m * d.n_bands;
@@ -322,7 +325,7 @@ __global__ void __launch_bounds__(128, LCF_LB_MINB) lbfgs_kernel(DeviceBatch d, 
 
 void launch_lbfgs(const DeviceBatch& d, int model_mask, cudaStream_t s) {
     if (d.n_bands == 0) return;
-    int block = 128;
+    int block = LCF_LB_BLOCK;
     int64_t threads = (int64_t)d.n_bands * 8 * 32;
     lbfgs_kernel<<<(int)((threads + block - 1) / block), block, 0, s>>>(d, model_mask);
 }
@@ -929,7 +932,10 @@ __device__ void svi_band(const DeviceBatch& d, int b) {
 // One warp per (band, model), model-major (the warps of a model run
 // together and share its code); a warp whose band selected another model
 // returns at once.
-__global__ void __launch_bounds__(128) svi_kernel(DeviceBatch d) {
+#ifndef LCF_SVI_BLOCK
+#define LCF_SVI_BLOCK 128
+#endif
+__global__ void __launch_bounds__(LCF_SVI_BLOCK) svi_kernel(DeviceBatch d) {
     const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     if (warp >= d.n_bands * 8) return;
     const int m = warp / d.n_bands, b = warp - m * d.n_bands;
@@ -947,7 +953,7 @@ __global__ void __launch_bounds__(128) svi_kernel(DeviceBatch d) {
 
 void launch_svi(const DeviceBatch& d, cudaStream_t s) {
     if (d.n_bands == 0) return;
-    int block = 128;
+    int block = LCF_SVI_BLOCK;
     int64_t threads = (int64_t)d.n_bands * 8 * 32;
     svi_kernel<<<(int)((threads + block - 1) / block), block, 0, s>>>(d);
 }
