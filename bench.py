@@ -275,11 +275,15 @@ def run_fused(args, ws, rank, local):
                "h2d_bytes_per_step": int(st_e2e["h2d_bytes"]), "d2h_bytes_per_step": int(st_e2e["d2h_bytes"])}
     else:
         e2e = None
+    # the launch autotuner explored its candidates during the warm-up fits of
+    # this workload's shape bucket; the other legs pin the candidate it chose
+    tune_table = ctx.autotune_table()
+    tuned = ctx.last_launch()
     plain = None
     if args.plain_steps > 0:
         plain = run_plain(args, batch, ptrs, dev, flush, stage, ws)
-    joint = run_joint(args, batch, dev, flush, ws) if args.joint_sources > 0 else None
-    scale = run_scale(args, dev, flush, ws, rank) if args.scale_sources > 0 else None
+    joint = run_joint(args, batch, dev, flush, ws, tuned["candidate"]) if args.joint_sources > 0 else None
+    scale = run_scale(args, dev, flush, ws, rank, tuned["candidate"]) if args.scale_sources > 0 else None
     if rank != 0:
         ctx.close()
         return
@@ -365,6 +369,10 @@ def run_fused(args, ws, rank, local):
         "plain_gpu": plain,
         "fit_parametric_multiband": joint,
         "full_scale": scale,
+        "autotune": {"candidates_block_staging_blocks_per_sm": ctx.autotune_candidates().tolist(),
+                     "chosen": tuned,
+                     "table_bucket_best_next_ms": tune_table.tolist(),
+                     "note": "explored during the warm-up fits; bit-identical results under every candidate"},
         "clocks": ck,
         "gpu_launches": int(s0["kernel_launches"]) * args.steps,
         "peaks": {**peaks, "fp64_tflops": peaks64["fp64_tflops"]},
@@ -414,7 +422,7 @@ def run_plain(args, batch, ptrs, dev, flush, fused_stats, ws):
     }
 
 
-def run_joint(args, batch, dev, flush, ws):
+def run_joint(args, batch, dev, flush, ws, candidate):
     """fit_parametric with fit_all_models = false (the reference's default):
     every source of this workload has 3 non-empty bands, so all take the
     joint multi-band Villar branch (SVI, MultiBazin), on the first
@@ -427,6 +435,7 @@ def run_joint(args, batch, dev, flush, ws):
             ["times", "flux", "flux_err", "band_obs_offsets", "source_band_offsets"]}
     ptrs = {k: v.data_ptr() for k, v in keep.items()}
     jctx = Context(dev.index)
+    jctx.set_autotune(1, candidate)
     jstream = torch.cuda.ExternalStream(jctx.stream, device=dev)
 
     def fit():
@@ -456,7 +465,7 @@ def run_joint(args, batch, dev, flush, ws):
                          "ms_refine": st["ms_refine"], "ms_multi_bazin": st["ms_multi_bazin"]}}
 
 
-def run_scale(args, dev, flush, ws, rank):
+def run_scale(args, dev, flush, ws, rank, candidate):
     """The full-scale workload: `scale_sources` sources x 3 bands, counts
     round(lognormal(ln 40, 0.9)) clipped to [5, 1000], the five generators,
     PSO + SVI with MultiBazin in one lcf_fit_parametric_device call (one
@@ -470,6 +479,7 @@ def run_scale(args, dev, flush, ws, rank):
             ["times", "flux", "flux_err", "band_obs_offsets", "source_band_offsets"]}
     ptrs = {k: v.data_ptr() for k, v in keep.items()}
     sctx = Context(dev.index)
+    sctx.set_autotune(1, candidate)
     sstream = torch.cuda.ExternalStream(sctx.stream, device=dev)
 
     def fit():

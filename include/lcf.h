@@ -195,6 +195,34 @@ void* lcf_ctx_stream(lcf_ctx* ctx);
  * (default 1), or launch the kernels one by one (0). */
 int lcf_set_graph(lcf_ctx* ctx, int enabled);
 
+/*
+ * Launch autotuner of the swarm kernel (no counterpart in the reference,
+ * whose CPU swarms have no launch shape).  Candidate c has a block size and
+ * a staging depth (observations a warp stages in shared memory; longer bands
+ * are read from global memory); every candidate gives bit-identical results.
+ * A context tunes online per shape bucket of the batch (ceil log2 of the
+ * band count, and of the 90th-percentile band length / 32): the first fits
+ * of a new bucket run the candidates in turn, timed by their swarm stages,
+ * and later fits of the bucket use the fastest.
+ *   lcf_set_autotune: mode 1 = online tuning (default), 0 = candidate 0;
+ *       forced_candidate >= 0 pins that candidate (-1: none).
+ *   lcf_autotune_candidates: out[3c..3c+2] = block, staging depth, resident
+ *       blocks per SM of candidate c; returns the number of candidates.
+ *   lcf_autotune_table: per bucket seen, 6 doubles (bucket, chosen candidate
+ *       or -1 while exploring, next candidate to explore, stage ms of each
+ *       candidate); returns the number of buckets (rows beyond max_rows are
+ *       not written).
+ *   lcf_autotune_load: installs rows of that form as explored buckets (the
+ *       table of an earlier context, to skip exploration).
+ *   lcf_last_launch: out = candidate, block, staging depth, bucket of the
+ *       last fused fit.
+ */
+int lcf_set_autotune(lcf_ctx* ctx, int mode, int forced_candidate);
+int lcf_autotune_candidates(const lcf_ctx* ctx, int* out9);
+int lcf_autotune_table(const lcf_ctx* ctx, double* rows, int max_rows);
+int lcf_autotune_load(lcf_ctx* ctx, const double* rows, int n_rows);
+int lcf_last_launch(const lcf_ctx* ctx, int* out4);
+
 /* Measured pipe peaks of the context's GPU: out[0] = FP32 FMA TFLOP/s,
  * out[1] = SFU (MUFU ex2) Gop/s, from dependent-chain probe kernels over a
  * full grid.  The roofline denominators of the fused kernels, which are

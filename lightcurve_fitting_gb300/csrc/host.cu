@@ -102,12 +102,48 @@ struct DevArr {
     size_t bytes = 0;
 };
 
+// ---------------------------------------------------------------------------
+// Launch autotuner.  The swarm kernel's launch shape (threads per block, and
+// with it the resident blocks per SM) and its staging depth (observations a
+// warp stages in shared memory; longer bands are read from global memory)
+// are chosen per shape bucket of the batch: log2 of the band count and of
+// the 90th-percentile band length.  A context tunes online: the first fits of
+// a new bucket run the candidates in turn, each timed by the stage events of
+// the fit (model-selection swarm + t0 search + MultiBazin), and later fits of
+// that bucket use the fastest.  The candidates change only where a warp reads
+// its band from and which warp runs which swarm, so every candidate gives
+// bit-identical results and an exploring fit is ordinary work.
+// ---------------------------------------------------------------------------
+struct TuneCand {
+    int block, smem_obs;
+};
+// (256, 512): 16 warps per SM, bands <= 512 staged (the default);
+// (256, 256): the same occupancy, a shallower stage;
+// (128, 1024): bands <= 1024 staged at 12 warps per SM (long-band batches)
+static const TuneCand TUNE_CAND[] = {{256, 512}, {256, 256}, {128, 1024}};
+constexpr int N_TUNE = 3;
+struct TuneEntry {
+    uint32_t bucket = 0;
+    int next = 0;     // next candidate to explore (N_TUNE: done)
+    int best = -1;    // chosen candidate once explored
+    double ms[N_TUNE] = {0.0, 0.0, 0.0};
+};
+
 struct lcf_ctx {
     int device = 0;
     int num_sms = 0;
     int pso_block = 256;
     int pso_blocks_per_sm = 1;
     int smem_obs = 512;
+    // autotuner state
+    int tune_mode = 1;       // 1: online tuning per shape bucket, 0: candidate 0
+    int tune_forced = -1;    // >= 0: always this candidate
+    int cand_bps[N_TUNE] = {1, 1, 1};
+    int max_pso_warps_per_sm = 1;
+    int cfg = 0;             // candidate of the current fit
+    bool exploring = false;
+    uint32_t bucket = 0;
+    std::vector<TuneEntry> tune;
     cudaStream_t stream = nullptr;
     std::string err;
     lcf_fit_stats stats{};
@@ -221,14 +257,25 @@ extern "C" int lcf_ctx_create(int device, lcf_ctx** out) {
         return LCF_E_CUDA;
     }
     for (int i = 0; i < N_EVENTS; i++) cudaEventCreate(&ctx->ev[i]);
-    int rc = pso_init_attributes(ctx->pso_block, ctx->smem_obs);
+    // the kernels accept the largest candidate's dynamic shared memory
+    int big = 0;
+    for (int c = 1; c < N_TUNE; c++)
+        if (pso_smem_bytes(TUNE_CAND[c].block, TUNE_CAND[c].smem_obs) >
+            pso_smem_bytes(TUNE_CAND[big].block, TUNE_CAND[big].smem_obs))
+            big = c;
+    int rc = pso_init_attributes(TUNE_CAND[big].block, TUNE_CAND[big].smem_obs);
     if (rc != 0) {
         lcf_ctx_destroy(ctx);
         return LCF_E_CUDA;
     }
-    // occupancy of the 7-dimension instantiation decides the persistent grid
-    int bps = pso_blocks_per_sm(ctx->pso_block, pso_smem_bytes(ctx->pso_block, ctx->smem_obs));
-    ctx->pso_blocks_per_sm = std::max(1, bps);
+    // occupancy of the 7-dimension instantiation decides each candidate's
+    // persistent grid
+    for (int c = 0; c < N_TUNE; c++) {
+        int bps = pso_blocks_per_sm(TUNE_CAND[c].block, pso_smem_bytes(TUNE_CAND[c].block, TUNE_CAND[c].smem_obs));
+        ctx->cand_bps[c] = std::max(1, bps);
+        ctx->max_pso_warps_per_sm = std::max(ctx->max_pso_warps_per_sm, ctx->cand_bps[c] * TUNE_CAND[c].block / 32);
+    }
+    ctx->pso_blocks_per_sm = ctx->cand_bps[0];
     // RNG tables
     std::vector<float> draws((size_t)3 * DRAWS_PER_SEED), eps((size_t)3 * SVI_STEPS * SVI_SAMPLES * 7);
     make_draw_tables(draws.data(), eps.data());
@@ -320,6 +367,68 @@ static double task_cost(int kind, int n) {
     return (double)n;
 }
 
+// Shape bucket of a batch: ceil(log2) of the band count, and of the
+// 90th-percentile band length over 32 (0: <= 32 ... 7: > 2048).
+static uint32_t shape_bucket(const std::vector<int64_t>& boff, int n_bands) {
+    std::vector<int64_t> n((size_t)std::max(n_bands, 1), 0);
+    for (int b = 0; b < n_bands; b++) n[b] = boff[b + 1] - boff[b];
+    size_t k = (n.size() * 9) / 10;
+    if (k >= n.size()) k = n.size() - 1;
+    std::nth_element(n.begin(), n.begin() + k, n.end());
+    int64_t p90 = n[k];
+    uint32_t lb = 0;
+    while (lb < 7 && ((int64_t)32 << lb) < p90) lb++;
+    uint32_t nb = 0;
+    while (nb < 31 && ((int64_t)1 << nb) < (int64_t)n_bands) nb++;
+    return (nb << 4) | lb;
+}
+
+// Candidate for the next fused fit: forced, the bucket's next unexplored
+// candidate, or its chosen one.
+static void choose_launch(lcf_ctx* ctx) {
+    int c = 0;
+    ctx->exploring = false;
+    if (ctx->tune_forced >= 0) {
+        c = ctx->tune_forced;
+    } else if (ctx->tune_mode) {
+        TuneEntry* e = nullptr;
+        for (auto& t : ctx->tune)
+            if (t.bucket == ctx->bucket) e = &t;
+        if (!e) {
+            ctx->tune.push_back(TuneEntry());
+            e = &ctx->tune.back();
+            e->bucket = ctx->bucket;
+        }
+        if (e->next < N_TUNE) {
+            c = e->next;
+            ctx->exploring = true;
+        } else {
+            c = e->best;
+        }
+    }
+    ctx->cfg = c;
+    ctx->pso_block = TUNE_CAND[c].block;
+    ctx->smem_obs = TUNE_CAND[c].smem_obs;
+    ctx->pso_blocks_per_sm = ctx->cand_bps[c];
+    ctx->db.smem_obs = ctx->smem_obs;
+}
+
+// After an exploring fit: the candidate's time, and the choice once all ran.
+static void record_launch(lcf_ctx* ctx) {
+    if (!ctx->exploring) return;
+    for (auto& e : ctx->tune) {
+        if (e.bucket != ctx->bucket || e.next >= N_TUNE || e.next != ctx->cfg) continue;
+        e.ms[e.next] = ctx->stats.ms_pso + ctx->stats.ms_t0_search + ctx->stats.ms_multi_bazin;
+        e.next++;
+        if (e.next == N_TUNE) {
+            e.best = 0;
+            for (int c = 1; c < N_TUNE; c++)
+                if (e.ms[c] < e.ms[e.best]) e.best = c;
+        }
+    }
+    ctx->exploring = false;
+}
+
 static int prepare_layout(lcf_ctx* ctx, int n_sources, int n_bands, int64_t n_obs, const lcf_fit_options& o) {
     uint64_t key = hash_layout(ctx->h_boff, ctx->h_soff, o);
     bool same = key == ctx->layout_key && ctx->n_bands == n_bands && ctx->n_obs == n_obs;
@@ -357,8 +466,8 @@ static int prepare_layout(lcf_ctx* ctx, int n_sources, int n_bands, int64_t n_ob
     rc |= grow(ctx, ctx->scratch64, no * 5 * 8);
     rc |= grow(ctx, ctx->scratch_svi, no * 20 * sizeof(float));
     rc |= grow(ctx, ctx->t0state, nb * 3 * 8);
-    int grid_pso = ctx->num_sms * ctx->pso_blocks_per_sm;
-    size_t warps = (size_t)grid_pso * (ctx->pso_block / 32);
+    // MetzgerKN scratch of every resident swarm warp under any candidate
+    size_t warps = (size_t)ctx->num_sms * ctx->max_pso_warps_per_sm;
     rc |= grow(ctx, ctx->scratch, warps * 32 * (size_t)n_max * sizeof(float));
     const int64_t caps[7] = {(int64_t)nb * 26, (int64_t)nb * 21, (int64_t)nb * 5, (int64_t)nb * 3, (int64_t)nb * 3,
                              (int64_t)nb * 3, (int64_t)nb * 3};
@@ -481,6 +590,7 @@ static int prepare_layout(lcf_ctx* ctx, int n_sources, int n_bands, int64_t n_ob
         CK(cudaMemcpyAsync(ctx->tasks[0].p, T.data(), T.size() * sizeof(PsoTask), cudaMemcpyHostToDevice,
                            ctx->stream));
         ctx->layout_key = hash_layout(ctx->h_boff, ctx->h_soff, o);
+        ctx->bucket = shape_bucket(ctx->h_boff, n_bands);
         if (ctx->graph) {
             cudaGraphExecDestroy(ctx->graph);
             ctx->graph = nullptr;
@@ -603,7 +713,8 @@ static void enqueue_pipeline(lcf_ctx* ctx) {
 
 static int run_pipeline(lcf_ctx* ctx) {
     cudaGetLastError();  // a failed query elsewhere in the process must not be reported as ours
-    uint64_t gkey = ctx->layout_key ^ ((uint64_t)(uintptr_t)ctx->db.times * 31) ^ ((uint64_t)ctx->n_obs << 7);
+    uint64_t gkey = ctx->layout_key ^ ((uint64_t)(uintptr_t)ctx->db.times * 31) ^ ((uint64_t)ctx->n_obs << 7) ^
+                    ((uint64_t)(ctx->cfg + 1) << 56);
     if (ctx->use_graph) {
         if (!ctx->graph || ctx->graph_key != gkey) {
             if (ctx->graph) {
@@ -829,8 +940,10 @@ extern "C" int lcf_fit_parametric_batch(lcf_ctx* ctx, const lcf_bands_csr* in, c
     CK(cudaMemcpyAsync(ctx->soff.p, hp + (size_t)n_obs * 24 + (size_t)(nb + 1) * 8, (size_t)(ns + 1) * 4,
                        cudaMemcpyHostToDevice, s));
     if (nb == 0) return 0;
+    choose_launch(ctx);
     if (int rc = run_pipeline(ctx)) return rc;
     if (int rc = finish_stats(ctx)) return rc;
+    record_launch(ctx);
     ctx->stats.h2d_bytes = (double)in_bytes;
     return unpack_outputs(ctx, out);
 }
@@ -859,8 +972,11 @@ extern "C" int lcf_fit_parametric_device(lcf_ctx* ctx, const lcf_bands_csr* dev,
     ctx->db.band_off = dev->band_obs_offsets;
     ctx->db.src_off = dev->source_band_offsets;
     if (nb == 0) return 0;
+    choose_launch(ctx);
     if (int rc = run_pipeline(ctx)) return rc;
-    return finish_stats(ctx);
+    if (int rc = finish_stats(ctx)) return rc;
+    record_launch(ctx);
+    return 0;
 }
 
 extern "C" int lcf_fit_plain_device(lcf_ctx* ctx, const lcf_bands_csr* dev, const lcf_fit_options* o) {
@@ -893,6 +1009,69 @@ extern "C" int lcf_fit_plain_device(lcf_ctx* ctx, const lcf_bands_csr* dev, cons
     enqueue_plain(ctx);
     CK(cudaGetLastError());
     return finish_stats(ctx);
+}
+
+extern "C" int lcf_set_autotune(lcf_ctx* ctx, int mode, int forced_candidate) {
+    if (!ctx) return LCF_E_INVALID;
+    if ((mode != 0 && mode != 1) || forced_candidate < -1 || forced_candidate >= N_TUNE)
+        return set_err(ctx, LCF_E_INVALID, "autotune mode must be 0 or 1 and the candidate -1 .. 2");
+    ctx->tune_mode = mode;
+    ctx->tune_forced = forced_candidate;
+    return 0;
+}
+
+extern "C" int lcf_autotune_candidates(const lcf_ctx* ctx, int* out9) {
+    if (!ctx || !out9) return LCF_E_INVALID;
+    for (int c = 0; c < N_TUNE; c++) {
+        out9[3 * c] = TUNE_CAND[c].block;
+        out9[3 * c + 1] = TUNE_CAND[c].smem_obs;
+        out9[3 * c + 2] = ctx->cand_bps[c];
+    }
+    return N_TUNE;
+}
+
+extern "C" int lcf_autotune_table(const lcf_ctx* ctx, double* rows, int max_rows) {
+    if (!ctx || (max_rows > 0 && !rows)) return LCF_E_INVALID;
+    int n = 0;
+    for (const auto& e : ctx->tune) {
+        if (n >= max_rows) break;
+        double* r = rows + (size_t)n * 6;
+        r[0] = (double)e.bucket;
+        r[1] = (double)e.best;
+        r[2] = (double)e.next;
+        for (int c = 0; c < N_TUNE; c++) r[3 + c] = e.ms[c];
+        n++;
+    }
+    return (int)ctx->tune.size();
+}
+
+extern "C" int lcf_autotune_load(lcf_ctx* ctx, const double* rows, int n_rows) {
+    if (!ctx || n_rows < 0 || (n_rows > 0 && !rows)) return LCF_E_INVALID;
+    for (int i = 0; i < n_rows; i++) {
+        const double* r = rows + (size_t)i * 6;
+        int best = (int)r[1];
+        if (r[0] < 0.0 || r[0] > 4294967295.0 || best < 0 || best >= N_TUNE)
+            return set_err(ctx, LCF_E_INVALID, "autotune row: bad bucket or candidate");
+        TuneEntry e;
+        e.bucket = (uint32_t)r[0];
+        e.best = best;
+        e.next = N_TUNE;
+        for (int c = 0; c < N_TUNE; c++) e.ms[c] = r[3 + c];
+        bool found = false;
+        for (auto& t : ctx->tune)
+            if (t.bucket == e.bucket) { t = e; found = true; }
+        if (!found) ctx->tune.push_back(e);
+    }
+    return 0;
+}
+
+extern "C" int lcf_last_launch(const lcf_ctx* ctx, int* out4) {
+    if (!ctx || !out4) return LCF_E_INVALID;
+    out4[0] = ctx->cfg;
+    out4[1] = ctx->pso_block;
+    out4[2] = ctx->smem_obs;
+    out4[3] = (int)ctx->bucket;
+    return 0;
 }
 
 extern "C" int lcf_download_outputs(lcf_ctx* ctx, lcf_fit_outputs* out) {

@@ -47,6 +47,11 @@ def load(path: str = LIB_PATH):
     L.lcf_ctx_stream.restype = vp
     L.lcf_set_graph.argtypes = [vp, i]
     L.lcf_band_cost.argtypes = [vp, i, vp, vp, vp, vp, vp, i, vp, i, i, vp]
+    L.lcf_set_autotune.argtypes = [vp, i, i]
+    L.lcf_autotune_candidates.argtypes = [vp, vp]
+    L.lcf_autotune_table.argtypes = [vp, vp, i]
+    L.lcf_autotune_load.argtypes = [vp, vp, i]
+    L.lcf_last_launch.argtypes = [vp, vp]
     L.lcf_svi_elbo_grad.argtypes = [vp, i, vp, vp, vp, vp, vp, i, vp, vp, i, vp, i, vp, vp, vp]
     L.lcf_probe_peaks.argtypes = [vp, vp]
     L.lcf_probe_fp64.argtypes = [vp, vp]
@@ -193,6 +198,32 @@ class Context:
                                          u.ctypes.data, uf.ctypes.data, t.size, p.ctypes.data, p.shape[0],
                                          int(bool(with_prior)), out.ctypes.data), "lcf_band_cost")
         return out
+
+    def set_autotune(self, mode: int = 1, forced_candidate: int = -1):
+        """Online launch tuning per shape bucket (mode 1), off (0), or a pinned candidate."""
+        self._check(self.L.lcf_set_autotune(self.h, int(mode), int(forced_candidate)), "lcf_set_autotune")
+
+    def autotune_candidates(self) -> np.ndarray:
+        """(n, 3): block, staging depth, resident blocks per SM of each candidate."""
+        out = np.zeros(9, np.int32)
+        n = self.L.lcf_autotune_candidates(self.h, out.ctypes.data)
+        return out[:3 * n].reshape(n, 3)
+
+    def autotune_table(self) -> np.ndarray:
+        """(buckets, 6): bucket, chosen candidate (-1 while exploring), next, stage ms per candidate."""
+        n = self.L.lcf_autotune_table(self.h, None, 0)
+        rows = np.zeros((max(n, 1), 6))
+        self.L.lcf_autotune_table(self.h, rows.ctypes.data, n)
+        return rows[:n]
+
+    def autotune_load(self, rows):
+        r = np.ascontiguousarray(np.atleast_2d(rows), np.float64)
+        self._check(self.L.lcf_autotune_load(self.h, r.ctypes.data, r.shape[0]), "lcf_autotune_load")
+
+    def last_launch(self) -> dict:
+        out = np.zeros(4, np.int32)
+        self._check(self.L.lcf_last_launch(self.h, out.ctypes.data), "lcf_last_launch")
+        return {"candidate": int(out[0]), "block": int(out[1]), "smem_obs": int(out[2]), "bucket": int(out[3])}
 
     def svi_elbo_grad(self, model: int, times, flux, obs_var, is_upper, upper_flux, prior_init, var_params, eps):
         """One SVI step's ELBO estimate and its gradient (the SVI kernel's
