@@ -20,9 +20,22 @@
 
 namespace lcf {
 
-// MINPACK cstep (Moré–Thuente), min/max with Rust's NaN-ignoring semantics
+// FP64 division and square root out of line: the IEEE-rounded results of
+// the operators themselves, one copy of their instruction sequences instead
+// of one per use.  The polish is bound by instruction fetch, and the line
+// search's many divisions dominated its code.
+#ifdef LCF_LB_INLINE_DIV
+__device__ __forceinline__ double lb_div(double a, double b) { return a / b; }
+__device__ __forceinline__ double lb_sqrt(double x) { return sqrt(x); }
+#else
+static __device__ __noinline__ double lb_div(double a, double b) { return a / b; }
+static __device__ __noinline__ double lb_sqrt(double x) { return sqrt(x); }
+#endif
+
+// MINPACK cstep (Moré–Thuente), min/max with Rust's NaN-ignoring semantics;
+// out of line (one copy shared by every call site and model)
 #ifndef LCF_CSTEP_ATTR
-#define LCF_CSTEP_ATTR static __device__ inline
+#define LCF_CSTEP_ATTR static __device__ __noinline__
 #endif
 LCF_CSTEP_ATTR int lb_cstep(double& stx, double& fx, double& dx, double& sty, double& fy, double& dy, double& stp, double fp,
                         double dp, bool& brackt, double stpmin, double stpmax) {
@@ -30,59 +43,59 @@ LCF_CSTEP_ATTR int lb_cstep(double& stx, double& fx, double& dx, double& sty, do
         return 0;
     int info;
     bool bound;
-    double sgnd = dp * (dx / fabs(dx));
+    double sgnd = dp * lb_div(dx, fabs(dx));
     double stpf, stpc, stpq, theta, s, gamma, p, q, r;
     if (fp > fx) {
         info = 1; bound = true;
-        theta = 3.0 * (fx - fp) / (stp - stx) + dx + dp;
+        theta = lb_div(3.0 * (fx - fp), stp - stx) + dx + dp;
         s = fmax(fmax(fabs(theta), fabs(dx)), fabs(dp));
-        gamma = s * sqrt((theta / s) * (theta / s) - (dx / s) * (dp / s));
+        gamma = s * lb_sqrt(lb_div(theta, s) * lb_div(theta, s) - lb_div(dx, s) * lb_div(dp, s));
         if (stp < stx) gamma = -gamma;
         p = (gamma - dx) + theta;
         q = ((gamma - dx) + gamma) + dp;
-        r = p / q;
+        r = lb_div(p, q);
         stpc = stx + r * (stp - stx);
-        stpq = stx + ((dx / ((fx - fp) / (stp - stx) + dx)) / 2.0) * (stp - stx);
+        stpq = stx + (lb_div(dx, lb_div(fx - fp, stp - stx) + dx) / 2.0) * (stp - stx);
         stpf = fabs(stpc - stx) < fabs(stpq - stx) ? stpc : stpc + (stpq - stpc) / 2.0;
         brackt = true;
     } else if (sgnd < 0.0) {
         info = 2; bound = false;
-        theta = 3.0 * (fx - fp) / (stp - stx) + dx + dp;
+        theta = lb_div(3.0 * (fx - fp), stp - stx) + dx + dp;
         s = fmax(fmax(fabs(theta), fabs(dx)), fabs(dp));
-        gamma = s * sqrt((theta / s) * (theta / s) - (dx / s) * (dp / s));
+        gamma = s * lb_sqrt(lb_div(theta, s) * lb_div(theta, s) - lb_div(dx, s) * lb_div(dp, s));
         if (stp > stx) gamma = -gamma;
         p = (gamma - dp) + theta;
         q = ((gamma - dp) + gamma) + dx;
-        r = p / q;
+        r = lb_div(p, q);
         stpc = stp + r * (stx - stp);
-        stpq = stp + (dp / (dp - dx)) * (stx - stp);
+        stpq = stp + lb_div(dp, dp - dx) * (stx - stp);
         stpf = fabs(stpc - stp) > fabs(stpq - stp) ? stpc : stpq;
         brackt = true;
     } else if (fabs(dp) < fabs(dx)) {
         info = 3; bound = true;
-        theta = 3.0 * (fx - fp) / (stp - stx) + dx + dp;
+        theta = lb_div(3.0 * (fx - fp), stp - stx) + dx + dp;
         s = fmax(fmax(fabs(theta), fabs(dx)), fabs(dp));
-        gamma = s * sqrt(fmax(0.0, (theta / s) * (theta / s) - (dx / s) * (dp / s)));
+        gamma = s * lb_sqrt(fmax(0.0, lb_div(theta, s) * lb_div(theta, s) - lb_div(dx, s) * lb_div(dp, s)));
         if (stp > stx) gamma = -gamma;
         p = (gamma - dp) + theta;
         q = (gamma + (dx - dp)) + gamma;
-        r = p / q;
+        r = lb_div(p, q);
         if (r < 0.0 && gamma != 0.0) stpc = stp + r * (stx - stp);
         else if (stp > stx) stpc = stpmax;
         else stpc = stpmin;
-        stpq = stp + (dp / (dp - dx)) * (stx - stp);
+        stpq = stp + lb_div(dp, dp - dx) * (stx - stp);
         if (brackt) stpf = fabs(stp - stpc) < fabs(stp - stpq) ? stpc : stpq;
         else stpf = fabs(stp - stpc) > fabs(stp - stpq) ? stpc : stpq;
     } else {
         info = 4; bound = false;
         if (brackt) {
-            theta = 3.0 * (fp - fy) / (sty - stp) + dy + dp;
+            theta = lb_div(3.0 * (fp - fy), sty - stp) + dy + dp;
             s = fmax(fmax(fabs(theta), fabs(dy)), fabs(dp));
-            gamma = s * sqrt((theta / s) * (theta / s) - (dy / s) * (dp / s));
+            gamma = s * lb_sqrt(lb_div(theta, s) * lb_div(theta, s) - lb_div(dy, s) * lb_div(dp, s));
             if (stp > sty) gamma = -gamma;
             p = (gamma - dp) + theta;
             q = ((gamma - dp) + gamma) + dy;
-            r = p / q;
+            r = lb_div(p, q);
             stpc = stp + r * (sty - stp);
             stpf = stpc;
         } else {

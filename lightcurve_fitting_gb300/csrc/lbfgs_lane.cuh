@@ -103,10 +103,10 @@ __device__ double lane_lbfgs_polish(Ctx& c, double& pj, double pso_cost) {
     for (int k = 0; k < M; k++) { S[k] = 0.0; Y[k] = 0.0; rho[k] = 0.0; }
     int cm = 0, it = 0;
     bool ok = true;
-    auto converged = [&]() { return sqrt(dot8(gj, gj)) < tol_grad || fabs(prev_f - f) < tol_cost; };
+    auto converged = [&]() { return lb_sqrt(dot8(gj, gj)) < tol_grad || fabs(prev_f - f) < tol_cost; };
     bool stop = converged() || it >= MAXIT;
     while (!stop) {
-        double gamma = cm > 0 ? dot8(S[0], Y[0]) / dot8(Y[0], Y[0]) : 1.0;
+        double gamma = cm > 0 ? lb_div(dot8(S[0], Y[0]), dot8(Y[0], Y[0])) : 1.0;
         // two-loop recursion: newest (index 0) to oldest, then back
         double q = gj, alpha[M];
 #pragma unroll
@@ -132,7 +132,7 @@ __device__ double lane_lbfgs_polish(Ctx& c, double& pj, double pso_cost) {
         for (int k = M - 1; k > 0; k--) { S[k] = S[k - 1]; Y[k] = Y[k - 1]; rho[k] = rho[k - 1]; }
         S[0] = sj;
         Y[0] = yj;
-        rho[0] = 1.0 / dot8(yj, sj);
+        rho[0] = lb_div(1.0, dot8(yj, sj));
         cm = cm < M ? cm + 1 : M;
         xj = xnj;
         gj = gnj;
