@@ -30,7 +30,7 @@
 // polish's seven model terms share one copy each instead of inlining dozens
 // (the kernel is otherwise bound by instruction fetch).
 #ifndef LCF_FF_BIG
-#define LCF_FF_BIG __device__ __noinline__
+#define LCF_FF_BIG static __device__ __noinline__
 #endif
 #ifndef LCF_FF_SMALL
 #define LCF_FF_SMALL __device__ __forceinline__

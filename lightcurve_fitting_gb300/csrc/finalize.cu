@@ -814,7 +814,7 @@ __global__ void t0_pick_kernel(DeviceBatch d, int fine, int64_t t0_base) {
         int fi = 0;
         for (int i = 0; i < np - 1; i++) {
             if (i == t0i) o.pso_params[fi++] = t0v;
-            o.pso_params[fi++] = (double)R.params[i];
+            o.pso_params[fi++] = pso_param(R, i);
         }
         if (t0i >= np - 1) o.pso_params[fi] = t0v;
         o.pso_cost = best_c;

@@ -54,11 +54,21 @@ struct Xoshiro {
     double f64() { return (double)(next() >> 11) * (1.0 / 9007199254740992.0); }
 };
 
-void make_draw_tables(float* draws, float* svi_eps) {
+void make_draw_tables(float* draws, double* draws64, float2* draws15, float* svi_eps) {
     const uint64_t seeds[3] = {42, 137, 271};
     for (int k = 0; k < 3; k++) {
         Xoshiro r(seeds[k]);
-        for (int i = 0; i < DRAWS_PER_SEED; i++) draws[(size_t)k * DRAWS_PER_SEED + i] = (float)r.f64();
+        for (int i = 0; i < DRAWS_PER_SEED; i++) {
+            const size_t q = (size_t)k * DRAWS_PER_SEED + i;
+            const double u = r.f64();
+            draws[q] = (float)u;
+            draws64[q] = u;
+            // c1 * r and c2 * r of the velocity update (c1 = c2 = 1.5), the
+            // FP64 product as a double-float pair
+            const double cu = 1.5 * u;
+            const float hi = (float)cu;
+            draws15[q] = make_float2(hi, (float)(cu - (double)hi));
+        }
     }
     // svi_fit, src/parametric.rs:2282-2288: SmallRng(42); per step, sample
     // and parameter: u1 = max(U, 1e-10), u2 = U, eps = sqrt(-2 ln u1) cos(2 pi u2)
@@ -150,6 +160,8 @@ struct lcf_ctx {
     cudaEvent_t ev[N_EVENTS]{};
     // tables
     float* d_draws = nullptr;
+    double* d_draws64 = nullptr;
+    float2* d_draws15 = nullptr;
     float* d_eps = nullptr;
     // device buffers (capacity-sized)
     DevArr times, flux, ferr, boff, soff, stats_b, obs, t64, f64, fe64, var64, uf64, mag64, up, ffa, ffb, res, fits, out, mb,
@@ -278,13 +290,19 @@ extern "C" int lcf_ctx_create(int device, lcf_ctx** out) {
     ctx->pso_blocks_per_sm = ctx->cand_bps[0];
     // RNG tables
     std::vector<float> draws((size_t)3 * DRAWS_PER_SEED), eps((size_t)3 * SVI_STEPS * SVI_SAMPLES * 7);
-    make_draw_tables(draws.data(), eps.data());
+    std::vector<double> draws64(draws.size());
+    std::vector<float2> draws15(draws.size());
+    make_draw_tables(draws.data(), draws64.data(), draws15.data(), eps.data());
     if (cudaMalloc(&ctx->d_draws, draws.size() * sizeof(float)) != cudaSuccess ||
+        cudaMalloc(&ctx->d_draws64, draws64.size() * sizeof(double)) != cudaSuccess ||
+        cudaMalloc(&ctx->d_draws15, draws15.size() * sizeof(float2)) != cudaSuccess ||
         cudaMalloc(&ctx->d_eps, eps.size() * sizeof(float)) != cudaSuccess) {
         lcf_ctx_destroy(ctx);
         return LCF_E_NOMEM;
     }
     cudaMemcpy(ctx->d_draws, draws.data(), draws.size() * sizeof(float), cudaMemcpyHostToDevice);
+    cudaMemcpy(ctx->d_draws64, draws64.data(), draws64.size() * sizeof(double), cudaMemcpyHostToDevice);
+    cudaMemcpy(ctx->d_draws15, draws15.data(), draws15.size() * sizeof(float2), cudaMemcpyHostToDevice);
     cudaMemcpy(ctx->d_eps, eps.data(), eps.size() * sizeof(float), cudaMemcpyHostToDevice);
     *out = ctx;
     return LCF_OK;
@@ -307,6 +325,8 @@ extern "C" void lcf_ctx_destroy(lcf_ctx* ctx) {
     if (ctx->h_in.p) cudaFreeHost(ctx->h_in.p);
     if (ctx->h_out.p) cudaFreeHost(ctx->h_out.p);
     if (ctx->d_draws) cudaFree(ctx->d_draws);
+    if (ctx->d_draws64) cudaFree(ctx->d_draws64);
+    if (ctx->d_draws15) cudaFree(ctx->d_draws15);
     if (ctx->d_eps) cudaFree(ctx->d_eps);
     for (int i = 0; i < N_EVENTS; i++)
         if (ctx->ev[i]) cudaEventDestroy(ctx->ev[i]);
@@ -619,6 +639,8 @@ static int prepare_layout(lcf_ctx* ctx, int n_sources, int n_bands, int64_t n_ob
     d.ffa = (float4*)ctx->ffa.p;
     d.ffb = (float2*)ctx->ffb.p;
     d.draws = ctx->d_draws;
+    d.draws64 = ctx->d_draws64;
+    d.draws15 = ctx->d_draws15;
     d.svi_eps = ctx->d_eps;
     d.pso_res = (PsoResult*)ctx->res.p;
     d.fits = (ModelFit*)ctx->fits.p;

@@ -160,6 +160,12 @@ struct PsoResult {
     float params[MB_MAXP];
     float pad[2];
 };
+// Parameter j of a swarm result.  The exact-trajectory swarms (models other
+// than MetzgerKN) store each component as a double-float pair, params[j] +
+// params[7 + j], and mark it with pad[0] == 1; the other swarms store FP32.
+__host__ __device__ inline double pso_param(const PsoResult& R, int j) {
+    return (R.pad[0] == 1.0f && j < 7) ? (double)R.params[j] + (double)R.params[7 + j] : (double)R.params[j];
+}
 
 // Result of one joint multi-band swarm run (one source, one restart).
 struct JointResult {
@@ -244,6 +250,8 @@ struct DeviceBatch {
     float2* ffb;
     // tables
     const float* draws;     // [3][DRAWS_PER_SEED] uniforms of seeds 42, 137, 271
+    const double* draws64;  // the same uniforms in FP64 (swarm initialisation)
+    const float2* draws15;  // 1.5 x those uniforms (FP64 products) as double-float pairs
     const float* svi_eps;   // [3][SVI_STEPS][SVI_SAMPLES][7] noise for 5, 6, 7 params
     // results
     PsoResult* pso_res;     // per task slot
@@ -323,7 +331,7 @@ void launch_band_cost(int model, const float4* obs, int n, float t_last, const d
                       int with_prior, double* costs, float* scratch, cudaStream_t s);
 
 // Host-side generation of the RNG tables (host.cpp)
-void make_draw_tables(float* draws, float* svi_eps);
+void make_draw_tables(float* draws, double* draws64, float2* draws15, float* svi_eps);
 void make_joint_draws(float* draws, int64_t per_seed);
 
 }  // namespace lcf

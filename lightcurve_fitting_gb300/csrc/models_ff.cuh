@@ -26,7 +26,7 @@
 // the upper-limit term runs for ~1/4 of the observations: out of line it keeps
 // the observation loop's hot code smaller (measured 1.5 % faster polish)
 #ifndef LCF_FF_UPPER
-#define LCF_FF_UPPER __device__ __noinline__
+#define LCF_FF_UPPER static __device__ __noinline__
 #endif
 
 namespace lcf {

@@ -21,13 +21,16 @@
 // view of the reference's sequence.
 #include <cuda_runtime.h>
 
+#include "lane_cost.cuh"
 #include "lcf_internal.cuh"
 #include "models_f32.cuh"
 #include "swarm_cost.cuh"
 
 namespace lcf {
 
+#ifndef FULL
 #define FULL 0xffffffffu
+#endif
 
 // ---------------------------------------------------------------------------
 // Band preparation (src/parametric.rs:3581-3630): warp per band.
@@ -205,6 +208,13 @@ __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t phase) {
 struct WarpSmem {
     uint64_t bar;
     uint64_t pad;
+    // exact-trajectory swarms: box, velocity limit and global best of the
+    // current run, double-float, one per swarm dimension
+    ff lo[7], hi[7], vmax[7], g[7];
+    // and the low halves of each lane's double-float state (the high halves
+    // stay in registers): [state][dimension][lane], state = position,
+    // velocity, personal best, position and velocity at the iteration start
+    float lo_state[5][7][32];
 };
 
 // One swarm run (pso_minimize / pso_minimize_seeded, src/parametric.rs:1646-1757,
@@ -428,6 +438,328 @@ __device__ __forceinline__ void run_swarm(const DeviceBatch& d, const PsoTask& t
     }
 }
 
+// ---------------------------------------------------------------------------
+// Exact-trajectory swarms: the models other than MetzgerKN, in model
+// selection and the profile t0 search.  The reference's choice of model is
+// chaotic at the 1e-7 level: with its own FP64 costs, rounding only the
+// particle positions to FP32 changes the selected model for ~1.2 % of bands
+// (measured with the FP64 restatement on 600 bands).  These swarms therefore
+// follow the reference's trajectory at double-float precision:
+//   * positions, velocities and bests are double-float pairs (high halves in
+//     registers, low halves in shared memory), initialised with the
+//     reference's FP64 draws and moved with its FP64 products 1.5 r
+//     (c1 = c2 = 1.5), ~1e-14 from the reference's FP64 arithmetic;
+//   * each particle's cost is evaluated in FP32 at the position's leading
+//     float, lane-split as in the other swarms (deciding near-tied FP32
+//     comparisons on accurate costs was measured and changed no result);
+//   * the run's result cost is the accurate cost of its best position (the
+//     polish's double-float cost, LaneLb), so that the choice among restarts
+//     and the t0 search's picks compare accurate costs, and the best position
+//     is stored as double-float pairs (pso_param).
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ bool ff_lt(ff a, ff b) { return a.hi < b.hi || (a.hi == b.hi && a.lo < b.lo); }
+__device__ __forceinline__ bool ff_le(ff a, ff b) { return a.hi < b.hi || (a.hi == b.hi && a.lo <= b.lo); }
+
+// Accurate cost of the double-float position pos[0..6] (every lane passes
+// the same position): component j of the full parameter vector in lane j,
+// t0 inserted for t0-fixed tasks.
+template <int KIND>
+__device__ __noinline__ double swarm_exact_cost(LaneLb<KIND>& lc, bool fixed, double t0_fixed, const ff* pos) {
+    constexpr int t0i = t0_idx_of(KIND);
+    const int j = threadIdx.x & 7;
+    double v = (fixed && j == t0i) ? t0_fixed : 0.0;
+#pragma unroll
+    for (int m = 0; m < 7; m++) {
+        const int k = (fixed && m >= t0i) ? m + 1 : m;
+        if (k == j && !(fixed && j == t0i)) v = (double)pos[m].hi + (double)pos[m].lo;
+    }
+    double f, g_unused;
+    lc.cost_grad(v, f, g_unused, false);
+    return f;
+}
+
+// The band and cost options of a swarm task for swarm_exact_cost.
+template <int KIND>
+__device__ __forceinline__ void exact_cost_setup(LaneLb<KIND>& lc, const DeviceBatch& d, const BandStats& bs,
+                                                 int flags) {
+    lc.t = d.t64 + bs.off;
+    lc.flux = d.f64 + bs.off;
+    lc.var = d.var64 + bs.off;
+    lc.uf = d.uf64 + bs.off;
+    lc.up = d.up + bs.off;
+    lc.fa = d.ffa + bs.off;
+    lc.fb = d.ffb + bs.off;
+    lc.t_first = bs.t_first;
+    lc.t_last = bs.t_last;
+    lc.n = bs.n;
+    lc.nd = (double)max(bs.n, 1);
+    lc.inv_nd = 1.0 / lc.nd;
+    lc.lo_j = -INFINITY;
+    lc.hi_j = INFINITY;
+    lc.evals = 0;
+    lc.iters = 0;
+    lc.fp64_evals = 0;
+    lc.with_prior = (flags & TASK_PRIOR) != 0;
+}
+
+template <int KIND>
+__device__ __forceinline__ void run_swarm_exact(const DeviceBatch& d, const PsoTask& task, const BandStats& bs,
+                                                TaskCtx& t, WarpSmem* ws, int slot) {
+    constexpr int m = KIND, np = n_params_of(m), t0i = t0_idx_of(m), MAXD = 7;
+    const int lane = threadIdx.x & 31;
+    const int p = lane;
+    const bool live = p < NP;
+    const bool seeded = (task.flags & TASK_SEEDED) != 0;
+    const bool fixed = (task.flags & TASK_T0_FIXED) != 0;
+    t.model = m;
+    t.np = np;
+    t.t0i = t0i;
+    t.D = fixed ? np - 1 : np;
+    const int D = t.D;
+    // low halves of this lane's state
+    float* XL = &ws->lo_state[0][0][lane];
+    float* VL = &ws->lo_state[1][0][lane];
+    float* PL = &ws->lo_state[2][0][lane];
+    float* X0L = &ws->lo_state[3][0][lane];
+    float* V0L = &ws->lo_state[4][0][lane];
+    // the box in FP64 (data-informed t0 bounds, src/parametric.rs:1881-1909);
+    // swarm dimension k is parameter k, or k + 1 past t0 when t0 is fixed
+    double blo[MAXD], bhi[MAXD], seed[MAXD];
+    {
+        double dlo[MAXP], dhi[MAXP];
+#pragma unroll
+        for (int j = 0; j < MAXP; j++) { dlo[j] = c_lo[m][j]; dhi[j] = c_hi[m][j]; }
+        if (task.flags & TASK_T0_BOUNDS) {
+            const double t0_lo = fmax(bs.t_first - 30.0, dlo[t0i]);
+            const double t0_hi = fmin(bs.t_peak + 10.0, dhi[t0i]);
+            if (t0_lo < t0_hi) { dlo[t0i] = t0_lo; dhi[t0i] = t0_hi; }
+        }
+#pragma unroll
+        for (int k = 0; k < MAXD; k++) {
+            const int jk = (fixed && k >= t0i) ? k + 1 : k;
+            blo[k] = k < D ? dlo[jk] : 0.0;
+            bhi[k] = k < D ? dhi[jk] : 0.0;
+            seed[k] = 0.0;
+        }
+        if (seeded) {
+            // seed particles of pso_fit_single_model, src/parametric.rs:1924-1964
+#pragma unroll
+            for (int j = 0; j < np; j++) seed[j] = fmin(fmax(c_pop_c[m][j], dlo[j]), dhi[j]);
+            const double t0s = task.restart == 1 ? bs.t_peak - 5.0 : bs.t_first - 15.0;
+            seed[t0i] = fmin(fmax(t0s, dlo[t0i]), dhi[t0i]);
+        }
+    }
+    double vmaxd[MAXD];
+#pragma unroll
+    for (int k = 0; k < MAXD; k++) vmaxd[k] = __dmul_rn(0.5, __dsub_rn(bhi[k], blo[k]));
+    __syncwarp();
+    if (lane == 0) {
+#pragma unroll
+        for (int k = 0; k < MAXD; k++) {
+            ws->lo[k] = ff_from(blo[k]);
+            ws->hi[k] = ff_from(bhi[k]);
+            ws->vmax[k] = ff_from(vmaxd[k]);
+            ws->g[k] = ffm(0.0f, 0.0f);
+        }
+    }
+    // ---- initialisation (src/parametric.rs:1677-1692, seeded :1189-1210) in
+    // FP64 as the reference, without contractions
+    const double* dr = d.draws64 + (size_t)task.restart * DRAWS_PER_SEED;
+    const float2* d15 = d.draws15 + (size_t)task.restart * DRAWS_PER_SEED;
+    float xh[MAXD], vh[MAXD], pbh[MAXD];
+    int base;
+    {
+        double xi[MAXD], vi[MAXD];
+#pragma unroll
+        for (int k = 0; k < MAXD; k++) { xi[k] = 0.0; vi[k] = 0.0; }
+        if (seeded) {
+            if (p == 0) {
+#pragma unroll
+                for (int k = 0; k < MAXD; k++)
+                    if (k < D) {
+                        xi[k] = seed[k];
+                        vi[k] = __dmul_rn(__dmul_rn(vmaxd[k], 0.2), __dsub_rn(2.0 * dr[k], 1.0));
+                    }
+            } else if (live) {
+                const int o = D + 2 * D * (p - 1);
+#pragma unroll
+                for (int k = 0; k < MAXD; k++)
+                    if (k < D) {
+                        xi[k] = __dadd_rn(blo[k], __dmul_rn(dr[o + k], __dsub_rn(bhi[k], blo[k])));
+                        vi[k] = __dmul_rn(__dmul_rn(vmaxd[k], 0.2), __dsub_rn(2.0 * dr[o + D + k], 1.0));
+                    }
+            }
+            base = 2 * D * NP - D;
+        } else {
+            if (live) {
+                const int o = 2 * D * p;
+#pragma unroll
+                for (int k = 0; k < MAXD; k++)
+                    if (k < D) {
+                        xi[k] = __dadd_rn(blo[k], __dmul_rn(dr[o + 2 * k], __dsub_rn(bhi[k], blo[k])));
+                        vi[k] = __dmul_rn(__dmul_rn(vmaxd[k], 0.2), __dsub_rn(2.0 * dr[o + 2 * k + 1], 1.0));
+                    }
+            }
+            base = 2 * D * NP;
+        }
+#pragma unroll
+        for (int k = 0; k < MAXD; k++) {
+            const ff xf = ff_from(xi[k]), vf = ff_from(vi[k]);
+            xh[k] = xf.hi;
+            XL[32 * k] = xf.lo;
+            vh[k] = vf.hi;
+            VL[32 * k] = vf.lo;
+            pbh[k] = xf.hi;
+            PL[32 * k] = xf.lo;
+        }
+    }
+    __syncwarp();
+    // one evaluation round over lanes start .. NP - 1 (lane-split FP32)
+    auto eval_round = [&](int start) -> double {
+        const int kk = NP - start;
+        const double cs = particle_cost_split<KIND>(t, xh, start, kk);
+        const double co = __shfl_sync(FULL, cs, ((p - start) * split_lanes(kk)) & 31);
+        return (live && p >= start) ? co : INFINITY;
+    };
+    // the global best <- the position of lane q
+    auto set_gbest = [&](int q) {
+        ff gq[MAXD];
+#pragma unroll
+        for (int k = 0; k < MAXD; k++) gq[k] = ffm(__shfl_sync(FULL, xh[k], q), __shfl_sync(FULL, XL[32 * k], q));
+        __syncwarp();
+        if (lane == 0) {
+#pragma unroll
+            for (int k = 0; k < MAXD; k++) ws->g[k] = gq[k];
+        }
+        __syncwarp();
+    };
+    double c = eval_round(0);
+    int evals = 1;
+    double pbc = c;
+    double gc = INFINITY;
+    {
+        // global best after the sequential initial loop: first strict minimum
+        double mn = c;
+        for (int k = 16; k; k >>= 1) mn = fmin(mn, __shfl_xor_sync(FULL, mn, k));
+        const unsigned mm = __ballot_sync(FULL, live && c == mn && mn < INFINITY);
+        if (mm) {
+            const int q = __ffs(mm) - 1;
+            gc = mn;
+            set_gbest(q);
+        }
+    }
+    // ---- iterations (src/parametric.rs:1694-1755)
+    int stall = 0;
+    double prev = gc;
+    const double inv_iters = 1.0 / (double)MAX_ITERS;
+    int it = 0;
+    for (; it < MAX_ITERS; it++) {
+        const double wd = __dsub_rn(0.9, __dmul_rn(__dmul_rn(__dsub_rn(0.9, 0.4), (double)it), inv_iters));
+        const ff w = ff_from(wd);
+        float x0h[MAXD], v0h[MAXD];
+#pragma unroll
+        for (int k = 0; k < MAXD; k++) {
+            x0h[k] = xh[k];
+            v0h[k] = vh[k];
+            X0L[32 * k] = XL[32 * k];
+            V0L[32 * k] = VL[32 * k];
+        }
+        const float2* r15 = d15 + base + it * 2 * D * NP + 2 * D * p;
+        int start = 0;
+        while (start < NP) {
+            const bool active = live && p >= start;
+            if (active) {
+#pragma unroll
+                for (int k = 0; k < MAXD; k++) {
+                    if (k < D) {
+                        const float2 a1 = r15[2 * k], a2 = r15[2 * k + 1];
+                        const ff x0 = ffm(x0h[k], X0L[32 * k]), v0 = ffm(v0h[k], V0L[32 * k]);
+                        const ff pbk = ffm(pbh[k], PL[32 * k]);
+                        ff vv = ff_add(ff_add(ff_mul(w, v0), ff_mul(ffm(a1.x, a1.y), ff_sub(pbk, x0))),
+                                       ff_mul(ffm(a2.x, a2.y), ff_sub(ws->g[k], x0)));
+                        const ff vm = ws->vmax[k];
+                        if (ff_lt(vv, ff_neg(vm))) vv = ff_neg(vm);
+                        if (ff_lt(vm, vv)) vv = vm;
+                        const ff nx = ff_add(x0, vv);
+                        const ff lo = ws->lo[k], hi = ws->hi[k];
+                        ff xn, vn;
+                        if (ff_le(nx, lo)) { xn = lo; vn = ffm(0.0f, 0.0f); }
+                        else if (ff_le(hi, nx)) { xn = hi; vn = ffm(0.0f, 0.0f); }
+                        else { xn = nx; vn = vv; }
+                        xh[k] = xn.hi;
+                        XL[32 * k] = xn.lo;
+                        vh[k] = vn.hi;
+                        VL[32 * k] = vn.lo;
+                    }
+                }
+            }
+            {
+                const double cr = eval_round(start);
+                if (active) {
+                    c = cr;
+                    evals++;
+                }
+            }
+            const unsigned mq = __ballot_sync(FULL, active && c < gc);
+            const int q = mq ? __ffs(mq) - 1 : NP - 1;
+            const bool acc = live && p >= start && p <= q;
+            if (acc && c < pbc) {
+                pbc = c;
+#pragma unroll
+                for (int k = 0; k < MAXD; k++) {
+                    pbh[k] = xh[k];
+                    PL[32 * k] = XL[32 * k];
+                }
+            }
+            if (mq) {
+                gc = __shfl_sync(FULL, c, q);
+                set_gbest(q);
+            }
+            start = q + 1;
+        }
+        bool improved = prev - gc > 0.01 * fmax(fabs(prev), 1e-10);
+        if (improved) {
+            stall = 0;
+            prev = gc;
+        } else if (++stall >= STALL_ITERS) {
+            it++;
+            break;
+        }
+    }
+    // ---- result: the accurate cost of the best position
+    double rc = gc;
+    if (gc < INFINITY) {
+        LaneLb<KIND> lc;
+        exact_cost_setup(lc, d, bs, task.flags);
+        ff gp[MAXD];
+#pragma unroll
+        for (int k = 0; k < MAXD; k++) gp[k] = ws->g[k];
+        rc = swarm_exact_cost<KIND>(lc, fixed, task.t0_fixed, gp);
+    }
+    int tot_evals = live ? evals : 0;
+    for (int k = 16; k; k >>= 1) tot_evals += __shfl_xor_sync(FULL, tot_evals, k);
+    if (lane == 0) {
+        PsoResult& R = d.pso_res[task.out];
+        R.cost = rc;
+        R.iters = it;
+        R.evals = tot_evals;
+        for (int j = 0; j < MB_MAXP; j++) R.params[j] = 0.0f;
+#pragma unroll
+        for (int k = 0; k < MAXD; k++)
+            if (k < D) {
+                R.params[k] = ws->g[k].hi;
+                R.params[7 + k] = ws->g[k].lo;
+            }
+        R.pad[0] = 1.0f;
+        atomicAdd(&d.ctr->particle_obs_evals, (unsigned long long)tot_evals * (unsigned long long)bs.n);
+        if (slot == 0) {
+            atomicAdd(&d.ctr->slot0_evals[KIND], (unsigned long long)tot_evals * (unsigned long long)bs.n);
+            atomicAdd(&d.ctr->slot0_particles[KIND], (unsigned long long)tot_evals);
+        }
+    }
+    __syncwarp();
+}
+
 // Blocks of 256 threads per SM the register budget is sized for (128
 // registers a thread): measured on GB300, two resident blocks (16 warps) with
 // a few spills run the swarms ~1.7x faster than one block without spills.
@@ -489,13 +821,13 @@ __global__ void __launch_bounds__(256, LCF_PSO_MINB7)
             constexpr int KMB = KIND_MB1 + (MAXD - 2) / 4 - 1;  // D = 4K + 2
             if (task.kind == KMB) run_swarm<MAXD, KMB>(d, task, bs, t, slot, gwarp);
         } else switch (task.kind) {
-            case BAZIN: run_swarm<MAXD, BAZIN>(d, task, bs, t, slot, gwarp); break;
-            case VILLAR: run_swarm<MAXD, VILLAR>(d, task, bs, t, slot, gwarp); break;
-            case TDE: run_swarm<MAXD, TDE>(d, task, bs, t, slot, gwarp); break;
-            case ARNETT: run_swarm<MAXD, ARNETT>(d, task, bs, t, slot, gwarp); break;
-            case MAGNETAR: run_swarm<MAXD, MAGNETAR>(d, task, bs, t, slot, gwarp); break;
-            case SHOCK: run_swarm<MAXD, SHOCK>(d, task, bs, t, slot, gwarp); break;
-            case AFTERGLOW: run_swarm<MAXD, AFTERGLOW>(d, task, bs, t, slot, gwarp); break;
+            case BAZIN: run_swarm_exact<BAZIN>(d, task, bs, t, ws, slot); break;
+            case VILLAR: run_swarm_exact<VILLAR>(d, task, bs, t, ws, slot); break;
+            case TDE: run_swarm_exact<TDE>(d, task, bs, t, ws, slot); break;
+            case ARNETT: run_swarm_exact<ARNETT>(d, task, bs, t, ws, slot); break;
+            case MAGNETAR: run_swarm_exact<MAGNETAR>(d, task, bs, t, ws, slot); break;
+            case SHOCK: run_swarm_exact<SHOCK>(d, task, bs, t, ws, slot); break;
+            case AFTERGLOW: run_swarm_exact<AFTERGLOW>(d, task, bs, t, ws, slot); break;
             case METZGER: run_swarm<MAXD, METZGER>(d, task, bs, t, slot, gwarp); break;
             case KIND_MB1: run_swarm<MAXD, KIND_MB1>(d, task, bs, t, slot, gwarp); break;
             default: break;
