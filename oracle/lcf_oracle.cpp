@@ -961,10 +961,11 @@ struct SingleFit {
     std::vector<double> params;
     double cost;
 };
-static SingleFit pso_fit_single_model(const Band& b, int m) {
-    std::vector<double> lo, hi;
+// The restarts' shared set-up of pso_fit_single_model (:1864-1964): the box
+// with data-informed t0 bounds and the two seed particles.
+static void single_model_setup(const Band& b, int m, std::vector<double>& lo, std::vector<double>& hi,
+                               std::vector<double>& seed_a, std::vector<double>& seed_b) {
     pso_bounds(m, lo, hi);
-    Cost prob(&b, m, true);
     int t0i = T0_IDX[m], n = b.n();
     double peak_time = b.t[0], peak_flux = -INF;
     for (int i = 0; i < n; i++) if (!b.up[i] && b.f[i] > peak_flux) { peak_flux = b.f[i]; peak_time = b.t[i]; }
@@ -978,7 +979,8 @@ static SingleFit pso_fit_single_model(const Band& b, int m) {
     std::vector<double> pc, pw;
     population_priors(m, pc, pw);
     int dim = (int)lo.size();
-    std::vector<double> seed_a(dim), seed_b(dim);
+    seed_a.assign(dim, 0.0);
+    seed_b.assign(dim, 0.0);
     for (int d = 0; d < dim; d++) {
         double v = d < (int)pc.size() ? clampd(pc[d], lo[d], hi[d]) : 0.5 * (lo[d] + hi[d]);
         seed_a[d] = v;
@@ -986,13 +988,33 @@ static SingleFit pso_fit_single_model(const Band& b, int m) {
     }
     seed_a[t0i] = clampd(peak_time - 5.0, lo[t0i], hi[t0i]);
     seed_b[t0i] = clampd(t_first - 15.0, lo[t0i], hi[t0i]);
+}
+
+// Restart r (0, 1, 2: seeds 42, 137, 271; seed particles for 1 and 2) of
+// the model-selection swarm; iters / evals from the swarm's counters.
+static double single_model_restart(const Band& b, int m, int r, std::vector<double>& gbest, long long* iters,
+                                   long long* evals) {
+    std::vector<double> lo, hi, seed_a, seed_b;
+    single_model_setup(b, m, lo, hi, seed_a, seed_b);
+    Cost prob(&b, m, true);
     const uint64_t seeds[3] = {42, 137, 271};
+    const double* sp = r == 1 ? seed_a.data() : (r == 2 ? seed_b.data() : nullptr);
+    PsoStats before = g_pso_stats;
+    double c = pso_minimize(prob, lo, hi, 30, 60, 12, seeds[r], b.n() > 0 ? sp : nullptr, gbest);
+    if (iters) *iters = g_pso_stats.iters - before.iters;
+    if (evals) *evals = g_pso_stats.evals - before.evals;
+    return c;
+}
+
+static SingleFit pso_fit_single_model(const Band& b, int m) {
+    std::vector<double> lo, hi, seed_a, seed_b;
+    single_model_setup(b, m, lo, hi, seed_a, seed_b);
+    Cost prob(&b, m, true);
     std::vector<double> best;
     double best_c = INF;
     for (int i = 0; i < 3; i++) {
         std::vector<double> gp;
-        const double* sp = i == 1 ? seed_a.data() : (i == 2 ? seed_b.data() : nullptr);
-        double c = pso_minimize(prob, lo, hi, 30, 60, 12, seeds[i], n > 0 ? sp : nullptr, gp);
+        double c = single_model_restart(b, m, i, gp, nullptr, nullptr);
         if (c < best_c) { best_c = c; best = gp; }
     }
     SingleFit r;
@@ -2009,6 +2031,21 @@ int orc_band_cost_grad(int m, const double* t, const double* f, const double* va
     Band b = make_band(t, f, var, up, uf, n);
     Cost c(&b, m, false);
     c.gradient(params, grad);
+    return 0;
+}
+// Restart r of the model-selection swarm of model m on one band (the swarm
+// of pso_fit_single_model): out = cost, iterations, evaluations, then the
+// best position (7 values, 0-padded).
+int orc_model_restart(int m, const double* t, const double* f, const double* var, const uint8_t* up,
+                      const double* uf, int n, int r, double* out) {
+    if (m < 0 || m > 7 || r < 0 || r > 2) return -1;
+    Band b = make_band(t, f, var, up, uf, n);
+    std::vector<double> g;
+    long long it = 0, ev = 0;
+    out[0] = single_model_restart(b, m, r, g, &it, &ev);
+    out[1] = (double)it;
+    out[2] = (double)ev;
+    for (int j = 0; j < 7; j++) out[3 + j] = j < (int)g.size() ? g[j] : 0.0;
     return 0;
 }
 // One PSO run of PsoCost(model, prior) within [lo, hi]; seed particle optional.

@@ -63,6 +63,7 @@ def lib():
         L.orc_lbfgs_refine.restype = d
         L.orc_svi_fit.argtypes = [i, vp, vp, vp, vp, vp, i, vp, i, i, d, vp, vp, vp]
         L.orc_laplace_fit.argtypes = [i, vp, vp, vp, vp, vp, i, vp, vp, vp]
+        L.orc_model_restart.argtypes = [i, vp, vp, vp, vp, vp, i, i, vp]
         L.orc_svi_elbo_grad.argtypes = [i, vp, vp, vp, vp, vp, i, vp, vp, vp, i, vp, vp]
         L.orc_fit_batch.argtypes = [C.POINTER(abi.BandsCSR), C.POINTER(abi.FitOptions), C.POINTER(abi.FitOutputs), i]
         L.orc_laplace_refine.argtypes = [i, vp, vp, vp, i, vp, vp, vp, vp]
@@ -153,6 +154,14 @@ def pso_run(model: int, band: Band, lo, hi, seed: int, seed_particle=None, with_
     c = lib().orc_pso_run(model, *band.args(), _p(lo), _p(hi), seed, None if sp is None else _p(sp),
                           int(with_prior), _p(g))
     return g, c
+
+
+def model_restart(model: int, band: Band, restart: int):
+    """Restart `restart` of the model-selection swarm (pso_fit_single_model):
+    (cost, iterations, evaluations, best position)."""
+    out = np.zeros(10)
+    assert lib().orc_model_restart(model, *band.args(), int(restart), _p(out)) == 0
+    return float(out[0]), int(out[1]), int(out[2]), out[3:3 + abi.N_PARAMS[model]].copy()
 
 
 def svi_fit(model: int, band: Band, init, n_steps=1000, n_samples=4, lr=0.01):

@@ -289,3 +289,48 @@ def test_svi_matches_oracle_on_equal_inputs(ctx, oracle):
     zs = np.array(zs)
     assert zs.size >= 40
     assert np.mean(zs < 0.1) >= 0.9, (np.mean(zs < 0.1), np.sort(zs)[-5:])
+
+
+def test_swarms_follow_the_reference_trajectory(ctx, oracle):
+    """The model-selection swarms of the analytic models (run_swarm_exact:
+    double-float positions from the reference's FP64 draws) against the
+    oracle's restarts of pso_fit_single_model on the same bands: the same
+    iteration count and the same best cost to 1e-10 for >= 95 % of the
+    (band, model, restart) runs (measured: all but a few runs of 600 bands,
+    which part on the FP32 cost evaluation)."""
+    batch = synth.config_uneven(8, seed=123)
+    res = ctx.fit_batch(batch, fit_all_models=True, method=abi.METHOD_LAPLACE, run_multi_bazin=False)
+    sw = ctx.swarm_results(batch.n_bands)
+    same, total = 0, 0
+    for s in range(batch.n_sources):
+        for k, (t, f, e) in enumerate(batch.bands_of(s)):
+            b = batch.source_band_offsets[s] + k
+            if res.model[b] < 0:
+                continue
+            band = oracle.Band(t, f, e)
+            for m in range(7):
+                for r in range(3):
+                    c, iters, _, _ = oracle.model_restart(m, band, r)
+                    row = sw[(b * 8 + m) * 3 + r]
+                    total += 1
+                    if int(row[1]) == iters and abs(row[0] - c) <= 1e-10 * max(abs(c), 1e-300):
+                        same += 1
+    assert total >= 400 and same >= 0.95 * total, (same, total)
+
+
+def test_model_selection_matches_oracle_on_600_bands(ctx, oracle):
+    """200 uneven sources, Laplace: the selected model agrees with the FP64
+    oracle for >= 99 % of bands (measured 99.3 %: the reference's choice is
+    chaotic at 1e-7, which the double-float swarms stay below), and the
+    polished per-model chi2 agree to a median 1e-9 (measured 1.1e-11)."""
+    batch = synth.config_uneven(200, seed=123)
+    res = ctx.fit_batch(batch, fit_all_models=True, method=abi.METHOD_LAPLACE, run_multi_bazin=False)
+    ref = oracle.fit_batch(batch, fit_all_models=True, method=abi.METHOD_LAPLACE, run_multi_bazin=False)
+    fitted = ref.model >= 0
+    assert np.array_equal(res.model >= 0, fitted)
+    agree = np.mean(res.model[fitted] == ref.model[fitted])
+    assert agree >= 0.99, agree
+    a, b = res.per_model_chi2[fitted], ref.per_model_chi2[fitted]
+    ok = np.isfinite(a) & np.isfinite(b)
+    rel = np.abs(a[ok] - b[ok]) / np.maximum(np.abs(b[ok]), 1e-300)
+    assert np.median(rel) < 1e-9, np.median(rel)
