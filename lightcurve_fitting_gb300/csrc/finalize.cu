@@ -510,9 +510,48 @@ __device__ void jacobi_eigen(double* a, int n, double* ev, double* V) {
     for (int i = 0; i < n; i++) ev[i] = a[i * n + i];
 }
 
+// ---------------------------------------------------------------------------
+// Bands grouped by their selected model (counting sort on 9 keys: MetzgerKN,
+// whose uncertainty and refinements cost the most, first, then models 0..6,
+// then the unfitted bands).  The per-band kernels take band_order[warp], so
+// the warps resident on an SM run one model's code and no warp slot is spent
+// on a band that selected another model.  The order inside a key is not
+// fixed; each band's computation does not depend on it.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ int band_order_key(const DeviceBatch& d, int b) {
+    const int m = d.out[b].model;
+    if (!d.stats[b].valid || m < 0) return 8;
+    return m == METZGER ? 0 : 1 + m;
+}
+__global__ void band_hist_kernel(DeviceBatch d) {
+    for (int b = blockIdx.x * blockDim.x + threadIdx.x; b < d.n_bands; b += gridDim.x * blockDim.x)
+        atomicAdd(&d.ctr->band_hist[band_order_key(d, b)], 1);
+}
+__global__ void band_scan_kernel(DeviceBatch d) {  // one thread
+    int run = 0;
+    for (int k = 0; k < 9; k++) {
+        const int v = d.ctr->band_hist[k];
+        d.ctr->band_hist[k] = run;
+        run += v;
+    }
+}
+__global__ void band_scatter_kernel(DeviceBatch d) {
+    for (int b = blockIdx.x * blockDim.x + threadIdx.x; b < d.n_bands; b += gridDim.x * blockDim.x)
+        d.band_order[atomicAdd(&d.ctr->band_hist[band_order_key(d, b)], 1)] = b;
+}
+void launch_band_order(const DeviceBatch& d, cudaStream_t s) {
+    if (d.n_bands == 0) return;
+    int grid = (d.n_bands + 255) / 256;
+    grid = grid < 1024 ? grid : 1024;
+    band_hist_kernel<<<grid, 256, 0, s>>>(d);
+    band_scan_kernel<<<1, 1, 0, s>>>(d);
+    band_scatter_kernel<<<grid, 256, 0, s>>>(d);
+}
+
 __global__ void laplace_kernel(DeviceBatch d) {
     int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     if (warp >= d.n_bands) return;
+    warp = d.band_order[warp];
     BandStats bs = d.stats[warp];
     BandOut& o = d.out[warp];
     if (!bs.valid || o.model < 0) return;
@@ -581,6 +620,7 @@ __global__ void refine_kernel(DeviceBatch d) {
     int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     int lane = threadIdx.x & 31;
     if (warp >= d.n_bands) return;
+    warp = d.band_order[warp];
     BandStats bs = d.stats[warp];
     BandOut& o = d.out[warp];
     if (!bs.valid || o.model < 0) return;

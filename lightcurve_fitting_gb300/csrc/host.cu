@@ -165,7 +165,7 @@ struct lcf_ctx {
     float* d_eps = nullptr;
     // device buffers (capacity-sized)
     DevArr times, flux, ferr, boff, soff, stats_b, obs, t64, f64, fe64, var64, uf64, mag64, up, ffa, ffb, res, fits, out, mb,
-        ctr, scratch, scratch64, scratch_svi, t0state, tasks[7], task_sorted, joint_flag, joint_src, joint_res,
+        ctr, scratch, scratch64, scratch_svi, t0state, tasks[7], task_sorted, band_order, joint_flag, joint_src, joint_res,
         joint_draws;
     int64_t joint_per_seed = 0;   // uniforms per seed held in joint_draws
     int n_joint = 0, joint_max_obs = 0, joint_max_d = 0;
@@ -316,7 +316,8 @@ extern "C" void lcf_ctx_destroy(lcf_ctx* ctx) {
     DevArr* all[] = {&ctx->times, &ctx->flux, &ctx->ferr, &ctx->boff, &ctx->soff, &ctx->stats_b, &ctx->obs,
                      &ctx->t64, &ctx->f64, &ctx->fe64, &ctx->var64, &ctx->uf64, &ctx->mag64, &ctx->up, &ctx->ffa, &ctx->ffb, &ctx->res,
                      &ctx->fits, &ctx->out, &ctx->mb, &ctx->ctr, &ctx->scratch, &ctx->scratch64, &ctx->scratch_svi,
-                     &ctx->t0state, &ctx->task_sorted, &ctx->joint_flag, &ctx->joint_src, &ctx->joint_res,
+                     &ctx->t0state, &ctx->task_sorted, &ctx->band_order, &ctx->joint_flag, &ctx->joint_src,
+                     &ctx->joint_res,
                      &ctx->joint_draws,
                      &ctx->bc_obs, &ctx->bc_params, &ctx->bc_costs, &ctx->bc_scratch, &ctx->plain_scr,
                      &ctx->sg_in, &ctx->sg_out, &ctx->sg_scratch};
@@ -496,6 +497,7 @@ static int prepare_layout(lcf_ctx* ctx, int n_sources, int n_bands, int64_t n_ob
         ctx->task_cap[s] = caps[s];
     }
     rc |= grow(ctx, ctx->task_sorted, (size_t)nb * 21 * sizeof(PsoTask));  // the largest of slots 1..6
+    rc |= grow(ctx, ctx->band_order, nb * sizeof(int32_t));
     if (rc) return rc;
     // stage-1 task list (bands, models, restarts; MultiBazin K = 1), longest first
     if (!same) {
@@ -653,6 +655,7 @@ static int prepare_layout(lcf_ctx* ctx, int n_sources, int n_bands, int64_t n_ob
     d.tasks[7] = nullptr;
     d.task_cap[7] = 0;
     d.task_sorted = (PsoTask*)ctx->task_sorted.p;
+    d.band_order = (int32_t*)ctx->band_order.p;
     d.n_joint = ctx->n_joint;
     d.joint_flag = ctx->n_joint > 0 ? (const uint8_t*)ctx->joint_flag.p : nullptr;
     d.joint_src = (const int32_t*)ctx->joint_src.p;
@@ -714,6 +717,7 @@ static void enqueue_pipeline(lcf_ctx* ctx) {
         launch_t0_pick(d, 3, 1, s); L++;
     }
     cudaEventRecordWithFlags(ctx->ev[4], s, cudaEventRecordExternal);
+    launch_band_order(d, s); L += 3;
     if (o.method == LCF_METHOD_SVI) launch_svi(d, s);
     else launch_laplace(d, s);
     L++;

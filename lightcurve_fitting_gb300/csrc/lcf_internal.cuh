@@ -220,6 +220,7 @@ struct Counters {
     unsigned long long lb_obs_evals_by_model[8];  // observation x (cost + gradient) evaluations, by model
     unsigned long long lb_fp64_obs_evals_by_model[8];  // of which in FP64 (ff range fallback)
     int32_t sort_hist[8][256];  // per slot: key histogram, then offsets, of the device task sort
+    int32_t band_hist[16];      // bands by selected model: histogram, then offsets (band_order)
     int32_t error;              // first error code raised on the device
     int32_t pad;
 };
@@ -261,6 +262,8 @@ struct DeviceBatch {
     PsoTask* tasks[8];      // per launch slot
     int task_cap[8];
     PsoTask* task_sorted;   // device-built task lists after the sort (capacity: the largest of slots 1..6)
+    int32_t* band_order;    // [n_bands] bands grouped by selected model (MetzgerKN first), for the
+                            // per-band uncertainty and refinement kernels
     Counters* ctr;
     float* scratch;         // MetzgerKN per-warp scratch: [warps][n_max][32]
     int64_t scratch_per_warp;
@@ -319,6 +322,8 @@ int launch_joint(const DeviceBatch& d, cudaStream_t s);
 size_t joint_smem_bytes(int max_obs, int max_d);
 // finalize.cu
 void launch_laplace(const DeviceBatch& d, cudaStream_t s);
+// bands grouped by selected model into d.band_order (three launches)
+void launch_band_order(const DeviceBatch& d, cudaStream_t s);
 void launch_refine(const DeviceBatch& d, cudaStream_t s);
 double probe_fp32_tflops(int num_sms);
 // polish.cu: FP64 peaks: out[m] = observation-term evaluations per second of

@@ -724,16 +724,17 @@ __device__ void svi_band(const DeviceBatch& d, int b) {
     }
 }
 
-// One warp per (band, model), model-major (the warps of a model run
-// together and share its code); a warp whose band selected another model
-// returns at once.
+// One warp per band, in band_order (grouped by selected model, so that the
+// warps of a model run together and share its code).
 #ifndef LCF_SVI_BLOCK
 #define LCF_SVI_BLOCK 128
 #endif
 __global__ void __launch_bounds__(LCF_SVI_BLOCK) svi_kernel(DeviceBatch d) {
     const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    if (warp >= d.n_bands * 8) return;
-    const int m = warp / d.n_bands, b = warp - m * d.n_bands;
+    if (warp >= d.n_bands) return;
+    const int b = d.band_order[warp];
+    const int m = d.out[b].model;
+    if (m < 0) return;
     switch (m) {
         case BAZIN: svi_band<BAZIN>(d, b); break;
         case VILLAR: svi_band<VILLAR>(d, b); break;
@@ -749,7 +750,7 @@ __global__ void __launch_bounds__(LCF_SVI_BLOCK) svi_kernel(DeviceBatch d) {
 void launch_svi(const DeviceBatch& d, cudaStream_t s) {
     if (d.n_bands == 0) return;
     int block = LCF_SVI_BLOCK;
-    int64_t threads = (int64_t)d.n_bands * 8 * 32;
+    int64_t threads = (int64_t)d.n_bands * 32;
     svi_kernel<<<(int)((threads + block - 1) / block), block, 0, s>>>(d);
 }
 
