@@ -634,7 +634,7 @@ __device__ void svi_band(const DeviceBatch& d, int b) {
     double b1t = 1.0, b2t = 1.0;
     double ema = -INFINITY, best_ema = -INFINITY, final_elbo = -INFINITY;
     int no_imp = 0, steps = 0;
-    // MetzgerKN: per step, lanes 0..3 sweep samples 0..3 (value + 4 derivatives per observation)
+    // MetzgerKN: per step, lanes 0..15 sweep samples 0..3 (value + 4 derivatives per observation)
     float* mscr = d.scratch_svi + 20 * bs.off;
     struct ObsTimes {
         const float4* o;
@@ -649,11 +649,34 @@ __device__ void svi_band(const DeviceBatch& d, int b) {
             double mu[MAXP], sg[MAXP];
 #pragma unroll
             for (int q = 0; q < np; q++) { mu[q] = __shfl_sync(FULL, mu_j, q); sg[q] = __shfl_sync(FULL, sg_j, q); }
-            if (lane < SVI_SAMPLES) {
-                const float* ep = eps_tab + ((size_t)step * SVI_SAMPLES + lane) * 7;
+            // lane 4 s + k sweeps sample s with the tangent of parameter k
+            // only (the four-tangent sweep's arithmetic, split over lanes)
+            const int smp = lane >> 2, tan = lane & 3;
+            bool mz_ok = false;
+            float mz_lp = 0.0f, mz_lpd = 0.0f;
+            if (lane < 4 * SVI_SAMPLES) {
+                const float* ep = eps_tab + ((size_t)step * SVI_SAMPLES + smp) * 7;
                 float pv[MAXP];
                 for (int q = 0; q < np; q++) pv[q] = (float)(mu[q] + sg[q] * (double)ep[q]);
-                metzger_dual_sweep(pv, (float)bs.t_last, otimes, n, mscr + (size_t)lane * 5 * n);
+                mz_ok = metzger_dual_raw<1>(pv, tan, (float)bs.t_last, otimes, n, mscr + (size_t)smp * 5 * n, mz_lp,
+                                            &mz_lpd);
+            }
+            __syncwarp();
+            // normalise by the peak (its tangent included): each lane its
+            // tangent column, then the value column
+            if (lane < 4 * SVI_SAMPLES) {
+                float* ms = mscr + (size_t)smp * 5 * n;
+                const float ip = 1.0f / mz_lp;
+                for (int q = 0; q < n; q++) {
+                    const float y = ms[q * 5] * ip;
+                    ms[q * 5 + 1 + tan] = mz_ok ? (ms[q * 5 + 1 + tan] - y * mz_lpd) * ip : 0.0f;
+                }
+            }
+            __syncwarp();
+            if (lane < 4 * SVI_SAMPLES && tan == 0) {
+                float* ms = mscr + (size_t)smp * 5 * n;
+                const float ip = 1.0f / mz_lp;
+                for (int q = 0; q < n; q++) ms[q * 5] = mz_ok ? ms[q * 5] * ip : 0.0f;
             }
             __syncwarp();
         }
