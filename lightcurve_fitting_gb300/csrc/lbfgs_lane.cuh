@@ -6,8 +6,10 @@
 // one FP64 operation per lane and a dot product is a three-step shuffle sum
 // inside each group of eight lanes (the four groups hold identical copies).
 // The curvature history is a shift register with the newest pair at index
-// 0, so every index is a compile-time constant and the history stays in
-// registers.  The scalar line-search state is uniform across the warp.
+// 0.  The two-loop recursion and the shift are not unrolled (the history
+// then lives in local memory, cached in L1): the polish is bound by
+// instruction fetch, and the unrolled loops were ~16 KB of its code per
+// model.  The scalar line-search state is uniform across the warp.
 //
 // Arithmetic is that of lbfgs.cuh except the order of the terms of each dot
 // product (a tree instead of a left-to-right sum) and 1 / (y.s) being kept
@@ -109,26 +111,21 @@ __device__ double lane_lbfgs_polish(Ctx& c, double& pj, double pso_cost) {
         double gamma = cm > 0 ? lb_div(dot8(S[0], Y[0]), dot8(Y[0], Y[0])) : 1.0;
         // two-loop recursion: newest (index 0) to oldest, then back
         double q = gj, alpha[M];
-#pragma unroll
-        for (int k = 0; k < M; k++) {
-            alpha[k] = 0.0;
-            if (k < cm) {
-                alpha[k] = rho[k] * dot8(S[k], q);
-                q -= Y[k] * alpha[k];
-            }
+#pragma unroll 1
+        for (int k = 0; k < cm; k++) {
+            alpha[k] = rho[k] * dot8(S[k], q);
+            q -= Y[k] * alpha[k];
         }
         double r = q * gamma;
-#pragma unroll
-        for (int k = M - 1; k >= 0; k--) {
-            if (k < cm) {
-                double beta = dot8(Y[k], r) * rho[k];
-                r += S[k] * (alpha[k] - beta);
-            }
+#pragma unroll 1
+        for (int k = cm - 1; k >= 0; k--) {
+            double beta = dot8(Y[k], r) * rho[k];
+            r += S[k] * (alpha[k] - beta);
         }
         double dj = -r, xnj, gnj, fnew;
         if (!lane_linesearch(c, xj, f, gj, dj, xnj, fnew, gnj)) { ok = false; break; }
         double sj = xnj - xj, yj = gnj - gj;
-#pragma unroll
+#pragma unroll 1
         for (int k = M - 1; k > 0; k--) { S[k] = S[k - 1]; Y[k] = Y[k - 1]; rho[k] = rho[k - 1]; }
         S[0] = sj;
         Y[0] = yj;
