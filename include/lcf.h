@@ -250,7 +250,9 @@ int lcf_probe_fp64(lcf_ctx* ctx, double* out9);
 int lcf_probe_ff(lcf_ctx* ctx, double* out80);
 
 /* Diagnostic: raw swarm results of the last fit, 21 doubles per result slot
- * (cost, iterations, particle evaluations, 18 parameters).  Slots
+ * (cost, iterations, particle evaluations, 18 parameters; the swarms of the
+ * models other than MetzgerKN report their best position at double-float
+ * precision and, in model selection, an FP32 estimate of its cost).  Slots
  * [0, 24 n_bands) hold (band * 8 + model) * 3 + restart of the model
  * selection, [24 n_bands, 32 n_bands) the profile-t0 runs, [32 n_bands,
  * 44 n_bands) the MultiBazin runs.  A slot that did not run has cost NaN. */

@@ -1206,7 +1206,8 @@ extern "C" int lcf_debug_swarm_results(lcf_ctx* ctx, double* out, int64_t max_ro
         o[0] = h[r].iters < 0 ? std::nan("") : h[r].cost;
         o[1] = h[r].iters;
         o[2] = h[r].evals;
-        for (int j = 0; j < MB_MAXP; j++) o[3 + j] = h[r].params[j];
+        for (int j = 0; j < MB_MAXP; j++)
+            o[3 + j] = j < 7 ? pso_param(h[r], j) : (h[r].pad[0] == 1.0f ? 0.0 : (double)h[r].params[j]);
     }
     return 0;
 }

@@ -32,6 +32,14 @@ namespace lcf {
 #define FULL 0xffffffffu
 
 // Best of the three restarts of (band, MODEL), then the polish.
+// Two swarm result costs closer than the FP32 estimate's error (3e-5 of the
+// reference value; the special values 1e99, +inf and the Villar constraint's
+// 1e12 + 1e4 c compare as they are).
+__device__ __forceinline__ bool swarm_cost_tie(double a, double ref) {
+    if (!(fabs(ref) < 1e11) || !(fabs(a) < 1e11)) return a == ref;
+    return fabs(a - ref) <= 3e-5 * fabs(ref);
+}
+
 template <int MODEL>
 __device__ void polish_band(const DeviceBatch& d, int b) {
     const BandStats bs = d.stats[b];
@@ -70,6 +78,36 @@ __device__ void polish_band(const DeviceBatch& d, int b) {
         double t0_lo = fmax(bs.t_first - 30.0, c_lo[MODEL][t0i]);
         double t0_hi = fmin(bs.t_peak + 10.0, c_hi[MODEL][t0i]);
         if (j == t0i && t0_lo < t0_hi) { c.lo_j = t0_lo; c.hi_j = t0_hi; }
+        // the restarts' swarms report FP32 estimates of their best costs: the
+        // chosen restart's cost, and the choice among restarts within the
+        // estimates' error of it, are settled on accurate costs (the first
+        // strict minimum, as the reference's restart loop)
+        {
+            auto accurate = [&](int r) {
+                const double pr = j < np ? pso_param(R[r], j) : 0.0;
+                double f, g_unused;
+                c.cost_grad(pr, f, g_unused, false);
+                c.evals--;  // not a polish evaluation
+                return f;
+            };
+            double acc[3] = {INFINITY, INFINITY, INFINITY};
+            int nc = 0;
+            for (int r = 0; r < 3; r++)
+                if (R[r].iters >= 0 && (r == best_r || swarm_cost_tie(R[r].cost, best_c))) {
+                    acc[r] = accurate(r);
+                    nc++;
+                }
+            if (nc > 1) {
+                best_r = -1;
+                best_c = INFINITY;
+                for (int r = 0; r < 3; r++)
+                    if (acc[r] < best_c) { best_c = acc[r]; best_r = r; }
+                if (best_r < 0) best_r = 0;
+                pj = j < np ? pso_param(R[best_r], j) : 0.0;
+            } else {
+                best_c = acc[best_r];
+            }
+        }
         cost = lane_lbfgs_polish(c, pj, best_c);
         if (lane == 0) {
             atomicAdd(&d.ctr->lb_polishes, 1ull);

@@ -452,10 +452,10 @@ __device__ __forceinline__ void run_swarm(const DeviceBatch& d, const PsoTask& t
 //   * each particle's cost is evaluated in FP32 at the position's leading
 //     float, lane-split as in the other swarms (deciding near-tied FP32
 //     comparisons on accurate costs was measured and changed no result);
-//   * the run's result cost is the accurate cost of its best position (the
-//     polish's double-float cost, LaneLb), so that the choice among restarts
-//     and the t0 search's picks compare accurate costs, and the best position
-//     is stored as double-float pairs (pso_param).
+//   * the best position is stored as double-float pairs (pso_param); the
+//     t0 search's runs report the accurate cost of their best position (the
+//     polish's double-float cost, LaneLb) for the picks, and the polish
+//     settles the model-selection restarts on accurate costs.
 // ---------------------------------------------------------------------------
 __device__ __forceinline__ bool ff_lt(ff a, ff b) { return a.hi < b.hi || (a.hi == b.hi && a.lo < b.lo); }
 __device__ __forceinline__ bool ff_le(ff a, ff b) { return a.hi < b.hi || (a.hi == b.hi && a.lo <= b.lo); }
@@ -726,9 +726,11 @@ __device__ __forceinline__ void run_swarm_exact(const DeviceBatch& d, const PsoT
             break;
         }
     }
-    // ---- result: the accurate cost of the best position
+    // ---- result: for the t0 search, the accurate cost of the best position
+    // (its picks compare it with the polished cost); model-selection runs
+    // report the FP32 estimate, which the polish settles
     double rc = gc;
-    if (gc < INFINITY) {
+    if (fixed && gc < INFINITY) {
         LaneLb<KIND> lc;
         exact_cost_setup(lc, d, bs, task.flags);
         ff gp[MAXD];
