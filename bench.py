@@ -61,6 +61,15 @@ MUFU_PER_ODE_STEP = 14
 # including the Kahan update of 4 adds); MetzgerKN ~60 per ODE step.
 FP32_PER_EVAL = {0: 24, 1: 34, 2: 30, 3: 30, 4: 26, 5: 30, 6: 32, 7: 16, 8: 24, 9: 34, 10: 44, 11: 54}
 FP32_PER_ODE_STEP = 60
+# DRAM traffic (dram__bytes_read.sum + dram__bytes_write.sum) per unit of
+# work of the two rooflined kernels, from one ncu capture of the 1,000-source
+# uneven workload (profiles/ncu_polish_swarm_1k.md): the polish moved 4.57 GB
+# for 1.507e8 observation-term evaluations, the model-selection swarm 88.6 MB
+# for 6.372e9 particle-observation evaluations.  A launch's traffic is scaled
+# from these by its own units (the traffic is mostly local-memory spill
+# write-back, which grows with the work).
+DRAM_BYTES_PER_LB_OBS_EVAL = 4.574e9 / 1.507e8
+DRAM_BYTES_PER_PSO_OBS_EVAL = 88.6e6 / 6.372e9
 
 
 def parse():
@@ -305,7 +314,9 @@ def run_fused(args, ws, rank, local):
         "peak": peaks["mufu_gops"] if bound_sfu else peaks["fp32_tflops"],
         "unit": "Gop/s" if bound_sfu else "TFLOP/s",
         "frac": frac_mufu if bound_sfu else frac_fp32,
-        "traffic": None,
+        "traffic": float(sum(ev)) * DRAM_BYTES_PER_PSO_OBS_EVAL,
+        "traffic_source": "ncu DRAM bytes per particle-observation evaluation of the 1,000-source launch, "
+                          "scaled by this launch's evaluations",
         "kernel": "pso_kernel<7> (model-selection swarm launch)",
         "peak_source": "measured live by lcf_probe_peaks (dependent ex2 / FMA chains over a full grid)",
         "other_pipe": ({"bound": "fp32", "achieved": fp32_rate, "peak": peaks["fp32_tflops"], "unit": "TFLOP/s",
@@ -333,7 +344,10 @@ def run_fused(args, ws, rank, local):
         "peak": lb_peak,
         "unit": "observation evaluations/s (value + gradient + cost term, double-float; FP64 where out of range)",
         "frac": lb_rate / lb_peak if lb_peak else None,
-        "traffic": None,
+        "traffic": float(sum(lb_ev[:7])) * DRAM_BYTES_PER_LB_OBS_EVAL,
+        "traffic_source": "ncu DRAM bytes per observation-term evaluation of the 1,000-source launch, scaled by "
+                          "this launch's evaluations (local-memory spill write-back: the resident threads' "
+                          "stacks exceed L2)",
         "kernel": "lbfgs_kernel (L-BFGS polish, the largest stage)",
         "peak_source": "measured live: the polish's own observation terms streamed at full occupancy "
                        "(lcf_probe_ff for the double-float term, lcf_probe_fp64 for the FP64 fallback), "
