@@ -173,6 +173,49 @@ int lcf_fit_parametric_device(lcf_ctx* ctx, const lcf_bands_csr* dev_bands,
 int lcf_download_outputs(lcf_ctx* ctx, lcf_fit_outputs* out);
 
 /*
+ * Selected swarm results supplied by the caller, one row per CSR band: the
+ * fields of the reference's GpuPsoBandResult (src/parametric.rs:3101-3114)
+ * that the finalisation reads, and optionally uncertainty outputs computed
+ * elsewhere (the reference's GPU SVI, src/gpu_cuda.rs:1315-1422).
+ *   model:          [n_bands] model id 0..7, or -1 to skip the band
+ *                   (an empty pso_params in the reference)
+ *   pso_params:     [n_bands * 7], the first n_params(model) are read
+ *   pso_cost:       [n_bands] or NULL (NaN), copied to pso_chi2
+ *   per_model_chi2: [n_bands * 8] or NULL (NaN), copied through
+ *   svi_mu, svi_log_sigma: [n_bands * 7] or NULL; svi_elbo: [n_bands] or
+ *                   NULL.  With svi_mu and svi_log_sigma given the
+ *                   uncertainty stage is not run (the *_with_gpu_svi forms).
+ */
+typedef struct lcf_pso_selection {
+    const int32_t* model;
+    const double* pso_params;
+    const double* pso_cost;
+    const double* per_model_chi2;
+    const double* svi_mu;
+    const double* svi_log_sigma;
+    const double* svi_elbo;
+} lcf_pso_selection;
+
+/*
+ * Batched finalisation of externally selected fits on the GPU, per band:
+ *   finalize_parametric_from_gpu (src/parametric.rs:3126-3257): SVI from
+ *     pso_params (1000 steps, 4 samples, lr 0.01) or Laplace at pso_params
+ *     (`method`), then profile_t0_refine, profile_refine_all and the
+ *     magnitude chi2;
+ *   finalize_parametric_with_gpu_svi (:3298-3421) and
+ *   finalize_all_models_with_gpu_svi (:3429-3553): the same from the
+ *     supplied svi_mu / svi_log_sigma / svi_elbo, without the uncertainty
+ *     stage (`method` is then ignored).
+ * The band preparation is fit_parametric_model's (:3581-3632); a band it
+ * skips gets model -1.  Outputs as lcf_fit_parametric_batch's; rank is the
+ * band's position in the by-count order, per_model_params and MultiBazin
+ * come back NaN / 0 (the caller holds its own).  A (band, model) pair list,
+ * as finalize_all_models_with_gpu_svi takes, is a CSR with the band repeated.
+ */
+int lcf_finalize_batch(lcf_ctx* ctx, const lcf_bands_csr* bands, const lcf_pso_selection* sel,
+                       int method, lcf_fit_outputs* out);
+
+/*
  * The plain FP64 GPU form of the same fit, the baseline the fused pipeline is
  * measured against: PSO model selection (one thread per particle, FP64,
  * observations from global memory, synchronous global best), L-BFGS polish,

@@ -49,6 +49,19 @@ class FitOptions(C.Structure):
     ]
 
 
+class PsoSelection(C.Structure):
+    """lcf_pso_selection: caller-selected fits, one row per CSR band."""
+    _fields_ = [
+        ("model", C.c_void_p),
+        ("pso_params", C.c_void_p),
+        ("pso_cost", C.c_void_p),
+        ("per_model_chi2", C.c_void_p),
+        ("svi_mu", C.c_void_p),
+        ("svi_log_sigma", C.c_void_p),
+        ("svi_elbo", C.c_void_p),
+    ]
+
+
 class FitOutputs(C.Structure):
     _fields_ = [
         ("model", C.c_void_p),
@@ -184,3 +197,27 @@ def options(fit_all_models=True, method=METHOD_SVI, forced_model=-1, run_multi_b
     o.run_multi_bazin = int(bool(run_multi_bazin))
     o.joint_multiband = int(bool(joint_multiband))
     return o
+
+
+def selection_struct(n_bands, model, pso_params, pso_cost=None, per_model_chi2=None, svi_mu=None,
+                     svi_log_sigma=None, svi_elbo=None, keep=None) -> PsoSelection:
+    """PsoSelection over host arrays: model [n_bands] (-1 skips a band),
+    pso_params [n_bands, 7], optional pso_cost [n_bands], per_model_chi2
+    [n_bands, 8], svi_mu / svi_log_sigma [n_bands, 7], svi_elbo [n_bands]."""
+    def arr(a, dtype, shape):
+        if a is None:
+            return None
+        v = np.ascontiguousarray(a, dtype=dtype)
+        if v.size != int(np.prod(shape)):
+            raise ValueError(f"selection array of size {v.size}, expected shape {shape}")
+        return v
+    fields = [arr(model, np.int32, (n_bands,)), arr(pso_params, np.float64, (n_bands, 7)),
+              arr(pso_cost, np.float64, (n_bands,)), arr(per_model_chi2, np.float64, (n_bands, 8)),
+              arr(svi_mu, np.float64, (n_bands, 7)), arr(svi_log_sigma, np.float64, (n_bands, 7)),
+              arr(svi_elbo, np.float64, (n_bands,))]
+    if keep is not None:
+        keep.extend(f for f in fields if f is not None)
+    s = PsoSelection()
+    (s.model, s.pso_params, s.pso_cost, s.per_model_chi2, s.svi_mu, s.svi_log_sigma,
+     s.svi_elbo) = [ptr(f) if f is not None else None for f in fields]
+    return s

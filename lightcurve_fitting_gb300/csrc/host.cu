@@ -171,7 +171,7 @@ struct lcf_ctx {
     int n_joint = 0, joint_max_obs = 0, joint_max_d = 0;
     int64_t task_cap[7] = {0, 0, 0, 0, 0, 0, 0};
     // pinned staging
-    DevArr h_in, h_out;
+    DevArr h_in, h_out, h_sel;
     // band-cost scratch
     DevArr bc_obs, bc_params, bc_costs, bc_scratch;
     // ELBO-gradient check buffers
@@ -325,6 +325,7 @@ extern "C" void lcf_ctx_destroy(lcf_ctx* ctx) {
     for (auto& a : ctx->tasks) free_arr(a);
     if (ctx->h_in.p) cudaFreeHost(ctx->h_in.p);
     if (ctx->h_out.p) cudaFreeHost(ctx->h_out.p);
+    if (ctx->h_sel.p) cudaFreeHost(ctx->h_sel.p);
     if (ctx->d_draws) cudaFree(ctx->d_draws);
     if (ctx->d_draws64) cudaFree(ctx->d_draws64);
     if (ctx->d_draws15) cudaFree(ctx->d_draws15);
@@ -932,12 +933,10 @@ static int check_opts(lcf_ctx* ctx, const lcf_fit_options* o) {
     return 0;
 }
 
-extern "C" int lcf_fit_parametric_batch(lcf_ctx* ctx, const lcf_bands_csr* in, const lcf_fit_options* o,
-                                        lcf_fit_outputs* out) {
-    if (!ctx) return LCF_E_INVALID;
-    if (!in || !out) return set_err(ctx, LCF_E_INVALID, "null argument");
-    if (int rc = check_opts(ctx, o)) return rc;
-    CK(cudaSetDevice(ctx->device));
+// Validates a host CSR, prepares the layout for options `o` and queues the
+// copies of its observations and offsets to the device through pinned
+// staging; *in_bytes = the bytes copied.
+static int stage_host_batch(lcf_ctx* ctx, const lcf_bands_csr* in, const lcf_fit_options& o, size_t* in_bytes) {
     int ns = in->n_sources, nb = in->n_bands;
     if (ns < 0 || nb < 0 || !in->source_band_offsets || (nb > 0 && !in->band_obs_offsets))
         return set_err(ctx, LCF_E_INVALID, "bad CSR header");
@@ -946,10 +945,9 @@ extern "C" int lcf_fit_parametric_batch(lcf_ctx* ctx, const lcf_bands_csr* in, c
     if (n_obs > 0 && (!in->times || !in->flux || !in->flux_err)) return set_err(ctx, LCF_E_INVALID, "null data array");
     ctx->h_boff.assign(in->band_obs_offsets, in->band_obs_offsets + nb + 1);
     ctx->h_soff.assign(in->source_band_offsets, in->source_band_offsets + ns + 1);
-    if (int rc = prepare_layout(ctx, ns, nb, n_obs, *o)) return rc;
-    // stage the inputs through pinned memory
-    size_t in_bytes = (size_t)n_obs * 24 + (size_t)(nb + 1) * 8 + (size_t)(ns + 1) * 4;
-    if (grow_pinned(ctx, ctx->h_in, in_bytes)) return LCF_E_NOMEM;
+    if (int rc = prepare_layout(ctx, ns, nb, n_obs, o)) return rc;
+    size_t bytes = (size_t)n_obs * 24 + (size_t)(nb + 1) * 8 + (size_t)(ns + 1) * 4;
+    if (grow_pinned(ctx, ctx->h_in, bytes)) return LCF_E_NOMEM;
     char* hp = (char*)ctx->h_in.p;
     std::memcpy(hp, in->times, (size_t)n_obs * 8);
     std::memcpy(hp + (size_t)n_obs * 8, in->flux, (size_t)n_obs * 8);
@@ -965,12 +963,111 @@ extern "C" int lcf_fit_parametric_batch(lcf_ctx* ctx, const lcf_bands_csr* in, c
     CK(cudaMemcpyAsync(ctx->boff.p, hp + (size_t)n_obs * 24, (size_t)(nb + 1) * 8, cudaMemcpyHostToDevice, s));
     CK(cudaMemcpyAsync(ctx->soff.p, hp + (size_t)n_obs * 24 + (size_t)(nb + 1) * 8, (size_t)(ns + 1) * 4,
                        cudaMemcpyHostToDevice, s));
-    if (nb == 0) return 0;
+    *in_bytes = bytes;
+    return 0;
+}
+
+extern "C" int lcf_fit_parametric_batch(lcf_ctx* ctx, const lcf_bands_csr* in, const lcf_fit_options* o,
+                                        lcf_fit_outputs* out) {
+    if (!ctx) return LCF_E_INVALID;
+    if (!in || !out) return set_err(ctx, LCF_E_INVALID, "null argument");
+    if (int rc = check_opts(ctx, o)) return rc;
+    CK(cudaSetDevice(ctx->device));
+    size_t in_bytes = 0;
+    if (int rc = stage_host_batch(ctx, in, *o, &in_bytes)) return rc;
+    if (in->n_bands == 0) return 0;
     choose_launch(ctx);
     if (int rc = run_pipeline(ctx)) return rc;
     if (int rc = finish_stats(ctx)) return rc;
     record_launch(ctx);
     ctx->stats.h2d_bytes = (double)in_bytes;
+    return unpack_outputs(ctx, out);
+}
+
+// ---------------------------------------------------------------------------
+// Batched finalisation of caller-selected fits (lcf_finalize_batch): band
+// preparation, then the uncertainty stage unless its outputs are supplied,
+// then the refinements and the magnitude chi2 -- the per-band kernels of the
+// fused pipeline, fed from the caller's selection instead of the swarms.
+// Stage events as in the fused pipeline (the swarm and polish stages empty).
+// ---------------------------------------------------------------------------
+static void enqueue_finalize(lcf_ctx* ctx, bool given, size_t sel_bytes) {
+    const DeviceBatch& d = ctx->db;
+    cudaStream_t s = ctx->stream;
+    int64_t L = 0;
+    cudaEventRecord(ctx->ev[0], s);
+    cudaMemsetAsync(ctx->ctr.p, 0, sizeof(Counters), s);
+    launch_prep(d, s); L++;
+    // the caller's selection rows (pinned staging)
+    cudaMemcpyAsync(ctx->out.p, (char*)ctx->h_sel.p, sel_bytes, cudaMemcpyHostToDevice, s);
+    cudaEventRecord(ctx->ev[1], s);
+    cudaEventRecord(ctx->ev[2], s);
+    cudaEventRecord(ctx->ev[3], s);
+    cudaEventRecord(ctx->ev[8], s);
+    launch_band_order(d, s); L += 3;
+    cudaEventRecord(ctx->ev[4], s);
+    if (!given) {
+        if (ctx->opts.method == LCF_METHOD_SVI) launch_svi(d, s);
+        else launch_laplace(d, s);
+        L++;
+    }
+    cudaEventRecord(ctx->ev[5], s);
+    launch_refine(d, s); L++;
+    cudaEventRecord(ctx->ev[6], s);
+    cudaEventRecord(ctx->ev[7], s);
+    ctx->launches = L;
+}
+
+extern "C" int lcf_finalize_batch(lcf_ctx* ctx, const lcf_bands_csr* in, const lcf_pso_selection* sel, int method,
+                                  lcf_fit_outputs* out) {
+    if (!ctx) return LCF_E_INVALID;
+    if (!in || !sel || !out) return set_err(ctx, LCF_E_INVALID, "null argument");
+    const bool given = sel->svi_mu != nullptr || sel->svi_log_sigma != nullptr;
+    if (given && !(sel->svi_mu && sel->svi_log_sigma))
+        return set_err(ctx, LCF_E_INVALID, "svi_mu and svi_log_sigma are given together");
+    if (!given && method != LCF_METHOD_SVI && method != LCF_METHOD_LAPLACE)
+        return set_err(ctx, LCF_E_INVALID, "method must be LCF_METHOD_SVI or LCF_METHOD_LAPLACE");
+    const int nb = in->n_bands;
+    if (nb > 0 && (!sel->model || !sel->pso_params)) return set_err(ctx, LCF_E_INVALID, "null selection array");
+    for (int b = 0; b < nb; b++)
+        if (sel->model[b] < -1 || sel->model[b] > 7) return set_err(ctx, LCF_E_INVALID, "selection model out of range");
+    CK(cudaSetDevice(ctx->device));
+    lcf_fit_options o;
+    o.fit_all_models = 0;
+    o.method = given ? LCF_METHOD_SVI : method;
+    o.forced_model = -1;
+    o.run_multi_bazin = 0;
+    o.joint_multiband = 0;
+    size_t in_bytes = 0;
+    if (int rc = stage_host_batch(ctx, in, o, &in_bytes)) return rc;
+    if (nb == 0) return 0;
+    // the per-band selection rows, in the device layout of the selected fit
+    const size_t sel_bytes = (size_t)nb * sizeof(BandOut);
+    if (grow_pinned(ctx, ctx->h_sel, sel_bytes)) return LCF_E_NOMEM;
+    BandOut* rows = (BandOut*)ctx->h_sel.p;
+    const double nan = std::nan("");
+    for (int b = 0; b < nb; b++) {
+        BandOut& r = rows[b];
+        const int m = sel->model[b];
+        const int np = m >= 0 ? n_params_of(m) : 0;
+        r.model = m;
+        r.svi_steps = 0;
+        r.pso_cost = sel->pso_cost ? sel->pso_cost[b] : nan;
+        for (int j = 0; j < MAXP; j++) {
+            r.pso_params[j] = j < np ? sel->pso_params[b * 7 + j] : nan;
+            r.mu[j] = given && j < np ? sel->svi_mu[b * 7 + j] : nan;
+            r.log_sigma[j] = given && j < np ? sel->svi_log_sigma[b * 7 + j] : nan;
+        }
+        r.elbo = given && sel->svi_elbo ? sel->svi_elbo[b] : nan;
+        r.mag_chi2 = nan;
+        for (int k = 0; k < 8; k++) r.per_chi2[k] = sel->per_model_chi2 ? sel->per_model_chi2[b * 8 + k] : nan;
+    }
+    cudaGetLastError();
+    enqueue_finalize(ctx, given, sel_bytes);
+    CK(cudaGetLastError());
+    if (int rc = finish_stats(ctx)) return rc;
+    ctx->stats.pso_tasks = 0;
+    ctx->stats.h2d_bytes = (double)(in_bytes + sel_bytes);
     return unpack_outputs(ctx, out);
 }
 

@@ -41,6 +41,8 @@ def load(path: str = LIB_PATH):
     L.lcf_fit_parametric_batch.argtypes = [vp, C.POINTER(abi.BandsCSR), C.POINTER(abi.FitOptions),
                                            C.POINTER(abi.FitOutputs)]
     L.lcf_fit_parametric_device.argtypes = [vp, C.POINTER(abi.BandsCSR), C.POINTER(abi.FitOptions)]
+    L.lcf_finalize_batch.argtypes = [vp, C.POINTER(abi.BandsCSR), C.POINTER(abi.PsoSelection), i,
+                                     C.POINTER(abi.FitOutputs)]
     L.lcf_fit_plain_device.argtypes = [vp, C.POINTER(abi.BandsCSR), C.POINTER(abi.FitOptions)]
     L.lcf_download_outputs.argtypes = [vp, C.POINTER(abi.FitOutputs)]
     L.lcf_ctx_stream.argtypes = [vp]
@@ -115,6 +117,20 @@ class Context:
         outs = res.as_struct()
         self._check(self.L.lcf_fit_parametric_batch(self.h, C.byref(csr), C.byref(opts), C.byref(outs)),
                     "lcf_fit_parametric_batch")
+        return res
+
+    def finalize_batch(self, batch, model, pso_params, pso_cost=None, per_model_chi2=None, svi_mu=None,
+                       svi_log_sigma=None, svi_elbo=None, method=abi.METHOD_SVI) -> abi.FitResult:
+        """lcf_finalize_batch: uncertainty (unless svi_mu / svi_log_sigma are
+        given), refinements and magnitude chi2 of caller-selected fits."""
+        keep = []
+        csr = abi.csr_struct(batch, keep)
+        sel = abi.selection_struct(batch.n_bands, model, pso_params, pso_cost, per_model_chi2, svi_mu,
+                                   svi_log_sigma, svi_elbo, keep)
+        res = abi.FitResult(batch.n_bands)
+        outs = res.as_struct()
+        self._check(self.L.lcf_finalize_batch(self.h, C.byref(csr), C.byref(sel), int(method), C.byref(outs)),
+                    "lcf_finalize_batch")
         return res
 
     def fit_device(self, dev_ptrs: dict, n_sources: int, n_bands: int, fit_all_models=True,

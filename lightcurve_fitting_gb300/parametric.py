@@ -170,3 +170,148 @@ def fit_parametric_model(bands: Dict[str, dict], model: str, fit_all_models: boo
                          ctx=None):
     """fit_parametric_model with a forced model (python/src/lib.rs:219-245)."""
     return fit_batch_parametric([bands], fit_all_models, method, model, ctx)[0]
+
+
+# ---------------------------------------------------------------------------
+# Batched finalisation of externally selected fits (lcf_finalize_batch):
+# finalize_parametric_from_gpu, finalize_parametric_with_gpu_svi and
+# finalize_all_models_with_gpu_svi (src/parametric.rs:3126-3553).  A
+# ``gpu_results`` entry is a dict with the fields of GpuPsoBandResult
+# (:3101-3114): "model" (name), "pso_params", "pso_cost", "per_model_chi2"
+# (name -> value or None), optionally "per_model_params" and "multi_bazin".
+# An ``svi_outputs`` entry is (mu, log_sigma, elbo).
+# ---------------------------------------------------------------------------
+def _fittable(bd: dict) -> bool:
+    v = np.asarray(bd["values"], np.float64)
+    return v.size > 0 and float(np.max(v)) > 0.0
+
+
+def _finalize_run(entries, gpu_rows, svi_rows, method: int, ctx):
+    """One lcf_finalize_batch call over (band dict, gpu result, svi output or
+    None) triples, each its own source; returns the FitResult."""
+    t, f, e, bo = [], [], [], [0]
+    nb = len(entries)
+    model = np.full(nb, -1, np.int32)
+    pso = np.full((nb, 7), np.nan)
+    cost = np.full(nb, np.nan)
+    given = svi_rows is not None
+    mu = np.full((nb, 7), np.nan) if given else None
+    ls = np.full((nb, 7), np.nan) if given else None
+    elbo = np.full(nb, np.nan) if given else None
+    for i, bd in enumerate(entries):
+        tt = np.asarray(bd["times"], np.float64)
+        t.append(tt)
+        f.append(np.asarray(bd["values"], np.float64))
+        e.append(np.asarray(bd["errors"], np.float64))
+        bo.append(bo[-1] + tt.size)
+        g = gpu_rows[i]
+        m = _model_id(g["model"])
+        n = abi.N_PARAMS[m]
+        p = np.asarray(g["pso_params"], np.float64)
+        model[i] = m
+        pso[i, :min(n, p.size)] = p[:n]
+        cost[i] = g.get("pso_cost", np.nan) if g.get("pso_cost") is not None else np.nan
+        if given:
+            smu, sls, sel = svi_rows[i]
+            mu[i, :n] = np.asarray(smu, np.float64)[:n]
+            ls[i, :n] = np.asarray(sls, np.float64)[:n]
+            elbo[i] = sel
+    cat = lambda xs: np.concatenate(xs) if xs else np.zeros(0)
+    batch = PhotometryBatch(cat(t), cat(f), cat(e), np.asarray(bo, np.int64), np.arange(nb + 1, dtype=np.int32),
+                            np.zeros(nb, np.int32), "finalize")
+    ctx = ctx or default_context()
+    return ctx.finalize_batch(batch, model, pso, cost, None, mu, ls, elbo, method=method)
+
+
+def _finalized(res, i, name, g, method: int, per_params, mb):
+    m = int(res.model[i])
+    n = abi.N_PARAMS[m]
+    r = {
+        "band": name,
+        "model": abi.MODEL_NAMES[m],
+        "pso_params": [float(x) for x in np.asarray(g["pso_params"], np.float64)],
+        "pso_chi2": _opt(g.get("pso_cost")),
+        "svi_mu": [float(x) for x in res.svi_mu[i, :n]],
+        "svi_log_sigma": [float(x) for x in res.svi_log_sigma[i, :n]],
+        "svi_elbo": _opt(res.svi_elbo[i]),
+        "n_obs": int(res.n_obs[i]),
+        "mag_chi2": _opt(res.mag_chi2[i]),
+        "per_model_chi2": dict(g.get("per_model_chi2") or {}),
+        "uncertainty_method": "Svi" if method == abi.METHOD_SVI else "Laplace",
+    }
+    if per_params:
+        r["per_model_params"] = per_params
+    if mb is not None:
+        r["multi_bazin"] = mb
+    return r
+
+
+def _sorted_entries(flux_bands: Dict[str, dict]):
+    """fit_parametric_model's band preparation order: fittable bands by
+    observation count, descending (ties in the dict's order)."""
+    names = [k for k, bd in flux_bands.items() if _fittable(bd)]
+    return sorted(names, key=lambda k: -len(flux_bands[k]["values"]))
+
+
+def _finalize_sorted(flux_bands, gpu_results, svi_outputs, method: int, ctx):
+    names = _sorted_entries(flux_bands)
+    pairs = []
+    for idx, name in enumerate(names):
+        if idx >= len(gpu_results) or (svi_outputs is not None and idx >= len(svi_outputs)):
+            break
+        if len(gpu_results[idx]["pso_params"]) == 0:
+            continue
+        pairs.append((idx, name))
+    if not pairs:
+        return []
+    res = _finalize_run([flux_bands[n] for _, n in pairs], [gpu_results[i] for i, _ in pairs],
+                        None if svi_outputs is None else [svi_outputs[i] for i, _ in pairs], method, ctx)
+    out = []
+    for k, (idx, name) in enumerate(pairs):
+        g = gpu_results[idx]
+        out.append(_finalized(res, k, name, g, method, g.get("per_model_params") or {},
+                              g.get("multi_bazin") if idx == 0 else None))
+    return out
+
+
+def finalize_parametric_from_gpu(flux_bands: Dict[str, dict], gpu_results: Sequence[dict], method: str = "svi",
+                                 ctx=None) -> List[dict]:
+    """finalize_parametric_from_gpu (src/parametric.rs:3126-3257): per band,
+    in the by-count order, SVI from (or Laplace at) the supplied PSO
+    parameters, then the refinements and the magnitude chi2."""
+    if not flux_bands or not gpu_results:
+        return []
+    return _finalize_sorted(flux_bands, gpu_results, None, _method(method), ctx)
+
+
+def finalize_parametric_with_gpu_svi(flux_bands: Dict[str, dict], gpu_results: Sequence[dict],
+                                     svi_outputs: Sequence[tuple], ctx=None) -> List[dict]:
+    """finalize_parametric_with_gpu_svi (src/parametric.rs:3298-3421): the
+    same from supplied SVI outputs."""
+    if not flux_bands or not gpu_results or not svi_outputs:
+        return []
+    return _finalize_sorted(flux_bands, gpu_results, svi_outputs, abi.METHOD_SVI, ctx)
+
+
+def finalize_all_models_with_gpu_svi(flux_bands: Dict[str, dict], gpu_results: Sequence[dict],
+                                     svi_outputs: Sequence[tuple], band_names: Sequence[str], ctx=None) -> List[dict]:
+    """finalize_all_models_with_gpu_svi (src/parametric.rs:3429-3553): one
+    result per (band, model) entry; band_names[i] names entry i's band."""
+    if not flux_bands or not gpu_results or not svi_outputs:
+        return []
+    picks = []
+    for idx, g in enumerate(gpu_results):
+        if idx >= len(svi_outputs) or idx >= len(band_names):
+            break
+        name = band_names[idx]
+        if name not in flux_bands or not _fittable(flux_bands[name]):
+            continue
+        if len(g["pso_params"]) == 0 or len(svi_outputs[idx][0]) == 0:
+            continue
+        picks.append(idx)
+    if not picks:
+        return []
+    res = _finalize_run([flux_bands[band_names[i]] for i in picks], [gpu_results[i] for i in picks],
+                        [svi_outputs[i] for i in picks], abi.METHOD_SVI, ctx)
+    return [_finalized(res, k, band_names[i], gpu_results[i], abi.METHOD_SVI, {}, gpu_results[i].get("multi_bazin"))
+            for k, i in enumerate(picks)]

@@ -1966,6 +1966,68 @@ static void fit_source(const lcf_bands_csr* in, const lcf_fit_options* o, int sr
     }
 }
 
+// finalize_parametric_from_gpu (src/parametric.rs:3126-3257),
+// finalize_parametric_with_gpu_svi (:3298-3421) and
+// finalize_all_models_with_gpu_svi (:3429-3553) for the bands of one source:
+// the caller's selected model and PSO parameters per band (model < 0: the
+// reference's empty pso_params, skipped); uncertainty by SVI from the PSO
+// parameters or Laplace at them, unless mu / log_sigma (/ elbo) are given;
+// then profile_t0_refine, profile_refine_all and the magnitude chi2.
+static void finalize_source(const lcf_bands_csr* in, int src, const int32_t* model, const double* pso_params,
+                            const double* pso_cost, const double* per_chi2, const double* g_mu, const double* g_ls,
+                            const double* g_elbo, int method, lcf_fit_outputs* out) {
+    int b0 = in->source_band_offsets[src], b1 = in->source_band_offsets[src + 1];
+    struct Entry { int band; Band data; };
+    std::vector<Entry> entries;
+    for (int bi = b0; bi < b1; bi++) {
+        out->model[bi] = -1;
+        out->rank[bi] = -1;
+        out->n_obs[bi] = 0;
+        out->mb_best_k[bi] = 0;
+        int64_t o0 = in->band_obs_offsets[bi], o1 = in->band_obs_offsets[bi + 1];
+        Entry e;
+        e.band = bi;
+        if (prepare_band(in->times + o0, in->flux + o0, in->flux_err + o0, (int)(o1 - o0), e.data))
+            entries.push_back(std::move(e));
+    }
+    std::stable_sort(entries.begin(), entries.end(),
+                     [](const Entry& a, const Entry& b) { return a.data.n() > b.data.n(); });
+    for (int rk = 0; rk < (int)entries.size(); rk++) {
+        const Band& b = entries[rk].data;
+        int bi = entries[rk].band;
+        int m = model[bi];
+        if (m < 0) continue;
+        int np = N_PARAMS[m];
+        std::vector<double> pp(pso_params + bi * 7, pso_params + bi * 7 + np);
+        Uncert u;
+        if (g_mu) {
+            u.mu.assign(g_mu + bi * 7, g_mu + bi * 7 + np);
+            u.log_sigma.assign(g_ls + bi * 7, g_ls + bi * 7 + np);
+            u.elbo = g_elbo ? g_elbo[bi] : NaN;
+        } else {
+            u = method == LCF_METHOD_SVI ? svi_fit(m, b, 1000, 4, 0.01, pp) : laplace_fit(m, b, pp);
+        }
+        profile_t0_refine(m, u, b);
+        profile_refine_all(m, u, b);
+        double mag_chi2 = magnitude_chi2(m, b, u, pp);
+        out->model[bi] = m;
+        out->rank[bi] = rk;
+        out->n_obs[bi] = b.n();
+        for (int j = 0; j < LCF_MAX_PARAMS; j++) {
+            out->pso_params[bi * 7 + j] = j < np ? pp[j] : NaN;
+            out->svi_mu[bi * 7 + j] = j < np ? u.mu[j] : NaN;
+            out->svi_log_sigma[bi * 7 + j] = j < np ? u.log_sigma[j] : NaN;
+        }
+        out->pso_chi2[bi] = fon(pso_cost ? pso_cost[bi] : NaN);
+        out->svi_elbo[bi] = fon(u.elbo);
+        out->mag_chi2[bi] = fon(mag_chi2);
+        for (int mm = 0; mm < 8; mm++) {
+            out->per_model_chi2[bi * 8 + mm] = per_chi2 ? per_chi2[bi * 8 + mm] : NaN;
+            for (int j = 0; j < 7; j++) out->per_model_params[(bi * 8 + mm) * 7 + j] = NaN;
+        }
+    }
+}
+
 }  // namespace orc
 
 // ---------------------------------------------------------------------------
@@ -2173,6 +2235,22 @@ int orc_fit_batch(const lcf_bands_csr* in, const lcf_fit_options* o, lcf_fit_out
 #pragma omp parallel for schedule(dynamic, 1)
 #endif
     for (int s = 0; s < in->n_sources; s++) fit_source(in, o, s, out);
+    return 0;
+}
+
+// Batched finalisation (finalize_source per source, OpenMP over sources).
+// mu / log_sigma / elbo may be NULL (then the uncertainty stage runs).
+int orc_finalize_batch(const lcf_bands_csr* in, const int32_t* model, const double* pso_params,
+                       const double* pso_cost, const double* per_chi2, const double* mu, const double* log_sigma,
+                       const double* elbo, int method, lcf_fit_outputs* out, int n_threads) {
+    if (!in || !model || !pso_params || !out || in->n_sources < 0) return -1;
+    if ((mu == nullptr) != (log_sigma == nullptr)) return -1;
+#ifdef _OPENMP
+    if (n_threads > 0) omp_set_num_threads(n_threads);
+#pragma omp parallel for schedule(dynamic, 1)
+#endif
+    for (int s = 0; s < in->n_sources; s++)
+        finalize_source(in, s, model, pso_params, pso_cost, per_chi2, mu, log_sigma, elbo, method, out);
     return 0;
 }
 

@@ -66,6 +66,8 @@ def lib():
         L.orc_model_restart.argtypes = [i, vp, vp, vp, vp, vp, i, i, vp]
         L.orc_svi_elbo_grad.argtypes = [i, vp, vp, vp, vp, vp, i, vp, vp, vp, i, vp, vp]
         L.orc_fit_batch.argtypes = [C.POINTER(abi.BandsCSR), C.POINTER(abi.FitOptions), C.POINTER(abi.FitOutputs), i]
+        L.orc_finalize_batch.argtypes = [C.POINTER(abi.BandsCSR), vp, vp, vp, vp, vp, vp, vp, i,
+                                         C.POINTER(abi.FitOutputs), i]
         L.orc_laplace_refine.argtypes = [i, vp, vp, vp, i, vp, vp, vp, vp]
         L.orc_svi_refine.argtypes = [i, vp, vp, vp, i, vp, vp, vp, vp]
         L.orc_joint_cost.argtypes = [C.POINTER(abi.BandsCSR), i, vp, vp]
@@ -239,6 +241,24 @@ def fit_batch(batch, fit_all_models=True, method=abi.METHOD_SVI, forced_model=-1
     rc = lib().orc_fit_batch(C.byref(csr), C.byref(opts), C.byref(outs), int(n_threads))
     if rc != 0:
         raise RuntimeError(f"oracle fit failed: {rc}")
+    return res
+
+
+def finalize_batch(batch, model, pso_params, pso_cost=None, per_model_chi2=None, svi_mu=None, svi_log_sigma=None,
+                   svi_elbo=None, method=abi.METHOD_SVI, n_threads=0) -> abi.FitResult:
+    """finalize_parametric_from_gpu / finalize_*_with_gpu_svi over a batch
+    (src/parametric.rs:3126-3553), selection rows as abi.selection_struct."""
+    keep = []
+    csr = abi.csr_struct(batch, keep)
+    sel = abi.selection_struct(batch.n_bands, model, pso_params, pso_cost, per_model_chi2, svi_mu, svi_log_sigma,
+                               svi_elbo, keep)
+    res = abi.FitResult(batch.n_bands)
+    outs = res.as_struct()
+    rc = lib().orc_finalize_batch(C.byref(csr), sel.model, sel.pso_params, sel.pso_cost, sel.per_model_chi2,
+                                  sel.svi_mu, sel.svi_log_sigma, sel.svi_elbo, int(method), C.byref(outs),
+                                  int(n_threads))
+    if rc != 0:
+        raise RuntimeError(f"oracle finalize failed: {rc}")
     return res
 
 

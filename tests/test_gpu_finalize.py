@@ -1,0 +1,188 @@
+"""GPU tests of the batched finalisation (lcf_finalize_batch): the reference's
+finalize_parametric_from_gpu, finalize_parametric_with_gpu_svi and
+finalize_all_models_with_gpu_svi (src/parametric.rs:3126-3553) on the
+per-band kernels of the fused pipeline, against the oracle's restatement and
+against the fused fit itself.
+
+Tolerances are those of the fused pipeline's refinement and SVI parity
+(test_gpu_parity.py): mu 1e-9, log sigma 1e-5, magnitude chi2 1e-6 for the
+refinements from identical inputs (>= 95 % of the bands of the models other
+than MetzgerKN); SVI posterior means within 0.1 posterior sigma for >= 90 %
+of the bands.
+"""
+import numpy as np
+import pytest
+
+from lightcurve_fitting_gb300 import abi, synth
+
+pytestmark = pytest.mark.gpu
+
+FIELDS = ["model", "rank", "n_obs", "pso_params", "pso_chi2", "svi_mu", "svi_log_sigma", "svi_elbo", "mag_chi2",
+          "per_model_chi2"]
+
+
+@pytest.fixture(scope="module")
+def ctx():
+    import torch
+    if not torch.cuda.is_available():
+        pytest.skip("no GPU")
+    from lightcurve_fitting_gb300 import build
+    build.build()
+    from lightcurve_fitting_gb300.lib import Context
+    c = Context(0)
+    yield c
+    c.close()
+
+
+def _same(a, b):
+    return np.array_equal(a, b, equal_nan=True) if a.dtype.kind == "f" else np.array_equal(a, b)
+
+
+@pytest.mark.parametrize("method", [abi.METHOD_LAPLACE, abi.METHOD_SVI])
+def test_finalize_of_the_fused_selection_reproduces_the_fused_fit(ctx, method):
+    """The fused fit's own selection (model, PSO parameters after the profile
+    t0 search) through lcf_finalize_batch gives the fused fit's outputs
+    bit for bit: the same kernels on the same inputs."""
+    batch = synth.config_uneven(12, seed=43)
+    fit = ctx.fit_batch(batch, fit_all_models=True, method=method, run_multi_bazin=False)
+    fin = ctx.finalize_batch(batch, fit.model, fit.pso_params, fit.pso_chi2, fit.per_model_chi2, method=method)
+    assert np.sum(fit.model >= 0) >= 24
+    for name in FIELDS:
+        assert _same(getattr(fin, name), getattr(fit, name)), name
+    st = ctx.stats()
+    assert st["kernel_launches"] == 6 and st["pso_tasks"] == 0
+
+
+def _refine_ok(fin, ref, b):
+    m = int(ref.model[b])
+    n = abi.N_PARAMS[m]
+    ok_mu = np.allclose(fin.svi_mu[b, :n], ref.svi_mu[b, :n], rtol=1e-9, atol=1e-9)
+    ok_ls = np.allclose(fin.svi_log_sigma[b, :n], ref.svi_log_sigma[b, :n], rtol=0.0, atol=1e-5)
+    ok_mag = np.allclose(fin.mag_chi2[b], ref.mag_chi2[b], rtol=1e-6, equal_nan=True)
+    return ok_mu and ok_ls and ok_mag
+
+
+def _oracle_selection(oracle, batch, method):
+    return oracle.fit_batch(batch, fit_all_models=True, method=method, run_multi_bazin=False)
+
+
+def test_finalize_laplace_matches_oracle(ctx, oracle):
+    """finalize_parametric_from_gpu with Laplace, from the oracle's selection."""
+    batch = synth.config_uneven(20, seed=47)
+    sel = _oracle_selection(oracle, batch, abi.METHOD_LAPLACE)
+    args = (sel.model, sel.pso_params, sel.pso_chi2, sel.per_model_chi2)
+    fin = ctx.finalize_batch(batch, *args, method=abi.METHOD_LAPLACE)
+    ref = oracle.finalize_batch(batch, *args, method=abi.METHOD_LAPLACE)
+    assert np.array_equal(fin.model, ref.model) and np.array_equal(fin.rank, ref.rank)
+    bands = [b for b in range(batch.n_bands) if ref.model[b] >= 0 and ref.model[b] != 7]
+    assert len(bands) >= 30
+    assert np.mean([_refine_ok(fin, ref, b) for b in bands]) >= 0.95
+    assert _same(fin.pso_chi2, ref.pso_chi2) and _same(fin.per_model_chi2, ref.per_model_chi2)
+
+
+def test_finalize_svi_matches_oracle(ctx, oracle):
+    """finalize_parametric_from_gpu with SVI from the oracle's selection:
+    posterior means within 0.1 posterior sigma."""
+    batch = synth.config_uneven(16, seed=53)
+    sel = _oracle_selection(oracle, batch, abi.METHOD_SVI)
+    args = (sel.model, sel.pso_params, sel.pso_chi2, sel.per_model_chi2)
+    fin = ctx.finalize_batch(batch, *args, method=abi.METHOD_SVI)
+    ref = oracle.finalize_batch(batch, *args, method=abi.METHOD_SVI)
+    zs = []
+    for b in range(batch.n_bands):
+        m = int(ref.model[b])
+        if m < 0:
+            continue
+        n = abi.N_PARAMS[m]
+        zs.append(float(np.max(np.abs(fin.svi_mu[b, :n] - ref.svi_mu[b, :n]) / np.exp(ref.svi_log_sigma[b, :n]))))
+    zs = np.array(zs)
+    assert zs.size >= 30
+    assert np.mean(zs < 0.1) >= 0.9, (np.mean(zs < 0.1), np.sort(zs)[-5:])
+
+
+def _given_svi(oracle, batch, sel):
+    nb = batch.n_bands
+    mu, ls, elbo = np.full((nb, 7), np.nan), np.full((nb, 7), np.nan), np.full(nb, np.nan)
+    for s in range(batch.n_sources):
+        for k, (t, f, e) in enumerate(batch.bands_of(s)):
+            b = batch.source_band_offsets[s] + k
+            m = int(sel.model[b])
+            if m < 0:
+                continue
+            n = abi.N_PARAMS[m]
+            u = oracle.svi_fit(m, oracle.Band(t, f, e), sel.pso_params[b, :n])
+            mu[b, :n], ls[b, :n], elbo[b] = u[0], u[1], u[2]
+    return mu, ls, elbo
+
+
+def test_finalize_with_given_svi_matches_oracle(ctx, oracle):
+    """finalize_parametric_with_gpu_svi: the supplied SVI outputs, then the
+    refinements and the magnitude chi2 from identical inputs; the ELBO is
+    carried through unchanged."""
+    batch = synth.config_uneven(20, seed=59)
+    sel = _oracle_selection(oracle, batch, abi.METHOD_LAPLACE)
+    mu, ls, elbo = _given_svi(oracle, batch, sel)
+    args = (sel.model, sel.pso_params, sel.pso_chi2, sel.per_model_chi2, mu, ls, elbo)
+    fin = ctx.finalize_batch(batch, *args)
+    ref = oracle.finalize_batch(batch, *args)
+    assert np.array_equal(fin.model, ref.model)
+    assert _same(fin.svi_elbo, ref.svi_elbo)
+    bands = [b for b in range(batch.n_bands) if ref.model[b] >= 0 and ref.model[b] != 7]
+    assert len(bands) >= 30
+    assert np.mean([_refine_ok(fin, ref, b) for b in bands]) >= 0.95
+
+
+def test_finalize_all_models_pairs(ctx, oracle):
+    """finalize_all_models_with_gpu_svi: one entry per (band, model) pair, the
+    band repeated in the CSR; every model's polished parameters of the fused
+    fit with the oracle's SVI outputs."""
+    from lightcurve_fitting_gb300 import parametric
+    batch = synth.config_basic(2, seed=61)
+    fit = ctx.fit_batch(batch, fit_all_models=True, method=abi.METHOD_SVI, run_multi_bazin=False)
+    flux_bands, gpu_results, svi_outputs, names = {}, [], [], []
+    s = 0
+    for k, (t, f, e) in enumerate(batch.bands_of(s)):
+        b = batch.source_band_offsets[s] + k
+        name = "gri"[k]
+        flux_bands[name] = {"times": list(t), "values": list(f), "errors": list(e)}
+        if fit.model[b] < 0:
+            continue
+        for m in range(8):
+            n = abi.N_PARAMS[m]
+            p = fit.per_model_params[b, m, :n]
+            if np.any(np.isnan(p)):
+                continue
+            gpu_results.append({"model": abi.MODEL_NAMES[m], "pso_params": list(p),
+                                "pso_cost": float(fit.per_model_chi2[b, m]), "per_model_chi2": {}})
+            u = oracle.svi_fit(m, oracle.Band(t, f, e), p)
+            svi_outputs.append((list(u[0]), list(u[1]), u[2]))
+            names.append(name)
+    assert len(gpu_results) >= 16
+    rows = parametric.finalize_all_models_with_gpu_svi(flux_bands, gpu_results, svi_outputs, names, ctx=ctx)
+    assert len(rows) == len(gpu_results)
+    ok = []
+    for r, g, (mu0, ls0, el0), name in zip(rows, gpu_results, svi_outputs, names):
+        assert r["model"] == g["model"] and r["band"] == name and r["uncertainty_method"] == "Svi"
+        bd = flux_bands[name]
+        m = abi.MODEL_NAMES.index(g["model"])
+        one = synth.PhotometryBatch(np.asarray(bd["times"]), np.asarray(bd["values"]), np.asarray(bd["errors"]),
+                                    np.array([0, len(bd["times"])], np.int64), np.array([0, 1], np.int32),
+                                    np.zeros(1, np.int32), "pair")
+        ref = oracle.finalize_batch(one, np.array([m]), np.asarray([list(g["pso_params"]) + [np.nan] * (7 - len(g["pso_params"]))]),
+                                    svi_mu=np.asarray([list(mu0) + [np.nan] * (7 - len(mu0))]),
+                                    svi_log_sigma=np.asarray([list(ls0) + [np.nan] * (7 - len(ls0))]),
+                                    svi_elbo=np.asarray([el0]))
+        n = abi.N_PARAMS[m]
+        ok.append(m == 7 or (np.allclose(r["svi_mu"], ref.svi_mu[0, :n], rtol=1e-9, atol=1e-9)
+                             and np.allclose(r["svi_log_sigma"], ref.svi_log_sigma[0, :n], rtol=0, atol=1e-5)))
+    assert np.mean(ok) >= 0.9, np.mean(ok)
+
+
+def test_finalize_rejects_bad_selection(ctx):
+    from lightcurve_fitting_gb300.lib import LcfError
+    batch = synth.config_basic(1, seed=67)
+    nb = batch.n_bands
+    with pytest.raises(LcfError):
+        ctx.finalize_batch(batch, np.full(nb, 9), np.zeros((nb, 7)))
+    with pytest.raises(LcfError):
+        ctx.finalize_batch(batch, np.zeros(nb), np.zeros((nb, 7)), svi_mu=np.zeros((nb, 7)))
