@@ -85,6 +85,8 @@ def parse():
     ap.add_argument("--plain-steps", type=int, default=1, help="timed steps of the plain FP64 GPU form (0: skip)")
     ap.add_argument("--scale-sources", type=int, default=100_000,
                     help="sources of the full-scale leg (counts clipped at 1000; 0: skip)")
+    ap.add_argument("--finalize-sources", type=int, default=10000,
+                    help="sources whose (band, model) pairs the finalisation leg runs (0: skip)")
     ap.add_argument("--joint-sources", type=int, default=2000,
                     help="sources of the fit_parametric multi-band (joint Villar) measurement (0: skip)")
     return ap.parse_args()
@@ -293,6 +295,7 @@ def run_fused(args, ws, rank, local):
         plain = run_plain(args, batch, ptrs, dev, flush, stage, ws)
     joint = run_joint(args, batch, dev, flush, ws, tuned["candidate"]) if args.joint_sources > 0 else None
     scale = run_scale(args, dev, flush, ws, rank, tuned["candidate"]) if args.scale_sources > 0 else None
+    final = run_finalize(args, batch, res, flush, dev, ws, rank) if args.finalize_sources > 0 and e2e_t else None
     if rank != 0:
         ctx.close()
         return
@@ -383,6 +386,7 @@ def run_fused(args, ws, rank, local):
         "plain_gpu": plain,
         "fit_parametric_multiband": joint,
         "full_scale": scale,
+        "finalize_all_models": final,
         "autotune": {"candidates_block_staging_blocks_per_sm": ctx.autotune_candidates().tolist(),
                      "chosen": tuned,
                      "table_bucket_best_next_ms": tune_table.tolist(),
@@ -477,6 +481,64 @@ def run_joint(args, batch, dev, flush, ws, candidate):
                       "1500 iterations, stall 60, 3 seeds), per-band SVI, refinements, MultiBazin",
             "stage_ms": {"ms_joint": st["ms_joint"], "ms_uncertainty": st["ms_uncertainty"],
                          "ms_refine": st["ms_refine"], "ms_multi_bazin": st["ms_multi_bazin"]}}
+
+
+def pair_batch(batch, res, n_sources: int):
+    """Every fitted (band, model) pair of the first `n_sources` sources as its
+    own one-band source (the band's observations repeated per model), with
+    that model's polished parameters and cost from a fit_all_models run."""
+    from lightcurve_fitting_gb300 import synth
+    nb = int(batch.source_band_offsets[min(n_sources, batch.n_sources)])
+    have = np.isfinite(res.per_model_params[:nb, :, 0]) & (res.model[:nb, None] >= 0)
+    b_idx, m_idx = np.nonzero(have)
+    off = batch.band_obs_offsets
+    cnt = (off[b_idx + 1] - off[b_idx]).astype(np.int64)
+    new_off = np.concatenate([[0], np.cumsum(cnt)]).astype(np.int64)
+    idx = np.repeat(off[b_idx] - new_off[:-1], cnt) + np.arange(int(new_off[-1]), dtype=np.int64)
+    pairs = synth.PhotometryBatch(batch.times[idx], batch.flux[idx], batch.flux_err[idx], new_off,
+                                  np.arange(b_idx.size + 1, dtype=np.int32), np.zeros(b_idx.size, np.int32), "pairs")
+    return pairs, m_idx.astype(np.int32), res.per_model_params[b_idx, m_idx, :], res.per_model_chi2[b_idx, m_idx]
+
+
+def run_finalize(args, batch, res, flush, dev, ws, rank):
+    """The reference CLI's finalisation of every (band, model) pair
+    (src/bin/extract_features.rs:640-740: batched SVI of each pair seeded
+    from its PSO parameters, then finalize_all_models_with_gpu_svi's
+    refinements and magnitude chi2) as one lcf_finalize_batch call with SVI
+    from each model's polished parameters, host buffers in and out; one
+    warm-up and one timed call.  Rank 0 also times the oracle's
+    restatement on the first pairs."""
+    import torch
+    from lightcurve_fitting_gb300 import abi
+    from lightcurve_fitting_gb300.lib import Context
+    pairs, model, pso, cost = pair_batch(batch, res, args.finalize_sources)
+    fctx = Context(dev.index)
+    fin = lambda: fctx.finalize_batch(pairs, model, pso, cost, method=abi.METHOD_SVI)
+    fin()
+    flush.fill_(1.0)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    fin()
+    dt = dist_max(time.perf_counter() - t0, ws, dev)
+    st = fctx.stats()
+    fctx.close()
+    out = {"value": ws * pairs.n_bands / dt, "unit": "(band, model) pairs/s", "ms_per_step": 1e3 * dt,
+           "pairs_per_gpu": pairs.n_bands, "n_obs_per_gpu": pairs.n_obs, "steps": 1, "warmup": 1,
+           "config": "every fitted (band, model) pair of the workload: SVI (1000 steps, 4 samples) from the "
+                     "model's polished parameters, profile refinements, magnitude chi2; host buffers",
+           "stage_ms": {k: st[k] for k in ["ms_total", "ms_uncertainty", "ms_refine"]},
+           "h2d_bytes": int(st["h2d_bytes"]), "d2h_bytes": int(st["d2h_bytes"])}
+    if rank == 0 and not args.no_cpu_baseline:
+        from oracle import oracle as O
+        k = min(1024, pairs.n_bands)
+        sub = pairs.subset(np.arange(k))
+        t0 = time.perf_counter()
+        O.finalize_batch(sub, model[:k], pso[:k], cost[:k], method=abi.METHOD_SVI)
+        dc = time.perf_counter() - t0
+        out["cpu_baseline"] = {"value": k / dc, "unit": "(band, model) pairs/s", "cores": O.max_threads(),
+                               "kind": "port", "sample": f"first {k} pairs, oracle restatement of the "
+                                                         f"finalisation, OpenMP over pairs ({dc:.1f} s wall)"}
+    return out
 
 
 def run_scale(args, dev, flush, ws, rank, candidate):
