@@ -127,7 +127,7 @@ typedef struct lcf_fit_stats {
     double ms_t0_search;        /* SVI-mode profile t0 search (two PSO launches) */
     double ms_uncertainty;      /* SVI or Laplace */
     double ms_refine;           /* profile refinements + mag chi2 */
-    double ms_multi_bazin;      /* MultiBazin K = 2..4 launches */
+    double ms_multi_bazin;      /* MultiBazin K = 2..4 launches (on their own stream when branched) */
     double particle_obs_evals;  /* device-counted particle x observation evaluations in PSO launches */
     double ode_steps;           /* device-counted MetzgerKN Euler steps in PSO launches */
     int64_t pso_tasks;          /* PSO runs executed */
@@ -237,6 +237,14 @@ void* lcf_ctx_stream(lcf_ctx* ctx);
 /* Replay the stage sequence from a CUDA graph captured per batch layout
  * (default 1), or launch the kernels one by one (0). */
 int lcf_set_graph(lcf_ctx* ctx, int enabled);
+
+/* Stage concurrency: MultiBazin K = 2..4 (fit_multi_bazin's greedy loop)
+ * depends only on the band preparation and its K = 1 swarms, so the fit can
+ * run it on a second stream beside the later stages.  mode 0: the stages
+ * run in sequence; 1 (default): the branch forks after the model-selection
+ * swarm launch and runs beside the polish; 2: it forks after the polish and
+ * BIC selection.  The results are the same under every mode. */
+int lcf_set_multi_bazin_branch(lcf_ctx* ctx, int mode);
 
 /*
  * Launch autotuner of the swarm kernel (no counterpart in the reference,

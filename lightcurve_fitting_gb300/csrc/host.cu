@@ -105,7 +105,7 @@ void make_joint_draws(float* draws, int64_t per_seed) {
 // ---------------------------------------------------------------------------
 // Context
 // ---------------------------------------------------------------------------
-enum { N_EVENTS = 10 };
+enum { N_EVENTS = 11 };
 
 struct DevArr {
     void* p = nullptr;
@@ -155,6 +155,14 @@ struct lcf_ctx {
     uint32_t bucket = 0;
     std::vector<TuneEntry> tune;
     cudaStream_t stream = nullptr;
+    // MultiBazin K = 2..4 branch: its own stream, forked from and joined to
+    // the main stage sequence (mb_branch: 0 = no branch, the stages run in
+    // sequence; 1 = fork after the model-selection swarm launch; 2 = fork
+    // after the polish and BIC selection)
+    cudaStream_t stream_mb = nullptr;
+    cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
+    int mb_branch = 1;
+    bool mb_timed = false;   // the last enqueued sequence recorded ev[9], ev[10]
     std::string err;
     lcf_fit_stats stats{};
     cudaEvent_t ev[N_EVENTS]{};
@@ -165,7 +173,7 @@ struct lcf_ctx {
     float* d_eps = nullptr;
     // device buffers (capacity-sized)
     DevArr times, flux, ferr, boff, soff, stats_b, obs, t64, f64, fe64, var64, uf64, mag64, up, ffa, ffb, res, fits, out, mb,
-        ctr, scratch, scratch64, scratch_svi, t0state, tasks[7], task_sorted, band_order, joint_flag, joint_src, joint_res,
+        ctr, scratch, scratch64, scratch_svi, t0state, tasks[7], task_sorted, task_sorted_mb, band_order, joint_flag, joint_src, joint_res,
         joint_draws;
     int64_t joint_per_seed = 0;   // uniforms per seed held in joint_draws
     int n_joint = 0, joint_max_obs = 0, joint_max_d = 0;
@@ -189,6 +197,7 @@ struct lcf_ctx {
     cudaGraphExec_t graph = nullptr;
     uint64_t graph_key = 0;
     bool use_graph = true;
+    bool capturing = false;   // enqueue_pipeline is recording into a graph
     DeviceBatch db{};
     int n_sources = 0, n_bands = 0;
     int64_t n_obs = 0;
@@ -269,6 +278,12 @@ extern "C" int lcf_ctx_create(int device, lcf_ctx** out) {
         return LCF_E_CUDA;
     }
     for (int i = 0; i < N_EVENTS; i++) cudaEventCreate(&ctx->ev[i]);
+    if (cudaStreamCreateWithFlags(&ctx->stream_mb, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaEventCreateWithFlags(&ctx->ev_fork, cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&ctx->ev_join, cudaEventDisableTiming) != cudaSuccess) {
+        lcf_ctx_destroy(ctx);
+        return LCF_E_CUDA;
+    }
     // the kernels accept the largest candidate's dynamic shared memory
     int big = 0;
     for (int c = 1; c < N_TUNE; c++)
@@ -316,7 +331,7 @@ extern "C" void lcf_ctx_destroy(lcf_ctx* ctx) {
     DevArr* all[] = {&ctx->times, &ctx->flux, &ctx->ferr, &ctx->boff, &ctx->soff, &ctx->stats_b, &ctx->obs,
                      &ctx->t64, &ctx->f64, &ctx->fe64, &ctx->var64, &ctx->uf64, &ctx->mag64, &ctx->up, &ctx->ffa, &ctx->ffb, &ctx->res,
                      &ctx->fits, &ctx->out, &ctx->mb, &ctx->ctr, &ctx->scratch, &ctx->scratch64, &ctx->scratch_svi,
-                     &ctx->t0state, &ctx->task_sorted, &ctx->band_order, &ctx->joint_flag, &ctx->joint_src,
+                     &ctx->t0state, &ctx->task_sorted, &ctx->task_sorted_mb, &ctx->band_order, &ctx->joint_flag, &ctx->joint_src,
                      &ctx->joint_res,
                      &ctx->joint_draws,
                      &ctx->bc_obs, &ctx->bc_params, &ctx->bc_costs, &ctx->bc_scratch, &ctx->plain_scr,
@@ -332,6 +347,9 @@ extern "C" void lcf_ctx_destroy(lcf_ctx* ctx) {
     if (ctx->d_eps) cudaFree(ctx->d_eps);
     for (int i = 0; i < N_EVENTS; i++)
         if (ctx->ev[i]) cudaEventDestroy(ctx->ev[i]);
+    if (ctx->ev_fork) cudaEventDestroy(ctx->ev_fork);
+    if (ctx->ev_join) cudaEventDestroy(ctx->ev_join);
+    if (ctx->stream_mb) cudaStreamDestroy(ctx->stream_mb);
     if (ctx->stream) cudaStreamDestroy(ctx->stream);
     delete ctx;
 }
@@ -497,7 +515,8 @@ static int prepare_layout(lcf_ctx* ctx, int n_sources, int n_bands, int64_t n_ob
         rc |= grow(ctx, ctx->tasks[s], (size_t)caps[s] * sizeof(PsoTask));
         ctx->task_cap[s] = caps[s];
     }
-    rc |= grow(ctx, ctx->task_sorted, (size_t)nb * 21 * sizeof(PsoTask));  // the largest of slots 1..6
+    rc |= grow(ctx, ctx->task_sorted, (size_t)nb * 21 * sizeof(PsoTask));     // slots 1..3
+    rc |= grow(ctx, ctx->task_sorted_mb, (size_t)nb * 3 * sizeof(PsoTask));   // slots 4..6 (MultiBazin branch)
     rc |= grow(ctx, ctx->band_order, nb * sizeof(int32_t));
     if (rc) return rc;
     // stage-1 task list (bands, models, restarts; MultiBazin K = 1), longest first
@@ -656,6 +675,7 @@ static int prepare_layout(lcf_ctx* ctx, int n_sources, int n_bands, int64_t n_ob
     d.tasks[7] = nullptr;
     d.task_cap[7] = 0;
     d.task_sorted = (PsoTask*)ctx->task_sorted.p;
+    d.task_sorted_mb = (PsoTask*)ctx->task_sorted_mb.p;
     d.band_order = (int32_t*)ctx->band_order.p;
     d.n_joint = ctx->n_joint;
     d.joint_flag = ctx->n_joint > 0 ? (const uint8_t*)ctx->joint_flag.p : nullptr;
@@ -680,6 +700,15 @@ static int prepare_layout(lcf_ctx* ctx, int n_sources, int n_bands, int64_t n_ob
 // ---------------------------------------------------------------------------
 // Stage sequence
 // ---------------------------------------------------------------------------
+// A stage-timing event: an external event node while the stage sequence is
+// captured into the graph (so that replays record it), a plain record when
+// the kernels are launched one by one (the external flag is only valid
+// during capture).
+static void stage_event(lcf_ctx* ctx, cudaEvent_t e, cudaStream_t q) {
+    if (ctx->capturing) cudaEventRecordWithFlags(e, q, cudaEventRecordExternal);
+    else cudaEventRecord(e, q);
+}
+
 static void enqueue_pipeline(lcf_ctx* ctx) {
     const DeviceBatch& d = ctx->db;
     const lcf_fit_options& o = ctx->opts;
@@ -687,61 +716,80 @@ static void enqueue_pipeline(lcf_ctx* ctx) {
     int grid = ctx->num_sms * ctx->pso_blocks_per_sm;
     int block = ctx->pso_block;
     int64_t L = 0;
-    cudaEventRecordWithFlags(ctx->ev[0], s, cudaEventRecordExternal);
+    stage_event(ctx, ctx->ev[0], s);
     cudaMemsetAsync(ctx->res.p, 0xff, (size_t)std::max(ctx->n_bands, 1) * 44 * sizeof(PsoResult), s);
     cudaMemsetAsync(ctx->ctr.p, 0, sizeof(Counters), s);
     cudaMemsetAsync(ctx->fits.p, 0xff, (size_t)std::max(ctx->n_bands, 1) * 8 * sizeof(ModelFit), s);
     launch_prep(d, s); L++;
-    cudaEventRecordWithFlags(ctx->ev[1], s, cudaEventRecordExternal);
+    stage_event(ctx, ctx->ev[1], s);
     launch_pso(d, 0, d.tasks[0], ctx->n_tasks0, 7, grid, block, s); L++;
-    cudaEventRecordWithFlags(ctx->ev[2], s, cudaEventRecordExternal);
+    stage_event(ctx, ctx->ev[2], s);
+    // MultiBazin K = 2..4 (fit_multi_bazin's greedy loop) needs only the band
+    // preparation and its K = 1 swarms of the launch above, so it can run on
+    // a branch beside the polish / selection / t0 / uncertainty / refinement
+    // stages and fill their tails; it owns slots 4..6, its own sorted task
+    // list and no state the main sequence reads
+    auto enqueue_mb = [&](cudaStream_t q) {
+        stage_event(ctx, ctx->ev[9], q);
+        launch_mb_pick(d, 1, q); L++;
+        for (int k = 2; k <= 4; k++) {
+            launch_mb_build(d, 2 + k, k, q); L++;
+            launch_task_sort(d, 2 + k, d.task_sorted_mb, q); L += 3;
+            launch_pso(d, 2 + k, d.task_sorted_mb, -1, 4 * k + 2, grid, block, q); L++;
+            launch_mb_pick(d, k, q); L++;
+        }
+        stage_event(ctx, ctx->ev[10], q);
+    };
+    const int branch = o.run_multi_bazin ? ctx->mb_branch : 0;
+    auto fork_mb = [&]() {
+        cudaEventRecord(ctx->ev_fork, s);
+        cudaStreamWaitEvent(ctx->stream_mb, ctx->ev_fork, 0);
+        enqueue_mb(ctx->stream_mb);
+        cudaEventRecord(ctx->ev_join, ctx->stream_mb);
+    };
+    ctx->mb_timed = o.run_multi_bazin != 0;
+    if (branch == 1) fork_mb();
     int gated = (o.forced_model < 0 && !o.fit_all_models);
     launch_lbfgs(d, gated ? 1 : 0xff, s); L++;
     if (gated) {
         launch_gate_build(d, 1, s); L++;
-        launch_task_sort(d, 1, s); L += 3;
+        launch_task_sort(d, 1, d.task_sorted, s); L += 3;
         launch_pso(d, 1, d.task_sorted, -1, 7, grid, block, s); L++;
         launch_lbfgs(d, 0xfe, s); L++;
     }
     launch_select(d, o.fit_all_models, o.forced_model, s); L++;
-    cudaEventRecordWithFlags(ctx->ev[3], s, cudaEventRecordExternal);
+    stage_event(ctx, ctx->ev[3], s);
+    if (branch == 2) fork_mb();
     if (d.n_joint > 0 && launch_joint(d, s) == 0) L += 2;
-    cudaEventRecordWithFlags(ctx->ev[8], s, cudaEventRecordExternal);
+    stage_event(ctx, ctx->ev[8], s);
     if (o.method == LCF_METHOD_SVI) {
         launch_t0_build(d, 2, 0, s); L++;
-        launch_task_sort(d, 2, s); L += 3;
+        launch_task_sort(d, 2, d.task_sorted, s); L += 3;
         launch_pso(d, 2, d.task_sorted, -1, 7, grid, block, s); L++;
         launch_t0_pick(d, 2, 0, s); L++;
         launch_t0_build(d, 3, 1, s); L++;
-        launch_task_sort(d, 3, s); L += 3;
+        launch_task_sort(d, 3, d.task_sorted, s); L += 3;
         launch_pso(d, 3, d.task_sorted, -1, 7, grid, block, s); L++;
         launch_t0_pick(d, 3, 1, s); L++;
     }
-    cudaEventRecordWithFlags(ctx->ev[4], s, cudaEventRecordExternal);
+    stage_event(ctx, ctx->ev[4], s);
     launch_band_order(d, s); L += 3;
     if (o.method == LCF_METHOD_SVI) launch_svi(d, s);
     else launch_laplace(d, s);
     L++;
-    cudaEventRecordWithFlags(ctx->ev[5], s, cudaEventRecordExternal);
+    stage_event(ctx, ctx->ev[5], s);
     launch_refine(d, s); L++;
-    cudaEventRecordWithFlags(ctx->ev[6], s, cudaEventRecordExternal);
-    if (o.run_multi_bazin) {
-        launch_mb_pick(d, 1, s); L++;
-        for (int k = 2; k <= 4; k++) {
-            launch_mb_build(d, 2 + k, k, s); L++;
-            launch_task_sort(d, 2 + k, s); L += 3;
-            launch_pso(d, 2 + k, d.task_sorted, -1, 4 * k + 2, grid, block, s); L++;
-            launch_mb_pick(d, k, s); L++;
-        }
-    }
-    cudaEventRecordWithFlags(ctx->ev[7], s, cudaEventRecordExternal);
+    stage_event(ctx, ctx->ev[6], s);
+    if (o.run_multi_bazin && branch == 0) enqueue_mb(s);
+    if (branch) cudaStreamWaitEvent(s, ctx->ev_join, 0);
+    stage_event(ctx, ctx->ev[7], s);
     ctx->launches = L;
 }
 
 static int run_pipeline(lcf_ctx* ctx) {
     cudaGetLastError();  // a failed query elsewhere in the process must not be reported as ours
     uint64_t gkey = ctx->layout_key ^ ((uint64_t)(uintptr_t)ctx->db.times * 31) ^ ((uint64_t)ctx->n_obs << 7) ^
-                    ((uint64_t)(ctx->cfg + 1) << 56);
+                    ((uint64_t)(ctx->cfg + 1) << 56) ^ ((uint64_t)(ctx->mb_branch + 1) << 52);
     if (ctx->use_graph) {
         if (!ctx->graph || ctx->graph_key != gkey) {
             if (ctx->graph) {
@@ -750,7 +798,9 @@ static int run_pipeline(lcf_ctx* ctx) {
             }
             cudaGraph_t g;
             CK(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
+            ctx->capturing = true;
             enqueue_pipeline(ctx);
+            ctx->capturing = false;
             CK(cudaStreamEndCapture(ctx->stream, &g));
             cudaError_t e = cudaGraphInstantiate(&ctx->graph, g, 0);
             cudaGraphDestroy(g);
@@ -777,6 +827,7 @@ static void enqueue_plain(lcf_ctx* ctx) {
     cudaStream_t s = ctx->stream;
     double* scr = (double*)ctx->plain_scr.p;
     int64_t L = 0;
+    ctx->mb_timed = false;
     cudaEventRecord(ctx->ev[0], s);
     cudaMemsetAsync(ctx->res.p, 0xff, (size_t)std::max(ctx->n_bands, 1) * 44 * sizeof(PsoResult), s);
     cudaMemsetAsync(ctx->ctr.p, 0, sizeof(Counters), s);
@@ -831,7 +882,10 @@ static int finish_stats(lcf_ctx* ctx) {
     st.ms_t0_search = mt0;
     st.ms_uncertainty = ms[5];
     st.ms_refine = ms[6];
-    st.ms_multi_bazin = ms[7];
+    float mmb = 0.0f;
+    if (!ctx->mb_timed || cudaEventElapsedTime(&mmb, ctx->ev[9], ctx->ev[10]) != cudaSuccess) mmb = 0.0f;
+    cudaGetLastError();
+    st.ms_multi_bazin = mmb;
     st.particle_obs_evals = (double)c.particle_obs_evals;
     st.ode_steps = (double)c.ode_steps;
     st.pso_tasks = ctx->n_tasks0;
@@ -995,6 +1049,7 @@ static void enqueue_finalize(lcf_ctx* ctx, bool given, size_t sel_bytes) {
     const DeviceBatch& d = ctx->db;
     cudaStream_t s = ctx->stream;
     int64_t L = 0;
+    ctx->mb_timed = false;
     cudaEventRecord(ctx->ev[0], s);
     cudaMemsetAsync(ctx->ctr.p, 0, sizeof(Counters), s);
     launch_prep(d, s); L++;
@@ -1132,6 +1187,13 @@ extern "C" int lcf_fit_plain_device(lcf_ctx* ctx, const lcf_bands_csr* dev, cons
     enqueue_plain(ctx);
     CK(cudaGetLastError());
     return finish_stats(ctx);
+}
+
+extern "C" int lcf_set_multi_bazin_branch(lcf_ctx* ctx, int mode) {
+    if (!ctx) return LCF_E_INVALID;
+    if (mode < 0 || mode > 2) return set_err(ctx, LCF_E_INVALID, "MultiBazin branch mode must be 0, 1 or 2");
+    ctx->mb_branch = mode;
+    return 0;
 }
 
 extern "C" int lcf_set_autotune(lcf_ctx* ctx, int mode, int forced_candidate) {

@@ -261,7 +261,8 @@ struct DeviceBatch {
     MbState* mb;            // [n_bands]
     PsoTask* tasks[8];      // per launch slot
     int task_cap[8];
-    PsoTask* task_sorted;   // device-built task lists after the sort (capacity: the largest of slots 1..6)
+    PsoTask* task_sorted;   // device-built task lists of slots 1..3 after the sort
+    PsoTask* task_sorted_mb;  // the same for slots 4..6 (the MultiBazin branch, which may run concurrently)
     int32_t* band_order;    // [n_bands] bands grouped by selected model (MetzgerKN first), for the
                             // per-band uncertainty and refinement kernels
     Counters* ctr;
@@ -293,9 +294,10 @@ void launch_prep(const DeviceBatch& d, cudaStream_t s);
 // counter of the slot).  `max_dim` selects the kernel instantiation.
 void launch_pso(const DeviceBatch& d, int slot, const PsoTask* tasks, int n_host, int max_dim, int grid, int block,
                 cudaStream_t s);
-// Sort the device-built task list of `slot` into d.task_sorted: MetzgerKN
-// first, then by kind, longest bands first within a kind.
-void launch_task_sort(const DeviceBatch& d, int slot, cudaStream_t s);
+// Sort the device-built task list of `slot` into `out` (d.task_sorted, or
+// d.task_sorted_mb for the MultiBazin branch): MetzgerKN first, then by
+// kind, longest bands first within a kind.
+void launch_task_sort(const DeviceBatch& d, int slot, PsoTask* out, cudaStream_t s);
 size_t pso_smem_bytes(int block, int smem_obs);
 int pso_blocks_per_sm(int block, size_t smem);
 int pso_init_attributes(int block, int smem_obs);

@@ -959,23 +959,23 @@ __global__ void task_scan_kernel(DeviceBatch d, int slot) {  // one block of 256
     d.ctr->sort_hist[slot][i] = sh[i] - v;  // exclusive prefix: first position of key i
 }
 
-__global__ void task_scatter_kernel(DeviceBatch d, int slot) {
+__global__ void task_scatter_kernel(DeviceBatch d, int slot, PsoTask* out) {
     const int n_tasks = d.ctr->task_count[slot];
     int* pos = d.ctr->sort_hist[slot];
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n_tasks; i += gridDim.x * blockDim.x) {
         const PsoTask t = d.tasks[slot][i];
         int p = atomicAdd(&pos[task_sort_key(t, d.stats[t.band].n)], 1);
-        d.task_sorted[p] = t;
+        out[p] = t;
     }
 }
 
-void launch_task_sort(const DeviceBatch& d, int slot, cudaStream_t s) {
+void launch_task_sort(const DeviceBatch& d, int slot, PsoTask* out, cudaStream_t s) {
     if (d.n_bands == 0 || d.task_cap[slot] == 0) return;
     int grid = (d.task_cap[slot] + 255) / 256;
     grid = grid < 1024 ? grid : 1024;
     task_hist_kernel<<<grid, 256, 0, s>>>(d, slot);
     task_scan_kernel<<<1, 256, 0, s>>>(d, slot);
-    task_scatter_kernel<<<grid, 256, 0, s>>>(d, slot);
+    task_scatter_kernel<<<grid, 256, 0, s>>>(d, slot, out);
 }
 
 }  // namespace lcf

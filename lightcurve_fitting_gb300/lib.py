@@ -50,6 +50,7 @@ def load(path: str = LIB_PATH):
     L.lcf_set_graph.argtypes = [vp, i]
     L.lcf_band_cost.argtypes = [vp, i, vp, vp, vp, vp, vp, i, vp, i, i, vp]
     L.lcf_set_autotune.argtypes = [vp, i, i]
+    L.lcf_set_multi_bazin_branch.argtypes = [vp, i]
     L.lcf_autotune_candidates.argtypes = [vp, vp]
     L.lcf_autotune_table.argtypes = [vp, vp, i]
     L.lcf_autotune_load.argtypes = [vp, vp, i]
@@ -214,6 +215,11 @@ class Context:
                                          u.ctypes.data, uf.ctypes.data, t.size, p.ctypes.data, p.shape[0],
                                          int(bool(with_prior)), out.ctypes.data), "lcf_band_cost")
         return out
+
+    def set_multi_bazin_branch(self, mode: int):
+        """0: stages in sequence; 1 / 2: MultiBazin K = 2..4 on a second
+        stream forked after the model-selection swarm / the selection."""
+        self._check(self.L.lcf_set_multi_bazin_branch(self.h, int(mode)), "lcf_set_multi_bazin_branch")
 
     def set_autotune(self, mode: int = 1, forced_candidate: int = -1):
         """Online launch tuning per shape bucket (mode 1), off (0), or a pinned candidate."""
