@@ -163,6 +163,7 @@ struct lcf_ctx {
     cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
     int mb_branch = 1;
     bool mb_timed = false;   // the last enqueued sequence recorded ev[9], ev[10]
+    bool mb_branched = false;  // ... and ran MultiBazin on its branch
     std::string err;
     lcf_fit_stats stats{};
     cudaEvent_t ev[N_EVENTS]{};
@@ -458,7 +459,10 @@ static void record_launch(lcf_ctx* ctx) {
     if (!ctx->exploring) return;
     for (auto& e : ctx->tune) {
         if (e.bucket != ctx->bucket || e.next >= N_TUNE || e.next != ctx->cfg) continue;
-        e.ms[e.next] = ctx->stats.ms_pso + ctx->stats.ms_t0_search + ctx->stats.ms_multi_bazin;
+        // the swarm stages; with the MultiBazin branch running beside the polish
+        // its span measures the overlap, not the swarms, so the whole fit is timed
+        e.ms[e.next] = ctx->mb_branched ? ctx->stats.ms_total
+                                        : ctx->stats.ms_pso + ctx->stats.ms_t0_search + ctx->stats.ms_multi_bazin;
         e.next++;
         if (e.next == N_TUNE) {
             e.best = 0;
@@ -747,7 +751,6 @@ static void enqueue_pipeline(lcf_ctx* ctx) {
         enqueue_mb(ctx->stream_mb);
         cudaEventRecord(ctx->ev_join, ctx->stream_mb);
     };
-    ctx->mb_timed = o.run_multi_bazin != 0;
     if (branch == 1) fork_mb();
     int gated = (o.forced_model < 0 && !o.fit_all_models);
     launch_lbfgs(d, gated ? 1 : 0xff, s); L++;
@@ -788,6 +791,9 @@ static void enqueue_pipeline(lcf_ctx* ctx) {
 
 static int run_pipeline(lcf_ctx* ctx) {
     cudaGetLastError();  // a failed query elsewhere in the process must not be reported as ours
+    // set per fit (a graph replay does not run enqueue_pipeline)
+    ctx->mb_timed = ctx->opts.run_multi_bazin != 0;
+    ctx->mb_branched = ctx->mb_timed && ctx->mb_branch != 0;
     uint64_t gkey = ctx->layout_key ^ ((uint64_t)(uintptr_t)ctx->db.times * 31) ^ ((uint64_t)ctx->n_obs << 7) ^
                     ((uint64_t)(ctx->cfg + 1) << 56) ^ ((uint64_t)(ctx->mb_branch + 1) << 52);
     if (ctx->use_graph) {

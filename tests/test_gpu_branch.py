@@ -55,3 +55,15 @@ def test_branch_mode_is_checked(ctx):
     from lightcurve_fitting_gb300.lib import LcfError
     with pytest.raises(LcfError):
         ctx.set_multi_bazin_branch(3)
+
+
+def test_branch_timing_survives_other_entry_points(ctx):
+    """A graph replay after a finalisation call still times the branch."""
+    ctx.set_graph(True)
+    ctx.set_multi_bazin_branch(1)
+    batch = synth.config_basic(8, seed=73)
+    r = ctx.fit_batch(batch, fit_all_models=True, method=abi.METHOD_LAPLACE)
+    ctx.finalize_batch(batch, r.model, r.pso_params, method=abi.METHOD_LAPLACE)
+    assert ctx.stats()["ms_multi_bazin"] == 0.0
+    ctx.fit_batch(batch, fit_all_models=True, method=abi.METHOD_LAPLACE)
+    assert ctx.stats()["ms_multi_bazin"] > 0.0
