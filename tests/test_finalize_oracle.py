@@ -84,3 +84,78 @@ def test_selection_struct_checks_shapes():
         abi.selection_struct(3, np.zeros(3), np.zeros((3, 6)))
     s = abi.selection_struct(2, np.zeros(2), np.zeros((2, 7)))
     assert s.pso_cost is None and s.svi_mu is None
+
+
+class _FakeCtx:
+    """Records the lcf_finalize_batch inputs and answers with the oracle."""
+
+    def __init__(self, oracle):
+        self.oracle = oracle
+        self.calls = []
+
+    def finalize_batch(self, batch, model, pso, cost, per_chi2, mu, ls, elbo, method):
+        self.calls.append((batch, np.array(model), np.array(pso), mu is not None))
+        return self.oracle.finalize_batch(batch, model, pso, cost, per_chi2, mu, ls, elbo, method=method)
+
+
+def _flux_bands(batch, s):
+    out = {}
+    for k, (t, f, e) in enumerate(batch.bands_of(s)):
+        out["gri"[k]] = {"times": list(t), "values": list(f), "errors": list(e)}
+    return out
+
+
+def test_python_mirror_pairs_results_in_count_order(oracle):
+    """finalize_parametric_from_gpu pairs gpu_results[i] with the i-th band in
+    descending observation count, stops at the shorter list and skips an
+    entry with empty pso_params (src/parametric.rs:3184-3199)."""
+    from lightcurve_fitting_gb300 import parametric
+    batch = synth.config_uneven(3, seed=79)
+    ref = oracle.fit_batch(batch, fit_all_models=True, method=abi.METHOD_LAPLACE, run_multi_bazin=False)
+    s = 0
+    fb = _flux_bands(batch, s)
+    b0 = batch.source_band_offsets[s]
+    order = sorted(range(3), key=lambda k: -len(fb["gri"[k]]["values"]))
+    gpu = []
+    for k in order:
+        b = b0 + k
+        m = int(ref.model[b])
+        gpu.append({"model": abi.MODEL_NAMES[m], "pso_params": list(ref.pso_params[b, :abi.N_PARAMS[m]]),
+                    "pso_cost": float(ref.pso_chi2[b]), "per_model_chi2": {abi.MODEL_NAMES[m]: 1.0}})
+    gpu[1] = dict(gpu[1], pso_params=[])
+    ctx = _FakeCtx(oracle)
+    rows = parametric.finalize_parametric_from_gpu(fb, gpu, method="laplace", ctx=ctx)
+    assert [r["band"] for r in rows] == ["gri"[order[0]], "gri"[order[2]]]
+    for r, k in zip(rows, [order[0], order[2]]):
+        b = b0 + k
+        n = abi.N_PARAMS[int(ref.model[b])]
+        assert np.array_equal(r["svi_mu"], ref.svi_mu[b, :n])
+        assert r["uncertainty_method"] == "Laplace" and r["per_model_chi2"]
+    assert len(ctx.calls) == 1 and ctx.calls[0][0].n_bands == 2 and not ctx.calls[0][3]
+    # two results for three bands: the third band is not finalised
+    assert len(parametric.finalize_parametric_from_gpu(fb, gpu[:1], method="laplace", ctx=ctx)) == 1
+
+
+def test_python_mirror_all_models_entries(oracle):
+    """finalize_all_models_with_gpu_svi: one row per (gpu result, svi output,
+    band name) entry; unknown band names and empty SVI outputs are skipped."""
+    from lightcurve_fitting_gb300 import parametric
+    batch = synth.config_basic(1, seed=83)
+    fb = _flux_bands(batch, 0)
+    t, f, e = batch.bands_of(0)[0]
+    gpu, svi, names = [], [], []
+    for m in (0, 3):
+        n = abi.N_PARAMS[m]
+        p = [float(x) for x in oracle.fit_batch(batch, fit_all_models=True, method=abi.METHOD_LAPLACE,
+                                                 run_multi_bazin=False).per_model_params[0, m, :n]]
+        u = oracle.svi_fit(m, oracle.Band(t, f, e), p)
+        gpu.append({"model": abi.MODEL_NAMES[m], "pso_params": p, "pso_cost": 1.0, "per_model_chi2": {}})
+        svi.append((list(u[0]), list(u[1]), u[2]))
+        names.append("g")
+    gpu.append(gpu[0]); svi.append(svi[0]); names.append("z")          # unknown band
+    gpu.append(gpu[0]); svi.append(([], [], 0.0)); names.append("g")    # empty SVI output
+    ctx = _FakeCtx(oracle)
+    rows = parametric.finalize_all_models_with_gpu_svi(fb, gpu, svi, names, ctx=ctx)
+    assert [r["model"] for r in rows] == ["Bazin", "Arnett"]
+    assert all(r["svi_elbo"] == pytest.approx(s[2]) for r, s in zip(rows, svi))
+    assert ctx.calls[0][3]

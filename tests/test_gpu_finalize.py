@@ -186,3 +186,23 @@ def test_finalize_rejects_bad_selection(ctx):
         ctx.finalize_batch(batch, np.full(nb, 9), np.zeros((nb, 7)))
     with pytest.raises(LcfError):
         ctx.finalize_batch(batch, np.zeros(nb), np.zeros((nb, 7)), svi_mu=np.zeros((nb, 7)))
+
+
+def test_finalize_edge_cases(ctx):
+    """An empty batch, a batch with every row skipped, and a band with
+    non-positive flux among selected ones."""
+    empty = synth.PhotometryBatch(np.zeros(0), np.zeros(0), np.zeros(0), np.zeros(1, np.int64),
+                                  np.zeros(1, np.int32), np.zeros(0, np.int32), "empty")
+    r0 = ctx.finalize_batch(empty, np.zeros(0), np.zeros((0, 7)))
+    assert r0.model.size == 0
+    batch = synth.config_basic(2, seed=89)
+    nb = batch.n_bands
+    skip = ctx.finalize_batch(batch, np.full(nb, -1), np.full((nb, 7), np.nan), method=abi.METHOD_LAPLACE)
+    assert np.all(skip.model == -1) and np.all(skip.rank == -1)
+    fit = ctx.fit_batch(batch, fit_all_models=True, method=abi.METHOD_LAPLACE, run_multi_bazin=False)
+    o0, o1 = batch.band_obs_offsets[2], batch.band_obs_offsets[3]
+    batch.flux[o0:o1] = -np.abs(batch.flux[o0:o1])
+    r = ctx.finalize_batch(batch, fit.model, fit.pso_params, method=abi.METHOD_LAPLACE)
+    assert r.model[2] == -1 and r.rank[2] == -1
+    keep = [b for b in range(nb) if b != 2 and fit.model[b] >= 0]
+    assert np.all(r.model[keep] == fit.model[keep])
