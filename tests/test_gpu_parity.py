@@ -271,7 +271,7 @@ def test_svi_matches_oracle_on_equal_inputs(ctx, oracle):
     GPU evaluates the ELBO gradient in FP32 (per-observation adjoint through
     the analytic model gradient; MetzgerKN by forward-mode duals where the
     reference takes forward differences), so the posterior means are held to
-    the spec criterion: within 0.1 posterior sigma for >= 90 % of the
+    the posterior-mean criterion: within 0.1 posterior sigma for >= 90 % of the
     bands (sigma = the oracle's reported, inflated sigma)."""
     batch = synth.config_uneven(20, seed=29)
     res = ctx.fit_batch(batch, fit_all_models=True, method=abi.METHOD_SVI, run_multi_bazin=False)
