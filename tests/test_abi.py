@@ -65,3 +65,31 @@ def test_build_flux_bands_matches_reference_rules():
     assert sorted(out) == ["g", "r"]
     assert out["g"]["times"] == [0.0, 3.0]
     np.testing.assert_allclose(out["r"]["values"][0], 10 ** (-0.4 * (19.0 - 23.9)))
+
+
+def test_struct_layouts_match_the_ctypes_mirror(tmp_path):
+    """Every struct of include/lcf.h, compiled by the C compiler, has the size
+    and field offsets of its ctypes Structure in abi.py."""
+    import subprocess
+    from lightcurve_fitting_gb300 import abi
+    pairs = {"lcf_bands_csr": abi.BandsCSR, "lcf_fit_options": abi.FitOptions, "lcf_fit_outputs": abi.FitOutputs,
+             "lcf_fit_stats": abi.FitStats, "lcf_pso_selection": abi.PsoSelection}
+    lines = ['#include <stdio.h>', '#include <stddef.h>', '#include "lcf.h"', "int main(void) {"]
+    for cname, cls in pairs.items():
+        lines.append(f'printf("{cname} size %zu\\n", sizeof({cname}));')
+        for f, _ in cls._fields_:
+            lines.append(f'printf("{cname} {f} %zu\\n", offsetof({cname}, {f}));')
+    lines.append("return 0; }")
+    src = tmp_path / "layout.c"
+    src.write_text("\n".join(lines))
+    exe = tmp_path / "layout"
+    subprocess.check_call(["gcc", "-std=c99", "-I", os.path.join(ROOT, "include"), str(src), "-o", str(exe)])
+    got = {}
+    for row in subprocess.check_output([str(exe)]).decode().split("\n"):
+        if row:
+            cname, field, v = row.split()
+            got[(cname, field)] = int(v)
+    for cname, cls in pairs.items():
+        assert got[(cname, "size")] == ctypes.sizeof(cls), cname
+        for f, _ in cls._fields_:
+            assert got[(cname, f)] == getattr(cls, f).offset, (cname, f)
