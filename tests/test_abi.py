@@ -93,3 +93,17 @@ def test_struct_layouts_match_the_ctypes_mirror(tmp_path):
         assert got[(cname, "size")] == ctypes.sizeof(cls), cname
         for f, _ in cls._fields_:
             assert got[(cname, f)] == getattr(cls, f).offset, (cname, f)
+
+
+def test_rust_bindings_in_the_integration_notes_match_the_header():
+    """The #[repr(C)] structs a maintainer adds to the Rust crate (written out
+    in INTEGRATION.md) list the header's fields in the header's order."""
+    from lightcurve_fitting_gb300 import abi
+    text = open(os.path.join(ROOT, "INTEGRATION.md")).read()
+    pairs = {"LcfBandsCsr": abi.BandsCSR, "LcfFitOptions": abi.FitOptions, "LcfFitOutputs": abi.FitOutputs,
+             "LcfPsoSelection": abi.PsoSelection}
+    for rname, cls in pairs.items():
+        m = re.search(r"pub struct " + rname + r"\s*\{(.*?)\}", text, flags=re.S)
+        assert m, rname
+        fields = re.findall(r"pub (\w+)\s*:", m.group(1))
+        assert fields == [f for f, _ in cls._fields_], rname
