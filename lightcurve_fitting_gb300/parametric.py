@@ -64,6 +64,26 @@ def build_flux_bands(times, mags, mag_errs, bands) -> Dict[str, dict]:
     return out
 
 
+def build_raw_flux_bands(times, fluxes, flux_errs, bands) -> Dict[str, dict]:
+    """build_raw_flux_bands (src/common.rs:117-149): linear fluxes grouped by
+    band, times relative to the earliest time, non-finite or <= 0 values and
+    errors dropped."""
+    times = np.asarray(times, np.float64)
+    if times.size == 0:
+        return {}
+    jd_min = times.min()
+    out: Dict[str, dict] = {}
+    for t, f, e, b in zip(times, fluxes, flux_errs, bands):
+        f, e = float(f), float(e)
+        if not (math.isfinite(f) and math.isfinite(e)) or f <= 0 or e <= 0:
+            continue
+        d = out.setdefault(b, {"times": [], "values": [], "errors": []})
+        d["times"].append(float(t) - jd_min)
+        d["values"].append(f)
+        d["errors"].append(e)
+    return out
+
+
 def _batch_from_sources(sources: Sequence[Dict[str, dict]]):
     t, f, e, bo, so, names = [], [], [], [0], [0], []
     for bands in sources:
@@ -315,3 +335,50 @@ def finalize_all_models_with_gpu_svi(flux_bands: Dict[str, dict], gpu_results: S
                         [svi_outputs[i] for i in picks], abi.METHOD_SVI, ctx)
     return [_finalized(res, k, band_names[i], gpu_results[i], abi.METHOD_SVI, {}, gpu_results[i].get("multi_bazin"))
             for k, i in enumerate(picks)]
+
+
+def fit_parametric_multiband(bands: Dict[str, dict], method: str = "svi", ctx=None) -> List[dict]:
+    """fit_parametric_multiband (python/src/lib.rs:257-269, src/parametric.rs:3813-4131):
+    the joint multi-band Villar fit of one source, then per-band uncertainty,
+    refinements and MultiBazin.  The library's joint swarm fits 2 to 6
+    non-empty bands; a source with fewer raises ValueError (the reference
+    runs its joint swarm on a single band too)."""
+    meth = _method(method)
+    if not bands:
+        return []
+    if sum(1 for b in bands.values() if len(b["values"]) > 0) < 2:
+        raise ValueError("fit_parametric_multiband needs at least two non-empty bands")
+    batch, names = _batch_from_sources([bands])
+    ctx = ctx or default_context()
+    res = ctx.fit_batch(batch, fit_all_models=False, method=meth, forced_model=-1, run_multi_bazin=True,
+                        joint_multiband=True)
+    return results_from_fit(res, batch, names, False, meth, -1, [True])[0]
+
+
+_EVAL_EXPORTS = ["launch_bazin", "launch_villar", "launch_tde", "launch_arnett", "launch_magnetar",
+                 "launch_shock_cooling", "launch_afterglow", "launch_metzger_kn"]
+
+
+def eval_model(model: str, params, times) -> List[float]:
+    """eval_model (python/src/lib.rs:316-326, eval_model_flux
+    src/parametric.rs:3082-3097): the model's normalised flux at `times`
+    from the internal parameter vector, evaluated on the GPU by the
+    library's drop-in launch_* kernels (MetzgerKN: one ODE over all times)."""
+    import torch
+    from .lib import load
+    m = _model_id(model)
+    p = np.asarray(params, np.float64)
+    t = np.asarray(times, np.float64)
+    if p.size < abi.N_PARAMS[m]:
+        raise ValueError(f"{abi.MODEL_NAMES[m]} takes {abi.N_PARAMS[m]} parameters, got {p.size}")
+    if t.size == 0:
+        return []
+    L = load()
+    dev = torch.device("cuda", torch.cuda.current_device())
+    dp = torch.from_numpy(p).to(dev)
+    dt = torch.from_numpy(t).to(dev)
+    do = torch.empty(t.size, dtype=torch.float64, device=dev)
+    torch.cuda.synchronize()
+    getattr(L, _EVAL_EXPORTS[m])(dp.data_ptr(), dt.data_ptr(), do.data_ptr(), 1, int(t.size), int(p.size), 1, 256)
+    torch.cuda.synchronize()
+    return [float(x) for x in do.cpu().numpy()]

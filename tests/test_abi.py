@@ -107,3 +107,30 @@ def test_rust_bindings_in_the_integration_notes_match_the_header():
         assert m, rname
         fields = re.findall(r"pub (\w+)\s*:", m.group(1))
         assert fields == [f for f, _ in cls._fields_], rname
+
+
+def test_build_raw_flux_bands_matches_reference_rules():
+    """build_raw_flux_bands (src/common.rs:117-149): times relative to the
+    earliest time of all rows (dropped rows included), non-finite or
+    non-positive fluxes and errors dropped, linear values kept."""
+    from lightcurve_fitting_gb300.parametric import build_raw_flux_bands
+    t = [10.0, 11.0, 12.0, 13.0, 14.0]
+    f = [5.0, -1.0, 7.0, float("nan"), 2.0]
+    e = [0.5, 0.5, 0.0, 0.5, 0.25]
+    b = ["g", "g", "r", "r", "r"]
+    out = build_raw_flux_bands(t, f, e, b)
+    assert out == {"g": {"times": [0.0], "values": [5.0], "errors": [0.5]},
+                   "r": {"times": [4.0], "values": [2.0], "errors": [0.25]}}
+    assert build_raw_flux_bands([], [], [], []) == {}
+
+
+def test_python_api_rejects_before_touching_the_gpu():
+    from lightcurve_fitting_gb300 import parametric
+    with pytest.raises(ValueError, match="two non-empty bands"):
+        parametric.fit_parametric_multiband({"g": {"times": [0.0], "values": [1.0], "errors": [0.1]},
+                                             "r": {"times": [], "values": [], "errors": []}})
+    assert parametric.fit_parametric_multiband({}) == []
+    with pytest.raises(ValueError, match="takes 6 parameters"):
+        parametric.eval_model("Bazin", [0.0, 0.1], [1.0])
+    with pytest.raises(ValueError):
+        parametric.eval_model("NoSuchModel", [0.0], [1.0])
