@@ -48,6 +48,18 @@ def test_eval_model_matches_the_oracle(gpu, oracle, m):
         assert np.all(np.abs(got - ref) <= 1e-8 * np.maximum(np.abs(ref), 1e-10))
 
 
+def _same(a, b):
+    """Deep equality of result dicts with NaN equal to NaN (a MultiBazin
+    result holds NaN for the K it did not fit)."""
+    if isinstance(a, dict):
+        return isinstance(b, dict) and a.keys() == b.keys() and all(_same(a[k], b[k]) for k in a)
+    if isinstance(a, (list, tuple)):
+        return isinstance(b, (list, tuple)) and len(a) == len(b) and all(_same(x, y) for x, y in zip(a, b))
+    if isinstance(a, float) and isinstance(b, float) and np.isnan(a) and np.isnan(b):
+        return True
+    return a == b
+
+
 def test_fit_parametric_multiband_is_the_joint_branch(gpu):
     """fit_parametric_multiband on a 3-band source gives what fit_parametric
     (fit_all_models=False) gives for it: the joint Villar fit."""
@@ -57,5 +69,5 @@ def test_fit_parametric_multiband_is_the_joint_branch(gpu):
              for k, (t, f, e) in enumerate(batch.bands_of(0))}
     a = parametric.fit_parametric_multiband(bands, method="laplace")
     b = parametric.fit_parametric(bands, fit_all_models=False, method="laplace")
-    assert a == b and len(a) == 3
+    assert _same(a, b) and len(a) == 3
     assert all(r["model"] == "Villar" for r in a)
