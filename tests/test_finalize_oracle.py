@@ -159,3 +159,24 @@ def test_python_mirror_all_models_entries(oracle):
     assert [r["model"] for r in rows] == ["Bazin", "Arnett"]
     assert all(r["svi_elbo"] == pytest.approx(s[2]) for r, s in zip(rows, svi))
     assert ctx.calls[0][3]
+
+
+def test_bench_pair_batch_repeats_each_band_per_fitted_model(oracle):
+    """The finalisation leg's input: one one-band source per fitted (band,
+    model) pair, holding that band's observations and that model's polished
+    parameters and cost."""
+    import bench
+    batch = synth.config_uneven(4, seed=101)
+    res = oracle.fit_batch(batch, fit_all_models=True, method=abi.METHOD_LAPLACE, run_multi_bazin=False)
+    pairs, model, pso, cost = bench.pair_batch(batch, res, 3)
+    nb3 = int(batch.source_band_offsets[3])
+    fitted = [(b, m) for b in range(nb3) for m in range(8)
+              if res.model[b] >= 0 and np.isfinite(res.per_model_params[b, m, 0])]
+    assert pairs.n_bands == pairs.n_sources == len(fitted) == model.size
+    for i, (b, m) in enumerate(fitted):
+        o0, o1 = batch.band_obs_offsets[b], batch.band_obs_offsets[b + 1]
+        q0, q1 = pairs.band_obs_offsets[i], pairs.band_obs_offsets[i + 1]
+        assert np.array_equal(pairs.times[q0:q1], batch.times[o0:o1])
+        assert np.array_equal(pairs.flux[q0:q1], batch.flux[o0:o1])
+        assert model[i] == m and np.array_equal(pso[i], res.per_model_params[b, m], equal_nan=True)
+        assert cost[i] == res.per_model_chi2[b, m]
