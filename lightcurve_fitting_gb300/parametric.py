@@ -230,7 +230,8 @@ def _finalize_run(entries, gpu_rows, svi_rows, method: int, ctx):
         p = np.asarray(g["pso_params"], np.float64)
         model[i] = m
         pso[i, :min(n, p.size)] = p[:n]
-        cost[i] = g.get("pso_cost", np.nan) if g.get("pso_cost") is not None else np.nan
+        pc = g.get("pso_cost")
+        cost[i] = np.nan if pc is None else float(pc)
         if given:
             smu, sls, sel = svi_rows[i]
             mu[i, :n] = np.asarray(smu, np.float64)[:n]
