@@ -204,10 +204,15 @@ __device__ __forceinline__ float model_grad_f32(int m, const float* p, float th,
 // (src/parametric.rs:1415-1417, :2349-2352), with cdf(z) =
 // 0.5 * (1 + erf_approx(z / sqrt 2)).  For z < 0 the FP64 sum 1 + erf
 // quantises P = poly * e^{-z^2/2} to multiples of 2^-53 (exact as
-// 1 - fl(1 - P)); that quantisation is reproduced, and `huge` is set where it
-// reaches 0 and the reference divides by 1e-300 (gradients ~1e285).
-__device__ __forceinline__ float upper_ratio_f32(float z, bool& huge) {
-    huge = false;
+// 1 - fl(1 - P)); that quantisation is reproduced.  Where it leaves fewer
+// than 64 units (P * 2^53 < 63.5) the step between neighbouring units is too
+// coarse for an FP32 estimate of P to pick the reference's: at 0 units the
+// CDF is the 1e-300 floor and the ratio phi / 1e-300 reaches ~1e285 (beyond
+// FP32), at 1 unit it is ~10.  There `defer` is set, 0 is returned, and the
+// caller forms that observation's gradient terms itself (svi_deferred_pass:
+// at full magnitude, with the unit count decided in FP64 near the boundary).
+__device__ __forceinline__ float upper_ratio_f32(float z, bool& defer) {
+    defer = false;
     const float inv_sqrt_2pi = 0.3989422804014327f;
     float x = fabsf(z) * 0.70710678118654752f;
     float t = 1.0f / (1.0f + 0.3275911f * x);
@@ -220,14 +225,24 @@ __device__ __forceinline__ float upper_ratio_f32(float z, bool& huge) {
     float P = poly * e;
     if (P < 2.0e-9f) {
         // FP64: 1 - fl(1 - P) = round_half_even(P * 2^53) * 2^-53
-        float k = rintf(P * 9007199254740992.0f);
-        if (k == 0.0f) {
-            huge = true;
+        const float kq = P * 9007199254740992.0f;
+        if (kq < 63.5f) {
+            defer = true;
             return 0.0f;
         }
+        const float k = rintf(kq);
         return inv_sqrt_2pi * e / (0.5f * k * 1.1102230246251565e-16f);
     }
     return inv_sqrt_2pi * 2.0f / poly;
+}
+
+// P * 2^53 of upper_ratio_f32 for z < 0 (the unit count of the reference's
+// quantised CDF before rounding).
+__device__ __forceinline__ float upper_units_f32(float z) {
+    float x = fabsf(z) * 0.70710678118654752f;
+    float t = 1.0f / (1.0f + 0.3275911f * x);
+    float poly = t * (0.254829592f + t * (-0.284496736f + t * (1.421413741f + t * (-1.453152027f + t * 1.061405429f))));
+    return poly * expf(-x * x) * 9007199254740992.0f;
 }
 
 }  // namespace lcf

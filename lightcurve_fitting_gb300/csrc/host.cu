@@ -54,7 +54,7 @@ struct Xoshiro {
     double f64() { return (double)(next() >> 11) * (1.0 / 9007199254740992.0); }
 };
 
-void make_draw_tables(float* draws, double* draws64, float2* draws15, float* svi_eps) {
+void make_draw_tables(float* draws, double* draws64, float2* draws15, double* svi_eps) {
     const uint64_t seeds[3] = {42, 137, 271};
     for (int k = 0; k < 3; k++) {
         Xoshiro r(seeds[k]);
@@ -74,15 +74,15 @@ void make_draw_tables(float* draws, double* draws64, float2* draws15, float* svi
     // and parameter: u1 = max(U, 1e-10), u2 = U, eps = sqrt(-2 ln u1) cos(2 pi u2)
     for (int np = 5; np <= 7; np++) {
         Xoshiro r(42);
-        float* tab = svi_eps + (size_t)(np - 5) * SVI_STEPS * SVI_SAMPLES * 7;
+        double* tab = svi_eps + (size_t)(np - 5) * SVI_STEPS * SVI_SAMPLES * 7;
         for (int s = 0; s < SVI_STEPS; s++)
             for (int k = 0; k < SVI_SAMPLES; k++)
                 for (int j = 0; j < 7; j++) {
-                    float v = 0.0f;
+                    double v = 0.0;
                     if (j < np) {
                         double u1 = std::fmax(r.f64(), 1e-10);
                         double u2 = r.f64();
-                        v = (float)(std::sqrt(-2.0 * std::log(u1)) * std::cos(2.0 * 3.14159265358979323846 * u2));
+                        v = std::sqrt(-2.0 * std::log(u1)) * std::cos(2.0 * 3.14159265358979323846 * u2);
                     }
                     tab[((size_t)s * SVI_SAMPLES + k) * 7 + j] = v;
                 }
@@ -171,7 +171,7 @@ struct lcf_ctx {
     float* d_draws = nullptr;
     double* d_draws64 = nullptr;
     float2* d_draws15 = nullptr;
-    float* d_eps = nullptr;
+    double* d_eps = nullptr;
     // device buffers (capacity-sized)
     DevArr times, flux, ferr, boff, soff, stats_b, obs, t64, f64, fe64, var64, uf64, mag64, up, ffa, ffb, res, fits, out, mb,
         ctr, scratch, scratch64, scratch_svi, t0state, tasks[7], task_sorted, task_sorted_mb, band_order, joint_flag, joint_src, joint_res,
@@ -305,21 +305,22 @@ extern "C" int lcf_ctx_create(int device, lcf_ctx** out) {
     }
     ctx->pso_blocks_per_sm = ctx->cand_bps[0];
     // RNG tables
-    std::vector<float> draws((size_t)3 * DRAWS_PER_SEED), eps((size_t)3 * SVI_STEPS * SVI_SAMPLES * 7);
+    std::vector<float> draws((size_t)3 * DRAWS_PER_SEED);
+    std::vector<double> eps((size_t)3 * SVI_STEPS * SVI_SAMPLES * 7);
     std::vector<double> draws64(draws.size());
     std::vector<float2> draws15(draws.size());
     make_draw_tables(draws.data(), draws64.data(), draws15.data(), eps.data());
     if (cudaMalloc(&ctx->d_draws, draws.size() * sizeof(float)) != cudaSuccess ||
         cudaMalloc(&ctx->d_draws64, draws64.size() * sizeof(double)) != cudaSuccess ||
         cudaMalloc(&ctx->d_draws15, draws15.size() * sizeof(float2)) != cudaSuccess ||
-        cudaMalloc(&ctx->d_eps, eps.size() * sizeof(float)) != cudaSuccess) {
+        cudaMalloc(&ctx->d_eps, eps.size() * sizeof(double)) != cudaSuccess) {
         lcf_ctx_destroy(ctx);
         return LCF_E_NOMEM;
     }
     cudaMemcpy(ctx->d_draws, draws.data(), draws.size() * sizeof(float), cudaMemcpyHostToDevice);
     cudaMemcpy(ctx->d_draws64, draws64.data(), draws64.size() * sizeof(double), cudaMemcpyHostToDevice);
     cudaMemcpy(ctx->d_draws15, draws15.data(), draws15.size() * sizeof(float2), cudaMemcpyHostToDevice);
-    cudaMemcpy(ctx->d_eps, eps.data(), eps.size() * sizeof(float), cudaMemcpyHostToDevice);
+    cudaMemcpy(ctx->d_eps, eps.data(), eps.size() * sizeof(double), cudaMemcpyHostToDevice);
     *out = ctx;
     return LCF_OK;
 }

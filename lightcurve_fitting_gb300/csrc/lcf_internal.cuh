@@ -253,7 +253,7 @@ struct DeviceBatch {
     const float* draws;     // [3][DRAWS_PER_SEED] uniforms of seeds 42, 137, 271
     const double* draws64;  // the same uniforms in FP64 (swarm initialisation)
     const float2* draws15;  // 1.5 x those uniforms (FP64 products) as double-float pairs
-    const float* svi_eps;   // [3][SVI_STEPS][SVI_SAMPLES][7] noise for 5, 6, 7 params
+    const double* svi_eps;  // [3][SVI_STEPS][SVI_SAMPLES][7] noise for 5, 6, 7 params (FP64, the reference's draws)
     // results
     PsoResult* pso_res;     // per task slot
     ModelFit* fits;         // [n_bands * 8]
@@ -338,7 +338,7 @@ void launch_band_cost(int model, const float4* obs, int n, float t_last, const d
                       int with_prior, double* costs, float* scratch, cudaStream_t s);
 
 // Host-side generation of the RNG tables (host.cpp)
-void make_draw_tables(float* draws, double* draws64, float2* draws15, float* svi_eps);
+void make_draw_tables(float* draws, double* draws64, float2* draws15, double* svi_eps);
 void make_joint_draws(float* draws, int64_t per_seed);
 
 }  // namespace lcf

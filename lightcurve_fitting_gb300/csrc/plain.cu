@@ -399,7 +399,7 @@ __global__ void plain_svi_kernel(DeviceBatch d, int m, double* mscr_base) {
     double vp = 0.0, am = 0.0, av = 0.0;
     if (lane < np) vp = init[lane];
     else if (lane < 2 * np) vp = -1.0;
-    const float* eps_tab = d.svi_eps + (size_t)(np - 5) * SVI_STEPS * SVI_SAMPLES * 7;
+    const double* eps_tab = d.svi_eps + (size_t)(np - 5) * SVI_STEPS * SVI_SAMPLES * 7;
     double pc[MAXP], pw2[MAXP];
     for (int j = 0; j < np; j++) {
         pc[j] = j == se ? c_pri_c[m][j] : init[j];
@@ -419,9 +419,9 @@ __global__ void plain_svi_kernel(DeviceBatch d, int m, double* mscr_base) {
         if (m == METZGER) {
             if (lane < SVI_SAMPLES * 5) {
                 int k = lane / 5, q = lane % 5;
-                const float* ep = eps_tab + ((size_t)step * SVI_SAMPLES + k) * 7;
+                const double* ep = eps_tab + ((size_t)step * SVI_SAMPLES + k) * 7;
                 double th[MAXP];
-                for (int j = 0; j < np; j++) th[j] = mu[j] + sg[j] * (double)ep[j];
+                for (int j = 0; j < np; j++) th[j] = mu[j] + sg[j] * ep[j];
                 if (q > 0) th[q - 1] += 1e-5;
                 metzger_f64(th, bv.t, n, mscr + (size_t)lane * n);
             }
@@ -431,10 +431,10 @@ __global__ void plain_svi_kernel(DeviceBatch d, int m, double* mscr_base) {
         for (int j = 0; j < np; j++) { gmu[j] = 0.0; gls[j] = 0.0; }
         double elbo_sum = 0.0;
         for (int k = 0; k < SVI_SAMPLES; k++) {
-            const float* ep = eps_tab + ((size_t)step * SVI_SAMPLES + k) * 7;
+            const double* ep = eps_tab + ((size_t)step * SVI_SAMPLES + k) * 7;
             double th[MAXP], eps[MAXP];
             for (int j = 0; j < np; j++) {
-                eps[j] = (double)ep[j];
+                eps[j] = ep[j];
                 th[j] = mu[j] + sg[j] * eps[j];
             }
             double sx = exp(th[se]), sx2 = sx * sx;

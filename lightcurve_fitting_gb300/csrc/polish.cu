@@ -545,19 +545,172 @@ __device__ __forceinline__ float reduce_scatter8f(const float* v) {
     return c;
 }
 
+// FP64 value and gradient of an analytic model in the reference's own forms
+// (eval_model / *_flux_grad, src/parametric.rs:199-538), out of line: the
+// rare FP64 cases of svi_deferred_pass, kept apart so that the FP64 code's
+// registers do not count against the pass or the SVI loop around it.
+template <int M>
+__device__ __noinline__ double svi_model64(const double* p64, double t, double* g64) {
+    model_grad_f64(M, p64, t, g64);
+    return eval_model_f64(M, p64, t);
+}
+
+// x * e^lr in FP64, for |x| in FP32's range and any lr: e^lr is split into
+// 2^k * 2^f (0 <= f < 1), the FP32 mantissa x * 2^f is widened and scaled by
+// 2^k exactly, in two factors 2^k1 * 2^k2 built from their exponent bits.
+// k is clamped to [-2044, 2046] so that both factors are normal doubles
+// (k1, k2 in [-1022, 1023]); beyond that range the product has already
+// underflowed to 0 or overflowed to +-inf, as the reference's FP64 product
+// does.  Relative error ~1e-4 for |lr| ~ 700 (lr is an FP32 value), far
+// inside what the terms it carries need: they reach Adam through their order
+// of magnitude and sign.
+__device__ __forceinline__ double scaled_exp(float x, float lr) {
+    const float y = fminf(fmaxf(lr * 1.4426950408889634f, -3000.0f), 3000.0f);
+    const float kf = floorf(y);
+    const double m = (double)(x * exp2f(y - kf));
+    int k = (int)kf;
+    k = max(-2044, min(2046, k));
+    const int k1 = k / 2, k2 = k - k1;
+    return m * __longlong_as_double((long long)(k1 + 1023) << 52) * __longlong_as_double((long long)(k2 + 1023) << 52);
+}
+
+struct SviDeferred {
+    double dlx;   // lane l's share: the warp total of component l & 7
+    int floored;  // a deferred upper limit hit the CDF floor (warp-uniform)
+};
+
+// The reference's gradient terms of the upper limits that upper_ratio_f32
+// deferred: those whose quantised CDF 0.5 (1 + erf) holds fewer than 64 units
+// of 2^-53 (src/parametric.rs:2336-2352: dpred = -phi / (cdf sigma) times each
+// model-gradient component, and the sigma_extra term).
+//  * Deep below the floor (the FP32 unit count P * 2^53 < 0.25, so that FP64's
+//    rounds to 0 as well): cdf = 1e-300 and the ratio phi / 1e-300 = e^lr,
+//    lr = 690.78 - ln sqrt(2 pi) - z^2 / 2, spans 0 .. ~1e285.  The terms are
+//    carried at full magnitude into FP64 (scaled_exp) and reach the ELBO
+//    gradient and Adam as in the reference, whose second moment overflows and
+//    stops the components they touch.  The FP32 model gradient is exact to
+//    FP32 rounding except where a component underflows FP32; a component that
+//    is 0 in FP32 while the ratio could lift its FP64 value into range is
+//    taken from the FP64 model gradient instead (analytic models; MetzgerKN
+//    keeps its FP32 sweep's derivatives).
+//  * Near the floor (0.25 <= P * 2^53 < 63.5): everything in FP64 from the
+//    sample's FP64 parameters, as the reference does, so that the unit count
+//    (0, 1, 2, ...) and with it the ratio are the reference's.
+// Observations: bit r of xm = observation c0 + 32 r + lane, marked by the
+// FP32 loop.  Out of line and called after that loop by the whole warp, so
+// the hot loop holds none of this code's registers.
+template <int M>
+__device__ __noinline__ SviDeferred svi_deferred_pass(const float4* obs, const float* ms, float scl, int c0,
+                                                      unsigned long long xm, double th_j, float sx2) {
+    constexpr int np = n_params_of(M), se = se_idx_of(M);
+    const int lane = threadIdx.x & 31;
+    const float ln_ratio0 = 690.77552789821368f - 0.91893853320467274f;  // ln(1e300) - ln sqrt(2 pi)
+    double p64[MAXP], dx[MAXP];
+    float pf[MAXP];  // the sample's FP32 parameters, as the caller forms them
+#pragma unroll
+    for (int q = 0; q < MAXP; q++) {
+        p64[q] = q < np ? __shfl_sync(FULL, th_j, q) : 0.0;
+        pf[q] = (float)p64[q];
+        dx[q] = 0.0;
+    }
+    int floored = 0;
+    while (xm) {
+        const int i = c0 + ((__ffsll((long long)xm) - 1) << 5) + lane;
+        xm &= xm - 1;
+        const float4 ob = obs[i];
+        float gb[MAXP];
+        float pr;
+        if constexpr (M == METZGER) {
+            pr = ms[i * 5] * scl;
+            for (int q = 0; q < 4; q++) gb[q] = ms[i * 5 + 1 + q] * scl;
+            gb[4] = 0.0f;
+        } else {
+            int st;
+            pr = model_grad_f32(M, pf, ob.x, ob.y, gb, st);
+        }
+        const float tv = fabsf(ob.w) + sx2;
+        const float stv = sqrtf(tv);
+        const float z = (ob.z - pr) / stv;
+        if (upper_units_f32(z) < 0.25f) {
+            floored = 1;
+            const float lr = fmaf(-0.5f * z, z, ln_ratio0);
+            bool rescue = false;
+#pragma unroll
+            for (int q = 0; q < np; q++) {
+                if (q == se || !isfinite(gb[q])) continue;
+                if (gb[q] != 0.0f) dx[q] += scaled_exp(-gb[q] / stv, lr);
+                else if (M != METZGER && lr > 60.0f) rescue = true;  // ratio > 1e26: an FP32 underflow may matter
+            }
+            dx[se] += scaled_exp(-(ob.z - pr) * sx2 / (stv * tv), lr);
+            if constexpr (M != METZGER) {
+                if (rescue) {
+                    double g64[MAXP];
+                    svi_model64<M>(p64, (double)ob.x + (double)ob.y, g64);
+                    const double sc = scaled_exp(-1.0f / stv, lr);
+#pragma unroll
+                    for (int q = 0; q < np; q++)
+                        if (q != se && gb[q] == 0.0f && isfinite(g64[q])) dx[q] += sc * g64[q];
+                }
+            }
+        } else {
+            double g64[MAXP];
+            double pd;
+            if constexpr (M == METZGER) {
+                pd = (double)pr;
+                for (int q = 0; q < np; q++) g64[q] = (double)gb[q];
+            } else {
+                pd = svi_model64<M>(p64, (double)ob.x + (double)ob.y, g64);
+            }
+            if (!isfinite(pd)) continue;
+            const double sx = exp(p64[se]);
+            const double sxx = sx * sx;
+            const double tvd = (double)fabsf(ob.w) + sxx;
+            const double sd = sqrt(tvd);
+            const double uf = (double)ob.z;
+            const double zd = (uf - pd) / sd;
+            const double phi = exp(-0.5 * zd * zd) * 0.39894228040143267794;
+            const double raw = 0.5 * (1.0 + erf_approx_f64(zd * 0.70710678118654752440));
+            const double cdf = fmax(raw, 1e-300);
+            if (!(raw > 1e-300)) floored = 1;
+            const double dpred = -phi / (cdf * sd);
+#pragma unroll
+            for (int q = 0; q < np; q++)
+                if (q != se && isfinite(g64[q])) dx[q] += dpred * g64[q];
+            dx[se] += (phi / cdf) * (-(uf - pd) * sxx / (sd * tvd));
+        }
+    }
+    SviDeferred r;
+    r.dlx = 0.0;
+#pragma unroll
+    for (int q = 0; q < np; q++) {
+        const double v = warp_sum_d(dx[q]);
+        if (q == (lane & 7)) r.dlx = v;
+    }
+    r.floored = warp_or(floored);
+    return r;
+}
+
 // One reparameterised sample's log-likelihood over the band and its
 // gradient, the adjoint through the analytic model gradient (the body of an
 // SVI step, src/parametric.rs:2280-2330).  pf = the sample's parameters in
-// FP32, held by every lane; ms = this sample's MetzgerKN sweep rows (value +
-// 4 derivatives per observation), unused by the other models.  Returns false
-// when the reference skips the sample (MetzgerKN peak rescale outside its
-// clamp).  Otherwise lls = the log-likelihood (every lane), dl_tot = lane l's
-// total d loglik / d theta_{(l >> 2) & 7} (reduce_scatter8f), huge = 1 when an
-// upper-limit ratio overflowed in some lane (the reference's CDF floor).
+// FP32, held by every lane; th_j = lane j's component in FP64 (j = lane & 7);
+// ms = this sample's MetzgerKN sweep rows (value + 4 derivatives per
+// observation), unused by the other models.  Returns false when the
+// reference skips the sample (MetzgerKN peak rescale outside its clamp).
+// Otherwise lls = the log-likelihood (every lane), dl_tot = lane l's FP32
+// total d loglik / d theta_{(l >> 2) & 7} (reduce_scatter8f), dlx = lane l's
+// FP64 part of d loglik / d theta_{l & 7} from the upper limits at or near the
+// reference's CDF floor (svi_deferred_pass), floored = 1 when one of them was
+// at the floor.  The observations are taken in chunks of 2048: the FP32 loop
+// marks the deferred ones in a per-lane bitmask of its 32-observation rounds,
+// and the out-of-line pass after the loop evaluates them (only in the samples
+// that have any), so the FP32 loop carries none of that code's registers.
 template <int M>
-__device__ __forceinline__ bool svi_sample_loglik(const float4* obs, int n, const float* pf, const float* ms,
-                                                  double& lls, float& dl_tot, int& huge_out) {
+__device__ __forceinline__ bool svi_sample_loglik(const float4* obs, int n, const float* pf, double th_j,
+                                                  const float* ms, double& lls, float& dl_tot, double& dlx,
+                                                  int& floored) {
     constexpr int np = n_params_of(M), se = se_idx_of(M);
+    constexpr int CHUNK = 64 * 32;
     const int lane = threadIdx.x & 31;
     float sx = expf(pf[se]);
     float sx2 = sx * sx;
@@ -566,8 +719,9 @@ __device__ __forceinline__ bool svi_sample_loglik(const float4* obs, int n, cons
     for (int q = 0; q < 8; q++) dll[q] = 0.0f;
     Nll ll;
     ll.reset();
-    int huge = 0;
-    bool skip_sample = false;
+    dlx = 0.0;
+    floored = 0;
+    float scl = 1.0f;
     if constexpr (M == METZGER) {
         // predictions and derivatives of the normalised model, then the
         // reference's peak rescale (src/parametric.rs:2303-2323)
@@ -575,27 +729,30 @@ __device__ __forceinline__ bool svi_sample_loglik(const float4* obs, int n, cons
         for (int i = lane; i < n; i += 32)
             if (obs[i].w >= 0.0f) mx = fmaxf(mx, ms[i * 5]);
         for (int kk = 16; kk; kk >>= 1) mx = fmaxf(mx, __shfl_xor_sync(FULL, mx, kk));
-        float scl = 1.0f;
+        bool skip_sample = false;
         if (mx > 1e-10f && isfinite(mx)) {
             float raw = 1.0f / mx;
             scl = fminf(fmaxf(raw, 0.1f), 10.0f);
             if (fabsf(raw - scl) / raw > 0.5f) skip_sample = true;
         }
-        if (!skip_sample) {
-            for (int i = lane; i < n; i += 32) {
-                float4 ob = obs[i];
+        if (skip_sample) return false;  // warp-uniform: mx and scl are the warp's
+    }
+    for (int c0 = 0; c0 < n; c0 += CHUNK) {
+        const int c1 = min(n, c0 + CHUNK);
+        unsigned long long xm = 0;  // rounds of this chunk with a deferred observation of this lane
+        for (int i = c0 + lane; i < c1; i += 32) {
+            float4 ob = obs[i];
+            bool defer = false;
+            if constexpr (M == METZGER) {
                 float pr = ms[i * 5] * scl;
-                float gb[MAXP];
+                float gb[4];
                 for (int q = 0; q < 4; q++) gb[q] = ms[i * 5 + 1 + q] * scl;
-                gb[4] = 0.0f;
                 float tv = fabsf(ob.w) + sx2;
                 float stv = sqrtf(tv);
                 if (ob.w < 0.0f) {
                     float z = (ob.z - pr) / stv;
                     ll.add(log_normal_cdf_f(z));
-                    bool hg;
-                    float ratio = upper_ratio_f32(z, hg);
-                    if (hg) huge = 1;
+                    float ratio = upper_ratio_f32(z, defer);
                     for (int q = 0; q < 4; q++) if (isfinite(gb[q])) dll[q] += -ratio / stv * gb[q];
                     dll[se] += ratio * (-(ob.z - pr) * sx2 / (stv * tv));
                 } else {
@@ -606,42 +763,41 @@ __device__ __forceinline__ bool svi_sample_loglik(const float4* obs, int n, cons
                     for (int q = 0; q < 4; q++) if (isfinite(gb[q])) dll[q] += res * it * gb[q];
                     dll[se] += (r2 * it * it - it) * sx2;
                 }
-            }
-        }
-    } else {
-        for (int i = lane; i < n; i += 32) {
-            float4 ob = obs[i];
-            float gb[MAXP];
-            int st;
-            float pr = model_grad_f32(M, pf, ob.x, ob.y, gb, st);
-            if (st == ST_NONFINITE || !isfinite(pr)) continue;
-            float tv = fabsf(ob.w) + sx2;
-            float stv = sqrtf(tv);
-            if (ob.w < 0.0f) {
-                float z = (ob.z - pr) / stv;
-                ll.add(log_normal_cdf_f(z));
-                bool hg;
-                float ratio = upper_ratio_f32(z, hg);
-                if (hg) huge = 1;
-                float dpred = -ratio / stv;
-#pragma unroll
-                for (int q = 0; q < np; q++)
-                    if (q != se && isfinite(gb[q])) dll[q] += dpred * gb[q];
-                dll[se] += ratio * (-(ob.z - pr) * sx2 / (stv * tv));
             } else {
-                float res = ob.z - pr;
-                float it = 1.0f / tv;
-                float r2 = res * res;
-                ll.add(-0.5f * (r2 * it + logf(6.283185307179586f * tv)));
+                float gb[MAXP];
+                int st;
+                float pr = model_grad_f32(M, pf, ob.x, ob.y, gb, st);
+                if (st == ST_NONFINITE || !isfinite(pr)) continue;
+                float tv = fabsf(ob.w) + sx2;
+                float stv = sqrtf(tv);
+                if (ob.w < 0.0f) {
+                    float z = (ob.z - pr) / stv;
+                    ll.add(log_normal_cdf_f(z));
+                    float ratio = upper_ratio_f32(z, defer);
+                    float dpred = -ratio / stv;
 #pragma unroll
-                for (int q = 0; q < np; q++)
-                    if (q != se && isfinite(gb[q])) dll[q] += res * it * gb[q];
-                dll[se] += (r2 * it * it - it) * sx2;
+                    for (int q = 0; q < np; q++)
+                        if (q != se && isfinite(gb[q])) dll[q] += dpred * gb[q];
+                    dll[se] += ratio * (-(ob.z - pr) * sx2 / (stv * tv));
+                } else {
+                    float res = ob.z - pr;
+                    float it = 1.0f / tv;
+                    float r2 = res * res;
+                    ll.add(-0.5f * (r2 * it + logf(6.283185307179586f * tv)));
+#pragma unroll
+                    for (int q = 0; q < np; q++)
+                        if (q != se && isfinite(gb[q])) dll[q] += res * it * gb[q];
+                    dll[se] += (r2 * it * it - it) * sx2;
+                }
             }
+            if (defer) xm |= 1ull << ((i - c0) >> 5);
+        }
+        if (__any_sync(FULL, xm != 0)) {
+            const SviDeferred r = svi_deferred_pass<M>(obs, ms, scl, c0, xm, th_j, sx2);
+            dlx += r.dlx;
+            floored |= r.floored;
         }
     }
-    if (__any_sync(FULL, skip_sample)) return false;
-    huge_out = warp_or(huge);
     lls = warp_sum_d((double)ll.s - (double)ll.c);
     dl_tot = reduce_scatter8f(dll);
     return true;
@@ -666,8 +822,7 @@ __device__ void svi_band(const DeviceBatch& d, int b) {
     double vp = 0.0, am = 0.0, av = 0.0;
     if (lane < np) vp = o.pso_params[lane];
     else if (lane < 2 * np) vp = -1.0;
-    bool frozen = false;
-    const float* eps_tab = d.svi_eps + (size_t)(np - 5) * SVI_STEPS * SVI_SAMPLES * 7;
+    const double* eps_tab = d.svi_eps + (size_t)(np - 5) * SVI_STEPS * SVI_SAMPLES * 7;
     const double ln_2pie = 2.8378770664093453;  // ln(2 pi e)
     double b1t = 1.0, b2t = 1.0;
     double ema = -INFINITY, best_ema = -INFINITY, final_elbo = -INFINITY;
@@ -693,9 +848,9 @@ __device__ void svi_band(const DeviceBatch& d, int b) {
             bool mz_ok = false;
             float mz_lp = 0.0f, mz_lpd = 0.0f;
             if (lane < 4 * SVI_SAMPLES) {
-                const float* ep = eps_tab + ((size_t)step * SVI_SAMPLES + smp) * 7;
+                const double* ep = eps_tab + ((size_t)step * SVI_SAMPLES + smp) * 7;
                 float pv[MAXP];
-                for (int q = 0; q < np; q++) pv[q] = (float)(mu[q] + sg[q] * (double)ep[q]);
+                for (int q = 0; q < np; q++) pv[q] = (float)(mu[q] + sg[q] * ep[q]);
                 mz_ok = metzger_dual_raw<1>(pv, tan, (float)bs.t_last, otimes, n, mscr + (size_t)smp * 5 * n, mz_lp,
                                             &mz_lpd);
             }
@@ -719,21 +874,21 @@ __device__ void svi_band(const DeviceBatch& d, int b) {
             __syncwarp();
         }
         double gmu_j = 0.0, gls_j = 0.0, elbo_sum = 0.0;
-        int huge_any = 0;
         for (int k = 0; k < SVI_SAMPLES; k++) {
-            const float* ep = eps_tab + ((size_t)step * SVI_SAMPLES + k) * 7;
-            const double eps_j = own ? (double)ep[j] : 0.0;
+            const double* ep = eps_tab + ((size_t)step * SVI_SAMPLES + k) * 7;
+            const double eps_j = own ? ep[j] : 0.0;
             const double th_j = mu_j + sg_j * eps_j;
             float pf[MAXP];
 #pragma unroll
             for (int q = 0; q < MAXP; q++) pf[q] = q < np ? __shfl_sync(FULL, (float)th_j, q) : 0.0f;
-            double lls;
+            double lls, dlx;
             float dl_tot;
-            int huge;
-            if (!svi_sample_loglik<M>(obs, n, pf, mscr + (size_t)k * 5 * n, lls, dl_tot, huge)) continue;
-            if (huge) huge_any = 1;
-            // lane j: total d loglik / d theta_j, then its prior and ELBO terms
-            const double dl_j = (double)__shfl_sync(FULL, dl_tot, (4 * j) & 31);
+            int floored;
+            if (!svi_sample_loglik<M>(obs, n, pf, th_j, mscr + (size_t)k * 5 * n, lls, dl_tot, dlx, floored))
+                continue;
+            // lane j: total d loglik / d theta_j (FP32 terms, plus the FP64
+            // terms of deferred upper limits), then its prior and ELBO terms
+            const double dl_j = (double)__shfl_sync(FULL, dl_tot, (4 * j) & 31) + dlx;
             double lp_j = 0.0;
             if (own) {
                 const double dd = th_j - pc_j;
@@ -756,8 +911,9 @@ __device__ void svi_band(const DeviceBatch& d, int b) {
         else if (lane < 2 * np) gi = -(gls_i / ns + 1.0);
         b1t *= 0.9;
         b2t *= 0.999;
-        if (huge_any) frozen = true;  // the reference's v overflows to +inf: updates stop
-        if (lane < 2 * np && isfinite(gi) && !frozen) {
+        // a component hit by a floored upper limit's ~1e285 term overflows its
+        // second moment to +inf and stops, as in the reference
+        if (lane < 2 * np && isfinite(gi)) {
             am = 0.9 * am + (1.0 - 0.9) * gi;
             av = 0.999 * av + (1.0 - 0.999) * gi * gi;
             double mh = am / (1.0 - b1t), vh = av / (1.0 - b2t);
@@ -841,7 +997,7 @@ __device__ void svi_grad_point(const float4* obs, int n, float t_last, const dou
         __device__ float operator()(int q) const { return o[q].x + o[q].y; }
     } otimes{obs};
     double gmu_j = 0.0, gls_j = 0.0, elbo_sum = 0.0;
-    int huge_any = 0, skipped = 0;
+    int floored_any = 0, skipped = 0;
     for (int k = 0; k < n_samples; k++) {
         const double eps_j = own ? eps[(size_t)k * np + j] : 0.0;
         const double th_j = mu_j + sg_j * eps_j;
@@ -852,17 +1008,17 @@ __device__ void svi_grad_point(const float4* obs, int n, float t_last, const dou
             if (lane == 0) metzger_dual_sweep(pf, t_last, otimes, n, mscr);
             __syncwarp();
         }
-        double lls;
+        double lls, dlx;
         float dl_tot;
-        int huge;
-        const bool ok = svi_sample_loglik<M>(obs, n, pf, mscr, lls, dl_tot, huge);
+        int floored;
+        const bool ok = svi_sample_loglik<M>(obs, n, pf, th_j, mscr, lls, dl_tot, dlx, floored);
         __syncwarp();  // the MetzgerKN rows are rewritten by the next sample
         if (!ok) {
             skipped = 1;
             continue;
         }
-        if (huge) huge_any = 1;
-        const double dl_j = (double)__shfl_sync(FULL, dl_tot, (4 * j) & 31);
+        if (floored) floored_any = 1;
+        const double dl_j = (double)__shfl_sync(FULL, dl_tot, (4 * j) & 31) + dlx;
         double lp_j = 0.0;
         if (own) {
             const double dd = th_j - pc_j;
@@ -882,7 +1038,7 @@ __device__ void svi_grad_point(const float4* obs, int n, float t_last, const dou
     }
     if (lane == 0) {
         *elbo_out = elbo_sum / ns + ent;
-        *flags_out = huge_any | (skipped << 1);
+        *flags_out = floored_any | (skipped << 1);
     }
 }
 

@@ -244,4 +244,6 @@ def test_autograd_wrapper_scales_by_incoming_gradient(ctx):
     elbo, _ = svi_elbo(x, band, 0, init, eps, ctx)
     w = torch.arange(1, vp.shape[0] + 1, dtype=torch.float64)
     (elbo * w).sum().backward()
-    assert np.array_equal(x.grad.numpy(), g_raw * w.numpy()[:, None])
+    # a point whose draws put an upper limit at the CDF floor has +-inf / NaN
+    # components, as the reference's gradient has there
+    assert np.array_equal(x.grad.numpy(), g_raw * w.numpy()[:, None], equal_nan=True)
