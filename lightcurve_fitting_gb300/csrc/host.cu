@@ -1276,11 +1276,17 @@ extern "C" int lcf_download_outputs(lcf_ctx* ctx, lcf_fit_outputs* out) {
 // ---------------------------------------------------------------------------
 // FP32 observation records of one peak-normalised band, sorted by time
 // (stable), as prep_kernel builds them for a fit; returns the last time.
+// NaN times sort after all others (in input order), the order
+// lcf_band_cost_static's device ranking uses.
 static double band_records(const double* times, const double* flux, const double* obs_var, const uint8_t* is_upper,
                            const double* upper_flux, int n_obs, std::vector<float4>& rec) {
     std::vector<int> ord(n_obs);
     for (int i = 0; i < n_obs; i++) ord[i] = i;
-    std::stable_sort(ord.begin(), ord.end(), [&](int a, int b) { return times[a] < times[b]; });
+    std::stable_sort(ord.begin(), ord.end(), [&](int a, int b) {
+        const bool na = std::isnan(times[a]), nb = std::isnan(times[b]);
+        if (na || nb) return !na && nb;
+        return times[a] < times[b];
+    });
     rec.assign(std::max(n_obs, 1), make_float4(0.0f, 0.0f, 0.0f, 0.0f));
     double t_last = -INFINITY;
     for (int k = 0; k < n_obs; k++) {

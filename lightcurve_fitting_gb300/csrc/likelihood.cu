@@ -80,6 +80,10 @@ static __device__ __align__(256) float g_band_cost_scratch[STATIC_SCRATCH_FLOATS
 
 // One block: time-sorted FP32 records of the caller's band and its last time
 // into the static array (same records as lcf_band_cost builds on the host).
+// Observation i goes to slot rank(i) = the number of observations before it
+// in a strict total order: times ascending, NaN times after all others, ties
+// in input order.  The ranks are therefore a permutation of 0..n-1 and every
+// record slot the cost kernel reads is written by this call.
 __global__ void static_prep_kernel(const double* t, const double* f, const double* var, const uint8_t* up,
                                    const double* uf, int n, float* scratch) {
     float4* rec = reinterpret_cast<float4*>(scratch);
@@ -88,10 +92,13 @@ __global__ void static_prep_kernel(const double* t, const double* f, const doubl
     for (int i = threadIdx.x; i < n; i += blockDim.x) {
         double ti = t[i];
         mx = fmax(mx, ti);
+        const bool ni = isnan(ti);
         int pos = 0;
         for (int j = 0; j < n; j++) {
             double tj = t[j];
-            pos += (tj < ti || (tj == ti && j < i)) ? 1 : 0;
+            const bool nj = isnan(tj);
+            const bool before = ni ? (!nj || j < i) : (!nj && (tj < ti || (tj == ti && j < i)));
+            pos += before ? 1 : 0;
         }
         float th = (float)ti;
         bool u = up[i] != 0;
