@@ -16,7 +16,8 @@
  *     device-resident pipeline.
  *
  *  2. Drop-in exports with the exact names and signatures the reference's
- *     Rust host binds (src/gpu_cuda.rs:31-40 and :102-164), so that an
+ *     Rust host binds (src/gpu_cuda.rs:31-40 and :102-164), and the
+ *     semantics of the reference kernels behind them, so that an
  *     unmodified `GpuContext` links against this library instead of the
  *     reference's `liblightcurve_cuda.a` (build.rs:14-18).  They take device
  *     pointers and launch on the legacy default stream, as the reference's do.
@@ -390,16 +391,52 @@ void launch_afterglow(const double* p, const double* t, double* o, int nd, int n
  * (src/parametric.rs:544-648). */
 void launch_metzger_kn(const double* p, const double* t, double* o, int nd, int nt, int np, int grid, int block);
 
-/* launch_batch_pso_cost, bound at src/gpu_cuda.rs:102-118:
- * costs[s * n_particles + k] = sum_obs NLL / n for positions
- * [s][k][n_params]; sigma_extra is the last parameter; 1e99 on a non-finite
- * prediction.  `grid` and `block` are accepted and ignored (the launch shape
- * is this library's). */
+/* launch_batch_pso_cost, bound at src/gpu_cuda.rs:102-118 (kernel
+ * cuda/models.cu:516-584): costs[s * n_particles + k] = sum over the
+ * source's observations of (pred - y)^2 / v + ln v (detections) or
+ * -ln Phi((u - pred) / sqrt v) (upper limits), v = obs_var + sigma_extra^2,
+ * divided by n, for positions [s][k][n_params]; sigma_extra is the last
+ * parameter; 1e99 for a source with no observations or a non-finite
+ * prediction.  As in the reference kernel (and unlike the CPU path's PsoCost)
+ * there is no prior, no Villar constraint and no MetzgerKN peak rescale, and
+ * MetzgerKN (model 7) is evaluated per observation on its own 100-point ODE
+ * grid (cuda/models_device.h:376-456).  `grid` and `block` are accepted and
+ * ignored (the launch shape is this library's). */
 void launch_batch_pso_cost(const double* all_times, const double* all_flux,
                            const double* all_obs_var, const int* all_is_upper,
                            const double* all_upper_flux, const int* source_offsets,
                            const double* positions, double* costs, int n_sources,
                            int n_particles, int n_params, int model_id, int grid, int block);
+
+/* launch_batch_pso_cost_multi_bazin, bound at src/gpu_cuda.rs:120-135
+ * (kernel cuda/models.cu:318-362): the same cost for MultiBazin, the sum of
+ * K = source_k[s] Bazin components (log A, t0, log tau_rise, log tau_fall
+ * each) plus the baseline B (position 4K) and log sigma_extra (4K + 1);
+ * rows padded to n_params = 4 max_K + 2. */
+void launch_batch_pso_cost_multi_bazin(const double* all_times, const double* all_flux,
+                                       const double* all_obs_var, const int* all_is_upper,
+                                       const double* all_upper_flux, const int* source_offsets,
+                                       const double* positions, double* costs, const int* source_k,
+                                       int n_sources, int n_particles, int n_params, int grid, int block);
+
+/* launch_batch_svi_fit, bound at src/gpu_cuda.rs:139-164 (kernel
+ * cuda/svi.cu:48-367): the reference GPU's SVI of each source from
+ * pso_params [n_sources * max_params], with model_ids, n_params_arr and
+ * se_idx_arr per source and Gaussian priors prior_centers / prior_widths
+ * [n_sources * max_params]; outputs out_mu, out_log_sigma
+ * [n_sources * max_params] (padded with 0) and out_elbo [n_sources].  Its
+ * semantics are that kernel's, not the CPU path's svi_fit: noise from
+ * xorshift64 seeded 42 + source * 123456789, MetzgerKN per observation with a
+ * forward-difference gradient, early stop after >= 50 steps on a 20-step
+ * stall, log sigma reported without the ln 4 inflation; a source without
+ * observations gets out_elbo = -1e99 and nothing else. */
+void launch_batch_svi_fit(const double* all_times, const double* all_flux,
+                          const double* all_obs_var, const int* all_is_upper,
+                          const double* all_upper_flux, const int* source_offsets,
+                          const double* pso_params, const int* model_ids, const int* n_params_arr,
+                          const int* se_idx_arr, const double* prior_centers, const double* prior_widths,
+                          double* out_mu, double* out_log_sigma, double* out_elbo, int n_sources,
+                          int max_params, int n_steps, int n_samples, double lr, int grid, int block);
 
 #ifdef __cplusplus
 }

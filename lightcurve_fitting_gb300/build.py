@@ -1,7 +1,7 @@
 """Build liblcf_gb300.so in-tree with nvcc for sm_103a.
 
-Seven translation units are compiled in parallel (pso, polish, finalize,
-plain, joint, likelihood, host) and linked into lightcurve_fitting_gb300/liblcf_gb300.so with the CUDA runtime
+Eight translation units are compiled in parallel (pso, polish, finalize,
+plain, joint, likelihood, compat, host) and linked into lightcurve_fitting_gb300/liblcf_gb300.so with the CUDA runtime
 linked statically.  No cmake; objects go to lightcurve_fitting_gb300/_build/.
 """
 from __future__ import annotations
@@ -17,7 +17,7 @@ ROOT = os.path.dirname(HERE)
 CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "liblcf_gb300.so")
-SOURCES = ["pso.cu", "polish.cu", "finalize.cu", "plain.cu", "joint.cu", "likelihood.cu", "host.cu"]
+SOURCES = ["pso.cu", "polish.cu", "finalize.cu", "plain.cu", "joint.cu", "likelihood.cu", "compat.cu", "host.cu"]
 # Units whose FP32 arithmetic (the swarms, SVI and the joint swarm) uses nvcc's
 # fast single-precision forms: SFU exp / log, approximate division and square
 # root, denormals flushed.  FP64 arithmetic is unaffected by the flag.  The

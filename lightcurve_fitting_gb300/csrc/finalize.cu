@@ -8,8 +8,7 @@
 //   * the profile t0 search (:1767-1849) and the greedy MultiBazin K = 1..4
 //     fit (:1008-1157), whose PSO runs execute in pso.cu and whose task lists
 //     are appended here on the device, so the whole sequence needs no host
-//     round trip;
-//   * the reference's drop-in `launch_*` exports (cuda/models.cu:590-636).
+//     round trip.
 // One warp per band; the lanes split the observations, the FP64 sums are
 // reduced across the warp.
 #include <cuda_runtime.h>
@@ -1016,143 +1015,3 @@ void launch_mb_build(const DeviceBatch& d, int slot, int k, cudaStream_t s) {
 }
 
 }  // namespace lcf
-
-// ---------------------------------------------------------------------------
-// Reference drop-in exports (cuda/models.cu:590-636 as bound by
-// src/gpu_cuda.rs:31-40, :102-118): FP64, device pointers, default stream.
-// ---------------------------------------------------------------------------
-namespace {
-
-__global__ void eval_draws_kernel(int m, const double* p, const double* t, double* o, int nd, int nt, int np) {
-    int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (idx >= (int64_t)nd * nt) return;
-    int dd = (int)(idx / nt), ti = (int)(idx % nt);
-    o[idx] = lcf::eval_model_f64(m, p + (int64_t)dd * np, t[ti]);
-}
-
-// MetzgerKN over the whole (unsorted) times array of one draw
-__global__ void metzger_draws_kernel(const double* p, const double* t, double* o, int nd, int nt, int np,
-                                     double* tmp) {
-    int dd = blockIdx.x * blockDim.x + threadIdx.x;
-    if (dd >= nd) return;
-    // sort the times by insertion into tmp (stable), evaluate, scatter back
-    double* ts = tmp + (int64_t)dd * 2 * nt;
-    double* ys = ts + nt;
-    for (int i = 0; i < nt; i++) {
-        double v = t[i];
-        int j = i;
-        while (j > 0 && ts[j - 1] > v) { ts[j] = ts[j - 1]; j--; }
-        ts[j] = v;
-    }
-    lcf::metzger_f64(p + (int64_t)dd * np, ts, nt, ys);
-    for (int i = 0; i < nt; i++) {
-        // position of t[i] in the sorted array (first match of equal times)
-        int lo = 0, hi = nt;
-        while (lo < hi) {
-            int mid = (lo + hi) / 2;
-            if (ts[mid] < t[i]) lo = mid + 1; else hi = mid;
-        }
-        o[(int64_t)dd * nt + i] = ys[lo];
-    }
-}
-
-void eval_draws(int m, const double* p, const double* t, double* o, int nd, int nt, int np) {
-    int64_t total = (int64_t)nd * nt;
-    if (total <= 0) return;
-    eval_draws_kernel<<<(int)((total + 255) / 256), 256>>>(m, p, t, o, nd, nt, np);
-}
-
-// tmp (MetzgerKN only): per (source, particle) 2 * n doubles at
-// 2 * (offs[s] * n_part + k * n)
-__global__ void pso_cost_compat_kernel(const double* all_t, const double* all_f, const double* all_var,
-                                       const int* all_up, const double* all_uf, const int* offs,
-                                       const double* pos, double* costs, int n_src, int n_part, int np, int model,
-                                       double* tmp) {
-    int idx = blockIdx.x * blockDim.x + threadIdx.x;
-    if (idx >= n_src * n_part) return;
-    int s = idx / n_part, k = idx % n_part;
-    int o0 = offs[s], o1 = offs[s + 1], n = o1 - o0;
-    const double* p = pos + (int64_t)idx * np;
-    double se = exp(p[np - 1]);
-    double se2 = se * se;
-    double nll = 0.0;
-    double* ts = nullptr;
-    double* ys = nullptr;
-    double scale = 1.0;
-    if (model == 7) {
-        ts = tmp + 2 * ((int64_t)o0 * n_part + (int64_t)k * n);
-        ys = ts + n;
-        for (int i = 0; i < n; i++) {
-            double v = all_t[o0 + i];
-            int j = i;
-            while (j > 0 && ts[j - 1] > v) { ts[j] = ts[j - 1]; j--; }
-            ts[j] = v;
-        }
-        lcf::metzger_f64(p, ts, n, ys);
-        double mx = -INFINITY;
-        for (int i = 0; i < n; i++) {
-            int lo = 0, hi = n;
-            while (lo < hi) { int mid = (lo + hi) / 2; if (ts[mid] < all_t[o0 + i]) lo = mid + 1; else hi = mid; }
-            if (!all_up[o0 + i]) mx = fmax(mx, ys[lo]);
-        }
-        if (mx > 1e-10 && isfinite(mx)) scale = fmin(fmax(1.0 / mx, 0.1), 10.0);
-    }
-    for (int i = 0; i < n; i++) {
-        double y;
-        if (model == 7) {
-            int lo = 0, hi = n;
-            while (lo < hi) { int mid = (lo + hi) / 2; if (ts[mid] < all_t[o0 + i]) lo = mid + 1; else hi = mid; }
-            y = ys[lo] * scale;
-        } else {
-            y = lcf::eval_model_f64(model, p, all_t[o0 + i]);
-        }
-        if (!isfinite(y)) { nll = 1e99; break; }
-        double tv = all_var[o0 + i] + se2;
-        if (all_up[o0 + i]) nll -= lcf::log_normal_cdf_f64((all_uf[o0 + i] - y) / sqrt(tv));
-        else {
-            double dd = y - all_f[o0 + i];
-            nll += dd * dd / tv + log(tv);
-        }
-    }
-    costs[idx] = nll >= 1e99 ? 1e99 : nll / (double)(n > 0 ? n : 1);
-}
-
-}  // namespace
-
-extern "C" {
-void launch_bazin(const double* p, const double* t, double* o, int nd, int nt, int np, int, int) { eval_draws(0, p, t, o, nd, nt, np); }
-void launch_villar(const double* p, const double* t, double* o, int nd, int nt, int np, int, int) { eval_draws(1, p, t, o, nd, nt, np); }
-void launch_tde(const double* p, const double* t, double* o, int nd, int nt, int np, int, int) { eval_draws(2, p, t, o, nd, nt, np); }
-void launch_arnett(const double* p, const double* t, double* o, int nd, int nt, int np, int, int) { eval_draws(3, p, t, o, nd, nt, np); }
-void launch_magnetar(const double* p, const double* t, double* o, int nd, int nt, int np, int, int) { eval_draws(4, p, t, o, nd, nt, np); }
-void launch_shock_cooling(const double* p, const double* t, double* o, int nd, int nt, int np, int, int) { eval_draws(5, p, t, o, nd, nt, np); }
-void launch_afterglow(const double* p, const double* t, double* o, int nd, int nt, int np, int, int) { eval_draws(6, p, t, o, nd, nt, np); }
-void launch_metzger_kn(const double* p, const double* t, double* o, int nd, int nt, int np, int, int) {
-    if (nd <= 0 || nt <= 0) return;
-    double* tmp = nullptr;
-    if (cudaMalloc(&tmp, (size_t)nd * 2 * nt * sizeof(double)) != cudaSuccess) return;
-    metzger_draws_kernel<<<(nd + 63) / 64, 64>>>(p, t, o, nd, nt, np, tmp);
-    cudaFree(tmp);
-}
-void launch_batch_pso_cost(const double* all_times, const double* all_flux, const double* all_obs_var,
-                           const int* all_is_upper, const double* all_upper_flux, const int* source_offsets,
-                           const double* positions, double* costs, int n_sources, int n_particles, int n_params,
-                           int model_id, int, int) {
-    int total = n_sources * n_particles;
-    if (total <= 0) return;
-    double* tmp = nullptr;
-    if (model_id == 7) {
-        int n_obs = 0;
-        if (cudaMemcpy(&n_obs, source_offsets + n_sources, sizeof(int), cudaMemcpyDeviceToHost) != cudaSuccess) return;
-        if (cudaMalloc(&tmp, (size_t)2 * n_particles * (size_t)(n_obs > 0 ? n_obs : 1) * sizeof(double)) != cudaSuccess)
-            return;
-    }
-    pso_cost_compat_kernel<<<(total + 127) / 128, 128>>>(all_times, all_flux, all_obs_var, all_is_upper,
-                                                         all_upper_flux, source_offsets, positions, costs, n_sources,
-                                                         n_particles, n_params, model_id, tmp);
-    if (tmp) {
-        cudaDeviceSynchronize();
-        cudaFree(tmp);
-    }
-}
-}

@@ -482,6 +482,65 @@ __device__ __forceinline__ bool metzger_sweep64(const double* p, const double* t
     return true;
 }
 
+// MetzgerKN at one observation as the reference's GPU cost and SVI kernels
+// evaluate it (cuda/models_device.h:376-456, cuda/models.cu:429-511): its
+// own 100-point log grid from 0.01 d to 1.05 x the observation's phase
+// (at least 0.02 d), the same explicit-Euler thermal / kinetic energy ODE as
+// the band sweep, the luminosity interpolated at the phase and divided by the
+// grid's running maximum; 0 before t0 or for a non-positive / non-finite
+// maximum.  This is a different model evaluation from the band sweep above
+// (whole-band grid, band peak) and from the CPU path; the operations keep the
+// reference kernel's order so that FP64 rounding matches it.
+__device__ inline double metzger_at_obs_f64(const double* p, double t) {
+    const double MSUN = 1.989e33, C = 2.998e10, SPD = 86400.0, PI = 3.14159265358979323846;
+    const double m_ej = pow(10.0, p[0]) * MSUN, v_ej = pow(10.0, p[1]) * C, kappa_r = pow(10.0, p[2]);
+    const double phase = t - p[3];
+    if (phase <= 0.0) return 0.0;
+    const double phase_max = fmax(phase * 1.05, 0.02);
+    const int NG = 100;
+    const double lmin = log(0.01), lmax = log(phase_max);
+    const double xn0 = 1.0 - 2.0 * 0.1;
+    const double xr = 1.0 - xn0;
+    const double e0 = 0.5 * m_ej * v_ej * v_ej;
+    double e_th = e0 / 1e40, e_kin = e0 / 1e40, v = v_ej;
+    const double gt0 = exp(lmin);
+    double r = gt0 * SPD * v;
+    double l_peak = 0.0, l_at = 0.0, prev_t = gt0, prev_l = 0.0;
+    for (int i = 0; i < NG; i++) {
+        const double t_day = exp(lmin + (lmax - lmin) * (double)i / (double)(NG - 1));
+        const double t_sec = t_day * SPD;
+        const double ef = 0.34 * pow(t_day, 0.74);
+        const double eth = 0.36 * (exp(-0.56 * t_day) + (ef > 1e-10 ? log(1.0 + ef) / ef : 1.0));
+        const double xn = xn0 * exp(-t_sec / 900.0);
+        const double tt = fmax(0.5 - atan((t_sec - 1.3) / 0.11) / PI, 1e-30);
+        const double eps_rp = 2e18 * eth * pow(tt, 1.3);
+        const double l_heat = m_ej * (3.2e14 * xn + eps_rp) / 1e40;
+        const double kappa_eff = 0.4 * (xn0 - xn) + kappa_r * xr;
+        const double t_diff = 3.0 * kappa_eff * m_ej / (4.0 * PI * C * v * t_sec) + r / C;
+        const double l_rad = (e_th > 0.0 && t_diff > 0.0) ? e_th / t_diff : 0.0;
+        if (l_rad > l_peak) l_peak = l_rad;
+        if (i > 0 && phase >= prev_t && phase <= t_day)
+            l_at = prev_l + (phase - prev_t) / (t_day - prev_t) * (l_rad - prev_l);
+        if (i == NG - 1 && phase >= t_day) l_at = l_rad;
+        if (i == 0 && phase <= t_day) l_at = l_rad;
+        prev_t = t_day;
+        prev_l = l_rad;
+        const double l_pdv = r > 0.0 ? e_th * v / r : 0.0;
+        if (i < NG - 1) {
+            const double t_next = exp(lmin + (lmax - lmin) * (double)(i + 1) / (double)(NG - 1));
+            const double dts = (t_next - t_day) * SPD;
+            e_th += (l_heat - l_pdv - l_rad) * dts;
+            if (e_th < 0.0) e_th = 0.0;
+            e_kin += l_pdv * dts;
+            v = sqrt(2.0 * e_kin * 1e40 / m_ej);
+            if (v > C) v = C;
+            r += v * dts;
+        }
+    }
+    if (l_peak <= 0.0 || !isfinite(l_peak)) return 0.0;
+    return l_at / l_peak;
+}
+
 // MetzgerKN predictions of the band (metzger_kn_eval_batch): the sweep's
 // interpolants divided by l_peak; all zeros when the reference returns
 // zeros (phase_max <= 0.01, or a non-positive / non-finite peak).

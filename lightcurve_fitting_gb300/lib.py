@@ -66,6 +66,10 @@ def load(path: str = LIB_PATH):
         getattr(L, name).restype = None
     L.launch_batch_pso_cost.argtypes = [vp, vp, vp, vp, vp, vp, vp, vp, i, i, i, i, i, i]
     L.launch_batch_pso_cost.restype = None
+    L.launch_batch_pso_cost_multi_bazin.argtypes = [vp, vp, vp, vp, vp, vp, vp, vp, vp, i, i, i, i, i]
+    L.launch_batch_pso_cost_multi_bazin.restype = None
+    L.launch_batch_svi_fit.argtypes = [vp] * 15 + [i, i, i, i, d, i, i]
+    L.launch_batch_svi_fit.restype = None
     _lib = L
     return L
 

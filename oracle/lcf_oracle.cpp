@@ -2035,6 +2035,209 @@ static void finalize_source(const lcf_bands_csr* in, int src, const int32_t* mod
 // ---------------------------------------------------------------------------
 using namespace orc;
 
+// ---------------------------------------------------------------------------
+// The reference's GPU kernels (cuda/models.cu, cuda/models_device.h,
+// cuda/svi.cu), whose semantics differ from the CPU path's: restated here so
+// that the library's drop-in exports of them can be checked.
+// ---------------------------------------------------------------------------
+// MetzgerKN at one observation, lc_metzger_kn_at_single
+// (cuda/models_device.h:376-456): a 100-point log grid from 0.01 d to
+// max(1.05 phase, 0.02) d, the ODE of metzger_batch, the luminosity
+// interpolated at the phase over the grid's running maximum.
+static double metzger_at_obs(const double* p, double obs_time) {
+    double m_ej = std::pow(10.0, p[0]) * MSUN_CGS;
+    double v_ej = std::pow(10.0, p[1]) * C_CGS;
+    double kappa_r = std::pow(10.0, p[2]);
+    double phase = obs_time - p[3];
+    if (phase <= 0.0) return 0.0;
+    double phase_max = phase * 1.05;
+    if (phase_max < 0.02) phase_max = 0.02;
+    double lmin = std::log(0.01), lmax = std::log(phase_max);
+    const int NG = 100;
+    double ye = 0.1, xn0 = 1.0 - 2.0 * ye, scale = 1e40;
+    double e0 = 0.5 * m_ej * v_ej * v_ej;
+    double e_th = e0 / scale, e_kin = e0 / scale, v = v_ej;
+    double g0 = std::exp(lmin);
+    double r = g0 * SECS_PER_DAY * v;
+    double l_peak = 0.0, l_at = 0.0, prev_t = g0, prev_l = 0.0;
+    for (int i = 0; i < NG; i++) {
+        double t_day = std::exp(lmin + (lmax - lmin) * (double)i / (double)(NG - 1));
+        double t_sec = t_day * SECS_PER_DAY;
+        double eth_factor = 0.34 * std::pow(t_day, 0.74);
+        double eth = 0.36 * (std::exp(-0.56 * t_day) + (eth_factor > 1e-10 ? std::log(1.0 + eth_factor) / eth_factor : 1.0));
+        double xn = xn0 * std::exp(-t_sec / 900.0);
+        double time_term = 0.5 - std::atan((t_sec - 1.3) / 0.11) / PI;
+        if (time_term < 1e-30) time_term = 1e-30;
+        double eps_rp = 2e18 * eth * std::pow(time_term, 1.3);
+        double l_heat = m_ej * (3.2e14 * xn + eps_rp) / scale;
+        double kappa_eff = 0.4 * (xn0 - xn) + kappa_r * (1.0 - xn0);
+        double t_diff = 3.0 * kappa_eff * m_ej / (4.0 * PI * C_CGS * v * t_sec) + r / C_CGS;
+        double l_rad = (e_th > 0.0 && t_diff > 0.0) ? e_th / t_diff : 0.0;
+        if (l_rad > l_peak) l_peak = l_rad;
+        if (i > 0 && phase >= prev_t && phase <= t_day) l_at = prev_l + (phase - prev_t) / (t_day - prev_t) * (l_rad - prev_l);
+        if (i == NG - 1 && phase >= t_day) l_at = l_rad;
+        if (i == 0 && phase <= t_day) l_at = l_rad;
+        prev_t = t_day;
+        prev_l = l_rad;
+        double l_pdv = r > 0.0 ? e_th * v / r : 0.0;
+        if (i < NG - 1) {
+            double t_next = std::exp(lmin + (lmax - lmin) * (double)(i + 1) / (double)(NG - 1));
+            double dt_sec = (t_next - t_day) * SECS_PER_DAY;
+            e_th += (l_heat - l_pdv - l_rad) * dt_sec;
+            if (e_th < 0.0) e_th = 0.0;
+            e_kin += l_pdv * dt_sec;
+            v = std::sqrt(2.0 * e_kin * scale / m_ej);
+            if (v > C_CGS) v = C_CGS;
+            r += v * dt_sec;
+        }
+    }
+    if (l_peak <= 0.0 || !std::isfinite(l_peak)) return 0.0;
+    return l_at / l_peak;
+}
+static double gpu_model_at(int m, const double* p, double t) { return m == METZGER ? metzger_at_obs(p, t) : eval_model(m, p, t); }
+
+// batch_pso_cost (cuda/models.cu:516-584) for one source: per particle, the
+// sum of (pred - y)^2 / v + ln v (detections) and -ln Phi((u - pred)/sqrt v)
+// (upper limits), v = var + sigma_extra^2 with sigma_extra the last
+// parameter, over n; 1e99 for no observations or a non-finite prediction.
+static double gpu_pso_cost(int m, const double* t, const double* f, const double* var, const int* up,
+                           const double* uf, int n, const double* p, int np) {
+    if (n <= 0) return 1e99;
+    double sx = std::exp(p[np - 1]);
+    double se2 = sx * sx, nll = 0.0;
+    for (int i = 0; i < n; i++) {
+        double pred = gpu_model_at(m, p, t[i]);
+        if (!std::isfinite(pred)) return 1e99;
+        double tv = var[i] + se2;
+        if (up[i]) nll -= log_normal_cdf((uf[i] - pred) / std::sqrt(tv));
+        else { double d = pred - f[i]; nll += d * d / tv + std::log(tv); }
+    }
+    return nll / (double)n;
+}
+// batch_pso_cost_multi_bazin (cuda/models.cu:318-362): K components, B at
+// 4K, log sigma_extra at 4K + 1.
+static double gpu_mb_cost(const double* t, const double* f, const double* var, const int* up, const double* uf,
+                          int n, const double* p, int k) {
+    if (n <= 0) return 1e99;
+    double sx = std::exp(p[4 * k + 1]);
+    double se2 = sx * sx, nll = 0.0;
+    for (int i = 0; i < n; i++) {
+        double pred = multi_bazin_eval(p, k, t[i]);
+        if (!std::isfinite(pred)) return 1e99;
+        double tv = var[i] + se2;
+        if (up[i]) nll -= log_normal_cdf((uf[i] - pred) / std::sqrt(tv));
+        else { double d = pred - f[i]; nll += d * d / tv + std::log(tv); }
+    }
+    return nll / (double)n;
+}
+// batch_svi_fit (cuda/svi.cu:48-330) for source index `src` (its seed):
+// xorshift64 seeded 42 + src * 123456789, uniforms (x & (2^53-1)) / (2^53-1),
+// per sample and parameter eps = sqrt(-2 ln max(u1, 1e-10)) cos(2 pi u2);
+// MetzgerKN per observation with forward differences h = max(1e-5,
+// 1e-5 |theta_j|); prior centres / widths given; Adam; log sigma clamped to
+// [-6, 2]; early stop after >= 50 steps on a 20-step EMA stall; no ln 4
+// inflation.  Returns the steps run; elbo -1e99 for no observations.
+static int gpu_svi_fit(int m, const double* t, const double* f, const double* var, const int* up, const double* uf,
+                       int n, const double* init, int np, int se, const double* pcen, const double* pwid,
+                       int n_steps, int n_samples, double lr, int src, double* mu_out, double* ls_out, double* elbo_out) {
+    if (n <= 0) { *elbo_out = -1e99; return 0; }
+    std::vector<double> mu(init, init + np), ls(np, -1.0), pw2(np), am(2 * np, 0.0), av(2 * np, 0.0);
+    for (int j = 0; j < np; j++) pw2[j] = pwid[j] * pwid[j];
+    uint64_t x = 42ULL + (uint64_t)src * 123456789ULL;
+    auto uni = [&]() {
+        x ^= x << 13; x ^= x >> 7; x ^= x << 17;
+        return (double)(x & 0x1FFFFFFFFFFFFFULL) / (double)0x1FFFFFFFFFFFFFULL;
+    };
+    double final_elbo = -1e300, ema = -1e300, best = -1e300;
+    int stall = 0, at = 0, steps = 0;
+    std::vector<double> sg(np), gmu(np), gls(np), th(np), eps(np), g(np), tp(np), dll(np);
+    for (int step = 0; step < n_steps; step++) {
+        steps = step + 1;
+        for (int j = 0; j < np; j++) { sg[j] = std::exp(ls[j]); gmu[j] = gls[j] = 0.0; }
+        double elbo_sum = 0.0;
+        for (int smp = 0; smp < n_samples; smp++) {
+            for (int j = 0; j < np; j++) {
+                double u1 = std::fmax(uni(), 1e-10), u2 = uni();
+                eps[j] = std::sqrt(-2.0 * std::log(u1)) * std::cos(2.0 * PI * u2);
+                th[j] = mu[j] + sg[j] * eps[j];
+            }
+            double sx = std::exp(th[se]), se2 = sx * sx, ll = 0.0;
+            for (int j = 0; j < np; j++) dll[j] = 0.0;
+            for (int i = 0; i < n; i++) {
+                double pred = gpu_model_at(m, th.data(), t[i]);
+                if (!std::isfinite(pred)) continue;
+                if (m != METZGER) {
+                    eval_grad(m, th.data(), t[i], g.data());
+                } else {
+                    tp = th;
+                    for (int j = 0; j < np; j++) {
+                        if (j == se) { g[j] = 0.0; continue; }
+                        double h = std::fmax(1e-5, 1e-5 * std::fabs(th[j]));
+                        tp[j] = th[j] + h;
+                        double pp = metzger_at_obs(tp.data(), t[i]);
+                        tp[j] = th[j];
+                        g[j] = std::isfinite(pp) ? (pp - pred) / h : 0.0;
+                    }
+                    g[se] = 0.0;
+                }
+                double tv = var[i] + se2, st = std::sqrt(tv), it = 1.0 / tv;
+                if (up[i]) {
+                    double z = (uf[i] - pred) / st;
+                    ll += log_normal_cdf(z);
+                    double phi = std::exp(-0.5 * z * z) / std::sqrt(2.0 * PI);
+                    double cdf = std::fmax(0.5 * (1.0 + erf_approx(z * 0.70710678118654752440)), 1e-300);
+                    double dpred = -phi / (cdf * st);
+                    for (int j = 0; j < np; j++) if (j != se && std::isfinite(g[j])) dll[j] += dpred * g[j];
+                    dll[se] += (phi / cdf) * (-(uf[i] - pred) * se2 / (st * tv));
+                } else {
+                    double res = f[i] - pred, r2 = res * res;
+                    ll += -0.5 * (r2 * it + std::log(2.0 * PI * tv));
+                    for (int j = 0; j < np; j++) if (j != se && std::isfinite(g[j])) dll[j] += res * it * g[j];
+                    dll[se] += (r2 * it * it - it) * se2;
+                }
+            }
+            double lp = 0.0;
+            for (int j = 0; j < np; j++) {
+                double d = th[j] - pcen[j];
+                lp += -0.5 * d * d / pw2[j];
+                double df = dll[j] + (-d / pw2[j]);
+                gmu[j] += df;
+                gls[j] += df * sg[j] * eps[j];
+            }
+            elbo_sum += ll + lp;
+        }
+        double ns = (double)n_samples, ent = 0.0;
+        for (int j = 0; j < np; j++) { gmu[j] /= ns; gls[j] /= ns; ent += ls[j]; }
+        ent += 0.5 * (double)np * std::log(2.0 * PI * 2.71828182845904523536);
+        final_elbo = elbo_sum / ns + ent;
+        at++;
+        double bc1 = 1.0 - std::pow(0.9, (double)at), bc2 = 1.0 - std::pow(0.999, (double)at);
+        for (int j = 0; j < np; j++) {
+            double g_mu = -gmu[j];
+            if (std::isfinite(g_mu)) {
+                am[j] = 0.9 * am[j] + 0.1 * g_mu;
+                av[j] = 0.999 * av[j] + 0.001 * g_mu * g_mu;
+                mu[j] -= lr * (am[j] / bc1) / (std::sqrt(av[j] / bc2) + 1e-8);
+            }
+            double g_ls = -(gls[j] + 1.0);
+            if (std::isfinite(g_ls)) {
+                am[np + j] = 0.9 * am[np + j] + 0.1 * g_ls;
+                av[np + j] = 0.999 * av[np + j] + 0.001 * g_ls * g_ls;
+                ls[j] -= lr * (am[np + j] / bc1) / (std::sqrt(av[np + j] / bc2) + 1e-8);
+            }
+        }
+        for (int j = 0; j < np; j++) ls[j] = std::fmax(-6.0, std::fmin(2.0, ls[j]));
+        if (step >= 50) {
+            ema = ema < -1e290 ? final_elbo : 0.1 * final_elbo + 0.9 * ema;
+            if (ema - best > 0.01 * std::fmax(std::fabs(best), 1e-10)) { best = ema; stall = 0; }
+            else if (++stall >= 20) break;
+        }
+    }
+    for (int j = 0; j < np; j++) { mu_out[j] = mu[j]; ls_out[j] = std::fmax(-6.0, std::fmin(2.0, ls[j])); }
+    *elbo_out = final_elbo;
+    return steps;
+}
+
 extern "C" {
 
 void orc_rng_stream(uint64_t seed, int n, uint64_t* out) {
@@ -2272,4 +2475,25 @@ int orc_max_threads(void) {
 #endif
 }
 
+// The reference GPU kernels' semantics (gpu_pso_cost, gpu_mb_cost,
+// gpu_svi_fit, metzger_at_obs above), one source per call.
+double orc_metzger_at_obs(const double* p, double t) { return metzger_at_obs(p, t); }
+int orc_gpu_pso_cost(int m, const double* t, const double* f, const double* var, const int* up, const double* uf,
+                     int n, const double* pos, int n_part, int np, double* costs) {
+    if (m < 0 || m > 7 || np < 1) return -1;
+    for (int k = 0; k < n_part; k++) costs[k] = gpu_pso_cost(m, t, f, var, up, uf, n, pos + (size_t)k * np, np);
+    return 0;
+}
+int orc_gpu_mb_cost(const double* t, const double* f, const double* var, const int* up, const double* uf, int n,
+                    const double* pos, int n_part, int np, int k, double* costs) {
+    if (k < 1 || 4 * k + 2 > np) return -1;
+    for (int q = 0; q < n_part; q++) costs[q] = gpu_mb_cost(t, f, var, up, uf, n, pos + (size_t)q * np, k);
+    return 0;
+}
+int orc_gpu_svi_fit(int m, const double* t, const double* f, const double* var, const int* up, const double* uf,
+                    int n, const double* init, int np, int se, const double* pcen, const double* pwid, int n_steps,
+                    int n_samples, double lr, int src, double* mu, double* ls, double* elbo) {
+    if (m < 0 || m > 7 || np < 1 || np > 7 || se < 0 || se >= np) return -1;
+    return gpu_svi_fit(m, t, f, var, up, uf, n, init, np, se, pcen, pwid, n_steps, n_samples, lr, src, mu, ls, elbo);
+}
 }  // extern "C"

@@ -22,7 +22,6 @@ from lightcurve_fitting_gb300 import abi  # noqa: E402
 
 LIB_PATH = os.path.join(HERE, "_build", "liblcf_oracle.so")
 REF_LIB_PATH = os.path.join(HERE, "_ref", "libref_models.so")
-REF_HEADER = "/root/reference/cuda/models_device.h"
 
 _lib = None
 
@@ -30,9 +29,9 @@ _lib = None
 def build(force: bool = False) -> str:
     """Compile the oracle (and the reference pin harness when the reference
     checkout is present).  Returns the oracle library path."""
-    target = ["all"]
-    if os.path.exists(REF_HEADER):
-        target.append("ref")
+    # the pin harness is built only where the reference checkout exists
+    # (oracle/Makefile knows where; LCF_REFERENCE_DIR overrides)
+    target = ["all", "ref-if-present"]
     if force:
         subprocess.check_call(["make", "-C", HERE, "clean"], stdout=subprocess.DEVNULL)
     subprocess.check_call(["make", "-C", HERE, *target], stdout=subprocess.DEVNULL)
@@ -73,6 +72,11 @@ def lib():
         L.orc_joint_cost.argtypes = [C.POINTER(abi.BandsCSR), i, vp, vp]
         L.orc_pso_stats.argtypes = [vp, i]
         L.orc_max_threads.restype = i
+        L.orc_metzger_at_obs.argtypes = [vp, d]
+        L.orc_metzger_at_obs.restype = d
+        L.orc_gpu_pso_cost.argtypes = [i, vp, vp, vp, vp, vp, i, vp, i, i, vp]
+        L.orc_gpu_mb_cost.argtypes = [vp, vp, vp, vp, vp, i, vp, i, i, i, vp]
+        L.orc_gpu_svi_fit.argtypes = [i, vp, vp, vp, vp, vp, i, vp, i, i, vp, vp, i, i, d, i, vp, vp, vp]
         _lib = L
     return _lib
 
@@ -270,3 +274,50 @@ def pso_stats(reset=True):
 
 def max_threads() -> int:
     return int(lib().orc_max_threads())
+
+
+# --- the reference's GPU kernels (cuda/models.cu, cuda/svi.cu) --------------
+def metzger_at_obs(params, t: float) -> float:
+    """MetzgerKN at one observation as the reference's GPU kernels evaluate it
+    (cuda/models_device.h:376-456)."""
+    p = np.ascontiguousarray(params, np.float64)
+    return float(lib().orc_metzger_at_obs(_p(p), float(t)))
+
+
+def _gpu_band(band: Band):
+    up = np.ascontiguousarray(band.up.astype(np.int32))
+    return up, (_p(band.t), _p(band.f), _p(band.var), _p(up), _p(band.uf), band.n)
+
+
+def gpu_pso_cost(model: int, band: Band, positions) -> np.ndarray:
+    """batch_pso_cost (cuda/models.cu:516-584) of each row of ``positions``."""
+    P = np.ascontiguousarray(np.atleast_2d(positions), np.float64)
+    out = np.zeros(P.shape[0])
+    up, args = _gpu_band(band)
+    assert lib().orc_gpu_pso_cost(int(model), *args, _p(P), P.shape[0], P.shape[1], _p(out)) == 0
+    return out
+
+
+def gpu_mb_cost(band: Band, positions, k: int) -> np.ndarray:
+    """batch_pso_cost_multi_bazin (cuda/models.cu:318-362), K = k, rows padded."""
+    P = np.ascontiguousarray(np.atleast_2d(positions), np.float64)
+    out = np.zeros(P.shape[0])
+    up, args = _gpu_band(band)
+    assert lib().orc_gpu_mb_cost(*args, _p(P), P.shape[0], P.shape[1], int(k), _p(out)) == 0
+    return out
+
+
+def gpu_svi_fit(model: int, band: Band, init, prior_c, prior_w, src: int, n_steps=1000, n_samples=4, lr=0.01):
+    """batch_svi_fit (cuda/svi.cu:48-330) of one source whose index (its
+    noise seed) is ``src``: (mu, log_sigma, elbo, steps)."""
+    npar = abi.N_PARAMS[model]
+    ini = np.ascontiguousarray(init[:npar], np.float64)
+    pc = np.ascontiguousarray(prior_c[:npar], np.float64)
+    pw = np.ascontiguousarray(prior_w[:npar], np.float64)
+    mu, ls, elbo = np.zeros(npar), np.zeros(npar), np.zeros(1)
+    up, args = _gpu_band(band)
+    steps = lib().orc_gpu_svi_fit(int(model), *args, _p(ini), npar, abi.SE_IDX[model], _p(pc), _p(pw), int(n_steps),
+                                  int(n_samples), float(lr), int(src), _p(mu), _p(ls), _p(elbo))
+    assert steps >= 0
+    return mu, ls, float(elbo[0]), steps
+

@@ -12,7 +12,12 @@ script samples it and writes the outputs as golden vectors:
     of src/parametric.rs:1541-1579) at 32 random times, values and analytic
     gradients;
   * log_normal_cdf and erf_approx on a grid (src/parametric.rs:866-901 restate
-    the same formulas as cuda/models_device.h:24-51).
+    the same formulas as cuda/models_device.h:24-51);
+  * MetzgerKN at single observations as the reference's GPU kernels evaluate
+    it (lc_metzger_kn_at_single, cuda/models_device.h:376-456, reached
+    through lc_eval_model_at(7, ...)): 32 parameter vectors in the MetzgerKN
+    PSO box at 24 times each, with their own generator so the sets above are
+    unchanged.
 
 Run from the repository root:  python tests/golden/make_golden.py
 """
@@ -116,6 +121,14 @@ def main():
     xe = np.linspace(-6.0, 6.0, 241)
     out["erf_x"] = xe
     out["erf_y"] = np.array([L.ref_erf_approx(float(v)) for v in xe])
+    # MetzgerKN per observation (bounds src/parametric.rs:1576-1578)
+    rng7 = np.random.default_rng(20261204)
+    lo7, hi7 = np.array([-3.0, -2.0, -1.0, -2.0, -5.0]), np.array([-0.5, -0.5, 2.0, 1.0, 0.0])
+    P7 = rng7.uniform(lo7, hi7, (32, 5))
+    T7 = np.sort(np.concatenate([rng7.uniform(-5.0, 3.0, 8), rng7.uniform(3.0, 60.0, 16)]))
+    out["single_m7_p"] = P7
+    out["single_m7_t"] = T7
+    out["single_m7_f"] = np.stack([ev(7, p, T7) for p in P7])
     path = os.path.join(HERE, "model_kats.npz")
     np.savez_compressed(path, **out)
     print("wrote", path, sum(v.size for v in out.values()), "values")

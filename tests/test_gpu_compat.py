@@ -1,0 +1,173 @@
+"""GPU tests of the reference-FFI exports that an unmodified `GpuContext`
+(src/gpu_cuda.rs:17-164) links against: launch_batch_pso_cost,
+launch_batch_pso_cost_multi_bazin and launch_batch_svi_fit, called through
+the C ABI with device pointers, against the oracle's restatement of the
+reference GPU kernels they replace (cuda/models.cu:295-362, :516-584,
+cuda/svi.cu:48-330).  Their semantics differ from the CPU path's: no prior,
+no Villar constraint, MetzgerKN per observation on its own 100-point grid
+(the oracle's form is pinned to the reference's lc_metzger_kn_at_single by
+the golden vectors), 1e99 for a source without observations, and for SVI
+the xorshift noise, the 50 / 20-step early stop and no ln 4 inflation.
+
+Tolerances: costs are FP64 on both sides, summed in different orders,
+1e-11 relative (MetzgerKN 1e-9: its Euler steps amplify last-bit
+differences of the device and host exp / pow / atan); SVI posterior means
+within 0.1 posterior sigma and the ELBO within 1e-3 for >= 90 % of sources
+(the Adam trajectory amplifies the summation-order differences).
+"""
+import numpy as np
+import pytest
+
+from lightcurve_fitting_gb300 import abi, synth
+
+pytestmark = pytest.mark.gpu
+
+BOUNDS = {
+    0: ([-3.0, -0.3, -100.0, -2.0, -2.0, -5.0], [3.0, 0.3, 100.0, 5.0, 6.0, 0.0]),
+    1: ([-1.5, -0.02, 1.0, -60.0, -1.0, 1.0, -6.0], [1.5, 0.05, 5.0, 40.0, 3.0, 5.5, 0.0]),
+    2: ([-3.0, -1.0, -100.0, -2.0, -1.0, 0.5, -5.0], [3.0, 1.0, 100.0, 5.0, 6.0, 4.0, 0.0]),
+    3: ([-3.0, -100.0, 0.5, -3.0, -5.0], [3.0, 100.0, 4.5, 3.0, 0.0]),
+    4: ([-3.0, -100.0, 0.0, 0.5, -5.0], [3.0, 100.0, 6.0, 4.5, 0.0]),
+    5: ([-3.0, -100.0, 0.1, -1.0, -5.0], [3.0, 100.0, 3.0, 4.0, 0.0]),
+    6: ([-3.0, -100.0, -2.0, -2.0, 0.5, -5.0], [3.0, 100.0, 6.0, 3.0, 5.0, 0.0]),
+    7: ([-3.0, -2.0, -1.0, -2.0, -5.0], [-0.5, -0.5, 2.0, 1.0, 0.0]),
+}
+
+
+@pytest.fixture(scope="module")
+def L():
+    import torch
+    if not torch.cuda.is_available():
+        pytest.skip("no GPU")
+    from lightcurve_fitting_gb300 import build
+    build.build()
+    from lightcurve_fitting_gb300.lib import load
+    return load()
+
+
+def _sources(oracle, n_src, seed, empty=()):
+    """Peak-normalised first bands of an uneven batch as reference GPU
+    sources (one band each); the sources listed in `empty` get no
+    observations."""
+    batch = synth.config_uneven(n_src, seed=seed)
+    bands = []
+    for s in range(batch.n_sources):
+        t, f, e = batch.bands_of(s)[0]
+        if len(t) and np.max(f) > 0:
+            bands.append(oracle.Band(t, f, e))
+    for i in empty:
+        nb = oracle.Band.__new__(oracle.Band)
+        nb.t, nb.f, nb.var, nb.uf = [np.zeros(0) for _ in range(4)]
+        nb.up = np.zeros(0, np.uint8)
+        bands[i] = nb
+    return bands
+
+
+def _csr(bands):
+    import torch
+    cat = lambda name, dt: torch.tensor(np.concatenate([getattr(b, name) for b in bands]).astype(dt), device="cuda")
+    offs = torch.tensor(np.cumsum([0] + [b.n for b in bands]).astype(np.int32), device="cuda")
+    return [cat("t", np.float64), cat("f", np.float64), cat("var", np.float64), cat("up", np.int32),
+            cat("uf", np.float64), offs]
+
+
+@pytest.mark.parametrize("m", range(8))
+def test_batch_pso_cost_matches_the_reference_kernel(L, oracle, m):
+    """launch_batch_pso_cost over 12 sources x 30 particles, one of them empty."""
+    import torch
+    bands = _sources(oracle, 16, seed=40 + m, empty=(3,))[:12]
+    rng = np.random.default_rng(70 + m)
+    lo, hi = [np.array(v) for v in BOUNDS[m]]
+    P = rng.uniform(lo, hi, (len(bands), 30, lo.size))
+    if m != 7:  # half the particles with t0 inside the span
+        P[:, :15, abi.T0_IDX[m]] = rng.uniform(0.0, 200.0, (len(bands), 15))
+    dev = _csr(bands)
+    pos = torch.tensor(P.reshape(-1), device="cuda")
+    out = torch.full((len(bands) * 30,), float("nan"), dtype=torch.float64, device="cuda")
+    L.launch_batch_pso_cost(*[x.data_ptr() for x in dev], pos.data_ptr(), out.data_ptr(), len(bands), 30, lo.size,
+                            m, 1, 256)
+    torch.cuda.synchronize()
+    got = out.cpu().numpy().reshape(len(bands), 30)
+    assert np.all(got[3] == 1e99)  # the empty source
+    rtol = 1e-9 if m == 7 else 1e-11
+    for i, b in enumerate(bands):
+        ref = oracle.gpu_pso_cost(m, b, P[i])
+        assert np.array_equal(got[i] >= 1e98, ref >= 1e98), (m, i)
+        fin = ref < 1e98
+        assert np.allclose(got[i][fin], ref[fin], rtol=rtol, atol=0.0), (m, i)
+
+
+def test_batch_pso_cost_multi_bazin_matches_the_reference_kernel(L, oracle):
+    """K = 1..4 per source in one launch, rows padded to 4 * 4 + 2 = 18."""
+    import torch
+    bands = _sources(oracle, 12, seed=91, empty=(5,))[:8]
+    ks = np.array([1, 2, 3, 4, 2, 1, 4, 3], np.int32)
+    rng = np.random.default_rng(5)
+    comp_lo, comp_hi = np.array([-1.0, 0.0, -1.0, 1.0]), np.array([1.0, 150.0, 3.0, 5.0])
+    P = np.zeros((len(bands), 30, 18))
+    for i, k in enumerate(ks):
+        for c in range(k):
+            P[i, :, 4 * c:4 * c + 4] = rng.uniform(comp_lo, comp_hi, (30, 4))
+        P[i, :, 4 * k] = rng.uniform(-0.3, 0.3, 30)
+        P[i, :, 4 * k + 1] = rng.uniform(-5.0, 0.0, 30)
+    dev = _csr(bands)
+    pos = torch.tensor(P.reshape(-1), device="cuda")
+    dk = torch.tensor(ks, device="cuda")
+    out = torch.full((len(bands) * 30,), float("nan"), dtype=torch.float64, device="cuda")
+    L.launch_batch_pso_cost_multi_bazin(*[x.data_ptr() for x in dev], pos.data_ptr(), out.data_ptr(),
+                                        dk.data_ptr(), len(bands), 30, 18, 1, 256)
+    torch.cuda.synchronize()
+    got = out.cpu().numpy().reshape(len(bands), 30)
+    assert np.all(got[5] == 1e99)
+    for i, b in enumerate(bands):
+        ref = oracle.gpu_mb_cost(b, P[i], int(ks[i]))
+        assert np.array_equal(got[i] >= 1e98, ref >= 1e98)
+        fin = ref < 1e98
+        assert np.allclose(got[i][fin], ref[fin], rtol=1e-11, atol=0.0), (i, int(ks[i]))
+
+
+@pytest.mark.parametrize("models", [(0, 1, 2, 3), (4, 5, 6, 7)])
+def test_batch_svi_fit_matches_the_reference_kernel(L, oracle, models):
+    """launch_batch_svi_fit over 16 sources (four per model), 300 steps x 4
+    samples, one source empty."""
+    import torch
+    n = 16
+    bands = _sources(oracle, 24, seed=11 + models[0], empty=(6,))[:n]
+    rng = np.random.default_rng(3 + models[0])
+    maxp = 7
+    mids = np.array([models[i % 4] for i in range(n)], np.int32)
+    nps = np.array([abi.N_PARAMS[m] for m in mids], np.int32)
+    ses = np.array([abi.SE_IDX[m] for m in mids], np.int32)
+    init = np.zeros((n, maxp))
+    pc = np.zeros((n, maxp))
+    pw = np.ones((n, maxp))
+    for i, m in enumerate(mids):
+        lo, hi = [np.array(v) for v in BOUNDS[m]]
+        x = rng.uniform(lo, hi)
+        if m != 7:
+            x[abi.T0_IDX[m]] = rng.uniform(20.0, 80.0)
+        init[i, :nps[i]] = x
+        pc[i, :nps[i]] = x
+        pw[i, :nps[i]] = rng.uniform(0.5, 2.0, nps[i])
+    dev = _csr(bands)
+    tens = [torch.tensor(a, device="cuda") for a in (init.reshape(-1), mids, nps, ses, pc.reshape(-1),
+                                                      pw.reshape(-1))]
+    mu = torch.full((n * maxp,), float("nan"), dtype=torch.float64, device="cuda")
+    ls = torch.full((n * maxp,), float("nan"), dtype=torch.float64, device="cuda")
+    el = torch.full((n,), float("nan"), dtype=torch.float64, device="cuda")
+    L.launch_batch_svi_fit(*[x.data_ptr() for x in dev], *[x.data_ptr() for x in tens], mu.data_ptr(),
+                           ls.data_ptr(), el.data_ptr(), n, maxp, 300, 4, 0.01, 1, 256)
+    torch.cuda.synchronize()
+    mu, ls, el = mu.cpu().numpy().reshape(n, maxp), ls.cpu().numpy().reshape(n, maxp), el.cpu().numpy()
+    assert el[6] == -1e99 and np.isnan(mu[6]).all()  # empty source: only the ELBO is written
+    ok = []
+    for i in range(n):
+        if i == 6:
+            continue
+        k = int(nps[i])
+        assert np.all(mu[i, k:] == 0.0) and np.all(ls[i, k:] == 0.0)  # padding
+        assert np.all(ls[i, :k] >= -6.0) and np.all(ls[i, :k] <= 2.0)
+        rmu, rls, relbo, _ = oracle.gpu_svi_fit(int(mids[i]), bands[i], init[i], pc[i], pw[i], src=i, n_steps=300)
+        z = np.abs(mu[i, :k] - rmu) / np.exp(rls)
+        ok.append(bool(np.all(z < 0.1) and abs(el[i] - relbo) <= 1e-3 * max(abs(relbo), 1.0)))
+    assert np.mean(ok) >= 0.9, ok

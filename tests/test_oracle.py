@@ -274,3 +274,41 @@ def test_svi_fit_uses_the_step_gradient(oracle):
     expect = 0.01 * g / (np.abs(g) + 1e-8)
     expect[npar:] = np.clip(vp0[npar:] + expect[npar:], -6.0, 2.0) - vp0[npar:]
     np.testing.assert_allclose(moved, expect, rtol=1e-9, atol=1e-12)
+
+
+def test_golden_metzger_at_single_observations(oracle, golden):
+    """The per-observation MetzgerKN of the reference's GPU kernels
+    (lc_metzger_kn_at_single, cuda/models_device.h:376-456), restated in the
+    oracle for the drop-in cost and SVI exports, against the reference's own
+    code sampled into the golden vectors."""
+    P, T, F = golden["single_m7_p"], golden["single_m7_t"], golden["single_m7_f"]
+    got = np.array([[oracle.metzger_at_obs(p, t) for t in T] for p in P])
+    assert np.mean(F != 0.0) > 0.5
+    assert np.allclose(got, F, rtol=1e-12, atol=0.0)
+
+
+def test_gpu_kernel_costs_follow_their_own_rules(oracle):
+    """The reference GPU cost (cuda/models.cu:516-584) has no prior and no 1/2,
+    and 1e99 for an empty source; MultiBazin with K = 1 equals Bazin's cost
+    with the parameters rearranged (cuda/models.cu:295-362)."""
+    from lightcurve_fitting_gb300 import synth
+    batch = synth.config_basic(1, seed=4)
+    t, f, e = batch.bands_of(0)[0]
+    band = oracle.Band(t, f, e)
+    p = np.array([0.2, 0.05, 40.0, 1.0, 3.0, -3.0])
+    c = oracle.gpu_pso_cost(0, band, p)[0]
+    pred = oracle.eval_model(0, p, band.t)
+    tv = band.var + np.exp(p[5]) ** 2
+    det = band.up == 0
+    expect = np.sum((pred[det] - band.f[det]) ** 2 / tv[det] + np.log(tv[det]))
+    from scipy.stats import norm
+    expect -= np.sum(norm.logcdf(((band.uf - pred) / np.sqrt(tv))[~det])) if (~det).any() else 0.0
+    assert abs(c - expect / band.n) <= 1e-3 * abs(expect / band.n)  # A&S erf vs scipy at the limits
+    mb = np.zeros(6)
+    mb[[0, 1, 2, 3, 4, 5]] = [p[0], p[2], p[3], p[4], p[1], p[5]]
+    assert np.isclose(oracle.gpu_mb_cost(band, mb, 1)[0], c, rtol=1e-14)
+    empty = oracle.Band.__new__(oracle.Band)
+    empty.t, empty.f, empty.var, empty.uf = [np.zeros(0) for _ in range(4)]
+    empty.up = np.zeros(0, np.uint8)
+    assert oracle.gpu_pso_cost(0, empty, p)[0] == 1e99
+    assert oracle.gpu_svi_fit(0, empty, p, p, np.ones(6), src=0)[2] == -1e99
