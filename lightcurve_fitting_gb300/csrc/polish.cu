@@ -556,22 +556,23 @@ __device__ __noinline__ double svi_model64(const double* p64, double t, double* 
 }
 
 // x * e^lr in FP64, for |x| in FP32's range and any lr: e^lr is split into
-// 2^k * 2^f (0 <= f < 1), the FP32 mantissa x * 2^f is widened and scaled by
-// 2^k exactly, in two factors 2^k1 * 2^k2 built from their exponent bits.
-// k is clamped to [-2044, 2046] so that both factors are normal doubles
-// (k1, k2 in [-1022, 1023]); beyond that range the product has already
-// underflowed to 0 or overflowed to +-inf, as the reference's FP64 product
-// does.  Relative error ~1e-4 for |lr| ~ 700 (lr is an FP32 value), far
-// inside what the terms it carries need: they reach Adam through their order
-// of magnitude and sign.
+// 2^k * 2^f (0 <= f < 1), the FP32 mantissa x * 2^f is widened and its FP64
+// exponent raised by k with integer arithmetic on the bits (no FP64
+// multiply: a warp FP64 instruction costs 16 SM cycles on this part).  A
+// result below FP64's normal range is 0 and one above it +-inf, as the
+// reference's FP64 product gives (up to its subnormals).  Relative error
+// ~1e-4 for |lr| ~ 700 (lr is an FP32 value), far inside what the terms it
+// carries need: they reach Adam through their order of magnitude and sign.
 __device__ __forceinline__ double scaled_exp(float x, float lr) {
     const float y = fminf(fmaxf(lr * 1.4426950408889634f, -3000.0f), 3000.0f);
     const float kf = floorf(y);
-    const double m = (double)(x * exp2f(y - kf));
-    int k = (int)kf;
-    k = max(-2044, min(2046, k));
-    const int k1 = k / 2, k2 = k - k1;
-    return m * __longlong_as_double((long long)(k1 + 1023) << 52) * __longlong_as_double((long long)(k2 + 1023) << 52);
+    const float m = x * exp2f(y - kf);
+    if (m == 0.0f || !isfinite(m)) return (double)m;
+    const long long bits = __double_as_longlong((double)m);
+    const int e = (int)((bits >> 52) & 0x7ff) + (int)kf;
+    if (e <= 0) return 0.0;
+    if (e >= 2047) return m > 0.0f ? INFINITY : -INFINITY;
+    return __longlong_as_double((bits & ~(0x7ffLL << 52)) | ((long long)e << 52));
 }
 
 struct SviDeferred {
@@ -583,9 +584,9 @@ struct SviDeferred {
 // deferred: those whose quantised CDF 0.5 (1 + erf) holds fewer than 64 units
 // of 2^-53 (src/parametric.rs:2336-2352: dpred = -phi / (cdf sigma) times each
 // model-gradient component, and the sigma_extra term).
-//  * Deep below the floor (the FP32 unit count P * 2^53 < 0.25, so that FP64's
-//    rounds to 0 as well): cdf = 1e-300 and the ratio phi / 1e-300 = e^lr,
-//    lr = 690.78 - ln sqrt(2 pi) - z^2 / 2, spans 0 .. ~1e285.  The terms are
+//  * Below the floor (the unit count k = rint(P * 2^53) is 0): cdf = 1e-300
+//    and the ratio phi / 1e-300 = e^lr, lr = 690.78 - ln sqrt(2 pi) - z^2 / 2,
+//    spans 0 .. ~1e285.  The terms are
 //    carried at full magnitude into FP64 (scaled_exp) and reach the ELBO
 //    gradient and Adam as in the reference, whose second moment overflows and
 //    stops the components they touch.  The FP32 model gradient is exact to
@@ -593,9 +594,12 @@ struct SviDeferred {
 //    is 0 in FP32 while the ratio could lift its FP64 value into range is
 //    taken from the FP64 model gradient instead (analytic models; MetzgerKN
 //    keeps its FP32 sweep's derivatives).
-//  * Near the floor (0.25 <= P * 2^53 < 63.5): everything in FP64 from the
-//    sample's FP64 parameters, as the reference does, so that the unit count
-//    (0, 1, 2, ...) and with it the ratio are the reference's.
+//  * Near the floor (1 <= k < 64): the ratio phi / (k 2^-54) is ~10 and the
+//    terms are formed in FP32 as in the main loop, with k rounded from the
+//    FP32 unit count.  Where that count lies within its own error of a
+//    rounding boundary (k or k + 1?  0, the floor, or 1?) the observation is
+//    evaluated in FP64 from the sample's FP64 parameters, as the reference
+//    does, so that the unit count and with it the ratio are the reference's.
 // Observations: bit r of xm = observation c0 + 32 r + lane, marked by the
 // FP32 loop.  Out of line and called after that loop by the whole warp, so
 // the hot loop holds none of this code's registers.
@@ -614,6 +618,7 @@ __device__ __noinline__ SviDeferred svi_deferred_pass(const float4* obs, const f
         dx[q] = 0.0;
     }
     int floored = 0;
+    const int any = xm != 0;
     while (xm) {
         const int i = c0 + ((__ffsll((long long)xm) - 1) << 5) + lane;
         xm &= xm - 1;
@@ -631,7 +636,19 @@ __device__ __noinline__ SviDeferred svi_deferred_pass(const float4* obs, const f
         const float tv = fabsf(ob.w) + sx2;
         const float stv = sqrtf(tv);
         const float z = (ob.z - pr) / stv;
-        if (upper_units_f32(z) < 0.25f) {
+        // the reference's unit count k: exact from the FP32 estimate unless
+        // that lies within its error (~1e-5 relative) of a rounding boundary
+        const float units = upper_units_f32(z);
+        const float kr = rintf(units);
+        const bool exact_k = fabsf(units - kr) < 0.5f - (1e-4f * units + 1e-4f);
+        if (exact_k && kr >= 1.0f) {
+            // 1 <= k < 64: the ratio phi / (k 2^-54) is ~10, inside FP32
+            const float ratio = 0.39894228040143268f * expf(-0.5f * z * z) / (0.5f * kr * 1.1102230246251565e-16f);
+#pragma unroll
+            for (int q = 0; q < np; q++)
+                if (q != se && isfinite(gb[q])) dx[q] += (double)(-ratio / stv * gb[q]);
+            dx[se] += (double)(ratio * (-(ob.z - pr) * sx2 / (stv * tv)));
+        } else if (exact_k) {
             floored = 1;
             const float lr = fmaf(-0.5f * z, z, ln_ratio0);
             bool rescue = false;
@@ -679,12 +696,22 @@ __device__ __noinline__ SviDeferred svi_deferred_pass(const float4* obs, const f
             dx[se] += (phi / cdf) * (-(uf - pd) * sxx / (sd * tvd));
         }
     }
+    // warp totals: only the lanes that deferred something contribute (few),
+    // so each of those lanes' components is broadcast and lane l keeps
+    // component l & 7
     SviDeferred r;
     r.dlx = 0.0;
+    unsigned act = __ballot_sync(FULL, any);
+    while (act) {
+        const int src = __ffs(act) - 1;
+        act &= act - 1;
+        double mine = 0.0;
 #pragma unroll
-    for (int q = 0; q < np; q++) {
-        const double v = warp_sum_d(dx[q]);
-        if (q == (lane & 7)) r.dlx = v;
+        for (int q = 0; q < np; q++) {
+            const double v = __shfl_sync(FULL, dx[q], src);
+            if (q == (lane & 7)) mine = v;
+        }
+        r.dlx += mine;
     }
     r.floored = warp_or(floored);
     return r;
