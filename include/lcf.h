@@ -164,6 +164,29 @@ int lcf_fit_parametric_batch(lcf_ctx* ctx, const lcf_bands_csr* bands,
                              const lcf_fit_options* opts, lcf_fit_outputs* out);
 
 /*
+ * Asynchronous form of lcf_fit_parametric_batch: the inputs are copied into
+ * the context's pinned staging before the call returns (the caller may reuse
+ * them), the pipeline and the output copies are queued on the context's
+ * stream, and the call returns without waiting.  The outputs are written
+ * into `out`'s arrays, which must stay valid, by lcf_wait().  Until then
+ * every other call that queues work on the context returns LCF_E_INVALID.
+ * The reference's GpuContext calls are synchronous; this is the boundary's
+ * async variant.
+ */
+int lcf_fit_parametric_batch_async(lcf_ctx* ctx, const lcf_bands_csr* bands,
+                                   const lcf_fit_options* opts, lcf_fit_outputs* out);
+
+/*
+ * Waits up to timeout_ms milliseconds (< 0: without limit) for the pending
+ * asynchronous fit.  Returns LCF_OK once it has finished and its outputs and
+ * statistics are written; LCF_E_TIMEOUT while it is still running (it stays
+ * pending: call again); the fit's own error otherwise.  With no fit pending
+ * it returns LCF_OK at once.  lcf_fit_parametric_batch is the asynchronous
+ * call followed by lcf_wait(ctx, -1).
+ */
+int lcf_wait(lcf_ctx* ctx, int timeout_ms);
+
+/*
  * Same pipeline on data that is already resident on the device: the three
  * observation arrays and two offset arrays are device pointers, the outputs
  * stay on the device in the context's buffers.  Used to time the kernels
@@ -238,6 +261,15 @@ void* lcf_ctx_stream(lcf_ctx* ctx);
 /* Replay the stage sequence from a CUDA graph captured per batch layout
  * (default 1), or launch the kernels one by one (0). */
 int lcf_set_graph(lcf_ctx* ctx, int enabled);
+
+/* Bound of the swarm kernel's one device wait (the barrier of the TMA bulk
+ * copy that stages a band in shared memory), in polls; default 2^24, 0 makes
+ * every staged band's wait expire at once.  No counterpart in the reference,
+ * whose swarms run on the host.  On expiry a warp records LCF_E_TIMEOUT, lets
+ * the copy it issued land (a second wait, bounded at 2^24 polls) and takes no
+ * further tasks; the fit returns LCF_E_TIMEOUT and the context stays usable.
+ * For tests of that path; a fit never needs it otherwise. */
+int lcf_set_wait_bound(lcf_ctx* ctx, int polls);
 
 /* Stage concurrency: MultiBazin K = 2..4 (fit_multi_bazin's greedy loop)
  * depends only on the band preparation and its K = 1 swarms, so the fit can

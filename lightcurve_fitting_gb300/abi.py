@@ -13,6 +13,14 @@ MAX_PARAMS = 7
 MB_MAX_K = 4
 MB_MAX_PARAMS = 18
 
+# status codes of include/lcf.h
+LCF_OK = 0
+LCF_E_INVALID = -1
+LCF_E_CUDA = -2
+LCF_E_NOMEM = -3
+LCF_E_TIMEOUT = -4
+LCF_E_UNSUPPORTED = -5
+LCF_E_CAPACITY = -6
 METHOD_SVI = 0
 METHOD_LAPLACE = 1
 

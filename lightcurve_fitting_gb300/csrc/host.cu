@@ -20,7 +20,9 @@
 #include <cstdio>
 #include <cstring>
 #include <new>
+#include <chrono>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "lcf.h"
@@ -180,7 +182,12 @@ struct lcf_ctx {
     int n_joint = 0, joint_max_obs = 0, joint_max_d = 0;
     int64_t task_cap[7] = {0, 0, 0, 0, 0, 0, 0};
     // pinned staging
-    DevArr h_in, h_out, h_sel;
+    DevArr h_in, h_out, h_sel, h_ctr;
+    // lcf_fit_parametric_batch_async: the fit waiting for lcf_wait()
+    bool pending = false;
+    lcf_fit_outputs pending_out{};
+    size_t pending_in_bytes = 0;
+    cudaEvent_t ev_done = nullptr;
     // band-cost scratch
     DevArr bc_obs, bc_params, bc_costs, bc_scratch;
     // ELBO-gradient check buffers
@@ -198,6 +205,7 @@ struct lcf_ctx {
     cudaGraphExec_t graph = nullptr;
     uint64_t graph_key = 0;
     bool use_graph = true;
+    int wait_polls = 1 << 24;  // bound of the staging barrier wait (lcf_set_wait_bound)
     bool capturing = false;   // enqueue_pipeline is recording into a graph
     DeviceBatch db{};
     int n_sources = 0, n_bands = 0;
@@ -281,7 +289,8 @@ extern "C" int lcf_ctx_create(int device, lcf_ctx** out) {
     for (int i = 0; i < N_EVENTS; i++) cudaEventCreate(&ctx->ev[i]);
     if (cudaStreamCreateWithFlags(&ctx->stream_mb, cudaStreamNonBlocking) != cudaSuccess ||
         cudaEventCreateWithFlags(&ctx->ev_fork, cudaEventDisableTiming) != cudaSuccess ||
-        cudaEventCreateWithFlags(&ctx->ev_join, cudaEventDisableTiming) != cudaSuccess) {
+        cudaEventCreateWithFlags(&ctx->ev_join, cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&ctx->ev_done, cudaEventDisableTiming) != cudaSuccess) {
         lcf_ctx_destroy(ctx);
         return LCF_E_CUDA;
     }
@@ -343,6 +352,8 @@ extern "C" void lcf_ctx_destroy(lcf_ctx* ctx) {
     if (ctx->h_in.p) cudaFreeHost(ctx->h_in.p);
     if (ctx->h_out.p) cudaFreeHost(ctx->h_out.p);
     if (ctx->h_sel.p) cudaFreeHost(ctx->h_sel.p);
+    if (ctx->h_ctr.p) cudaFreeHost(ctx->h_ctr.p);
+    if (ctx->ev_done) cudaEventDestroy(ctx->ev_done);
     if (ctx->d_draws) cudaFree(ctx->d_draws);
     if (ctx->d_draws64) cudaFree(ctx->d_draws64);
     if (ctx->d_draws15) cudaFree(ctx->d_draws15);
@@ -699,6 +710,7 @@ static int prepare_layout(lcf_ctx* ctx, int n_sources, int n_bands, int64_t n_ob
     d.t0_slot_base = (int64_t)n_bands * 24;
     d.mb_slot_base = (int64_t)n_bands * 32;
     d.smem_obs = ctx->smem_obs;
+    d.wait_polls = ctx->wait_polls;
     return 0;
 }
 
@@ -867,11 +879,9 @@ static void enqueue_plain(lcf_ctx* ctx) {
     ctx->launches = L;
 }
 
-static int finish_stats(lcf_ctx* ctx) {
-    CK(cudaStreamSynchronize(ctx->stream));
-    CK(cudaGetLastError());
-    Counters c;
-    CK(cudaMemcpy(&c, ctx->ctr.p, sizeof(Counters), cudaMemcpyDeviceToHost));
+// Stage times (from the stage events) and device counters of the fit that
+// just completed; LCF_E_TIMEOUT when a bounded device wait expired in it.
+static int stats_from_counters(lcf_ctx* ctx, const Counters& c) {
     float ms[8] = {0};
     for (int i = 1; i < 8; i++)
         if (cudaEventElapsedTime(&ms[i], ctx->ev[i - 1], ctx->ev[i]) != cudaSuccess) ms[i] = 0.0f;
@@ -911,10 +921,20 @@ static int finish_stats(lcf_ctx* ctx) {
     return 0;
 }
 
+static int finish_stats(lcf_ctx* ctx) {
+    CK(cudaStreamSynchronize(ctx->stream));
+    CK(cudaGetLastError());
+    Counters c;
+    CK(cudaMemcpy(&c, ctx->ctr.p, sizeof(Counters), cudaMemcpyDeviceToHost));
+    return stats_from_counters(ctx, c);
+}
+
 // ---------------------------------------------------------------------------
 // Output unpacking
 // ---------------------------------------------------------------------------
-static int unpack_outputs(lcf_ctx* ctx, lcf_fit_outputs* out) {
+// Queues the copies of the device results into the pinned output buffer
+// (lcf_fit_outputs order is filled from there by fill_outputs).
+static int enqueue_download(lcf_ctx* ctx) {
     int nb = ctx->n_bands;
     size_t bytes = (size_t)nb * (sizeof(BandOut) + sizeof(BandStats) + sizeof(MbState) +
                                  (ctx->opts.fit_all_models ? 8 * sizeof(ModelFit) : 0));
@@ -936,8 +956,19 @@ static int unpack_outputs(lcf_ctx* ctx, lcf_fit_outputs* out) {
         if (ctx->opts.fit_all_models)
             CK(cudaMemcpyAsync(hf, ctx->fits.p, (size_t)nb * 8 * sizeof(ModelFit), cudaMemcpyDeviceToHost,
                                ctx->stream));
-        CK(cudaStreamSynchronize(ctx->stream));
     }
+    return 0;
+}
+
+// The caller's output arrays from the pinned output buffer (after the copies
+// of enqueue_download have completed).
+static void fill_outputs(lcf_ctx* ctx, lcf_fit_outputs* out) {
+    int nb = ctx->n_bands;
+    char* hp = (char*)ctx->h_out.p;
+    BandOut* ho = (BandOut*)hp;
+    BandStats* hs = (BandStats*)(hp + (size_t)nb * sizeof(BandOut));
+    MbState* hm = (MbState*)((char*)hs + (size_t)nb * sizeof(BandStats));
+    ModelFit* hf = (ModelFit*)((char*)hm + (size_t)nb * sizeof(MbState));
     const double nan = std::nan("");
     for (int b = 0; b < nb; b++) {
         const BandStats& st = hs[b];
@@ -983,6 +1014,12 @@ static int unpack_outputs(lcf_ctx* ctx, lcf_fit_outputs* out) {
             }
         }
     }
+}
+
+static int unpack_outputs(lcf_ctx* ctx, lcf_fit_outputs* out) {
+    if (int rc = enqueue_download(ctx)) return rc;
+    if (ctx->n_bands > 0) CK(cudaStreamSynchronize(ctx->stream));
+    fill_outputs(ctx, out);
     return 0;
 }
 
@@ -1028,9 +1065,16 @@ static int stage_host_batch(lcf_ctx* ctx, const lcf_bands_csr* in, const lcf_fit
     return 0;
 }
 
-extern "C" int lcf_fit_parametric_batch(lcf_ctx* ctx, const lcf_bands_csr* in, const lcf_fit_options* o,
-                                        lcf_fit_outputs* out) {
+// Rejects a call that would enqueue work behind an asynchronous fit still
+// waiting for lcf_wait().
+static int busy(lcf_ctx* ctx) {
+    return ctx->pending ? set_err(ctx, LCF_E_INVALID, "an asynchronous fit is pending: call lcf_wait first") : 0;
+}
+
+extern "C" int lcf_fit_parametric_batch_async(lcf_ctx* ctx, const lcf_bands_csr* in, const lcf_fit_options* o,
+                                              lcf_fit_outputs* out) {
     if (!ctx) return LCF_E_INVALID;
+    if (int rc = busy(ctx)) return rc;
     if (!in || !out) return set_err(ctx, LCF_E_INVALID, "null argument");
     if (int rc = check_opts(ctx, o)) return rc;
     CK(cudaSetDevice(ctx->device));
@@ -1039,10 +1083,48 @@ extern "C" int lcf_fit_parametric_batch(lcf_ctx* ctx, const lcf_bands_csr* in, c
     if (in->n_bands == 0) return 0;
     choose_launch(ctx);
     if (int rc = run_pipeline(ctx)) return rc;
-    if (int rc = finish_stats(ctx)) return rc;
+    if (grow_pinned(ctx, ctx->h_ctr, sizeof(Counters))) return LCF_E_NOMEM;
+    CK(cudaMemcpyAsync(ctx->h_ctr.p, ctx->ctr.p, sizeof(Counters), cudaMemcpyDeviceToHost, ctx->stream));
+    if (int rc = enqueue_download(ctx)) return rc;
+    CK(cudaEventRecord(ctx->ev_done, ctx->stream));
+    ctx->pending = true;
+    ctx->pending_out = *out;
+    ctx->pending_in_bytes = in_bytes;
+    return 0;
+}
+
+extern "C" int lcf_wait(lcf_ctx* ctx, int timeout_ms) {
+    if (!ctx) return LCF_E_INVALID;
+    if (!ctx->pending) return 0;
+    CK(cudaSetDevice(ctx->device));
+    const auto t0 = std::chrono::steady_clock::now();
+    while (true) {
+        cudaError_t e = cudaEventQuery(ctx->ev_done);
+        if (e == cudaSuccess) break;
+        if (e != cudaErrorNotReady) {
+            ctx->pending = false;
+            return set_err(ctx, LCF_E_CUDA, std::string("cudaEventQuery: ") + cudaGetErrorString(e));
+        }
+        if (timeout_ms >= 0 &&
+            std::chrono::steady_clock::now() - t0 >= std::chrono::milliseconds(timeout_ms))
+            return set_err(ctx, LCF_E_TIMEOUT, "the asynchronous fit has not finished yet");
+        std::this_thread::sleep_for(std::chrono::microseconds(50));
+    }
+    ctx->pending = false;
+    CK(cudaGetLastError());
+    Counters c;
+    std::memcpy(&c, ctx->h_ctr.p, sizeof(Counters));
+    const int rc = stats_from_counters(ctx, c);
     record_launch(ctx);
-    ctx->stats.h2d_bytes = (double)in_bytes;
-    return unpack_outputs(ctx, out);
+    ctx->stats.h2d_bytes = (double)ctx->pending_in_bytes;
+    fill_outputs(ctx, &ctx->pending_out);
+    return rc;
+}
+
+extern "C" int lcf_fit_parametric_batch(lcf_ctx* ctx, const lcf_bands_csr* in, const lcf_fit_options* o,
+                                        lcf_fit_outputs* out) {
+    if (int rc = lcf_fit_parametric_batch_async(ctx, in, o, out)) return rc;
+    return lcf_wait(ctx, -1);
 }
 
 // ---------------------------------------------------------------------------
@@ -1083,6 +1165,7 @@ static void enqueue_finalize(lcf_ctx* ctx, bool given, size_t sel_bytes) {
 extern "C" int lcf_finalize_batch(lcf_ctx* ctx, const lcf_bands_csr* in, const lcf_pso_selection* sel, int method,
                                   lcf_fit_outputs* out) {
     if (!ctx) return LCF_E_INVALID;
+    if (int rc = busy(ctx)) return rc;
     if (!in || !sel || !out) return set_err(ctx, LCF_E_INVALID, "null argument");
     const bool given = sel->svi_mu != nullptr || sel->svi_log_sigma != nullptr;
     if (given && !(sel->svi_mu && sel->svi_log_sigma))
@@ -1135,6 +1218,7 @@ extern "C" int lcf_finalize_batch(lcf_ctx* ctx, const lcf_bands_csr* in, const l
 
 extern "C" int lcf_fit_parametric_device(lcf_ctx* ctx, const lcf_bands_csr* dev, const lcf_fit_options* o) {
     if (!ctx) return LCF_E_INVALID;
+    if (int rc = busy(ctx)) return rc;
     if (!dev) return set_err(ctx, LCF_E_INVALID, "null argument");
     if (int rc = check_opts(ctx, o)) return rc;
     CK(cudaSetDevice(ctx->device));
@@ -1166,6 +1250,7 @@ extern "C" int lcf_fit_parametric_device(lcf_ctx* ctx, const lcf_bands_csr* dev,
 
 extern "C" int lcf_fit_plain_device(lcf_ctx* ctx, const lcf_bands_csr* dev, const lcf_fit_options* o) {
     if (!ctx) return LCF_E_INVALID;
+    if (int rc = busy(ctx)) return rc;
     if (!dev) return set_err(ctx, LCF_E_INVALID, "null argument");
     if (int rc = check_opts(ctx, o)) return rc;
     if (o->method != LCF_METHOD_SVI) return set_err(ctx, LCF_E_UNSUPPORTED, "the plain form runs SVI only");
@@ -1268,6 +1353,7 @@ extern "C" int lcf_last_launch(const lcf_ctx* ctx, int* out4) {
 
 extern "C" int lcf_download_outputs(lcf_ctx* ctx, lcf_fit_outputs* out) {
     if (!ctx || !out) return LCF_E_INVALID;
+    if (int rc = busy(ctx)) return rc;
     return unpack_outputs(ctx, out);
 }
 
@@ -1305,6 +1391,7 @@ extern "C" int lcf_band_cost(lcf_ctx* ctx, int model, const double* times, const
                              const uint8_t* is_upper, const double* upper_flux, int n_obs, const double* params,
                              int n_eval, int with_prior, double* costs) {
     if (!ctx) return LCF_E_INVALID;
+    if (int rc = busy(ctx)) return rc;
     if (model < 0 || model > 7 || n_obs < 0 || n_eval < 0) return set_err(ctx, LCF_E_INVALID, "bad argument");
     if (n_eval == 0) return 0;
     CK(cudaSetDevice(ctx->device));
@@ -1333,6 +1420,7 @@ extern "C" int lcf_svi_elbo_grad(lcf_ctx* ctx, int model, const double* times, c
                                  const double* prior_init, const double* var_params, int n_points, const double* eps,
                                  int n_samples, double* elbo, double* grad, int* flags) {
     if (!ctx) return LCF_E_INVALID;
+    if (int rc = busy(ctx)) return rc;
     if (model < 0 || model > 7 || n_obs < 1 || n_points < 0 || n_samples < 1)
         return set_err(ctx, LCF_E_INVALID, "bad argument");
     if (!times || !flux || !obs_var || !is_upper || !upper_flux || !prior_init)
@@ -1416,4 +1504,12 @@ extern "C" int lcf_set_graph(lcf_ctx* ctx, int enabled) {
     if (!ctx) return LCF_E_INVALID;
     ctx->use_graph = enabled != 0;
     return 0;
+}
+
+extern "C" int lcf_set_wait_bound(lcf_ctx* ctx, int polls) {
+    if (!ctx || polls < 0) return LCF_E_INVALID;
+    ctx->wait_polls = polls;
+    ctx->db.wait_polls = polls;
+    ctx->graph_key = 0;  // the bound is a kernel argument: capture the graph again
+    return LCF_OK;
 }

@@ -274,6 +274,7 @@ struct DeviceBatch {
     int64_t t0_slot_base;   // first PsoResult slot of the t0 search region
     int64_t mb_slot_base;   // first PsoResult slot of the MultiBazin region
     int smem_obs;           // observations staged per warp in the PSO kernel
+    int wait_polls;         // bound of the staging copy's barrier wait, in polls (lcf_set_wait_bound)
     // joint multi-band fit
     const uint8_t* joint_flag;   // per source: 1 if fitted jointly
     const int32_t* joint_src;    // the jointly fitted sources

@@ -186,10 +186,11 @@ __device__ __forceinline__ void bulk_copy_g2s(void* dst, const void* src, uint32
         "l"(src), "r"(bytes), "r"(smem_u32(bar))
         : "memory");
 }
-// Bounded wait on the barrier phase; returns false if the bound expired.
-__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t phase) {
+// Bounded wait on the barrier phase: at most `polls` polls; returns false if
+// the bound expired (at once for polls = 0).
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t phase, int polls) {
     uint32_t done = 0;
-    for (int it = 0; it < (1 << 24); it++) {
+    for (int it = 0; it < polls; it++) {
         asm volatile(
             "{\n\t.reg .pred p;\n\t"
             "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
@@ -805,15 +806,21 @@ __global__ void __launch_bounds__(256, LCF_PSO_MINB7)
         if (bs.n <= smem_obs && bs.n > 0) {
             __syncwarp();
             if (lane == 0) bulk_copy_g2s(sobs, gobs, (uint32_t)bs.n * 16u, &ws->bar);
-            bool ok = mbar_wait(&ws->bar, phase);
-            __syncwarp();
-            phase ^= 1u;
+            // the lanes agree on the outcome, so the warp stays converged
+            const bool ok = __all_sync(FULL, mbar_wait(&ws->bar, phase, d.wait_polls));
             if (!ok) {
+                // the bound expired: record it, let the copy already issued
+                // into this warp's stage land (a second bounded wait), and
+                // stop taking tasks; the barrier is not re-armed and the
+                // stage is not reused.  The tasks left behind keep their
+                // "not run" results, and the host reports LCF_E_TIMEOUT.
                 if (lane == 0) atomicCAS(&d.ctr->error, 0, LCF_E_TIMEOUT);
-                t.obs = gobs;
-            } else {
-                t.obs = sobs;
+                mbar_wait(&ws->bar, phase, 1 << 24);
+                __syncwarp();
+                break;
             }
+            phase ^= 1u;
+            t.obs = sobs;
         } else {
             t.obs = gobs;
         }

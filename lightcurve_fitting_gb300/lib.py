@@ -40,6 +40,9 @@ def load(path: str = LIB_PATH):
     L.lcf_last_stats.argtypes = [vp, C.POINTER(abi.FitStats)]
     L.lcf_fit_parametric_batch.argtypes = [vp, C.POINTER(abi.BandsCSR), C.POINTER(abi.FitOptions),
                                            C.POINTER(abi.FitOutputs)]
+    L.lcf_fit_parametric_batch_async.argtypes = [vp, C.POINTER(abi.BandsCSR), C.POINTER(abi.FitOptions),
+                                                 C.POINTER(abi.FitOutputs)]
+    L.lcf_wait.argtypes = [vp, i]
     L.lcf_fit_parametric_device.argtypes = [vp, C.POINTER(abi.BandsCSR), C.POINTER(abi.FitOptions)]
     L.lcf_finalize_batch.argtypes = [vp, C.POINTER(abi.BandsCSR), C.POINTER(abi.PsoSelection), i,
                                      C.POINTER(abi.FitOutputs)]
@@ -48,6 +51,7 @@ def load(path: str = LIB_PATH):
     L.lcf_ctx_stream.argtypes = [vp]
     L.lcf_ctx_stream.restype = vp
     L.lcf_set_graph.argtypes = [vp, i]
+    L.lcf_set_wait_bound.argtypes = [vp, i]
     L.lcf_band_cost.argtypes = [vp, i, vp, vp, vp, vp, vp, i, vp, i, i, vp]
     L.lcf_set_autotune.argtypes = [vp, i, i]
     L.lcf_set_multi_bazin_branch.argtypes = [vp, i]
@@ -109,6 +113,11 @@ class Context:
     def stream(self) -> int:
         return int(self.L.lcf_ctx_stream(self.h) or 0)
 
+    def set_wait_bound(self, polls: int):
+        """Bound of the swarm kernel's staging wait, in polls (test hook: 0
+        makes every wait expire; the fit then returns LCF_E_TIMEOUT)."""
+        self._check(self.L.lcf_set_wait_bound(self.h, int(polls)), "lcf_set_wait_bound")
+
     def set_graph(self, enabled: bool):
         self._check(self.L.lcf_set_graph(self.h, int(bool(enabled))), "lcf_set_graph")
 
@@ -123,6 +132,30 @@ class Context:
         self._check(self.L.lcf_fit_parametric_batch(self.h, C.byref(csr), C.byref(opts), C.byref(outs)),
                     "lcf_fit_parametric_batch")
         return res
+
+    def fit_batch_async(self, batch, fit_all_models=True, method=abi.METHOD_SVI, forced_model=-1,
+                        run_multi_bazin=True, joint_multiband=False) -> abi.FitResult:
+        """lcf_fit_parametric_batch_async: queues the fit and returns its
+        (not yet filled) result; wait() fills it."""
+        keep = []
+        csr = abi.csr_struct(batch, keep)
+        opts = abi.options(fit_all_models, method, forced_model, run_multi_bazin, joint_multiband)
+        res = abi.FitResult(batch.n_bands)
+        outs = res.as_struct()
+        self._check(self.L.lcf_fit_parametric_batch_async(self.h, C.byref(csr), C.byref(opts), C.byref(outs)),
+                    "lcf_fit_parametric_batch_async")
+        self._pending = (res, outs)  # the output arrays stay alive until wait()
+        return res
+
+    def wait(self, timeout_ms: int = -1) -> int:
+        """lcf_wait: 0 once the pending fit is written, LCF_E_TIMEOUT (-4)
+        while it runs; raises on the fit's own errors."""
+        rc = self.L.lcf_wait(self.h, int(timeout_ms))
+        if rc == abi.LCF_E_TIMEOUT and "not finished" in self.L.lcf_last_error(self.h).decode(errors="replace"):
+            return rc
+        self._pending = None
+        self._check(rc, "lcf_wait")
+        return rc
 
     def finalize_batch(self, batch, model, pso_params, pso_cost=None, per_model_chi2=None, svi_mu=None,
                        svi_log_sigma=None, svi_elbo=None, method=abi.METHOD_SVI) -> abi.FitResult:

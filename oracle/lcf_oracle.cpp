@@ -502,6 +502,24 @@ static bool prepare_band(const double* times, const double* flux, const double* 
 // ---------------------------------------------------------------------------
 // PsoCost, src/parametric.rs:1285-1446
 // ---------------------------------------------------------------------------
+// Test hook: a deterministic relative perturbation of every swarm / polish
+// cost (PsoCost and the MultiBazin cost), +-rel by a hash of the parameter
+// vector.  With rel ~1e-7 it stands in for FP32 rounding of the costs, so
+// the tests can measure how far the reference's own results move under it.
+// 0 (the default) leaves the arithmetic untouched.
+static double g_cost_rel = 0.0;
+static inline double perturb_cost(double c, const double* p, int np) {
+    if (g_cost_rel == 0.0 || !(std::fabs(c) < 1e11)) return c;
+    uint64_t h = 0x9E3779B97F4A7C15ULL;
+    for (int j = 0; j < np; j++) {
+        uint64_t b;
+        std::memcpy(&b, &p[j], 8);
+        h = (h ^ b) * 0xBF58476D1CE4E5B9ULL;
+        h ^= h >> 31;
+    }
+    return c * ((h >> 63) ? 1.0 + g_cost_rel : 1.0 - g_cost_rel);
+}
+
 struct Cost {
     const Band* b;
     int m;
@@ -558,7 +576,7 @@ struct Cost {
             }
             nll += nlp / nn;
         }
-        return nll / nn;
+        return perturb_cost(nll / nn, p, N_PARAMS[m]);
     }
     // gradient, :1387-1445 (population prior and Villar constraint are not differentiated)
     void gradient(const double* p, double* g) const {
@@ -1573,7 +1591,7 @@ struct MultiBazinCost {
                 nll += d * d / tv + std::log(tv);
             }
         }
-        return nll / nn;
+        return perturb_cost(nll / nn, p, 4 * k + 2);
     }
 };
 static double multi_bazin_eval(const double* p, int k, double t) {
@@ -2496,4 +2514,5 @@ int orc_gpu_svi_fit(int m, const double* t, const double* f, const double* var, 
     if (m < 0 || m > 7 || np < 1 || np > 7 || se < 0 || se >= np) return -1;
     return gpu_svi_fit(m, t, f, var, up, uf, n, init, np, se, pcen, pwid, n_steps, n_samples, lr, src, mu, ls, elbo);
 }
+void orc_set_cost_perturbation(double rel) { g_cost_rel = rel; }
 }  // extern "C"
