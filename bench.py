@@ -12,11 +12,16 @@ One JSON line on rank 0:
   e2e       the same metric through lcf_fit_parametric_batch with host
             buffers (pinned staging, H2D copies, pipeline, D2H of the results
             all inside the timed region);
-  roofline  the model-selection PSO kernel against the measured SFU (MUFU)
-            and FP32 pipe peaks (the kernel is bound by those pipes, not by
-            HBM or the tensor cores);
+  roofline  the dominant kernel, the model-selection swarm (pso_kernel<7>),
+            against the measured SFU (MUFU) and FP32 pipe peaks (the kernel
+            is bound by those pipes, not by HBM or the tensor cores); the
+            L-BFGS polish beside it with its pipe shares from ncu;
   cpu_baseline  the FP64 C++ restatement of the reference's CPU path
-            (oracle/, "port") on a bounded sample, all host threads;
+            (oracle/, "port") on a bounded sample with all host threads, a
+            1-thread sample, and a calibration on the reference's published
+            CPU case (100 sources x 3 bands x 30 points, Laplace);
+  basic, precision  side legs on the basic (100 x 3 x 30, Laplace) and
+            precision (1,000 x 3 x 2,000, Laplace) workloads;
   plain_gpu the plain FP64 GPU form (lcf_fit_plain_device: one thread per
             particle, FP64, global-memory observations, one launch per model
             per stage, no graph) on the same 10,000 sources, and the fused
@@ -26,8 +31,9 @@ One JSON line on rank 0:
             observations) in one call, device-resident, one timed step.
 
 ``--impl reference`` times that CPU path alone (rank 0) on the same workload.
-Under torchrun each rank fits its own 10,000 sources (weak scaling, no
-collective on the data path); value = all ranks' sources / max rank time.
+Under torchrun the ranks partition one workload of N x 10,000 sources by
+estimated work (lightcurve_fitting_gb300.shard, weak scaling, no collective
+on the data path) and value = all sources / the slowest rank's time.
 """
 from __future__ import annotations
 
@@ -62,14 +68,20 @@ MUFU_PER_ODE_STEP = 14
 FP32_PER_EVAL = {0: 24, 1: 34, 2: 30, 3: 30, 4: 26, 5: 30, 6: 32, 7: 16, 8: 24, 9: 34, 10: 44, 11: 54}
 FP32_PER_ODE_STEP = 60
 # DRAM traffic (dram__bytes_read.sum + dram__bytes_write.sum) per unit of
-# work of the two rooflined kernels, from one ncu capture of the 1,000-source
-# uneven workload (profiles/ncu_polish_swarm_1k.md): the polish moved 4.57 GB
-# for 1.507e8 observation-term evaluations, the model-selection swarm 88.6 MB
-# for 6.372e9 particle-observation evaluations.  A launch's traffic is scaled
-# from these by its own units (the traffic is mostly local-memory spill
-# write-back, which grows with the work).
+# work of the two reported kernels, from ncu captures of the 1,000-source
+# uneven workload: the model-selection swarm moved 86.3 MB for 6.372e9
+# particle-observation evaluations, the polish 4.57 GB for 1.507e8
+# observation-term evaluations (its local-memory spill write-back).  A
+# launch's traffic is scaled from these by its own units of work.
+DRAM_BYTES_PER_PSO_OBS_EVAL = 86.32e6 / 6.372e9
 DRAM_BYTES_PER_LB_OBS_EVAL = 4.574e9 / 1.507e8
-DRAM_BYTES_PER_PSO_OBS_EVAL = 88.6e6 / 6.372e9
+# The polish's pipe shares in that capture (% of peak sustained): FMA 9.4,
+# FP64 41.0, issue slots 16.4, instruction-cache hit rate 53.4 %.
+LBFGS_NCU = {"fma_pipe_pct": 9.4, "fp64_pipe_pct": 41.0, "issue_active_pct": 16.4, "icache_hit_pct": 53.4}
+# The reference's published CPU figure for its benchmark case (100 sources x
+# 3 bands x 30 points, fit_parametric(.., false, Laplace), one thread, Skylake
+# Xeon): 113-116 sources/s (benchmarks/parametric_sources.csv:2-8).
+PUBLISHED_CPU_SRC_S = (113.0, 116.0)
 
 
 def parse():
@@ -79,7 +91,11 @@ def parse():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="fused", choices=["fused", "reference"])
     ap.add_argument("--sources", type=int, default=10000)
-    ap.add_argument("--cpu-sample", type=int, default=96, help="sources in the CPU-baseline sample")
+    ap.add_argument("--cpu-sample", type=int, default=512, help="sources in the all-threads CPU-baseline sample")
+    ap.add_argument("--cpu-sample-1t", type=int, default=12, help="sources in the 1-thread CPU-baseline sample")
+    ap.add_argument("--basic-steps", type=int, default=2, help="timed steps of the basic-workload leg (0: skip)")
+    ap.add_argument("--precision-steps", type=int, default=1,
+                    help="timed steps of the precision-workload leg (0: skip)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true", help="skip the host entry-point measurement (profiling runs)")
     ap.add_argument("--plain-steps", type=int, default=1, help="timed steps of the plain FP64 GPU form (0: skip)")
@@ -105,11 +121,15 @@ def dist_setup():
     return ws, rank, local
 
 
-def rank_workload(n_sources: int, rank: int):
-    """This rank's shard: its own n_sources sources of the uneven workload
-    (seed 2 + rank), fitted with no exchange between ranks (weak scaling)."""
-    from lightcurve_fitting_gb300 import synth
-    return synth.config_uneven(n_sources, seed=2 + rank)
+def rank_workload(n_sources: int, rank: int, ws: int = 1):
+    """This rank's shard of one workload of ws x n_sources uneven sources
+    (seed 2): the partition by estimated work of lightcurve_fitting_gb300.
+    shard, fitted with no exchange between ranks (weak scaling)."""
+    from lightcurve_fitting_gb300 import shard, synth
+    full = synth.config_uneven(n_sources * ws, seed=2)
+    if ws == 1:
+        return full
+    return full.subset(shard.partition(full, ws)[rank])
 
 
 def job_value(n_sources_per_rank: int, ws: int, max_ms: float) -> float:
@@ -182,37 +202,90 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
-def cpu_baseline(batch, n_sample: int, threads: int = 0):
-    """The oracle (FP64 port of the reference CPU path) on a bounded sample."""
+def _oracle_rate(batch, threads: int, **kw):
+    """Sources/s of the oracle (FP64 port of the reference CPU path) fitting
+    `batch` on `threads` host threads (0: all), OpenMP over sources with
+    dynamic scheduling."""
     from lightcurve_fitting_gb300 import abi
     from oracle import oracle as O
     O.build()
-    sub = batch.subset(np.arange(min(n_sample, batch.n_sources)))
+    opts = dict(fit_all_models=True, method=abi.METHOD_SVI, run_multi_bazin=True)
+    opts.update(kw)
     t = time.perf_counter()
-    O.fit_batch(sub, fit_all_models=True, method=abi.METHOD_SVI, n_threads=threads)
+    O.fit_batch(batch, n_threads=threads, **opts)
     dt = time.perf_counter() - t
-    cores = threads if threads > 0 else O.max_threads()
-    return sub.n_sources / dt, cores, sub.n_sources, dt
+    return batch.n_sources / dt, dt
+
+
+def cpu_baseline(batch, args):
+    """The reference's CPU path (the oracle port) on this workload: a sample of
+    `cpu_sample` sources on all host threads (the reported value), a sample
+    of `cpu_sample_1t` sources on one thread, and a calibration on the
+    reference's own published CPU case."""
+    from lightcurve_fitting_gb300 import abi, synth
+    from oracle import oracle as O
+    O.build()
+    cores = O.max_threads()
+    n = min(args.cpu_sample, batch.n_sources)
+    v, dt = _oracle_rate(batch.subset(np.arange(n)), 0)
+    n1 = min(args.cpu_sample_1t, batch.n_sources)
+    v1, dt1 = _oracle_rate(batch.subset(np.arange(n1)), 1)
+    # the published case: 100 x 3 x 30, fit_parametric(.., false, Laplace),
+    # one thread.  The current reference routes three bands with
+    # fit_all_models = false to its joint multi-band fit; per-band
+    # fit_parametric_model with the Bazin gate is the published case's
+    # per-band path.  Both are timed (the joint fit on a smaller sample).
+    basic = synth.config_basic(100, seed=1)
+    vg, _ = _oracle_rate(basic, 1, fit_all_models=False, method=abi.METHOD_LAPLACE)
+    vj, _ = _oracle_rate(basic.subset(np.arange(4)), 1, fit_all_models=False, method=abi.METHOD_LAPLACE,
+                         joint_multiband=True)
+    return {
+        "value": v, "unit": "sources/s", "cores": cores, "kind": "port",
+        "sample": f"first {n} sources of the workload, all {cores} host threads, OpenMP over sources "
+                  f"({dt:.1f} s wall); FP64 C++ restatement of the reference CPU path (PSO + SVI, "
+                  f"fit_all_models, MultiBazin)",
+        "single_thread": {"value": v1, "unit": "sources/s", "cores": 1,
+                          "sample": f"first {n1} sources of the workload ({dt1:.1f} s wall)"},
+        "calibration": {
+            "case": "100 sources x 3 bands x 30 points, fit_parametric(.., false, Laplace), one thread",
+            "published_reference_src_s": list(PUBLISHED_CPU_SRC_S),
+            "published_host": "Skylake Xeon, an earlier version of the reference crate",
+            "port_per_band_gated_src_s": vg,
+            "port_joint_multiband_src_s": vj,
+            "note": "the current reference routes this case to its joint multi-band fit (port: "
+                    f"{vj:.2f} src/s), so the published figure predates that routing; the per-band path "
+                    "with 3 restarts and MultiBazin runs at the port figure above",
+        },
+    }
 
 
 def run_reference(args, ws, rank):
+    """The reference's CPU path (the oracle port, all host threads) on the
+    workload: each step fits a bounded sample of its sources (a window that
+    moves by step)."""
     if rank != 0:
         return
     from lightcurve_fitting_gb300 import synth
+    from oracle import oracle as O
+    O.build()
     batch = synth.config_uneven(args.sources, seed=2)
-    vals, cores, n = [], 0, 0
+    n = min(256, batch.n_sources)
+    dts = []
     for i in range(args.warmup + args.steps):
-        v, cores, n, dt = cpu_baseline(batch.subset(np.arange(i * 7 % 100, batch.n_sources)), args.cpu_sample)
+        start = (i * n) % max(batch.n_sources - n, 1)
+        _, dt = _oracle_rate(batch.subset(np.arange(start, start + n)), 0)
         if i >= args.warmup:
-            vals.append(dt)
-    value = args.steps * n / sum(vals)
+            dts.append(dt)
+    value = args.steps * n / sum(dts)
+    cores = O.max_threads()
     line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": "sources/s", "n_gpus": 0,
-        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * sum(vals) / len(vals),
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * sum(dts) / len(dts),
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
         "config": {"workload": WORKLOAD, "sample_sources_per_step": n},
         "cpu_baseline": {"value": value, "unit": "sources/s", "cores": cores, "kind": "port",
-                         "sample": f"{n} sources of the workload per step, OpenMP over sources"},
+                         "sample": f"{n} sources of the workload per step (a window moving by step), all "
+                                   f"{cores} host threads, OpenMP over sources (dynamic)"},
         "e2e": {"value": value, "unit": "sources/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
@@ -225,7 +298,7 @@ def run_fused(args, ws, rank, local):
     from lightcurve_fitting_gb300.lib import Context
     torch.cuda.set_device(local)
     dev = torch.device("cuda", local)
-    batch = rank_workload(args.sources, rank)
+    batch = rank_workload(args.sources, rank, ws)
     ctx = Context(local)
     stream = torch.cuda.ExternalStream(ctx.stream, device=dev)
     peaks = ctx.probe_peaks()
@@ -268,7 +341,7 @@ def run_fused(args, ws, rank, local):
     dist_barrier(ws)
     ms = float(np.mean(times))
     ms_max = dist_max(ms, ws, dev)
-    value = job_value(batch.n_sources, ws, ms_max)
+    value = job_value(args.sources, ws, ms_max)
     # end-to-end through the host entry point
     e2e_t = []
     if not args.no_e2e:
@@ -282,7 +355,7 @@ def run_fused(args, ws, rank, local):
     st_e2e = ctx.stats()
     if e2e_t:
         e2e_s = dist_max(float(np.mean(e2e_t)), ws, dev)
-        e2e = {"value": ws * batch.n_sources / e2e_s, "unit": "sources/s",
+        e2e = {"value": ws * args.sources / e2e_s, "unit": "sources/s",
                "h2d_bytes_per_step": int(st_e2e["h2d_bytes"]), "d2h_bytes_per_step": int(st_e2e["d2h_bytes"])}
     else:
         e2e = None
@@ -296,6 +369,8 @@ def run_fused(args, ws, rank, local):
     joint = run_joint(args, batch, dev, flush, ws, tuned["candidate"]) if args.joint_sources > 0 else None
     scale = run_scale(args, dev, flush, ws, rank, tuned["candidate"]) if args.scale_sources > 0 else None
     final = run_finalize(args, batch, res, flush, dev, ws, rank) if args.finalize_sources > 0 and e2e_t else None
+    basic = run_side(args, "basic", dev, flush, ws, rank) if args.basic_steps > 0 else None
+    precision = run_side(args, "precision", dev, flush, ws, rank) if args.precision_steps > 0 else None
     if rank != 0:
         ctx.close()
         return
@@ -329,54 +404,51 @@ def run_fused(args, ws, rank, local):
         "launch_ms": pso_ms,
         "particle_obs_evals": float(sum(ev)),
     }
-    # roofline of the polish: its observation-term evaluations per second of
-    # the launch, against the rate at which its own observation terms stream at
-    # full occupancy - the double-float term (probe_ff) for the evaluations it
-    # ran, the FP64 term (probe_fp64) for the range fallbacks - for the same
-    # model mix
+    # the L-BFGS polish beside it: its observation-term evaluations per second
+    # of the launch, its pipe shares from ncu (it is bound by instruction fetch
+    # and the FP64 pipe of its line search, not by one arithmetic pipe), and
+    # the rate its own observation terms reach streamed at full occupancy (the
+    # double-float term for the evaluations it ran, the FP64 term for the range
+    # fallbacks, weighted by this launch's per-model evaluations)
     lb_ev = s0["lbfgs_obs_evals_by_model"]
     lb_fb = s0["lbfgs_fp64_obs_evals_by_model"]
     lb_ms = float(np.mean([s["ms_lbfgs"] for s in stage]))
     pk64, pkff = peaks64["obs_evals_per_s"], peaks_ff["obs_evals_per_s"]
     ideal_s = sum((lb_ev[m] - lb_fb[m]) / pkff[m] + lb_fb[m] / pk64[m] for m in range(7) if pk64[m] > 0 and pkff[m] > 0)
     lb_rate = sum(lb_ev[:7]) / (lb_ms * 1e-3)
-    lb_peak = sum(lb_ev[:7]) / ideal_s if ideal_s > 0 else None
-    roofline = {
-        "bound": "fp32 (double-float arithmetic)",
+    lb_term_peak = sum(lb_ev[:7]) / ideal_s if ideal_s > 0 else None
+    polish = {
+        "kernel": "lbfgs_kernel (L-BFGS polish)",
+        "launch_ms": lb_ms,
+        "lbfgs_obs_evals": float(sum(lb_ev[:7])),
         "achieved": lb_rate,
-        "peak": lb_peak,
-        "unit": "observation evaluations/s (value + gradient + cost term, double-float; FP64 where out of range)",
-        "frac": lb_rate / lb_peak if lb_peak else None,
+        "unit": "observation-term evaluations/s (value + gradient + cost, double-float; FP64 where out of range)",
+        "ncu_pipes_pct_of_peak": LBFGS_NCU,
+        "own_term_rate_at_full_occupancy": lb_term_peak,
+        "frac_of_own_term_rate": lb_rate / lb_term_peak if lb_term_peak else None,
         "traffic": float(sum(lb_ev[:7])) * DRAM_BYTES_PER_LB_OBS_EVAL,
         "traffic_source": "ncu DRAM bytes per observation-term evaluation of the 1,000-source launch, scaled by "
-                          "this launch's evaluations (local-memory spill write-back: the resident threads' "
-                          "stacks exceed L2)",
-        "kernel": "lbfgs_kernel (L-BFGS polish, the largest stage)",
-        "peak_source": "measured live: the polish's own observation terms streamed at full occupancy "
-                       "(lcf_probe_ff for the double-float term, lcf_probe_fp64 for the FP64 fallback), "
-                       "weighted by this launch's per-model evaluations",
+                          "this launch's evaluations (local-memory spill write-back)",
         "ff_term_rate_by_model": pkff,
         "fp64_term_rate_by_model": pk64[:7],
         "ff_vs_fp64_worst_rel_by_model": peaks_ff["worst_rel"],
         "fp64_fallback_share": float(sum(lb_fb[:7]) / max(sum(lb_ev[:7]), 1.0)),
         "fp64_dfma_tflops": peaks64["fp64_tflops"],
-        "launch_ms": lb_ms,
-        "lbfgs_obs_evals": float(sum(lb_ev[:7])),
-        "pso_kernel": roofline_pso,
     }
+    roofline = dict(roofline_pso)
+    roofline["lbfgs_kernel"] = polish
     cpu = None
     if not args.no_cpu_baseline:
-        v, cores, n, dt = cpu_baseline(batch, args.cpu_sample)
-        cpu = {"value": v, "unit": "sources/s", "cores": cores, "kind": "port",
-               "sample": f"first {n} sources of the workload, FP64 C++ restatement of the reference CPU path, "
-                         f"OpenMP over sources ({dt:.1f} s wall)"}
+        cpu = cpu_baseline(batch, args)
     line = {
         "metric": METRIC, "value": value, "unit": "sources/s", "n_gpus": ws, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms_max, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-        "config": {"workload": WORKLOAD, "n_sources_per_gpu": batch.n_sources, "n_bands": batch.n_bands,
-                   "n_obs": batch.n_obs, "l2": "flushed between timed steps (256 MB write)",
-                   "parallelism": f"independent shards x{ws}"},
+        "config": {"workload": WORKLOAD, "n_sources_per_gpu": args.sources, "n_sources_rank0": batch.n_sources,
+                   "n_bands_rank0": batch.n_bands, "n_obs_rank0": batch.n_obs,
+                   "l2": "flushed between timed steps (256 MB write)",
+                   "parallelism": f"one workload of {ws} x {args.sources} sources partitioned by estimated work "
+                                  f"over {ws} rank(s)" if ws > 1 else "one GPU"},
         "stage_ms": {k: float(np.mean([s[k] for s in stage])) for k in
                      ["ms_total", "ms_pso", "ms_lbfgs", "ms_t0_search", "ms_uncertainty", "ms_refine",
                       "ms_multi_bazin"]},
@@ -387,6 +459,8 @@ def run_fused(args, ws, rank, local):
         "fit_parametric_multiband": joint,
         "full_scale": scale,
         "finalize_all_models": final,
+        "basic": basic,
+        "precision": precision,
         "autotune": {"candidates_block_staging_blocks_per_sm": ctx.autotune_candidates().tolist(),
                      "chosen": tuned,
                      "table_bucket_best_next_ms": tune_table.tolist(),
@@ -542,6 +616,52 @@ def run_finalize(args, batch, res, flush, dev, ws, rank):
                                "kind": "port", "sample": f"first {k} pairs, oracle restatement of the "
                                                          f"finalisation, OpenMP over pairs ({dc:.1f} s wall)"}
     return out
+
+
+def run_side(args, which, dev, flush, ws, rank):
+    """A side leg on another of the path's workloads, device-resident, one
+    warm-up and `basic_steps` / `precision_steps` timed steps, each rank its
+    own copy (seed + rank):
+      basic      100 sources x 3 bands x 30 points (the reference's CPU
+                 benchmark case), fit_all_models, Laplace, MultiBazin;
+      precision  1,000 sources x 3 bands x 2,000 points, flux range 1e5,
+                 fit_all_models, Laplace, MultiBazin."""
+    import torch
+    from lightcurve_fitting_gb300 import abi, synth
+    from lightcurve_fitting_gb300.lib import Context
+    if which == "basic":
+        batch, steps = synth.config_basic(100, seed=1 + rank), args.basic_steps
+    else:
+        batch, steps = synth.config_precision(1000, seed=4 + rank), args.precision_steps
+    keep = {k: torch.from_numpy(getattr(batch, k)).to(dev) for k in
+            ["times", "flux", "flux_err", "band_obs_offsets", "source_band_offsets"]}
+    ptrs = {k: v.data_ptr() for k, v in keep.items()}
+    sctx = Context(dev.index)
+    sstream = torch.cuda.ExternalStream(sctx.stream, device=dev)
+
+    def fit():
+        sctx.fit_device(ptrs, batch.n_sources, batch.n_bands, fit_all_models=True, method=abi.METHOD_LAPLACE)
+
+    fit()
+    torch.cuda.synchronize()
+    times = []
+    for _ in range(steps):
+        flush.fill_(1.0)
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(sstream)
+        fit()
+        e1.record(sstream)
+        torch.cuda.synchronize()
+        times.append(e0.elapsed_time(e1))
+    st = sctx.stats()
+    sctx.close()
+    ms = dist_max(float(np.mean(times)), ws, dev)
+    return {"value": job_value(batch.n_sources, ws, ms), "unit": "sources/s", "ms_per_step": ms,
+            "sources_per_gpu": batch.n_sources, "n_obs_per_gpu": batch.n_obs, "steps": steps, "warmup": 1,
+            "config": batch.name + ": fit_all_models=true, Laplace, MultiBazin, device-resident",
+            "stage_ms": {k: st[k] for k in ["ms_total", "ms_pso", "ms_lbfgs", "ms_uncertainty", "ms_refine",
+                                            "ms_multi_bazin"]}}
 
 
 def run_scale(args, dev, flush, ws, rank, candidate):

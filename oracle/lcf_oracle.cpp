@@ -124,15 +124,34 @@ static void prior_params(int m, std::vector<double>& c, std::vector<double>& w) 
 // ---------------------------------------------------------------------------
 // Model formulas and analytic gradients, src/parametric.rs:199-538
 // ---------------------------------------------------------------------------
-static inline double bazin(const double* p, double t) {
-    double a = std::exp(p[0]), b = p[1], t0 = p[2], tr = std::exp(p[3]), tf = std::exp(p[4]);
+// exp(p[k]) of a parameter vector, as the model functions below take it:
+// computed at each use (DirectExp), or once per parameter vector for a batch
+// of times (CachedExp) -- the same values, so the same results bit for bit
+// (the reference's batch loops call the per-time functions, whose
+// parameter-only exponentials its compiler may hoist out of the loop).
+struct DirectExp {
+    const double* p;
+    double operator()(int k) const { return std::exp(p[k]); }
+};
+struct CachedExp {
+    double e[LCF_MAX_PARAMS];
+    CachedExp(const double* p, int np) {
+        for (int k = 0; k < np; k++) e[k] = std::exp(p[k]);
+    }
+    double operator()(int k) const { return e[k]; }
+};
+
+template <class X>
+static inline double bazin(const double* p, const X& ex, double t) {
+    double a = ex(0), b = p[1], t0 = p[2], tr = ex(3), tf = ex(4);
     double dt = t - t0;
     double e_fall = std::exp(-dt / tf);
     double sig = 1.0 / (1.0 + std::exp(-dt / tr));
     return a * e_fall * sig + b;
 }
-static inline void bazin_grad(const double* p, double t, double* o) {
-    double a = std::exp(p[0]), t0 = p[2], tr = std::exp(p[3]), tf = std::exp(p[4]);
+template <class X>
+static inline void bazin_grad(const double* p, const X& ex, double t, double* o) {
+    double a = ex(0), t0 = p[2], tr = ex(3), tf = ex(4);
     double dt = t - t0;
     double e_fall = std::exp(-dt / tf);
     double sig = 1.0 / (1.0 + std::exp(-dt / tr));
@@ -144,9 +163,10 @@ static inline void bazin_grad(const double* p, double t, double* o) {
     o[4] = base * dt / tf;
     o[5] = 0.0;
 }
-static inline double villar(const double* p, double t) {
-    double a = std::exp(p[0]), beta = p[1], gamma = std::exp(p[2]), t0 = p[3];
-    double tr = std::exp(p[4]), tf = std::exp(p[5]);
+template <class X>
+static inline double villar(const double* p, const X& ex, double t) {
+    double a = ex(0), beta = p[1], gamma = ex(2), t0 = p[3];
+    double tr = ex(4), tf = ex(5);
     double phase = t - t0;
     double sig_rise = 1.0 / (1.0 + std::exp(-phase / tr));
     double k = 10.0;
@@ -156,9 +176,10 @@ static inline double villar(const double* p, double t) {
     double piece = (1.0 - w) * pl + w * pr;
     return a * sig_rise * piece;
 }
-static inline void villar_grad(const double* p, double t, double* o) {
-    double a = std::exp(p[0]), beta = p[1], gamma = std::exp(p[2]), t0 = p[3];
-    double tr = std::exp(p[4]), tf = std::exp(p[5]);
+template <class X>
+static inline void villar_grad(const double* p, const X& ex, double t, double* o) {
+    double a = ex(0), beta = p[1], gamma = ex(2), t0 = p[3];
+    double tr = ex(4), tf = ex(5);
     double phase = t - t0;
     double k = 10.0;
     double sig_rise = 1.0 / (1.0 + std::exp(-phase / tr));
@@ -191,8 +212,9 @@ static inline void villar_grad(const double* p, double t, double* o) {
     o[5] = a * sig_rise * w * d_pr_dlogtf;
     o[6] = 0.0;
 }
-static inline double tde(const double* p, double t) {
-    double a = std::exp(p[0]), b = p[1], t0 = p[2], tr = std::exp(p[3]), tf = std::exp(p[4]), alpha = p[5];
+template <class X>
+static inline double tde(const double* p, const X& ex, double t) {
+    double a = ex(0), b = p[1], t0 = p[2], tr = ex(3), tf = ex(4), alpha = p[5];
     double phase = t - t0;
     double sig = 1.0 / (1.0 + std::exp(-phase / tr));
     double ps = std::log(1.0 + std::exp(phase)) + 1e-6;
@@ -200,8 +222,9 @@ static inline double tde(const double* p, double t) {
     double decay = std::pow(w, -alpha);
     return a * sig * decay + b;
 }
-static inline void tde_grad(const double* p, double t, double* o) {
-    double a = std::exp(p[0]), t0 = p[2], tr = std::exp(p[3]), tf = std::exp(p[4]), alpha = p[5];
+template <class X>
+static inline void tde_grad(const double* p, const X& ex, double t, double* o) {
+    double a = ex(0), t0 = p[2], tr = ex(3), tf = ex(4), alpha = p[5];
     double phase = t - t0;
     double sig = 1.0 / (1.0 + std::exp(-phase / tr));
     double ps = std::log(1.0 + std::exp(phase)) + 1e-6;
@@ -220,8 +243,9 @@ static inline void tde_grad(const double* p, double t, double* o) {
     o[6] = 0.0;
 }
 static const double TAU_NI = 8.8, TAU_CO = 111.3;
-static inline double arnett(const double* p, double t) {
-    double a = std::exp(p[0]), t0 = p[1], tm = std::exp(p[2]), lf = p[3];
+template <class X>
+static inline double arnett(const double* p, const X& ex, double t) {
+    double a = ex(0), t0 = p[1], tm = ex(2), lf = p[3];
     double phase = t - t0;
     double ps = std::log(1.0 + std::exp(phase)) + 1e-6;
     double f = 1.0 / (1.0 + std::exp(-lf));
@@ -231,8 +255,9 @@ static inline double arnett(const double* p, double t) {
     double trap = 1.0 - std::exp(-x * x);
     return a * heat * trap;
 }
-static inline void arnett_grad(const double* p, double t, double* o) {
-    double a = std::exp(p[0]), t0 = p[1], tm = std::exp(p[2]), lf = p[3];
+template <class X>
+static inline void arnett_grad(const double* p, const X& ex, double t, double* o) {
+    double a = ex(0), t0 = p[1], tm = ex(2), lf = p[3];
     double phase = t - t0;
     double ps = std::log(1.0 + std::exp(phase)) + 1e-6;
     double sig_p = std::exp(phase) / (1.0 + std::exp(phase));
@@ -251,8 +276,9 @@ static inline void arnett_grad(const double* p, double t, double* o) {
     o[3] = a * trap * (e_ni - e_co) * f * (1.0 - f);
     o[4] = 0.0;
 }
-static inline double magnetar(const double* p, double t) {
-    double a = std::exp(p[0]), t0 = p[1], tsd = std::exp(p[2]), tdiff = std::exp(p[3]);
+template <class X>
+static inline double magnetar(const double* p, const X& ex, double t) {
+    double a = ex(0), t0 = p[1], tsd = ex(2), tdiff = ex(3);
     double phase = t - t0;
     double ps = std::log(1.0 + std::exp(phase)) + 1e-6;
     double w = 1.0 + ps / tsd;
@@ -261,8 +287,9 @@ static inline double magnetar(const double* p, double t) {
     double trap = 1.0 - std::exp(-x * x);
     return a * spindown * trap;
 }
-static inline void magnetar_grad(const double* p, double t, double* o) {
-    double a = std::exp(p[0]), t0 = p[1], tsd = std::exp(p[2]), tdiff = std::exp(p[3]);
+template <class X>
+static inline void magnetar_grad(const double* p, const X& ex, double t, double* o) {
+    double a = ex(0), t0 = p[1], tsd = ex(2), tdiff = ex(3);
     double phase = t - t0;
     double ps = std::log(1.0 + std::exp(phase)) + 1e-6;
     double sig_p = std::exp(phase) / (1.0 + std::exp(phase));
@@ -281,8 +308,9 @@ static inline void magnetar_grad(const double* p, double t, double* o) {
     o[3] = -2.0 * a * spindown * exp_x2 * x * x;
     o[4] = 0.0;
 }
-static inline double shock(const double* p, double t) {
-    double a = std::exp(p[0]), t0 = p[1], n = p[2], ttr = std::exp(p[3]);
+template <class X>
+static inline double shock(const double* p, const X& ex, double t) {
+    double a = ex(0), t0 = p[1], n = p[2], ttr = ex(3);
     double phase = t - t0;
     double sig5 = 1.0 / (1.0 + std::exp(-phase * 5.0));
     double ps = std::log(1.0 + std::exp(phase)) + 1e-6;
@@ -291,8 +319,9 @@ static inline double shock(const double* p, double t) {
     double cutoff = std::exp(-ratio * ratio);
     return a * sig5 * cooling * cutoff;
 }
-static inline void shock_grad(const double* p, double t, double* o) {
-    double a = std::exp(p[0]), t0 = p[1], n = p[2], ttr = std::exp(p[3]);
+template <class X>
+static inline void shock_grad(const double* p, const X& ex, double t, double* o) {
+    double a = ex(0), t0 = p[1], n = p[2], ttr = ex(3);
     double phase = t - t0;
     double sig5 = 1.0 / (1.0 + std::exp(-phase * 5.0));
     double ps = std::log(1.0 + std::exp(phase)) + 1e-6;
@@ -308,16 +337,18 @@ static inline void shock_grad(const double* p, double t, double* o) {
     o[3] = flux * 2.0 * ratio * ratio;
     o[4] = 0.0;
 }
-static inline double afterglow(const double* p, double t) {
-    double a = std::exp(p[0]), t0 = p[1], tb = std::exp(p[2]), a1 = p[3], a2 = p[4];
+template <class X>
+static inline double afterglow(const double* p, const X& ex, double t) {
+    double a = ex(0), t0 = p[1], tb = ex(2), a1 = p[3], a2 = p[4];
     double phase = t - t0;
     double ps = std::log(1.0 + std::exp(phase)) + 1e-6;
     double ln_r = std::log(ps / tb);
     double u1 = std::exp(2.0 * a1 * ln_r), u2 = std::exp(2.0 * a2 * ln_r);
     return a * std::pow(u1 + u2, -0.5);
 }
-static inline void afterglow_grad(const double* p, double t, double* o) {
-    double a = std::exp(p[0]), t0 = p[1], tb = std::exp(p[2]), a1 = p[3], a2 = p[4];
+template <class X>
+static inline void afterglow_grad(const double* p, const X& ex, double t, double* o) {
+    double a = ex(0), t0 = p[1], tb = ex(2), a1 = p[3], a2 = p[4];
     double phase = t - t0;
     double ps = std::log(1.0 + std::exp(phase)) + 1e-6;
     double sig_p = std::exp(phase) / (1.0 + std::exp(phase));
@@ -337,28 +368,32 @@ static inline void afterglow_grad(const double* p, double t, double* o) {
     o[5] = 0.0;
 }
 
-static inline double eval_model(int m, const double* p, double t) {
+template <class X>
+static inline double eval_model_x(int m, const double* p, const X& ex, double t) {
     switch (m) {
-        case BAZIN: return bazin(p, t);
-        case VILLAR: return villar(p, t);
-        case TDE: return tde(p, t);
-        case ARNETT: return arnett(p, t);
-        case MAGNETAR: return magnetar(p, t);
-        case SHOCK: return shock(p, t);
-        default: return afterglow(p, t);
+        case BAZIN: return bazin(p, ex, t);
+        case VILLAR: return villar(p, ex, t);
+        case TDE: return tde(p, ex, t);
+        case ARNETT: return arnett(p, ex, t);
+        case MAGNETAR: return magnetar(p, ex, t);
+        case SHOCK: return shock(p, ex, t);
+        default: return afterglow(p, ex, t);
     }
 }
-static inline void eval_grad(int m, const double* p, double t, double* o) {
+template <class X>
+static inline void eval_grad_x(int m, const double* p, const X& ex, double t, double* o) {
     switch (m) {
-        case BAZIN: bazin_grad(p, t, o); break;
-        case VILLAR: villar_grad(p, t, o); break;
-        case TDE: tde_grad(p, t, o); break;
-        case ARNETT: arnett_grad(p, t, o); break;
-        case MAGNETAR: magnetar_grad(p, t, o); break;
-        case SHOCK: shock_grad(p, t, o); break;
-        default: afterglow_grad(p, t, o); break;
+        case BAZIN: bazin_grad(p, ex, t, o); break;
+        case VILLAR: villar_grad(p, ex, t, o); break;
+        case TDE: tde_grad(p, ex, t, o); break;
+        case ARNETT: arnett_grad(p, ex, t, o); break;
+        case MAGNETAR: magnetar_grad(p, ex, t, o); break;
+        case SHOCK: shock_grad(p, ex, t, o); break;
+        default: afterglow_grad(p, ex, t, o); break;
     }
 }
+static inline double eval_model(int m, const double* p, double t) { return eval_model_x(m, p, DirectExp{p}, t); }
+static inline void eval_grad(int m, const double* p, double t, double* o) { eval_grad_x(m, p, DirectExp{p}, t, o); }
 
 // ---------------------------------------------------------------------------
 // MetzgerKN one-zone kilonova, metzger_kn_eval_batch src/parametric.rs:544-648
@@ -445,8 +480,17 @@ static void metzger_grad_batch(const double* p, const double* times, int n, doub
 static void eval_batch(int m, const double* p, const double* times, int n, double* out) {
     if (m == METZGER) {
         metzger_batch(p, times, n, out);
-    } else {
-        for (int i = 0; i < n; i++) out[i] = eval_model(m, p, times[i]);
+        return;
+    }
+    const CachedExp ex(p, N_PARAMS[m]);
+    switch (m) {
+        case BAZIN: for (int i = 0; i < n; i++) out[i] = bazin(p, ex, times[i]); break;
+        case VILLAR: for (int i = 0; i < n; i++) out[i] = villar(p, ex, times[i]); break;
+        case TDE: for (int i = 0; i < n; i++) out[i] = tde(p, ex, times[i]); break;
+        case ARNETT: for (int i = 0; i < n; i++) out[i] = arnett(p, ex, times[i]); break;
+        case MAGNETAR: for (int i = 0; i < n; i++) out[i] = magnetar(p, ex, times[i]); break;
+        case SHOCK: for (int i = 0; i < n; i++) out[i] = shock(p, ex, times[i]); break;
+        default: for (int i = 0; i < n; i++) out[i] = afterglow(p, ex, times[i]); break;
     }
 }
 
@@ -504,13 +548,15 @@ static bool prepare_band(const double* times, const double* flux, const double* 
 // ---------------------------------------------------------------------------
 // Test hook: a deterministic relative perturbation of every swarm / polish
 // cost (PsoCost and the MultiBazin cost), +-rel by a hash of the parameter
-// vector.  With rel ~1e-7 it stands in for FP32 rounding of the costs, so
+// vector (and `salt`, which picks another sign pattern).  With rel ~1e-7 it
+// stands in for FP32 rounding of the costs, so
 // the tests can measure how far the reference's own results move under it.
 // 0 (the default) leaves the arithmetic untouched.
 static double g_cost_rel = 0.0;
+static uint64_t g_cost_salt = 0;
 static inline double perturb_cost(double c, const double* p, int np) {
     if (g_cost_rel == 0.0 || !(std::fabs(c) < 1e11)) return c;
-    uint64_t h = 0x9E3779B97F4A7C15ULL;
+    uint64_t h = 0x9E3779B97F4A7C15ULL ^ (g_cost_salt * 0xD1B54A32D192ED03ULL);
     for (int j = 0; j < np; j++) {
         uint64_t b;
         std::memcpy(&b, &p[j], 8);
@@ -592,6 +638,7 @@ struct Cost {
             kn.resize((size_t)n * 5);
             metzger_grad_batch(p, b->t.data(), n, kn.data());
         }
+        const CachedExp gex(p, N_PARAMS[m]);
         for (int i = 0; i < n; i++) {
             double pr = pred[i];
             if (!std::isfinite(pr)) {
@@ -602,7 +649,7 @@ struct Cost {
             if (m == METZGER) {
                 for (int j = 0; j < np; j++) mg[j] = kn[(size_t)i * 5 + j];
             } else {
-                eval_grad(m, p, b->t[i], mg);
+                eval_grad_x(m, p, gex, b->t[i], mg);
             }
             if (b->up[i]) {
                 double sv = std::sqrt(tv);
@@ -1166,6 +1213,7 @@ static int svi_step_terms(int m, const Band& b, const std::vector<double>& init,
         for (int j = 0; j < np; j++) th[j] = vp[j] + sg[j] * eps[j];
         double sx = std::exp(th[se]);
         double sx2 = sx * sx;
+        const CachedExp tex(th.data(), np);
         if (m == METZGER) {
             metzger_batch(th.data(), b.t.data(), n, preds.data());
             metzger_grad_batch(th.data(), b.t.data(), n, kn.data());
@@ -1179,7 +1227,7 @@ static int svi_step_terms(int m, const Band& b, const std::vector<double>& init,
                 for (auto& g : kn) g *= scl;
             }
         } else {
-            for (int i = 0; i < n; i++) preds[i] = eval_model(m, th.data(), b.t[i]);
+            for (int i = 0; i < n; i++) preds[i] = eval_model_x(m, th.data(), tex, b.t[i]);
         }
         double ll = 0.0;
         for (int j = 0; j < np; j++) dll[j] = 0.0;
@@ -1191,7 +1239,7 @@ static int svi_step_terms(int m, const Band& b, const std::vector<double>& init,
             if (m == METZGER) {
                 for (int j = 0; j < np; j++) gb[j] = kn[(size_t)i * np + j];
             } else {
-                eval_grad(m, th.data(), b.t[i], gb.data());
+                eval_grad_x(m, th.data(), tex, b.t[i], gb.data());
             }
             if (b.up[i]) {
                 double z = (b.uf[i] - pr) / st;
@@ -2180,12 +2228,13 @@ static int gpu_svi_fit(int m, const double* t, const double* f, const double* va
                 th[j] = mu[j] + sg[j] * eps[j];
             }
             double sx = std::exp(th[se]), se2 = sx * sx, ll = 0.0;
+            const CachedExp tex(th.data(), np);
             for (int j = 0; j < np; j++) dll[j] = 0.0;
             for (int i = 0; i < n; i++) {
                 double pred = gpu_model_at(m, th.data(), t[i]);
                 if (!std::isfinite(pred)) continue;
                 if (m != METZGER) {
-                    eval_grad(m, th.data(), t[i], g.data());
+                    eval_grad_x(m, th.data(), tex, t[i], g.data());
                 } else {
                     tp = th;
                     for (int j = 0; j < np; j++) {
@@ -2281,7 +2330,8 @@ int orc_eval_grad(int m, const double* p, const double* times, int n, double* ou
         return 0;
     }
     int np = N_PARAMS[m];
-    for (int i = 0; i < n; i++) eval_grad(m, p, times[i], out + (size_t)i * np);
+    const CachedExp ex(p, np);
+    for (int i = 0; i < n; i++) eval_grad_x(m, p, ex, times[i], out + (size_t)i * np);
     return 0;
 }
 
@@ -2514,5 +2564,5 @@ int orc_gpu_svi_fit(int m, const double* t, const double* f, const double* var, 
     if (m < 0 || m > 7 || np < 1 || np > 7 || se < 0 || se >= np) return -1;
     return gpu_svi_fit(m, t, f, var, up, uf, n, init, np, se, pcen, pwid, n_steps, n_samples, lr, src, mu, ls, elbo);
 }
-void orc_set_cost_perturbation(double rel) { g_cost_rel = rel; }
+void orc_set_cost_perturbation(double rel, uint64_t salt) { g_cost_rel = rel; g_cost_salt = salt; }
 }  // extern "C"

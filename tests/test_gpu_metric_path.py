@@ -16,7 +16,10 @@ oracle itself:
   * >= 99 % of bands select the oracle's model, and every disagreement is a
     near tie (BIC gap below 1e-3 of the best) or a band where the reference
     is unstable: its choice, or its polished cost of one of the two models,
-    moves under the 1e-7 perturbation;
+    moves under one of three perturbations (+-1e-7 with two sign patterns,
+    +-1e-9).  The oracle's own choice can differ between hosts: on this
+    workload it picks Afterglow for one band on x86 and Tde on Arm, whose
+    libm rounds differently;
   * the reported cost of the selected model (the t0 search's on rank-0
     bands): median within 1e-9, and within 1e-6 at least as often as the
     perturbed oracle agrees with itself;
@@ -47,8 +50,11 @@ def ctx():
     c.close()
 
 
-def _perturbed(oracle, batch, rel, **kw):
-    oracle.set_cost_perturbation(rel)
+PERTURBATIONS = [(1e-7, 0), (1e-7, 1), (1e-9, 2)]
+
+
+def _perturbed(oracle, batch, rel, salt=0, **kw):
+    oracle.set_cost_perturbation(rel, salt)
     try:
         return oracle.fit_batch(batch, **kw)
     finally:
@@ -60,9 +66,9 @@ def _bic(r, b, m):
     return 2.0 * r.per_model_chi2[b, m] * n + abi.N_PARAMS[m] * np.log(n)
 
 
-def selection_check(res, ref, pert):
+def selection_check(res, ref, perts):
     """(agreement, bad): bad lists the disagreements that are neither near
-    ties nor at bands where the perturbed oracle moves."""
+    ties nor at bands where one of the perturbed oracles moves."""
     fitted = ref.model >= 0
     assert np.array_equal(res.model >= 0, fitted)
     assert np.array_equal(res.rank, ref.rank)
@@ -72,9 +78,9 @@ def selection_check(res, ref, pert):
         mg, mo = int(res.model[b]), int(ref.model[b])
         gap = abs(_bic(ref, b, mg) - _bic(ref, b, mo))
         tie = gap <= 1e-3 * abs(_bic(ref, b, mo)) + 1e-9
-        moved = lambda m: abs(pert.per_model_chi2[b, m] - ref.per_model_chi2[b, m]) > 1e-4 * max(
+        moved = lambda pr, m: abs(pr.per_model_chi2[b, m] - ref.per_model_chi2[b, m]) > 1e-4 * max(
             abs(ref.per_model_chi2[b, m]), 1e-12)
-        unstable = pert.model[b] != mo or moved(mg) or moved(mo)
+        unstable = any(pr.model[b] != mo or moved(pr, mg) or moved(pr, mo) for pr in perts)
         if not (tie or unstable):
             bad.append((int(b), mo, mg, float(gap)))
     return float(agree.mean()), bad
@@ -91,8 +97,9 @@ def test_metric_path_matches_oracle(ctx, oracle):
     kw = dict(fit_all_models=True, method=abi.METHOD_SVI, run_multi_bazin=True)
     res = ctx.fit_batch(batch, **kw)
     ref = oracle.fit_batch(batch, **kw)
-    pert = _perturbed(oracle, batch, 1e-7, **kw)
-    frac, bad = selection_check(res, ref, pert)
+    perts = [_perturbed(oracle, batch, rel, salt, **kw) for rel, salt in PERTURBATIONS]
+    pert = perts[0]
+    frac, bad = selection_check(res, ref, perts)
     assert frac >= 0.99 and not bad, (frac, bad)
     same = (ref.model >= 0) & (res.model == ref.model)
     same_p = same & (pert.model == ref.model)
@@ -136,8 +143,8 @@ def test_basic_workload_laplace_matches_oracle(ctx, oracle):
     kw = dict(fit_all_models=True, method=abi.METHOD_LAPLACE, run_multi_bazin=True)
     res = ctx.fit_batch(batch, **kw)
     ref = oracle.fit_batch(batch, **kw)
-    pert = _perturbed(oracle, batch, 1e-7, **kw)
-    frac, bad = selection_check(res, ref, pert)
+    perts = [_perturbed(oracle, batch, rel, salt, **kw) for rel, salt in PERTURBATIONS]
+    frac, bad = selection_check(res, ref, perts)
     assert frac >= 0.99 and not bad, (frac, bad)
     fitted = ref.model >= 0
     a, b = res.per_model_chi2[fitted], ref.per_model_chi2[fitted]
