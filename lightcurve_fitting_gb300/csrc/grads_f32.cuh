@@ -227,6 +227,10 @@ __device__ __forceinline__ float upper_ratio_f32(float z, bool& defer) {
         // FP64: 1 - fl(1 - P) = round_half_even(P * 2^53) * 2^-53
         const float kq = P * 9007199254740992.0f;
         if (kq < 63.5f) {
+            // below z = -38.7 the reference's pdf e^(-z^2/2) / sqrt(2 pi) is
+            // exactly 0 in FP64 (past -745.13 in the exponent), so are its
+            // gradient terms for this limit: nothing to defer
+            if (z < -38.7f) return 0.0f;
             defer = true;
             return 0.0f;
         }

@@ -128,11 +128,14 @@ struct DevArr {
 // ---------------------------------------------------------------------------
 struct TuneCand {
     int block, smem_obs;
+    int minb;  // register budget of the model-selection swarm (blocks per SM)
 };
-// (256, 512): 16 warps per SM, bands <= 512 staged (the default);
-// (256, 256): the same occupancy, a shallower stage;
-// (128, 1024): bands <= 1024 staged at 12 warps per SM (long-band batches)
-static const TuneCand TUNE_CAND[] = {{256, 512}, {256, 256}, {128, 1024}};
+// (256, 512, 2): 16 warps per SM, bands <= 512 staged (the default);
+// (256, 256, 3): a shallower stage, and the model-selection swarm at 24 warps
+//   per SM on the three-block register budget (the later swarms, fewer and
+//   longer tasks, keep the two-block build);
+// (128, 1024, 2): bands <= 1024 staged at 12 warps per SM (long-band batches)
+static const TuneCand TUNE_CAND[] = {{256, 512, 2}, {256, 256, 3}, {128, 1024, 2}};
 constexpr int N_TUNE = 3;
 struct TuneEntry {
     uint32_t bucket = 0;
@@ -145,12 +148,15 @@ struct lcf_ctx {
     int device = 0;
     int num_sms = 0;
     int pso_block = 256;
-    int pso_blocks_per_sm = 1;
+    int pso_blocks_per_sm = 1;   // the model-selection swarm's
+    int pso_rest_per_sm = 1;     // the t0-search, gate and MultiBazin swarms'
+    int pso_minb = 2;
     int smem_obs = 512;
     // autotuner state
     int tune_mode = 1;       // 1: online tuning per shape bucket, 0: candidate 0
     int tune_forced = -1;    // >= 0: always this candidate
-    int cand_bps[N_TUNE] = {1, 1, 1};
+    int cand_bps[N_TUNE] = {1, 1, 1};       // blocks per SM, model-selection swarm
+    int cand_bps_rest[N_TUNE] = {1, 1, 1};  // blocks per SM, the other swarms
     int max_pso_warps_per_sm = 1;
     int cfg = 0;             // candidate of the current fit
     bool exploring = false;
@@ -305,14 +311,17 @@ extern "C" int lcf_ctx_create(int device, lcf_ctx** out) {
         lcf_ctx_destroy(ctx);
         return LCF_E_CUDA;
     }
-    // occupancy of the 7-dimension instantiation decides each candidate's
-    // persistent grid
+    // occupancy of the 7-dimension instantiations decides each candidate's
+    // persistent grids
     for (int c = 0; c < N_TUNE; c++) {
-        int bps = pso_blocks_per_sm(TUNE_CAND[c].block, pso_smem_bytes(TUNE_CAND[c].block, TUNE_CAND[c].smem_obs));
-        ctx->cand_bps[c] = std::max(1, bps);
-        ctx->max_pso_warps_per_sm = std::max(ctx->max_pso_warps_per_sm, ctx->cand_bps[c] * TUNE_CAND[c].block / 32);
+        size_t smem = pso_smem_bytes(TUNE_CAND[c].block, TUNE_CAND[c].smem_obs);
+        ctx->cand_bps[c] = std::max(1, pso_blocks_per_sm(TUNE_CAND[c].block, smem, TUNE_CAND[c].minb));
+        ctx->cand_bps_rest[c] = std::max(1, pso_blocks_per_sm(TUNE_CAND[c].block, smem, 2));
+        int bps = std::max(ctx->cand_bps[c], ctx->cand_bps_rest[c]);
+        ctx->max_pso_warps_per_sm = std::max(ctx->max_pso_warps_per_sm, bps * TUNE_CAND[c].block / 32);
     }
     ctx->pso_blocks_per_sm = ctx->cand_bps[0];
+    ctx->pso_rest_per_sm = ctx->cand_bps_rest[0];
     // RNG tables
     std::vector<float> draws((size_t)3 * DRAWS_PER_SEED);
     std::vector<double> eps((size_t)3 * SVI_STEPS * SVI_SAMPLES * 7);
@@ -463,6 +472,8 @@ static void choose_launch(lcf_ctx* ctx) {
     ctx->pso_block = TUNE_CAND[c].block;
     ctx->smem_obs = TUNE_CAND[c].smem_obs;
     ctx->pso_blocks_per_sm = ctx->cand_bps[c];
+    ctx->pso_rest_per_sm = ctx->cand_bps_rest[c];
+    ctx->pso_minb = TUNE_CAND[c].minb;
     ctx->db.smem_obs = ctx->smem_obs;
 }
 
@@ -730,7 +741,8 @@ static void enqueue_pipeline(lcf_ctx* ctx) {
     const DeviceBatch& d = ctx->db;
     const lcf_fit_options& o = ctx->opts;
     cudaStream_t s = ctx->stream;
-    int grid = ctx->num_sms * ctx->pso_blocks_per_sm;
+    int grid0 = ctx->num_sms * ctx->pso_blocks_per_sm;
+    int grid = ctx->num_sms * ctx->pso_rest_per_sm;
     int block = ctx->pso_block;
     int64_t L = 0;
     stage_event(ctx, ctx->ev[0], s);
@@ -739,7 +751,7 @@ static void enqueue_pipeline(lcf_ctx* ctx) {
     cudaMemsetAsync(ctx->fits.p, 0xff, (size_t)std::max(ctx->n_bands, 1) * 8 * sizeof(ModelFit), s);
     launch_prep(d, s); L++;
     stage_event(ctx, ctx->ev[1], s);
-    launch_pso(d, 0, d.tasks[0], ctx->n_tasks0, 7, grid, block, s); L++;
+    launch_pso(d, 0, d.tasks[0], ctx->n_tasks0, 7, grid0, block, s, ctx->pso_minb); L++;
     stage_event(ctx, ctx->ev[2], s);
     // MultiBazin K = 2..4 (fit_multi_bazin's greedy loop) needs only the band
     // preparation and its K = 1 swarms of the launch above, so it can run on

@@ -293,14 +293,16 @@ struct DeviceBatch {
 void launch_prep(const DeviceBatch& d, cudaStream_t s);
 // Run the PSO tasks of `slot` (count = n_host if >= 0, else the device
 // counter of the slot).  `max_dim` selects the kernel instantiation.
+// `minb`: the register budget of the 7-dimension swarm (resident 256-thread
+// blocks per SM it is built for: 2 or 3); the other swarms are built for 2.
 void launch_pso(const DeviceBatch& d, int slot, const PsoTask* tasks, int n_host, int max_dim, int grid, int block,
-                cudaStream_t s);
+                cudaStream_t s, int minb = 2);
 // Sort the device-built task list of `slot` into `out` (d.task_sorted, or
 // d.task_sorted_mb for the MultiBazin branch): MetzgerKN first, then by
 // kind, longest bands first within a kind.
 void launch_task_sort(const DeviceBatch& d, int slot, PsoTask* out, cudaStream_t s);
 size_t pso_smem_bytes(int block, int smem_obs);
-int pso_blocks_per_sm(int block, size_t smem);
+int pso_blocks_per_sm(int block, size_t smem, int minb);
 int pso_init_attributes(int block, int smem_obs);
 void launch_t0_build(const DeviceBatch& d, int slot, int fine, cudaStream_t s);
 void launch_t0_pick(const DeviceBatch& d, int slot, int fine, cudaStream_t s);

@@ -763,14 +763,15 @@ __device__ __forceinline__ void run_swarm_exact(const DeviceBatch& d, const PsoT
     __syncwarp();
 }
 
-// Blocks of 256 threads per SM the register budget is sized for (128
-// registers a thread): measured on GB300, two resident blocks (16 warps) with
-// a few spills run the swarms ~1.7x faster than one block without spills.
-#ifndef LCF_PSO_MINB7
-#define LCF_PSO_MINB7 2
-#endif
-template <int MAXD>
-__global__ void __launch_bounds__(256, LCF_PSO_MINB7)
+// MINB: blocks of 256 threads per SM the register budget is sized for.  Two
+// (128 registers a thread, 16 warps) is the default: measured on GB300 it runs
+// the swarms ~1.7x faster than one block without spills.  The 7-dimension
+// swarm also has a three-block build (80 registers, 24 warps, more spills):
+// on the 10k uneven workload it runs the model-selection launch 14 % faster
+// (495 -> 426 ms) but the t0-search launches, fewer and longer tasks, 30 %
+// slower, so the launch autotuner offers it for model selection only.
+template <int MAXD, int MINB>
+__global__ void __launch_bounds__(256, MINB)
     pso_kernel(DeviceBatch d, int slot, const PsoTask* tasks, int n_host, int smem_obs) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const int lane = threadIdx.x & 31;
@@ -904,29 +905,32 @@ size_t pso_smem_bytes(int block, int smem_obs) {
 
 int pso_init_attributes(int block, int smem_obs) {
     int smem = (int)pso_smem_bytes(block, smem_obs);
-    cudaError_t e = cudaSuccess;
-    e = cudaFuncSetAttribute(pso_kernel<7>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
-    if (e == cudaSuccess) e = cudaFuncSetAttribute(pso_kernel<10>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
-    if (e == cudaSuccess) e = cudaFuncSetAttribute(pso_kernel<14>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
-    if (e == cudaSuccess) e = cudaFuncSetAttribute(pso_kernel<18>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    const cudaFuncAttribute a = cudaFuncAttributeMaxDynamicSharedMemorySize;
+    cudaError_t e = cudaFuncSetAttribute(pso_kernel<7, 2>, a, smem);
+    if (e == cudaSuccess) e = cudaFuncSetAttribute(pso_kernel<7, 3>, a, smem);
+    if (e == cudaSuccess) e = cudaFuncSetAttribute(pso_kernel<10, 2>, a, smem);
+    if (e == cudaSuccess) e = cudaFuncSetAttribute(pso_kernel<14, 2>, a, smem);
+    if (e == cudaSuccess) e = cudaFuncSetAttribute(pso_kernel<18, 2>, a, smem);
     return (int)e;
 }
 
-int pso_blocks_per_sm(int block, size_t smem) {
+int pso_blocks_per_sm(int block, size_t smem, int minb) {
     int n = 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, pso_kernel<7>, block, smem) != cudaSuccess) return 1;
-    return n;
+    cudaError_t e = minb == 3 ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, pso_kernel<7, 3>, block, smem)
+                              : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, pso_kernel<7, 2>, block, smem);
+    return e == cudaSuccess ? n : 1;
 }
 
 void launch_pso(const DeviceBatch& d, int slot, const PsoTask* tasks, int n_host, int max_dim, int grid, int block,
-                cudaStream_t s) {
+                cudaStream_t s, int minb) {
     if (n_host == 0) return;
     int smem_obs = d.smem_obs;
     size_t smem = pso_smem_bytes(block, smem_obs);
-    if (max_dim <= 7) pso_kernel<7><<<grid, block, smem, s>>>(d, slot, tasks, n_host, smem_obs);
-    else if (max_dim <= 10) pso_kernel<10><<<grid, block, smem, s>>>(d, slot, tasks, n_host, smem_obs);
-    else if (max_dim <= 14) pso_kernel<14><<<grid, block, smem, s>>>(d, slot, tasks, n_host, smem_obs);
-    else pso_kernel<18><<<grid, block, smem, s>>>(d, slot, tasks, n_host, smem_obs);
+    if (max_dim <= 7 && minb == 3) pso_kernel<7, 3><<<grid, block, smem, s>>>(d, slot, tasks, n_host, smem_obs);
+    else if (max_dim <= 7) pso_kernel<7, 2><<<grid, block, smem, s>>>(d, slot, tasks, n_host, smem_obs);
+    else if (max_dim <= 10) pso_kernel<10, 2><<<grid, block, smem, s>>>(d, slot, tasks, n_host, smem_obs);
+    else if (max_dim <= 14) pso_kernel<14, 2><<<grid, block, smem, s>>>(d, slot, tasks, n_host, smem_obs);
+    else pso_kernel<18, 2><<<grid, block, smem, s>>>(d, slot, tasks, n_host, smem_obs);
 }
 
 // ---------------------------------------------------------------------------
