@@ -158,6 +158,7 @@ struct lcf_ctx {
     int cand_bps[N_TUNE] = {1, 1, 1};       // blocks per SM, model-selection swarm
     int cand_bps_rest[N_TUNE] = {1, 1, 1};  // blocks per SM, the other swarms
     int max_pso_warps_per_sm = 1;
+    int lb_grid = 1;          // blocks of the persistent polish grid
     int cfg = 0;             // candidate of the current fit
     bool exploring = false;
     uint32_t bucket = 0;
@@ -182,8 +183,8 @@ struct lcf_ctx {
     double* d_eps = nullptr;
     // device buffers (capacity-sized)
     DevArr times, flux, ferr, boff, soff, stats_b, obs, t64, f64, fe64, var64, uf64, mag64, up, ffa, ffb, res, fits, out, mb,
-        ctr, scratch, scratch64, scratch_svi, t0state, tasks[7], task_sorted, task_sorted_mb, band_order, joint_flag, joint_src, joint_res,
-        joint_draws;
+        ctr, scratch, scratch64, scratch_svi, t0state, tasks[7], task_sorted, task_sorted_mb, band_order, polish_order, joint_flag, joint_src,
+        joint_res, joint_draws;
     int64_t joint_per_seed = 0;   // uniforms per seed held in joint_draws
     int n_joint = 0, joint_max_obs = 0, joint_max_d = 0;
     int64_t task_cap[7] = {0, 0, 0, 0, 0, 0, 0};
@@ -322,6 +323,7 @@ extern "C" int lcf_ctx_create(int device, lcf_ctx** out) {
     }
     ctx->pso_blocks_per_sm = ctx->cand_bps[0];
     ctx->pso_rest_per_sm = ctx->cand_bps_rest[0];
+    ctx->lb_grid = lbfgs_grid(ctx->num_sms);
     // RNG tables
     std::vector<float> draws((size_t)3 * DRAWS_PER_SEED);
     std::vector<double> eps((size_t)3 * SVI_STEPS * SVI_SAMPLES * 7);
@@ -351,8 +353,8 @@ extern "C" void lcf_ctx_destroy(lcf_ctx* ctx) {
     DevArr* all[] = {&ctx->times, &ctx->flux, &ctx->ferr, &ctx->boff, &ctx->soff, &ctx->stats_b, &ctx->obs,
                      &ctx->t64, &ctx->f64, &ctx->fe64, &ctx->var64, &ctx->uf64, &ctx->mag64, &ctx->up, &ctx->ffa, &ctx->ffb, &ctx->res,
                      &ctx->fits, &ctx->out, &ctx->mb, &ctx->ctr, &ctx->scratch, &ctx->scratch64, &ctx->scratch_svi,
-                     &ctx->t0state, &ctx->task_sorted, &ctx->task_sorted_mb, &ctx->band_order, &ctx->joint_flag, &ctx->joint_src,
-                     &ctx->joint_res,
+                     &ctx->t0state, &ctx->task_sorted, &ctx->task_sorted_mb, &ctx->band_order, &ctx->polish_order, &ctx->joint_flag,
+                     &ctx->joint_src, &ctx->joint_res,
                      &ctx->joint_draws,
                      &ctx->bc_obs, &ctx->bc_params, &ctx->bc_costs, &ctx->bc_scratch, &ctx->plain_scr,
                      &ctx->sg_in, &ctx->sg_out, &ctx->sg_scratch};
@@ -545,6 +547,7 @@ static int prepare_layout(lcf_ctx* ctx, int n_sources, int n_bands, int64_t n_ob
     rc |= grow(ctx, ctx->task_sorted, (size_t)nb * 21 * sizeof(PsoTask));     // slots 1..3
     rc |= grow(ctx, ctx->task_sorted_mb, (size_t)nb * 3 * sizeof(PsoTask));   // slots 4..6 (MultiBazin branch)
     rc |= grow(ctx, ctx->band_order, nb * sizeof(int32_t));
+    rc |= grow(ctx, ctx->polish_order, nb * sizeof(int32_t));
     if (rc) return rc;
     // stage-1 task list (bands, models, restarts; MultiBazin K = 1), longest first
     if (!same) {
@@ -704,6 +707,8 @@ static int prepare_layout(lcf_ctx* ctx, int n_sources, int n_bands, int64_t n_ob
     d.task_sorted = (PsoTask*)ctx->task_sorted.p;
     d.task_sorted_mb = (PsoTask*)ctx->task_sorted_mb.p;
     d.band_order = (int32_t*)ctx->band_order.p;
+    d.polish_order = (int32_t*)ctx->polish_order.p;
+    d.lb_grid = ctx->lb_grid;
     d.n_joint = ctx->n_joint;
     d.joint_flag = ctx->n_joint > 0 ? (const uint8_t*)ctx->joint_flag.p : nullptr;
     d.joint_src = (const int32_t*)ctx->joint_src.p;
@@ -778,6 +783,7 @@ static void enqueue_pipeline(lcf_ctx* ctx) {
     };
     if (branch == 1) fork_mb();
     int gated = (o.forced_model < 0 && !o.fit_all_models);
+    launch_polish_order(d, s); L += 3;
     launch_lbfgs(d, gated ? 1 : 0xff, s); L++;
     if (gated) {
         launch_gate_build(d, 1, s); L++;

@@ -3,13 +3,13 @@
 // out across the lanes of a warp: component j of the vector in lane j, the
 // observations split over the lanes, double-float observation terms with the
 // FP64 term wherever an exponent or the prediction could leave FP32's range.
-// Used by the L-BFGS polish (polish.cu) and by the swarms' accurate re-check
-// of near-tied comparisons (pso.cu).
+// Used by the swarms' accurate re-check of near-tied comparisons (pso.cu);
+// the L-BFGS polish evaluates per group of eight lanes (lbfgs_group.cuh)
+// with the same observation terms.
 #pragma once
 
 #include <cuda_runtime.h>
 
-#include "lbfgs_lane.cuh"
 #include "lcf_internal.cuh"
 #include "models_f32.cuh"
 #include "models_f64.cuh"
@@ -20,6 +20,16 @@
 #endif
 
 namespace lcf {
+
+// a.b over lanes j = lane & 7 (xor 4, 2, 1 sums; the four groups of eight
+// lanes hold identical copies in the warp-wide uses)
+__device__ __forceinline__ double dot8(double a, double b) {
+    double v = a * b;
+    v += __shfl_xor_sync(0xffffffffu, v, 4);
+    v += __shfl_xor_sync(0xffffffffu, v, 2);
+    v += __shfl_xor_sync(0xffffffffu, v, 1);
+    return v;
+}
 
 __device__ __forceinline__ double warp_sum_d(double v) {
     for (int k = 16; k; k >>= 1) v += __shfl_xor_sync(FULL, v, k);

@@ -221,6 +221,8 @@ struct Counters {
     unsigned long long lb_fp64_obs_evals_by_model[8];  // of which in FP64 (ff range fallback)
     int32_t sort_hist[8][256];  // per slot: key histogram, then offsets, of the device task sort
     int32_t band_hist[16];      // bands by selected model: histogram, then offsets (band_order)
+    int32_t polish_hist[256];   // bands by length: histogram, then offsets (polish_order)
+    int32_t lb_next[8];         // per model: next index of the polish queue
     int32_t error;              // first error code raised on the device
     int32_t pad;
 };
@@ -244,9 +246,10 @@ struct DeviceBatch {
     double* uf64;           // upper flux
     double* mag64;          // observed magnitude
     uint8_t* up;            // is_upper
-    // the same observations as double-float pairs for the polish (ff.cuh):
-    // ffa = (t hi, t lo, y hi, y lo), y = flux / peak, or the upper flux for
-    // an upper limit; ffb = obs_var (hi, lo), negated for upper limits
+    // the same observations as double-float pairs for the polish (ff.cuh),
+    // each band's detections first, then its upper limits (each in time
+    // order): ffa = (t hi, t lo, y hi, y lo), y = flux / peak, or the upper
+    // flux for an upper limit; ffb = obs_var (hi, lo), negated for upper limits
     float4* ffa;
     float2* ffb;
     // tables
@@ -265,6 +268,8 @@ struct DeviceBatch {
     PsoTask* task_sorted_mb;  // the same for slots 4..6 (the MultiBazin branch, which may run concurrently)
     int32_t* band_order;    // [n_bands] bands grouped by selected model (MetzgerKN first), for the
                             // per-band uncertainty and refinement kernels
+    int32_t* polish_order;  // [n_bands] bands longest first: the polish's queue order
+    int lb_grid;            // blocks of the persistent polish grid
     Counters* ctr;
     float* scratch;         // MetzgerKN per-warp scratch: [warps][n_max][32]
     int64_t scratch_per_warp;
@@ -311,6 +316,10 @@ void launch_mb_pick(const DeviceBatch& d, int k, cudaStream_t s);
 void launch_mb_build(const DeviceBatch& d, int slot, int k, cudaStream_t s);
 // polish.cu
 void launch_lbfgs(const DeviceBatch& d, int model_mask, cudaStream_t s);
+// the polish queue's band order (three launches); before the first launch_lbfgs
+void launch_polish_order(const DeviceBatch& d, cudaStream_t s);
+// blocks of the persistent polish grid on `num_sms` SMs
+int lbfgs_grid(int num_sms);
 void launch_select(const DeviceBatch& d, int fit_all, int forced, cudaStream_t s);
 void launch_svi(const DeviceBatch& d, cudaStream_t s);
 // one SVI step's ELBO estimate and gradient at given variational parameters

@@ -2,12 +2,12 @@
 // selection (pso_fit_single_model / pso_model_select, src/parametric.rs:
 // 1864-2066), and the SVI uncertainty kernel (svi_fit, :2215-2454).
 //
-// L-BFGS: one warp per (band, model).  Cost and gradient are accumulated by
-// the lanes over the band's observations in FP32 (Kahan for the cost) and
-// reduced across the warp; the quasi-Newton algebra (two-loop recursion,
-// memory 7) and the Moré–Thuente line search run in FP64, identically in
-// every lane, following the argmin 0.11 algorithm the reference calls
-// (restated from the published method, as in the test oracle).
+// L-BFGS: four polishes per warp, eight lanes each (lbfgs_group.cuh): the
+// lanes of a group split its band's observations (double-float terms, FP64
+// where FP32's range would not hold them); the quasi-Newton algebra (two-loop
+// recursion, memory 7) and the Moré–Thuente line search run in FP64,
+// following the argmin 0.11 algorithm the reference calls (restated from the
+// published method, as in the test oracle).
 //
 // SVI: one warp per band.  Per step the four reparameterised samples
 // theta = mu + sigma * eps are evaluated with the lanes over observations;
@@ -20,7 +20,7 @@
 
 #include "grads_f32.cuh"
 #include "lane_cost.cuh"
-#include "lbfgs_lane.cuh"
+#include "lbfgs_group.cuh"
 #include "lcf_internal.cuh"
 #include "models_f32.cuh"
 #include "metzger_dual.cuh"
@@ -31,136 +31,73 @@ namespace lcf {
 
 #define FULL 0xffffffffu
 
-// Best of the three restarts of (band, MODEL), then the polish.
-// Two swarm result costs closer than the FP32 estimate's error (3e-5 of the
-// reference value; the special values 1e99, +inf and the Villar constraint's
-// 1e12 + 1e4 c compare as they are).
-__device__ __forceinline__ bool swarm_cost_tie(double a, double ref) {
-    if (!(fabs(ref) < 1e11) || !(fabs(a) < 1e11)) return a == ref;
-    return fabs(a - ref) <= 3e-5 * fabs(ref);
-}
-
-template <int MODEL>
-__device__ void polish_band(const DeviceBatch& d, int b) {
-    const BandStats bs = d.stats[b];
-    if (!bs.valid) return;
-    const PsoResult* R = d.pso_res + (size_t)(b * 8 + MODEL) * 3;
-    if (R[0].iters < 0) return;  // this model was not fitted for this band
-    double best_c = INFINITY;
-    int best_r = -1;
-    for (int r = 0; r < 3; r++)
-        if (R[r].iters >= 0 && R[r].cost < best_c) { best_c = R[r].cost; best_r = r; }
-    constexpr int np = n_params_of(MODEL);
-    const int lane = threadIdx.x & 31, j = lane & 7;
-    double pj = (best_r >= 0 && j < np) ? pso_param(R[best_r], j) : 0.0;
-    double cost = best_c;
-    if (MODEL != METZGER && best_r >= 0) {
-        LaneLb<MODEL> c;
-        c.t = d.t64 + bs.off;
-        c.flux = d.f64 + bs.off;
-        c.var = d.var64 + bs.off;
-        c.uf = d.uf64 + bs.off;
-        c.up = d.up + bs.off;
-        c.fa = d.ffa + bs.off;
-        c.fb = d.ffb + bs.off;
-        c.t_first = bs.t_first;
-        c.t_last = bs.t_last;
-        c.n = bs.n;
-        c.nd = (double)max(bs.n, 1);
-        c.inv_nd = 1.0 / c.nd;
-        c.evals = 0;
-        c.iters = 0;
-        c.fp64_evals = 0;
-        c.with_prior = true;
-        c.lo_j = j < np ? c_lo[MODEL][j] : 0.0;
-        c.hi_j = j < np ? c_hi[MODEL][j] : 0.0;
-        constexpr int t0i = t0_idx_of(MODEL);
-        double t0_lo = fmax(bs.t_first - 30.0, c_lo[MODEL][t0i]);
-        double t0_hi = fmin(bs.t_peak + 10.0, c_hi[MODEL][t0i]);
-        if (j == t0i && t0_lo < t0_hi) { c.lo_j = t0_lo; c.hi_j = t0_hi; }
-        // the restarts' swarms report FP32 estimates of their best costs: the
-        // chosen restart's cost, and the choice among restarts within the
-        // estimates' error of it, are settled on accurate costs (the first
-        // strict minimum, as the reference's restart loop)
-        {
-            auto accurate = [&](int r) {
-                const double pr = j < np ? pso_param(R[r], j) : 0.0;
-                double f, g_unused;
-                c.cost_grad(pr, f, g_unused, false);
-                c.evals--;  // not a polish evaluation
-                return f;
-            };
-            double acc[3] = {INFINITY, INFINITY, INFINITY};
-            int nc = 0;
-            for (int r = 0; r < 3; r++)
-                if (R[r].iters >= 0 && (r == best_r || swarm_cost_tie(R[r].cost, best_c))) {
-                    acc[r] = accurate(r);
-                    nc++;
-                }
-            if (nc > 1) {
-                best_r = -1;
-                best_c = INFINITY;
-                for (int r = 0; r < 3; r++)
-                    if (acc[r] < best_c) { best_c = acc[r]; best_r = r; }
-                if (best_r < 0) best_r = 0;
-                pj = j < np ? pso_param(R[best_r], j) : 0.0;
-            } else {
-                best_c = acc[best_r];
-            }
-        }
-        cost = lane_lbfgs_polish(c, pj, best_c);
-        if (lane == 0) {
-            atomicAdd(&d.ctr->lb_polishes, 1ull);
-            atomicAdd(&d.ctr->lb_iters, (unsigned long long)c.iters);
-            atomicAdd(&d.ctr->lb_evals, (unsigned long long)c.evals);
-            atomicAdd(&d.ctr->lb_obs_evals, (unsigned long long)c.evals * (unsigned long long)bs.n);
-            atomicAdd(&d.ctr->lb_obs_evals_by_model[MODEL], (unsigned long long)c.evals * (unsigned long long)bs.n);
-            if (c.fp64_evals)
-                atomicAdd(&d.ctr->lb_fp64_obs_evals_by_model[MODEL],
-                          (unsigned long long)c.fp64_evals * (unsigned long long)bs.n);
-        }
-    }
-    ModelFit& F = d.fits[b * 8 + MODEL];
-    if (lane == 0) F.cost = cost;
-    if (lane < MAXP) F.params[lane] = lane < np ? pj : NAN;
-}
-
-// One warp per (band, model), model-major: consecutive warps (and so the
-// warps resident on an SM) polish the same model, whose code then stays in
-// the instruction cache.
-// Blocks of 128 threads per SM the polish's register budget is sized for
-// (64 registers a thread): measured on GB300 at 10k sources, 32 resident
-// warps polish in 607 ms against 644 ms with 20 warps, 712 ms with 12 and
-// 812 ms with 8, spills included (the double-float polish is bound by
-// latency and instruction fetch, not by one pipe).
+// The polish (lbfgs_group.cuh): a persistent grid whose warps drain the
+// models' queues in turn, four polishes per warp.
+// Blocks of 128 threads per SM the register budget is sized for: two (255
+// registers a thread, no spills), 8 warps = 32 polishes per SM.
 #ifndef LCF_LB_MINB
-#define LCF_LB_MINB 8
+#define LCF_LB_MINB 2
 #endif
 #ifndef LCF_LB_BLOCK
 #define LCF_LB_BLOCK 128
 #endif
 __global__ void __launch_bounds__(LCF_LB_BLOCK, LCF_LB_MINB) lbfgs_kernel(DeviceBatch d, int model_mask) {
-    const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    if (warp >= d.n_bands * 8) return;
-    const int m = warp / d.n_bands, b = warp - m * d.n_bands;
-    if (!((model_mask >> m) & 1)) return;
-    switch (m) {
-        case BAZIN: polish_band<BAZIN>(d, b); break;
-        case VILLAR: polish_band<VILLAR>(d, b); break;
-        case TDE: polish_band<TDE>(d, b); break;
-        case ARNETT: polish_band<ARNETT>(d, b); break;
-        case MAGNETAR: polish_band<MAGNETAR>(d, b); break;
-        case SHOCK: polish_band<SHOCK>(d, b); break;
-        case AFTERGLOW: polish_band<AFTERGLOW>(d, b); break;
-        default: polish_band<METZGER>(d, b); break;
-    }
+    __shared__ LbWarpShared sh[LCF_LB_BLOCK / 32];
+    LbWarpShared& w = sh[threadIdx.x >> 5];
+    if (model_mask & (1 << BAZIN)) polish_queue<BAZIN>(d, w);
+    if (model_mask & (1 << VILLAR)) polish_queue<VILLAR>(d, w);
+    if (model_mask & (1 << TDE)) polish_queue<TDE>(d, w);
+    if (model_mask & (1 << ARNETT)) polish_queue<ARNETT>(d, w);
+    if (model_mask & (1 << MAGNETAR)) polish_queue<MAGNETAR>(d, w);
+    if (model_mask & (1 << SHOCK)) polish_queue<SHOCK>(d, w);
+    if (model_mask & (1 << AFTERGLOW)) polish_queue<AFTERGLOW>(d, w);
+    if (model_mask & (1 << METZGER)) polish_queue<METZGER>(d, w);
+}
+
+int lbfgs_grid(int num_sms) {
+    int n = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, lbfgs_kernel, LCF_LB_BLOCK, 0) != cudaSuccess || n < 1) n = 1;
+    return num_sms * n;
 }
 
 void launch_lbfgs(const DeviceBatch& d, int model_mask, cudaStream_t s) {
     if (d.n_bands == 0) return;
-    int block = LCF_LB_BLOCK;
-    int64_t threads = (int64_t)d.n_bands * 8 * 32;
-    lbfgs_kernel<<<(int)((threads + block - 1) / block), block, 0, s>>>(d, model_mask);
+    lbfgs_kernel<<<d.lb_grid, LCF_LB_BLOCK, 0, s>>>(d, model_mask);
+}
+
+// The polish queue's band order: longest first (counting sort on 256 keys,
+// 8 observations a key), so that the groups of a warp take bands of similar
+// length.  The order inside a key is not fixed; no result depends on it.
+__device__ __forceinline__ int polish_key(const DeviceBatch& d, int b) { return 255 - min(d.stats[b].n >> 3, 255); }
+__global__ void polish_hist_kernel(DeviceBatch d) {
+    for (int b = blockIdx.x * blockDim.x + threadIdx.x; b < d.n_bands; b += gridDim.x * blockDim.x)
+        atomicAdd(&d.ctr->polish_hist[polish_key(d, b)], 1);
+}
+__global__ void polish_scan_kernel(DeviceBatch d) {  // one block of 256 threads
+    __shared__ int sh[256];
+    const int i = threadIdx.x;
+    const int v = d.ctr->polish_hist[i];
+    sh[i] = v;
+    __syncthreads();
+    for (int off = 1; off < 256; off <<= 1) {
+        const int a = i >= off ? sh[i - off] : 0;
+        __syncthreads();
+        sh[i] += a;
+        __syncthreads();
+    }
+    d.ctr->polish_hist[i] = sh[i] - v;
+}
+__global__ void polish_scatter_kernel(DeviceBatch d) {
+    for (int b = blockIdx.x * blockDim.x + threadIdx.x; b < d.n_bands; b += gridDim.x * blockDim.x)
+        d.polish_order[atomicAdd(&d.ctr->polish_hist[polish_key(d, b)], 1)] = b;
+}
+void launch_polish_order(const DeviceBatch& d, cudaStream_t s) {
+    if (d.n_bands == 0) return;
+    int grid = (d.n_bands + 255) / 256;
+    grid = grid < 1024 ? grid : 1024;
+    polish_hist_kernel<<<grid, 256, 0, s>>>(d);
+    polish_scan_kernel<<<1, 256, 0, s>>>(d);
+    polish_scatter_kernel<<<grid, 256, 0, s>>>(d);
 }
 
 // ---------------------------------------------------------------------------

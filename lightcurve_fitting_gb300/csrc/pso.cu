@@ -120,42 +120,72 @@ __global__ void prep_kernel(DeviceBatch d) {
     for (int i = lane; i + 1 < n; i += 32)
         if (d.times[o0 + i + 1] < d.times[o0 + i]) sorted = false;
     sorted = __all_sync(FULL, sorted);
+    // The double-float copy for the polish holds the band's detections first,
+    // then its upper limits, each in time order: the lanes of one iteration of
+    // its observation loop then take the same branch of the term.
+    int n_det = 0;
     for (int i = lane; i < n; i += 32) {
-        double t = d.times[o0 + i];
-        int pos = i;
-        if (!sorted) {
-            pos = 0;
-            for (int j = 0; j < n; j++) {
-                double tj = d.times[o0 + j];
-                pos += (tj < t || (tj == t && j < i)) ? 1 : 0;
+        const double f = d.flux[o0 + i], e = d.err[o0 + i];
+        n_det += (e > 0.0 && (f / e) < 3.0) ? 0 : 1;
+    }
+    for (int k = 16; k; k >>= 1) n_det += __shfl_xor_sync(FULL, n_det, k);
+    int det_run = 0;
+    for (int base = 0; base < n; base += 32) {
+        const int i = base + lane;
+        const bool in = i < n;
+        double t = 0.0, f = 0.0, e = 0.0;
+        bool up = false;
+        if (in) {
+            t = d.times[o0 + i];
+            f = d.flux[o0 + i];
+            e = d.err[o0 + i];
+            up = e > 0.0 && (f / e) < 3.0;
+        }
+        const unsigned detm = __ballot_sync(FULL, in && !up);
+        if (in) {
+            int pos = i, pos_ff;
+            if (!sorted) {
+                pos = 0;
+                int cls = 0;  // earlier observations of the same class
+                for (int j = 0; j < n; j++) {
+                    const double tj = d.times[o0 + j];
+                    if (tj < t || (tj == t && j < i)) {
+                        pos++;
+                        const double fj = d.flux[o0 + j], ej = d.err[o0 + j];
+                        cls += ((ej > 0.0 && (fj / ej) < 3.0) == up) ? 1 : 0;
+                    }
+                }
+                pos_ff = up ? n_det + cls : cls;
+            } else {
+                const int det_before = det_run + __popc(detm & ((1u << lane) - 1u));
+                pos_ff = up ? n_det + (i - det_before) : det_before;
             }
+            const double fn = f / peak, fe = e / peak;
+            const double uf = 3.0 * e / peak;
+            const double var = fe * fe + 1e-10;
+            const int64_t q = o0 + pos;
+            const float th = (float)t;
+            float4 rec;
+            rec.x = th;
+            rec.y = (float)(t - (double)th);
+            rec.z = (float)(up ? uf : fn);
+            rec.w = up ? -(float)var : (float)var;
+            d.obs[q] = rec;
+            d.t64[q] = t;
+            d.f64[q] = fn;
+            d.fe64[q] = fe;
+            d.var64[q] = var;
+            d.uf64[q] = uf;
+            d.up[q] = up ? 1 : 0;
+            {
+                const double y = up ? uf : fn;
+                const float yh = (float)y, vh = (float)var, vl = (float)(var - (double)vh);
+                d.ffa[o0 + pos_ff] = make_float4(th, rec.y, yh, (float)(y - (double)yh));
+                d.ffb[o0 + pos_ff] = up ? make_float2(-vh, -vl) : make_float2(vh, vl);
+            }
+            d.mag64[q] = -2.5 * log10(f) + 23.9;
         }
-        double f = d.flux[o0 + i], e = d.err[o0 + i];
-        double fn = f / peak, fe = e / peak;
-        bool up = e > 0.0 && (f / e) < 3.0;
-        double uf = 3.0 * e / peak;
-        double var = fe * fe + 1e-10;
-        int64_t q = o0 + pos;
-        float th = (float)t;
-        float4 rec;
-        rec.x = th;
-        rec.y = (float)(t - (double)th);
-        rec.z = (float)(up ? uf : fn);
-        rec.w = up ? -(float)var : (float)var;
-        d.obs[q] = rec;
-        d.t64[q] = t;
-        d.f64[q] = fn;
-        d.fe64[q] = fe;
-        d.var64[q] = var;
-        d.uf64[q] = uf;
-        d.up[q] = up ? 1 : 0;
-        {
-            double y = up ? uf : fn;
-            float yh = (float)y, vh = (float)var, vl = (float)(var - (double)vh);
-            d.ffa[q] = make_float4(th, rec.y, yh, (float)(y - (double)yh));
-            d.ffb[q] = up ? make_float2(-vh, -vl) : make_float2(vh, vl);
-        }
-        d.mag64[q] = -2.5 * log10(f) + 23.9;
+        det_run += __popc(detm);
     }
     if (lane == 0) d.stats[b] = st;
 }

@@ -552,18 +552,28 @@ static bool prepare_band(const double* times, const double* flux, const double* 
 // stands in for FP32 rounding of the costs, so
 // the tests can measure how far the reference's own results move under it.
 // 0 (the default) leaves the arithmetic untouched.
-static double g_cost_rel = 0.0;
+static double g_cost_rel = 0.0, g_grad_rel = 0.0;
 static uint64_t g_cost_salt = 0;
-static inline double perturb_cost(double c, const double* p, int np) {
-    if (g_cost_rel == 0.0 || !(std::fabs(c) < 1e11)) return c;
-    uint64_t h = 0x9E3779B97F4A7C15ULL ^ (g_cost_salt * 0xD1B54A32D192ED03ULL);
+static inline uint64_t perturb_hash(const double* p, int np, uint64_t extra) {
+    uint64_t h = 0x9E3779B97F4A7C15ULL ^ (g_cost_salt * 0xD1B54A32D192ED03ULL) ^ (extra * 0x94D049BB133111EBULL);
     for (int j = 0; j < np; j++) {
         uint64_t b;
         std::memcpy(&b, &p[j], 8);
         h = (h ^ b) * 0xBF58476D1CE4E5B9ULL;
         h ^= h >> 31;
     }
-    return c * ((h >> 63) ? 1.0 + g_cost_rel : 1.0 - g_cost_rel);
+    return h;
+}
+static inline double perturb_cost(double c, const double* p, int np) {
+    if (g_cost_rel == 0.0 || !(std::fabs(c) < 1e11)) return c;
+    return c * ((perturb_hash(p, np, 0) >> 63) ? 1.0 + g_cost_rel : 1.0 - g_cost_rel);
+}
+// each gradient component scaled by 1 +- g_grad_rel (sign from the point,
+// the component and the salt)
+static inline void perturb_grad(double* g, const double* p, int np) {
+    if (g_grad_rel == 0.0) return;
+    for (int j = 0; j < np; j++)
+        g[j] *= (perturb_hash(p, np, 1 + (uint64_t)j) >> 63) ? 1.0 + g_grad_rel : 1.0 - g_grad_rel;
 }
 
 struct Cost {
@@ -668,6 +678,7 @@ struct Cost {
             }
         }
         for (int j = 0; j < np; j++) g[j] /= nn;
+        perturb_grad(g, p, np);
     }
 };
 
@@ -2564,5 +2575,9 @@ int orc_gpu_svi_fit(int m, const double* t, const double* f, const double* var, 
     if (m < 0 || m > 7 || np < 1 || np > 7 || se < 0 || se >= np) return -1;
     return gpu_svi_fit(m, t, f, var, up, uf, n, init, np, se, pcen, pwid, n_steps, n_samples, lr, src, mu, ls, elbo);
 }
-void orc_set_cost_perturbation(double rel, uint64_t salt) { g_cost_rel = rel; g_cost_salt = salt; }
+void orc_set_cost_perturbation(double rel, uint64_t salt, double grad_rel) {
+    g_cost_rel = rel;
+    g_cost_salt = salt;
+    g_grad_rel = grad_rel;
+}
 }  // extern "C"

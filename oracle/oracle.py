@@ -72,7 +72,7 @@ def lib():
         L.orc_joint_cost.argtypes = [C.POINTER(abi.BandsCSR), i, vp, vp]
         L.orc_pso_stats.argtypes = [vp, i]
         L.orc_max_threads.restype = i
-        L.orc_set_cost_perturbation.argtypes = [d, u64]
+        L.orc_set_cost_perturbation.argtypes = [d, u64, d]
         L.orc_metzger_at_obs.argtypes = [vp, d]
         L.orc_metzger_at_obs.restype = d
         L.orc_gpu_pso_cost.argtypes = [i, vp, vp, vp, vp, vp, i, vp, i, i, vp]
@@ -323,10 +323,11 @@ def gpu_svi_fit(model: int, band: Band, init, prior_c, prior_w, src: int, n_step
     return mu, ls, float(elbo[0]), steps
 
 
-def set_cost_perturbation(rel: float, salt: int = 0) -> None:
+def set_cost_perturbation(rel: float, salt: int = 0, grad_rel: float = 0.0) -> None:
     """Perturb every swarm / polish / MultiBazin cost of the oracle by +-rel
-    (a hash of the parameter vector and `salt` picks the sign); 0 restores
-    the exact arithmetic.  A test hook: with rel ~1e-7 it measures how far the
-    reference's own results move under FP32-sized rounding of its costs."""
-    lib().orc_set_cost_perturbation(float(rel), int(salt))
+    and each polish gradient component by +-grad_rel (a hash of the parameter
+    vector, the component and `salt` picks the signs); 0 restores the exact
+    arithmetic.  A test hook: it measures how far the reference's own results
+    move under rounding-sized changes of its costs and gradients."""
+    lib().orc_set_cost_perturbation(float(rel), int(salt), float(grad_rel))
 
