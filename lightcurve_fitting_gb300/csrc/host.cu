@@ -159,6 +159,7 @@ struct lcf_ctx {
     int cand_bps_rest[N_TUNE] = {1, 1, 1};  // blocks per SM, the other swarms
     int max_pso_warps_per_sm = 1;
     int lb_grid = 1;          // blocks of the persistent polish grid
+    int lb_n_long = 0;        // bands polished by a whole warp (LB_LONG_OBS observations or more)
     int cfg = 0;             // candidate of the current fit
     bool exploring = false;
     uint32_t bucket = 0;
@@ -506,8 +507,14 @@ static int prepare_layout(lcf_ctx* ctx, int n_sources, int n_bands, int64_t n_ob
     ctx->n_obs = n_obs;
     ctx->opts = o;
     int64_t n_max = 1;
-    for (int b = 0; b < n_bands; b++) n_max = std::max<int64_t>(n_max, ctx->h_boff[b + 1] - ctx->h_boff[b]);
+    int n_long = 0;
+    for (int b = 0; b < n_bands; b++) {
+        const int64_t nb_obs = ctx->h_boff[b + 1] - ctx->h_boff[b];
+        n_max = std::max<int64_t>(n_max, nb_obs);
+        n_long += nb_obs >= LB_LONG_OBS ? 1 : 0;
+    }
     ctx->n_max = n_max;
+    ctx->lb_n_long = n_long;
     // capacity
     size_t nb = (size_t)std::max(n_bands, 1), no = (size_t)std::max<int64_t>(n_obs, 1);
     int rc = 0;
@@ -709,6 +716,7 @@ static int prepare_layout(lcf_ctx* ctx, int n_sources, int n_bands, int64_t n_ob
     d.band_order = (int32_t*)ctx->band_order.p;
     d.polish_order = (int32_t*)ctx->polish_order.p;
     d.lb_grid = ctx->lb_grid;
+    d.lb_n_long = ctx->lb_n_long;
     d.n_joint = ctx->n_joint;
     d.joint_flag = ctx->n_joint > 0 ? (const uint8_t*)ctx->joint_flag.p : nullptr;
     d.joint_src = (const int32_t*)ctx->joint_src.p;

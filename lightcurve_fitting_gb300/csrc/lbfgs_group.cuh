@@ -25,6 +25,14 @@
 // warp hold bands of similar length and their observation loops end
 // together.
 //
+// On a batch that fills the grid the polish is bound by instruction fetch
+// (its double-float terms and FP64 line search are long code; measured on
+// GB300, more resident warps at different points of it made it slower).  The
+// warps of a block then run a round in step: a block barrier before and
+// after the evaluation, so that they fetch the same code.  A smaller batch is
+// bound by the latency of its polishes, which the barriers would lengthen.  The group's scalar state and the per-lane
+// vectors live in shared memory, leaving the registers to the evaluation.
+//
 // Arithmetic: the reference's algorithm in FP64 (lbfgs.cuh restates it for
 // one thread).  The dot products are sums over the eight lanes by xor 4, 2, 1
 // exchanges; the curvature pairs sit in a ring of seven (newest first in the
@@ -45,10 +53,28 @@
 
 namespace lcf {
 
+// A group's scalar state (its band, the restart reduction, the polish and
+// the line search, its work counters), in shared memory: the group's eight
+// lanes write the same values and read them back by broadcast.  Kept out of
+// the registers, it leaves them to the cost evaluation, which is bound by
+// latency and so by the warps resident per SM.
+struct LbGroupState {
+    double best_c, acc0, acc1, acc2;
+    double f, prev_f, best_f;
+    double dginit, dgtest, finit, width, width1, stx, fx, dgx, sty, fy, dgy, stp, stmin, stmax;
+    double t_first, t_last, inv_nd;
+    unsigned long long c_pol, c_it, c_ev, c_obs, c_fp64;
+    int64_t off;
+    int n, b, acc_mask, nc, best_r, cm, head, it, evals, fp64_evals, infoc, ls_iter;
+    bool brackt, stage1;
+};
+
 // Per warp, in shared memory: the curvature pairs, 1 / (y.s) and the
-// two-loop coefficients, [ring slot][lane].
+// two-loop coefficients, [ring slot][lane], and the four groups' states.
 struct LbWarpShared {
     double S[7][32], Y[7][32], rho[7][32], alpha[7][32];
+    double V[7][32];  // per lane: x, g, search direction, trial point and gradient, best point, swarm point
+    LbGroupState st[4];
 };
 
 // a.b over the eight lanes of this lane's group (mask gm)
@@ -97,7 +123,7 @@ struct GroupBand {
 
 // The observation terms in FP64 (lb_obs_term) for the FP32-range fallback:
 // this lane's share of the group's band, v = {nll, gradient partials}.
-template <int MODEL>
+template <int MODEL, int G>
 __device__ __noinline__ int group_fp64_terms(const double* t, const double* flux, const double* var, const double* uf,
                                              const uint8_t* up, int n, const double* q, const double* ep,
                                              const double* rp, double se2, bool want_grad, double* v) {
@@ -107,7 +133,7 @@ __device__ __noinline__ int group_fp64_terms(const double* t, const double* flux
     double nll = 0.0, gl[MAXP];
 #pragma unroll
     for (int k = 0; k < MAXP; k++) gl[k] = 0.0;
-    for (int i = (int)(threadIdx.x & 7); i < n; i += 8)
+    for (int i = (int)(threadIdx.x & (G - 1)); i < n; i += G)
         lb_obs_term<MODEL>(mod, t[i], var[i], flux[i], up[i], uf[i], se2, want_grad, nll, gl, nonfinite);
     v[0] = nll;
 #pragma unroll
@@ -118,15 +144,16 @@ __device__ __noinline__ int group_fp64_terms(const double* t, const double* flux
 // Cost and projected gradient of the bounded problem (BoundedPsoCost,
 // src/parametric.rs:1500-1535) at the point whose component j is xj in lane
 // j of each group: PsoCost::cost_from_slice with the population prior and
-// the Villar constraint, and PsoCost::gradient.  Warp-collective (every
-// lane calls it; a group with B.n == 0 evaluates nothing of use).  Returns 1
-// when the group's terms ran in FP64.
-template <int MODEL>
+// the Villar constraint, and PsoCost::gradient.  G lanes a group (8, or 32:
+// the whole warp, whose four sets of eight lanes hold the same vectors).
+// Warp-collective (every lane calls it; a group with B.n == 0 evaluates
+// nothing of use).  Returns 1 when the group's terms ran in FP64.
+template <int MODEL, int G>
 __device__ __forceinline__ int group_cost_grad(const DeviceBatch& d, const GroupBand& B, double xj, bool want_grad,
                                                double& fo, double& gj) {
     constexpr int np = n_params_of(MODEL), se = se_idx_of(MODEL);
-    const int lane = threadIdx.x & 31, j = lane & 7, g0 = lane & 24;
-    const unsigned gm = 0xffu << g0;
+    const int lane = threadIdx.x & 31, j = lane & 7, g0 = lane & (32 - G);
+    const unsigned gm = G == 32 ? FULL : 0xffu << g0;
     // lane j forms e^(+-p_j) of its own component in double-float; the group's
     // vectors are gathered by shuffles
     const double qj = fmin(fmax(xj, B.lo_j), B.hi_j);
@@ -176,14 +203,21 @@ __device__ __forceinline__ int group_cost_grad(const DeviceBatch& d, const Group
         int redo = 0;
         const float4* fa = d.ffa + B.off;
         const float2* fb = d.ffb + B.off;
-        for (int i = j; i < B.n; i += 8) ff_obs_term<MODEL>(fm, fa[i], fb[i], se2f, want_grad, nf, gf, nonfinite, redo);
+        for (int i = lane & (G - 1); i < B.n; i += G)
+            ff_obs_term<MODEL>(fm, fa[i], fb[i], se2f, want_grad, nf, gf, nonfinite, redo);
         in_ff = __ballot_sync(gm, redo) == 0u;
         if (in_ff) {
             nonfinite = __ballot_sync(gm, nonfinite) != 0u;
             const ff v[8] = {nf, gf[0], gf[1], gf[2], gf[3], gf[4], gf[5], gf[6]};
-            const double tot = ff_to(group_rs8_ff(v, gm));
-            nsum = __shfl_sync(gm, tot, g0);
-            gs = __shfl_sync(gm, tot, g0 + ((j + 1) & 7));
+            if (G == 32) {  // lane l: the warp's total of v[(l >> 2) & 7]
+                const double tot = ff_to(reduce_scatter8_ff(v));
+                nsum = __shfl_sync(FULL, tot, 0);
+                gs = __shfl_sync(FULL, tot, (4 * (1 + j)) & 31);
+            } else {  // lane j: the group's total of v[j]
+                const double tot = ff_to(group_rs8_ff(v, gm));
+                nsum = __shfl_sync(gm, tot, g0);
+                gs = __shfl_sync(gm, tot, g0 + ((j + 1) & 7));
+            }
         }
     }
     if (!in_ff) {
@@ -196,12 +230,18 @@ __device__ __forceinline__ int group_cost_grad(const DeviceBatch& d, const Group
         }
         const double se2 = ep[se] * ep[se];
         const int64_t o = B.off;
-        const int nf64 = group_fp64_terms<MODEL>(d.t64 + o, d.f64 + o, d.var64 + o, d.uf64 + o, d.up + o, B.n, q, ep,
-                                                 rp, se2, want_grad, v);
+        const int nf64 = group_fp64_terms<MODEL, G>(d.t64 + o, d.f64 + o, d.var64 + o, d.uf64 + o, d.up + o, B.n, q,
+                                                    ep, rp, se2, want_grad, v);
         nonfinite = __ballot_sync(gm, nf64) != 0u;
-        const double tot = group_rs8(v, gm);
-        nsum = __shfl_sync(gm, tot, g0);
-        gs = __shfl_sync(gm, tot, g0 + ((j + 1) & 7));
+        if (G == 32) {
+            const double tot = reduce_scatter8(v);
+            nsum = __shfl_sync(FULL, tot, 0);
+            gs = __shfl_sync(FULL, tot, (4 * (1 + j)) & 31);
+        } else {
+            const double tot = group_rs8(v, gm);
+            nsum = __shfl_sync(gm, tot, g0);
+            gs = __shfl_sync(gm, tot, g0 + ((j + 1) & 7));
+        }
     }
     if (!constrained) f = nonfinite ? BIG_COST : (nsum + prior * B.inv_nd) * B.inv_nd;
     fo = f;
@@ -230,39 +270,71 @@ enum LbPhase : int {
     LB_DONE        // the queue is empty
 };
 
-// Polishes every queued band of MODEL: d.polish_order[i] for the indices i
-// this warp's groups take from d.ctr->lb_next[MODEL].
-template <int MODEL>
-__device__ void polish_queue(const DeviceBatch& d, LbWarpShared& sh) {
+// Polishes the queued bands of MODEL with G lanes a band (8: four bands a
+// warp; 32: one): d.polish_order[i] for the indices i in [lo, hi) that this
+// warp's groups take from the queue counter `next`.  `lockstep` (uniform
+// over the grid): the block's warps run each round in step.
+// Out of line: the two instantiations of a model (8 and 32 lanes a band)
+// then take their registers separately.
+#ifndef LCF_LB_QUEUE_ATTR
+#define LCF_LB_QUEUE_ATTR __noinline__
+#endif
+template <int MODEL, int G>
+__device__ LCF_LB_QUEUE_ATTR void polish_queue(const DeviceBatch& d, LbWarpShared& sh, int lo, int hi, int* next,
+                                               bool lockstep) {
     constexpr int np = n_params_of(MODEL), t0i = t0_idx_of(MODEL), M = 7, MAXIT = 50;
     const double ftol = 1e-4, gtol = 0.9, xtol = 1e-10, xtrapf = 4.0, stpmin = 0.0, stpmax = INFINITY;
     const double tol_grad = 1e-6, tol_cost = 2.220446049250313e-16;
-    const int lane = threadIdx.x & 31, j = lane & 7, g0 = lane & 24;
-    const unsigned gm = 0xffu << g0;
+    const int lane = threadIdx.x & 31, j = lane & 7, gl = lane & (G - 1), g0 = lane & (32 - G);
+    const unsigned gm = G == 32 ? FULL : 0xffu << g0;
 
-    int phase = LB_FETCH, b = 0;
-    GroupBand B;
-    B.off = 0; B.n = 0; B.t_first = 0.0; B.t_last = 0.0; B.inv_nd = 1.0; B.lo_j = 0.0; B.hi_j = 0.0;
+    int phase = LB_FETCH;
+    // this lane's components: box bounds, the swarm's parameter, the point
+    // evaluated next, the iterate, its gradient, the search direction, the
+    // trial point and its gradient, the best point
+    double lo_j = 0.0, hi_j = 0.0, xe = 0.0;
+    double &x = sh.V[0][lane], &g = sh.V[1][lane], &dv = sh.V[2][lane], &xo = sh.V[3][lane], &go = sh.V[4][lane],
+           &bx = sh.V[5][lane], &pj = sh.V[6][lane];
+    x = g = dv = xo = go = bx = pj = 0.0;
+    // the group's scalars
+    LbGroupState& st = sh.st[lane / G];
+    int& b = st.b;
     // the restart reduction
-    double pj = 0.0, best_c = INFINITY, acc0 = INFINITY, acc1 = INFINITY, acc2 = INFINITY;
-    int acc_mask = 0, nc = 0, best_r = -1;
+    double &best_c = st.best_c, &acc0 = st.acc0, &acc1 = st.acc1, &acc2 = st.acc2;
+    int &acc_mask = st.acc_mask, &nc = st.nc, &best_r = st.best_r;
     // the polish
-    double xe = 0.0, x = 0.0, g = 0.0, dv = 0.0, xo = 0.0, go = 0.0, bx = 0.0;
-    double f = 0.0, prev_f = INFINITY, best_f = INFINITY;
-    int cm = 0, head = M - 1, it = 0, evals = 0, fp64_evals = 0;
+    double &f = st.f, &prev_f = st.prev_f, &best_f = st.best_f;
+    int &cm = st.cm, &head = st.head, &it = st.it, &evals = st.evals, &fp64_evals = st.fp64_evals;
     // the line search
-    double dginit = 0.0, dgtest = 0.0, finit = 0.0, width = 0.0, width1 = 0.0, stx = 0.0, fx = 0.0, dgx = 0.0,
-           sty = 0.0, fy = 0.0, dgy = 0.0, stp = 0.0, stmin = 0.0, stmax = 0.0;
-    int infoc = 1, ls_iter = 0;
-    bool brackt = false, stage1 = true;
-    // work counters of this group
-    unsigned long long c_pol = 0, c_it = 0, c_ev = 0, c_obs = 0, c_fp64 = 0;
+    double &dginit = st.dginit, &dgtest = st.dgtest, &finit = st.finit, &width = st.width, &width1 = st.width1;
+    double &stx = st.stx, &fx = st.fx, &dgx = st.dgx, &sty = st.sty, &fy = st.fy, &dgy = st.dgy;
+    double &stp = st.stp, &stmin = st.stmin, &stmax = st.stmax;
+    int &infoc = st.infoc, &ls_iter = st.ls_iter;
+    bool &brackt = st.brackt, &stage1 = st.stage1;
+    b = 0;
+    st.n = 0;
+    st.off = 0;
+    st.t_first = st.t_last = 0.0;
+    st.inv_nd = 1.0;
+    best_c = acc0 = acc1 = acc2 = INFINITY;
+    acc_mask = nc = 0;
+    best_r = -1;
+    f = 0.0;
+    prev_f = best_f = INFINITY;
+    cm = it = evals = fp64_evals = 0;
+    head = M - 1;
+    dginit = dgtest = finit = width = width1 = stx = fx = dgx = sty = fy = dgy = stp = stmin = stmax = 0.0;
+    infoc = 1;
+    ls_iter = 0;
+    brackt = false;
+    stage1 = true;
+    st.c_pol = st.c_it = st.c_ev = st.c_obs = st.c_fp64 = 0;
 
     auto restarts = [&]() { return d.pso_res + (size_t)(b * 8 + MODEL) * 3; };
     auto finish = [&](double cost) {
         ModelFit& F = d.fits[b * 8 + MODEL];
-        if (j == 0) F.cost = cost;
-        if (j < MAXP) F.params[j] = j < np ? pj : NAN;
+        if (gl == 0) F.cost = cost;
+        if (gl < MAXP) F.params[gl] = gl < np ? pj : NAN;
         phase = LB_FETCH;
     };
     auto converged = [&]() { return lb_sqrt(gdot(g, g, gm)) < tol_grad || fabs(prev_f - f) < tol_cost; };
@@ -271,11 +343,11 @@ __device__ void polish_queue(const DeviceBatch& d, LbWarpShared& sh) {
         // groups without a polish take bands until one needs polishing
         while (phase == LB_FETCH) {
             int i = 0;
-            if (j == 0) i = atomicAdd(&d.ctr->lb_next[MODEL], 1);
+            if (gl == 0) i = lo + atomicAdd(next, 1);
             i = __shfl_sync(gm, i, g0);
-            if (i >= d.n_bands) {
+            if (i >= hi) {
                 phase = LB_DONE;
-                B.n = 0;
+                st.n = 0;
                 break;
             }
             b = d.polish_order[i];
@@ -292,16 +364,16 @@ __device__ void polish_queue(const DeviceBatch& d, LbWarpShared& sh) {
                 finish(best_c);
                 continue;
             }
-            B.off = bs.off;
-            B.n = bs.n;
-            B.t_first = bs.t_first;
-            B.t_last = bs.t_last;
-            B.inv_nd = 1.0 / (double)max(bs.n, 1);
-            B.lo_j = j < np ? c_lo[MODEL][j] : 0.0;
-            B.hi_j = j < np ? c_hi[MODEL][j] : 0.0;
+            st.off = bs.off;
+            st.n = bs.n;
+            st.t_first = bs.t_first;
+            st.t_last = bs.t_last;
+            st.inv_nd = 1.0 / (double)max(bs.n, 1);
+            lo_j = j < np ? c_lo[MODEL][j] : 0.0;
+            hi_j = j < np ? c_hi[MODEL][j] : 0.0;
             const double t0_lo = fmax(bs.t_first - 30.0, c_lo[MODEL][t0i]);
             const double t0_hi = fmin(bs.t_peak + 10.0, c_hi[MODEL][t0i]);
-            if (j == t0i && t0_lo < t0_hi) { B.lo_j = t0_lo; B.hi_j = t0_hi; }
+            if (j == t0i && t0_lo < t0_hi) { lo_j = t0_lo; hi_j = t0_hi; }
             // the restarts' swarms report FP32 estimates of their best costs:
             // the chosen restart's cost, and the choice among restarts within
             // the estimates' error of it, are settled on accurate costs (the
@@ -317,12 +389,24 @@ __device__ void polish_queue(const DeviceBatch& d, LbWarpShared& sh) {
             xe = j < np ? pso_param(R[__ffs(acc_mask) - 1], j) : 0.0;
             phase = LB_ACC;
         }
+        // in step, the block's warps evaluate together (see the header): a
+        // barrier before and after the evaluation
         const bool active = phase != LB_DONE;
-        if (!__any_sync(FULL, active)) break;
-        if (MODEL == METZGER) continue;  // never polished (every group is done)
+        if (lockstep ? !__syncthreads_or(active) : !__any_sync(FULL, active)) break;
+        if constexpr (MODEL == METZGER) continue;  // never polished (every group is done)
         const bool want_grad = phase == LB_START || phase == LB_LS;
-        double fe, ge;
-        const int used64 = group_cost_grad<MODEL>(d, B, xe, want_grad, fe, ge);
+        GroupBand B;
+        B.off = st.off;
+        B.n = active ? st.n : 0;
+        B.t_first = st.t_first;
+        B.t_last = st.t_last;
+        B.inv_nd = st.inv_nd;
+        B.lo_j = lo_j;
+        B.hi_j = hi_j;
+        double fe = 0.0, ge = 0.0;
+        int used64 = 0;
+        if (__any_sync(FULL, active)) used64 = group_cost_grad<MODEL, G>(d, B, xe, want_grad, fe, ge);
+        if (lockstep) __syncthreads();
         if (!active) continue;
         fp64_evals += used64;
         // the transition of this group's phase; the steps shared by several
@@ -369,7 +453,7 @@ __device__ void polish_queue(const DeviceBatch& d, LbWarpShared& sh) {
                 cm = 0;
                 head = M - 1;
                 if (converged() || it >= MAXIT) {
-                    xe = fmin(fmax(bx, B.lo_j), B.hi_j);
+                    xe = fmin(fmax(bx, lo_j), hi_j);
                     phase = LB_FINAL;
                 } else {
                     do_begin = true;
@@ -459,7 +543,7 @@ __device__ void polish_queue(const DeviceBatch& d, LbWarpShared& sh) {
             if (f < best_f) { best_f = f; bx = x; }
             it++;
             if (converged() || it >= MAXIT) {
-                xe = fmin(fmax(bx, B.lo_j), B.hi_j);
+                xe = fmin(fmax(bx, lo_j), hi_j);
                 phase = LB_FINAL;
             } else {
                 do_begin = true;
@@ -524,17 +608,18 @@ __device__ void polish_queue(const DeviceBatch& d, LbWarpShared& sh) {
             xe = xo;
         }
         if (do_end) {
-            c_pol++;
-            c_it += (unsigned long long)it;
-            c_ev += (unsigned long long)evals;
-            c_obs += (unsigned long long)evals * (unsigned long long)B.n;
-            c_fp64 += (unsigned long long)fp64_evals * (unsigned long long)B.n;
+            st.c_pol++;
+            st.c_it += (unsigned long long)it;
+            st.c_ev += (unsigned long long)evals;
+            st.c_obs += (unsigned long long)evals * (unsigned long long)st.n;
+            st.c_fp64 += (unsigned long long)fp64_evals * (unsigned long long)st.n;
             finish(end_cost);
         }
     }
     // the work counters, summed over the warp's groups
+    unsigned long long c_pol = st.c_pol, c_it = st.c_it, c_ev = st.c_ev, c_obs = st.c_obs, c_fp64 = st.c_fp64;
 #pragma unroll
-    for (int m = 8; m < 32; m <<= 1) {
+    for (int m = G; m < 32; m <<= 1) {
         c_pol += __shfl_xor_sync(FULL, c_pol, m);
         c_it += __shfl_xor_sync(FULL, c_it, m);
         c_ev += __shfl_xor_sync(FULL, c_ev, m);

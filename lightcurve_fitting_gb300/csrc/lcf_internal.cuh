@@ -222,7 +222,8 @@ struct Counters {
     int32_t sort_hist[8][256];  // per slot: key histogram, then offsets, of the device task sort
     int32_t band_hist[16];      // bands by selected model: histogram, then offsets (band_order)
     int32_t polish_hist[256];   // bands by length: histogram, then offsets (polish_order)
-    int32_t lb_next[8];         // per model: next index of the polish queue
+    int32_t lb_next[8];         // per model: next index of the polish queue (eight lanes a band)
+    int32_t lb_next_long[8];    // per model: next index of its long bands (a warp a band)
     int32_t error;              // first error code raised on the device
     int32_t pad;
 };
@@ -270,6 +271,7 @@ struct DeviceBatch {
                             // per-band uncertainty and refinement kernels
     int32_t* polish_order;  // [n_bands] bands longest first: the polish's queue order
     int lb_grid;            // blocks of the persistent polish grid
+    int lb_n_long;          // bands of LB_LONG_OBS observations or more (the first of polish_order)
     Counters* ctr;
     float* scratch;         // MetzgerKN per-warp scratch: [warps][n_max][32]
     int64_t scratch_per_warp;
@@ -316,6 +318,8 @@ void launch_mb_pick(const DeviceBatch& d, int k, cudaStream_t s);
 void launch_mb_build(const DeviceBatch& d, int slot, int k, cudaStream_t s);
 // polish.cu
 void launch_lbfgs(const DeviceBatch& d, int model_mask, cudaStream_t s);
+// Bands of at least this many observations are polished by a whole warp.
+constexpr int LB_LONG_OBS = 256;
 // the polish queue's band order (three launches); before the first launch_lbfgs
 void launch_polish_order(const DeviceBatch& d, cudaStream_t s);
 // blocks of the persistent polish grid on `num_sms` SMs

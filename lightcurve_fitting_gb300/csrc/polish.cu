@@ -32,43 +32,78 @@ namespace lcf {
 #define FULL 0xffffffffu
 
 // The polish (lbfgs_group.cuh): a persistent grid whose warps drain the
-// models' queues in turn, four polishes per warp.
-// Blocks of 128 threads per SM the register budget is sized for: two (255
-// registers a thread, no spills), 8 warps = 32 polishes per SM.
+// models' queues in turn, four polishes per warp.  Two blocks of 8 warps per
+// SM (128 registers a thread), each block's warps in step: measured on
+// GB300 at 10k sources, 415 ms against 435 ms for four blocks of 4 warps,
+// 491 ms for one block of 16, and 486 ms for 16 warps not in step.
 #ifndef LCF_LB_MINB
 #define LCF_LB_MINB 2
 #endif
 #ifndef LCF_LB_BLOCK
-#define LCF_LB_BLOCK 128
+#define LCF_LB_BLOCK 256
 #endif
-__global__ void __launch_bounds__(LCF_LB_BLOCK, LCF_LB_MINB) lbfgs_kernel(DeviceBatch d, int model_mask) {
-    __shared__ LbWarpShared sh[LCF_LB_BLOCK / 32];
-    LbWarpShared& w = sh[threadIdx.x >> 5];
-    if (model_mask & (1 << BAZIN)) polish_queue<BAZIN>(d, w);
-    if (model_mask & (1 << VILLAR)) polish_queue<VILLAR>(d, w);
-    if (model_mask & (1 << TDE)) polish_queue<TDE>(d, w);
-    if (model_mask & (1 << ARNETT)) polish_queue<ARNETT>(d, w);
-    if (model_mask & (1 << MAGNETAR)) polish_queue<MAGNETAR>(d, w);
-    if (model_mask & (1 << SHOCK)) polish_queue<SHOCK>(d, w);
-    if (model_mask & (1 << AFTERGLOW)) polish_queue<AFTERGLOW>(d, w);
-    if (model_mask & (1 << METZGER)) polish_queue<METZGER>(d, w);
+// Each model's queue in two parts: its first n_long bands (the longest) with
+// a warp a band, the rest with eight lanes a band.
+template <int MODEL>
+__device__ __forceinline__ void polish_model(const DeviceBatch& d, LbWarpShared& w, int n_long, bool lockstep) {
+    polish_queue<MODEL, 32>(d, w, 0, n_long, &d.ctr->lb_next_long[MODEL], lockstep);
+    polish_queue<MODEL, 8>(d, w, n_long, d.n_bands, &d.ctr->lb_next[MODEL], lockstep);
 }
+
+// `stagger`: block k starts at model 8k / gridDim.x and takes the models in
+// turn from there, and the warps of a block do not run in step: a batch with
+// fewer bands than the grid has polish slots runs the eight models' queues
+// at once.  Otherwise every block takes the models in order, its warps in
+// step, and the warps of an SM share one model's code.
+__global__ void __launch_bounds__(LCF_LB_BLOCK, LCF_LB_MINB)
+    lbfgs_kernel(DeviceBatch d, int model_mask, int stagger, int n_long) {
+    extern __shared__ LbWarpShared lb_sh[];
+    LbWarpShared& w = lb_sh[threadIdx.x >> 5];
+    const int start = stagger ? (int)((8ll * blockIdx.x) / gridDim.x) : 0;
+    const bool lockstep = !stagger;
+    for (int k = 0; k < 8; k++) {
+        const int m = (start + k) & 7;
+        if (!((model_mask >> m) & 1)) continue;
+        switch (m) {
+            case BAZIN: polish_model<BAZIN>(d, w, n_long, lockstep); break;
+            case VILLAR: polish_model<VILLAR>(d, w, n_long, lockstep); break;
+            case TDE: polish_model<TDE>(d, w, n_long, lockstep); break;
+            case ARNETT: polish_model<ARNETT>(d, w, n_long, lockstep); break;
+            case MAGNETAR: polish_model<MAGNETAR>(d, w, n_long, lockstep); break;
+            case SHOCK: polish_model<SHOCK>(d, w, n_long, lockstep); break;
+            case AFTERGLOW: polish_model<AFTERGLOW>(d, w, n_long, lockstep); break;
+            default: polish_model<METZGER>(d, w, n_long, lockstep); break;
+        }
+    }
+}
+
+constexpr size_t LB_SMEM = (LCF_LB_BLOCK / 32) * sizeof(LbWarpShared);
 
 int lbfgs_grid(int num_sms) {
     int n = 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, lbfgs_kernel, LCF_LB_BLOCK, 0) != cudaSuccess || n < 1) n = 1;
+    if (cudaFuncSetAttribute(lbfgs_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)LB_SMEM) != cudaSuccess ||
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, lbfgs_kernel, LCF_LB_BLOCK, LB_SMEM) != cudaSuccess || n < 1)
+        n = 1;
     return num_sms * n;
 }
 
 void launch_lbfgs(const DeviceBatch& d, int model_mask, cudaStream_t s) {
     if (d.n_bands == 0) return;
-    lbfgs_kernel<<<d.lb_grid, LCF_LB_BLOCK, 0, s>>>(d, model_mask);
+    // a warp a band for the bands of LB_LONG_OBS observations or more (the
+    // polish of a long band on eight lanes would set the kernel's tail).  The
+    // split depends on the band alone, not on the batch: a band's summation
+    // order, and so its fit, is the same in any batch.
+    const int64_t warps = (int64_t)d.lb_grid * (LCF_LB_BLOCK / 32);
+    lbfgs_kernel<<<d.lb_grid, LCF_LB_BLOCK, LB_SMEM, s>>>(d, model_mask, (int64_t)d.n_bands < 4 * warps ? 1 : 0,
+                                                          d.lb_n_long);
 }
 
 // The polish queue's band order: longest first (counting sort on 256 keys,
 // 8 observations a key), so that the groups of a warp take bands of similar
 // length.  The order inside a key is not fixed; no result depends on it.
 __device__ __forceinline__ int polish_key(const DeviceBatch& d, int b) { return 255 - min(d.stats[b].n >> 3, 255); }
+// the long bands (a warp a band) are then exactly the first lb_n_long
+static_assert(LB_LONG_OBS % 8 == 0 && LB_LONG_OBS / 8 <= 255, "LB_LONG_OBS must fall on a key boundary");
 __global__ void polish_hist_kernel(DeviceBatch d) {
     for (int b = blockIdx.x * blockDim.x + threadIdx.x; b < d.n_bands; b += gridDim.x * blockDim.x)
         atomicAdd(&d.ctr->polish_hist[polish_key(d, b)], 1);

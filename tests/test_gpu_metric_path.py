@@ -20,7 +20,9 @@ model polishes where the other build agrees with it, better and worse
 about equally often.  Its MultiBazin fits do not move.  The criteria are
 therefore stated against the oracle itself:
   * fitted bands and their ranks are identical;
-  * >= 99 % of bands select the oracle's model; every disagreement is a near
+  * >= 99 % of bands select the oracle's model (or as many as the perturbed
+    oracles agree with the oracle, where that is fewer: 98.7 % on the basic
+    workload's 300 bands, x86 and Arm); every disagreement is a near
     tie (BIC gap below 1e-3 of the best), a band where the reference is
     unstable (its choice, or its polished cost of one of the two models,
     moves under one of the perturbations: +-1e-7 with two sign patterns,
@@ -87,11 +89,12 @@ def _moved(pr, ref, b, m):
 
 
 def selection_check(res, ref, perts):
-    """(agreement, bad, n, n_orc): bad lists the disagreements that are
-    neither near ties, nor at bands where a perturbed oracle moves, nor at
-    bands where the GPU's polish of one of the two models ended elsewhere; n
-    counts the disagreements that are not near ties, n_orc the most such
-    disagreements of a perturbed oracle with the oracle."""
+    """(agreement, floor, bad, n, n_orc): floor = min(0.99, the lowest
+    agreement of a perturbed oracle with the oracle); bad lists the
+    disagreements that are neither near ties, nor at bands where a perturbed
+    oracle moves, nor at bands where the GPU's polish of one of the two models
+    ended elsewhere; n counts the disagreements that are not near ties, n_orc
+    the most such disagreements of a perturbed oracle with the oracle."""
     fitted = ref.model >= 0
     assert np.array_equal(res.model >= 0, fitted)
     assert np.array_equal(res.rank, ref.rank)
@@ -108,7 +111,8 @@ def selection_check(res, ref, perts):
             bad.append((int(b), mo, mg))
     n_orc = max(int(sum(1 for b in np.flatnonzero(fitted) if pr.model[b] != ref.model[b]
                         and not _tie(ref, b, int(pr.model[b]), int(ref.model[b])))) for pr in perts)
-    return float(agree.mean()), bad, n, n_orc
+    floor = min([0.99] + [float(np.mean(pr.model[fitted] == ref.model[fitted])) for pr in perts])
+    return float(agree.mean()), floor, bad, n, n_orc
 
 
 def _within(a, b, tol):
@@ -124,8 +128,8 @@ def test_metric_path_matches_oracle(ctx, oracle):
     ref = oracle.fit_batch(batch, **kw)
     perts = [_perturbed(oracle, batch, *p, **kw) for p in PERTURBATIONS]
     pert = perts[0]
-    frac, bad, n, n_orc = selection_check(res, ref, perts)
-    assert frac >= 0.99 and not bad and n <= n_orc, (frac, bad, n, n_orc)
+    frac, floor, bad, n, n_orc = selection_check(res, ref, perts)
+    assert frac >= floor and not bad and n <= n_orc, (frac, floor, bad, n, n_orc)
     same = (ref.model >= 0) & (res.model == ref.model)
     same_p = same & (pert.model == ref.model)
     # the selected model's reported cost (post t0 search on rank-0 bands)
@@ -169,8 +173,8 @@ def test_basic_workload_laplace_matches_oracle(ctx, oracle):
     res = ctx.fit_batch(batch, **kw)
     ref = oracle.fit_batch(batch, **kw)
     perts = [_perturbed(oracle, batch, *p, **kw) for p in PERTURBATIONS]
-    frac, bad, n, n_orc = selection_check(res, ref, perts)
-    assert frac >= 0.99 and not bad and n <= max(n_orc, 1), (frac, bad, n, n_orc)
+    frac, floor, bad, n, n_orc = selection_check(res, ref, perts)
+    assert frac >= floor and not bad and n <= max(n_orc, 1), (frac, floor, bad, n, n_orc)
     fitted = ref.model >= 0
     a, b = res.per_model_chi2[fitted], ref.per_model_chi2[fitted]
     ok = np.isfinite(a) & np.isfinite(b)
