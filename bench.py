@@ -69,15 +69,18 @@ FP32_PER_EVAL = {0: 24, 1: 34, 2: 30, 3: 30, 4: 26, 5: 30, 6: 32, 7: 16, 8: 24, 
 FP32_PER_ODE_STEP = 60
 # DRAM traffic (dram__bytes_read.sum + dram__bytes_write.sum) per unit of
 # work of the two reported kernels, from ncu captures of the 1,000-source
-# uneven workload: the model-selection swarm moved 86.3 MB for 6.372e9
-# particle-observation evaluations, the polish 4.57 GB for 1.507e8
-# observation-term evaluations (its local-memory spill write-back).  A
-# launch's traffic is scaled from these by its own units of work.
-DRAM_BYTES_PER_PSO_OBS_EVAL = 86.32e6 / 6.372e9
-DRAM_BYTES_PER_LB_OBS_EVAL = 4.574e9 / 1.507e8
-# The polish's pipe shares in that capture (% of peak sustained): FMA 9.4,
-# FP64 41.0, issue slots 16.4, instruction-cache hit rate 53.4 %.
-LBFGS_NCU = {"fma_pipe_pct": 9.4, "fp64_pipe_pct": 41.0, "issue_active_pct": 16.4, "icache_hit_pct": 53.4}
+# uneven workload: the model-selection swarm moved 86.5 MB for 6.372e9
+# particle-observation evaluations, the polish 17.3 MB for 1.510e8
+# observation-term evaluations (its bands, its swarm results and its fits;
+# no spill traffic).  A launch's traffic is scaled from these by its own
+# units of work.
+DRAM_BYTES_PER_PSO_OBS_EVAL = 86.54e6 / 6.372e9
+DRAM_BYTES_PER_LB_OBS_EVAL = 17.26e6 / 1.510e8
+# The polish's pipe shares in that capture (% of peak sustained): FMA 9.5,
+# FP64 23.0, issue slots 14.8, instruction-cache hit rate 56.5 %, with 18.7
+# "no instruction" stall cycles per issued instruction (bound by fetch).
+LBFGS_NCU = {"fma_pipe_pct": 9.5, "fp64_pipe_pct": 23.0, "issue_active_pct": 14.8, "icache_hit_pct": 56.5,
+             "no_instruction_stall_per_issue": 18.7}
 # The reference's published CPU figure for its benchmark case (100 sources x
 # 3 bands x 30 points, fit_parametric(.., false, Laplace), one thread, Skylake
 # Xeon): 113-116 sources/s (benchmarks/parametric_sources.csv:2-8).
@@ -405,8 +408,8 @@ def run_fused(args, ws, rank, local):
         "particle_obs_evals": float(sum(ev)),
     }
     # the L-BFGS polish beside it: its observation-term evaluations per second
-    # of the launch, its pipe shares from ncu (it is bound by instruction fetch
-    # and the FP64 pipe of its line search, not by one arithmetic pipe), and
+    # of the launch, its pipe shares from ncu (it is bound by instruction
+    # fetch, not by one arithmetic pipe), and
     # the rate its own observation terms reach streamed at full occupancy (the
     # double-float term for the evaluations it ran, the FP64 term for the range
     # fallbacks, weighted by this launch's per-model evaluations)
@@ -428,7 +431,7 @@ def run_fused(args, ws, rank, local):
         "frac_of_own_term_rate": lb_rate / lb_term_peak if lb_term_peak else None,
         "traffic": float(sum(lb_ev[:7])) * DRAM_BYTES_PER_LB_OBS_EVAL,
         "traffic_source": "ncu DRAM bytes per observation-term evaluation of the 1,000-source launch, scaled by "
-                          "this launch's evaluations (local-memory spill write-back)",
+                          "this launch's evaluations",
         "ff_term_rate_by_model": pkff,
         "fp64_term_rate_by_model": pk64[:7],
         "ff_vs_fp64_worst_rel_by_model": peaks_ff["worst_rel"],
