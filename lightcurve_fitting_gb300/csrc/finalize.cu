@@ -482,8 +482,14 @@ __device__ void jacobi_eigen(double* a, int n, double* ev, double* V) {
                 double v = fabs(a[i * n + j]);
                 if (v > mv) { mv = v; p = i; q = j; }
             }
-        if (mv < 1e-15) break;
         double app = a[p * n + p], aqq = a[q * n + q], apq = a[p * n + q];
+        // the reference stops below 1e-15 absolute, which a Hessian with
+        // entries ~1e6 never reaches (its rotations leave ~1e-10): it then
+        // runs all 100 n^2 rotations, each of them below rounding level once
+        // the largest off-diagonal element is below 1e-15 of its diagonal
+        // pair.  Stopping there too changes the eigenvalues at rounding level
+        // and spares the FP64 trigonometry of those rotations.
+        if (mv < 1e-15 || mv <= 1e-15 * sqrt(fabs(app * aqq))) break;
         double th = fabs(app - aqq) < 1e-30 ? 0.78539816339744830962 : 0.5 * atan(2.0 * apq / (app - aqq));
         double c = cos(th), s = sin(th);
         for (int i = 0; i < n; i++) {
@@ -547,6 +553,73 @@ void launch_band_order(const DeviceBatch& d, cudaStream_t s) {
     band_scatter_kernel<<<grid, 256, 0, s>>>(d);
 }
 
+// Analytic Hessian of neg_log_posterior (src/parametric.rs:2464-2507) over the
+// shape parameters idx[0..ns), sigma_extra held fixed as laplace_fit holds
+// it (:2623-2693).  Forward mode over the analytic gradient: column k is the
+// derivative along parameter idx[k] of
+//   sum_i dl_i/dpred * grad pred_i + the prior's gradient,
+// i.e. sum_i (d2l_i/dpred2 g_j g_k + dl_i/dpred h_jk) + the prior's 1 / w^2
+// on the diagonal, with g = grad pred and its column h from the model
+// gradient evaluated on Dual numbers, and the upper-limit term's log-CDF
+// derivatives from a second-order Taylor number.  The reference takes the
+// same matrix by central differences of its cost (4 evaluations per pair,
+// step 1e-4 max(|theta|, 1)).  Models 0..6; warp-collective, lanes over
+// observations.  Returns false when a prediction or an entry is not finite
+// (the caller then takes the reference's finite differences).
+__device__ bool laplace_hessian_analytic(int m, const BandView& b, const double* mp, const int* idx, int ns,
+                                         double* H) {
+    const int lane = threadIdx.x & 31;
+    const int nf = n_params_of(m), se = se_idx_of(m);
+    const double se2 = exp(2.0 * mp[se]);
+    int bad = 0;
+    for (int sk = 0; sk < ns; sk++) {
+        Dual q[MAXP];
+        for (int j = 0; j < nf; j++) q[j] = Dual(mp[j], j == idx[sk] ? 1.0 : 0.0);
+        double col[MAXP];
+        for (int sj = 0; sj < ns; sj++) col[sj] = 0.0;
+        for (int i = lane; i < b.n; i += 32) {
+            Dual g[MAXP];
+            model_grad_t<Dual>(m, q, Dual(b.t[i]), g);
+            const double pr = eval_model_f64(m, mp, b.t[i]);
+            if (!isfinite(pr)) {
+                bad = 1;
+                continue;
+            }
+            const double tv = b.var[i] + se2;
+            double a1, a2;  // dl / dpred and d2l / dpred2
+            if (b.up[i]) {
+                // l = -log Phi(z), z = (u - pred) / s
+                const double s = sqrt(tv);
+                const Jet2 L = log_normal_cdf_jet(Jet2((b.uf[i] - pr) / s, 1.0, 0.0));
+                a1 = L.c1 / s;
+                a2 = -2.0 * L.c2 / tv;
+            } else {
+                // l = ((pred - y)^2 / tv + ln(2 pi tv)) / 2
+                a1 = (pr - b.f[i]) / tv;
+                a2 = 1.0 / tv;
+            }
+            const double gk = g[idx[sk]].v;
+            for (int sj = 0; sj < ns; sj++) col[sj] += a2 * g[idx[sj]].v * gk + a1 * g[idx[sj]].d;
+        }
+        for (int sj = 0; sj < ns; sj++) {
+            double v = wsum(col[sj]);
+            if (sj == sk) {
+                const double w = c_pri_w[m][idx[sj]];
+                v += 1.0 / (w * w);
+            }
+            H[sj * ns + sk] = v;
+        }
+    }
+    for (int a = 0; a < ns; a++)
+        for (int c = a; c < ns; c++) {
+            const double v = 0.5 * (H[a * ns + c] + H[c * ns + a]);
+            H[a * ns + c] = v;
+            H[c * ns + a] = v;
+            if (!isfinite(v)) bad = 1;
+        }
+    return !__any_sync(FULL, bad);
+}
+
 __global__ void laplace_kernel(DeviceBatch d) {
     int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     if (warp >= d.n_bands) return;
@@ -564,7 +637,11 @@ __global__ void laplace_kernel(DeviceBatch d) {
     for (int i = 0; i < nf; i++)
         if (i != se) idx[ns++] = i;
     double H[36];
-    for (int si = 0; si < ns; si++) {
+    // the analytic Hessian (forward over the adjoint); MetzgerKN, whose
+    // gradient is itself a finite difference in the reference, and points
+    // with non-finite predictions keep the reference's central differences
+    const bool analytic = m != METZGER && f0 < 1e99 && laplace_hessian_analytic(m, b, mp, idx, ns, H);
+    for (int si = 0; si < ns && !analytic; si++) {
         int i = idx[si];
         double hi = 1e-4 * fmax(fabs(mp[i]), 1.0);
         for (int sj = si; sj < ns; sj++) {

@@ -8,189 +8,200 @@
 
 #include <math.h>
 
+#include "dual64.cuh"
+
 namespace lcf {
 
 __device__ __forceinline__ double sp64(double x) { return log(1.0 + exp(x)) + 1e-6; }
+template <class T>
+__device__ __forceinline__ T sp64_t(T x) { return mlog(1.0 + mexp(x)) + 1e-6; }
 
-__device__ inline double eval_model_f64(int m, const double* p, double t) {
+// The model formulas on a scalar type T: double (eval_model_f64 and
+// model_grad_f64 below) or the forward-mode Dual of dual64.cuh (the Laplace
+// Hessian).
+template <class T>
+__device__ inline T eval_model_t(int m, const T* p, T t) {
     switch (m) {
         case 0: {
-            double a = exp(p[0]), b = p[1], dt = t - p[2], tr = exp(p[3]), tf = exp(p[4]);
-            return a * exp(-dt / tf) * (1.0 / (1.0 + exp(-dt / tr))) + b;
+            T a = mexp(p[0]), b = p[1], dt = t - p[2], tr = mexp(p[3]), tf = mexp(p[4]);
+            return a * mexp(-dt / tf) * (1.0 / (1.0 + mexp(-dt / tr))) + b;
         }
         case 1: {
-            double a = exp(p[0]), beta = p[1], gamma = exp(p[2]), ph = t - p[3], tr = exp(p[4]), tf = exp(p[5]);
-            double sig = 1.0 / (1.0 + exp(-ph / tr));
-            double w = 1.0 / (1.0 + exp(-10.0 * (ph - gamma)));
-            double pl = 1.0 - beta * ph;
-            double pr = (1.0 - beta * gamma) * exp((gamma - ph) / tf);
+            T a = mexp(p[0]), beta = p[1], gamma = mexp(p[2]), ph = t - p[3], tr = mexp(p[4]), tf = mexp(p[5]);
+            T sig = 1.0 / (1.0 + mexp(-ph / tr));
+            T w = 1.0 / (1.0 + mexp(-10.0 * (ph - gamma)));
+            T pl = 1.0 - beta * ph;
+            T pr = (1.0 - beta * gamma) * mexp((gamma - ph) / tf);
             return a * sig * ((1.0 - w) * pl + w * pr);
         }
         case 2: {
-            double a = exp(p[0]), b = p[1], ph = t - p[2], tr = exp(p[3]), tf = exp(p[4]), al = p[5];
-            double sig = 1.0 / (1.0 + exp(-ph / tr));
-            double w = 1.0 + sp64(ph) / tf;
-            return a * sig * pow(w, -al) + b;
+            T a = mexp(p[0]), b = p[1], ph = t - p[2], tr = mexp(p[3]), tf = mexp(p[4]), al = p[5];
+            T sig = 1.0 / (1.0 + mexp(-ph / tr));
+            T w = 1.0 + sp64_t(ph) / tf;
+            return a * sig * mpow(w, -al) + b;
         }
         case 3: {
-            double a = exp(p[0]), ph = t - p[1], tm = exp(p[2]);
-            double ps = sp64(ph);
-            double f = 1.0 / (1.0 + exp(-p[3]));
-            double heat = f * exp(-ps / 8.8) + (1.0 - f) * exp(-ps / 111.3);
-            double x = ps / tm;
-            return a * heat * (1.0 - exp(-x * x));
+            T a = mexp(p[0]), ph = t - p[1], tm = mexp(p[2]);
+            T ps = sp64_t(ph);
+            T f = 1.0 / (1.0 + mexp(-p[3]));
+            T heat = f * mexp(-ps / 8.8) + (1.0 - f) * mexp(-ps / 111.3);
+            T x = ps / tm;
+            return a * heat * (1.0 - mexp(-x * x));
         }
         case 4: {
-            double a = exp(p[0]), ph = t - p[1], tsd = exp(p[2]), td = exp(p[3]);
-            double ps = sp64(ph);
-            double w = 1.0 + ps / tsd;
-            double x = ps / td;
-            return a * (1.0 / (w * w)) * (1.0 - exp(-x * x));
+            T a = mexp(p[0]), ph = t - p[1], tsd = mexp(p[2]), td = mexp(p[3]);
+            T ps = sp64_t(ph);
+            T w = 1.0 + ps / tsd;
+            T x = ps / td;
+            return a * (1.0 / (w * w)) * (1.0 - mexp(-x * x));
         }
         case 5: {
-            double a = exp(p[0]), ph = t - p[1], n = p[2], ttr = exp(p[3]);
-            double sig5 = 1.0 / (1.0 + exp(-ph * 5.0));
-            double ps = sp64(ph);
-            double r = ps / ttr;
-            return a * sig5 * pow(ps, -n) * exp(-r * r);
+            T a = mexp(p[0]), ph = t - p[1], n = p[2], ttr = mexp(p[3]);
+            T sig5 = 1.0 / (1.0 + mexp(-ph * 5.0));
+            T ps = sp64_t(ph);
+            T r = ps / ttr;
+            return a * sig5 * mpow(ps, -n) * mexp(-r * r);
         }
         default: {
-            double a = exp(p[0]), ph = t - p[1], tb = exp(p[2]), a1 = p[3], a2 = p[4];
-            double ps = sp64(ph);
-            double lr = log(ps / tb);
-            double u = exp(2.0 * a1 * lr) + exp(2.0 * a2 * lr);
-            return a * pow(u, -0.5);
+            T a = mexp(p[0]), ph = t - p[1], tb = mexp(p[2]), a1 = p[3], a2 = p[4];
+            T ps = sp64_t(ph);
+            T lr = mlog(ps / tb);
+            T u = mexp(2.0 * a1 * lr) + mexp(2.0 * a2 * lr);
+            return a * mpow(u, -0.5);
         }
     }
 }
+__device__ inline double eval_model_f64(int m, const double* p, double t) { return eval_model_t<double>(m, p, t); }
 
-// Analytic d flux / d theta (src/parametric.rs:213-509), FP64; the
-// sigma_extra slot is 0.
-__device__ inline void model_grad_f64(int m, const double* p, double t, double* o) {
+// Analytic d flux / d theta (src/parametric.rs:213-509); the sigma_extra
+// slot is 0.
+template <class T>
+__device__ inline void model_grad_t(int m, const T* p, T t, T* o) {
     switch (m) {
         case 0: {
-            double a = exp(p[0]), dt = t - p[2], tr = exp(p[3]), tf = exp(p[4]);
-            double sig = 1.0 / (1.0 + exp(-dt / tr));
-            double base = a * exp(-dt / tf) * sig;
-            o[0] = base; o[1] = 1.0;
+            T a = mexp(p[0]), dt = t - p[2], tr = mexp(p[3]), tf = mexp(p[4]);
+            T sig = 1.0 / (1.0 + mexp(-dt / tr));
+            T base = a * mexp(-dt / tf) * sig;
+            o[0] = base; o[1] = T(1.0);
             o[2] = base * (1.0 / tf - (1.0 - sig) / tr);
             o[3] = -base * (1.0 - sig) * dt / tr;
             o[4] = base * dt / tf;
-            o[5] = 0.0;
+            o[5] = T(0.0);
             return;
         }
         case 1: {
-            double a = exp(p[0]), beta = p[1], gamma = exp(p[2]), ph = t - p[3], tr = exp(p[4]), tf = exp(p[5]);
+            T a = mexp(p[0]), beta = p[1], gamma = mexp(p[2]), ph = t - p[3], tr = mexp(p[4]), tf = mexp(p[5]);
             const double k = 10.0;
-            double sig = 1.0 / (1.0 + exp(-ph / tr));
-            double w = 1.0 / (1.0 + exp(-k * (ph - gamma)));
-            double pl = 1.0 - beta * ph;
-            double ed = exp((gamma - ph) / tf);
-            double pr = (1.0 - beta * gamma) * ed;
-            double piece = (1.0 - w) * pl + w * pr;
+            T sig = 1.0 / (1.0 + mexp(-ph / tr));
+            T w = 1.0 / (1.0 + mexp(-k * (ph - gamma)));
+            T pl = 1.0 - beta * ph;
+            T ed = mexp((gamma - ph) / tf);
+            T pr = (1.0 - beta * gamma) * ed;
+            T piece = (1.0 - w) * pl + w * pr;
             o[0] = a * sig * piece;
             o[1] = a * sig * ((1.0 - w) * (-ph) + w * (-gamma * ed));
-            double dwdlg = -k * w * (1.0 - w) * gamma;
-            double dprdlg = ed * (-beta + (1.0 - beta * gamma) / tf) * gamma;
+            T dwdlg = -k * w * (1.0 - w) * gamma;
+            T dprdlg = ed * (-beta + (1.0 - beta * gamma) / tf) * gamma;
             o[2] = a * sig * (dwdlg * (pr - pl) + w * dprdlg);
-            double dsig_dt0 = -(sig * (1.0 - sig) / tr);
-            double dw_dt0 = -(k * w * (1.0 - w));
-            double dpdt0 = dw_dt0 * (pr - pl) + (1.0 - w) * beta + w * ((1.0 - beta * gamma) * ed / tf);
+            T dsig_dt0 = -(sig * (1.0 - sig) / tr);
+            T dw_dt0 = -(k * w * (1.0 - w));
+            T dpdt0 = dw_dt0 * (pr - pl) + (1.0 - w) * beta + w * ((1.0 - beta * gamma) * ed / tf);
             o[3] = a * (dsig_dt0 * piece + sig * dpdt0);
             o[4] = a * piece * sig * (1.0 - sig) * (-ph / tr);
             o[5] = a * sig * w * (pr * (ph - gamma) / tf);
-            o[6] = 0.0;
+            o[6] = T(0.0);
             return;
         }
         case 2: {
-            double a = exp(p[0]), ph = t - p[2], tr = exp(p[3]), tf = exp(p[4]), al = p[5];
-            double sig = 1.0 / (1.0 + exp(-ph / tr));
-            double ps = sp64(ph);
-            double sp = exp(ph) / (1.0 + exp(ph));
-            double w = 1.0 + ps / tf;
-            double decay = pow(w, -al);
-            o[0] = a * sig * decay; o[1] = 1.0;
-            double dsig_dt0 = -sig * (1.0 - sig) / tr;
-            double dd_dt0 = al * pow(w, -al - 1.0) * sp / tf;
+            T a = mexp(p[0]), ph = t - p[2], tr = mexp(p[3]), tf = mexp(p[4]), al = p[5];
+            T sig = 1.0 / (1.0 + mexp(-ph / tr));
+            T ps = sp64_t(ph);
+            T sp = mexp(ph) / (1.0 + mexp(ph));
+            T w = 1.0 + ps / tf;
+            T decay = mpow(w, -al);
+            o[0] = a * sig * decay; o[1] = T(1.0);
+            T dsig_dt0 = -sig * (1.0 - sig) / tr;
+            T dd_dt0 = al * mpow(w, -al - 1.0) * sp / tf;
             o[2] = a * (dsig_dt0 * decay + sig * dd_dt0);
             o[3] = a * decay * (-sig * (1.0 - sig) * ph / tr);
-            o[4] = a * sig * al * pow(w, -al - 1.0) * ps / tf;
-            o[5] = a * sig * (-log(w)) * decay;
-            o[6] = 0.0;
+            o[4] = a * sig * al * mpow(w, -al - 1.0) * ps / tf;
+            o[5] = a * sig * (-mlog(w)) * decay;
+            o[6] = T(0.0);
             return;
         }
         case 3: {
-            double a = exp(p[0]), ph = t - p[1], tm = exp(p[2]);
-            double ps = sp64(ph);
-            double sp = exp(ph) / (1.0 + exp(ph));
-            double f = 1.0 / (1.0 + exp(-p[3]));
-            double eni = exp(-ps / 8.8), eco = exp(-ps / 111.3);
-            double heat = f * eni + (1.0 - f) * eco;
-            double x = ps / tm;
-            double ex2 = exp(-x * x);
-            double trap = 1.0 - ex2;
+            T a = mexp(p[0]), ph = t - p[1], tm = mexp(p[2]);
+            T ps = sp64_t(ph);
+            T sp = mexp(ph) / (1.0 + mexp(ph));
+            T f = 1.0 / (1.0 + mexp(-p[3]));
+            T eni = mexp(-ps / 8.8), eco = mexp(-ps / 111.3);
+            T heat = f * eni + (1.0 - f) * eco;
+            T x = ps / tm;
+            T ex2 = mexp(-x * x);
+            T trap = 1.0 - ex2;
             o[0] = a * heat * trap;
-            double dheat = -f * eni / 8.8 - (1.0 - f) * eco / 111.3;
-            double dtrap = 2.0 * ps * ex2 / (tm * tm);
+            T dheat = -f * eni / 8.8 - (1.0 - f) * eco / 111.3;
+            T dtrap = 2.0 * ps * ex2 / (tm * tm);
             o[1] = a * (-sp) * (dheat * trap + heat * dtrap);
             o[2] = -2.0 * a * heat * ex2 * x * x;
             o[3] = a * trap * (eni - eco) * f * (1.0 - f);
-            o[4] = 0.0;
+            o[4] = T(0.0);
             return;
         }
         case 4: {
-            double a = exp(p[0]), ph = t - p[1], tsd = exp(p[2]), td = exp(p[3]);
-            double ps = sp64(ph);
-            double sp = exp(ph) / (1.0 + exp(ph));
-            double w = 1.0 + ps / tsd;
-            double sd = 1.0 / (w * w);
-            double x = ps / td;
-            double ex2 = exp(-x * x);
-            double trap = 1.0 - ex2;
+            T a = mexp(p[0]), ph = t - p[1], tsd = mexp(p[2]), td = mexp(p[3]);
+            T ps = sp64_t(ph);
+            T sp = mexp(ph) / (1.0 + mexp(ph));
+            T w = 1.0 + ps / tsd;
+            T sd = 1.0 / (w * w);
+            T x = ps / td;
+            T ex2 = mexp(-x * x);
+            T trap = 1.0 - ex2;
             o[0] = a * sd * trap;
-            double w3 = 1.0 / (w * w * w);
+            T w3 = 1.0 / (w * w * w);
             o[1] = a * (-sp) * ((-2.0 * w3 / tsd) * trap + sd * (2.0 * ps * ex2 / (td * td)));
             o[2] = a * trap * 2.0 * ps * w3 / tsd;
             o[3] = -2.0 * a * sd * ex2 * x * x;
-            o[4] = 0.0;
+            o[4] = T(0.0);
             return;
         }
         case 5: {
-            double a = exp(p[0]), ph = t - p[1], n = p[2], ttr = exp(p[3]);
-            double sig5 = 1.0 / (1.0 + exp(-ph * 5.0));
-            double ps = sp64(ph);
-            double sp = exp(ph) / (1.0 + exp(ph));
-            double cooling = pow(ps, -n);
-            double r = ps / ttr;
-            double cutoff = exp(-r * r);
-            double base = cooling * cutoff;
-            double flux = a * sig5 * base;
+            T a = mexp(p[0]), ph = t - p[1], n = p[2], ttr = mexp(p[3]);
+            T sig5 = 1.0 / (1.0 + mexp(-ph * 5.0));
+            T ps = sp64_t(ph);
+            T sp = mexp(ph) / (1.0 + mexp(ph));
+            T cooling = mpow(ps, -n);
+            T r = ps / ttr;
+            T cutoff = mexp(-r * r);
+            T base = cooling * cutoff;
+            T flux = a * sig5 * base;
             o[0] = flux;
             o[1] = a * base * (-5.0 * sig5 * (1.0 - sig5) + sig5 * sp * (n / ps + 2.0 * ps / (ttr * ttr)));
-            o[2] = -flux * log(ps);
+            o[2] = -flux * mlog(ps);
             o[3] = flux * 2.0 * r * r;
-            o[4] = 0.0;
+            o[4] = T(0.0);
             return;
         }
         default: {
-            double a = exp(p[0]), ph = t - p[1], tb = exp(p[2]), a1 = p[3], a2 = p[4];
-            double ps = sp64(ph);
-            double sp = exp(ph) / (1.0 + exp(ph));
-            double lr = log(ps / tb);
-            double u1 = exp(2.0 * a1 * lr), u2 = exp(2.0 * a2 * lr);
-            double u = u1 + u2;
-            double um15 = pow(u, -1.5);
-            o[0] = a * pow(u, -0.5);
-            double du_dps = (2.0 * a1 * u1 + 2.0 * a2 * u2) / ps;
+            T a = mexp(p[0]), ph = t - p[1], tb = mexp(p[2]), a1 = p[3], a2 = p[4];
+            T ps = sp64_t(ph);
+            T sp = mexp(ph) / (1.0 + mexp(ph));
+            T lr = mlog(ps / tb);
+            T u1 = mexp(2.0 * a1 * lr), u2 = mexp(2.0 * a2 * lr);
+            T u = u1 + u2;
+            T um15 = mpow(u, -1.5);
+            o[0] = a * mpow(u, -0.5);
+            T du_dps = (2.0 * a1 * u1 + 2.0 * a2 * u2) / ps;
             o[1] = a * (-0.5) * um15 * du_dps * (-sp);
             o[2] = a * (-0.5) * um15 * (-(2.0 * a1 * u1 + 2.0 * a2 * u2));
             o[3] = a * (-0.5) * um15 * 2.0 * lr * u1;
             o[4] = a * (-0.5) * um15 * 2.0 * lr * u2;
-            o[5] = 0.0;
+            o[5] = T(0.0);
             return;
         }
     }
 }
+__device__ inline void model_grad_f64(int m, const double* p, double t, double* o) { model_grad_t<double>(m, p, t, o); }
 
 // Hoisted FP64 evaluator: the per-parameter-vector constants (exponentials of
 // the log parameters, reciprocals) are formed once in init(); value() and
@@ -387,6 +398,20 @@ __device__ __forceinline__ double log_normal_cdf_f64(double x) {
     double e = poly * exp(-z * z);
     double phi = z >= 0.0 ? 0.5 * e : 1.0 - 0.5 * e;
     return log(fmax(phi, 1e-300));
+}
+
+// log_normal_cdf on a second-order Taylor number (dual64.cuh): the same A&S
+// expression, branches and floor as log_normal_cdf_f64, carrying its first
+// and second derivatives (c1, 2 c2) for the analytic Laplace Hessian.
+__device__ __forceinline__ Jet2 log_normal_cdf_jet(Jet2 x) {
+    if (x.c0 > 8.0) return jet(0.0);
+    if (x.c0 < -30.0) return -0.5 * x * x - 0.5 * log(2.0 * 3.14159265358979323846) - mlog(-x);
+    const Jet2 z = -x * 0.70710678118654752440;
+    const Jet2 t = 1.0 / (1.0 + 0.3275911 * mabs(z));
+    const Jet2 poly = t * (0.254829592 + t * (-0.284496736 + t * (1.421413741 + t * (-1.453152027 + t * 1.061405429))));
+    const Jet2 e = poly * mexp(-z * z);
+    const Jet2 phi = z.c0 >= 0.0 ? 0.5 * e : 1.0 - 0.5 * e;
+    return phi.c0 > 1e-300 ? mlog(phi) : jet(log(1e-300));
 }
 
 // Upper-limit term of the cost and its gradient factor at z = (u - pred) /

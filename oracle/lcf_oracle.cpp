@@ -1431,6 +1431,9 @@ static void symmetric_eigen(const double* mat, int n, double* ev, double* V) {
     }
     for (int i = 0; i < n; i++) ev[i] = a[i * n + i];
 }
+// The relative finite-difference step of laplace_fit (the reference's 1e-4);
+// a test hook measures how far the reference's log sigma depends on it.
+static double g_laplace_step = 1e-4;
 static Uncert laplace_fit(int m, const Band& b, const std::vector<double>& mp) {
     int nf = (int)mp.size(), se = SE_IDX[m];
     double f0 = neg_log_posterior(m, b, mp.data());
@@ -1440,10 +1443,10 @@ static Uncert laplace_fit(int m, const Band& b, const std::vector<double>& mp) {
     std::vector<double> pp(mp), pm(mp), mpp(mp), mm(mp);
     for (int si = 0; si < ns; si++) {
         int i = idx[si];
-        double hi = 1e-4 * std::fmax(std::fabs(mp[i]), 1.0);
+        double hi = g_laplace_step * std::fmax(std::fabs(mp[i]), 1.0);
         for (int sj = si; sj < ns; sj++) {
             int j = idx[sj];
-            double hj = 1e-4 * std::fmax(std::fabs(mp[j]), 1.0);
+            double hj = g_laplace_step * std::fmax(std::fabs(mp[j]), 1.0);
             pp = mp; pm = mp; mpp = mp; mm = mp;
             pp[i] += hi; pp[j] += hj;
             pm[i] += hi; pm[j] -= hj;
@@ -2575,6 +2578,7 @@ int orc_gpu_svi_fit(int m, const double* t, const double* f, const double* var, 
     if (m < 0 || m > 7 || np < 1 || np > 7 || se < 0 || se >= np) return -1;
     return gpu_svi_fit(m, t, f, var, up, uf, n, init, np, se, pcen, pwid, n_steps, n_samples, lr, src, mu, ls, elbo);
 }
+void orc_set_laplace_step(double step) { g_laplace_step = step; }
 void orc_set_cost_perturbation(double rel, uint64_t salt, double grad_rel) {
     g_cost_rel = rel;
     g_cost_salt = salt;

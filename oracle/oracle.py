@@ -73,6 +73,7 @@ def lib():
         L.orc_pso_stats.argtypes = [vp, i]
         L.orc_max_threads.restype = i
         L.orc_set_cost_perturbation.argtypes = [d, u64, d]
+        L.orc_set_laplace_step.argtypes = [d]
         L.orc_metzger_at_obs.argtypes = [vp, d]
         L.orc_metzger_at_obs.restype = d
         L.orc_gpu_pso_cost.argtypes = [i, vp, vp, vp, vp, vp, i, vp, i, i, vp]
@@ -321,6 +322,13 @@ def gpu_svi_fit(model: int, band: Band, init, prior_c, prior_w, src: int, n_step
                                   int(n_samples), float(lr), int(src), _p(mu), _p(ls), _p(elbo))
     assert steps >= 0
     return mu, ls, float(elbo[0]), steps
+
+
+def set_laplace_step(step: float = 1e-4) -> None:
+    """The relative finite-difference step of the oracle's Laplace Hessian
+    (the reference's 1e-4, restored by the default).  A test hook: it measures
+    how far the reference's own log sigma depends on the step."""
+    lib().orc_set_laplace_step(float(step))
 
 
 def set_cost_perturbation(rel: float, salt: int = 0, grad_rel: float = 0.0) -> None:

@@ -66,6 +66,24 @@ def _oracle_selection(oracle, batch, method):
     return oracle.fit_batch(batch, fit_all_models=True, method=method, run_multi_bazin=False)
 
 
+def laplace_floor(agree_with, oracle, n_bands):
+    """The share of bands the GPU's Laplace must match: 95 %, or as many as
+    the oracle matches itself with its Hessian's finite-difference step
+    doubled and halved where that is fewer, less one band.  The GPU's Hessian
+    is analytic (the step -> 0 limit); the reference's central differences
+    carry their own truncation and rounding, which ill-conditioned Hessians
+    turn into log sigma changes above 1e-5 (measured on the oracle: 3.5-8 %
+    of bands under a 2x step change)."""
+    shares = []
+    for step in (2e-4, 5e-5):
+        oracle.set_laplace_step(step)
+        try:
+            shares.append(agree_with())
+        finally:
+            oracle.set_laplace_step()
+    return min([0.95] + shares) - 1.0 / n_bands
+
+
 def test_finalize_laplace_matches_oracle(ctx, oracle):
     """finalize_parametric_from_gpu with Laplace, from the oracle's selection."""
     batch = synth.config_uneven(20, seed=47)
@@ -76,7 +94,15 @@ def test_finalize_laplace_matches_oracle(ctx, oracle):
     assert np.array_equal(fin.model, ref.model) and np.array_equal(fin.rank, ref.rank)
     bands = [b for b in range(batch.n_bands) if ref.model[b] >= 0 and ref.model[b] != 7]
     assert len(bands) >= 30
-    assert np.mean([_refine_ok(fin, ref, b) for b in bands]) >= 0.95
+    frac = np.mean([_refine_ok(fin, ref, b) for b in bands])
+    floor = laplace_floor(lambda: np.mean([_refine_ok(oracle.finalize_batch(batch, *args, method=abi.METHOD_LAPLACE),
+                                                      ref, b) for b in bands]), oracle, len(bands))
+    assert frac >= floor, (frac, floor)
+    # the means hardly depend on the Hessian (the refinement scans' grids do):
+    # 1e-9 for >= 95 % of bands, as before the analytic Hessian
+    mu_ok = [np.allclose(fin.svi_mu[b, :abi.N_PARAMS[int(ref.model[b])]], ref.svi_mu[b, :abi.N_PARAMS[int(ref.model[b])]],
+                         rtol=1e-9, atol=1e-9) for b in bands]
+    assert np.mean(mu_ok) >= 0.95, np.mean(mu_ok)
     assert _same(fin.pso_chi2, ref.pso_chi2) and _same(fin.per_model_chi2, ref.per_model_chi2)
 
 
