@@ -553,6 +553,100 @@ void launch_band_order(const DeviceBatch& d, cudaStream_t s) {
     band_scatter_kernel<<<grid, 256, 0, s>>>(d);
 }
 
+// neg_log_posterior (src/parametric.rs:2464-2511) of MetzgerKN at one
+// parameter vector, by one lane: a first FP64 sweep for the rescale's peak
+// (the largest non-upper prediction), a second for the terms in observation
+// order, as the reference sums them.
+__device__ double metzger_nlp_lane(const BandView& b, const double* p) {
+    struct Peak {
+        const uint8_t* up;
+        double mx;
+        __device__ void operator()(int j, double l) {
+            if (!up[j]) mx = fmax(mx, l);
+        }
+    } pk{b.up, -INFINITY};
+    int j_start;
+    double l_peak;
+    bool ok = metzger_sweep64(p, b.t, b.n, pk, j_start, l_peak) && l_peak > 0.0 && isfinite(l_peak);
+    // the predictions before the first visited observation are 0
+    double mx = pk.mx / l_peak;
+    for (int j = 0; j < (ok ? j_start : b.n); j++)
+        if (!b.up[j]) mx = ok ? fmax(mx, 0.0) : 0.0;
+    if (!ok) mx = b.n > 0 ? 0.0 : -INFINITY;
+    const double scale = (mx > 1e-10 && isfinite(mx)) ? fmin(fmax(1.0 / mx, 0.1), 10.0) : 1.0;
+    const double se2 = exp(2.0 * p[se_idx_of(METZGER)]);
+    struct Terms {
+        const BandView* b;
+        double peak, scale, se2, nll;
+        int nonfinite;
+        __device__ void term(int i, double pr) {
+            if (!isfinite(pr)) { nonfinite = 1; return; }
+            const double tv = b->var[i] + se2;
+            if (b->up[i]) nll -= log_normal_cdf_f64((b->uf[i] - pr) / sqrt(tv));
+            else {
+                const double dd = pr - b->f[i];
+                nll += 0.5 * (dd * dd / tv + log(2.0 * 3.14159265358979323846 * tv));
+            }
+        }
+        __device__ void operator()(int j, double l) { term(j, (l / peak) * scale); }
+    } tm{&b, l_peak, scale, se2, 0.0, 0};
+    if (ok) {
+        for (int j = 0; j < j_start; j++) tm.term(j, 0.0 * scale);
+        metzger_sweep64(p, b.t, b.n, tm, j_start, l_peak);
+    } else {
+        for (int j = 0; j < b.n; j++) tm.term(j, 0.0 * scale);
+    }
+    if (tm.nonfinite) return 1e99;
+    double nlp = 0.0;
+    for (int j = 0; j < n_params_of(METZGER); j++) {
+        const double w = c_pri_w[METZGER][j], dd = p[j] - c_pri_c[METZGER][j];
+        nlp += 0.5 * dd * dd / (w * w);
+    }
+    return tm.nll + nlp;
+}
+
+// MetzgerKN's Laplace Hessian as the reference takes it (central differences
+// of the cost, :2623-2693), with the stencil's points spread over the lanes:
+// point 0 is the MAP (its cost f0), points 1 + 4k .. 4 + 4k the four
+// evaluations of the k-th pair (si <= sj).  Warp-collective.
+__device__ void laplace_fd_metzger(const BandView& b, const double* mp, const int* idx, int ns, double* H,
+                                   double& f0) {
+    const int lane = threadIdx.x & 31;
+    const int npts = 1 + 2 * ns * (ns + 1);
+    double c[2] = {0.0, 0.0};
+    for (int r = 0; r < 2; r++) {
+        const int pt = lane + 32 * r;
+        if (pt >= npts) continue;
+        double q[MAXP];
+        for (int t = 0; t < n_params_of(METZGER); t++) q[t] = mp[t];
+        if (pt > 0) {
+            int k = (pt - 1) >> 2, si = 0;
+            while (k >= ns - si) { k -= ns - si; si++; }
+            const int sj = si + k, s4 = (pt - 1) & 3;
+            const int i = idx[si], j = idx[sj];
+            const double hi = 1e-4 * fmax(fabs(mp[i]), 1.0), hj = 1e-4 * fmax(fabs(mp[j]), 1.0);
+            q[i] += (s4 < 2 ? 1.0 : -1.0) * hi;
+            q[j] += ((s4 & 1) == 0 ? 1.0 : -1.0) * hj;
+        }
+        c[r] = metzger_nlp_lane(b, q);
+    }
+    auto cost = [&](int pt) {
+        const double v = pt < 32 ? c[0] : c[1];
+        return __shfl_sync(FULL, v, pt & 31);
+    };
+    f0 = cost(0);
+    int k = 0;
+    for (int si = 0; si < ns; si++) {
+        const double hi = 1e-4 * fmax(fabs(mp[idx[si]]), 1.0);
+        for (int sj = si; sj < ns; sj++, k++) {
+            const double hj = 1e-4 * fmax(fabs(mp[idx[sj]]), 1.0);
+            const double h = (cost(1 + 4 * k) - cost(2 + 4 * k) - cost(3 + 4 * k) + cost(4 + 4 * k)) / (4.0 * hi * hj);
+            H[si * ns + sj] = h;
+            H[sj * ns + si] = h;
+        }
+    }
+}
+
 // Analytic Hessian of neg_log_posterior (src/parametric.rs:2464-2507) over the
 // shape parameters idx[0..ns), sigma_extra held fixed as laplace_fit holds
 // it (:2623-2693).  Forward mode over the analytic gradient: column k is the
@@ -632,7 +726,6 @@ __global__ void laplace_kernel(DeviceBatch d) {
     double* scr = d.scratch64 + 5 * bs.off;
     double mp[MAXP];
     for (int j = 0; j < nf; j++) mp[j] = o.pso_params[j];
-    double f0 = neg_log_posterior_w(m, b, mp, scr);
     int idx[MAXP], ns = 0;
     for (int i = 0; i < nf; i++)
         if (i != se) idx[ns++] = i;
@@ -640,7 +733,11 @@ __global__ void laplace_kernel(DeviceBatch d) {
     // the analytic Hessian (forward over the adjoint); MetzgerKN, whose
     // gradient is itself a finite difference in the reference, and points
     // with non-finite predictions keep the reference's central differences
-    const bool analytic = m != METZGER && f0 < 1e99 && laplace_hessian_analytic(m, b, mp, idx, ns, H);
+    // (MetzgerKN's with one stencil point per lane)
+    double f0;
+    if (m == METZGER) laplace_fd_metzger(b, mp, idx, ns, H, f0);
+    else f0 = neg_log_posterior_w(m, b, mp, scr);
+    const bool analytic = m == METZGER || (f0 < 1e99 && laplace_hessian_analytic(m, b, mp, idx, ns, H));
     for (int si = 0; si < ns && !analytic; si++) {
         int i = idx[si];
         double hi = 1e-4 * fmax(fabs(mp[i]), 1.0);
