@@ -327,10 +327,23 @@ extern "C" int lcf_ctx_create(int device, lcf_ctx** out) {
     ctx->lb_grid = lbfgs_grid(ctx->num_sms);
     // RNG tables
     std::vector<float> draws((size_t)3 * DRAWS_PER_SEED);
-    std::vector<double> eps((size_t)3 * SVI_STEPS * SVI_SAMPLES * 7);
+    // the SVI noise, then Adam's bias corrections 1 / (1 - 0.9^t) and
+    // 1 / (1 - 0.999^t) for t = 1 .. SVI_STEPS (the powers by the repeated FP64
+    // products Adam's recurrence forms)
+    std::vector<double> eps((size_t)3 * SVI_STEPS * SVI_SAMPLES * 7 + 2 * SVI_STEPS);
     std::vector<double> draws64(draws.size());
     std::vector<float2> draws15(draws.size());
     make_draw_tables(draws.data(), draws64.data(), draws15.data(), eps.data());
+    {
+        double* bc = eps.data() + (size_t)3 * SVI_STEPS * SVI_SAMPLES * 7;
+        double b1t = 1.0, b2t = 1.0;
+        for (int t = 0; t < SVI_STEPS; t++) {
+            b1t *= 0.9;
+            b2t *= 0.999;
+            bc[t] = 1.0 / (1.0 - b1t);
+            bc[SVI_STEPS + t] = 1.0 / (1.0 - b2t);
+        }
+    }
     if (cudaMalloc(&ctx->d_draws, draws.size() * sizeof(float)) != cudaSuccess ||
         cudaMalloc(&ctx->d_draws64, draws64.size() * sizeof(double)) != cudaSuccess ||
         cudaMalloc(&ctx->d_draws15, draws15.size() * sizeof(float2)) != cudaSuccess ||
@@ -701,6 +714,7 @@ static int prepare_layout(lcf_ctx* ctx, int n_sources, int n_bands, int64_t n_ob
     d.draws64 = ctx->d_draws64;
     d.draws15 = ctx->d_draws15;
     d.svi_eps = ctx->d_eps;
+    d.svi_adam_bc = ctx->d_eps + (size_t)3 * SVI_STEPS * SVI_SAMPLES * 7;
     d.pso_res = (PsoResult*)ctx->res.p;
     d.fits = (ModelFit*)ctx->fits.p;
     d.out = (BandOut*)ctx->out.p;

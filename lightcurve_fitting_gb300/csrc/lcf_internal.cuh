@@ -258,6 +258,7 @@ struct DeviceBatch {
     const double* draws64;  // the same uniforms in FP64 (swarm initialisation)
     const float2* draws15;  // 1.5 x those uniforms (FP64 products) as double-float pairs
     const double* svi_eps;  // [3][SVI_STEPS][SVI_SAMPLES][7] noise for 5, 6, 7 params (FP64, the reference's draws)
+    const double* svi_adam_bc;  // [2][SVI_STEPS] Adam's bias corrections 1 / (1 - b1^t), 1 / (1 - b2^t)
     // results
     PsoResult* pso_res;     // per task slot
     ModelFit* fits;         // [n_bands * 8]

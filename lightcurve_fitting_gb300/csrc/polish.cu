@@ -817,13 +817,15 @@ __device__ void svi_band(const DeviceBatch& d, int b) {
     const double init_j = own ? o.pso_params[j] : 0.0;
     const double pc_j = own ? (j == se ? c_pri_c[M][j] : init_j) : 0.0;
     const double pw2_j = own ? c_pri_w[M][j] * c_pri_w[M][j] : 1.0;
+    // 1 / variance, formed once: the FP64 divisions of the step are its
+    // costliest instructions on this part (a few are left: sqrt, Adam's step)
+    const double ipw2_j = own ? 1.0 / pw2_j : 0.0;
     // lane i < 2 np owns variational parameter i (mu_i, then log sigma_i)
     double vp = 0.0, am = 0.0, av = 0.0;
     if (lane < np) vp = o.pso_params[lane];
     else if (lane < 2 * np) vp = -1.0;
     const double* eps_tab = d.svi_eps + (size_t)(np - 5) * SVI_STEPS * SVI_SAMPLES * 7;
     const double ln_2pie = 2.8378770664093453;  // ln(2 pi e)
-    double b1t = 1.0, b2t = 1.0;
     double ema = -INFINITY, best_ema = -INFINITY, final_elbo = -INFINITY;
     int no_imp = 0, steps = 0;
     // MetzgerKN: per step, lanes 0..15 sweep samples 0..3 (value + 4 derivatives per observation)
@@ -891,8 +893,9 @@ __device__ void svi_band(const DeviceBatch& d, int b) {
             double lp_j = 0.0;
             if (own) {
                 const double dd = th_j - pc_j;
-                lp_j = -0.5 * dd * dd / pw2_j;
-                const double df = dl_j + (-dd / pw2_j);
+                const double dq = dd * ipw2_j;
+                lp_j = -0.5 * dd * dq;
+                const double df = dl_j - dq;
                 gmu_j += df;
                 gls_j += df * sg_j * eps_j;
             }
@@ -908,14 +911,12 @@ __device__ void svi_band(const DeviceBatch& d, int b) {
         double gi = 0.0;
         if (lane < np) gi = -(gmu_i / ns);
         else if (lane < 2 * np) gi = -(gls_i / ns + 1.0);
-        b1t *= 0.9;
-        b2t *= 0.999;
         // a component hit by a floored upper limit's ~1e285 term overflows its
         // second moment to +inf and stops, as in the reference
         if (lane < 2 * np && isfinite(gi)) {
             am = 0.9 * am + (1.0 - 0.9) * gi;
             av = 0.999 * av + (1.0 - 0.999) * gi * gi;
-            double mh = am / (1.0 - b1t), vh = av / (1.0 - b2t);
+            const double mh = am * d.svi_adam_bc[step], vh = av * d.svi_adam_bc[SVI_STEPS + step];
             vp -= SVI_LR * mh / (sqrt(vh) + 1e-8);
         }
         if (lane >= np && lane < 2 * np) vp = fmin(fmax(vp, -6.0), 2.0);
