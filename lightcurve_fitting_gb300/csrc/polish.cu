@@ -838,7 +838,10 @@ __device__ void svi_band(const DeviceBatch& d, int b) {
         steps = step + 1;
         const double mu_j = __shfl_sync(FULL, vp, j);
         const double ls_j = __shfl_sync(FULL, vp, (np + j) & 31);
-        const double sg_j = own ? exp(ls_j) : 0.0;
+        // sigma = e^(log sigma) in double-float on the FP32 pipe (log sigma is
+        // clamped to [-6, 2]; ~1e-14 relative): the FP64 exp was the step's
+        // costliest remaining FP64 call
+        const double sg_j = own ? ff_to(ff_exp(ff_from(ls_j))) : 0.0;
         if constexpr (M == METZGER) {
             double mu[MAXP], sg[MAXP];
 #pragma unroll
