@@ -235,4 +235,23 @@ LCF_FF_BIG ff ff_log(ff x) {
     return ff_norm(s, err);
 }
 
+// Ordering of double-float pairs (normalised: |lo| <= ulp(hi) / 2).
+__device__ __forceinline__ bool ff_lt(ff a, ff b) { return a.hi < b.hi || (a.hi == b.hi && a.lo < b.lo); }
+__device__ __forceinline__ bool ff_le(ff a, ff b) { return a.hi < b.hi || (a.hi == b.hi && a.lo <= b.lo); }
+
+// One dimension of a particle move (src/parametric.rs:1721-1735) in
+// double-float: velocity w v0 + 1.5 r1 (pb - x0) + 1.5 r2 (g - x0) with the
+// draws' products 1.5 r as pairs (a1, a2), clamped to +-vmax; the position
+// clamped to the box, where the velocity becomes 0.
+__device__ __forceinline__ void ff_move(ff x0, ff v0, ff pb, ff g, ff w, float2 a1, float2 a2, ff vm, ff lo, ff hi,
+                                        ff& xn, ff& vn) {
+    ff vv = ff_add(ff_add(ff_mul(w, v0), ff_mul(ffm(a1.x, a1.y), ff_sub(pb, x0))), ff_mul(ffm(a2.x, a2.y), ff_sub(g, x0)));
+    if (ff_lt(vv, ff_neg(vm))) vv = ff_neg(vm);
+    if (ff_lt(vm, vv)) vv = vm;
+    const ff nx = ff_add(x0, vv);
+    if (ff_le(nx, lo)) { xn = lo; vn = ffm(0.0f, 0.0f); }
+    else if (ff_le(hi, nx)) { xn = hi; vn = ffm(0.0f, 0.0f); }
+    else { xn = nx; vn = vv; }
+}
+
 }  // namespace lcf

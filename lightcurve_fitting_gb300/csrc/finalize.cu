@@ -1114,9 +1114,9 @@ __global__ void mb_pick_kernel(DeviceBatch d, int k, int64_t mb_base) {
         S.best_bic = kb;
         S.best_cost = c1;
         S.best_k = k;
-        for (int j = 0; j < MB_MAXP; j++) S.best_params[j] = j < np ? (double)R[best].params[j] : NAN;
+        for (int j = 0; j < MB_MAXP; j++) S.best_params[j] = j < np ? pso_param(R[best], j) : NAN;
     }
-    for (int j = 0; j < MB_MAXP; j++) S.prev_params[j] = j < np ? (double)R[best].params[j] : NAN;
+    for (int j = 0; j < MB_MAXP; j++) S.prev_params[j] = j < np ? pso_param(R[best], j) : NAN;
     S.k_done = k;
     if (k > 1 && kb > S.per_k_bic[k - 2] + 2.0) S.done = 1;
 }

@@ -93,12 +93,22 @@ void make_draw_tables(float* draws, double* draws64, float2* draws15, double* sv
 
 // The same three streams, longer: the joint multi-band swarm (200 particles,
 // up to 42 dimensions, 1500 iterations) draws up to ~25 M uniforms per seed.
-void make_joint_draws(float* draws, int64_t per_seed) {
+// Its exact-trajectory swarm reads each draw as the FP64 product 1.5 u in a
+// double-float pair, and the first init_per_seed draws (the initialisation)
+// as FP64 uniforms.
+void make_joint_draws(float2* draws15, double* draws64, int64_t per_seed, int64_t init_per_seed) {
     const uint64_t seeds[3] = {42, 137, 271};
     for (int k = 0; k < 3; k++) {
         Xoshiro r(seeds[k]);
-        float* out = draws + (size_t)k * per_seed;
-        for (int64_t i = 0; i < per_seed; i++) out[i] = (float)r.f64();
+        float2* out = draws15 + (size_t)k * per_seed;
+        double* init = draws64 + (size_t)k * init_per_seed;
+        for (int64_t i = 0; i < per_seed; i++) {
+            const double u = r.f64();
+            if (i < init_per_seed) init[i] = u;
+            const double cu = 1.5 * u;
+            const float hi = (float)cu;
+            out[i] = make_float2(hi, (float)(cu - (double)hi));
+        }
     }
 }
 
@@ -185,8 +195,10 @@ struct lcf_ctx {
     // device buffers (capacity-sized)
     DevArr times, flux, ferr, boff, soff, stats_b, obs, t64, f64, fe64, var64, uf64, mag64, up, ffa, ffb, res, fits, out, mb,
         ctr, scratch, scratch64, scratch_svi, t0state, tasks[7], task_sorted, task_sorted_mb, band_order, polish_order, joint_flag, joint_src,
-        joint_res, joint_draws;
-    int64_t joint_per_seed = 0;   // uniforms per seed held in joint_draws
+        joint_res, joint_draws15, joint_draws64, joint_state;
+    int64_t joint_per_seed = 0;   // draws per seed held in joint_draws15
+    int64_t joint_init_per_seed = 0;
+    int joint_grid = 0;
     int n_joint = 0, joint_max_obs = 0, joint_max_d = 0;
     int64_t task_cap[7] = {0, 0, 0, 0, 0, 0, 0};
     // pinned staging
@@ -302,16 +314,14 @@ extern "C" int lcf_ctx_create(int device, lcf_ctx** out) {
         lcf_ctx_destroy(ctx);
         return LCF_E_CUDA;
     }
-    // the kernels accept the largest candidate's dynamic shared memory
-    int big = 0;
-    for (int c = 1; c < N_TUNE; c++)
-        if (pso_smem_bytes(TUNE_CAND[c].block, TUNE_CAND[c].smem_obs) >
-            pso_smem_bytes(TUNE_CAND[big].block, TUNE_CAND[big].smem_obs))
-            big = c;
-    int rc = pso_init_attributes(TUNE_CAND[big].block, TUNE_CAND[big].smem_obs);
-    if (rc != 0) {
-        lcf_ctx_destroy(ctx);
-        return LCF_E_CUDA;
+    // each instantiation accepts the largest candidate's dynamic shared memory
+    {
+        int blocks[N_TUNE], obs[N_TUNE];
+        for (int c = 0; c < N_TUNE; c++) { blocks[c] = TUNE_CAND[c].block; obs[c] = TUNE_CAND[c].smem_obs; }
+        if (pso_init_attributes(blocks, obs, N_TUNE) != 0) {
+            lcf_ctx_destroy(ctx);
+            return LCF_E_CUDA;
+        }
     }
     // occupancy of the 7-dimension instantiations decides each candidate's
     // persistent grids
@@ -369,7 +379,7 @@ extern "C" void lcf_ctx_destroy(lcf_ctx* ctx) {
                      &ctx->fits, &ctx->out, &ctx->mb, &ctx->ctr, &ctx->scratch, &ctx->scratch64, &ctx->scratch_svi,
                      &ctx->t0state, &ctx->task_sorted, &ctx->task_sorted_mb, &ctx->band_order, &ctx->polish_order, &ctx->joint_flag,
                      &ctx->joint_src, &ctx->joint_res,
-                     &ctx->joint_draws,
+                     &ctx->joint_draws15, &ctx->joint_draws64, &ctx->joint_state,
                      &ctx->bc_obs, &ctx->bc_params, &ctx->bc_costs, &ctx->bc_scratch, &ctx->plain_scr,
                      &ctx->sg_in, &ctx->sg_out, &ctx->sg_scratch};
     for (DevArr* a : all) free_arr(*a);
@@ -605,15 +615,26 @@ static int prepare_layout(lcf_ctx* ctx, int n_sources, int n_bands, int64_t n_ob
             rc2 |= grow(ctx, ctx->joint_flag, (size_t)std::max(n_sources, 1));
             rc2 |= grow(ctx, ctx->joint_src, jsrc.size() * sizeof(int32_t));
             rc2 |= grow(ctx, ctx->joint_res, jsrc.size() * 3 * sizeof(JointResult));
-            // uniforms per seed: init (2 D P) + 1500 iterations x 2 D P
+            // the persistent swarm's grid and its blocks' state
+            ctx->joint_grid = joint_grid(jmax_obs, ctx->joint_max_d, ctx->num_sms);
+            rc2 |= grow(ctx, ctx->joint_state,
+                        (size_t)ctx->joint_grid * JOINT_STATE_ARRAYS * ctx->joint_max_d * 200 * sizeof(float));
+            // draws per seed: init (2 D P) + 1500 iterations x 2 D P
             int64_t need = (int64_t)3002 * ctx->joint_max_d * 200;
+            int64_t need_init = (int64_t)2 * ctx->joint_max_d * 200;
             if (need > ctx->joint_per_seed) {
-                rc2 |= grow(ctx, ctx->joint_draws, (size_t)need * 3 * sizeof(float));
+                rc2 |= grow(ctx, ctx->joint_draws15, (size_t)need * 3 * sizeof(float2));
+                rc2 |= grow(ctx, ctx->joint_draws64, (size_t)need_init * 3 * sizeof(double));
                 if (!rc2) {
-                    std::vector<float> h((size_t)need * 3);
-                    make_joint_draws(h.data(), need);
-                    CK(cudaMemcpy(ctx->joint_draws.p, h.data(), h.size() * sizeof(float), cudaMemcpyHostToDevice));
+                    std::vector<float2> h15((size_t)need * 3);
+                    std::vector<double> h64((size_t)need_init * 3);
+                    make_joint_draws(h15.data(), h64.data(), need, need_init);
+                    CK(cudaMemcpy(ctx->joint_draws15.p, h15.data(), h15.size() * sizeof(float2),
+                                  cudaMemcpyHostToDevice));
+                    CK(cudaMemcpy(ctx->joint_draws64.p, h64.data(), h64.size() * sizeof(double),
+                                  cudaMemcpyHostToDevice));
                     ctx->joint_per_seed = need;
+                    ctx->joint_init_per_seed = need_init;
                 }
             }
             if (rc2) return rc2;
@@ -735,8 +756,12 @@ static int prepare_layout(lcf_ctx* ctx, int n_sources, int n_bands, int64_t n_ob
     d.joint_flag = ctx->n_joint > 0 ? (const uint8_t*)ctx->joint_flag.p : nullptr;
     d.joint_src = (const int32_t*)ctx->joint_src.p;
     d.joint_res = (JointResult*)ctx->joint_res.p;
-    d.joint_draws = (const float*)ctx->joint_draws.p;
+    d.joint_draws15 = (const float2*)ctx->joint_draws15.p;
+    d.joint_draws64 = (const double*)ctx->joint_draws64.p;
     d.joint_draws_per_seed = ctx->joint_per_seed;
+    d.joint_init_per_seed = ctx->joint_init_per_seed;
+    d.joint_state = (float*)ctx->joint_state.p;
+    d.joint_grid = ctx->joint_grid;
     d.joint_max_obs = ctx->joint_max_obs;
     d.joint_max_d = ctx->joint_max_d;
     d.ctr = (Counters*)ctx->ctr.p;
@@ -1507,7 +1532,7 @@ extern "C" int lcf_debug_swarm_results(lcf_ctx* ctx, double* out, int64_t max_ro
         o[1] = h[r].iters;
         o[2] = h[r].evals;
         for (int j = 0; j < MB_MAXP; j++)
-            o[3 + j] = j < 7 ? pso_param(h[r], j) : (h[r].pad[0] == 1.0f ? 0.0 : (double)h[r].params[j]);
+            o[3 + j] = pso_param(h[r], j);
     }
     return 0;
 }

@@ -2,13 +2,14 @@
 // src/parametric.rs:3815-4131) that fit_parametric uses for sources with two
 // or more bands when fit_all_models is false (:3742-3761).
 //
-// One block per (source, restart): 200 particles (threads 0..199 of 224)
-// search the 7 * n_bands joint space (the most populated band's Villar
-// parameters, then per-band offsets) with the reference's PSO (200
-// particles, 1500 iterations, stall 60; seeds 42 / 137 / 271, restart 1
-// seeded).  The source's bands are staged in shared memory; positions,
-// velocities, their pre-iteration copies and the personal bests live in
-// shared memory, column-major (parameter j of particle p at [j * 200 + p]).
+// A persistent grid of blocks takes (source, restart) tasks: 200 particles
+// (threads 0..199 of 224) search the 7 * n_bands joint space (the most
+// populated band's Villar parameters, then per-band offsets) with the
+// reference's PSO (200 particles, 1500 iterations, stall 60; seeds 42 / 137 /
+// 271, restart 1 seeded).  The source's bands are staged in shared memory;
+// positions, velocities and personal bests are double-float pairs in the
+// block's global slice, column-major (parameter j of particle p at
+// [j * 200 + p]).
 // The reference's asynchronous global best (each particle moves with the
 // best after the particles before it) is reproduced by speculative rounds,
 // as in the per-band swarm: the particles from `start` on move with the
@@ -24,6 +25,9 @@
 // refinements, magnitude chi2 and MultiBazin stages run unchanged.
 #include <cuda_runtime.h>
 
+#include <algorithm>
+
+#include "ff.cuh"
 #include "lcf_internal.cuh"
 #include "models_f32.cuh"
 
@@ -43,6 +47,17 @@ static __device__ __constant__ float c_rel_mean[7] = {-0.015f * 2.302585093f, -0
 static __device__ __constant__ float c_rel_sigma[7] = {0.08f * 2.302585093f, 0.008f, 0.25f * 2.302585093f, 1.5f,
                                                        0.35f * 2.302585093f, 0.25f * 2.302585093f,
                                                        0.30f * 2.302585093f};
+
+// the same in FP64 for the box and the seed particle (as the reference
+// computes them)
+static __device__ __constant__ double c_rel_mean64[7] = {-0.015 * 2.302585092994045684, -0.001,
+                                                         -0.095 * 2.302585092994045684, -1.181,
+                                                         -0.195 * 2.302585092994045684, -0.323 * 2.302585092994045684,
+                                                         -0.025 * 2.302585092994045684};
+static __device__ __constant__ double c_rel_sigma64[7] = {0.08 * 2.302585092994045684, 0.008,
+                                                          0.25 * 2.302585092994045684, 1.5,
+                                                          0.35 * 2.302585092994045684, 0.25 * 2.302585092994045684,
+                                                          0.30 * 2.302585092994045684};
 
 struct JointBands {
     int nb;                 // bands in rank order
@@ -123,190 +138,250 @@ __device__ int block_first(bool flag, int* s_warp) {
     return q == 0x7fffffff ? -1 : q;
 }
 
+// The persistent joint swarm: each block takes (source, restart) tasks from a
+// device counter.  Positions, velocities and personal bests are double-float
+// pairs, private to each particle's thread and kept in the block's slice of
+// joint_state (L1/L2-resident, coalesced: parameter j of particle p at
+// [j * 200 + p]), so that shared memory holds only the staged observations
+// and up to four blocks share an SM.  They move with the reference's FP64
+// draws and box:
+// rounding only the joint swarm's positions to FP32 in the FP64
+// restatement moves the joint cost of 29 of the reference's 30 real ZTF
+// sources by more than 1e-4, 13 of them by more than 1 % (up to 72 %).  A
+// trial move is evaluated in FP32 at its leading floats (xt) and dropped;
+// the particles accepted in a round recompute the same move (same inputs,
+// the global best not yet updated) and commit it, so the particles not yet
+// accepted still hold their iteration-start state and no copy of it is kept.
 __global__ void __launch_bounds__(J_THREADS) joint_pso_kernel(DeviceBatch d) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    const int js = blockIdx.x / 3, restart = blockIdx.x % 3;
-    const int src = d.joint_src[js];
     const int tid = threadIdx.x;
     const bool live = tid < JP;
     __shared__ JointBands jb;
-    __shared__ double s_cost[J_THREADS];
     __shared__ int s_warp[J_THREADS / 32];
     __shared__ double s_gc;
-    __shared__ int s_D;
-    // ---- the source's valid bands in rank order
-    if (tid == 0) {
-        int nb = 0, tot = 0;
-        for (int r = 0; r < J_MAX_BANDS; r++) {
-            for (int b = d.src_off[src]; b < d.src_off[src + 1]; b++) {
-                const BandStats& bs = d.stats[b];
-                if (bs.valid && bs.rank == r) {
-                    jb.n[nb] = bs.n;
-                    jb.off[nb] = tot;
-                    tot += bs.n;
-                    nb++;
-                }
-            }
-        }
-        jb.nb = nb;
-        jb.n_total = tot;
-        s_D = 7 * nb;
-    }
-    __syncthreads();
-    const int nb = jb.nb, D = s_D;
-    if (nb == 0) return;
+    __shared__ int s_task;
+    __shared__ ff s_lo[J_MAX_D], s_hi[J_MAX_D], s_vm[J_MAX_D], s_g[J_MAX_D];
+    __shared__ double s_tpeak;
+    const int DM = d.joint_max_d;
     float4* obs = reinterpret_cast<float4*>(smem_raw);
-    float* xs = reinterpret_cast<float*>(obs + d.joint_max_obs);
-    float* vs = xs + (size_t)D * JP;
-    float* x0s = vs + (size_t)D * JP;
-    float* v0s = x0s + (size_t)D * JP;
-    float* pbs = v0s + (size_t)D * JP;
-    float* gs = pbs + (size_t)D * JP;      // global best, D
-    float* lo = gs + J_MAX_D;              // bounds, D each
-    float* hi = lo + J_MAX_D;
-    // stage the bands' records
-    for (int r = 0; r < nb; r++) {
-        int b_idx = -1;
-        for (int b = d.src_off[src]; b < d.src_off[src + 1]; b++)
-            if (d.stats[b].valid && d.stats[b].rank == r) b_idx = b;
-        const BandStats bs = d.stats[b_idx];
-        for (int i = tid; i < bs.n; i += J_THREADS) obs[jb.off[r] + i] = d.obs[bs.off + i];
-    }
-    // ---- bounds (src/parametric.rs:3860-3882): Villar box with the reference
-    // band's data-informed t0 (no lo < hi check), offsets at +-3 sigma
-    __shared__ float s_tpeak;
-    if (tid < D) {
-        int j = tid % 7;
-        if (tid < 7) { lo[tid] = (float)c_lo[VILLAR][tid]; hi[tid] = (float)c_hi[VILLAR][tid]; }
-        else { lo[tid] = -3.0f * c_rel_sigma[j]; hi[tid] = 3.0f * c_rel_sigma[j]; }
-    }
-    __syncthreads();
-    if (tid == 0) {
-        int b_ref = -1;
-        for (int b = d.src_off[src]; b < d.src_off[src + 1]; b++)
-            if (d.stats[b].valid && d.stats[b].rank == 0) b_ref = b;
-        const BandStats bs = d.stats[b_ref];
-        lo[3] = (float)fmax(bs.t_first - 30.0, c_lo[VILLAR][3]);
-        hi[3] = (float)fmin(bs.t_peak + 10.0, c_hi[VILLAR][3]);
-        s_tpeak = (float)bs.t_peak;
-    }
-    __syncthreads();
-    const float t_peak = s_tpeak;
-    const float* dr = d.joint_draws + (size_t)restart * d.joint_draws_per_seed;
-    const bool seeded = restart == 1;
-    // ---- initialisation (pso_minimize :1677-1692; seeded :1189-1210)
-    if (live) {
-        for (int j = 0; j < D; j++) {
-            float vmax = 0.5f * (hi[j] - lo[j]);
-            float x, v;
-            if (seeded) {
-                if (tid == 0) {
-                    float c;
-                    if (j < 7) c = (float)c_pop_c[VILLAR][j];
-                    else c = c_rel_mean[j % 7];
-                    if (j == 3) c = t_peak - 5.0f;
-                    x = fminf(fmaxf(c, lo[j]), hi[j]);
-                    v = vmax * 0.2f * (2.0f * dr[j] - 1.0f);
-                } else {
-                    int o = D + 2 * D * (tid - 1);
-                    x = lo[j] + dr[o + j] * (hi[j] - lo[j]);
-                    v = vmax * 0.2f * (2.0f * dr[o + D + j] - 1.0f);
-                }
-            } else {
-                int o = 2 * D * tid;
-                x = lo[j] + dr[o + 2 * j] * (hi[j] - lo[j]);
-                v = vmax * 0.2f * (2.0f * dr[o + 2 * j + 1] - 1.0f);
-            }
-            xs[j * JP + tid] = x;
-            vs[j * JP + tid] = v;
-            pbs[j * JP + tid] = x;
-        }
-    }
-    __syncthreads();
-    double c = live ? joint_cost(jb, obs, xs, tid) : INFINITY;
-    double pbc = c;
-    int evals = live ? 1 : 0;
-    // global best after the sequential initial loop: the first strict minimum
-    s_cost[tid] = c;
-    __syncthreads();
-    if (tid == 0) {
-        double gc = INFINITY;
-        int q = -1;
-        for (int k = 0; k < JP; k++)
-            if (s_cost[k] < gc) { gc = s_cost[k]; q = k; }
-        s_gc = gc;
-        s_warp[0] = q;
-    }
-    __syncthreads();
-    {
-        const int q = s_warp[0];
-        if (tid < D) gs[tid] = q >= 0 ? xs[tid * JP + q] : 0.0f;
-    }
-    __syncthreads();
-    const int base = seeded ? 2 * D * JP - D : 2 * D * JP;
-    int stall = 0, it = 0;
-    double prev = s_gc;
-    for (; it < J_MAXIT; it++) {
-        const float w = (float)(0.9 - (0.9 - 0.4) * (double)it / (double)J_MAXIT);
-        if (live)
-            for (int j = 0; j < D; j++) { x0s[j * JP + tid] = xs[j * JP + tid]; v0s[j * JP + tid] = vs[j * JP + tid]; }
+    // the block's slice of the swarm state: high and low halves of the
+    // positions, velocities and personal bests, and the trial positions
+    float* xh = d.joint_state + (size_t)blockIdx.x * JOINT_STATE_ARRAYS * DM * JP;
+    float* xl = xh + (size_t)DM * JP;
+    float* vh = xl + (size_t)DM * JP;
+    float* vl = vh + (size_t)DM * JP;
+    float* pbh = vl + (size_t)DM * JP;
+    float* pl = pbh + (size_t)DM * JP;
+    float* xt = pl + (size_t)DM * JP;
+    const int n_tasks = 3 * d.n_joint;
+    while (true) {
         __syncthreads();
-        int start = 0;
-        while (start < JP) {
-            const bool active = live && tid >= start;
-            if (active) {
-                const float* r = dr + base + (size_t)it * 2 * D * JP + (size_t)2 * D * tid;
-                for (int j = 0; j < D; j++) {
-                    float vmax = 0.5f * (hi[j] - lo[j]);
-                    float x0 = x0s[j * JP + tid], v0 = v0s[j * JP + tid];
-                    float vv = w * v0 + 1.5f * r[2 * j] * (pbs[j * JP + tid] - x0) + 1.5f * r[2 * j + 1] * (gs[j] - x0);
-                    vv = fminf(fmaxf(vv, -vmax), vmax);
-                    float nx = x0 + vv;
-                    if (nx <= lo[j]) { xs[j * JP + tid] = lo[j]; vs[j * JP + tid] = 0.0f; }
-                    else if (nx >= hi[j]) { xs[j * JP + tid] = hi[j]; vs[j * JP + tid] = 0.0f; }
-                    else { xs[j * JP + tid] = nx; vs[j * JP + tid] = vv; }
+        if (tid == 0) s_task = atomicAdd(&d.ctr->joint_head, 1);
+        __syncthreads();
+        const int task = s_task;
+        if (task >= n_tasks) break;
+        const int js = task / 3, restart = task % 3;
+        const int src = d.joint_src[js];
+        // ---- the source's valid bands in rank order
+        if (tid == 0) {
+            int nb = 0, tot = 0;
+            for (int r = 0; r < J_MAX_BANDS; r++) {
+                for (int b = d.src_off[src]; b < d.src_off[src + 1]; b++) {
+                    const BandStats& bs = d.stats[b];
+                    if (bs.valid && bs.rank == r) {
+                        jb.n[nb] = bs.n;
+                        jb.off[nb] = tot;
+                        tot += bs.n;
+                        nb++;
+                    }
                 }
-                c = joint_cost(jb, obs, xs, tid);
-                evals++;
+            }
+            jb.nb = nb;
+            jb.n_total = tot;
+        }
+        __syncthreads();
+        const int nb = jb.nb, D = 7 * nb;
+        if (nb == 0) continue;
+        // stage the bands' records
+        for (int r = 0; r < nb; r++) {
+            int b_idx = -1;
+            for (int b = d.src_off[src]; b < d.src_off[src + 1]; b++)
+                if (d.stats[b].valid && d.stats[b].rank == r) b_idx = b;
+            const BandStats bs = d.stats[b_idx];
+            for (int i = tid; i < bs.n; i += J_THREADS) obs[jb.off[r] + i] = d.obs[bs.off + i];
+        }
+        // ---- bounds in FP64 (src/parametric.rs:3860-3882): Villar box with the
+        // reference band's data-informed t0 (no lo < hi check), offsets at
+        // +-3 sigma of the relative priors; vmax = (hi - lo) / 2
+        if (tid == 0) {
+            int b_ref = -1;
+            for (int b = d.src_off[src]; b < d.src_off[src + 1]; b++)
+                if (d.stats[b].valid && d.stats[b].rank == 0) b_ref = b;
+            const BandStats bs = d.stats[b_ref];
+            s_tpeak = bs.t_peak;
+            for (int j = 0; j < D; j++) {
+                double lo, hi;
+                if (j < 7) {
+                    lo = c_lo[VILLAR][j];
+                    hi = c_hi[VILLAR][j];
+                    if (j == 3) {
+                        lo = fmax(bs.t_first - 30.0, lo);
+                        hi = fmin(bs.t_peak + 10.0, hi);
+                    }
+                } else {
+                    lo = -3.0 * c_rel_sigma64[j % 7];
+                    hi = 3.0 * c_rel_sigma64[j % 7];
+                }
+                s_lo[j] = ff_from(lo);
+                s_hi[j] = ff_from(hi);
+                s_vm[j] = ff_from(__dmul_rn(0.5, __dsub_rn(hi, lo)));
+            }
+        }
+        __syncthreads();
+        const double t_peak = s_tpeak;
+        const double* dr = d.joint_draws64 + (size_t)restart * d.joint_init_per_seed;
+        const float2* d15 = d.joint_draws15 + (size_t)restart * d.joint_draws_per_seed;
+        const bool seeded = restart == 1;
+        // ---- initialisation (pso_minimize :1677-1692; seeded :1189-1210) in
+        // FP64 without contractions; the seed particle (:3884-3895) is the
+        // population prior centre with t0 = t_peak - 5 and the relative
+        // priors' means, clamped to the box
+        if (live) {
+            for (int j = 0; j < D; j++) {
+                const double lo = ff_to(s_lo[j]), hi = ff_to(s_hi[j]), vmax = ff_to(s_vm[j]);
+                double x, v;
+                if (seeded) {
+                    if (tid == 0) {
+                        double c = j < 7 ? c_pop_c[VILLAR][j] : c_rel_mean64[j % 7];
+                        if (j == 3) c = t_peak - 5.0;
+                        x = fmin(fmax(c, lo), hi);
+                        v = __dmul_rn(__dmul_rn(vmax, 0.2), __dsub_rn(2.0 * dr[j], 1.0));
+                    } else {
+                        const int o = D + 2 * D * (tid - 1);
+                        x = __dadd_rn(lo, __dmul_rn(dr[o + j], __dsub_rn(hi, lo)));
+                        v = __dmul_rn(__dmul_rn(vmax, 0.2), __dsub_rn(2.0 * dr[o + D + j], 1.0));
+                    }
+                } else {
+                    const int o = 2 * D * tid;
+                    x = __dadd_rn(lo, __dmul_rn(dr[o + 2 * j], __dsub_rn(hi, lo)));
+                    v = __dmul_rn(__dmul_rn(vmax, 0.2), __dsub_rn(2.0 * dr[o + 2 * j + 1], 1.0));
+                }
+                const ff xf = ff_from(x), vf = ff_from(v);
+                const size_t k = (size_t)j * JP + tid;
+                xh[k] = xf.hi;
+                xl[k] = xf.lo;
+                vh[k] = vf.hi;
+                vl[k] = vf.lo;
+                pbh[k] = xf.hi;
+                pl[k] = xf.lo;
+                xt[k] = xf.hi;
+            }
+        }
+        __syncthreads();
+        double c = live ? joint_cost(jb, obs, xt, tid) : INFINITY;
+        double pbc = c;
+        int evals = live ? 1 : 0;
+        // global best after the sequential initial loop: the first strict
+        // minimum, in particle order
+        {
+            __shared__ double s_min[J_THREADS / 32];
+            double mn = c;
+            for (int k = 16; k; k >>= 1) mn = fmin(mn, __shfl_xor_sync(FULL, mn, k));
+            if ((tid & 31) == 0) s_min[tid >> 5] = mn;
+            __syncthreads();
+            double g = INFINITY;
+            for (int w = 0; w < J_THREADS / 32; w++) g = fmin(g, s_min[w]);
+            const int q = block_first(live && c == g && g < INFINITY, s_warp);
+            if (tid == 0) s_gc = q >= 0 ? g : INFINITY;
+            if (tid < D) s_g[tid] = q >= 0 ? ffm(xh[(size_t)tid * JP + q], xl[(size_t)tid * JP + q]) : ffm(0.0f, 0.0f);
+        }
+        __syncthreads();
+        const int base = seeded ? 2 * D * JP - D : 2 * D * JP;
+        const double inv_iters = 1.0 / (double)J_MAXIT;
+        int stall = 0, it = 0;
+        double prev = s_gc;
+        for (; it < J_MAXIT; it++) {
+            const double wd = __dsub_rn(0.9, __dmul_rn(__dmul_rn(__dsub_rn(0.9, 0.4), (double)it), inv_iters));
+            const ff w = ff_from(wd);
+            const float2* r = d15 + base + (size_t)it * 2 * D * JP + (size_t)2 * D * tid;
+            // the move of this particle from its iteration-start state: trial
+            // (leading floats to xt) or commit (the full state, and the
+            // personal best when `to_pb`).  A plain loop over the dimensions:
+            // unrolling it by band needs ~128 registers, two blocks per SM
+            // instead of four, and measured 20 % slower.
+            auto move = [&](bool commit, bool to_pb) {
+                for (int j = 0; j < D; j++) {
+                    const size_t k = (size_t)j * JP + tid;
+                    ff xn, vn;
+                    ff_move(ffm(xh[k], xl[k]), ffm(vh[k], vl[k]), ffm(pbh[k], pl[k]), s_g[j], w, r[2 * j],
+                            r[2 * j + 1], s_vm[j], s_lo[j], s_hi[j], xn, vn);
+                    if (commit) {
+                        xh[k] = xn.hi;
+                        xl[k] = xn.lo;
+                        vh[k] = vn.hi;
+                        vl[k] = vn.lo;
+                        if (to_pb) {
+                            pbh[k] = xn.hi;
+                            pl[k] = xn.lo;
+                        }
+                    } else {
+                        xt[k] = xn.hi;
+                    }
+                }
+            };
+            int start = 0;
+            while (start < JP) {
+                const bool active = live && tid >= start;
+                if (active) {
+                    move(false, false);
+                    c = joint_cost(jb, obs, xt, tid);
+                    evals++;
+                }
+                const double gc = s_gc;
+                const int q = block_first(active && c < gc, s_warp);
+                const int qe = q < 0 ? JP - 1 : q;
+                if (active && tid <= qe) {
+                    const bool to_pb = c < pbc;
+                    move(true, to_pb);
+                    if (to_pb) pbc = c;
+                }
+                __syncthreads();
+                if (q >= 0) {
+                    if (tid < D) s_g[tid] = ffm(xh[(size_t)tid * JP + q], xl[(size_t)tid * JP + q]);
+                    if (tid == q) s_gc = c;
+                }
+                __syncthreads();
+                start = qe + 1;
             }
             const double gc = s_gc;
-            int q = block_first(active && c < gc, s_warp);
-            const int qe = q < 0 ? JP - 1 : q;
-            if (live && tid >= start && tid <= qe && c < pbc) {
-                pbc = c;
-                for (int j = 0; j < D; j++) pbs[j * JP + tid] = xs[j * JP + tid];
+            if (prev - gc > 0.01 * fmax(fabs(prev), 1e-10)) {
+                stall = 0;
+                prev = gc;
+            } else if (++stall >= J_STALL) {
+                it++;
+                break;
             }
-            if (q >= 0) {
-                if (tid < D) gs[tid] = xs[tid * JP + q];
-                if (tid == q) s_gc = c;
-            }
-            __syncthreads();
-            start = qe + 1;
         }
-        const double gc = s_gc;
-        if (prev - gc > 0.01 * fmax(fabs(prev), 1e-10)) {
-            stall = 0;
-            prev = gc;
-        } else if (++stall >= J_STALL) {
-            it++;
-            break;
-        }
-    }
-    // ---- result
-    int tot = evals;
-    for (int k = 16; k; k >>= 1) tot += __shfl_xor_sync(FULL, tot, k);
-    if ((tid & 31) == 0) s_warp[tid >> 5] = tot;
-    __syncthreads();
-    if (tid == 0) {
-        int all = 0;
-        for (int w = 0; w < J_THREADS / 32; w++) all += s_warp[w];
+        // ---- result
+        int tot = evals;
+        for (int k = 16; k; k >>= 1) tot += __shfl_xor_sync(FULL, tot, k);
+        __syncthreads();
+        if ((tid & 31) == 0) s_warp[tid >> 5] = tot;
+        __syncthreads();
         JointResult& R = d.joint_res[(size_t)js * 3 + restart];
-        R.cost = s_gc;
-        R.iters = it;
-        R.evals = all;
-        atomicAdd(&d.ctr->particle_obs_evals, (unsigned long long)all * (unsigned long long)jb.n_total);
+        if (tid == 0) {
+            int all = 0;
+            for (int w = 0; w < J_THREADS / 32; w++) all += s_warp[w];
+            R.cost = s_gc;
+            R.iters = it;
+            R.evals = all;
+            atomicAdd(&d.ctr->particle_obs_evals, (unsigned long long)all * (unsigned long long)jb.n_total);
+        }
+        if (tid < J_MAX_D) {
+            R.params[tid] = tid < D ? s_g[tid].hi : 0.0f;
+            R.params_lo[tid] = tid < D ? s_g[tid].lo : 0.0f;
+        }
     }
-    if (tid < J_MAX_D) d.joint_res[(size_t)js * 3 + restart].params[tid] = tid < D ? gs[tid] : 0.0f;
 }
 
 // Best of the three restarts; each band (rank k) gets reference + offset k.
@@ -330,14 +405,27 @@ __global__ void joint_pick_kernel(DeviceBatch d) {
         o.pso_cost = best;
         o.per_chi2[VILLAR] = isfinite(best) ? best : NAN;
         for (int j = 0; j < MAXP; j++) {
-            double ref = (double)R[br].params[j];
-            o.pso_params[j] = j < 7 ? (k == 0 ? ref : ref + (double)R[br].params[7 * k + j]) : NAN;
+            if (j >= 7) { o.pso_params[j] = NAN; continue; }
+            const double ref = (double)R[br].params[j] + (double)R[br].params_lo[j];
+            const double off = (double)R[br].params[7 * k + j] + (double)R[br].params_lo[7 * k + j];
+            o.pso_params[j] = k == 0 ? ref : ref + off;
         }
     }
 }
 
 size_t joint_smem_bytes(int max_obs, int max_d) {
-    return (size_t)max_obs * sizeof(float4) + ((size_t)5 * max_d * JP + 3 * J_MAX_D) * sizeof(float);
+    (void)max_d;
+    return (size_t)max_obs * sizeof(float4);
+}
+
+// Blocks of the persistent joint swarm: as many as are resident at once.
+int joint_grid(int max_obs, int max_d, int num_sms) {
+    const size_t smem = joint_smem_bytes(max_obs, max_d);
+    int per_sm = 0;
+    if (cudaFuncSetAttribute(joint_pso_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess ||
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, joint_pso_kernel, J_THREADS, smem) != cudaSuccess)
+        per_sm = 1;
+    return std::max(1, per_sm) * num_sms;
 }
 
 int launch_joint(const DeviceBatch& d, cudaStream_t s) {
@@ -345,7 +433,8 @@ int launch_joint(const DeviceBatch& d, cudaStream_t s) {
     size_t smem = joint_smem_bytes(d.joint_max_obs, d.joint_max_d);
     if (cudaFuncSetAttribute(joint_pso_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
         return -1;
-    joint_pso_kernel<<<d.n_joint * 3, J_THREADS, smem, s>>>(d);
+    const int grid = std::min(d.joint_grid, 3 * d.n_joint);
+    joint_pso_kernel<<<grid, J_THREADS, smem, s>>>(d);
     joint_pick_kernel<<<(d.n_joint + 127) / 128, 128, 0, s>>>(d);
     return 0;
 }

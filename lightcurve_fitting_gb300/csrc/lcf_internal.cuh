@@ -34,6 +34,9 @@ constexpr double SVI_LR = 0.01;
 // 42 joint parameters.
 constexpr int J_MAX_BANDS = 6;
 constexpr int J_MAX_D = 7 * J_MAX_BANDS;
+// Per-particle arrays of the joint swarm's state: position, velocity and
+// personal best as double-float pairs, and the trial position.
+constexpr int JOINT_STATE_ARRAYS = 7;
 
 __host__ __device__ constexpr int n_params_of(int m) {
     return m == BAZIN ? 6 : m == VILLAR ? 7 : m == TDE ? 7 : m == ARNETT ? 5 : m == MAGNETAR ? 5 : m == SHOCK ? 5
@@ -158,13 +161,14 @@ struct PsoResult {
     int32_t iters;
     int32_t evals;
     float params[MB_MAXP];
+    float params_lo[MB_MAXP];
     float pad[2];
 };
-// Parameter j of a swarm result.  The exact-trajectory swarms (models other
-// than MetzgerKN) store each component as a double-float pair, params[j] +
-// params[7 + j], and mark it with pad[0] == 1; the other swarms store FP32.
+// Parameter j of a swarm result.  The exact-trajectory swarms (every swarm
+// but MetzgerKN's) store each component as a double-float pair, params[j] +
+// params_lo[j], and mark it with pad[0] == 1; MetzgerKN's stores FP32.
 __host__ __device__ inline double pso_param(const PsoResult& R, int j) {
-    return (R.pad[0] == 1.0f && j < 7) ? (double)R.params[j] + (double)R.params[7 + j] : (double)R.params[j];
+    return R.pad[0] == 1.0f ? (double)R.params[j] + (double)R.params_lo[j] : (double)R.params[j];
 }
 
 // Result of one joint multi-band swarm run (one source, one restart).
@@ -172,7 +176,8 @@ struct JointResult {
     double cost;
     int32_t iters;
     int32_t evals;
-    float params[J_MAX_D];
+    float params[J_MAX_D];     // the best position as double-float pairs,
+    float params_lo[J_MAX_D];  // params[j] + params_lo[j]
 };
 
 // Per (band, model) polished fit.
@@ -225,7 +230,7 @@ struct Counters {
     int32_t lb_next[8];         // per model: next index of the polish queue (eight lanes a band)
     int32_t lb_next_long[8];    // per model: next index of its long bands (a warp a band)
     int32_t error;              // first error code raised on the device
-    int32_t pad;
+    int32_t joint_head;         // next (source, restart) task of the joint multi-band swarm
 };
 
 struct DeviceBatch {
@@ -288,8 +293,12 @@ struct DeviceBatch {
     const int32_t* joint_src;    // the jointly fitted sources
     int n_joint;
     JointResult* joint_res;      // [n_joint][3]
-    const float* joint_draws;    // [3][joint_draws_per_seed] uniforms of seeds 42, 137, 271
+    const float2* joint_draws15;  // [3][joint_draws_per_seed] 1.5 u of seeds 42, 137, 271 as double-float
+    const double* joint_draws64;  // [3][joint_init_per_seed] the first uniforms (initialisation) in FP64
     int64_t joint_draws_per_seed;
+    int64_t joint_init_per_seed;
+    float* joint_state;          // [joint_grid][JOINT_STATE_ARRAYS][joint_max_d][200] swarm state
+    int joint_grid;              // blocks of the persistent joint swarm
     int joint_max_obs;           // most observations of a joint source
     int joint_max_d;             // most joint parameters of a joint source
 };
@@ -309,9 +318,10 @@ void launch_pso(const DeviceBatch& d, int slot, const PsoTask* tasks, int n_host
 // d.task_sorted_mb for the MultiBazin branch): MetzgerKN first, then by
 // kind, longest bands first within a kind.
 void launch_task_sort(const DeviceBatch& d, int slot, PsoTask* out, cudaStream_t s);
-size_t pso_smem_bytes(int block, int smem_obs);
+size_t pso_smem_bytes(int block, int smem_obs, int max_dim = 7);
 int pso_blocks_per_sm(int block, size_t smem, int minb);
-int pso_init_attributes(int block, int smem_obs);
+int pso_init_attributes(const int* blocks, const int* smem_obs, int n);
+int pso_stage_obs(int block, int smem_obs, int max_dim);
 void launch_t0_build(const DeviceBatch& d, int slot, int fine, cudaStream_t s);
 void launch_t0_pick(const DeviceBatch& d, int slot, int fine, cudaStream_t s);
 void launch_gate_build(const DeviceBatch& d, int slot, cudaStream_t s);
@@ -356,6 +366,7 @@ void launch_band_cost(int model, const float4* obs, int n, float t_last, const d
 
 // Host-side generation of the RNG tables (host.cpp)
 void make_draw_tables(float* draws, double* draws64, float2* draws15, double* svi_eps);
-void make_joint_draws(float* draws, int64_t per_seed);
+void make_joint_draws(float2* draws15, double* draws64, int64_t per_seed, int64_t init_per_seed);
+int joint_grid(int max_obs, int max_d, int num_sms);
 
 }  // namespace lcf

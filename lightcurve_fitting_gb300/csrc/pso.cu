@@ -21,6 +21,8 @@
 // view of the reference's sequence.
 #include <cuda_runtime.h>
 
+#include <algorithm>
+
 #include "lane_cost.cuh"
 #include "lcf_internal.cuh"
 #include "models_f32.cuh"
@@ -246,6 +248,24 @@ struct WarpSmem {
     // stay in registers): [state][dimension][lane], state = position,
     // velocity, personal best, position and velocity at the iteration start
     float lo_state[5][7][32];
+};
+// The MultiBazin instantiations (swarm dimensions 4K + 2 = 10, 14, 18): the
+// same, with three state planes (position, velocity, personal best; the
+// MultiBazin swarm recomputes a move instead of keeping its start state).
+template <int MAXD>
+struct WarpSmemMB {
+    uint64_t bar;
+    uint64_t pad;
+    ff lo[MAXD], hi[MAXD], vmax[MAXD], g[MAXD];
+    float lo_state[3][MAXD][32];
+};
+template <int MAXD>
+struct WarpSmemOf {
+    using type = WarpSmemMB<MAXD>;
+};
+template <>
+struct WarpSmemOf<7> {
+    using type = WarpSmem;
 };
 
 // One swarm run (pso_minimize / pso_minimize_seeded, src/parametric.rs:1646-1757,
@@ -488,8 +508,6 @@ __device__ __forceinline__ void run_swarm(const DeviceBatch& d, const PsoTask& t
 //     polish's double-float cost, LaneLb) for the picks, and the polish
 //     settles the model-selection restarts on accurate costs.
 // ---------------------------------------------------------------------------
-__device__ __forceinline__ bool ff_lt(ff a, ff b) { return a.hi < b.hi || (a.hi == b.hi && a.lo < b.lo); }
-__device__ __forceinline__ bool ff_le(ff a, ff b) { return a.hi < b.hi || (a.hi == b.hi && a.lo <= b.lo); }
 
 // Accurate cost of the double-float position pos[0..6] (every lane passes
 // the same position): component j of the full parameter vector in lane j,
@@ -703,20 +721,11 @@ __device__ __forceinline__ void run_swarm_exact(const DeviceBatch& d, const PsoT
 #pragma unroll
                 for (int k = 0; k < MAXD; k++) {
                     if (k < D) {
-                        const float2 a1 = r15[2 * k], a2 = r15[2 * k + 1];
                         const ff x0 = ffm(x0h[k], X0L[32 * k]), v0 = ffm(v0h[k], V0L[32 * k]);
                         const ff pbk = ffm(pbh[k], PL[32 * k]);
-                        ff vv = ff_add(ff_add(ff_mul(w, v0), ff_mul(ffm(a1.x, a1.y), ff_sub(pbk, x0))),
-                                       ff_mul(ffm(a2.x, a2.y), ff_sub(ws->g[k], x0)));
-                        const ff vm = ws->vmax[k];
-                        if (ff_lt(vv, ff_neg(vm))) vv = ff_neg(vm);
-                        if (ff_lt(vm, vv)) vv = vm;
-                        const ff nx = ff_add(x0, vv);
-                        const ff lo = ws->lo[k], hi = ws->hi[k];
                         ff xn, vn;
-                        if (ff_le(nx, lo)) { xn = lo; vn = ffm(0.0f, 0.0f); }
-                        else if (ff_le(hi, nx)) { xn = hi; vn = ffm(0.0f, 0.0f); }
-                        else { xn = nx; vn = vv; }
+                        ff_move(x0, v0, pbk, ws->g[k], w, r15[2 * k], r15[2 * k + 1], ws->vmax[k], ws->lo[k],
+                                ws->hi[k], xn, vn);
                         xh[k] = xn.hi;
                         XL[32 * k] = xn.lo;
                         vh[k] = vn.hi;
@@ -776,13 +785,226 @@ __device__ __forceinline__ void run_swarm_exact(const DeviceBatch& d, const PsoT
         R.cost = rc;
         R.iters = it;
         R.evals = tot_evals;
-        for (int j = 0; j < MB_MAXP; j++) R.params[j] = 0.0f;
+        for (int j = 0; j < MB_MAXP; j++) R.params[j] = R.params_lo[j] = 0.0f;
 #pragma unroll
         for (int k = 0; k < MAXD; k++)
             if (k < D) {
                 R.params[k] = ws->g[k].hi;
-                R.params[7 + k] = ws->g[k].lo;
+                R.params_lo[k] = ws->g[k].lo;
             }
+        R.pad[0] = 1.0f;
+        atomicAdd(&d.ctr->particle_obs_evals, (unsigned long long)tot_evals * (unsigned long long)bs.n);
+        if (slot == 0) {
+            atomicAdd(&d.ctr->slot0_evals[KIND], (unsigned long long)tot_evals * (unsigned long long)bs.n);
+            atomicAdd(&d.ctr->slot0_particles[KIND], (unsigned long long)tot_evals);
+        }
+    }
+    __syncwarp();
+}
+
+// ---------------------------------------------------------------------------
+// Exact-trajectory MultiBazin swarms (fit_multi_bazin's pso_minimize runs,
+// src/parametric.rs:1008-1157).  With a 30-particle, 60-iteration swarm and
+// no polish after it, the reference's K and costs are its swarm's end points:
+// rounding only the swarm positions to FP32 in the FP64 restatement changes
+// K for 3 of the 30 real ZTF sources and 4 of 200 uneven synthetic ones.  So
+// these swarms follow the reference's trajectory in double-float as the
+// model-selection swarms do, with one difference in the state kept: a lane's
+// position, velocity and personal best are double-float (high halves in
+// registers, low halves in shared memory, st[plane][dimension][lane]), and
+// the iteration-start state is not copied.  A trial move is evaluated at its
+// leading float and dropped; the lanes accepted in a round recompute the
+// same move (same inputs, the global best not yet updated, so the same bits)
+// and commit it, and lanes not yet accepted still hold the iteration start.
+// One extra move per particle and iteration; 18 dimensions need 7.5 KB of
+// shared memory a warp instead of 12.1 KB.
+// ---------------------------------------------------------------------------
+template <int MAXD, int KIND>
+__device__ __forceinline__ void run_swarm_exact_mb(const DeviceBatch& d, const PsoTask& task, const BandStats& bs,
+                                                   TaskCtx& t, ff* s_lo, ff* s_hi, ff* s_vm, ff* s_g, float* st,
+                                                   int slot) {
+    constexpr int K = KIND - KIND_MB1 + 1, D = 4 * K + 2;
+    static_assert(D <= MAXD, "MultiBazin swarm wider than the instantiation");
+    const int lane = threadIdx.x & 31;
+    const int p = lane;
+    const bool live = p < NP;
+    const bool seeded = (task.flags & TASK_SEEDED) != 0;
+    t.model = BAZIN;
+    t.np = D;
+    t.D = D;
+    t.t0i = -1;
+    float* XL = st + lane;
+    float* VL = st + 32 * MAXD + lane;
+    float* PL = st + 64 * MAXD + lane;
+    // the box in FP64 (multi_bazin_bounds, src/parametric.rs:958-970)
+    double blo[D], bhi[D], vmaxd[D];
+#pragma unroll
+    for (int c = 0; c < K; c++) {
+        blo[4 * c] = -3.0; bhi[4 * c] = 3.0;
+        blo[4 * c + 1] = bs.t_first - 30.0; bhi[4 * c + 1] = bs.t_last + 30.0;
+        blo[4 * c + 2] = -2.0; bhi[4 * c + 2] = 5.0;
+        blo[4 * c + 3] = -2.0; bhi[4 * c + 3] = 6.0;
+    }
+    blo[4 * K] = -0.3; bhi[4 * K] = 0.3;
+    blo[4 * K + 1] = -5.0; bhi[4 * K + 1] = 0.0;
+#pragma unroll
+    for (int k = 0; k < D; k++) vmaxd[k] = __dmul_rn(0.5, __dsub_rn(bhi[k], blo[k]));
+    __syncwarp();
+    if (lane == 0) {
+#pragma unroll
+        for (int k = 0; k < D; k++) {
+            s_lo[k] = ff_from(blo[k]);
+            s_hi[k] = ff_from(bhi[k]);
+            s_vm[k] = ff_from(vmaxd[k]);
+            s_g[k] = ffm(0.0f, 0.0f);
+        }
+    }
+    // ---- initialisation (src/parametric.rs:1677-1692, seeded :1189-1210) in
+    // FP64 as the reference, without contractions; the seed particle is the
+    // K - 1 fit extended at the largest residual (mb_build_kernel)
+    const double* dr = d.draws64 + (size_t)task.restart * DRAWS_PER_SEED;
+    const float2* d15 = d.draws15 + (size_t)task.restart * DRAWS_PER_SEED;
+    const double* seed = (seeded && task.aux >= 0) ? d.mb[task.aux].seed : nullptr;
+    float xh[D], vh[D], pbh[D], xt[D];
+#pragma unroll
+    for (int k = 0; k < D; k++) {
+        double xi = 0.0, vi = 0.0;
+        if (seeded) {
+            if (p == 0) {
+                xi = seed ? seed[k] : 0.0;
+                vi = __dmul_rn(__dmul_rn(vmaxd[k], 0.2), __dsub_rn(2.0 * dr[k], 1.0));
+            } else if (live) {
+                const int o = D + 2 * D * (p - 1);
+                xi = __dadd_rn(blo[k], __dmul_rn(dr[o + k], __dsub_rn(bhi[k], blo[k])));
+                vi = __dmul_rn(__dmul_rn(vmaxd[k], 0.2), __dsub_rn(2.0 * dr[o + D + k], 1.0));
+            }
+        } else if (live) {
+            const int o = 2 * D * p;
+            xi = __dadd_rn(blo[k], __dmul_rn(dr[o + 2 * k], __dsub_rn(bhi[k], blo[k])));
+            vi = __dmul_rn(__dmul_rn(vmaxd[k], 0.2), __dsub_rn(2.0 * dr[o + 2 * k + 1], 1.0));
+        }
+        const ff xf = ff_from(xi), vf = ff_from(vi);
+        xh[k] = xf.hi;
+        XL[32 * k] = xf.lo;
+        vh[k] = vf.hi;
+        VL[32 * k] = vf.lo;
+        pbh[k] = xf.hi;
+        PL[32 * k] = xf.lo;
+        xt[k] = xf.hi;
+    }
+    const int base = seeded ? 2 * D * NP - D : 2 * D * NP;
+    __syncwarp();
+    // one evaluation round over lanes start .. NP - 1 at the trial positions
+    auto eval_round = [&](int start) -> double {
+        const int kk = NP - start;
+        const double cs = particle_cost_split<KIND>(t, xt, start, kk);
+        const double co = __shfl_sync(FULL, cs, ((p - start) * split_lanes(kk)) & 31);
+        return (live && p >= start) ? co : INFINITY;
+    };
+    auto set_gbest = [&](int q) {
+        ff gq[D];
+#pragma unroll
+        for (int k = 0; k < D; k++) gq[k] = ffm(__shfl_sync(FULL, xh[k], q), __shfl_sync(FULL, XL[32 * k], q));
+        __syncwarp();
+        if (lane == 0) {
+#pragma unroll
+            for (int k = 0; k < D; k++) s_g[k] = gq[k];
+        }
+        __syncwarp();
+    };
+    double c = eval_round(0);
+    int evals = 1;
+    double pbc = c;
+    double gc = INFINITY;
+    {
+        double mn = c;
+        for (int k = 16; k; k >>= 1) mn = fmin(mn, __shfl_xor_sync(FULL, mn, k));
+        const unsigned mm = __ballot_sync(FULL, live && c == mn && mn < INFINITY);
+        if (mm) {
+            gc = mn;
+            set_gbest(__ffs(mm) - 1);
+        }
+    }
+    // ---- iterations (src/parametric.rs:1694-1755)
+    int stall = 0;
+    double prev = gc;
+    const double inv_iters = 1.0 / (double)MAX_ITERS;
+    int it = 0;
+    for (; it < MAX_ITERS; it++) {
+        const double wd = __dsub_rn(0.9, __dmul_rn(__dmul_rn(__dsub_rn(0.9, 0.4), (double)it), inv_iters));
+        const ff w = ff_from(wd);
+        const float2* r15 = d15 + base + it * 2 * D * NP + 2 * D * p;
+        // the move from the iteration-start state against the current global
+        // best: trial (leading floats to xt) or commit (the full state)
+        auto move = [&](bool commit) {
+#pragma unroll
+            for (int k = 0; k < D; k++) {
+                ff xn, vn;
+                ff_move(ffm(xh[k], XL[32 * k]), ffm(vh[k], VL[32 * k]), ffm(pbh[k], PL[32 * k]), s_g[k], w,
+                        r15[2 * k], r15[2 * k + 1], s_vm[k], s_lo[k], s_hi[k], xn, vn);
+                if (commit) {
+                    xh[k] = xn.hi;
+                    XL[32 * k] = xn.lo;
+                    vh[k] = vn.hi;
+                    VL[32 * k] = vn.lo;
+                } else {
+                    xt[k] = xn.hi;
+                }
+            }
+        };
+        int start = 0;
+        while (start < NP) {
+            const bool active = live && p >= start;
+            if (active) move(false);
+            {
+                const double cr = eval_round(start);
+                if (active) {
+                    c = cr;
+                    evals++;
+                }
+            }
+            const unsigned mq = __ballot_sync(FULL, active && c < gc);
+            const int q = mq ? __ffs(mq) - 1 : NP - 1;
+            if (active && p <= q) {
+                move(true);
+                if (c < pbc) {
+                    pbc = c;
+#pragma unroll
+                    for (int k = 0; k < D; k++) {
+                        pbh[k] = xh[k];
+                        PL[32 * k] = XL[32 * k];
+                    }
+                }
+            }
+            __syncwarp();
+            if (mq) {
+                gc = __shfl_sync(FULL, c, q);
+                set_gbest(q);
+            }
+            start = q + 1;
+        }
+        bool improved = prev - gc > 0.01 * fmax(fabs(prev), 1e-10);
+        if (improved) {
+            stall = 0;
+            prev = gc;
+        } else if (++stall >= STALL_ITERS) {
+            it++;
+            break;
+        }
+    }
+    int tot_evals = live ? evals : 0;
+    for (int k = 16; k; k >>= 1) tot_evals += __shfl_xor_sync(FULL, tot_evals, k);
+    if (lane == 0) {
+        PsoResult& R = d.pso_res[task.out];
+        R.cost = gc;
+        R.iters = it;
+        R.evals = tot_evals;
+        for (int j = 0; j < MB_MAXP; j++) R.params[j] = R.params_lo[j] = 0.0f;
+#pragma unroll
+        for (int k = 0; k < D; k++) {
+            R.params[k] = s_g[k].hi;
+            R.params_lo[k] = s_g[k].lo;
+        }
         R.pad[0] = 1.0f;
         atomicAdd(&d.ctr->particle_obs_evals, (unsigned long long)tot_evals * (unsigned long long)bs.n);
         if (slot == 0) {
@@ -808,7 +1030,8 @@ __global__ void __launch_bounds__(256, MINB)
     const int warp = threadIdx.x >> 5;
     const int nwarps = blockDim.x >> 5;
     float4* sobs = reinterpret_cast<float4*>(smem_raw) + (size_t)warp * smem_obs;
-    WarpSmem* ws = reinterpret_cast<WarpSmem*>(reinterpret_cast<float4*>(smem_raw) + (size_t)nwarps * smem_obs) + warp;
+    using WS = typename WarpSmemOf<MAXD>::type;
+    WS* ws = reinterpret_cast<WS*>(reinterpret_cast<float4*>(smem_raw) + (size_t)nwarps * smem_obs) + warp;
     if (lane == 0) mbar_init(&ws->bar);
     __syncwarp();
     uint32_t phase = 0;
@@ -859,7 +1082,9 @@ __global__ void __launch_bounds__(256, MINB)
         // (the queue is grouped by kind) run one kind's code
         if constexpr (MAXD != 7) {
             constexpr int KMB = KIND_MB1 + (MAXD - 2) / 4 - 1;  // D = 4K + 2
-            if (task.kind == KMB) run_swarm<MAXD, KMB>(d, task, bs, t, slot, gwarp);
+            if (task.kind == KMB)
+                run_swarm_exact_mb<MAXD, KMB>(d, task, bs, t, ws->lo, ws->hi, ws->vmax, ws->g, &ws->lo_state[0][0][0],
+                                              slot);
         } else switch (task.kind) {
             case BAZIN: run_swarm_exact<BAZIN>(d, task, bs, t, ws, slot); break;
             case VILLAR: run_swarm_exact<VILLAR>(d, task, bs, t, ws, slot); break;
@@ -869,7 +1094,10 @@ __global__ void __launch_bounds__(256, MINB)
             case SHOCK: run_swarm_exact<SHOCK>(d, task, bs, t, ws, slot); break;
             case AFTERGLOW: run_swarm_exact<AFTERGLOW>(d, task, bs, t, ws, slot); break;
             case METZGER: run_swarm<MAXD, METZGER>(d, task, bs, t, slot, gwarp); break;
-            case KIND_MB1: run_swarm<MAXD, KIND_MB1>(d, task, bs, t, slot, gwarp); break;
+            case KIND_MB1:
+                run_swarm_exact_mb<MAXD, KIND_MB1>(d, task, bs, t, ws->lo, ws->hi, ws->vmax, ws->g,
+                                                   &ws->lo_state[0][0][0], slot);
+                break;
             default: break;
         }
         __syncwarp();
@@ -929,18 +1157,44 @@ static double time_probe(void (*k)(float*, int), int num_sms, int iters) {
 double probe_fp32_tflops(int num_sms) { return 2.0 * time_probe(probe_fma_kernel, num_sms, 1 << 16) * 1e-12; }
 double probe_mufu_gops(int num_sms) { return time_probe(probe_ex2_kernel, num_sms, 1 << 14) * 1e-9; }
 
-size_t pso_smem_bytes(int block, int smem_obs) {
-    return (size_t)(block / 32) * ((size_t)smem_obs * sizeof(float4) + sizeof(WarpSmem));
+static size_t warp_smem_bytes(int max_dim) {
+    return max_dim <= 7 ? sizeof(WarpSmem) : max_dim <= 10 ? sizeof(WarpSmemMB<10>)
+         : max_dim <= 14 ? sizeof(WarpSmemMB<14>) : sizeof(WarpSmemMB<18>);
 }
 
-int pso_init_attributes(int block, int smem_obs) {
-    int smem = (int)pso_smem_bytes(block, smem_obs);
+// Observations a warp stages in shared memory: smem_obs, except in the
+// MultiBazin instantiations, whose larger swarm state would otherwise leave
+// room for one block per SM; there as many (a multiple of 32) as keep two
+// blocks of `block` threads within 220 KB.  Longer bands are read from
+// global memory, with the same values.
+int pso_stage_obs(int block, int smem_obs, int max_dim) {
+    if (max_dim <= 7) return smem_obs;
+    const size_t per_warp = (size_t)110 * 1024 / (size_t)(block / 32);
+    const size_t ws = warp_smem_bytes(max_dim);
+    int n = per_warp > ws ? (int)((per_warp - ws) / sizeof(float4)) : 0;
+    n &= ~31;
+    return std::max(32, std::min(smem_obs, n));
+}
+
+size_t pso_smem_bytes(int block, int smem_obs, int max_dim) {
+    const int so = pso_stage_obs(block, smem_obs, max_dim);
+    return (size_t)(block / 32) * ((size_t)so * sizeof(float4) + warp_smem_bytes(max_dim));
+}
+
+int pso_init_attributes(const int* blocks, const int* smem_obs, int n) {
+    size_t m7 = 0, m10 = 0, m14 = 0, m18 = 0;
+    for (int c = 0; c < n; c++) {
+        m7 = std::max(m7, pso_smem_bytes(blocks[c], smem_obs[c], 7));
+        m10 = std::max(m10, pso_smem_bytes(blocks[c], smem_obs[c], 10));
+        m14 = std::max(m14, pso_smem_bytes(blocks[c], smem_obs[c], 14));
+        m18 = std::max(m18, pso_smem_bytes(blocks[c], smem_obs[c], 18));
+    }
     const cudaFuncAttribute a = cudaFuncAttributeMaxDynamicSharedMemorySize;
-    cudaError_t e = cudaFuncSetAttribute(pso_kernel<7, 2>, a, smem);
-    if (e == cudaSuccess) e = cudaFuncSetAttribute(pso_kernel<7, 3>, a, smem);
-    if (e == cudaSuccess) e = cudaFuncSetAttribute(pso_kernel<10, 2>, a, smem);
-    if (e == cudaSuccess) e = cudaFuncSetAttribute(pso_kernel<14, 2>, a, smem);
-    if (e == cudaSuccess) e = cudaFuncSetAttribute(pso_kernel<18, 2>, a, smem);
+    cudaError_t e = cudaFuncSetAttribute(pso_kernel<7, 2>, a, (int)m7);
+    if (e == cudaSuccess) e = cudaFuncSetAttribute(pso_kernel<7, 3>, a, (int)m7);
+    if (e == cudaSuccess) e = cudaFuncSetAttribute(pso_kernel<10, 2>, a, (int)m10);
+    if (e == cudaSuccess) e = cudaFuncSetAttribute(pso_kernel<14, 2>, a, (int)m14);
+    if (e == cudaSuccess) e = cudaFuncSetAttribute(pso_kernel<18, 2>, a, (int)m18);
     return (int)e;
 }
 
@@ -954,8 +1208,8 @@ int pso_blocks_per_sm(int block, size_t smem, int minb) {
 void launch_pso(const DeviceBatch& d, int slot, const PsoTask* tasks, int n_host, int max_dim, int grid, int block,
                 cudaStream_t s, int minb) {
     if (n_host == 0) return;
-    int smem_obs = d.smem_obs;
-    size_t smem = pso_smem_bytes(block, smem_obs);
+    const int smem_obs = pso_stage_obs(block, d.smem_obs, max_dim);
+    const size_t smem = pso_smem_bytes(block, d.smem_obs, max_dim);
     if (max_dim <= 7 && minb == 3) pso_kernel<7, 3><<<grid, block, smem, s>>>(d, slot, tasks, n_host, smem_obs);
     else if (max_dim <= 7) pso_kernel<7, 2><<<grid, block, smem, s>>>(d, slot, tasks, n_host, smem_obs);
     else if (max_dim <= 10) pso_kernel<10, 2><<<grid, block, smem, s>>>(d, slot, tasks, n_host, smem_obs);

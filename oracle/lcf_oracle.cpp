@@ -547,11 +547,11 @@ static bool prepare_band(const double* times, const double* flux, const double* 
 // PsoCost, src/parametric.rs:1285-1446
 // ---------------------------------------------------------------------------
 // Test hook: a deterministic relative perturbation of every swarm / polish
-// cost (PsoCost and the MultiBazin cost), +-rel by a hash of the parameter
-// vector (and `salt`, which picks another sign pattern).  With rel ~1e-7 it
-// stands in for FP32 rounding of the costs, so
-// the tests can measure how far the reference's own results move under it.
-// 0 (the default) leaves the arithmetic untouched.
+// cost (PsoCost, the MultiBazin cost and the joint multi-band cost), +-rel by
+// a hash of the parameter vector (and `salt`, which picks another sign
+// pattern).  With rel ~1e-7 to 1e-6 it stands in for FP32 rounding of the
+// costs, so the tests can measure how far the reference's own results move
+// under it.  0 (the default) leaves the arithmetic untouched.
 static double g_cost_rel = 0.0, g_grad_rel = 0.0;
 static uint64_t g_cost_salt = 0;
 static inline uint64_t perturb_hash(const double* p, int np, uint64_t extra) {
@@ -1840,7 +1840,7 @@ struct JointCost {
                     neg_lp += 0.5 * z * z;
                 }
             }
-        return (balanced + neg_lp) / nt;
+        return perturb_cost((balanced + neg_lp) / nt, p, NPV * nb);
     }
 };
 

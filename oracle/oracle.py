@@ -332,7 +332,7 @@ def set_laplace_step(step: float = 1e-4) -> None:
 
 
 def set_cost_perturbation(rel: float, salt: int = 0, grad_rel: float = 0.0) -> None:
-    """Perturb every swarm / polish / MultiBazin cost of the oracle by +-rel
+    """Perturb every swarm / polish / MultiBazin / joint multi-band cost of the oracle by +-rel
     and each polish gradient component by +-grad_rel (a hash of the parameter
     vector, the component and `salt` picks the signs); 0 restores the exact
     arithmetic.  A test hook: it measures how far the reference's own results

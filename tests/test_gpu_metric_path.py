@@ -38,13 +38,17 @@ therefore stated against the oracle itself:
   * posterior means within 0.1 posterior sigma at least as often as the
     perturbed oracle's (less 2 points) and for >= 90 % of the bands;
   * MultiBazin: the same K for >= 98 % of rank-0 bands, and the cost of that K
-    within 1e-4 for >= 95 % of them (its swarms, unlike the other models',
-    move FP32 positions; measured 99 % / 97 %).
+    within 1e-4 for >= 95 % of them (measured 99 % / 97 %).  Its swarms end
+    the fit (no polish), on the reference's trajectory in double-float with
+    FP32 cost comparisons; the reference's own K and costs move as much
+    under cost perturbations of 1e-6 to 1e-5, the FP32 evaluation's level.
 """
 import numpy as np
 import pytest
 
 from lightcurve_fitting_gb300 import abi, synth
+
+from criteria import PERTURBATIONS, perturbed as _perturbed, selection_check, within as _within
 
 pytestmark = pytest.mark.gpu
 
@@ -60,63 +64,6 @@ def ctx():
     c = Context(0)
     yield c
     c.close()
-
-
-# (cost, salt, gradient) relative perturbations of the oracle
-PERTURBATIONS = [(1e-7, 0, 0.0), (1e-7, 1, 0.0), (1e-9, 2, 0.0), (0.0, 3, 1e-12), (0.0, 4, 1e-14)]
-
-
-def _perturbed(oracle, batch, rel, salt=0, grad_rel=0.0, **kw):
-    oracle.set_cost_perturbation(rel, salt, grad_rel)
-    try:
-        return oracle.fit_batch(batch, **kw)
-    finally:
-        oracle.set_cost_perturbation(0.0)
-
-
-def _bic(r, b, m):
-    n = r.n_obs[b]
-    return 2.0 * r.per_model_chi2[b, m] * n + abi.N_PARAMS[m] * np.log(n)
-
-
-def _tie(r, b, m1, m2):
-    gap = abs(_bic(r, b, m1) - _bic(r, b, m2))
-    return gap <= 1e-3 * abs(_bic(r, b, m2)) + 1e-9
-
-
-def _moved(pr, ref, b, m):
-    return abs(pr.per_model_chi2[b, m] - ref.per_model_chi2[b, m]) > 1e-4 * max(abs(ref.per_model_chi2[b, m]), 1e-12)
-
-
-def selection_check(res, ref, perts):
-    """(agreement, floor, bad, n, n_orc): floor = min(0.99, the lowest
-    agreement of a perturbed oracle with the oracle); bad lists the
-    disagreements that are neither near ties, nor at bands where a perturbed
-    oracle moves, nor at bands where the GPU's polish of one of the two models
-    ended elsewhere; n counts the disagreements that are not near ties, n_orc
-    the most such disagreements of a perturbed oracle with the oracle."""
-    fitted = ref.model >= 0
-    assert np.array_equal(res.model >= 0, fitted)
-    assert np.array_equal(res.rank, ref.rank)
-    agree = res.model[fitted] == ref.model[fitted]
-    bad, n = [], 0
-    for b in np.flatnonzero(fitted)[~agree]:
-        mg, mo = int(res.model[b]), int(ref.model[b])
-        if _tie(ref, b, mg, mo):
-            continue
-        n += 1
-        unstable = any(pr.model[b] != mo or _moved(pr, ref, b, mg) or _moved(pr, ref, b, mo) for pr in perts)
-        elsewhere = _moved(res, ref, b, mg) or _moved(res, ref, b, mo)
-        if not (unstable or elsewhere):
-            bad.append((int(b), mo, mg))
-    n_orc = max(int(sum(1 for b in np.flatnonzero(fitted) if pr.model[b] != ref.model[b]
-                        and not _tie(ref, b, int(pr.model[b]), int(ref.model[b])))) for pr in perts)
-    floor = min([0.99] + [float(np.mean(pr.model[fitted] == ref.model[fitted])) for pr in perts])
-    return float(agree.mean()), floor, bad, n, n_orc
-
-
-def _within(a, b, tol):
-    return np.abs(a - b) <= tol * np.maximum(np.abs(b), 1e-12)
 
 
 def test_metric_path_matches_oracle(ctx, oracle):

@@ -1,0 +1,93 @@
+"""The fit on the reference's 30 real ZTF sources (tests/fixtures/
+real_sources.json after build_flux_bands, src/common.rs:79-111: 83 bands of
+3 to 1,005 points, SN Ia/Ib/Ic/II/IIP/IIn/IIb, cataclysmic variables, AGN
+and TDEs), through the C ABI against the FP64 oracle.  Real light curves are
+gappy, sparse on the rise and fitted by none of the models exactly, unlike
+the synthetic workloads; the criteria are the synthetic workloads' own,
+stated against the oracle's sensitivity to rounding-sized perturbations
+(criteria.py), with counts rounded to whole bands at this size:
+  * the metric's path (all models, SVI, MultiBazin): fitted bands and ranks
+    identical; the selection rule of the synthetic metric-path test; the
+    reported cost median within 1e-9; posterior means within 0.1 posterior
+    sigma for >= 90 % of the bands selecting the oracle's model; the
+    MultiBazin K of the 30 rank-0 bands identical, its cost within 1e-6
+    (measured 1.4e-7 at most), and >= 95 % of the per-K costs within 1e-4;
+  * Laplace: the same selection rule, and the polished cost of every
+    (band, model) pair to a median 1e-9;
+  * the joint multi-band Villar branch (fit_all_models = false): the joint
+    cost the GPU reports is the oracle's FP64 joint cost at the GPU's vector
+    (1e-6), the search agrees with the oracle's to a median 1e-6, and no more
+    sources depart from it by 1e-4 than the oracle perturbed at 1e-6 (the
+    FP32 cost level) departs from itself (criteria.check_joint).
+"""
+import numpy as np
+import pytest
+
+from lightcurve_fitting_gb300 import abi
+
+import real_sources
+from criteria import PERTURBATIONS, check_joint, perturbed, selection_check, within
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def ctx():
+    import torch
+    if not torch.cuda.is_available():
+        pytest.skip("no GPU")
+    from lightcurve_fitting_gb300 import build
+    build.build()
+    from lightcurve_fitting_gb300.lib import Context
+    c = Context(0)
+    yield c
+    c.close()
+
+
+@pytest.fixture(scope="module")
+def batch():
+    return real_sources.batch()
+
+
+def test_real_sources_metric_path_match_oracle(ctx, oracle, batch):
+    kw = dict(fit_all_models=True, method=abi.METHOD_SVI, run_multi_bazin=True)
+    res = ctx.fit_batch(batch, **kw)
+    ref = oracle.fit_batch(batch, **kw)
+    perts = [perturbed(oracle, batch, *p, **kw) for p in PERTURBATIONS]
+    frac, floor, bad, n, n_orc = selection_check(res, ref, perts)
+    assert frac >= floor and not bad and n <= max(n_orc, 1), (frac, floor, bad, n, n_orc)
+    same = (ref.model >= 0) & (res.model == ref.model)
+    rel = np.abs(res.pso_chi2[same] - ref.pso_chi2[same]) / np.maximum(np.abs(ref.pso_chi2[same]), 1e-12)
+    assert np.median(rel) < 1e-9, np.median(rel)
+    z = []
+    for b in np.flatnonzero(same):
+        k = abi.N_PARAMS[ref.model[b]]
+        z.append(np.max(np.abs(res.svi_mu[b, :k] - ref.svi_mu[b, :k]) / np.exp(ref.svi_log_sigma[b, :k])))
+    assert np.mean(np.array(z) < 0.1) >= 0.9, sorted(z)[-10:]
+    r0 = ref.rank == 0
+    assert r0.sum() == batch.n_sources and np.all(ref.mb_best_k[r0] >= 1)
+    assert np.array_equal(res.mb_best_k[r0], ref.mb_best_k[r0]), (res.mb_best_k[r0], ref.mb_best_k[r0])
+    assert within(res.mb_cost[r0], ref.mb_cost[r0], 1e-6).all(), (res.mb_cost[r0], ref.mb_cost[r0])
+    a, b = res.mb_per_k_cost[r0], ref.mb_per_k_cost[r0]
+    assert np.array_equal(np.isfinite(a), np.isfinite(b))
+    ok = np.isfinite(b)
+    assert within(a[ok], b[ok], 1e-4).mean() >= 0.95
+
+
+def test_real_sources_laplace_match_oracle(ctx, oracle, batch):
+    kw = dict(fit_all_models=True, method=abi.METHOD_LAPLACE, run_multi_bazin=False)
+    res = ctx.fit_batch(batch, **kw)
+    ref = oracle.fit_batch(batch, **kw)
+    perts = [perturbed(oracle, batch, *p, **kw) for p in PERTURBATIONS]
+    frac, floor, bad, n, n_orc = selection_check(res, ref, perts)
+    assert frac >= floor and not bad and n <= max(n_orc, 1), (frac, floor, bad, n, n_orc)
+    a, b = res.per_model_chi2, ref.per_model_chi2
+    ok = np.isfinite(a) & np.isfinite(b)
+    assert np.array_equal(np.isfinite(a), np.isfinite(b))
+    rel = np.abs(a[ok] - b[ok]) / np.maximum(np.abs(b[ok]), 1e-12)
+    assert np.median(rel) < 1e-9, np.median(rel)
+
+
+def test_real_sources_joint_branch_matches_oracle(ctx, oracle, batch):
+    kw = dict(fit_all_models=False, method=abi.METHOD_LAPLACE, run_multi_bazin=False, joint_multiband=True)
+    check_joint(ctx.fit_batch(batch, **kw), oracle, batch, kw)
