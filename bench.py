@@ -373,6 +373,7 @@ def run_fused(args, ws, rank, local):
     scale = run_scale(args, dev, flush, ws, rank, tuned["candidate"]) if args.scale_sources > 0 else None
     final = run_finalize(args, batch, res, flush, dev, ws, rank) if args.finalize_sources > 0 and e2e_t else None
     basic = run_side(args, "basic", dev, flush, ws, rank) if args.basic_steps > 0 else None
+    basic_joint = run_side(args, "basic_joint", dev, flush, ws, rank) if args.basic_steps > 0 else None
     precision = run_side(args, "precision", dev, flush, ws, rank) if args.precision_steps > 0 else None
     if rank != 0:
         ctx.close()
@@ -463,6 +464,7 @@ def run_fused(args, ws, rank, local):
         "full_scale": scale,
         "finalize_all_models": final,
         "basic": basic,
+        "basic_fit_parametric": basic_joint,
         "precision": precision,
         "autotune": {"candidates_block_staging_blocks_per_sm": ctx.autotune_candidates().tolist(),
                      "chosen": tuned,
@@ -627,12 +629,16 @@ def run_side(args, which, dev, flush, ws, rank):
     own copy (seed + rank):
       basic      100 sources x 3 bands x 30 points (the reference's CPU
                  benchmark case), fit_all_models, Laplace, MultiBazin;
+      basic_joint  the same sources as the reference's benchmark calls them,
+                 fit_parametric(.., false, Laplace): with three bands every
+                 source takes the joint multi-band Villar branch;
       precision  1,000 sources x 3 bands x 2,000 points, flux range 1e5,
                  fit_all_models, Laplace, MultiBazin."""
     import torch
     from lightcurve_fitting_gb300 import abi, synth
     from lightcurve_fitting_gb300.lib import Context
-    if which == "basic":
+    joint = which == "basic_joint"
+    if which in ("basic", "basic_joint"):
         batch, steps = synth.config_basic(100, seed=1 + rank), args.basic_steps
     else:
         batch, steps = synth.config_precision(1000, seed=4 + rank), args.precision_steps
@@ -643,7 +649,8 @@ def run_side(args, which, dev, flush, ws, rank):
     sstream = torch.cuda.ExternalStream(sctx.stream, device=dev)
 
     def fit():
-        sctx.fit_device(ptrs, batch.n_sources, batch.n_bands, fit_all_models=True, method=abi.METHOD_LAPLACE)
+        sctx.fit_device(ptrs, batch.n_sources, batch.n_bands, fit_all_models=not joint, method=abi.METHOD_LAPLACE,
+                        joint_multiband=joint)
 
     fit()
     torch.cuda.synchronize()
@@ -662,9 +669,11 @@ def run_side(args, which, dev, flush, ws, rank):
     ms = dist_max(float(np.mean(times)), ws, dev)
     return {"value": job_value(batch.n_sources, ws, ms), "unit": "sources/s", "ms_per_step": ms,
             "sources_per_gpu": batch.n_sources, "n_obs_per_gpu": batch.n_obs, "steps": steps, "warmup": 1,
-            "config": batch.name + ": fit_all_models=true, Laplace, MultiBazin, device-resident",
+            "config": batch.name + (": fit_parametric(fit_all_models=false, Laplace): the joint multi-band Villar "
+                                    "branch, then per-band Laplace, refinements, MultiBazin, device-resident" if joint
+                                    else ": fit_all_models=true, Laplace, MultiBazin, device-resident"),
             "stage_ms": {k: st[k] for k in ["ms_total", "ms_pso", "ms_lbfgs", "ms_uncertainty", "ms_refine",
-                                            "ms_multi_bazin"]}}
+                                            "ms_multi_bazin"] + (["ms_joint"] if joint else [])}}
 
 
 def run_scale(args, dev, flush, ws, rank, candidate):

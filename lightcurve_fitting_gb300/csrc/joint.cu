@@ -64,6 +64,12 @@ struct JointBands {
     int n[J_MAX_BANDS];     // observations per band
     int off[J_MAX_BANDS];   // first observation in the staged records
     int n_total;
+    // the band balancing (n_total / nb) / n[b] and 1 / max(n_total, 1),
+    // formed once per task: the FP64 divisions of the reference's cost
+    // (src/parametric.rs:3815-4131) become multiplications, which move the
+    // cost by ~1e-16, far below its FP32 evaluation's ~1e-7
+    double w[J_MAX_BANDS];
+    double inv_total;
 };
 
 // The joint cost of one particle (column p of the position array xs).
@@ -75,7 +81,6 @@ __device__ double joint_cost(const JointBands& jb, const float4* obs, const floa
         float c = VillarF::constraint(ref);
         if (c > 0.0f) return 1e12 + 10000.0 * (double)c;
     }
-    const double scale = (double)jb.n_total / (double)jb.nb;
     double balanced = 0.0;
     for (int b = 0; b < jb.nb; b++) {
         float bp[7];
@@ -105,7 +110,7 @@ __device__ double joint_cost(const JointBands& jb, const float4* obs, const floa
             if (acc.big > LN_DBL_MAX) return INFINITY;
             band_nll += exp((double)acc.big);
         }
-        if (jb.n[b] > 0) balanced += (band_nll / (double)jb.n[b]) * scale;
+        if (jb.n[b] > 0) balanced += band_nll * jb.w[b];
     }
     // population prior of the reference band, relative priors of the offsets
     float lp = 0.0f;
@@ -123,7 +128,7 @@ __device__ double joint_cost(const JointBands& jb, const float4* obs, const floa
             float z = (xs[(7 * b + j) * JP + p] - c_rel_mean[j]) / c_rel_sigma[j];
             lp += 0.5f * z * z;
         }
-    return (balanced + (double)lp) / (double)max(jb.n_total, 1);
+    return (balanced + (double)lp) * jb.inv_total;
 }
 
 // Block-wide first index q in [start, JP) with improve[q] (or -1).
@@ -198,6 +203,9 @@ __global__ void __launch_bounds__(J_THREADS) joint_pso_kernel(DeviceBatch d) {
             }
             jb.nb = nb;
             jb.n_total = tot;
+            const double scale = (double)tot / (double)max(nb, 1);
+            for (int b = 0; b < nb; b++) jb.w[b] = jb.n[b] > 0 ? scale / (double)jb.n[b] : 0.0;
+            jb.inv_total = 1.0 / (double)max(tot, 1);
         }
         __syncthreads();
         const int nb = jb.nb, D = 7 * nb;
