@@ -248,6 +248,7 @@ struct WarpSmem {
     // stay in registers): [state][dimension][lane], state = position,
     // velocity, personal best, position and velocity at the iteration start
     float lo_state[5][7][32];
+    double s_pos[8];  // a position the warp evaluates in FP64 (MultiBazin K = 1 near ties)
 };
 // The MultiBazin instantiations (swarm dimensions 4K + 2 = 10, 14, 18): the
 // same, with three state planes (position, velocity, personal best; the
@@ -258,6 +259,7 @@ struct WarpSmemMB {
     uint64_t pad;
     ff lo[MAXD], hi[MAXD], vmax[MAXD], g[MAXD];
     float lo_state[3][MAXD][32];
+    double s_pos[MAXD];  // a position the warp evaluates in FP64 (near ties)
 };
 template <int MAXD>
 struct WarpSmemOf {
@@ -803,6 +805,62 @@ __device__ __forceinline__ void run_swarm_exact(const DeviceBatch& d, const PsoT
 }
 
 // ---------------------------------------------------------------------------
+// FP64 MultiBazin cost (multi_bazin_cost, src/parametric.rs:973-1004, in the
+// oracle's FP64 form) of the position pos[0 .. 4K + 1], read by every lane:
+// the warp splits the band's observations, then sums its partial sums.  A
+// non-finite prediction makes the cost 1e99, as in the reference.  Every lane
+// of the warp must call it.  It gives each run's reported cost: the swarm
+// compares FP32 costs, the reference reports (and fit_multi_bazin compares
+// across restarts and K) the FP64 cost of the best position.
+// ---------------------------------------------------------------------------
+template <int K>
+__device__ __noinline__ double mb_cost_fp64(const DeviceBatch& d, const BandStats& bs, const double* pos) {
+    const int lane = threadIdx.x & 31;
+    double a[K], t0[K], tr[K], tf[K];
+#pragma unroll
+    for (int c = 0; c < K; c++) {
+        a[c] = exp(pos[4 * c]);
+        t0[c] = pos[4 * c + 1];
+        tr[c] = exp(pos[4 * c + 2]);
+        tf[c] = exp(pos[4 * c + 3]);
+    }
+    const double B = pos[4 * K];
+    const double se = exp(pos[4 * K + 1]);
+    const double se2 = se * se;
+    const double* t = d.t64 + bs.off;
+    const double* f = d.f64 + bs.off;
+    const double* var = d.var64 + bs.off;
+    const double* uf = d.uf64 + bs.off;
+    const uint8_t* up = d.up + bs.off;
+    double nll = 0.0;
+    int bad = 0;
+    for (int i = lane; i < bs.n; i += 32) {
+        double sum = 0.0;
+#pragma unroll
+        for (int c = 0; c < K; c++) {
+            const double dt = t[i] - t0[c];
+            sum += a[c] * exp(-dt / tf[c]) * (1.0 / (1.0 + exp(-dt / tr[c])));
+        }
+        const double pr = sum + B;
+        if (!isfinite(pr)) {
+            bad = 1;
+            continue;
+        }
+        const double tv = var[i] + se2;
+        if (up[i]) {
+            nll -= log_normal_cdf_f64((uf[i] - pr) / sqrt(tv));
+        } else {
+            const double dd = pr - f[i];
+            nll += dd * dd / tv + log(tv);
+        }
+    }
+    for (int o = 16; o; o >>= 1) nll += __shfl_xor_sync(FULL, nll, o);
+    if (__any_sync(FULL, bad)) return 1e99;
+    return nll / (double)max(bs.n, 1);
+}
+
+
+// ---------------------------------------------------------------------------
 // Exact-trajectory MultiBazin swarms (fit_multi_bazin's pso_minimize runs,
 // src/parametric.rs:1008-1157).  With a 30-particle, 60-iteration swarm and
 // no polish after it, the reference's K and costs are its swarm's end points:
@@ -822,7 +880,7 @@ __device__ __forceinline__ void run_swarm_exact(const DeviceBatch& d, const PsoT
 template <int MAXD, int KIND>
 __device__ __forceinline__ void run_swarm_exact_mb(const DeviceBatch& d, const PsoTask& task, const BandStats& bs,
                                                    TaskCtx& t, ff* s_lo, ff* s_hi, ff* s_vm, ff* s_g, float* st,
-                                                   int slot) {
+                                                   double* s_pos, int slot) {
     constexpr int K = KIND - KIND_MB1 + 1, D = 4 * K + 2;
     static_assert(D <= MAXD, "MultiBazin swarm wider than the instantiation");
     const int lane = threadIdx.x & 31;
@@ -925,6 +983,20 @@ __device__ __forceinline__ void run_swarm_exact_mb(const DeviceBatch& d, const P
             set_gbest(__ffs(mm) - 1);
         }
     }
+    // FP64 cost of the position lane `src` writes into s_pos (warp-uniform)
+    auto fp64_of = [&](int src, auto&& write) -> double {
+        if (lane == src) write();
+        __syncwarp();
+        const double v = mb_cost_fp64<K>(d, bs, s_pos);
+        __syncwarp();
+        return v;
+    };
+    auto fp64_g = [&]() -> double {
+        return fp64_of(0, [&]() {
+#pragma unroll
+            for (int k = 0; k < D; k++) s_pos[k] = ff_to(s_g[k]);
+        });
+    };
     // ---- iterations (src/parametric.rs:1694-1755)
     int stall = 0;
     double prev = gc;
@@ -992,11 +1064,14 @@ __device__ __forceinline__ void run_swarm_exact_mb(const DeviceBatch& d, const P
             break;
         }
     }
+    // ---- result: the FP64 cost of the best position, as the reference
+    // reports it (fit_multi_bazin compares the restarts' costs and the BICs)
+    const double rc = gc < INFINITY ? fp64_g() : gc;
     int tot_evals = live ? evals : 0;
     for (int k = 16; k; k >>= 1) tot_evals += __shfl_xor_sync(FULL, tot_evals, k);
     if (lane == 0) {
         PsoResult& R = d.pso_res[task.out];
-        R.cost = gc;
+        R.cost = rc;
         R.iters = it;
         R.evals = tot_evals;
         for (int j = 0; j < MB_MAXP; j++) R.params[j] = R.params_lo[j] = 0.0f;
@@ -1084,7 +1159,7 @@ __global__ void __launch_bounds__(256, MINB)
             constexpr int KMB = KIND_MB1 + (MAXD - 2) / 4 - 1;  // D = 4K + 2
             if (task.kind == KMB)
                 run_swarm_exact_mb<MAXD, KMB>(d, task, bs, t, ws->lo, ws->hi, ws->vmax, ws->g, &ws->lo_state[0][0][0],
-                                              slot);
+                                              ws->s_pos, slot);
         } else switch (task.kind) {
             case BAZIN: run_swarm_exact<BAZIN>(d, task, bs, t, ws, slot); break;
             case VILLAR: run_swarm_exact<VILLAR>(d, task, bs, t, ws, slot); break;
@@ -1096,7 +1171,7 @@ __global__ void __launch_bounds__(256, MINB)
             case METZGER: run_swarm<MAXD, METZGER>(d, task, bs, t, slot, gwarp); break;
             case KIND_MB1:
                 run_swarm_exact_mb<MAXD, KIND_MB1>(d, task, bs, t, ws->lo, ws->hi, ws->vmax, ws->g,
-                                                   &ws->lo_state[0][0][0], slot);
+                                                   &ws->lo_state[0][0][0], ws->s_pos, slot);
                 break;
             default: break;
         }

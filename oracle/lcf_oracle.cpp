@@ -568,6 +568,21 @@ static inline double perturb_cost(double c, const double* p, int np) {
     if (g_cost_rel == 0.0 || !(std::fabs(c) < 1e11)) return c;
     return c * ((perturb_hash(p, np, 0) >> 63) ? 1.0 + g_cost_rel : 1.0 - g_cost_rel);
 }
+// Test hook: every new interior swarm position component scaled by 1 +- rel
+// (the sign a hash of the value, the component, the particle, the iteration
+// and `salt`), so the tests can measure how far the reference's own results
+// move when its swarm trajectories change by a rounding (rel ~1e-15).
+static double g_pos_rel = 0.0;
+static uint64_t g_pos_salt = 0;
+static inline double perturb_position(double x, int d, int p, int it) {
+    uint64_t b;
+    std::memcpy(&b, &x, 8);
+    uint64_t h = 0x9E3779B97F4A7C15ULL ^ (g_pos_salt * 0xD1B54A32D192ED03ULL);
+    h = (h ^ b) * 0xBF58476D1CE4E5B9ULL;
+    h = (h ^ ((uint64_t)d << 32 ^ (uint64_t)p << 16 ^ (uint64_t)it)) * 0x94D049BB133111EBULL;
+    h ^= h >> 31;
+    return x * ((h >> 63) ? 1.0 + g_pos_rel : 1.0 - g_pos_rel);
+}
 // each gradient component scaled by 1 +- g_grad_rel (sign from the point,
 // the component and the salt)
 static inline void perturb_grad(double* g, const double* p, int np) {
@@ -747,7 +762,7 @@ static double pso_minimize(F& cost_fn, const std::vector<double>& lo, const std:
                 double np = x[d] + vv;
                 if (np <= lo[d]) { x[d] = lo[d]; v[d] = 0.0; }
                 else if (np >= hi[d]) { x[d] = hi[d]; v[d] = 0.0; }
-                else { x[d] = np; v[d] = vv; }
+                else { x[d] = g_pos_rel != 0.0 ? perturb_position(np, d, p, it) : np; v[d] = vv; }
             }
             double c = cost_fn(x);
             g_pso_stats.evals++;
@@ -2583,5 +2598,9 @@ void orc_set_cost_perturbation(double rel, uint64_t salt, double grad_rel) {
     g_cost_rel = rel;
     g_cost_salt = salt;
     g_grad_rel = grad_rel;
+}
+void orc_set_position_perturbation(double rel, uint64_t salt) {
+    g_pos_rel = rel;
+    g_pos_salt = salt;
 }
 }  // extern "C"

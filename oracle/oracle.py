@@ -73,6 +73,7 @@ def lib():
         L.orc_pso_stats.argtypes = [vp, i]
         L.orc_max_threads.restype = i
         L.orc_set_cost_perturbation.argtypes = [d, u64, d]
+        L.orc_set_position_perturbation.argtypes = [d, u64]
         L.orc_set_laplace_step.argtypes = [d]
         L.orc_metzger_at_obs.argtypes = [vp, d]
         L.orc_metzger_at_obs.restype = d
@@ -338,4 +339,13 @@ def set_cost_perturbation(rel: float, salt: int = 0, grad_rel: float = 0.0) -> N
     arithmetic.  A test hook: it measures how far the reference's own results
     move under rounding-sized changes of its costs and gradients."""
     lib().orc_set_cost_perturbation(float(rel), int(salt), float(grad_rel))
+
+
+def set_position_perturbation(rel: float, salt: int = 0) -> None:
+    """Scale every new interior swarm position component of the oracle by
+    1 +- rel (a hash of the value, component, particle, iteration and `salt`
+    picks the sign); 0 restores the exact arithmetic.  A test hook: it
+    measures how far the reference's own results move when its swarm
+    trajectories change by a rounding."""
+    lib().orc_set_position_perturbation(float(rel), int(salt))
 

@@ -11,7 +11,8 @@ stated against the oracle's sensitivity to rounding-sized perturbations
     reported cost median within 1e-9; posterior means within 0.1 posterior
     sigma for >= 90 % of the bands selecting the oracle's model; the
     MultiBazin K of the 30 rank-0 bands identical, its cost within 1e-6
-    (measured 1.4e-7 at most), and >= 95 % of the per-K costs within 1e-4;
+    (measured 1e-13 at most: the reported cost is the FP64 cost of the
+    swarm's best position), and >= 95 % of the per-K costs within 1e-4;
   * Laplace: the same selection rule, and the polished cost of every
     (band, model) pair to a median 1e-9;
   * the joint multi-band Villar branch (fit_all_models = false): the joint

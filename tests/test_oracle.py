@@ -312,3 +312,26 @@ def test_gpu_kernel_costs_follow_their_own_rules(oracle):
     empty.up = np.zeros(0, np.uint8)
     assert oracle.gpu_pso_cost(0, empty, p)[0] == 1e99
     assert oracle.gpu_svi_fit(0, empty, p, p, np.ones(6), src=0)[2] == -1e99
+
+
+def test_perturbation_hooks_restore_the_exact_arithmetic(oracle):
+    """The oracle's test hooks (cost / gradient and swarm-position
+    perturbations) move its results when set and leave them bit-identical
+    once reset to 0."""
+    batch = synth.config_basic(6, seed=11)
+    kw = dict(fit_all_models=True, method=abi.METHOD_LAPLACE, run_multi_bazin=True)
+    base = oracle.fit_batch(batch, **kw)
+    moved = []
+    for set_hook in (lambda: oracle.set_cost_perturbation(1e-7, 0, 1e-12),
+                     lambda: oracle.set_position_perturbation(1e-13, 0)):
+        set_hook()
+        try:
+            pert = oracle.fit_batch(batch, **kw)
+        finally:
+            oracle.set_cost_perturbation(0.0)
+            oracle.set_position_perturbation(0.0)
+        moved.append(not np.array_equal(pert.per_model_chi2, base.per_model_chi2, equal_nan=True))
+    again = oracle.fit_batch(batch, **kw)
+    assert all(moved)
+    for f in ("model", "per_model_chi2", "pso_params", "mb_cost", "mb_per_k_cost"):
+        assert np.array_equal(getattr(again, f), getattr(base, f), equal_nan=True), f
