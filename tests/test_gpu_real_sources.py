@@ -92,3 +92,46 @@ def test_real_sources_laplace_match_oracle(ctx, oracle, batch):
 def test_real_sources_joint_branch_matches_oracle(ctx, oracle, batch):
     kw = dict(fit_all_models=False, method=abi.METHOD_LAPLACE, run_multi_bazin=False, joint_multiband=True)
     check_joint(ctx.fit_batch(batch, **kw), oracle, batch, kw)
+
+
+def test_real_sources_through_the_python_api(ctx, oracle, batch):
+    """The user's path on the real sources: fit_batch_parametric on band
+    dicts (all models, SVI) and extract_param_features on its results, against
+    the same conversion of the oracle's fit of the same sources: band order,
+    names and counts, MultiBazin K and cost, the reference's 34 feature keys,
+    and the selected model for >= 95 % of bands (the selection criterion of
+    the metric-path test above holds the rest)."""
+    import math
+    from lightcurve_fitting_gb300 import features, parametric
+    a = real_sources.arrays()
+    bo, so, names = a["band_obs_offsets"], a["source_band_offsets"], a["band_names"]
+    sources = []
+    for s in range(batch.n_sources):
+        bands = {}
+        for b in range(so[s], so[s + 1]):
+            lo, hi = bo[b], bo[b + 1]
+            bands[str(names[b])] = {"times": list(a["times"][lo:hi]), "values": list(a["flux"][lo:hi]),
+                                    "errors": list(a["flux_err"][lo:hi])}
+        sources.append(bands)
+    gpu = parametric.fit_batch_parametric(sources, fit_all_models=True, method="svi", ctx=ctx)
+    ref = oracle.fit_batch(batch, fit_all_models=True, method=abi.METHOD_SVI, run_multi_bazin=True)
+    orc = parametric.results_from_fit(ref, batch, [list(d.keys()) for d in sources], True, abi.METHOD_SVI, -1)
+    assert len(gpu) == len(orc) == batch.n_sources
+    same, total = 0, 0
+    for g, o in zip(gpu, orc):
+        assert [r["band"] for r in g] == [r["band"] for r in o]
+        assert [r["n_obs"] for r in g] == [r["n_obs"] for r in o]
+        for rg, ro in zip(g, o):
+            total += 1
+            same += rg["model"] == ro["model"]
+            assert ("multi_bazin" in rg) == ("multi_bazin" in ro)
+            if "multi_bazin" in rg:
+                assert rg["multi_bazin"]["best_k"] == ro["multi_bazin"]["best_k"]
+                assert math.isclose(rg["multi_bazin"]["cost"], ro["multi_bazin"]["cost"], rel_tol=1e-6)
+    assert same >= 0.95 * total, (same, total)
+    fg = features.extract_param_features_batch(gpu, "ztfr")
+    fo = features.extract_param_features_batch(orc, "ztfr")
+    for x, y in zip(fg, fo):
+        assert x.keys() == y.keys() and len(x) == 34
+        for k in ("param_n_obs", "param_n_bands_fit", "mb_best_k"):
+            assert x[k] == y[k], k
