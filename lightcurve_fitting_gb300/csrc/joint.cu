@@ -3,7 +3,7 @@
 // or more bands when fit_all_models is false (:3742-3761).
 //
 // A persistent grid of blocks takes (source, restart) tasks: 200 particles
-// (threads 0..199 of 224) search the 7 * n_bands joint space (the most
+// (two threads each, threads 0..399 of 448) search the 7 * n_bands joint space (the most
 // populated band's Villar parameters, then per-band offsets) with the
 // reference's PSO (200 particles, 1500 iterations, stall 60; seeds 42 / 137 /
 // 271, restart 1 seeded).  The source's bands are staged in shared memory;
@@ -38,7 +38,7 @@ namespace lcf {
 constexpr int JP = 200;          // particles (src/parametric.rs:3951-3956)
 constexpr int J_MAXIT = 1500;
 constexpr int J_STALL = 60;
-constexpr int J_THREADS = 224;
+constexpr int J_THREADS = 448;  // two threads per particle
 
 // de Soto et al. relative priors of the offsets, src/parametric.rs:3771-3786
 static __device__ __constant__ float c_rel_mean[7] = {-0.015f * 2.302585093f, -0.001f, -0.095f * 2.302585093f,
@@ -72,8 +72,12 @@ struct JointBands {
     double inv_total;
 };
 
-// The joint cost of one particle (column p of the position array xs).
-__device__ double joint_cost(const JointBands& jb, const float4* obs, const float* xs, int p) {
+// The joint cost of one particle (column p of the position array xs),
+// evaluated by the particle's two threads (h = 0, 1: observations h, h + 2,
+// ...; pm = the pair's lane mask).  Each band's partial sums are combined
+// before any decision, by a commutative sum, so both threads return the same
+// cost.
+__device__ double joint_cost(const JointBands& jb, const float4* obs, const float* xs, int p, int h, unsigned pm) {
     float ref[7];
 #pragma unroll
     for (int j = 0; j < 7; j++) ref[j] = xs[j * JP + p];
@@ -97,18 +101,24 @@ __device__ double joint_cost(const JointBands& jb, const float4* obs, const floa
         Nll acc;
         acc.reset();
         const float4* o = obs + jb.off[b];
-        for (int i = 0; i < jb.n[b]; i++) {
+        for (int i = h; i < jb.n[b]; i += 2) {
             float4 r = o[i];
             int st = ST_OK;
             float pr = e.eval(r.x, r.y, st);
             acc.obs(r, pr, st, se2);
         }
-        if (acc.nonfinite) return BIG_COST;
-        if (acc.inf) return INFINITY;
-        double band_nll = (double)acc.s - (double)acc.c;
-        if (acc.big > -INFINITY) {
-            if (acc.big > LN_DBL_MAX) return INFINITY;
-            band_nll += exp((double)acc.big);
+        const double part = (double)acc.s - (double)acc.c;
+        double band_nll = part + __shfl_xor_sync(pm, part, 1);
+        const float ob = __shfl_xor_sync(pm, acc.big, 1);
+        float big = acc.big;
+        if (ob > -INFINITY) big = big > -INFINITY ? fmaxf(big, ob) + log1pf(expf(-fabsf(big - ob))) : ob;
+        const int fl = acc.nonfinite | (acc.inf << 1);
+        const int flags = fl | __shfl_xor_sync(pm, fl, 1);
+        if (flags & 1) return BIG_COST;
+        if (flags & 2) return INFINITY;
+        if (big > -INFINITY) {
+            if (big > LN_DBL_MAX) return INFINITY;
+            band_nll += exp((double)big);
         }
         if (jb.n[b] > 0) balanced += band_nll * jb.w[b];
     }
@@ -160,7 +170,9 @@ __device__ int block_first(bool flag, int* s_warp) {
 __global__ void __launch_bounds__(J_THREADS) joint_pso_kernel(DeviceBatch d) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const int tid = threadIdx.x;
-    const bool live = tid < JP;
+    const int p = tid >> 1, h = tid & 1;       // particle, half
+    const unsigned pm = 3u << (tid & 30);      // the particle's two lanes
+    const bool live = p < JP;
     __shared__ JointBands jb;
     __shared__ int s_warp[J_THREADS / 32];
     __shared__ double s_gc;
@@ -255,27 +267,27 @@ __global__ void __launch_bounds__(J_THREADS) joint_pso_kernel(DeviceBatch d) {
         // population prior centre with t0 = t_peak - 5 and the relative
         // priors' means, clamped to the box
         if (live) {
-            for (int j = 0; j < D; j++) {
+            for (int j = h; j < D; j += 2) {
                 const double lo = ff_to(s_lo[j]), hi = ff_to(s_hi[j]), vmax = ff_to(s_vm[j]);
                 double x, v;
                 if (seeded) {
-                    if (tid == 0) {
+                    if (p == 0) {
                         double c = j < 7 ? c_pop_c[VILLAR][j] : c_rel_mean64[j % 7];
                         if (j == 3) c = t_peak - 5.0;
                         x = fmin(fmax(c, lo), hi);
                         v = __dmul_rn(__dmul_rn(vmax, 0.2), __dsub_rn(2.0 * dr[j], 1.0));
                     } else {
-                        const int o = D + 2 * D * (tid - 1);
+                        const int o = D + 2 * D * (p - 1);
                         x = __dadd_rn(lo, __dmul_rn(dr[o + j], __dsub_rn(hi, lo)));
                         v = __dmul_rn(__dmul_rn(vmax, 0.2), __dsub_rn(2.0 * dr[o + D + j], 1.0));
                     }
                 } else {
-                    const int o = 2 * D * tid;
+                    const int o = 2 * D * p;
                     x = __dadd_rn(lo, __dmul_rn(dr[o + 2 * j], __dsub_rn(hi, lo)));
                     v = __dmul_rn(__dmul_rn(vmax, 0.2), __dsub_rn(2.0 * dr[o + 2 * j + 1], 1.0));
                 }
                 const ff xf = ff_from(x), vf = ff_from(v);
-                const size_t k = (size_t)j * JP + tid;
+                const size_t k = (size_t)j * JP + p;
                 xh[k] = xf.hi;
                 xl[k] = xf.lo;
                 vh[k] = vf.hi;
@@ -286,9 +298,9 @@ __global__ void __launch_bounds__(J_THREADS) joint_pso_kernel(DeviceBatch d) {
             }
         }
         __syncthreads();
-        double c = live ? joint_cost(jb, obs, xt, tid) : INFINITY;
+        double c = live ? joint_cost(jb, obs, xt, p, h, pm) : INFINITY;
         double pbc = c;
-        int evals = live ? 1 : 0;
+        int evals = live && h == 0 ? 1 : 0;
         // global best after the sequential initial loop: the first strict
         // minimum, in particle order
         {
@@ -299,7 +311,8 @@ __global__ void __launch_bounds__(J_THREADS) joint_pso_kernel(DeviceBatch d) {
             __syncthreads();
             double g = INFINITY;
             for (int w = 0; w < J_THREADS / 32; w++) g = fmin(g, s_min[w]);
-            const int q = block_first(live && c == g && g < INFINITY, s_warp);
+            const int qt = block_first(live && h == 0 && c == g && g < INFINITY, s_warp);
+            const int q = qt >= 0 ? qt >> 1 : -1;
             if (tid == 0) s_gc = q >= 0 ? g : INFINITY;
             if (tid < D) s_g[tid] = q >= 0 ? ffm(xh[(size_t)tid * JP + q], xl[(size_t)tid * JP + q]) : ffm(0.0f, 0.0f);
         }
@@ -311,15 +324,15 @@ __global__ void __launch_bounds__(J_THREADS) joint_pso_kernel(DeviceBatch d) {
         for (; it < J_MAXIT; it++) {
             const double wd = __dsub_rn(0.9, __dmul_rn(__dmul_rn(__dsub_rn(0.9, 0.4), (double)it), inv_iters));
             const ff w = ff_from(wd);
-            const float2* r = d15 + base + (size_t)it * 2 * D * JP + (size_t)2 * D * tid;
-            // the move of this particle from its iteration-start state: trial
-            // (leading floats to xt) or commit (the full state, and the
-            // personal best when `to_pb`).  A plain loop over the dimensions:
-            // unrolling it by band needs ~128 registers, two blocks per SM
-            // instead of four, and measured 20 % slower.
+            const float2* r = d15 + base + (size_t)it * 2 * D * JP + (size_t)2 * D * p;
+            // the move of this particle from its iteration-start state, the
+            // pair's two threads taking alternate dimensions: trial (leading
+            // floats to xt) or commit (the full state, and the personal best
+            // when `to_pb`).  A plain loop: unrolling it by band needed ~128
+            // registers a thread and measured 20 % slower.
             auto move = [&](bool commit, bool to_pb) {
-                for (int j = 0; j < D; j++) {
-                    const size_t k = (size_t)j * JP + tid;
+                for (int j = h; j < D; j += 2) {
+                    const size_t k = (size_t)j * JP + p;
                     ff xn, vn;
                     ff_move(ffm(xh[k], xl[k]), ffm(vh[k], vl[k]), ffm(pbh[k], pl[k]), s_g[j], w, r[2 * j],
                             r[2 * j + 1], s_vm[j], s_lo[j], s_hi[j], xn, vn);
@@ -339,16 +352,18 @@ __global__ void __launch_bounds__(J_THREADS) joint_pso_kernel(DeviceBatch d) {
             };
             int start = 0;
             while (start < JP) {
-                const bool active = live && tid >= start;
+                const bool active = live && p >= start;
                 if (active) {
                     move(false, false);
-                    c = joint_cost(jb, obs, xt, tid);
-                    evals++;
+                    __syncwarp(pm);  // the pair's trial dimensions, before its cost
+                    c = joint_cost(jb, obs, xt, p, h, pm);
+                    evals += h == 0;
                 }
                 const double gc = s_gc;
-                const int q = block_first(active && c < gc, s_warp);
+                const int qt = block_first(active && h == 0 && c < gc, s_warp);
+                const int q = qt >= 0 ? qt >> 1 : -1;
                 const int qe = q < 0 ? JP - 1 : q;
-                if (active && tid <= qe) {
+                if (active && p <= qe) {
                     const bool to_pb = c < pbc;
                     move(true, to_pb);
                     if (to_pb) pbc = c;
@@ -356,7 +371,7 @@ __global__ void __launch_bounds__(J_THREADS) joint_pso_kernel(DeviceBatch d) {
                 __syncthreads();
                 if (q >= 0) {
                     if (tid < D) s_g[tid] = ffm(xh[(size_t)tid * JP + q], xl[(size_t)tid * JP + q]);
-                    if (tid == q) s_gc = c;
+                    if (tid == 2 * q) s_gc = c;
                 }
                 __syncthreads();
                 start = qe + 1;
