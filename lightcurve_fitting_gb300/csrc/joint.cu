@@ -70,6 +70,8 @@ struct JointBands {
     // cost by ~1e-16, far below its FP32 evaluation's ~1e-7
     double w[J_MAX_BANDS];
     double inv_total;
+    ff wf[J_MAX_BANDS];     // the same as double-float pairs (the cost's sums run on the FP32 pipe)
+    ff inv_total_f;
 };
 
 // The joint cost of one particle (column p of the position array xs),
@@ -85,7 +87,10 @@ __device__ double joint_cost(const JointBands& jb, const float4* obs, const floa
         float c = VillarF::constraint(ref);
         if (c > 0.0f) return 1e12 + 10000.0 * (double)c;
     }
-    double balanced = 0.0;
+    // the band sums as double-float pairs: ~1e-14 relative, far below the FP32
+    // terms' own error, on the FP32 pipe instead of FP64's 1/64 rate; ff_add
+    // is commutative, so both threads of the pair form the same cost
+    ff balanced = ffm(0.0f, 0.0f);
     for (int b = 0; b < jb.nb; b++) {
         float bp[7];
 #pragma unroll
@@ -107,8 +112,8 @@ __device__ double joint_cost(const JointBands& jb, const float4* obs, const floa
             float pr = e.eval(r.x, r.y, st);
             acc.obs(r, pr, st, se2);
         }
-        const double part = (double)acc.s - (double)acc.c;
-        double band_nll = part + __shfl_xor_sync(pm, part, 1);
+        const ff part = ff_add(ffm(acc.s, 0.0f), -acc.c);
+        ff band_nll = ff_add(part, ffm(__shfl_xor_sync(pm, part.hi, 1), __shfl_xor_sync(pm, part.lo, 1)));
         const float ob = __shfl_xor_sync(pm, acc.big, 1);
         float big = acc.big;
         if (ob > -INFINITY) big = big > -INFINITY ? fmaxf(big, ob) + log1pf(expf(-fabsf(big - ob))) : ob;
@@ -118,9 +123,9 @@ __device__ double joint_cost(const JointBands& jb, const float4* obs, const floa
         if (flags & 2) return INFINITY;
         if (big > -INFINITY) {
             if (big > LN_DBL_MAX) return INFINITY;
-            band_nll += exp((double)big);
+            band_nll = ff_add(band_nll, ff_from(exp((double)big)));
         }
-        if (jb.n[b] > 0) balanced += band_nll * jb.w[b];
+        if (jb.n[b] > 0) balanced = ff_add(balanced, ff_mul(band_nll, jb.wf[b]));
     }
     // population prior of the reference band, relative priors of the offsets
     float lp = 0.0f;
@@ -138,7 +143,7 @@ __device__ double joint_cost(const JointBands& jb, const float4* obs, const floa
             float z = (xs[(7 * b + j) * JP + p] - c_rel_mean[j]) / c_rel_sigma[j];
             lp += 0.5f * z * z;
         }
-    return (balanced + (double)lp) * jb.inv_total;
+    return ff_to(ff_mul(ff_add(balanced, lp), jb.inv_total_f));
 }
 
 // Block-wide first index q in [start, JP) with improve[q] (or -1).
@@ -216,8 +221,12 @@ __global__ void __launch_bounds__(J_THREADS) joint_pso_kernel(DeviceBatch d) {
             jb.nb = nb;
             jb.n_total = tot;
             const double scale = (double)tot / (double)max(nb, 1);
-            for (int b = 0; b < nb; b++) jb.w[b] = jb.n[b] > 0 ? scale / (double)jb.n[b] : 0.0;
+            for (int b = 0; b < nb; b++) {
+                jb.w[b] = jb.n[b] > 0 ? scale / (double)jb.n[b] : 0.0;
+                jb.wf[b] = ff_from(jb.w[b]);
+            }
             jb.inv_total = 1.0 / (double)max(tot, 1);
+            jb.inv_total_f = ff_from(jb.inv_total);
         }
         __syncthreads();
         const int nb = jb.nb, D = 7 * nb;
