@@ -335,3 +335,19 @@ def test_perturbation_hooks_restore_the_exact_arithmetic(oracle):
     assert all(moved)
     for f in ("model", "per_model_chi2", "pso_params", "mb_cost", "mb_per_k_cost"):
         assert np.array_equal(getattr(again, f), getattr(base, f), equal_nan=True), f
+
+
+def test_oracle_on_a_ragged_batch(oracle):
+    """Empty bands are skipped, one- to four-point bands and a source without
+    bands are handled, MultiBazin runs on rank-0 bands of >= 5 points, and a
+    source with a single band of data leaves the joint branch for the per-band
+    fit (src/parametric.rs:3742-3761)."""
+    import ragged
+    b = ragged.batch()
+    n = b.band_counts()
+    for kw in (dict(fit_all_models=True, method=abi.METHOD_SVI, run_multi_bazin=True),
+               dict(fit_all_models=False, method=abi.METHOD_LAPLACE, run_multi_bazin=True, joint_multiband=True)):
+        r = oracle.fit_batch(b, **kw)
+        assert np.array_equal(r.model >= 0, n > 0) and np.array_equal(r.n_obs, n)
+        assert np.array_equal(r.mb_best_k > 0, (r.rank == 0) & (n >= 5))
+    assert r.model[11] != 1 and np.all(r.model[(n > 0) & (np.arange(b.n_bands) != 11)] == 1)
