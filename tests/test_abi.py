@@ -101,8 +101,9 @@ def test_struct_layouts_match_the_ctypes_mirror(tmp_path):
 
 
 def test_rust_bindings_in_the_integration_notes_match_the_header():
-    """The #[repr(C)] structs a maintainer adds to the Rust crate (written out
-    in INTEGRATION.md) list the header's fields in the header's order."""
+    """A documentation-sync test: the #[repr(C)] structs a maintainer adds to
+    the Rust crate (written out in INTEGRATION.md, which this test reads)
+    list the header's fields in the header's order."""
     from lightcurve_fitting_gb300 import abi
     text = open(os.path.join(ROOT, "INTEGRATION.md")).read()
     pairs = {"LcfBandsCsr": abi.BandsCSR, "LcfFitOptions": abi.FitOptions, "LcfFitOutputs": abi.FitOutputs,
